@@ -1,0 +1,276 @@
+/*
+ * salvia_gb300.h -- C ABI of the GB300 rasterization pipeline.
+ *
+ * This is the drop-in boundary for Salvia's draw path.  Every entry point
+ * below replaces one call of the reference C++ renderer interface
+ * (salvia/include/salvia/core/renderer.h:42-147) with a plain-pointer,
+ * plain-size C function; the C++ facade in salvia_gb300/renderer.hpp maps the
+ * reference's classes (renderer, raster_state, depth_stencil_state, sampler,
+ * input_layout, cpp_*_shader) onto it.
+ *
+ * Conventions
+ *  - Status codes mirror `enum class result` (salvia/include/salvia/common/
+ *    constants.h:9): SG_OK, SG_FAILED, SG_OUT_OF_MEMORY, SG_INVALID_PARAMETER,
+ *    plus SG_TIMEOUT for bounded device waits and SG_CUDA_ERROR.
+ *  - Enumerations keep the reference's numeric values (primitive topology,
+ *    cull mode, compare function, stencil op, filter, address mode, pixel
+ *    format, index format) so a caller can pass the reference's enums through.
+ *  - Resources are addressed by 32-bit handles; handle 0 means "none".
+ *  - All calls are stream-ordered on the device's CUDA stream; only the
+ *    *_download / sg_sync calls block the host.
+ *  - No call takes or returns a torch or CUDA type: streams are `void*`.
+ */
+#ifndef SALVIA_GB300_H
+#define SALVIA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status ------------------------------------------------------------- */
+enum {
+  SG_OK = 0,
+  SG_FAILED = 1,
+  SG_OUT_OF_MEMORY = 2,
+  SG_INVALID_PARAMETER = 3,
+  SG_TIMEOUT = 4,
+  SG_CUDA_ERROR = 5
+};
+
+/* ---- capacities (salvia/include/salvia/common/renderer_capacity.h) ------- */
+#define SG_MAX_VS_INPUTS 8    /* MAX_VS_INPUT_ATTRS */
+#define SG_MAX_VARYINGS 5     /* vs_output op table covers 0..5 attributes (shader.cpp:45-78) */
+#define SG_MAX_STREAMS 8
+#define SG_MAX_RT_SIZE 8192   /* MAX_RENDER_TARGET_WIDTH/HEIGHT */
+#define SG_MAX_SHADER_CONSTANTS 48
+#define SG_MAX_SHADER_SAMPLERS 2
+
+/* ---- enumerations (reference numeric values) ----------------------------- */
+/* primitive_topology (constants.h:44-52) */
+enum { SG_TOPOLOGY_TRIANGLE_LIST = 2, SG_TOPOLOGY_TRIANGLE_STRIP = 4 };
+/* cull_mode (constants.h:58-63) */
+enum { SG_CULL_NONE = 0, SG_CULL_FRONT = 1, SG_CULL_BACK = 2 };
+/* fill_mode */
+enum { SG_FILL_WIREFRAME = 0, SG_FILL_SOLID = 1 };
+/* compare_function (constants.h:143-152) */
+enum {
+  SG_CMP_NEVER = 0, SG_CMP_LESS = 1, SG_CMP_EQUAL = 2, SG_CMP_LESS_EQUAL = 3,
+  SG_CMP_GREATER = 4, SG_CMP_NOT_EQUAL = 5, SG_CMP_GREATER_EQUAL = 6, SG_CMP_ALWAYS = 7
+};
+/* stencil_op (constants.h:154-163) */
+enum {
+  SG_SOP_KEEP = 1, SG_SOP_ZERO = 2, SG_SOP_REPLACE = 3, SG_SOP_INCR_SAT = 4,
+  SG_SOP_DECR_SAT = 5, SG_SOP_INVERT = 6, SG_SOP_INCR_WRAP = 7, SG_SOP_DECR_WRAP = 8
+};
+/* filter_type / address_mode / mip_quality (constants.h:82-102) */
+enum { SG_FILTER_POINT = 0, SG_FILTER_LINEAR = 1, SG_FILTER_ANISOTROPIC = 2 };
+enum { SG_ADDRESS_WRAP = 0, SG_ADDRESS_MIRROR = 1, SG_ADDRESS_CLAMP = 2, SG_ADDRESS_BORDER = 3 };
+enum { SG_MIP_LO_QUALITY = 0, SG_MIP_MI_QUALITY = 1, SG_MIP_HI_QUALITY = 2 };
+/* clear_flag (constants.h:165) */
+enum { SG_CLEAR_DEPTH = 1, SG_CLEAR_STENCIL = 2 };
+/* pixel formats: the reference's pixel_format codes (colors_convertors.h:39-45)
+ * plus three formats the reference does not have (documented extensions). */
+enum {
+  SG_FMT_RGBA32F = 0, SG_FMT_RGB32F = 1, SG_FMT_BGRA8 = 2, SG_FMT_RGBA8 = 3,
+  SG_FMT_R32F = 4, SG_FMT_RG32F = 5, SG_FMT_R32I = 6,
+  SG_FMT_RGBA16F = 16,   /* extension: half colour, round-to-nearest-even */
+  SG_FMT_D32F = 17,      /* extension: float depth, no stencil */
+  SG_FMT_D24S8 = 18      /* extension: 24-bit unorm depth (low) + 8-bit stencil (high) */
+};
+/* vertex element formats (salvia/include/salvia/common/format.h) */
+enum {
+  SG_VFMT_R32G32B32A32_FLOAT = 2, SG_VFMT_R32G32B32A32_SINT = 4, SG_VFMT_R32G32B32_FLOAT = 6,
+  SG_VFMT_R32G32_FLOAT = 16, SG_VFMT_R32_FLOAT = 41
+};
+/* index formats */
+enum { SG_INDEX_U32 = 42, SG_INDEX_U16 = 57 };
+/* vs_output::attrib_modifier_type (shader_regs.h:49-55) */
+enum {
+  SG_AM_LINEAR = 1, SG_AM_CENTROID = 2, SG_AM_NOINTERPOLATION = 4,
+  SG_AM_NOPERSPECTIVE = 8, SG_AM_SAMPLE = 16
+};
+/* semantic of a vertex-shader input register: POSITION fills w with 1 when
+ * the element has fewer than four components, anything else with 0
+ * (salvia/include/salvia/shader/constants.h:119). */
+enum { SG_SEMANTIC_POSITION = 0, SG_SEMANTIC_TEXCOORD = 1, SG_SEMANTIC_COLOR = 2, SG_SEMANTIC_NORMAL = 3 };
+
+/* ---- stock shader programs --------------------------------------------------
+ * The reference runs user C++ virtual shaders on the CPU (shader.h:159-215).
+ * Device code cannot call host virtuals, so the ABI names compiled device
+ * programs; their bodies are written once per program and documented here
+ * with the reference call each one makes.                                   */
+enum {
+  /* out.position = transform(in[0], M)  (eflib::transform row-vector x matrix,
+   * eflib/src/math.cpp:142-154); out.attr[i] = in[i+1] for i < num_varyings.
+   * constants[0..15] = M, row-major (m[r][c] at 4r+c). */
+  SG_VS_TRANSFORM = 1,
+  /* Morph + vertex-texture displacement (the VertexTextureFetch/Morph
+   * samples' pattern): p = p0 + (p1 - p0) * k[16]; n = in[2];
+   * h = vs_sampler0.sample(in[3].x, in[3].y, 0).r; p.xyz += n.xyz * (h * k[17]);
+   * out.position = transform(p, M); out.attr[0] = in[3]; out.attr[1] = n;
+   * constants[0..15] = M, k[16] = morph weight, k[17] = displacement scale. */
+  SG_VS_MORPH_DISPLACE = 2
+};
+enum {
+  SG_PS_COLOR = 1,          /* out.color[0] = in.attr[0] */
+  SG_PS_CONSTANT = 2,       /* out.color[0] = constants[0..3] */
+  /* out.color[0] = tex2d(sampler0, 0) * in.attr[1]; tex2d computes the LOD
+   * once per quad from quad differences (cpp_pixel_shader.cpp:23-31). */
+  SG_PS_TEX_MODULATE = 3,
+  /* out.color[0] = sampler0.sample_2d_grad(in.attr[0].xy, ddx(0).xy,
+   * ddy(0).xy, 0) * in.attr[1]  (sampler.cpp:854-873; the anisotropic path). */
+  SG_PS_TEX_GRAD_MODULATE = 4
+};
+enum {
+  SG_BS_REPLACE = 1,        /* color(0, s) = in.color[0] */
+  SG_BS_LERP_SRC_ALPHA = 2, /* color(0, s) = lerp(dst, src, src.a) (TextureAndBlending.cpp:168-176) */
+  SG_BS_ADD = 3             /* color(0, s) = dst + src */
+};
+
+/* ---- descriptors ------------------------------------------------------------ */
+typedef struct sg_viewport {           /* salvia/include/salvia/core/viewport.h */
+  float x, y, w, h, minz, maxz;
+} sg_viewport;
+
+typedef struct sg_raster_desc {        /* raster_state.h:17-40 */
+  uint32_t fill_mode;                  /* SG_FILL_SOLID */
+  uint32_t cull_mode;                  /* SG_CULL_* */
+  uint32_t front_ccw;
+  uint32_t reserved;
+} sg_raster_desc;
+
+typedef struct sg_stencil_face_desc {  /* framebuffer.h:20-33 */
+  uint32_t fail_op, depth_fail_op, pass_op, func;
+} sg_stencil_face_desc;
+
+typedef struct sg_depth_stencil_desc { /* framebuffer.h:35-52 */
+  uint32_t depth_enable;
+  uint32_t depth_write;
+  uint32_t depth_func;
+  uint32_t stencil_enable;
+  uint32_t stencil_read_mask;
+  uint32_t stencil_write_mask;
+  sg_stencil_face_desc front, back;
+} sg_depth_stencil_desc;
+
+typedef struct sg_sampler_desc {       /* sampler.h:16-45 */
+  uint32_t min_filter, mag_filter, mip_filter, mip_quality;
+  uint32_t address_u, address_v, address_w;
+  uint32_t max_anisotropy;
+  float lod_bias;
+  float border_color[4];
+  float min_lod, max_lod;
+} sg_sampler_desc;
+
+typedef struct sg_vertex_stream {      /* set_vertex_buffers (renderer.h:66-70) */
+  uint32_t buffer;
+  uint32_t stride;
+  uint32_t offset;
+} sg_vertex_stream;
+
+typedef struct sg_vs_input {           /* input_element_desc (input_layout.h:20-47) bound to a register */
+  uint32_t semantic;                   /* SG_SEMANTIC_* */
+  uint32_t semantic_index;
+  uint32_t format;                     /* SG_VFMT_* */
+  uint32_t slot;
+  uint32_t offset;                     /* aligned_byte_offset */
+} sg_vs_input;
+
+typedef struct sg_shader {
+  uint32_t program;                    /* SG_VS_* / SG_PS_* / SG_BS_* */
+  uint32_t samplers[SG_MAX_SHADER_SAMPLERS];
+  uint32_t reserved;
+  float constants[SG_MAX_SHADER_CONSTANTS];
+} sg_shader;
+
+/* One draw / draw_index call with the state it runs under
+ * (render_state, salvia/include/salvia/core/render_state.h:46-94). */
+typedef struct sg_draw_desc {
+  uint32_t color_target;               /* texture handle (level 0), 0 = none */
+  uint32_t ds_target;                  /* texture handle, 0 = none */
+  sg_viewport viewport;
+  uint32_t topology;
+  uint32_t indexed;                    /* 0: draw(start, count), 1: draw_index(start, count, base) */
+  uint32_t index_buffer;
+  uint32_t index_format;
+  uint32_t start;
+  uint32_t prim_count;
+  int32_t base_vertex;
+  uint32_t num_streams;
+  sg_vertex_stream streams[SG_MAX_STREAMS];
+  uint32_t num_inputs;
+  sg_vs_input inputs[SG_MAX_VS_INPUTS];
+  uint32_t num_varyings;               /* cpp_vertex_shader::num_output_attributes */
+  uint32_t varying_modifiers[SG_MAX_VARYINGS];
+  sg_raster_desc raster;
+  sg_depth_stencil_desc depth_stencil;
+  int32_t stencil_ref;
+  sg_shader vs, ps, bs;
+} sg_draw_desc;
+
+/* Pipeline counters of one draw (async_object.h:90-175). */
+typedef struct sg_draw_stats {
+  uint64_t ia_primitives;              /* input primitives */
+  uint64_t cprimitives;                /* triangles after clipping and culling */
+  uint64_t ps_invocations;             /* pixel-shader invocations, helpers included */
+  uint64_t backend_input_pixels;       /* pixels of quads that reached the output merger */
+} sg_draw_stats;
+
+/* ---- device (create_benchmark_renderer, renderer.h:133-134) --------------- */
+typedef struct sg_device sg_device;
+
+/* Creates a device on CUDA device `cuda_device`, issuing all work on
+ * `cuda_stream` (a cudaStream_t, or NULL for a stream the device owns). */
+int32_t sg_device_create(int32_t cuda_device, void* cuda_stream, sg_device** out_device);
+void sg_device_destroy(sg_device* dev);
+/* renderer::flush (renderer.h:128): waits until all submitted work is done. */
+int32_t sg_sync(sg_device* dev);
+/* Last CUDA error text seen by the device (empty when none). */
+const char* sg_last_error(sg_device* dev);
+
+/* ---- buffers (create_buffer + map/unmap, renderer.h:45,61-63) -------------- */
+int32_t sg_buffer_create(sg_device* dev, size_t size, uint32_t* out_buffer);
+int32_t sg_buffer_upload(sg_device* dev, uint32_t buffer, size_t offset, const void* src, size_t size);
+int32_t sg_buffer_download(sg_device* dev, uint32_t buffer, size_t offset, void* dst, size_t size);
+int32_t sg_buffer_destroy(sg_device* dev, uint32_t buffer);
+
+/* ---- textures / surfaces (create_tex2d, texture.h, surface.h) ---------------
+ * Level 0 of a texture is the surface a render target names.  Texel storage
+ * matches surface.cpp:277-295: ((y * w + x) * samples + s) * elem_size. */
+int32_t sg_texture_create(sg_device* dev, uint32_t width, uint32_t height, uint32_t samples,
+                          uint32_t format, uint32_t* out_texture);
+int32_t sg_texture_upload(sg_device* dev, uint32_t texture, uint32_t level, const void* src, size_t size);
+int32_t sg_texture_download(sg_device* dev, uint32_t texture, uint32_t level, void* dst, size_t size);
+/* texture_2d::gen_mipmap(filter, true) (texture2d.cpp:25-36). */
+int32_t sg_texture_gen_mipmap(sg_device* dev, uint32_t texture, uint32_t filter);
+int32_t sg_texture_info(sg_device* dev, uint32_t texture, uint32_t level, uint32_t* width,
+                        uint32_t* height, uint32_t* samples, uint32_t* format, uint32_t* levels);
+int32_t sg_texture_destroy(sg_device* dev, uint32_t texture);
+
+/* ---- samplers (create_sampler, renderer.h:49) ------------------------------- */
+int32_t sg_sampler_create(sg_device* dev, const sg_sampler_desc* desc, uint32_t texture,
+                          uint32_t* out_sampler);
+int32_t sg_sampler_destroy(sg_device* dev, uint32_t sampler);
+
+/* ---- commands --------------------------------------------------------------- */
+/* renderer::draw / draw_index (renderer.h:121-122).  `stats` may be NULL;
+ * when given, the counters are written once the draw has completed on the
+ * device (the call then synchronises). */
+int32_t sg_draw(sg_device* dev, const sg_draw_desc* desc, sg_draw_stats* stats);
+/* renderer::clear_color (renderer.h:124). */
+int32_t sg_clear_color(sg_device* dev, uint32_t texture, const float rgba[4]);
+/* renderer::clear_depth_stencil (renderer.h:125-126). */
+int32_t sg_clear_depth_stencil(sg_device* dev, uint32_t texture, uint32_t flags, float depth,
+                               uint32_t stencil);
+/* surface::resolve (surface.cpp:123-140): box average of the samples of
+ * `src` (level 0) into the single-sample `dst` (level 0). */
+int32_t sg_resolve(sg_device* dev, uint32_t src, uint32_t dst);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SALVIA_GB300_H */

@@ -1,0 +1,151 @@
+"""ctypes mirror of include/salvia_gb300.h.
+
+The structures below are field-for-field copies of the C descriptors; the
+`bind()` helper attaches argtypes/restype to every entry point of a loaded
+library that exports the ABI.
+"""
+import ctypes as C
+
+SG_OK, SG_FAILED, SG_OUT_OF_MEMORY, SG_INVALID_PARAMETER, SG_TIMEOUT, SG_CUDA_ERROR = range(6)
+STATUS_NAMES = {0: "ok", 1: "failed", 2: "out_of_memory", 3: "invalid_parameter",
+                4: "timeout", 5: "cuda_error"}
+
+SG_MAX_VS_INPUTS = 8
+SG_MAX_VARYINGS = 5
+SG_MAX_STREAMS = 8
+SG_MAX_SHADER_CONSTANTS = 48
+SG_MAX_SHADER_SAMPLERS = 2
+
+TOPOLOGY_TRIANGLE_LIST, TOPOLOGY_TRIANGLE_STRIP = 2, 4
+CULL_NONE, CULL_FRONT, CULL_BACK = 0, 1, 2
+FILL_WIREFRAME, FILL_SOLID = 0, 1
+CMP_NEVER, CMP_LESS, CMP_EQUAL, CMP_LESS_EQUAL, CMP_GREATER, CMP_NOT_EQUAL, \
+    CMP_GREATER_EQUAL, CMP_ALWAYS = range(8)
+SOP_KEEP, SOP_ZERO, SOP_REPLACE, SOP_INCR_SAT, SOP_DECR_SAT, SOP_INVERT, SOP_INCR_WRAP, \
+    SOP_DECR_WRAP = range(1, 9)
+FILTER_POINT, FILTER_LINEAR, FILTER_ANISOTROPIC = 0, 1, 2
+ADDRESS_WRAP, ADDRESS_MIRROR, ADDRESS_CLAMP, ADDRESS_BORDER = 0, 1, 2, 3
+MIP_LO_QUALITY, MIP_MI_QUALITY, MIP_HI_QUALITY = 0, 1, 2
+CLEAR_DEPTH, CLEAR_STENCIL = 1, 2
+FMT_RGBA32F, FMT_RGB32F, FMT_BGRA8, FMT_RGBA8, FMT_R32F, FMT_RG32F, FMT_R32I = range(7)
+FMT_RGBA16F, FMT_D32F, FMT_D24S8 = 16, 17, 18
+FORMAT_BYTES = {FMT_RGBA32F: 16, FMT_RGB32F: 12, FMT_BGRA8: 4, FMT_RGBA8: 4, FMT_R32F: 4,
+                FMT_RG32F: 8, FMT_R32I: 4, FMT_RGBA16F: 8, FMT_D32F: 4, FMT_D24S8: 4}
+VFMT_R32G32B32A32_FLOAT, VFMT_R32G32B32A32_SINT, VFMT_R32G32B32_FLOAT = 2, 4, 6
+VFMT_R32G32_FLOAT, VFMT_R32_FLOAT = 16, 41
+INDEX_U32, INDEX_U16 = 42, 57
+AM_LINEAR, AM_CENTROID, AM_NOINTERPOLATION, AM_NOPERSPECTIVE, AM_SAMPLE = 1, 2, 4, 8, 16
+SEMANTIC_POSITION, SEMANTIC_TEXCOORD, SEMANTIC_COLOR, SEMANTIC_NORMAL = 0, 1, 2, 3
+
+VS_TRANSFORM, VS_MORPH_DISPLACE = 1, 2
+PS_COLOR, PS_CONSTANT, PS_TEX_MODULATE, PS_TEX_GRAD_MODULATE = 1, 2, 3, 4
+BS_REPLACE, BS_LERP_SRC_ALPHA, BS_ADD = 1, 2, 3
+
+
+class Viewport(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("w", C.c_float), ("h", C.c_float),
+                ("minz", C.c_float), ("maxz", C.c_float)]
+
+
+class RasterDesc(C.Structure):
+    _fields_ = [("fill_mode", C.c_uint32), ("cull_mode", C.c_uint32),
+                ("front_ccw", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class StencilFaceDesc(C.Structure):
+    _fields_ = [("fail_op", C.c_uint32), ("depth_fail_op", C.c_uint32),
+                ("pass_op", C.c_uint32), ("func", C.c_uint32)]
+
+
+class DepthStencilDesc(C.Structure):
+    _fields_ = [("depth_enable", C.c_uint32), ("depth_write", C.c_uint32),
+                ("depth_func", C.c_uint32), ("stencil_enable", C.c_uint32),
+                ("stencil_read_mask", C.c_uint32), ("stencil_write_mask", C.c_uint32),
+                ("front", StencilFaceDesc), ("back", StencilFaceDesc)]
+
+
+class SamplerDesc(C.Structure):
+    _fields_ = [("min_filter", C.c_uint32), ("mag_filter", C.c_uint32),
+                ("mip_filter", C.c_uint32), ("mip_quality", C.c_uint32),
+                ("address_u", C.c_uint32), ("address_v", C.c_uint32),
+                ("address_w", C.c_uint32), ("max_anisotropy", C.c_uint32),
+                ("lod_bias", C.c_float), ("border_color", C.c_float * 4),
+                ("min_lod", C.c_float), ("max_lod", C.c_float)]
+
+
+class VertexStream(C.Structure):
+    _fields_ = [("buffer", C.c_uint32), ("stride", C.c_uint32), ("offset", C.c_uint32)]
+
+
+class VSInput(C.Structure):
+    _fields_ = [("semantic", C.c_uint32), ("semantic_index", C.c_uint32),
+                ("format", C.c_uint32), ("slot", C.c_uint32), ("offset", C.c_uint32)]
+
+
+class Shader(C.Structure):
+    _fields_ = [("program", C.c_uint32), ("samplers", C.c_uint32 * SG_MAX_SHADER_SAMPLERS),
+                ("reserved", C.c_uint32), ("constants", C.c_float * SG_MAX_SHADER_CONSTANTS)]
+
+
+class DrawDesc(C.Structure):
+    _fields_ = [("color_target", C.c_uint32), ("ds_target", C.c_uint32),
+                ("viewport", Viewport), ("topology", C.c_uint32), ("indexed", C.c_uint32),
+                ("index_buffer", C.c_uint32), ("index_format", C.c_uint32),
+                ("start", C.c_uint32), ("prim_count", C.c_uint32), ("base_vertex", C.c_int32),
+                ("num_streams", C.c_uint32), ("streams", VertexStream * SG_MAX_STREAMS),
+                ("num_inputs", C.c_uint32), ("inputs", VSInput * SG_MAX_VS_INPUTS),
+                ("num_varyings", C.c_uint32),
+                ("varying_modifiers", C.c_uint32 * SG_MAX_VARYINGS),
+                ("raster", RasterDesc), ("depth_stencil", DepthStencilDesc),
+                ("stencil_ref", C.c_int32), ("vs", Shader), ("ps", Shader), ("bs", Shader)]
+
+
+class DrawStats(C.Structure):
+    _fields_ = [("ia_primitives", C.c_uint64), ("cprimitives", C.c_uint64),
+                ("ps_invocations", C.c_uint64), ("backend_input_pixels", C.c_uint64)]
+
+
+_u32p = C.POINTER(C.c_uint32)
+
+SIGNATURES = {
+    "sg_device_create": (C.c_int32, [C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "sg_device_destroy": (None, [C.c_void_p]),
+    "sg_sync": (C.c_int32, [C.c_void_p]),
+    "sg_last_error": (C.c_char_p, [C.c_void_p]),
+    "sg_buffer_create": (C.c_int32, [C.c_void_p, C.c_size_t, _u32p]),
+    "sg_buffer_upload": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_size_t, C.c_void_p, C.c_size_t]),
+    "sg_buffer_download": (C.c_int32,
+                           [C.c_void_p, C.c_uint32, C.c_size_t, C.c_void_p, C.c_size_t]),
+    "sg_buffer_destroy": (C.c_int32, [C.c_void_p, C.c_uint32]),
+    "sg_texture_create": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                      C.c_uint32, _u32p]),
+    "sg_texture_upload": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                      C.c_size_t]),
+    "sg_texture_download": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                        C.c_size_t]),
+    "sg_texture_gen_mipmap": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "sg_texture_info": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, _u32p, _u32p, _u32p,
+                                    _u32p, _u32p]),
+    "sg_texture_destroy": (C.c_int32, [C.c_void_p, C.c_uint32]),
+    "sg_sampler_create": (C.c_int32, [C.c_void_p, C.POINTER(SamplerDesc), C.c_uint32, _u32p]),
+    "sg_sampler_destroy": (C.c_int32, [C.c_void_p, C.c_uint32]),
+    "sg_draw": (C.c_int32, [C.c_void_p, C.POINTER(DrawDesc), C.POINTER(DrawStats)]),
+    "sg_clear_color": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(C.c_float)]),
+    "sg_clear_depth_stencil": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,
+                                           C.c_uint32]),
+    "sg_resolve": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32]),
+}
+
+
+def bind(lib, extra=None):
+    """Attach the ABI's signatures to the functions exported by `lib`."""
+    sigs = dict(SIGNATURES)
+    if extra:
+        sigs.update(extra)
+    for name, (restype, argtypes) in sigs.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = restype
+        fn.argtypes = argtypes
+    return lib

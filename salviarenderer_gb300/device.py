@@ -1,0 +1,200 @@
+"""Host-side wrapper over a library that exports the salvia_gb300.h C ABI.
+
+`Device` mirrors the reference renderer's resource and command calls
+(salvia/include/salvia/core/renderer.h:42-147): create_buffer, create_tex2d,
+create_sampler, draw / draw_index, clear_color, clear_depth_stencil,
+surface::resolve.  Every call goes through the C ABI; a non-ok status raises
+`SalviaError` carrying the reference's result name.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class SalviaError(RuntimeError):
+    def __init__(self, fn, status, detail=""):
+        name = abi.STATUS_NAMES.get(status, str(status))
+        super().__init__(f"{fn} returned {name}" + (f": {detail}" if detail else ""))
+        self.status = status
+
+
+class Device:
+    """One renderer instance on one backend library."""
+
+    def __init__(self, lib, cuda_device=0, stream=None):
+        self.lib = lib
+        handle = C.c_void_p()
+        self._check("sg_device_create",
+                    lib.sg_device_create(cuda_device, C.c_void_p(stream or 0), C.byref(handle)))
+        self.handle = handle
+        self._textures = {}
+
+    def _check(self, fn, status):
+        if status != abi.SG_OK:
+            detail = ""
+            if getattr(self, "handle", None) is not None and hasattr(self.lib, "sg_last_error"):
+                detail = (self.lib.sg_last_error(self.handle) or b"").decode()
+            raise SalviaError(fn, status, detail)
+
+    def close(self):
+        if self.handle is not None:
+            self.lib.sg_device_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        self._check("sg_sync", self.lib.sg_sync(self.handle))
+
+    # -- buffers -------------------------------------------------------------
+    def buffer(self, data):
+        data = np.ascontiguousarray(data)
+        h = C.c_uint32()
+        self._check("sg_buffer_create",
+                    self.lib.sg_buffer_create(self.handle, data.nbytes, C.byref(h)))
+        self._check("sg_buffer_upload",
+                    self.lib.sg_buffer_upload(self.handle, h.value, 0,
+                                              data.ctypes.data_as(C.c_void_p), data.nbytes))
+        return h.value
+
+    def buffer_download(self, buf, nbytes, dtype=np.uint8):
+        out = np.empty(nbytes, dtype=np.uint8)
+        self._check("sg_buffer_download",
+                    self.lib.sg_buffer_download(self.handle, buf, 0,
+                                                out.ctypes.data_as(C.c_void_p), nbytes))
+        return out.view(dtype)
+
+    # -- textures ------------------------------------------------------------
+    def texture(self, width, height, samples=1, fmt=abi.FMT_RGBA8):
+        h = C.c_uint32()
+        self._check("sg_texture_create",
+                    self.lib.sg_texture_create(self.handle, width, height, samples, fmt,
+                                               C.byref(h)))
+        self._textures[h.value] = (width, height, samples, fmt)
+        return h.value
+
+    def texture_info(self, tex, level=0):
+        vals = [C.c_uint32() for _ in range(5)]
+        self._check("sg_texture_info",
+                    self.lib.sg_texture_info(self.handle, tex, level, *[C.byref(v) for v in vals]))
+        return tuple(v.value for v in vals)
+
+    def texture_upload(self, tex, data, level=0):
+        data = np.ascontiguousarray(data)
+        self._check("sg_texture_upload",
+                    self.lib.sg_texture_upload(self.handle, tex, level,
+                                               data.ctypes.data_as(C.c_void_p), data.nbytes))
+
+    def texture_download(self, tex, level=0):
+        w, h, s, fmt, _ = self.texture_info(tex, level)
+        nbytes = w * h * s * abi.FORMAT_BYTES[fmt]
+        out = np.empty(nbytes, dtype=np.uint8)
+        self._check("sg_texture_download",
+                    self.lib.sg_texture_download(self.handle, tex, level,
+                                                 out.ctypes.data_as(C.c_void_p), nbytes))
+        return out
+
+    def gen_mipmap(self, tex, filt=abi.FILTER_LINEAR):
+        self._check("sg_texture_gen_mipmap", self.lib.sg_texture_gen_mipmap(self.handle, tex, filt))
+
+    def levels(self, tex):
+        return self.texture_info(tex)[4]
+
+    # -- samplers ------------------------------------------------------------
+    def sampler(self, tex, **kw):
+        d = abi.SamplerDesc()
+        d.min_filter = kw.get("min_filter", abi.FILTER_LINEAR)
+        d.mag_filter = kw.get("mag_filter", abi.FILTER_LINEAR)
+        d.mip_filter = kw.get("mip_filter", abi.FILTER_LINEAR)
+        d.mip_quality = kw.get("mip_quality", abi.MIP_MI_QUALITY)
+        d.address_u = kw.get("address_u", abi.ADDRESS_WRAP)
+        d.address_v = kw.get("address_v", abi.ADDRESS_WRAP)
+        d.address_w = kw.get("address_w", abi.ADDRESS_WRAP)
+        d.max_anisotropy = kw.get("max_anisotropy", 0)
+        d.lod_bias = 0.0
+        for i, v in enumerate(kw.get("border_color", (0.0, 0.0, 0.0, 0.0))):
+            d.border_color[i] = v
+        d.min_lod, d.max_lod = -1e20, 1e20
+        h = C.c_uint32()
+        self._check("sg_sampler_create",
+                    self.lib.sg_sampler_create(self.handle, C.byref(d), tex, C.byref(h)))
+        return h.value
+
+    # -- commands ------------------------------------------------------------
+    def draw(self, desc, stats=False):
+        st = abi.DrawStats() if stats else None
+        self._check("sg_draw", self.lib.sg_draw(self.handle, C.byref(desc),
+                                                C.byref(st) if st is not None else None))
+        if st is None:
+            return None
+        return {k: getattr(st, k) for k, _ in abi.DrawStats._fields_}
+
+    def clear_color(self, tex, rgba):
+        arr = (C.c_float * 4)(*rgba)
+        self._check("sg_clear_color", self.lib.sg_clear_color(self.handle, tex, arr))
+
+    def clear_depth_stencil(self, tex, flags, depth, stencil):
+        self._check("sg_clear_depth_stencil",
+                    self.lib.sg_clear_depth_stencil(self.handle, tex, flags, depth, stencil))
+
+    def resolve(self, src, dst):
+        self._check("sg_resolve", self.lib.sg_resolve(self.handle, src, dst))
+
+
+def default_depth_stencil(depth_func=abi.CMP_LESS, depth_enable=1, depth_write=1):
+    ds = abi.DepthStencilDesc()
+    ds.depth_enable, ds.depth_write, ds.depth_func = depth_enable, depth_write, depth_func
+    ds.stencil_enable = 0
+    ds.stencil_read_mask = ds.stencil_write_mask = 0xFF
+    for face in (ds.front, ds.back):
+        face.fail_op = face.depth_fail_op = face.pass_op = abi.SOP_KEEP
+        face.func = abi.CMP_ALWAYS
+    return ds
+
+
+def make_draw_desc(**kw):
+    """Builds an sg_draw_desc; keyword names follow the C fields."""
+    d = abi.DrawDesc()
+    d.topology = kw.get("topology", abi.TOPOLOGY_TRIANGLE_LIST)
+    d.raster.fill_mode = abi.FILL_SOLID
+    d.raster.cull_mode = kw.get("cull_mode", abi.CULL_NONE)
+    d.raster.front_ccw = kw.get("front_ccw", 0)
+    d.depth_stencil = kw.get("depth_stencil") or default_depth_stencil()
+    d.stencil_ref = kw.get("stencil_ref", 0)
+    vp = kw["viewport"]
+    d.viewport = abi.Viewport(*vp)
+    d.color_target = kw.get("color_target", 0)
+    d.ds_target = kw.get("ds_target", 0)
+    d.indexed = 1 if kw.get("index_buffer") else 0
+    d.index_buffer = kw.get("index_buffer", 0)
+    d.index_format = kw.get("index_format", abi.INDEX_U32)
+    d.start = kw.get("start", 0)
+    d.prim_count = kw["prim_count"]
+    d.base_vertex = kw.get("base_vertex", 0)
+    streams = kw["streams"]
+    d.num_streams = len(streams)
+    for i, (buf, stride, off) in enumerate(streams):
+        d.streams[i] = abi.VertexStream(buf, stride, off)
+    inputs = kw["inputs"]
+    d.num_inputs = len(inputs)
+    for i, (sem, sidx, fmt, slot, off) in enumerate(inputs):
+        d.inputs[i] = abi.VSInput(sem, sidx, fmt, slot, off)
+    mods = kw.get("varying_modifiers")
+    d.num_varyings = kw.get("num_varyings", len(mods) if mods else 0)
+    for i in range(d.num_varyings):
+        d.varying_modifiers[i] = mods[i] if mods else abi.AM_LINEAR
+    for name in ("vs", "ps", "bs"):
+        spec = kw[name]
+        sh = getattr(d, name)
+        sh.program = spec["program"]
+        for i, s in enumerate(spec.get("samplers", ())):
+            sh.samplers[i] = s
+        for i, v in enumerate(np.asarray(spec.get("constants", ()), dtype=np.float32).ravel()):
+            sh.constants[i] = float(v)
+    return d

@@ -1,0 +1,339 @@
+"""Seeded synthetic scenes for the rasterization pipeline's workloads.
+
+Every scene is built from a seed with numpy's PCG64 generator, so the same
+seed gives the same vertex, index and texture data on any backend.  A scene
+records the calls it makes (clears, draws, resolve) as plain data, and
+`render(dev, scene)` replays them on any `Device`.
+
+Workloads (sizes are the defaults; tests use smaller ones):
+  c1_scene      512x512 RGBA8, 1x, 10,000 independent clip-space triangles,
+                per-vertex colour, MVP vertex shader, depth LESS, overwrite.
+  c2_scene      1920x1080 RGBA8, 4x MSAA, a 317x317-vertex height-field grid
+                (199,712 triangles) with UVs in [0,8] (WRAP), one 2048^2
+                value-noise texture with a full box mip chain; half the draws
+                trilinear, half 16x anisotropic; src-alpha blending; LESS.
+  stencil_mirror_scene   quad written with stencil REPLACE, then a
+                reflected draw tested with stencil EQUAL.
+"""
+import math
+
+import numpy as np
+
+from . import abi
+from .device import default_depth_stencil, make_draw_desc
+
+
+# --------------------------------------------------------------------------
+# matrices (row-vector convention: clip = v x M, as eflib::transform)
+def look_at_lh(eye, target, up):
+    eye, target, up = (np.asarray(a, dtype=np.float64) for a in (eye, target, up))
+    z = target - eye
+    z /= np.linalg.norm(z)
+    x = np.cross(up, z)
+    x /= np.linalg.norm(x)
+    y = np.cross(z, x)
+    m = np.identity(4)
+    m[0:3, 0] = x
+    m[0:3, 1] = y
+    m[0:3, 2] = z
+    m[3, 0:3] = [-x @ eye, -y @ eye, -z @ eye]
+    return m
+
+
+def perspective_fov_lh(fovy, aspect, zn, zf):
+    ys = 1.0 / math.tan(fovy / 2)
+    xs = ys / aspect
+    m = np.zeros((4, 4))
+    m[0, 0], m[1, 1] = xs, ys
+    m[2, 2] = zf / (zf - zn)
+    m[2, 3] = 1.0
+    m[3, 2] = -zn * zf / (zf - zn)
+    return m
+
+
+def value_noise(rng, size, octaves=6, channels=4):
+    """Seeded multi-octave value noise in [0,1], shape (size, size, channels)."""
+    out = np.zeros((size, size, channels), dtype=np.float64)
+    amp_sum = 0.0
+    for o in range(octaves):
+        cells = max(2, 4 << o)
+        if cells > size:
+            break
+        lattice = rng.random((cells + 1, cells + 1, channels))
+        lattice[cells, :] = lattice[0, :]
+        lattice[:, cells] = lattice[:, 0]
+        t = np.arange(size) * (cells / size)
+        i0 = np.floor(t).astype(np.int64)
+        f = t - i0
+        f = f * f * (3 - 2 * f)
+        a = lattice[i0][:, i0]
+        b = lattice[i0][:, i0 + 1]
+        c = lattice[i0 + 1][:, i0]
+        d = lattice[i0 + 1][:, i0 + 1]
+        fx = f[None, :, None]
+        fy = f[:, None, None]
+        layer = (a * (1 - fx) + b * fx) * (1 - fy) + (c * (1 - fx) + d * fx) * fy
+        amp = 0.5 ** o
+        out += layer * amp
+        amp_sum += amp
+    return out / amp_sum
+
+
+def to_rgba8(img):
+    return np.clip(np.rint(img * 255.0), 0, 255).astype(np.uint8)
+
+
+# --------------------------------------------------------------------------
+class Scene:
+    """Recorded calls of one frame plus the host data they reference."""
+
+    def __init__(self, name, width, height, samples, color_fmt=abi.FMT_RGBA8,
+                 ds_fmt=abi.FMT_RG32F):
+        self.name = name
+        self.width, self.height, self.samples = width, height, samples
+        self.color_fmt, self.ds_fmt = color_fmt, ds_fmt
+        self.buffers = {}       # name -> np array
+        self.textures = {}      # name -> (rgba8 level-0 array, gen_mips)
+        self.samplers = {}      # name -> (texture name, kwargs)
+        self.draws = []         # list of dict (make_draw_desc kwargs with names for resources)
+        self.clear_color = (0.0, 0.0, 0.0, 0.0)
+        self.clear_depth = 1.0
+        self.clear_stencil = 0
+        self.resolve = samples > 1
+
+    @property
+    def triangles(self):
+        return sum(d["prim_count"] for d in self.draws)
+
+
+class Bound:
+    """Device handles of a scene's resources on one backend."""
+
+    def __init__(self, dev, scene):
+        self.dev, self.scene = dev, scene
+        self.buf = {k: dev.buffer(v) for k, v in scene.buffers.items()}
+        self.tex = {}
+        for k, (img, mips) in scene.textures.items():
+            h, w = img.shape[0], img.shape[1]
+            fmt = abi.FMT_R32F if img.dtype == np.float32 and img.ndim == 2 else abi.FMT_RGBA8
+            t = dev.texture(w, h, 1, fmt)
+            dev.texture_upload(t, img)
+            if mips:
+                dev.gen_mipmap(t, abi.FILTER_LINEAR)
+            self.tex[k] = t
+        self.samp = {k: dev.sampler(self.tex[t], **kw) for k, (t, kw) in scene.samplers.items()}
+        s = scene
+        self.color = dev.texture(s.width, s.height, s.samples, s.color_fmt) if s.color_fmt is not None else 0
+        self.ds = dev.texture(s.width, s.height, s.samples, s.ds_fmt) if s.ds_fmt is not None else 0
+        self.resolved = dev.texture(s.width, s.height, 1, s.color_fmt) if (s.resolve and self.color) else 0
+        self.descs = [self._desc(d) for d in scene.draws]
+
+    def _shader(self, spec):
+        spec = dict(spec)
+        spec["samplers"] = [self.samp[n] for n in spec.get("samplers", ())]
+        return spec
+
+    def _desc(self, d):
+        kw = dict(d)
+        kw["streams"] = [(self.buf[b], stride, off) for b, stride, off in d["streams"]]
+        if d.get("index_buffer"):
+            kw["index_buffer"] = self.buf[d["index_buffer"]]
+        kw["color_target"] = self.color
+        kw["ds_target"] = self.ds
+        for n in ("vs", "ps", "bs"):
+            kw[n] = self._shader(d[n])
+        return make_draw_desc(**kw)
+
+    def clear(self):
+        s = self.scene
+        if self.color:
+            self.dev.clear_color(self.color, s.clear_color)
+        if self.ds:
+            self.dev.clear_depth_stencil(self.ds, abi.CLEAR_DEPTH | abi.CLEAR_STENCIL,
+                                         s.clear_depth, s.clear_stencil)
+
+    def draw_all(self, stats=False):
+        out = []
+        for desc in self.descs:
+            out.append(self.dev.draw(desc, stats=stats))
+        return out
+
+    def finish(self):
+        if self.resolved:
+            self.dev.resolve(self.color, self.resolved)
+
+    def frame(self, stats=False):
+        self.clear()
+        st = self.draw_all(stats)
+        self.finish()
+        return st
+
+    def outputs(self):
+        d = self.dev
+        out = {}
+        if self.color:
+            out["color"] = d.texture_download(self.color)
+        if self.ds:
+            out["depth_stencil"] = d.texture_download(self.ds)
+        if self.resolved:
+            out["resolved"] = d.texture_download(self.resolved)
+        return out
+
+
+def render(dev, scene, stats=False):
+    b = Bound(dev, scene)
+    st = b.frame(stats)
+    out = b.outputs()
+    if stats:
+        out["stats"] = st
+    return out
+
+
+# --------------------------------------------------------------------------
+VS_POS_COLOR_INPUTS = [(abi.SEMANTIC_POSITION, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 0),
+                       (abi.SEMANTIC_COLOR, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 16)]
+
+
+def c1_scene(seed=20261204, width=512, height=512, ntris=10000, samples=1,
+             ds_fmt=abi.FMT_RG32F, cull=abi.CULL_NONE, eye_dist=(3.0, 4.0), fov=math.pi / 2):
+    """Random clip-space triangles with per-vertex colour under a seeded MVP."""
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(-1.0, 1.0, size=(ntris * 3, 4))
+    pos[:, 3] = 1.0
+    col = rng.uniform(0.0, 1.0, size=(ntris * 3, 4))
+    verts = np.concatenate([pos, col], axis=1).astype(np.float32)
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    eye = d * rng.uniform(*eye_dist)
+    up = np.array([0.0, 1.0, 0.0]) if abs(d[1]) < 0.9 else np.array([1.0, 0.0, 0.0])
+    mvp = (look_at_lh(eye, [0, 0, 0], up) @
+           perspective_fov_lh(fov, width / height, 0.1, 100.0)).astype(np.float32)
+    s = Scene("c1", width, height, samples, ds_fmt=ds_fmt)
+    s.buffers["vb"] = verts
+    s.draws.append(dict(
+        viewport=(0, 0, width, height, 0.0, 1.0), prim_count=ntris,
+        streams=[("vb", 32, 0)], inputs=VS_POS_COLOR_INPUTS,
+        num_varyings=1, varying_modifiers=[abi.AM_LINEAR], cull_mode=cull,
+        vs=dict(program=abi.VS_TRANSFORM, constants=mvp),
+        ps=dict(program=abi.PS_COLOR), bs=dict(program=abi.BS_REPLACE)))
+    s.mvp = mvp
+    return s
+
+
+def grid_mesh(rng, n, uv_scale=8.0, z_amp=0.2, alpha=(0.3, 1.0)):
+    """n x n vertex grid over [-1,1]^2 (x, y) with z in [0, z_amp]."""
+    lin = np.linspace(-1.0, 1.0, n)
+    gx, gy = np.meshgrid(lin, lin)
+    z = rng.uniform(0.0, z_amp, size=(n, n))
+    u = (gx + 1.0) * 0.5 * uv_scale
+    v = (gy + 1.0) * 0.5 * uv_scale
+    a = rng.uniform(alpha[0], alpha[1], size=(n, n))
+    verts = np.zeros((n * n, 12), dtype=np.float32)
+    verts[:, 0] = gx.ravel()
+    verts[:, 1] = gy.ravel()
+    verts[:, 2] = z.ravel()
+    verts[:, 3] = 1.0
+    verts[:, 4] = u.ravel()
+    verts[:, 5] = v.ravel()
+    verts[:, 8] = 1.0
+    verts[:, 9] = 1.0
+    verts[:, 10] = 1.0
+    verts[:, 11] = a.ravel()
+    q = np.arange((n - 1) * (n - 1))
+    r, c = q // (n - 1), q % (n - 1)
+    i00 = r * n + c
+    i01 = i00 + 1
+    i10 = i00 + n
+    i11 = i10 + 1
+    idx = np.stack([i00, i10, i01, i01, i10, i11], axis=1).reshape(-1).astype(np.uint32)
+    return verts, idx
+
+
+GRID_INPUTS = [(abi.SEMANTIC_POSITION, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 0),
+               (abi.SEMANTIC_TEXCOORD, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 16),
+               (abi.SEMANTIC_COLOR, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 32)]
+
+
+def c2_scene(seed=20261204, width=1920, height=1080, samples=4, grid=317, tex_size=2048,
+             ndraws=8, ds_fmt=abi.FMT_RG32F, max_aniso=16, af_draws=True):
+    """Textured, filtered, alpha-blended height-field grid (the 1080p 4x workload)."""
+    rng = np.random.default_rng(seed)
+    verts, idx = grid_mesh(rng, grid)
+    tex = to_rgba8(value_noise(rng, tex_size))
+    jitter = rng.uniform(-0.05, 0.05, size=3)
+    eye = np.array([0.0, -0.7, -0.6]) + jitter
+    view = look_at_lh(eye, [0.0, -0.2, 0.1], [0.0, 0.0, -1.0])
+    proj = perspective_fov_lh(math.radians(60.0), width / height, 0.1, 100.0)
+    mvp = (view @ proj).astype(np.float32)
+    s = Scene("c2", width, height, samples, ds_fmt=ds_fmt)
+    s.buffers["vb"] = verts
+    s.buffers["ib"] = idx
+    s.textures["noise"] = (tex, True)
+    s.samplers["trilinear"] = ("noise", dict(min_filter=abi.FILTER_LINEAR,
+                                             mag_filter=abi.FILTER_LINEAR,
+                                             mip_filter=abi.FILTER_LINEAR))
+    s.samplers["aniso"] = ("noise", dict(min_filter=abi.FILTER_LINEAR,
+                                         mag_filter=abi.FILTER_LINEAR,
+                                         mip_filter=abi.FILTER_ANISOTROPIC,
+                                         max_anisotropy=max_aniso))
+    ntris = idx.size // 3
+    bounds = np.linspace(0, ntris, ndraws + 1).astype(np.int64)
+    for i in range(ndraws):
+        aniso = af_draws and (i % 2 == 1)
+        s.draws.append(dict(
+            viewport=(0, 0, width, height, 0.0, 1.0),
+            start=int(bounds[i] * 3), prim_count=int(bounds[i + 1] - bounds[i]),
+            index_buffer="ib", index_format=abi.INDEX_U32,
+            streams=[("vb", 48, 0)], inputs=GRID_INPUTS,
+            num_varyings=2, varying_modifiers=[abi.AM_LINEAR, abi.AM_LINEAR],
+            vs=dict(program=abi.VS_TRANSFORM, constants=mvp),
+            ps=dict(program=abi.PS_TEX_GRAD_MODULATE if aniso else abi.PS_TEX_MODULATE,
+                    samplers=["aniso" if aniso else "trilinear"]),
+            bs=dict(program=abi.BS_LERP_SRC_ALPHA)))
+    s.clear_color = (0.1, 0.2, 0.3, 1.0)
+    s.mvp = mvp
+    return s
+
+
+def stencil_mirror_scene(seed=7, width=128, height=128, samples=1, ntris=40):
+    """Stencil-mirror pattern: REPLACE the stencil under a quad, then draw
+    reflected geometry with stencil EQUAL (StencilMirror.cpp:560-578)."""
+    rng = np.random.default_rng(seed)
+    s = Scene("stencil_mirror", width, height, samples, ds_fmt=abi.FMT_RG32F)
+    quad = np.array([[-0.6, -0.6, 0.5, 1, 0.2, 0.2, 0.8, 1],
+                     [0.6, -0.6, 0.5, 1, 0.2, 0.2, 0.8, 1],
+                     [-0.6, 0.6, 0.5, 1, 0.2, 0.2, 0.8, 1],
+                     [0.6, 0.6, 0.5, 1, 0.2, 0.2, 0.8, 1]], dtype=np.float32)
+    s.buffers["quad"] = quad
+    s.buffers["quad_ib"] = np.array([0, 2, 1, 1, 2, 3], dtype=np.uint16)
+    pos = rng.uniform(-1, 1, size=(ntris * 3, 4))
+    pos[:, 2] = rng.uniform(0.05, 0.95, size=ntris * 3)
+    pos[:, 3] = 1.0
+    col = rng.uniform(0, 1, size=(ntris * 3, 4))
+    s.buffers["geo"] = np.concatenate([pos, col], axis=1).astype(np.float32)
+    ident = np.identity(4, dtype=np.float32)
+    mirror = np.diag([-1.0, 1.0, 1.0, 1.0]).astype(np.float32)
+    vp = (0, 0, width, height, 0.0, 1.0)
+    ds_write = default_depth_stencil()
+    ds_write.stencil_enable = 1
+    ds_write.depth_write = 0
+    for face in (ds_write.front, ds_write.back):
+        face.func = abi.CMP_ALWAYS
+        face.pass_op = abi.SOP_REPLACE
+    ds_test = default_depth_stencil()
+    ds_test.stencil_enable = 1
+    for face in (ds_test.front, ds_test.back):
+        face.func = abi.CMP_EQUAL
+        face.pass_op = abi.SOP_KEEP
+    s.draws.append(dict(viewport=vp, prim_count=2, index_buffer="quad_ib",
+                        index_format=abi.INDEX_U16, streams=[("quad", 32, 0)],
+                        inputs=VS_POS_COLOR_INPUTS, num_varyings=1,
+                        depth_stencil=ds_write, stencil_ref=1,
+                        vs=dict(program=abi.VS_TRANSFORM, constants=ident),
+                        ps=dict(program=abi.PS_COLOR), bs=dict(program=abi.BS_REPLACE)))
+    s.draws.append(dict(viewport=vp, prim_count=ntris, streams=[("geo", 32, 0)],
+                        inputs=VS_POS_COLOR_INPUTS, num_varyings=1,
+                        depth_stencil=ds_test, stencil_ref=1,
+                        vs=dict(program=abi.VS_TRANSFORM, constants=mirror),
+                        ps=dict(program=abi.PS_COLOR), bs=dict(program=abi.BS_REPLACE)))
+    return s
