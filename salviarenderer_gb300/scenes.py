@@ -254,6 +254,11 @@ GRID_INPUTS = [(abi.SEMANTIC_POSITION, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 0),
                (abi.SEMANTIC_COLOR, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 32)]
 
 
+COLOR_FIRST_INPUTS = [(abi.SEMANTIC_POSITION, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 0),
+                      (abi.SEMANTIC_COLOR, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 32),
+                      (abi.SEMANTIC_TEXCOORD, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 16)]
+
+
 def c2_scene(seed=20261204, width=1920, height=1080, samples=4, grid=317, tex_size=2048,
              ndraws=8, ds_fmt=abi.FMT_RG32F, max_aniso=16, af_draws=True):
     """Textured, filtered, alpha-blended height-field grid (the 1080p 4x workload)."""
@@ -336,4 +341,71 @@ def stencil_mirror_scene(seed=7, width=128, height=128, samples=1, ntris=40):
                         depth_stencil=ds_test, stencil_ref=1,
                         vs=dict(program=abi.VS_TRANSFORM, constants=mirror),
                         ps=dict(program=abi.PS_COLOR), bs=dict(program=abi.BS_REPLACE)))
+    return s
+
+
+def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=abi.TOPOLOGY_TRIANGLE_LIST,
+                  index_format=None, base_vertex=0, cull=abi.CULL_NONE, front_ccw=0,
+                  depth_func=abi.CMP_LESS, depth_write=1, depth_enable=1, blend=abi.BS_REPLACE,
+                  ps=abi.PS_COLOR, sampler=None, modifiers=(abi.AM_LINEAR, abi.AM_LINEAR),
+                  color_fmt=abi.FMT_RGBA8, ds_fmt=abi.FMT_RG32F, tex_size=64, uv_scale=3.0,
+                  eye_dist=(2.2, 3.2), draws=1, clear_depth=1.0):
+    """A small scene that exercises one combination of pipeline state.
+
+    Vertices carry position, a (u, v) pair and an RGBA colour.  Strips and
+    indexed draws reuse the same vertex pool; `draws` splits the primitives
+    over several draw calls sharing the state.
+    """
+    rng = np.random.default_rng(seed)
+    nv = ntris * 3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else ntris + 2
+    npool = nv if index_format is None else max(8, nv // 2)
+    pos = rng.uniform(-1.0, 1.0, size=(npool, 4))
+    pos[:, 3] = 1.0
+    uv = rng.uniform(-uv_scale, uv_scale, size=(npool, 4))
+    uv[:, 2:] = 0.0
+    col = rng.uniform(0.0, 1.0, size=(npool, 4))
+    col[:, 3] = rng.uniform(0.25, 1.0, size=npool)
+    pad = np.zeros((base_vertex, 12), dtype=np.float32)
+    verts = np.concatenate([pad, np.concatenate([pos, uv, col], axis=1).astype(np.float32)])
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    eye = d * rng.uniform(*eye_dist)
+    up = np.array([0.0, 1.0, 0.0]) if abs(d[1]) < 0.9 else np.array([1.0, 0.0, 0.0])
+    mvp = (look_at_lh(eye, [0, 0, 0], up) @
+           perspective_fov_lh(math.pi / 2, width / height, 0.1, 100.0)).astype(np.float32)
+    s = Scene("feature", width, height, samples, color_fmt=color_fmt, ds_fmt=ds_fmt)
+    s.clear_depth = clear_depth
+    s.clear_color = (0.05, 0.1, 0.15, 0.5)
+    s.buffers["vb"] = verts
+    if index_format is not None:
+        idx = rng.integers(0, npool, size=nv)
+        s.buffers["ib"] = idx.astype(np.uint16 if index_format == abi.INDEX_U16 else np.uint32)
+    if ps in (abi.PS_TEX_MODULATE, abi.PS_TEX_GRAD_MODULATE):
+        s.textures["tex"] = (to_rgba8(value_noise(rng, tex_size, octaves=4)), True)
+        s.samplers["s0"] = ("tex", dict(sampler or {}))
+    dsd = default_depth_stencil(depth_func=depth_func, depth_enable=depth_enable,
+                                depth_write=depth_write)
+    bounds = np.linspace(0, ntris, draws + 1).astype(np.int64)
+    for i in range(draws):
+        count = int(bounds[i + 1] - bounds[i])
+        if count == 0:
+            continue
+        first = int(bounds[i])
+        dd = dict(viewport=(0, 0, width, height, 0.0, 1.0), prim_count=count,
+                  topology=topology, streams=[("vb", 48, 0)],
+                  inputs=COLOR_FIRST_INPUTS if ps in (abi.PS_COLOR, abi.PS_CONSTANT) else GRID_INPUTS,
+                  num_varyings=len(modifiers), varying_modifiers=list(modifiers),
+                  cull_mode=cull, front_ccw=front_ccw, depth_stencil=dsd,
+                  base_vertex=base_vertex,
+                  vs=dict(program=abi.VS_TRANSFORM, constants=mvp),
+                  ps=dict(program=ps, samplers=["s0"] if "s0" in s.samplers else []),
+                  bs=dict(program=blend))
+        if index_format is not None:
+            dd.update(index_buffer="ib", index_format=index_format,
+                      start=first * (3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else 1))
+        else:
+            # draw(start, count) ignores `start` in the reference
+            # (index_fetcher.cpp:96-100); split draws use base_vertex instead.
+            dd["base_vertex"] = base_vertex + first * (3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else 1)
+        s.draws.append(dd)
     return s

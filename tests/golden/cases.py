@@ -1,0 +1,77 @@
+"""Golden cases: small seeded scenes rendered by the reference renderer.
+
+Each case is a name plus a zero-argument builder returning a
+salviarenderer_gb300.scenes.Scene.  make_golden.py renders every case with
+the reference's own compiled code (oracle/_ref) and stores the outputs;
+tests/test_oracle_golden.py checks the CPU restatement against them and the
+GPU tests reuse the same scenes.
+"""
+import math
+
+from salviarenderer_gb300 import abi, scenes
+
+F = scenes.feature_scene
+TRILINEAR = dict(min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+                 mip_filter=abi.FILTER_LINEAR)
+POINT = dict(min_filter=abi.FILTER_POINT, mag_filter=abi.FILTER_POINT, mip_filter=abi.FILTER_POINT)
+AF16 = dict(min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+            mip_filter=abi.FILTER_ANISOTROPIC, max_anisotropy=16)
+AF8 = dict(AF16, max_anisotropy=8)
+
+CASES = {
+    # C1 pattern: independent clip-space triangles, colour pass-through, LESS
+    "c1_128_1x": lambda: scenes.c1_scene(width=128, height=128, ntris=300),
+    "c1_128x96_4x": lambda: scenes.c1_scene(width=128, height=96, ntris=400, samples=4, seed=11),
+    "c1_64_2x": lambda: scenes.c1_scene(width=64, height=64, ntris=100, samples=2, seed=12),
+    "c1_near_clip_cull_back": lambda: scenes.c1_scene(width=128, height=128, ntris=600, seed=5,
+                                                      eye_dist=(0.4, 1.2), cull=abi.CULL_BACK),
+    "c1_odd_size_1x": lambda: scenes.c1_scene(width=100, height=76, ntris=250, seed=13),
+    # topology / index fetch
+    "strip_u16_base": lambda: F(seed=2, topology=abi.TOPOLOGY_TRIANGLE_STRIP, ntris=90,
+                                index_format=abi.INDEX_U16, base_vertex=5),
+    "list_u32_split": lambda: F(seed=3, index_format=abi.INDEX_U32, ntris=150, draws=3),
+    "strip_nonindexed": lambda: F(seed=4, topology=abi.TOPOLOGY_TRIANGLE_STRIP, ntris=60),
+    # raster state
+    "cull_front_ccw": lambda: F(seed=5, cull=abi.CULL_FRONT, front_ccw=1),
+    "cull_back_cw_4x": lambda: F(seed=6, cull=abi.CULL_BACK, samples=4),
+    # depth state
+    "depth_greater": lambda: F(seed=7, depth_func=abi.CMP_GREATER, clear_depth=0.0),
+    "depth_lequal_nowrite": lambda: F(seed=8, depth_func=abi.CMP_LESS_EQUAL, depth_write=0),
+    "depth_disabled_add": lambda: F(seed=9, depth_enable=0, blend=abi.BS_ADD),
+    # interpolation modifiers
+    "centroid_4x": lambda: F(seed=10, samples=4, modifiers=(abi.AM_CENTROID, abi.AM_LINEAR)),
+    "noperspective_nointerp": lambda: F(seed=11, modifiers=(abi.AM_NOPERSPECTIVE,
+                                                             abi.AM_NOINTERPOLATION)),
+    # colour formats
+    "rgba32f_target": lambda: F(seed=12, color_fmt=abi.FMT_RGBA32F, blend=abi.BS_LERP_SRC_ALPHA),
+    "bgra8_target_4x": lambda: F(seed=13, color_fmt=abi.FMT_BGRA8, samples=4),
+    # textures: filters, addressing, LOD quality
+    "tex_trilinear_wrap": lambda: F(seed=14, ps=abi.PS_TEX_MODULATE, sampler=TRILINEAR),
+    "tex_point_mirror": lambda: F(seed=15, ps=abi.PS_TEX_MODULATE,
+                                  sampler=dict(POINT, address_u=abi.ADDRESS_MIRROR,
+                                               address_v=abi.ADDRESS_MIRROR)),
+    "tex_linear_clamp_mippoint": lambda: F(seed=16, ps=abi.PS_TEX_MODULATE,
+                                           sampler=dict(TRILINEAR, mip_filter=abi.FILTER_POINT,
+                                                        address_u=abi.ADDRESS_CLAMP,
+                                                        address_v=abi.ADDRESS_CLAMP)),
+    "tex_mixed_address_lo_quality": lambda: F(seed=17, ps=abi.PS_TEX_MODULATE,
+                                              sampler=dict(TRILINEAR, address_u=abi.ADDRESS_WRAP,
+                                                           address_v=abi.ADDRESS_MIRROR,
+                                                           mip_quality=abi.MIP_LO_QUALITY)),
+    "tex_point_border_hi_quality": lambda: F(seed=18, ps=abi.PS_TEX_MODULATE,
+                                             sampler=dict(POINT, address_u=abi.ADDRESS_BORDER,
+                                                          address_v=abi.ADDRESS_BORDER,
+                                                          border_color=(1.0, 0.0, 1.0, 1.0),
+                                                          mip_quality=abi.MIP_HI_QUALITY)),
+    "tex_grad_af16_blend": lambda: F(seed=19, ps=abi.PS_TEX_GRAD_MODULATE, sampler=AF16,
+                                     blend=abi.BS_LERP_SRC_ALPHA, uv_scale=6.0),
+    "tex_grad_af8_4x": lambda: F(seed=20, ps=abi.PS_TEX_GRAD_MODULATE, sampler=AF8, samples=4),
+    "tex_grad_trilinear": lambda: F(seed=21, ps=abi.PS_TEX_GRAD_MODULATE, sampler=TRILINEAR),
+    # C2 pattern (textured grid, trilinear + 16x AF, src-alpha blend)
+    "c2_160x96_4x": lambda: scenes.c2_scene(width=160, height=96, grid=33, tex_size=128, ndraws=4),
+    "c2_128x72_1x": lambda: scenes.c2_scene(width=128, height=72, grid=25, tex_size=64, samples=1,
+                                            ndraws=2, seed=3),
+    # stencil mirror (REPLACE then EQUAL)
+    "stencil_mirror_1x": lambda: scenes.stencil_mirror_scene(),
+    "stencil_mirror_4x": lambda: scenes.stencil_mirror_scene(samples=4, seed=8),
+}

@@ -1,0 +1,68 @@
+"""Regenerates the golden fixtures from the reference renderer itself.
+
+Needs the reference library built from the reference's own sources:
+    make -C oracle/ref REF=<path to SalviaRenderer>
+then, from the repository root:
+    python tests/golden/make_golden.py
+
+For every case in cases.py it renders the scene through the reference's
+public API (oracle/_ref/libsalvia_ref.so) and stores, per case, the colour,
+depth-stencil and resolved targets, the pipeline counters and a digest of the
+scene's inputs in <case>.npz.  A mip-chain fixture pins
+texture_2d::gen_mipmap.
+"""
+import ctypes
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+from salviarenderer_gb300 import abi, Device, scenes  # noqa: E402
+import cases  # noqa: E402
+
+
+def scene_digest(scene):
+    h = hashlib.sha256()
+    for k in sorted(scene.buffers):
+        h.update(k.encode())
+        h.update(np.ascontiguousarray(scene.buffers[k]).tobytes())
+    for k in sorted(scene.textures):
+        h.update(k.encode())
+        h.update(np.ascontiguousarray(scene.textures[k][0]).tobytes())
+    return h.hexdigest()
+
+
+def mip_texture():
+    rng = np.random.default_rng(99)
+    return scenes.to_rgba8(scenes.value_noise(rng, 64, octaves=4))[:, :, :]
+
+
+def main():
+    lib = abi.bind(ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libsalvia_ref.so")))
+    dev = Device(lib)
+    for name, build in cases.CASES.items():
+        s = build()
+        out = scenes.render(dev, s, stats=True)
+        stats = np.array([[st[k] for k, _ in abi.DrawStats._fields_] for st in out.pop("stats")],
+                         dtype=np.uint64)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), digest=scene_digest(s),
+                            stats=stats, **out)
+        print(name, {k: v.shape for k, v in out.items()}, stats.sum(axis=0).tolist())
+    # texture_2d::gen_mipmap(filter_linear) on a 64x64 RGBA8 texture
+    img = mip_texture()
+    t = dev.texture(64, 64, 1, abi.FMT_RGBA8)
+    dev.texture_upload(t, img)
+    dev.gen_mipmap(t, abi.FILTER_LINEAR)
+    levels = {f"level{i}": dev.texture_download(t, i) for i in range(dev.levels(t))}
+    np.savez_compressed(os.path.join(HERE, "mipchain_64.npz"), **levels)
+    print("mipchain_64", len(levels))
+
+
+if __name__ == "__main__":
+    main()
