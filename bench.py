@@ -1,0 +1,343 @@
+#!/usr/bin/env python
+"""Benchmark: frames/s (and Gpix/s) of the 1080p 4x MSAA textured workload.
+
+Workload ("c2"): 1920x1080 RGBA8, 4x MSAA, RG32F depth-stencil (the
+reference's depth format), a 317x317-vertex height-field grid (199,712
+triangles) in 8 indexed draws; one 2048^2 RGBA8 value-noise texture with a
+12-level box mip chain, trilinear on even draws and 16x anisotropic on odd
+draws; src-alpha blending; depth LESS; clear + 8 draws + MSAA resolve per
+frame.  Inputs are synthetic and seeded (numpy PCG64, seed 20261204).
+
+One step = one frame.  `value` times the frame with every input resident in
+HBM (CUDA events on the renderer's stream, L2 flushed between steps with a
+256 MiB write); `e2e` times the same frame through the C ABI from pinned
+host memory: vertex and index upload, the frame, and the download of the
+resolved image.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+--impl reference times the reference's CPU path on the host cores: the
+CPU restatement of the reference renderer (oracle/), one frame per process
+across all host cores.  Multi-GPU runs are replicas (each rank renders its own
+frames; no data exchange).
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s at 1920x1080 4xMSAA (textured trilinear+16xAF, src-alpha blend, 199,712 tris)"
+UNIT = "frames/s"
+SEED = 20261204
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(scene):
+    return {"workload": "c2_1080p_4xmsaa_textured_af16_blend", "width": scene.width,
+            "height": scene.height, "samples": scene.samples, "triangles": scene.triangles,
+            "draws": len(scene.draws), "texture": "2048x2048 RGBA8 + 11 mips",
+            "depth_format": "RG32F", "l2": "flushed between steps (256 MiB write)",
+            "seed": SEED}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes of the raster stage for one frame (every item once)
+def raster_bytes(scene):
+    npx = scene.width * scene.height
+    s = scene.samples
+    ds = 8   # RG32F
+    col = 4  # RGBA8
+    fb = 2 * npx * s * ds + 2 * npx * s * col          # depth RMW (early-Z) + colour RMW (blend)
+    tex = 0
+    for img, mips in scene.textures.values():
+        level0 = img.nbytes
+        tex += level0 * 4 // 3 if mips else level0      # every level sampled at most once
+    rec_bytes = (5 + 3 * 3) * 16                         # triangle record, 2 varyings
+    tris = rec_bytes * scene.triangles
+    return fb + tex + tris
+
+
+def read_traffic():
+    """Per-launch DRAM traffic of k_raster from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_raster_c2_1080p_4x.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def measured_peak():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, index):
+        self.index, self.samples, self.proc = index, [], None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for s in self.samples for n, v in zip(names, s[4:8]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons}
+
+
+# ---------------------------------------------------------------------------
+def cpu_oracle_fps(scene_kw, frames=1):
+    """The CPU restatement on one host core: seconds for `frames` full frames."""
+    from salviarenderer_gb300 import abi, Device, scenes
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    lib = abi.bind(ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", "libsg_oracle.so")))
+    dev = Device(lib)
+    scene = scenes.c2_scene(**scene_kw)
+    b = scenes.Bound(dev, scene)
+    b.frame()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        b.frame()
+    return time.perf_counter() - t0
+
+
+_WORKER = {}
+
+
+def _worker_init(scene_kw):
+    from salviarenderer_gb300 import abi, Device, scenes
+    lib = abi.bind(ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", "libsg_oracle.so")))
+    dev = Device(lib)
+    _WORKER["b"] = scenes.Bound(dev, scenes.c2_scene(**scene_kw))
+    _WORKER["dev"] = dev
+
+
+def _worker_frame(_):
+    t0 = time.perf_counter()
+    _WORKER["b"].frame()
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    """CPU reference arm: the restatement, one frame per process on every core."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    from salviarenderer_gb300 import scenes
+    cores = os.cpu_count() or 1
+    kw = dict(seed=SEED)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_worker_init, initargs=(kw,)) as pool:
+        for _ in range(args.warmup):
+            pool.map(_worker_frame, range(cores))
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            pool.map(_worker_frame, range(cores))
+        dt = time.perf_counter() - t0
+    fps = args.steps * cores / dt
+    scene = scenes.c2_scene(**kw)
+    line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": workload_config(scene),
+            "cpu_baseline": {"value": fps, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{cores} full frames per step, one per process"},
+            "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from salviarenderer_gb300 import abi, Device, scenes
+    from salviarenderer_gb300 import build as pbuild
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    # a dedicated stream: the renderer and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    lib = abi.bind(ctypes.CDLL(pbuild.ensure_built()))
+    dev = Device(lib, cuda_device=local, stream=stream.cuda_stream)
+    scene = scenes.c2_scene(seed=SEED + rank)
+    b = scenes.Bound(dev, scene)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    for _ in range(args.warmup):
+        b.frame()
+    dev.sync()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    # device-resident timing, profiled per stage
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    dev.profile_enable(True)
+    barrier()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            b.frame()
+            ends[i].record(stream)
+        barrier()
+    dev.sync()
+    prof = dev.profile_read()
+    dev.profile_enable(False)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(step_ms) / 1000.0
+    if world > 1:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    frames = args.steps * world
+    fps = frames / total_s
+
+    # end to end through the C ABI from pinned host memory
+    vb_host = torch.from_numpy(scene.buffers["vb"]).pin_memory()
+    ib_host = torch.from_numpy(scene.buffers["ib"]).pin_memory()
+    out_bytes = scene.width * scene.height * 4
+    res_host = torch.empty(out_bytes, dtype=torch.uint8).pin_memory()
+    vb_h, ib_h = b.buf["vb"], b.buf["ib"]
+
+    def e2e_frame():
+        lib.sg_buffer_upload(dev.handle, vb_h, 0, ctypes.c_void_p(vb_host.data_ptr()), vb_host.numel() * 4)
+        lib.sg_buffer_upload(dev.handle, ib_h, 0, ctypes.c_void_p(ib_host.data_ptr()), ib_host.numel() * 4)
+        b.frame()
+        st = lib.sg_texture_download(dev.handle, b.resolved, 0, ctypes.c_void_p(res_host.data_ptr()), out_bytes)
+        if st != abi.SG_OK:
+            raise RuntimeError("sg_texture_download failed")
+
+    for _ in range(args.warmup):
+        e2e_frame()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        e2e_frame()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_fps = frames / e2e_s
+
+    if rank == 0:
+        peak, peak_kind = measured_peak()
+        raster_launch_ms = prof["raster_ms"] / max(1, prof["raster_launches"])
+        bytes_per_launch = raster_bytes(scene) / len(scene.draws)
+        achieved = bytes_per_launch / (raster_launch_ms / 1000.0) / 1e9
+        cpu = None
+        if not args.no_cpu_baseline:
+            frames_cpu = 2
+            dt = cpu_oracle_fps(dict(seed=SEED), frames=frames_cpu)
+            cpu = {"value": frames_cpu / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": f"{frames_cpu} full frames of the same workload, single-threaded CPU restatement"}
+        line = {
+            "metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded height-field grid + value-noise texture)",
+            "config": dict(workload_config(scene), parallelism=f"replicas x{world}"),
+            "gpix_per_s": fps * scene.width * scene.height / 1e9,
+            "gsamples_per_s": fps * scene.width * scene.height * scene.samples / 1e9,
+            "mtris_per_s": fps * scene.triangles / 1e6,
+            "stage_ms_per_frame": {"geometry": prof["geometry_ms"] / args.steps,
+                                   "binning": prof["binning_ms"] / args.steps,
+                                   "raster": prof["raster_ms"] / args.steps},
+            "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": read_traffic(),
+                         "algorithmic_bytes_per_launch": bytes_per_launch,
+                         "launch_ms": raster_launch_ms},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_fps, "unit": UNIT,
+                    "h2d_bytes_per_step": int(vb_host.numel() * 4 + ib_host.numel() * 4),
+                    "d2h_bytes_per_step": out_bytes},
+            "gpu_launches": int(prof["launches"]),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

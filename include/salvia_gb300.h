@@ -219,6 +219,24 @@ typedef struct sg_draw_stats {
   uint64_t backend_input_pixels;       /* pixels of quads that reached the output merger */
 } sg_draw_stats;
 
+/* Per-stage device time and launch counts, accumulated while profiling is
+ * enabled (the pipeline_profiles query, async_object.h:177-233): geometry
+ * covers the reference's vtx_proc/clipping/compact_clip/vp_trans stages,
+ * binning its tri_dispatch stage, raster its ras stage.  Times come from
+ * CUDA events recorded on the device's stream around each stage; the
+ * reference's ras stage is split into cover, shade and merge here. */
+typedef struct sg_profile_data {
+  double geometry_ms;
+  double binning_ms;
+  double raster_ms;           /* cover + shade + merge */
+  double cover_ms;            /* coverage + early-Z */
+  double shade_ms;            /* attribute interpolation + pixel shader */
+  double merge_ms;            /* depth-stencil + blend */
+  uint64_t draws;
+  uint64_t launches;          /* kernels launched (all stages, clears, resolves) */
+  uint64_t raster_launches;
+} sg_profile_data;
+
 /* ---- device (create_benchmark_renderer, renderer.h:133-134) --------------- */
 typedef struct sg_device sg_device;
 
@@ -230,6 +248,12 @@ void sg_device_destroy(sg_device* dev);
 int32_t sg_sync(sg_device* dev);
 /* Last CUDA error text seen by the device (empty when none). */
 const char* sg_last_error(sg_device* dev);
+/* Starts (enable != 0) or stops per-stage timing and resets the counters
+ * (renderer::begin/end on a pipeline_profiles query, renderer.h:116-119). */
+int32_t sg_profile_enable(sg_device* dev, int32_t enable);
+/* Waits for the device and returns the accumulated profile
+ * (renderer::get_data, renderer.h:118). */
+int32_t sg_profile_read(sg_device* dev, sg_profile_data* out);
 
 /* ---- buffers (create_buffer + map/unmap, renderer.h:45,61-63) -------------- */
 int32_t sg_buffer_create(sg_device* dev, size_t size, uint32_t* out_buffer);

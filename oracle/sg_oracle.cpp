@@ -1387,6 +1387,17 @@ void attr_one(draw_ctx const& c, vso& out, vso const& in, float s0, vso const& d
 void draw_quad(rasterizer_state& rs, tri_info const& ti, uint32_t left, uint32_t top,
                uint64_t quad_mask, bool full, float const* aa) {
   draw_ctx const& c = *rs.c;
+  // EXTENSION: pixels outside the render target are not covered.  The
+  // reference writes past the row end there (targets whose width or height
+  // is not a multiple of 4); for multiple-of-4 sizes this never triggers.
+  for (int i = 0; i < 4; ++i) {
+    if (left + (i & 1) >= static_cast<uint32_t>(c.target_w) ||
+        top + ((i & 2) >> 1) >= static_cast<uint32_t>(c.target_h)) {
+      quad_mask &= ~(0xFFFFull << (16 * i));
+      full = false;
+    }
+  }
+  if (quad_mask == 0) return;
   vso px[4];
   vso const& v0 = *ti.v0;
   float dx = 0.5f + left - v0.r[0][0];
@@ -1725,6 +1736,13 @@ int32_t sg_device_create(int32_t, void*, sg_device** out) {
 void sg_device_destroy(sg_device* d) { delete d; }
 int32_t sg_sync(sg_device*) { return SG_OK; }
 const char* sg_last_error(sg_device*) { return ""; }
+// The restatement is synchronous and keeps no stage timers.
+int32_t sg_profile_enable(sg_device*, int32_t) { return SG_OK; }
+int32_t sg_profile_read(sg_device*, sg_profile_data* out) {
+  if (!out) return SG_INVALID_PARAMETER;
+  std::memset(out, 0, sizeof(*out));
+  return SG_OK;
+}
 
 int32_t sg_buffer_create(sg_device* d, size_t size, uint32_t* out) {
   *out = d->st.next++;

@@ -100,6 +100,12 @@ class DrawDesc(C.Structure):
                 ("stencil_ref", C.c_int32), ("vs", Shader), ("ps", Shader), ("bs", Shader)]
 
 
+class ProfileData(C.Structure):
+    _fields_ = [("geometry_ms", C.c_double), ("binning_ms", C.c_double), ("raster_ms", C.c_double),
+                ("cover_ms", C.c_double), ("shade_ms", C.c_double), ("merge_ms", C.c_double),
+                ("draws", C.c_uint64), ("launches", C.c_uint64), ("raster_launches", C.c_uint64)]
+
+
 class DrawStats(C.Structure):
     _fields_ = [("ia_primitives", C.c_uint64), ("cprimitives", C.c_uint64),
                 ("ps_invocations", C.c_uint64), ("backend_input_pixels", C.c_uint64)]
@@ -112,6 +118,8 @@ SIGNATURES = {
     "sg_device_destroy": (None, [C.c_void_p]),
     "sg_sync": (C.c_int32, [C.c_void_p]),
     "sg_last_error": (C.c_char_p, [C.c_void_p]),
+    "sg_profile_enable": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "sg_profile_read": (C.c_int32, [C.c_void_p, C.POINTER(ProfileData)]),
     "sg_buffer_create": (C.c_int32, [C.c_void_p, C.c_size_t, _u32p]),
     "sg_buffer_upload": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_size_t, C.c_void_p, C.c_size_t]),
     "sg_buffer_download": (C.c_int32,

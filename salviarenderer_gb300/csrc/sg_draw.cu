@@ -1,0 +1,559 @@
+// sg_draw.cu -- the draw pipeline as sm_103a kernels.
+//
+//   k_geometry   one thread per input primitive: index fetch, vertex shader,
+//                near/far clipping and culling, viewport transform and
+//                projection, triangle setup -> compact triangle records.
+//   k_bin<count/fill>   one warp per chunk of triangle slots, walking them in
+//                API order: the reference's per-tile trivial reject/accept
+//                test, emitted into per-(tile, chunk) runs so that every
+//                tile list comes out in API order without a sort.
+//   k_scan_*     exclusive scan of the per-(tile, chunk) counts.
+//   k_raster     one CTA per 64x64 tile (dynamically scheduled); each thread
+//                owns a 4x4 pixel block and replays the reference's 64->16->4
+//                classification, quad coverage and early-Z for its block in
+//                primitive order, emitting quad fragments; fragments are
+//                shaded in parallel (4 lanes per quad, derivatives by
+//                shuffle) and merged by their owners in primitive order.
+#include <cuda_runtime.h>
+
+#include "sg_draw.cuh"
+
+namespace sg {
+
+// ---------------------------------------------------------------------------
+// vertex processing
+template <int NA>
+struct vtx {
+  v4 r[1 + NA];
+};
+
+// Reads past the end of a buffer are undefined in the reference; here they
+// read zeros and are counted in fetch_oob.
+__device__ inline uint32_t fetch_index(DrawParams const& p, uint32_t id) {
+  if (!p.index_base) return id + static_cast<uint32_t>(p.base_vertex);
+  if (id >= p.index_count) {
+    atomicAdd(&p.counters->fetch_oob, 1u);
+    return static_cast<uint32_t>(p.base_vertex);
+  }
+  uint32_t v = p.index_stride == 2 ? reinterpret_cast<uint16_t const*>(p.index_base)[id]
+                                   : reinterpret_cast<uint32_t const*>(p.index_base)[id];
+  return v + static_cast<uint32_t>(p.base_vertex);
+}
+
+// stream_assembler::fetch_vertex / get_vec4 (stream_assembler.cpp:26-93)
+__device__ inline v4 fetch_input(DrawParams const& p, int r, uint32_t index) {
+  uint32_t slot = p.in_slot[r];
+  uint64_t off = static_cast<uint64_t>(p.stream_stride[slot]) * index + p.in_off[r];
+  uint32_t n = p.in_fmt[r] == SG_VFMT_R32_FLOAT ? 4 : p.in_fmt[r] == SG_VFMT_R32G32_FLOAT ? 8
+             : p.in_fmt[r] == SG_VFMT_R32G32B32_FLOAT ? 12 : 16;
+  if (off + n > p.stream_bytes[slot] || (off & 3)) {
+    atomicAdd(&p.counters->fetch_oob, 1u);
+    return mk4(0, 0, 0, 0);
+  }
+  float const* f = reinterpret_cast<float const*>(p.stream_base[slot] + off);
+  float dw = p.in_dw[r];
+  switch (p.in_fmt[r]) {
+  case SG_VFMT_R32_FLOAT: return mk4(f[0], 0.0f, 0.0f, dw);
+  case SG_VFMT_R32G32_FLOAT: return mk4(f[0], f[1], 0.0f, dw);
+  case SG_VFMT_R32G32B32_FLOAT: return mk4(f[0], f[1], f[2], dw);
+  default: return mk4(f[0], f[1], f[2], f[3]);
+  }
+}
+
+// eflib::transform(out, v, m) (eflib/src/math.cpp:142-154): out[j] = dot_prod4(v, column j)
+__device__ inline v4 transform(v4 v, float const* m) {
+  float o[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) o[j] = v.x * m[j] + v.y * m[4 + j] + v.z * m[8 + j] + v.w * m[12 + j];
+  return mk4(o[0], o[1], o[2], o[3]);
+}
+
+template <int NA>
+__device__ void run_vs(DrawParams const& p, uint32_t index, vtx<NA>& out) {
+  v4 in[SG_MAX_VS_INPUTS];
+#pragma unroll
+  for (int r = 0; r < SG_MAX_VS_INPUTS; ++r) in[r] = mk4(0, 0, 0, 0);
+  for (int r = 0; r < static_cast<int>(p.num_inputs); ++r) in[r] = fetch_input(p, r, index);
+  switch (p.vs_prog) {
+  case SG_VS_TRANSFORM:
+    out.r[0] = transform(in[0], p.vs_k);
+#pragma unroll
+    for (int i = 0; i < NA; ++i) out.r[1 + i] = in[1 + i];
+    break;
+  case SG_VS_MORPH_DISPLACE: {
+    v4 pp = in[0] + (in[1] - in[0]) * p.vs_k[16];
+    v4 n = in[2];
+    float h = sample_impl(p.vs_samp, in[3].x, in[3].y, 0.0f, nullptr).x;
+    float hs = h * p.vs_k[17];
+    pp.x = pp.x + n.x * hs;
+    pp.y = pp.y + n.y * hs;
+    pp.z = pp.z + n.z * hs;
+    out.r[0] = transform(pp, p.vs_k);
+    if constexpr (NA > 0) out.r[1] = in[3];
+    if constexpr (NA > 1) out.r[2] = n;
+#pragma unroll
+    for (int i = 2; i < NA; ++i) out.r[1 + i] = mk4(0, 0, 0, 0);
+    break;
+  }
+  default:
+    out.r[0] = mk4(0, 0, 0, 1);
+#pragma unroll
+    for (int i = 0; i < NA; ++i) out.r[1 + i] = mk4(0, 0, 0, 0);
+    break;
+  }
+}
+
+// cull functions (raster_state.cpp:10-32)
+__device__ inline bool cull(DrawParams const& p, float area) {
+  if (p.cull_mode == SG_CULL_NONE) return false;
+  bool cull_ccw = (p.cull_mode == SG_CULL_FRONT) ? (p.front_ccw != 0) : (p.front_ccw == 0);
+  return cull_ccw ? (area <= 0) : (area >= 0);
+}
+
+// vs_output_op lerp_n (shader.cpp:170-180)
+template <int NA>
+__device__ inline void vtx_lerp(DrawParams const& p, vtx<NA>& out, vtx<NA> const& a, vtx<NA> const& b, float t) {
+  out.r[0] = a.r[0] + (b.r[0] - a.r[0]) * t;
+#pragma unroll
+  for (int i = 0; i < NA; ++i) {
+    out.r[1 + i] = a.r[1 + i];
+    if (!(p.mods[i] & SG_AM_NOINTERPOLATION)) out.r[1 + i] = out.r[1 + i] + (b.r[1 + i] - a.r[1 + i]) * t;
+  }
+}
+
+__device__ inline float clip_d(int plane, v4 q) {  // dot_prod4 with planes (0,0,1,0), (0,0,-1,1)
+  return plane == 0 ? (((0.0f * q.x + 0.0f * q.y) + 1.0f * q.z) + 0.0f * q.w)
+                    : (((0.0f * q.x + 0.0f * q.y) + -1.0f * q.z) + 1.0f * q.w);
+}
+
+// viewport_transform + project_n (shader.cpp:499-511, 117-134)
+template <int NA>
+__device__ inline void vp_project(DrawParams const& p, vtx<NA>& v) {
+  v4 q = v.r[0];
+  float invw = eq_eps(q.w, 0.0f) ? 1.0f : 1.0f / q.w;
+  v4 pos = q * invw;
+  float ox = (p.vp_x + p.vp_w) * 0.5f;
+  float oy = (p.vp_y + p.vp_h) * 0.5f;
+  v.r[0] = mk4((p.vp_w * 0.5f) * pos.x + ox, (p.vp_h * 0.5f) * -pos.y + oy,
+               (p.vp_maxz - p.vp_minz) * pos.z + p.vp_minz, invw);
+#pragma unroll
+  for (int i = 0; i < NA; ++i)
+    if (!(p.mods[i] & SG_AM_NOPERSPECTIVE)) v.r[1 + i] = v.r[1 + i] * invw;
+}
+
+// rasterizer::compute_triangle_info (rasterizer.cpp:864-945) + compute_derivative_n
+// (shader.cpp:414-449); writes the record, returns false for zero area.
+template <int NA>
+__device__ bool setup_triangle(DrawParams const& p, vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c,
+                               float4* rec) {
+  vtx<NA> const* verts[3] = {&a, &b, &c};
+  double dist[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    dist[i] = fabs(static_cast<double>(verts[i]->r[0].x)) + fabs(static_cast<double>(verts[i]->r[0].y));
+  int r0;
+  if (dist[0] < dist[1])
+    r0 = dist[0] < dist[2] ? 0 : 2;
+  else
+    r0 = dist[1] < dist[2] ? 1 : 2;
+  int r1 = (r0 + 1) % 3, r2 = (r1 + 1) % 3;
+  vtx<NA> const& v0 = *verts[r0];
+  vtx<NA> const& v1 = *verts[r1];
+  vtx<NA> const& v2 = *verts[r2];
+  v4 e01p = v1.r[0] - v0.r[0], e02p = v2.r[0] - v0.r[0];
+  float area = e02p.x * e01p.y - e02p.y * e01p.x;
+  if (eq_eps(area, 0.0f)) return false;
+  float inv_area = 1.0f / area;
+  v4 pa = a.r[0], pb = b.r[0], pc = c.r[0];
+  float4 bb = make_float4(smin(smin(pa.x, pb.x), pc.x), smax(smax(pa.x, pb.x), pc.x),
+                          smin(smin(pa.y, pb.y), pc.y), smax(smax(pa.y, pb.y), pc.y));
+  v4 vp[3] = {pa, pb, pc};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    v4 s = vp[i], e = vp[(i + 1) % 3];
+    rec[i] = make_float4(s.y - e.y, e.x - s.x, e.x * s.y - e.y * s.x, 0.0f);
+  }
+  rec[3] = bb;
+  rec[4] = make_float4(area > 0.0f ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f);
+  float e01x = e01p.x, e01y = e01p.y, e02x = e02p.x, e02y = e02p.y;
+  constexpr int R = 1 + NA;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    v4 e01 = v1.r[i] - v0.r[i], e02 = v2.r[i] - v0.r[i];
+    float xd[4], yd[4];
+    float const* p01 = &e01.x;
+    float const* p02 = &e02.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      xd[k] = (p02[k] * e01y - p01[k] * e02y) * inv_area;
+      yd[k] = (p01[k] * e02x - p02[k] * e01x) * inv_area;
+    }
+    rec[5 + i] = make_float4(v0.r[i].x, v0.r[i].y, v0.r[i].z, v0.r[i].w);
+    rec[5 + R + i] = make_float4(xd[0], xd[1], xd[2], xd[3]);
+    rec[5 + 2 * R + i] = make_float4(yd[0], yd[1], yd[2], yd[3]);
+  }
+  return true;
+}
+
+template <int NA>
+__device__ void emit_triangle(DrawParams const& p, uint32_t slot, vtx<NA> a, vtx<NA> b, vtx<NA> c,
+                              unsigned long long& ntri) {
+  ++ntri;
+  vp_project(p, a);
+  vp_project(p, b);
+  vp_project(p, c);
+  alignas(16) float4 rec[rec_stride_for(NA)];
+  bool ok = setup_triangle(p, a, b, c, rec);
+  uint32_t idx = NO_REC;
+  if (ok) {
+    idx = atomicAdd(&p.counters->rec_count, 1u);
+    float4* dst = p.recs + static_cast<size_t>(idx) * p.rec_stride;
+#pragma unroll
+    for (int i = 0; i < static_cast<int>(rec_stride_for(NA)); ++i) dst[i] = rec[i];
+  }
+  p.slot_rec[slot] = idx;
+}
+
+// clipper::clip_solid_triangle + clip_triangle_to_poly_general (clipper.cpp:43-228)
+template <int NA>
+__global__ void __launch_bounds__(128) k_geometry(DrawParams p) {
+  uint32_t prim = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long ntri = 0;
+  if (prim < p.prim_count) {
+    uint32_t ids[3];
+    if (p.strip) {
+      ids[0] = prim;
+      ids[1] = prim + 1;
+      ids[2] = prim + 2;
+      if (prim & 1) {
+        uint32_t t = ids[0];
+        ids[0] = ids[2];
+        ids[2] = t;
+      }
+    } else {
+      ids[0] = prim * 3;
+      ids[1] = prim * 3 + 1;
+      ids[2] = prim * 3 + 2;
+    }
+    vtx<NA> tv[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) run_vs(p, fetch_index(p, ids[i]), tv[i]);
+    uint32_t slot0 = prim * 3;
+    p.slot_rec[slot0 + 1] = NO_REC;
+    p.slot_rec[slot0 + 2] = NO_REC;
+    bool in_frustum = true;
+#pragma unroll
+    for (int pl = 0; pl < 2; ++pl)
+#pragma unroll
+      for (int v = 0; v < 3; ++v)
+        if (clip_d(pl, tv[v].r[0]) < 0) in_frustum = false;
+    if (in_frustum) {
+      float pv[3][2];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        float iw = 1.0f / tv[i].r[0].w;
+        pv[i][0] = tv[i].r[0].x * iw;
+        pv[i][1] = tv[i].r[0].y * iw;
+      }
+      float area = (pv[2][0] - pv[0][0]) * (pv[1][1] - pv[0][1]) - (pv[2][1] - pv[0][1]) * (pv[1][0] - pv[0][0]);
+      bool front = area > 0.0f;
+      if (cull(p, front ? 1.0f : -1.0f)) {
+        p.slot_rec[slot0] = NO_REC;
+      } else if (front) {
+        emit_triangle<NA>(p, slot0, tv[0], tv[1], tv[2], ntri);
+      } else {
+        emit_triangle<NA>(p, slot0, tv[0], tv[2], tv[1], ntri);
+      }
+    } else {
+      // Sutherland-Hodgman against the near (z >= 0) and far (z <= w) planes.
+      vtx<NA> pool[7];
+      pool[0] = tv[0];
+      pool[1] = tv[1];
+      pool[2] = tv[2];
+      int npool = 3;
+      int poly[2][5];
+      int n[2] = {3, 0};
+      poly[0][0] = 0;
+      poly[0][1] = 1;
+      poly[0][2] = 2;
+      int src = 0, dst = 1;
+      bool is_front = false, culled = false;
+      float d0 = 0.0f, d1 = 0.0f;
+      for (int pl = 0; pl < 2 && !culled; ++pl) {
+        n[dst] = 0;
+        if (n[src] != 0) d0 = clip_d(pl, pool[poly[src][0]].r[0]);
+        for (int i = 0, j = 1; i < n[src]; ++i, ++j) {
+          j %= n[src];
+          d1 = clip_d(pl, pool[poly[src][j]].r[0]);
+          if (d0 >= 0.0f) {
+            poly[dst][n[dst]++] = poly[src][i];
+            if (d1 < 0.0f) {
+              vtx_lerp(p, pool[npool], pool[poly[src][i]], pool[poly[src][j]], d0 / (d0 - d1));
+              poly[dst][n[dst]++] = npool++;
+            }
+          } else if (d1 >= 0.0f) {
+            vtx_lerp(p, pool[npool], pool[poly[src][j]], pool[poly[src][i]], d1 / (d1 - d0));
+            poly[dst][n[dst]++] = npool++;
+          }
+          d0 = d1;
+        }
+        if (pl == 0 && n[dst] >= 3) {
+          float pv[3][2];
+          for (int i = 0; i < 3; ++i) {
+            v4 q = pool[poly[dst][i]].r[0];
+            float inv_abs_w = 1.0f / fabsf(q.w);
+            pv[i][0] = q.x * inv_abs_w;
+            pv[i][1] = q.y * inv_abs_w;
+          }
+          float area = (pv[2][0] - pv[0][0]) * (pv[1][1] - pv[0][1]) - (pv[2][1] - pv[0][1]) * (pv[1][0] - pv[0][0]);
+          is_front = area > 0.0f;
+          if (cull(p, area)) culled = true;
+        }
+        src ^= 1;
+        dst ^= 1;
+      }
+      int nv = culled ? 0 : n[src];
+      p.slot_rec[slot0] = NO_REC;
+      for (int t = 1; t + 1 < nv; ++t) {
+        int ia = poly[src][0], ib = poly[src][is_front ? t : t + 1], ic = poly[src][is_front ? t + 1 : t];
+        emit_triangle<NA>(p, slot0 + (t - 1), pool[ia], pool[ib], pool[ic], ntri);
+      }
+    }
+  }
+  // warp-aggregated counter update
+  for (int o = 16; o > 0; o >>= 1) ntri += __shfl_down_sync(0xFFFFFFFFu, ntri, o);
+  if ((threadIdx.x & 31) == 0 && ntri) atomicAdd(&p.counters->cprimitives, ntri);
+}
+
+// ---------------------------------------------------------------------------
+// binning (rasterizer::threaded_dispatch_primitive, rasterizer.cpp:775-862)
+template <bool FILL>
+__global__ void __launch_bounds__(128) k_bin(DrawParams p, uint32_t nslots) {
+  uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= p.nchunks) return;
+  uint32_t begin = warp * p.chunk, end = min(begin + p.chunk, nslots);
+  int const tx_n = p.tiles_x, ty_n = p.tiles_y;
+  uint32_t* cnt = p.bin_counts;
+  for (uint32_t base = begin; base < end; base += 32) {
+    // every lane fetches its own slot's triangle (parallel loads)
+    uint32_t slot = base + lane;
+    uint32_t rec = slot < end ? p.slot_rec[slot] : NO_REC;
+    float4 e0 = make_float4(0, 0, 0, 0), e1 = e0, e2 = e0;
+    int sx = 0, sy = 0, ex = 0, ey = 0;
+    if (rec != NO_REC) {
+      float4 const* R = p.recs + static_cast<size_t>(rec) * p.rec_stride;
+      e0 = R[0];
+      e1 = R[1];
+      e2 = R[2];
+      float4 bb = R[3];
+      sx = min(fast_floori(static_cast<double>(smax(0.0f, bb.x) / TILE)), tx_n);
+      sy = min(fast_floori(static_cast<double>(smax(0.0f, bb.z) / TILE)), ty_n);
+      ex = min(fast_ceili(static_cast<double>(smax(0.0f, bb.y) / TILE)) + 1, tx_n);
+      ey = min(fast_ceili(static_cast<double>(smax(0.0f, bb.w) / TILE)) + 1, ty_n);
+      // finite inputs always land in [0, n]; the clamps only bound non-finite ones
+      sx = max(sx, 0);
+      sy = max(sy, 0);
+      ex = max(ex, 0);
+      ey = max(ey, 0);
+    }
+    uint32_t valid = __ballot_sync(0xFFFFFFFFu, rec != NO_REC);
+    // then the warp walks them in slot order (API order), one at a time
+    while (valid) {
+      int i = __ffs(valid) - 1;
+      valid &= valid - 1;
+      uint32_t r = __shfl_sync(0xFFFFFFFFu, rec, i);
+      int tsx = __shfl_sync(0xFFFFFFFFu, sx, i), tsy = __shfl_sync(0xFFFFFFFFu, sy, i);
+      int tex = __shfl_sync(0xFFFFFFFFu, ex, i), tey = __shfl_sync(0xFFFFFFFFu, ey, i);
+      if (tsx + 1 == tex && tsy + 1 == tey) {
+        // single-tile primitive: pushed without the tile tests (rasterizer.cpp:809-811)
+        if (lane == 0) {
+          uint32_t* c = cnt + static_cast<size_t>(tsy * tx_n + tsx) * p.nchunks + warp;
+          if (FILL) {
+            uint32_t pos = *c;
+            *c = pos + 1;
+            if (pos < p.bin_capacity) p.bin_entries[pos] = r << 1;
+          } else {
+            atomicAdd(c, 1u);
+          }
+        }
+      } else if (tsx < tex && tsy < tey) {
+        float4 e[3];
+        e[0] = make_float4(__shfl_sync(0xFFFFFFFFu, e0.x, i), __shfl_sync(0xFFFFFFFFu, e0.y, i),
+                           __shfl_sync(0xFFFFFFFFu, e0.z, i), 0.0f);
+        e[1] = make_float4(__shfl_sync(0xFFFFFFFFu, e1.x, i), __shfl_sync(0xFFFFFFFFu, e1.y, i),
+                           __shfl_sync(0xFFFFFFFFu, e1.z, i), 0.0f);
+        e[2] = make_float4(__shfl_sync(0xFFFFFFFFu, e2.x, i), __shfl_sync(0xFFFFFFFFu, e2.y, i),
+                           __shfl_sync(0xFFFFFFFFu, e2.z, i), 0.0f);
+        bool mx[3], my[3];
+        float r2a[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          mx[k] = e[k].x > 0;
+          my[k] = e[k].y > 0;
+          float stx = TILE * e[k].x, sty = TILE * e[k].y;
+          r2a[k] = -fabsf(stx) - fabsf(sty);
+        }
+        int w = tex - tsx, nt = w * (tey - tsy);
+        for (int j = lane; j < nt; j += 32) {
+          int x = tsx + j % w, y = tsy + j / w;
+          int rej = 0, acc = 1;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            float evv = e[k].z - (static_cast<float>(x + mx[k]) * TILE * e[k].x +
+                                  static_cast<float>(y + my[k]) * TILE * e[k].y);
+            rej |= (0 < evv);
+            acc &= (r2a[k] >= evv);
+          }
+          if (!rej) {
+            uint32_t* c = cnt + static_cast<size_t>(y * tx_n + x) * p.nchunks + warp;
+            if (FILL) {
+              // the chunk's cursor of this tile: only this warp touches it, and the
+              // __syncwarp below orders one step's update before the next step's read
+              uint32_t pos = *c;
+              *c = pos + 1;
+              if (pos < p.bin_capacity) p.bin_entries[pos] = (r << 1) | static_cast<uint32_t>(acc);
+            } else {
+              atomicAdd(c, 1u);
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan of n uint32 values in place; block sums in `sums`
+constexpr int SCAN_BLOCK = 1024;
+constexpr int SCAN_ITEMS = 4;
+
+__device__ inline uint32_t block_exclusive_scan(uint32_t v, uint32_t* smem, uint32_t& total) {
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t s = lane < static_cast<int>(blockDim.x >> 5) ? smem[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, o);
+      if (lane >= o) s += y;
+    }
+    smem[lane] = s;
+  }
+  __syncthreads();
+  uint32_t warp_off = wid > 0 ? smem[wid - 1] : 0;
+  total = smem[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_local(uint32_t* data, uint32_t n, uint32_t* sums) {
+  __shared__ uint32_t smem[32];
+  size_t base = static_cast<size_t>(blockIdx.x) * SCAN_BLOCK * SCAN_ITEMS + threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS], s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) {
+    v[i] = base + i < n ? data[base + i] : 0;
+    s += v[i];
+  }
+  uint32_t total;
+  uint32_t off = block_exclusive_scan(s, smem, total);
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) {
+    if (base + i < n) data[base + i] = off;
+    off += v[i];
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// single-block scan of the block sums (nsums <= SCAN_BLOCK * SCAN_ITEMS * many)
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_sums(uint32_t* sums, uint32_t nsums, DrawCounters* ctr) {
+  __shared__ uint32_t smem[32];
+  uint32_t carry = 0;
+  for (uint32_t start = 0; start < nsums; start += SCAN_BLOCK * SCAN_ITEMS) {
+    uint32_t base = start + threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS], s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+      v[i] = base + i < nsums ? sums[base + i] : 0;
+      s += v[i];
+    }
+    uint32_t total;
+    uint32_t off = block_exclusive_scan(s, smem, total) + carry;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+      if (base + i < nsums) sums[base + i] = off;
+      off += v[i];
+    }
+    carry += total;
+  }
+  if (threadIdx.x == 0) ctr->bin_entries = carry;
+}
+
+__global__ void k_scan_add(uint32_t* data, uint32_t n, uint32_t const* sums) {
+  size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) data[i] += sums[i / (SCAN_BLOCK * SCAN_ITEMS)];
+}
+
+// tile ranges from the scanned counts, and the overflow check
+__global__ void k_tile_ranges(DrawParams p, uint32_t ntiles) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < ntiles) p.tile_begin[t] = p.bin_counts[static_cast<size_t>(t) * p.nchunks];
+  if (t == 0) {
+    p.tile_begin[ntiles] = p.counters->bin_entries;
+    if (p.counters->bin_entries > p.bin_capacity) atomicOr(&p.counters->overflow, 1u);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers
+template <int NA>
+static void launch_geometry_t(DrawParams const& p, cudaStream_t s) {
+  uint32_t blocks = (p.prim_count + 127) / 128;
+  if (blocks) k_geometry<NA><<<blocks, 128, 0, s>>>(p);
+}
+void launch_geometry(DrawParams const& p, int nattr, cudaStream_t s) {
+  switch (nattr) {
+  case 0: launch_geometry_t<0>(p, s); break;
+  case 1: launch_geometry_t<1>(p, s); break;
+  case 2: launch_geometry_t<2>(p, s); break;
+  case 3: launch_geometry_t<3>(p, s); break;
+  case 4: launch_geometry_t<4>(p, s); break;
+  default: launch_geometry_t<5>(p, s); break;
+  }
+}
+
+void launch_bin(DrawParams const& p, uint32_t nslots, bool fill, cudaStream_t s) {
+  uint32_t warps = p.nchunks;
+  uint32_t blocks = (warps * 32 + 127) / 128;
+  if (!blocks) return;
+  if (fill)
+    k_bin<true><<<blocks, 128, 0, s>>>(p, nslots);
+  else
+    k_bin<false><<<blocks, 128, 0, s>>>(p, nslots);
+}
+
+// exclusive scan of `n` counts in place; `sums` needs ceil(n / 4096) entries
+void launch_scan(uint32_t* data, uint32_t n, uint32_t* sums, DrawCounters* ctr, cudaStream_t s) {
+  uint32_t nblocks = (n + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS);
+  if (nblocks == 0) return;
+  k_scan_local<<<nblocks, SCAN_BLOCK, 0, s>>>(data, n, sums);
+  k_scan_sums<<<1, SCAN_BLOCK, 0, s>>>(sums, nblocks, ctr);
+  k_scan_add<<<(n + 255) / 256, 256, 0, s>>>(data, n, sums);
+}
+
+void launch_tile_ranges(DrawParams const& p, uint32_t ntiles, cudaStream_t s) {
+  k_tile_ranges<<<(ntiles + 255) / 256, 256, 0, s>>>(p, ntiles);
+}
+
+cudaError_t upload_ewa_table_geometry(float const* tab, cudaStream_t s) {
+  return cudaMemcpyToSymbolAsync(c_ewa, tab, 256 * sizeof(float), 0, cudaMemcpyHostToDevice, s);
+}
+
+}  // namespace sg

@@ -1,0 +1,955 @@
+// sg_raster.cuh -- rasterization, pixel shading and output merging.
+//
+// Three kernels per draw after binning:
+//   k_cover   one CTA per 64x64 tile (dynamically scheduled), 256 threads;
+//             thread t owns the 4x4 pixel block t of the tile and replays,
+//             for its block and in primitive order, the reference's
+//             64 -> 16 -> 4 -> sample classification, quad coverage and
+//             early-Z.  Surviving quads become fragments, written per round
+//             in owner-major order.
+//   k_shade   every fragment of the draw, 4 lanes per quad (one per pixel):
+//             attribute interpolation and the pixel-shader program, with
+//             ddx/ddy from the quad's lanes.
+//   k_merge   one CTA per tile; each owner walks its fragments in primitive
+//             order and applies depth-stencil (when early-Z is off) and the
+//             blend program per covered sample.
+// Included by sg_raster_a.cu / _b.cu / _c.cu, which instantiate k_shade for
+// two varying counts each so the translation units compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sg_draw.cuh"
+
+namespace sg {
+
+// ---------------------------------------------------------------------------
+// rasterization + pixel shading + output merger
+
+struct TriView {
+  float4 const* R;
+  int nreg;
+  __device__ float4 edge(int i) const { return R[i]; }
+  __device__ float4 bbox() const { return R[3]; }
+  __device__ bool front() const { return R[4].x != 0.0f; }
+  __device__ v4 v0(int i) const { return ld4(R + 5 + i); }
+  __device__ v4 ddx(int i) const { return ld4(R + 5 + nreg + i); }
+  __device__ v4 ddy(int i) const { return ld4(R + 5 + 2 * nreg + i); }
+};
+
+__device__ inline bool cmpf(uint32_t f, float a, float b) {
+  switch (f) {
+  case SG_CMP_NEVER: return false;
+  case SG_CMP_LESS: return a < b;
+  case SG_CMP_EQUAL: return a == b;
+  case SG_CMP_LESS_EQUAL: return a <= b;
+  case SG_CMP_GREATER: return a > b;
+  case SG_CMP_NOT_EQUAL: return a != b;
+  case SG_CMP_GREATER_EQUAL: return a >= b;
+  default: return true;
+  }
+}
+__device__ inline bool cmpu(uint32_t f, uint32_t a, uint32_t b) {
+  switch (f) {
+  case SG_CMP_NEVER: return false;
+  case SG_CMP_LESS: return a < b;
+  case SG_CMP_EQUAL: return a == b;
+  case SG_CMP_LESS_EQUAL: return a <= b;
+  case SG_CMP_GREATER: return a > b;
+  case SG_CMP_NOT_EQUAL: return a != b;
+  case SG_CMP_GREATER_EQUAL: return a >= b;
+  default: return true;
+  }
+}
+__device__ inline uint32_t stencil_op(uint32_t op, uint32_t ref, uint32_t cur) {  // framebuffer.cpp:136-166
+  switch (op) {
+  case SG_SOP_KEEP: return cur;
+  case SG_SOP_ZERO: return 0;
+  case SG_SOP_REPLACE: return ref;
+  case SG_SOP_INCR_SAT: return min(0xFFu, cur + 1);
+  case SG_SOP_DECR_SAT: return cur - 1;  // std::max<uint32_t>(0, cur - 1) keeps the wrapped value
+  case SG_SOP_INVERT: return ~cur;
+  case SG_SOP_INCR_WRAP: return (cur + 1) & 0xFF;
+  case SG_SOP_DECR_WRAP: return (cur - 1 + 256) & 0xFF;
+  default: return cur;
+  }
+}
+// EXTENSION (D24S8): depth quantised to 24-bit unorm, round to nearest even
+__device__ inline uint32_t d24_quantize(float z) {
+  float c = fminf(fmaxf(z, 0.0f), 1.0f) * 16777215.0f;
+  return __float2uint_rn(c);
+}
+
+struct DSVal {
+  float depth;
+  uint32_t q;
+  uint32_t stencil;
+};
+
+__device__ inline DSVal ds_read(DrawParams const& p, uint8_t const* a) {
+  DSVal v{0.0f, 0u, 0u};
+  switch (p.ds_fmt) {
+  case SG_FMT_RG32F:
+    if (p.read_depth) v.depth = *reinterpret_cast<float const*>(a);
+    if (p.stencil) v.stencil = reinterpret_cast<uint32_t const*>(a)[1] & p.read_mask;
+    break;
+  case SG_FMT_D32F:
+    if (p.read_depth) v.depth = *reinterpret_cast<float const*>(a);
+    break;
+  case SG_FMT_D24S8: {
+    uint32_t w = *reinterpret_cast<uint32_t const*>(a);
+    if (p.read_depth) v.q = w & 0xFFFFFFu;
+    if (p.stencil) v.stencil = (w >> 24) & p.read_mask;
+    break;
+  }
+  default: break;
+  }
+  return v;
+}
+__device__ inline void ds_write(DrawParams const& p, uint8_t* a, float depth, uint32_t stencil, uint32_t wmask) {
+  switch (p.ds_fmt) {
+  case SG_FMT_RG32F:
+    if (p.write_depth) *reinterpret_cast<float*>(a) = depth;
+    if (p.stencil) reinterpret_cast<uint32_t*>(a)[1] = stencil & wmask;
+    break;
+  case SG_FMT_D32F:
+    if (p.write_depth) *reinterpret_cast<float*>(a) = depth;
+    break;
+  case SG_FMT_D24S8: {
+    uint32_t w = *reinterpret_cast<uint32_t*>(a);
+    if (p.write_depth) w = (w & 0xFF000000u) | d24_quantize(depth);
+    if (p.stencil) w = (w & 0x00FFFFFFu) | ((stencil & wmask & 0xFFu) << 24);
+    *reinterpret_cast<uint32_t*>(a) = w;
+    break;
+  }
+  default: break;
+  }
+}
+__device__ inline bool depth_pass(DrawParams const& p, float depth, DSVal const& old) {
+  if (p.ds_fmt == SG_FMT_D24S8 && p.read_depth) return cmpu(p.depth_func, d24_quantize(depth), old.q);
+  return cmpf(p.depth_func, depth, old.depth);
+}
+__device__ inline uint8_t* ds_addr(DrawParams const& p, uint32_t x, uint32_t y, uint32_t s) {
+  return p.ds + ((static_cast<size_t>(y) * p.ds_width + x) * p.samples + s) * p.ds_esz;
+}
+__device__ inline uint8_t* color_addr(DrawParams const& p, uint32_t x, uint32_t y, uint32_t s) {
+  return p.color + ((static_cast<size_t>(y) * p.width + x) * p.samples + s) * p.color_esz;
+}
+
+// cpp_blend_shader programs
+__device__ inline void blend(DrawParams const& p, uint32_t x, uint32_t y, uint32_t s, v4 src) {
+  if (!p.color) return;
+  uint8_t* a = color_addr(p, x, y, s);
+  switch (p.bs_prog) {
+  case SG_BS_LERP_SRC_ALPHA: {
+    v4 d = read_texel(p.color_fmt, a);
+    write_texel(p.color_fmt, a, mk4(lerp1(d.x, src.x, src.w), lerp1(d.y, src.y, src.w), lerp1(d.z, src.z, src.w),
+                                    lerp1(d.w, src.w, src.w)));
+    break;
+  }
+  case SG_BS_ADD: write_texel(p.color_fmt, a, read_texel(p.color_fmt, a) + src); break;
+  default: write_texel(p.color_fmt, a, src); break;
+  }
+}
+
+// framebuffer::render_sample (framebuffer.cpp:445-479)
+__device__ inline void render_sample(DrawParams const& p, uint32_t x, uint32_t y, uint32_t s, v4 src, float depth,
+                                     bool front) {
+  if (p.early_z || !p.ds) {
+    blend(p, x, y, s, src);
+    return;
+  }
+  uint8_t* a = ds_addr(p, x, y, s);
+  DSVal old = ds_read(p, a);
+  bool dp = depth_pass(p, depth, old);
+  uint32_t func = front ? p.front_func : p.back_func;
+  bool sp = p.stencil ? cmpu(func, p.stencil_ref, old.stencil) : true;
+  if (dp && sp) {
+    uint32_t ns = p.stencil ? stencil_op(front ? p.front_pass : p.back_pass, p.stencil_ref, old.stencil) : 0u;
+    blend(p, x, y, s, src);
+    ds_write(p, a, depth, ns, p.write_mask);
+  }
+}
+
+// early_z_test on one pixel (framebuffer.cpp:522-590); returns the passing samples
+__device__ inline uint32_t early_z_px(DrawParams const& p, uint32_t x, uint32_t y, uint32_t m, float depth,
+                                      float const* aa) {
+  if (p.samples == 1) {
+    uint8_t* a = ds_addr(p, x, y, 0);
+    DSVal old = ds_read(p, a);
+    if (depth_pass(p, depth, old)) {
+      ds_write(p, a, depth, 0, 0);
+      return 1;
+    }
+    return 0;
+  }
+  uint32_t out = 0;
+  for (uint32_t s = 0; s < p.samples; ++s) {
+    if (!(m & (1u << s))) continue;
+    uint8_t* a = ds_addr(p, x, y, s);
+    DSVal old = ds_read(p, a);
+    float nd = aa[s] + depth;
+    if (depth_pass(p, nd, old)) {
+      out |= 1u << s;
+      ds_write(p, a, nd, 0, 0);
+    }
+  }
+  return out;
+}
+
+// Coverage-pass copy of a triangle in shared memory: what coverage and early-Z
+// read (edges, bounding box, the position register of v0 / ddx / ddy).
+struct TriStage {
+  float4 bbox, e0, e1, e2, p0, dpx, dpy;
+  uint32_t entry, pad0, pad1, pad2;
+};
+struct StageView {
+  TriStage const* S;
+  __device__ float4 edge(int i) const { return i == 0 ? S->e0 : i == 1 ? S->e1 : S->e2; }
+  __device__ float4 bbox() const { return S->bbox; }
+  __device__ v4 v0(int) const { return mk4(S->p0.x, S->p0.y, S->p0.z, S->p0.w); }
+  __device__ v4 ddx(int) const { return mk4(S->dpx.x, S->dpx.y, S->dpx.z, S->dpx.w); }
+  __device__ v4 ddy(int) const { return mk4(S->dpy.x, S->dpy.y, S->dpy.z, S->dpy.w); }
+};
+
+// Depth of the tile staged in shared memory for early-Z: one 32-bit word per
+// sample, ((y_in_tile * 64 + x_in_tile) * samples + s).  For RG32F and D32F
+// the word is the float depth, for D24S8 the packed depth-stencil word.
+__device__ inline float zword_depth(DrawParams const& p, uint32_t w) {
+  return p.ds_fmt == SG_FMT_D24S8 ? 0.0f : __uint_as_float(w);
+}
+// early_z_test on one pixel against the staged depth (framebuffer.cpp:522-590)
+__device__ inline uint32_t early_z_px_smem(DrawParams const& p, uint32_t* z, uint32_t m, float depth, float const* aa) {
+  uint32_t out = 0;
+  for (uint32_t s = 0; s < p.samples; ++s) {
+    if (!(m & (1u << s))) continue;
+    float nd = p.samples == 1 ? depth : aa[s] + depth;
+    uint32_t w = z[s];
+    DSVal old{0.0f, 0u, 0u};
+    if (p.read_depth) {
+      if (p.ds_fmt == SG_FMT_D24S8)
+        old.q = w & 0xFFFFFFu;
+      else
+        old.depth = zword_depth(p, w);
+    }
+    if (depth_pass(p, nd, old)) {
+      out |= 1u << s;
+      if (p.write_depth)
+        z[s] = p.ds_fmt == SG_FMT_D24S8 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
+    }
+  }
+  return out;
+}
+
+// early_z_test_quad on the staged depth (framebuffer.cpp:556-614): the four
+// pixels of a quad at z (row stride `row` words), pixel depths zq, per-sample
+// offsets aa.  `cfg` packs samples (bits 0-3), read_depth (4), write_depth (5),
+// D24S8 storage (6) and the depth function (bits 8-11).  Out of line with
+// scalar arguments only, so callers keep their state in registers.
+static __device__ __noinline__ uint64_t early_z_quad(uint32_t* z, uint32_t row, uint64_t mask, float4 zq, float4 aa,
+                                                     uint32_t cfg) {
+  uint32_t const samples = cfg & 15u, func = (cfg >> 8) & 15u;
+  bool const rd = (cfg >> 4) & 1u, wr = (cfg >> 5) & 1u, d24 = (cfg >> 6) & 1u;
+  float const zz[4] = {zq.x, zq.y, zq.z, zq.w};
+  float const off[4] = {aa.x, aa.y, aa.z, aa.w};
+  uint64_t out = 0;
+  for (int i = 0; i < 4; ++i) {
+    uint32_t pm = static_cast<uint32_t>(mask >> (16 * i)) & 0xFFFFu;
+    if (!pm) continue;
+    uint32_t* zp = z + (i >> 1) * row + (i & 1) * samples;
+    for (uint32_t s = 0; s < samples; ++s) {
+      if (!(pm & (1u << s))) continue;
+      float nd = samples == 1 ? zz[i] : off[s] + zz[i];
+      uint32_t w = zp[s];
+      bool pass;
+      if (d24) {
+        pass = cmpu(func, d24_quantize(nd), rd ? (w & 0xFFFFFFu) : 0u);
+      } else {
+        pass = cmpf(func, nd, rd ? __uint_as_float(w) : 0.0f);
+      }
+      if (pass) {
+        out |= 1ull << (16 * i + s);
+        if (wr) zp[s] = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
+      }
+    }
+  }
+  return out;
+}
+
+// step_2d_unproj_pos_quad, one pixel of the quad (shader.cpp:257-287)
+template <class TV>
+__device__ inline v4 quad_pos(TV const& t, float dx, float dy, int q) {
+  v4 in = t.v0(0), d0 = t.ddx(0), d1 = t.ddy(0);
+  v4 p00 = mk4(in.x + (d0.x * dx + d1.x * dy), in.y + (d0.y * dx + d1.y * dy), in.z + (d0.z * dx + d1.z * dy),
+               in.w + (d0.w * dx + d1.w * dy));
+  if (q == 0) return p00;
+  if (q == 1) return p00 + d0;
+  if (q == 2) return p00 + d1;
+  return (p00 + d0) + d1;
+}
+
+// 64-bit quad mask (16 bits per pixel, <= 4 samples used) <-> 16-bit compact form
+__device__ inline uint32_t compact_mask(uint64_t m) {
+  return static_cast<uint32_t>((m & 0xF) | ((m >> 12) & 0xF0) | ((m >> 24) & 0xF00) | ((m >> 36) & 0xF000));
+}
+__device__ inline uint64_t expand_mask(uint32_t c) {
+  return static_cast<uint64_t>(c & 0xF) | (static_cast<uint64_t>((c >> 4) & 0xF) << 16) |
+         (static_cast<uint64_t>((c >> 8) & 0xF) << 32) | (static_cast<uint64_t>((c >> 12) & 0xF) << 48);
+}
+
+
+// An owner's append cursor into its chunked fragment list.
+struct OwnerList {
+  uint32_t first, cur, count;  // first chunk, current chunk, slots used in it
+  unsigned long long emitted;
+};
+
+__device__ inline void owner_append(DrawParams const& p, OwnerList& L, uint32_t rec, uint32_t pos, uint32_t mask) {
+  if (L.cur == NO_CHUNK || L.count == FRAG_CHUNK) {
+    uint32_t c = atomicAdd(&p.counters->chunk_total, 1u);
+    if (c >= p.chunk_capacity) {
+      atomicOr(&p.counters->overflow, 4u);
+      return;
+    }
+    if (L.cur == NO_CHUNK) {
+      L.first = c;
+    } else {
+      p.chunk_next[L.cur] = c;
+      p.chunk_count[L.cur] = FRAG_CHUNK;
+    }
+    L.cur = c;
+    L.count = 0;
+  }
+  uint32_t f = L.cur * FRAG_CHUNK + L.count++;
+  p.frag_rec[f] = rec;
+  p.frag_pos[f] = pos;
+  p.frag_mask[f] = mask;
+  ++L.emitted;
+}
+
+// Emits one quad (draw_full_quad / draw_quad up to the pixel shader,
+// rasterizer.cpp:1245-1421) after its early-Z test.
+__device__ inline void emit_quad(DrawParams const& p, StageView const& t, uint32_t rec, uint32_t qx_abs, uint32_t qy_abs,
+                                 uint64_t mask, bool full, float4 aa, OwnerList& L, uint32_t* ztile, int tile_x0,
+                                 int tile_y0) {
+  // EXTENSION: pixels outside the render target are not covered.
+  if (qx_abs + 1 >= p.width || qy_abs + 1 >= p.height) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (qx_abs + (i & 1) >= p.width || qy_abs + (i >> 1) >= p.height) {
+        mask &= ~(0xFFFFull << (16 * i));
+        full = false;
+      }
+    }
+    if (mask == 0) return;
+  }
+  uint64_t tested = mask;
+  if (p.early_z) {
+    v4 v0 = t.v0(0);
+    float dx = 0.5f + static_cast<float>(qx_abs) - v0.x;
+    float dy = 0.5f + static_cast<float>(qy_abs) - v0.y;
+    float4 zq = make_float4(quad_pos(t, dx, dy, 0).z, quad_pos(t, dx, dy, 1).z, quad_pos(t, dx, dy, 2).z,
+                            quad_pos(t, dx, dy, 3).z);
+    uint32_t cfg = p.samples | (p.read_depth << 4) | (p.write_depth << 5) |
+                   ((p.ds_fmt == SG_FMT_D24S8) ? 64u : 0u) | (p.depth_func << 8);
+    uint32_t px = qx_abs - tile_x0, py = qy_abs - tile_y0;
+    tested = early_z_quad(ztile + (py * TILE + px) * p.samples, TILE * p.samples, mask, zq, aa, cfg);
+  }
+  if (tested == 0) return;
+  owner_append(p, L, rec, (qx_abs >> 1) | ((qy_abs >> 1) << 12) | (full ? 1u << 24 : 0u),
+               compact_mask(tested) | (compact_mask(mask) << 16));
+}
+
+// The per-sample coverage of one 4x4 block (rasterizer::draw_partial_tile, SSE path,
+// rasterizer.cpp:298-439) followed by the quad emission.
+__device__ inline void partial_block(DrawParams const& p, StageView const& t, uint32_t rec, int left, int top,
+                                     float4 aa, OwnerList& L, uint32_t* ztile, int tile_x0, int tile_y0) {
+  float lf = static_cast<float>(left), tf = static_cast<float>(top);
+  float4 e[3] = {t.edge(0), t.edge(1), t.edge(2)};
+  float ev[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) ev[k] = e[k].z - (lf * e[k].x + tf * e[k].y);
+  // per-pixel sample masks packed four samples per nibble: pixel (ix, iy) of
+  // the block at bit 4 * (iy * 4 + ix) (registers only)
+  uint64_t pm = 0;
+  for (uint32_t s = 0; s < p.samples; ++s) {
+#pragma unroll
+    for (int iy = 0; iy < 4; ++iy) {
+      float my = p.sp_y[s] + static_cast<float>(iy);
+#pragma unroll
+      for (int ix = 0; ix < 4; ++ix) {
+        float mx = p.sp_x[s] + static_cast<float>(ix);
+        bool rej = false;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) rej = rej || ((mx * e[k].x + my * e[k].y) < ev[k]);
+        if (!rej) pm |= 1ull << (4 * (iy * 4 + ix) + s);
+      }
+    }
+  }
+  uint32_t fm = (1u << p.samples) - 1u;
+  uint64_t qfull = static_cast<uint64_t>(fm) | (static_cast<uint64_t>(fm) << 16) |
+                   (static_cast<uint64_t>(fm) << 32) | (static_cast<uint64_t>(fm) << 48);
+#pragma unroll 1
+  for (int q = 0; q < 4; ++q) {
+    int qx = (q & 1) << 1, qy = q & 2;
+    int st = qx | (qy << 2);
+    uint64_t m = ((pm >> (4 * st)) & 0xF) | (((pm >> (4 * (st + 1))) & 0xF) << 16) |
+                 (((pm >> (4 * (st + 4))) & 0xF) << 32) | (((pm >> (4 * (st + 5))) & 0xF) << 48);
+    if (m == 0) continue;
+    emit_quad(p, t, rec, left + qx, top + qy, m, m == qfull, aa, L, ztile, tile_x0, tile_y0);
+  }
+}
+
+// Per-level edge parameters of one triangle: TILE * e, then * 0.25 per level
+// (rasterizer.cpp:668-710).
+struct LevelParams {
+  float stx[3], sty[3], r2a[3], ev[3];
+};
+__device__ inline void level_params(float4 const* e, LevelParams& l1, LevelParams& l2) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    bool mx = e[k].x > 0, my = e[k].y > 0;
+    float stx = TILE * e[k].x, sty = TILE * e[k].y;
+    float r2a = -fabsf(stx) - fabsf(sty);
+    float pev = static_cast<float>(mx * TILE) * e[k].x + static_cast<float>(my * TILE) * e[k].y;
+    stx *= 0.25f; sty *= 0.25f; r2a *= 0.25f; pev *= 0.25f;
+    l1.stx[k] = stx; l1.sty[k] = sty; l1.r2a[k] = r2a; l1.ev[k] = e[k].z - pev;
+    stx *= 0.25f; sty *= 0.25f; r2a *= 0.25f; pev *= 0.25f;
+    l2.stx[k] = stx; l2.sty[k] = sty; l2.r2a[k] = r2a; l2.ev[k] = e[k].z - pev;
+  }
+}
+
+// subdivide_tile's trivial reject / accept of child (ix, iy) of the region at
+// (left, top) (rasterizer.cpp:485-540): 0 = rejected, 1 = partial, 2 = accepted.
+__device__ inline int child_class(float4 const* e, LevelParams const& l, float left, float top, int ix, int iy) {
+  bool rej = false, accf = false;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float ev3 = l.ev[k] - (left * e[k].x + top * e[k].y);
+    float srej = l.stx[k] * static_cast<float>(ix) + l.sty[k] * static_cast<float>(iy);
+    rej = rej || (srej < ev3);
+    accf = accf || ((srej + l.r2a[k]) < ev3);
+  }
+  return rej ? 0 : (accf ? 1 : 2);
+}
+
+// One triangle against this thread's 4x4 block.  `full16` says the block's
+// 16x16 region (or the whole tile) was accepted; otherwise the 16x16 region
+// was partial and the block passed the level-2 bounding-box test, and the
+// reference's level-2 edge test decides (rasterizer.cpp:617-773).
+__device__ inline void raster_block(DrawParams const& p, TriStage const* st, bool full16, int tile_x0, int tile_y0,
+                                   int bx, int by, OwnerList& L, uint32_t* ztile) {
+  uint32_t rec = st->entry >> 1;
+  StageView t{st};
+  float const trr = p.target_w, trb = p.target_h;
+  float4 aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (p.samples > 1) {
+    float dz = t.ddx(0).z, dyz = t.ddy(0).z;
+    aa.x = (p.sp_x[0] - 0.5f) * dz + (p.sp_y[0] - 0.5f) * dyz;
+    aa.y = (p.sp_x[1] - 0.5f) * dz + (p.sp_y[1] - 0.5f) * dyz;
+    if (p.samples > 2) {
+      aa.z = (p.sp_x[2] - 0.5f) * dz + (p.sp_y[2] - 0.5f) * dyz;
+      aa.w = (p.sp_x[3] - 0.5f) * dz + (p.sp_y[3] - 0.5f) * dyz;
+    }
+  }
+  int const bx_abs = tile_x0 + bx * 4, by_abs = tile_y0 + by * 4;
+  bool draw_all = full16;
+  if (!full16) {
+    float4 e[3] = {t.edge(0), t.edge(1), t.edge(2)};
+    LevelParams l1, l2;
+    level_params(e, l1, l2);
+    int r16x = tile_x0 + (bx >> 2) * 16, r16y = tile_y0 + (by >> 2) * 16;
+    int c = child_class(e, l2, static_cast<float>(r16x), static_cast<float>(r16y), bx & 3, by & 3);
+    if (c == 0) return;
+    if (static_cast<float>(bx_abs) >= trr || static_cast<float>(by_abs) >= trb) return;
+    if (c == 1) {
+      partial_block(p, t, rec, bx_abs, by_abs, aa, L, ztile, tile_x0, tile_y0);
+      return;
+    }
+    draw_all = true;
+  }
+  if (draw_all) {
+    // draw_full_tile over a region containing this block: quads left of the
+    // target's right edge and above its bottom edge (rasterizer.cpp:285-296,738-742)
+    uint32_t fm = (1u << p.samples) - 1u;
+    uint64_t qfull = static_cast<uint64_t>(fm) | (static_cast<uint64_t>(fm) << 16) |
+                     (static_cast<uint64_t>(fm) << 32) | (static_cast<uint64_t>(fm) << 48);
+    uint32_t vr = static_cast<uint32_t>(trr), vb = static_cast<uint32_t>(trb);
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+      uint32_t qx = bx_abs + ((q & 1) << 1), qy = by_abs + (q & 2);
+      if (qx < vr && qy < vb) emit_quad(p, t, rec, qx, qy, qfull, true, aa, L, ztile, tile_x0, tile_y0);
+    }
+  }
+}
+
+#ifdef SG_RASTER_COVER_MERGE  // defined by the one translation unit that owns these kernels
+constexpr int STAGE_TRIS = 256;  // triangles staged in shared memory per batch
+constexpr int MASK_WORDS = STAGE_TRIS / 32;
+constexpr int COVER_THREADS = 128;  // one CTA per 32x32 quadrant of a tile
+constexpr int QUAD_PX = 32;
+constexpr size_t COVER_SMEM_BASE = STAGE_TRIS * sizeof(TriStage) + (64 + 4) * MASK_WORDS * sizeof(uint32_t);
+// plus the staged depth: QUAD_PX * QUAD_PX * samples words (only when early-Z is on)
+__host__ __device__ constexpr size_t cover_smem(uint32_t samples, bool early_z) {
+  return COVER_SMEM_BASE + (early_z ? static_cast<size_t>(QUAD_PX) * QUAD_PX * samples * 4 : 0);
+}
+
+// One (triangle, 4x4 block) pair processed by the whole warp: the block's
+// level-2 classification (rasterizer.cpp:441-571), the per-sample coverage
+// of draw_partial_tile (rasterizer.cpp:298-439) and early-Z
+// (framebuffer.cpp:522-614) over the block's 16 pixels x samples, one sample
+// slot per lane and pass; the quads' masks are assembled with warp
+// reductions and the block's owner lane appends the surviving quads.
+__device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool full16, int tile_x0, int tile_y0, int blk,
+                                 int owner, OwnerList& L, uint32_t* ztile, int zx0, int zy0, int zpitch, int lane) {
+  StageView t{st};
+  uint32_t const rec = st->entry >> 1;
+  int const bx = blk & 15, by = blk >> 4;
+  int const bx_abs = tile_x0 + bx * 4, by_abs = tile_y0 + by * 4;
+  float const trr = p.target_w, trb = p.target_h;
+  float4 e[3] = {t.edge(0), t.edge(1), t.edge(2)};
+  bool region_full = full16;
+  if (!full16) {
+    LevelParams l1, l2;
+    level_params(e, l1, l2);
+    int r16x = tile_x0 + (bx >> 2) * 16, r16y = tile_y0 + (by >> 2) * 16;
+    int c = child_class(e, l2, static_cast<float>(r16x), static_cast<float>(r16y), bx & 3, by & 3);
+    if (c == 0) return;
+    if (static_cast<float>(bx_abs) >= trr || static_cast<float>(by_abs) >= trb) return;
+    region_full = c == 2;
+  }
+  uint32_t const S = p.samples, nslots = 16 * S;
+  uint32_t const W = p.width, H = p.height;
+  float const lf = static_cast<float>(bx_abs), tf = static_cast<float>(by_abs);
+  float ev[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) ev[k] = e[k].z - (lf * e[k].x + tf * e[k].y);
+  // coverage: unclipped (uc) and clipped to the target (cv), 4 bits per pixel,
+  // quads 0/1 in the low word, 2/3 in the high word
+  uint32_t uc_lo = 0, uc_hi = 0, cv_lo = 0, cv_hi = 0;
+  uint32_t slot_bit[2] = {0, 0};
+  bool slot_hi[2] = {false, false};
+#pragma unroll
+  for (int pass = 0; pass < 2; ++pass) {
+    uint32_t slot = lane + 32 * pass;
+    if (slot >= nslots) continue;
+    uint32_t i16 = slot / S, sm = slot % S;
+    uint32_t ix = i16 & 3, iy = i16 >> 2;
+    uint32_t q = ((iy >> 1) << 1) | (ix >> 1), i = ((iy & 1) << 1) | (ix & 1);
+    uint32_t bit = 1u << (4 * i + sm + 16 * (q & 1));
+    slot_bit[pass] = bit;
+    slot_hi[pass] = q >= 2;
+    bool in;
+    if (region_full) {
+      in = true;
+    } else {
+      float mx = p.sp_x[sm] + static_cast<float>(ix), my = p.sp_y[sm] + static_cast<float>(iy);
+      bool rej = false;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) rej = rej || ((mx * e[k].x + my * e[k].y) < ev[k]);
+      in = !rej;
+    }
+    bool inside = bx_abs + ix < W && by_abs + iy < H;  // EXTENSION: pixels outside the target are not covered
+    if (in) {
+      if (q >= 2) uc_hi |= bit; else uc_lo |= bit;
+      if (inside) {
+        if (q >= 2) cv_hi |= bit; else cv_lo |= bit;
+      }
+    }
+  }
+  uc_lo = __reduce_or_sync(0xFFFFFFFFu, uc_lo);
+  uc_hi = __reduce_or_sync(0xFFFFFFFFu, uc_hi);
+  cv_lo = __reduce_or_sync(0xFFFFFFFFu, cv_lo);
+  cv_hi = __reduce_or_sync(0xFFFFFFFFu, cv_hi);
+  if ((cv_lo | cv_hi) == 0) return;
+  uint32_t const fm = (1u << S) - 1u;
+  uint32_t const qfull = fm | (fm << 4) | (fm << 8) | (fm << 12);
+  // a full region's quads are drawn when their left / top pixel is inside the
+  // target (draw_full_tile, rasterizer.cpp:738-742): no quad of this block is
+  // dropped by that rule once its covered pixels are clipped to the target.
+  uint32_t tested_lo = cv_lo, tested_hi = cv_hi;
+  if (p.early_z) {
+    v4 v0 = t.v0(0);
+    float dz = t.ddx(0).z, dyz = t.ddy(0).z;
+    uint32_t t_lo = 0, t_hi = 0;
+    uint32_t cfg_rd = p.read_depth, cfg_wr = p.write_depth;
+    bool d24 = p.ds_fmt == SG_FMT_D24S8;
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      uint32_t slot = lane + 32 * pass;
+      if (slot >= nslots) continue;
+      uint32_t bit = slot_bit[pass];
+      bool covered = slot_hi[pass] ? (cv_hi & bit) : (cv_lo & bit);
+      if (!covered) continue;
+      uint32_t i16 = slot / S, sm = slot % S;
+      uint32_t ix = i16 & 3, iy = i16 >> 2;
+      uint32_t q = ((iy >> 1) << 1) | (ix >> 1), i = ((iy & 1) << 1) | (ix & 1);
+      uint32_t qx = bx_abs + ((q & 1) << 1), qy = by_abs + (q & 2);
+      float dx = 0.5f + static_cast<float>(qx) - v0.x;
+      float dy = 0.5f + static_cast<float>(qy) - v0.y;
+      float z = quad_pos(t, dx, dy, static_cast<int>(i)).z;
+      float nd = S == 1 ? z : ((p.sp_x[sm] - 0.5f) * dz + (p.sp_y[sm] - 0.5f) * dyz) + z;
+      uint32_t* zp = ztile + ((by_abs - zy0 + iy) * zpitch + (bx_abs - zx0 + ix)) * S + sm;
+      uint32_t w = *zp;
+      bool pass_z = d24 ? cmpu(p.depth_func, d24_quantize(nd), cfg_rd ? (w & 0xFFFFFFu) : 0u)
+                        : cmpf(p.depth_func, nd, cfg_rd ? __uint_as_float(w) : 0.0f);
+      if (pass_z) {
+        if (cfg_wr) *zp = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
+        if (slot_hi[pass]) t_hi |= bit; else t_lo |= bit;
+      }
+    }
+    tested_lo = __reduce_or_sync(0xFFFFFFFFu, t_lo);
+    tested_hi = __reduce_or_sync(0xFFFFFFFFu, t_hi);
+  }
+  if (lane == owner) {
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+      uint32_t tq = ((q < 2 ? tested_lo : tested_hi) >> (16 * (q & 1))) & 0xFFFFu;
+      if (!tq) continue;
+      uint32_t cq = ((q < 2 ? cv_lo : cv_hi) >> (16 * (q & 1))) & 0xFFFFu;
+      uint32_t uq = ((q < 2 ? uc_lo : uc_hi) >> (16 * (q & 1))) & 0xFFFFu;
+      bool full = region_full ? cq == qfull : (uq == qfull && cq == uq);
+      uint32_t qx = bx_abs + ((q & 1) << 1), qy = by_abs + (q & 2);
+      owner_append(p, L, rec, (qx >> 1) | ((qy >> 1) << 12) | (full ? 1u << 24 : 0u), tq | (cq << 16));
+    }
+  }
+}
+
+__device__ inline int tile_x0_of(DrawParams const& p, uint32_t tile) { return static_cast<int>(tile % p.tiles_x) * TILE; }
+__device__ inline int tile_y0_of(DrawParams const& p, uint32_t tile) { return static_cast<int>(tile / p.tiles_x) * TILE; }
+
+__global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nreg) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  TriStage* stage = reinterpret_cast<TriStage*>(smem);
+  // triangle sets of the staged batch (word-major): per 4x4 block of the
+  // quadrant (its 16x16 region partial, block inside the bounding box) and per
+  // 16x16 region of the quadrant (region accepted)
+  uint32_t* mask4 = reinterpret_cast<uint32_t*>(smem + STAGE_TRIS * sizeof(TriStage));
+  uint32_t* mask16 = mask4 + 64 * MASK_WORDS;
+  uint32_t* ztile = mask16 + 4 * MASK_WORDS;
+  __shared__ uint32_t s_item;
+  if (p.counters->overflow & 1u) return;
+  int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // lane l < 16 of warp w owns quadrant block lb = 4 l + w (blocks of a warp
+  // are interleaved over the quadrant so that dense rows spread over warps)
+  int const lb = 4 * (lane & 15) + warp;
+  bool const owns = lane < 16;
+  int const lbx = lb & 7, lby = lb >> 3;
+  int const nitems = p.tiles_x * p.tiles_y * 4;
+  float const trr = p.target_w, trb = p.target_h;
+  OwnerList L{NO_CHUNK, NO_CHUNK, 0, 0};
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(&p.counters->tile_cursor, 1u);
+    __syncthreads();
+    uint32_t item = s_item;
+    __syncthreads();
+    if (item >= static_cast<uint32_t>(nitems)) break;
+    uint32_t const tile = item >> 2, qd = item & 3;
+    uint32_t begin = p.tile_begin[tile], end = p.tile_begin[tile + 1];
+    int tile_x0 = tile_x0_of(p, tile), tile_y0 = tile_y0_of(p, tile);
+    int const qx0 = tile_x0 + (qd & 1) * QUAD_PX, qy0 = tile_y0 + (qd >> 1) * QUAD_PX;
+    int const q16x = (qd & 1) * 2, q16y = (qd >> 1) * 2;  // first 16x16 region of the quadrant
+    int const blk = ((qd >> 1) * 8 + lby) * 16 + (qd & 1) * 8 + lbx;  // owned block, tile numbering
+    int const own16 = (lby >> 2) * 2 + (lbx >> 2);                   // its 16x16 region, quadrant numbering
+    float const tx0f = static_cast<float>(tile_x0), ty0f = static_cast<float>(tile_y0);
+    L.first = L.cur = NO_CHUNK;
+    L.count = 0;
+    bool const stage_z = p.early_z && begin < end;
+    uint32_t const qw = min(static_cast<uint32_t>(QUAD_PX), p.width - min(p.width, static_cast<uint32_t>(qx0)));
+    uint32_t const qh = min(static_cast<uint32_t>(QUAD_PX), p.height - min(p.height, static_cast<uint32_t>(qy0)));
+    uint32_t const S = p.samples;
+    if (stage_z) {
+      for (uint32_t i = tid; i < qh * QUAD_PX * S; i += COVER_THREADS) {
+        uint32_t y = i / (QUAD_PX * S), k = i % (QUAD_PX * S);
+        if (k >= qw * S) continue;
+        uint32_t x = k / S, sm = k % S;
+        ztile[(y * QUAD_PX + x) * S + sm] = *reinterpret_cast<uint32_t const*>(ds_addr(p, qx0 + x, qy0 + y, sm));
+      }
+    }
+    for (uint32_t bstart = begin; bstart < end; bstart += STAGE_TRIS) {
+      uint32_t nb = min(static_cast<uint32_t>(STAGE_TRIS), end - bstart);
+      __syncthreads();
+      for (int i = tid; i < (64 + 4) * MASK_WORDS; i += COVER_THREADS) mask4[i] = 0;
+      __syncthreads();
+      // stage the batch and classify each triangle against the quadrant's 16x16 regions
+      for (uint32_t i = tid; i < nb; i += COVER_THREADS) {
+        uint32_t e = p.bin_entries[bstart + i];
+        float4 const* R = p.recs + static_cast<size_t>(e >> 1) * p.rec_stride;
+        TriStage ts;
+        ts.e0 = R[0];
+        ts.e1 = R[1];
+        ts.e2 = R[2];
+        ts.bbox = R[3];
+        ts.p0 = R[5];
+        ts.dpx = R[5 + nreg];
+        ts.dpy = R[5 + 2 * nreg];
+        ts.entry = e;
+        stage[i] = ts;
+        uint32_t bit = 1u << (i & 31), word = i >> 5;
+        if (e & 1u) {  // accepted for the whole tile by the binner
+          for (int r = 0; r < 4; ++r) atomicOr(&mask16[word * 4 + r], bit);
+          continue;
+        }
+        float x_min = ts.bbox.x - tx0f, x_max = ts.bbox.y - tx0f, y_min = ts.bbox.z - ty0f, y_max = ts.bbox.w - ty0f;
+        float4 ed[3] = {ts.e0, ts.e1, ts.e2};
+        LevelParams l1, l2;
+        level_params(ed, l1, l2);
+        for (int iy = q16y; iy < q16y + 2; ++iy) {
+          int m16y = iy * 16;
+          if (y_min >= static_cast<float>(m16y + 16) || y_max < static_cast<float>(m16y)) continue;
+          for (int ix = q16x; ix < q16x + 2; ++ix) {
+            int m16x = ix * 16;
+            if (x_min >= static_cast<float>(m16x + 16) || x_max < static_cast<float>(m16x)) continue;
+            int c = child_class(ed, l1, tx0f, ty0f, ix, iy);
+            if (c == 0) continue;
+            // a region whose origin is right of / below the target is skipped
+            if (static_cast<float>(tile_x0 + m16x) >= trr || static_cast<float>(tile_y0 + m16y) >= trb) continue;
+            int r16 = (iy - q16y) * 2 + (ix - q16x);
+            if (c == 2) {
+              atomicOr(&mask16[word * 4 + r16], bit);
+              continue;
+            }
+            // partial: the 4x4 children that pass the level-2 bounding-box test
+            for (int jy = 0; jy < 4; ++jy) {
+              int m4y = m16y + jy * 4;
+              if (y_min >= static_cast<float>(m4y + 4) || y_max < static_cast<float>(m4y)) continue;
+              for (int jx = 0; jx < 4; ++jx) {
+                int m4x = m16x + jx * 4;
+                if (x_min >= static_cast<float>(m4x + 4) || x_max < static_cast<float>(m4x)) continue;
+                int qb = ((iy - q16y) * 4 + jy) * 8 + (ix - q16x) * 4 + jx;  // quadrant block
+                atomicOr(&mask4[word * 64 + qb], bit);
+              }
+            }
+          }
+        }
+      }
+      __syncthreads();
+      // Each warp walks the batch's triangles in primitive order and, for
+      // each, the owned blocks the triangle reaches, processing every
+      // (triangle, block) pair with the whole warp; per block this is the
+      // reference's primitive order.
+      for (int w = 0; w < MASK_WORDS; ++w) {
+        uint32_t m16 = owns ? mask16[w * 4 + own16] : 0u;
+        uint32_t mine = owns ? (mask4[w * 64 + lb] | m16) : 0u;
+        uint32_t tris = __reduce_or_sync(0xFFFFFFFFu, mine);
+        while (tris) {
+          int b = __ffs(tris) - 1;
+          tris &= tris - 1;
+          uint32_t blocks = __ballot_sync(0xFFFFFFFFu, (mine >> b) & 1u);
+          uint32_t fulls = __ballot_sync(0xFFFFFFFFu, (m16 >> b) & 1u);
+          while (blocks) {
+            int l = __ffs(blocks) - 1;
+            blocks &= blocks - 1;
+            int olb = 4 * l + warp;
+            int oblk = ((qd >> 1) * 8 + (olb >> 3)) * 16 + (qd & 1) * 8 + (olb & 7);
+            pair_warp(p, stage + (w << 5) + b, (fulls >> l) & 1u, tile_x0, tile_y0, oblk, l, L, ztile, qx0, qy0, QUAD_PX,
+                      lane);
+          }
+        }
+      }
+    }
+    if (stage_z) {
+      __syncthreads();
+      for (uint32_t i = tid; i < qh * QUAD_PX * S; i += COVER_THREADS) {
+        uint32_t y = i / (QUAD_PX * S), k = i % (QUAD_PX * S);
+        if (k >= qw * S) continue;
+        uint32_t x = k / S, sm = k % S;
+        *reinterpret_cast<uint32_t*>(ds_addr(p, qx0 + x, qy0 + y, sm)) = ztile[(y * QUAD_PX + x) * S + sm];
+      }
+    }
+    // close the owned block's list for the tile
+    if (owns) {
+      if (L.cur != NO_CHUNK) {
+        p.chunk_next[L.cur] = NO_CHUNK;
+        p.chunk_count[L.cur] = L.count;
+      }
+      p.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + blk] = L.first;
+    }
+  }
+  unsigned long long ps_inv = 4ull * L.emitted;
+  for (int o = 16; o > 0; o >>= 1) ps_inv += __shfl_down_sync(0xFFFFFFFFu, ps_inv, o);
+  if (lane == 0 && ps_inv) atomicAdd(&p.counters->ps_invocations, ps_inv);
+}
+
+#endif  // SG_RASTER_COVER_MERGE
+
+// cpp_pixel_shader programs for one pixel `q` of a quad shaded by four lanes
+// (lanes 4k..4k+3 of the warp); tex2d's LOD uses the quad differences
+// (cpp_pixel_shader.cpp:13-31).
+template <int NA>
+__device__ inline v4 run_ps(DrawParams const& p, v4 const* attr, int q) {
+  v4 a0 = NA > 0 ? attr[0] : mk4(0, 0, 0, 0);
+  v4 a1 = NA > 1 ? attr[1 < NA ? 1 : 0] : mk4(0, 0, 0, 0);
+  int base = (threadIdx.x & 31) & ~3;
+  unsigned mask = 0xFu << base;
+  float u0 = __shfl_sync(mask, a0.x, base), v0 = __shfl_sync(mask, a0.y, base);
+  float u1 = __shfl_sync(mask, a0.x, base + 1), v1 = __shfl_sync(mask, a0.y, base + 1);
+  float u2 = __shfl_sync(mask, a0.x, base + 2), v2 = __shfl_sync(mask, a0.y, base + 2);
+  switch (p.ps_prog) {
+  case SG_PS_COLOR: return a0;
+  case SG_PS_CONSTANT: return mk4(p.ps_k[0], p.ps_k[1], p.ps_k[2], p.ps_k[3]);
+  case SG_PS_TEX_MODULATE: {
+    float lod = calc_lod_2d(p.ps_samp, u1 - u0, v1 - v0, u2 - u0, v2 - v0);
+    return mulv(sample_impl(p.ps_samp, a0.x, a0.y, lod, nullptr), a1);
+  }
+  case SG_PS_TEX_GRAD_MODULATE:
+    return mulv(sample_2d_grad(p.ps_samp, a0.x, a0.y, u1 - u0, v1 - v0, u2 - u0, v2 - v0, 0.0f), a1);
+  default: return mk4(0, 0, 0, 0);
+  }
+}
+
+// Attribute interpolation (step_2d_unproj_attr_n_quad / step_2d_unproj_attr_n
+// with the centroid adjustment, shader.cpp:208-367, rasterizer.cpp:1363-1398)
+// and the pixel shader, for every fragment of the draw.
+template <int NA>
+__global__ void __launch_bounds__(256) k_shade(DrawParams p) {
+  uint32_t const nfrag = min(p.counters->chunk_total, p.chunk_capacity) * FRAG_CHUNK;
+  if (p.counters->overflow & 5u) return;
+  int const q = threadIdx.x & 3;
+  uint32_t const groups = gridDim.x * (blockDim.x >> 2);
+  uint32_t const start = blockIdx.x * (blockDim.x >> 2) + (threadIdx.x >> 2);
+  uint32_t const rounds = (nfrag + groups - 1) / groups;
+  for (uint32_t it = 0; it < rounds; ++it) {
+    uint32_t f = start + it * groups;
+    bool live = f < nfrag && (f % FRAG_CHUNK) < p.chunk_count[f / FRAG_CHUNK];
+    v4 attr[NA > 0 ? NA : 1];
+#pragma unroll
+    for (int i = 0; i < (NA > 0 ? NA : 1); ++i) attr[i] = mk4(0, 0, 0, 0);
+    if (live) {
+      uint32_t rec = p.frag_rec[f], pos = p.frag_pos[f], masks = p.frag_mask[f];
+      TriView t{p.recs + static_cast<size_t>(rec) * p.rec_stride, 1 + NA};
+      uint32_t qx = (pos & 0xFFFu) << 1, qy = ((pos >> 12) & 0xFFFu) << 1;
+      bool full = (pos >> 24) & 1u;
+      v4 v0p = t.v0(0);
+      float dx = 0.5f + static_cast<float>(qx) - v0p.x;
+      float dy = 0.5f + static_cast<float>(qy) - v0p.y;
+      float w = quad_pos(t, dx, dy, q).w;
+      float invw = 1.0f / w;
+      bool centroid = !full && p.has_centroid;
+      float pdx = dx, pdy = dy;
+      if (centroid) {
+        pdx = dx + static_cast<float>(q & 1);
+        pdy = dy + static_cast<float>(q >> 1);
+        uint64_t m = expand_mask(masks >> 16);  // coverage before early-Z (rasterizer.cpp:1373)
+        uint32_t pm = static_cast<uint32_t>(m >> (16 * q)) & 0xFFFFu;
+        uint32_t fm = (1u << p.samples) - 1u;
+        if (pm != fm && pm != 0) {
+          float cx = 0.0f, cy = 0.0f;
+          int n = 0;
+          for (uint32_t s = 0; s < p.samples; ++s)
+            if (pm & (1u << s)) {
+              cx += p.sp_x[s];
+              cy += p.sp_y[s];
+              ++n;
+            }
+          float inv = 1.0f / static_cast<float>(n);
+          cx *= inv;
+          cy *= inv;
+          pdx += cx - 0.5f;
+          pdy += cy - 0.5f;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < NA; ++i) {
+        v4 in = t.v0(1 + i), d0 = t.ddx(1 + i), d1 = t.ddy(1 + i);
+        v4 a;
+        if (p.mods[i] & SG_AM_NOINTERPOLATION) {
+          a = in;
+        } else if (centroid) {
+          a = mk4(in.x + (d0.x * pdx + d1.x * pdy), in.y + (d0.y * pdx + d1.y * pdy), in.z + (d0.z * pdx + d1.z * pdy),
+                  in.w + (d0.w * pdx + d1.w * pdy));
+        } else {
+          v4 a00 = mk4(in.x + (d0.x * dx + d1.x * dy), in.y + (d0.y * dx + d1.y * dy), in.z + (d0.z * dx + d1.z * dy),
+                       in.w + (d0.w * dx + d1.w * dy));
+          a = q == 0 ? a00 : q == 1 ? a00 + d0 : q == 2 ? a00 + d1 : (a00 + d0) + d1;
+        }
+        attr[i] = (p.mods[i] & SG_AM_NOPERSPECTIVE) ? a : a * invw;
+      }
+    }
+    v4 out = run_ps<NA>(p, attr, q);  // all four lanes of a quad take the same path
+    if (live) {
+      p.frag_color[static_cast<size_t>(f) * 4 + q] = make_float4(out.x, out.y, out.z, out.w);
+      if (q == 0) p.frag_ps[f] = 0xF;  // the stock programs never discard
+    }
+  }
+}
+
+#ifdef SG_RASTER_COVER_MERGE
+// Output merging per tile: owners replay their fragments in primitive order
+// (framebuffer::render_sample_quad, framebuffer.cpp:481-520).
+__global__ void __launch_bounds__(RASTER_THREADS) k_merge(DrawParams p, int nreg) {
+  __shared__ uint32_t s_tile;
+  if (p.counters->overflow & 5u) return;
+  int const tid = threadIdx.x, lane = tid & 31;
+  int const ntiles = p.tiles_x * p.tiles_y;
+  unsigned long long backend = 0;
+  for (;;) {
+    if (tid == 0) s_tile = atomicAdd(&p.counters->merge_cursor, 1u);
+    __syncthreads();
+    uint32_t tile = s_tile;
+    __syncthreads();
+    if (tile >= static_cast<uint32_t>(ntiles)) break;
+    uint32_t c = p.tile_begin[tile] == p.tile_begin[tile + 1]
+                     ? NO_CHUNK
+                     : p.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + tid];
+    while (c != NO_CHUNK) {
+      uint32_t n = p.chunk_count[c];
+      for (uint32_t k = 0; k < n; ++k) {
+        uint32_t f = c * FRAG_CHUNK + k;
+        uint32_t rec = p.frag_rec[f], pos = p.frag_pos[f], masks = p.frag_mask[f];
+        uint64_t m = expand_mask(masks & 0xFFFFu);
+        uint32_t ps = p.frag_ps[f];
+        uint64_t psm = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (ps & (1u << i)) psm |= 0xFFFFull << (16 * i);
+        m &= psm;
+        bool full = (pos >> 24) & 1u;
+        if (full && m == 0) continue;
+        backend += 4;
+        TriView t{p.recs + static_cast<size_t>(rec) * p.rec_stride, nreg};
+        uint32_t qx = (pos & 0xFFFu) << 1, qy = ((pos >> 12) & 0xFFFu) << 1;
+        bool front = t.front();
+        float depth[4] = {0, 0, 0, 0};
+        float aa[4] = {0, 0, 0, 0};
+        if (!p.early_z && p.ds) {
+          v4 v0p = t.v0(0);
+          float dx = 0.5f + static_cast<float>(qx) - v0p.x;
+          float dy = 0.5f + static_cast<float>(qy) - v0p.y;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) depth[i] = quad_pos(t, dx, dy, i).z;
+          if (p.samples > 1) {
+            float dz = t.ddx(0).z, dyz = t.ddy(0).z;
+            for (uint32_t s = 0; s < p.samples; ++s) aa[s] = (p.sp_x[s] - 0.5f) * dz + (p.sp_y[s] - 0.5f) * dyz;
+          }
+        }
+        for (int i = 0; i < 4; ++i) {
+          uint32_t pm = static_cast<uint32_t>(m >> (16 * i)) & 0xFFFFu;
+          if (!pm) continue;
+          float4 c = p.frag_color[static_cast<size_t>(f) * 4 + i];
+          v4 src = mk4(c.x, c.y, c.z, c.w);
+          uint32_t x = qx + (i & 1), y = qy + (i >> 1);
+          if (p.samples == 1) {
+            render_sample(p, x, y, 0, src, depth[i], front);
+          } else {
+            for (uint32_t s = 0; s < p.samples; ++s)
+              if (pm & (1u << s)) render_sample(p, x, y, s, src, depth[i] + aa[s], front);
+          }
+        }
+      }
+      c = p.chunk_next[c];
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) backend += __shfl_down_sync(0xFFFFFFFFu, backend, o);
+  if (lane == 0 && backend) atomicAdd(&p.counters->backend_input_pixels, backend);
+}
+
+#endif  // SG_RASTER_COVER_MERGE
+
+// ---------------------------------------------------------------------------
+template <int NA>
+void launch_shade_t(DrawParams const& p, uint32_t grid, cudaStream_t s) {
+  k_shade<NA><<<grid, 256, 0, s>>>(p);
+}
+
+}  // namespace sg

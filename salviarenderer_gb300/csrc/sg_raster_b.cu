@@ -1,0 +1,15 @@
+// sg_raster_b.cu -- k_shade instances for 2 and 3 varyings.
+#include "sg_raster.cuh"
+
+namespace sg {
+
+void launch_shade_2(DrawParams const& p, uint32_t grid, cudaStream_t s) { launch_shade_t<2>(p, grid, s); }
+void launch_shade_3(DrawParams const& p, uint32_t grid, cudaStream_t s) { launch_shade_t<3>(p, grid, s); }
+
+// The EWA table of this translation unit's sampler (each translation unit
+// has its own copy of the __constant__ table).
+cudaError_t upload_ewa_table_raster_b(float const* tab, cudaStream_t s) {
+  return cudaMemcpyToSymbolAsync(c_ewa, tab, 256 * sizeof(float), 0, cudaMemcpyHostToDevice, s);
+}
+
+}  // namespace sg

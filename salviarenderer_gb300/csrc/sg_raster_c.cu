@@ -1,0 +1,15 @@
+// sg_raster_c.cu -- k_shade instances for 4 and 5 varyings.
+#include "sg_raster.cuh"
+
+namespace sg {
+
+void launch_shade_4(DrawParams const& p, uint32_t grid, cudaStream_t s) { launch_shade_t<4>(p, grid, s); }
+void launch_shade_5(DrawParams const& p, uint32_t grid, cudaStream_t s) { launch_shade_t<5>(p, grid, s); }
+
+// The EWA table of this translation unit's sampler (each translation unit
+// has its own copy of the __constant__ table).
+cudaError_t upload_ewa_table_raster_c(float const* tab, cudaStream_t s) {
+  return cudaMemcpyToSymbolAsync(c_ewa, tab, 256 * sizeof(float), 0, cudaMemcpyHostToDevice, s);
+}
+
+}  // namespace sg

@@ -52,6 +52,14 @@ class Device:
     def sync(self):
         self._check("sg_sync", self.lib.sg_sync(self.handle))
 
+    def profile_enable(self, on=True):
+        self._check("sg_profile_enable", self.lib.sg_profile_enable(self.handle, 1 if on else 0))
+
+    def profile_read(self):
+        d = abi.ProfileData()
+        self._check("sg_profile_read", self.lib.sg_profile_read(self.handle, C.byref(d)))
+        return {k: getattr(d, k) for k, _ in abi.ProfileData._fields_}
+
     # -- buffers -------------------------------------------------------------
     def buffer(self, data):
         data = np.ascontiguousarray(data)

@@ -1,0 +1,93 @@
+"""GPU pipeline against the CPU oracle, through the C ABI.
+
+Bar: depth-stencil and pipeline counters bit-exact; colour within one
+UNORM8 step (8-bit targets) or 1e-5 relative (float targets).  In practice
+the kernels reproduce the reference's float operation order, so colour is
+expected to match exactly as well; the tolerance is the stated bar.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cases
+from salviarenderer_gb300 import abi, Device, scenes
+from salviarenderer_gb300 import build as pbuild
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gdev():
+    lib = abi.bind(ctypes.CDLL(pbuild.ensure_built()))
+    return Device(lib, cuda_device=0)
+
+
+@pytest.fixture(scope="module")
+def odev(oracle_lib):
+    return Device(oracle_lib)
+
+
+def assert_color_close(a, b, fmt, what):
+    if fmt in (abi.FMT_RGBA8, abi.FMT_BGRA8):
+        d = np.abs(a.astype(np.int16) - b.astype(np.int16))
+        assert d.max() <= 1, f"{what}: max diff {d.max()} in {np.count_nonzero(d)} bytes"
+    else:
+        dt = np.float16 if fmt == abi.FMT_RGBA16F else np.float32
+        fa = a.view(dt).astype(np.float32)
+        fb = b.view(dt).astype(np.float32)
+        np.testing.assert_allclose(fa, fb, rtol=1e-5, atol=1e-6, err_msg=what)
+
+
+def compare(gdev, odev, scene):
+    got = scenes.render(gdev, scene, stats=True)
+    want = scenes.render(odev, scene, stats=True)
+    assert got["stats"] == want["stats"], (got["stats"], want["stats"])
+    assert np.array_equal(got["depth_stencil"], want["depth_stencil"]), \
+        f"depth-stencil differs in {(got['depth_stencil'] != want['depth_stencil']).sum()} bytes"
+    for k in ("color", "resolved"):
+        if k in want:
+            assert_color_close(got[k], want[k], scene.color_fmt, k)
+    return got, want
+
+
+@pytest.mark.parametrize("name", sorted(cases.CASES))
+def test_golden_scene_matches_oracle(gdev, odev, name):
+    compare(gdev, odev, cases.CASES[name]())
+
+
+def test_c1_full_size(gdev, odev):
+    got, want = compare(gdev, odev, scenes.c1_scene())
+    assert np.array_equal(got["color"], want["color"])
+
+
+def test_c2_reduced(gdev, odev):
+    compare(gdev, odev, scenes.c2_scene(width=480, height=272, grid=101, tex_size=512, ndraws=4))
+
+
+@pytest.mark.parametrize("fmt", [abi.FMT_D32F, abi.FMT_D24S8])
+def test_depth_extension_formats(gdev, odev, fmt):
+    compare(gdev, odev, scenes.c1_scene(width=128, height=128, ntris=400, samples=4, ds_fmt=fmt, seed=31))
+
+
+def test_rgba16f_target(gdev, odev):
+    compare(gdev, odev, scenes.feature_scene(seed=41, color_fmt=abi.FMT_RGBA16F, blend=abi.BS_LERP_SRC_ALPHA,
+                                             samples=4))
+
+
+def test_stencil_d24s8(gdev, odev):
+    s = scenes.stencil_mirror_scene(seed=5, samples=4)
+    s.ds_fmt = abi.FMT_D24S8
+    compare(gdev, odev, s)
+
+
+def test_odd_target_size_is_clipped(gdev, odev):
+    compare(gdev, odev, scenes.c1_scene(width=98, height=66, ntris=300, seed=17))
+
+
+def test_repeat_is_deterministic(gdev):
+    s = scenes.c2_scene(width=256, height=144, grid=49, tex_size=128, ndraws=4)
+    a = scenes.render(gdev, s)
+    b = scenes.render(gdev, s)
+    for k in a:
+        assert np.array_equal(a[k], b[k])
