@@ -284,6 +284,43 @@ int32_t sg_sampler_destroy(sg_device* dev, uint32_t sampler);
  * when given, the counters are written once the draw has completed on the
  * device (the call then synchronises). */
 int32_t sg_draw(sg_device* dev, const sg_draw_desc* desc, sg_draw_stats* stats);
+
+/* Size of the static scratch used by sg_draw_static_scratch, per CUDA device. */
+#define SG_STATIC_SCRATCH_BYTES (64u << 20)
+/* Part of it that the draw-sized tables may take (see below). */
+#define SG_STATIC_SCRATCH_TABLE_LIMIT (48u << 20)
+
+/* sg_draw that allocates nothing: no counterpart in the reference.
+ *
+ * Same pipeline, kernels and results as sg_draw, but every per-draw scratch
+ * buffer (triangle records, bin counters and entries, fragment chunks, tile
+ * tables, draw counters) is carved from one file-scope device array of
+ * SG_STATIC_SCRATCH_BYTES instead of the device's grow-only arenas, and no
+ * profiling events are taken.  It serves callers that must not allocate
+ * device memory during a frame: a host whose device memory is budgeted by
+ * another allocator (a pre-reserved pool that a cudaMalloc would go around
+ * or fail against), and frame loops that cannot take the device-wide
+ * synchronisation of the cudaFree/cudaMalloc pair an arena grows with.
+ *
+ * Limits: the draw-sized tables (3 slots per primitive of 4 + 16 * (8 + 3 *
+ * num_varyings) bytes, tiles x bin chunks counters, 1 KiB per 64x64 tile)
+ * must fit in SG_STATIC_SCRATCH_TABLE_LIMIT; a larger draw is rejected with
+ * SG_INVALID_PARAMETER and a message in sg_last_error before any kernel is
+ * launched.  Bin entries and fragment chunks share the rest; a draw whose
+ * coverage needs more returns SG_OUT_OF_MEMORY (with `stats`; otherwise at
+ * the next sg_sync) and leaves its targets partly drawn, as sg_draw does on
+ * an overflow.
+ *
+ * The first call on each CUDA device does setup: the device's module is
+ * loaded and the array's address looked up (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  Only the
+ * draw counters must start at zero, and the call clears them on its stream.
+ * All callers on one CUDA device share the array: calls whose work may
+ * overlap on the device (other sg_device handles, other streams) race and
+ * must be ordered by the caller; calls through one handle are ordered by
+ * its stream. */
+int32_t sg_draw_static_scratch(sg_device* dev, const sg_draw_desc* desc, sg_draw_stats* stats);
+
 /* renderer::clear_color (renderer.h:124). */
 int32_t sg_clear_color(sg_device* dev, uint32_t texture, const float rgba[4]);
 /* renderer::clear_depth_stencil (renderer.h:125-126). */

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -101,6 +102,25 @@ void make_ewa_table(float* tab) {
   }
   tab[0] = 1.0f;
   tab[255] = 0.0f;
+}
+
+// Scratch of sg_draw_static_scratch: one array per CUDA device, loaded with
+// this file's module.
+static __device__ __align__(256) uint8_t g_static_scratch[SG_STATIC_SCRATCH_BYTES];
+
+// Address of g_static_scratch on `ordinal`, which must be the current device;
+// looked up once per device.
+uint8_t* static_scratch_address(int ordinal) {
+  static std::mutex m;
+  static uint8_t* addr[128] = {};
+  if (ordinal < 0 || ordinal >= 128) return nullptr;
+  std::lock_guard<std::mutex> g(m);
+  if (!addr[ordinal]) {
+    void* a = nullptr;
+    if (cudaGetSymbolAddress(&a, g_static_scratch) != cudaSuccess) return nullptr;
+    addr[ordinal] = static_cast<uint8_t*>(a);
+  }
+  return addr[ordinal];
 }
 
 }  // namespace
@@ -209,7 +229,61 @@ void stage_end(sg_device* d, int stage, cudaEvent_t b) {
   d->marks.push_back({stage, {b, e}});
 }
 
-int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats) {
+// Lays the scratch of one draw out in the static array `base`: the draw
+// counters, the tables sized by the draw (records, bin counters, tile tables;
+// at most SG_STATIC_SCRATCH_TABLE_LIMIT bytes) and, in the rest, one quarter
+// for bin entries and three quarters for fragment chunks.
+int32_t carve_static_scratch(sg_device* d, uint8_t* base, DrawParams& p, uint32_t nslots, uint32_t ntiles,
+                             size_t ncounts, void** scan_sums) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    uint8_t* q = base + off;
+    off += (bytes + 255) & ~size_t(255);
+    return q;
+  };
+  take(sizeof(DrawCounters));
+  p.slot_rec = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(nslots) * 4));
+  p.recs = reinterpret_cast<float4*>(take(static_cast<size_t>(nslots) * p.rec_stride * sizeof(float4)));
+  p.bin_counts = reinterpret_cast<uint32_t*>(take(ncounts * 4));
+  *scan_sums = take((ncounts / 4096 + 2) * 4);
+  p.tile_begin = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(ntiles) + 1) * 4));
+  p.owner_first = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(ntiles) * RASTER_THREADS * 4));
+  if (off > SG_STATIC_SCRATCH_TABLE_LIMIT) {
+    char msg[200];
+    std::snprintf(msg, sizeof(msg),
+                  "sg_draw_static_scratch: the draw's tables need %zu bytes; the static scratch allows %u "
+                  "(%u primitives, %u tiles)",
+                  off, SG_STATIC_SCRATCH_TABLE_LIMIT, nslots / 3, ntiles);
+    d->error = msg;
+    return SG_INVALID_PARAMETER;
+  }
+  size_t rest = SG_STATIC_SCRATCH_BYTES - off;
+  uint32_t entries = static_cast<uint32_t>(rest / 4 / 4);
+  p.bin_entries = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(entries) * 4));
+  p.bin_capacity = entries;
+  // per fragment chunk: FRAG_CHUNK x (record, position, mask, 4 colours, ps flag) + next + count
+  size_t per_chunk = FRAG_CHUNK * (4 + 4 + 4 + 4 * sizeof(float4) + 1) + 8;
+  uint32_t chunks = static_cast<uint32_t>((SG_STATIC_SCRATCH_BYTES - off - 6 * 256) / per_chunk);
+  size_t nfrag = static_cast<size_t>(chunks) * FRAG_CHUNK;
+  p.frag_rec = reinterpret_cast<uint32_t*>(take(nfrag * 4));
+  p.frag_pos = reinterpret_cast<uint32_t*>(take(nfrag * 4));
+  p.frag_mask = reinterpret_cast<uint32_t*>(take(nfrag * 4));
+  p.frag_color = reinterpret_cast<float4*>(take(nfrag * 4 * sizeof(float4)));
+  p.frag_ps = take(nfrag);
+  p.chunk_next = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(chunks) * 4));
+  p.chunk_count = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(chunks) * 4));
+  p.chunk_capacity = chunks;
+  if (off > SG_STATIC_SCRATCH_BYTES) {  // layout arithmetic guard
+    d->error = "sg_draw_static_scratch: scratch layout exceeds the static array";
+    return SG_FAILED;
+  }
+  return SG_OK;
+}
+
+// `fixed` (sg_draw_static_scratch) is the static scratch array: all per-draw
+// scratch is carved from it and no profiling events are taken; otherwise the
+// device's arenas hold the scratch.
+int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats, uint8_t* fixed = nullptr) {
   cudaStream_t s = d->stream;
   if (desc->raster.fill_mode != SG_FILL_SOLID) return SG_INVALID_PARAMETER;
   if (desc->topology != SG_TOPOLOGY_TRIANGLE_LIST && desc->topology != SG_TOPOLOGY_TRIANGLE_STRIP)
@@ -339,8 +413,9 @@ int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats) 
   uint32_t nslots = desc->prim_count * 3;
   uint32_t ntiles = static_cast<uint32_t>(p.tiles_x * p.tiles_y);
   p.rec_stride = rec_stride_for(nattr);
-  p.counters = d->counters;
-  SG_CUDA(d, cudaMemsetAsync(d->counters, 0, sizeof(DrawCounters), s));
+  DrawCounters* counters = fixed ? reinterpret_cast<DrawCounters*>(fixed) : d->counters;
+  p.counters = counters;
+  SG_CUDA(d, cudaMemsetAsync(counters, 0, sizeof(DrawCounters), s));
   if (desc->prim_count == 0 || ntiles == 0) {
     if (stats) {
       std::memset(stats, 0, sizeof(*stats));
@@ -348,13 +423,17 @@ int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats) 
     }
     return SG_OK;
   }
-  SG_CUDA(d, d->slot_rec.ensure(static_cast<size_t>(nslots) * 4));
-  SG_CUDA(d, d->recs.ensure(static_cast<size_t>(nslots) * p.rec_stride * sizeof(float4)));
   uint32_t chunk = BIN_CHUNK_MIN;
   uint32_t max_chunks = static_cast<uint32_t>(d->num_sms) * 32;
   while ((nslots + chunk - 1) / chunk > max_chunks) chunk *= 2;
   uint32_t nchunks = (nslots + chunk - 1) / chunk;
   size_t ncounts = static_cast<size_t>(ntiles) * nchunks;
+  void* scan_sums = nullptr;
+  if (fixed) {
+    if (int32_t r = carve_static_scratch(d, fixed, p, nslots, ntiles, ncounts, &scan_sums)) return r;
+  } else {
+  SG_CUDA(d, d->slot_rec.ensure(static_cast<size_t>(nslots) * 4));
+  SG_CUDA(d, d->recs.ensure(static_cast<size_t>(nslots) * p.rec_stride * sizeof(float4)));
   if (ncounts >= (1u << 31)) return SG_OUT_OF_MEMORY;
   SG_CUDA(d, d->bin_counts.ensure(ncounts * 4));
   SG_CUDA(d, d->scan_sums.ensure((ncounts / 4096 + 2) * 4));
@@ -375,8 +454,6 @@ int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats) 
   p.bin_entries = static_cast<uint32_t*>(d->bin_entries.ptr);
   p.tile_begin = static_cast<uint32_t*>(d->tile_begin.ptr);
   p.bin_capacity = d->entry_capacity;
-  p.nchunks = nchunks;
-  p.chunk = chunk;
   p.frag_rec = static_cast<uint32_t*>(d->frag_rec.ptr);
   p.frag_pos = static_cast<uint32_t*>(d->frag_pos.ptr);
   p.frag_mask = static_cast<uint32_t*>(d->frag_mask.ptr);
@@ -386,25 +463,30 @@ int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats) 
   p.chunk_count = static_cast<uint32_t*>(d->chunk_count.ptr);
   p.chunk_capacity = d->chunk_capacity;
   p.owner_first = static_cast<uint32_t*>(d->owner_first.ptr);
+  scan_sums = d->scan_sums.ptr;
+  }
+  p.nchunks = nchunks;
+  p.chunk = chunk;
   uint32_t tile_grid = std::min<uint32_t>(ntiles, static_cast<uint32_t>(d->num_sms) * 3);
   uint32_t cover_grid = std::min<uint32_t>(ntiles * 4, static_cast<uint32_t>(d->num_sms) * 4);
   uint32_t shade_grid = static_cast<uint32_t>(d->num_sms) * 8;
   int const nreg = 1 + nattr;
 
-  cudaEvent_t ev = stage_begin(d);
+  auto begin = [&]() { return fixed ? nullptr : stage_begin(d); };
+  cudaEvent_t ev = begin();
   launch_geometry(p, nattr, s);
   stage_end(d, 0, ev);
-  ev = stage_begin(d);
+  ev = begin();
   SG_CUDA(d, cudaMemsetAsync(p.bin_counts, 0, ncounts * 4, s));
   launch_bin(p, nslots, false, s);
-  launch_scan(p.bin_counts, static_cast<uint32_t>(ncounts), static_cast<uint32_t*>(d->scan_sums.ptr), d->counters, s);
+  launch_scan(p.bin_counts, static_cast<uint32_t>(ncounts), static_cast<uint32_t*>(scan_sums), counters, s);
   launch_tile_ranges(p, ntiles, s);
   launch_bin(p, nslots, true, s);
   stage_end(d, 1, ev);
-  ev = stage_begin(d);
+  ev = begin();
   launch_cover(p, nreg, cover_grid, s);
   stage_end(d, 2, ev);
-  ev = stage_begin(d);
+  ev = begin();
   switch (nattr) {
   case 0: launch_shade_0(p, shade_grid, s); break;
   case 1: launch_shade_1(p, shade_grid, s); break;
@@ -414,17 +496,25 @@ int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats) 
   default: launch_shade_5(p, shade_grid, s); break;
   }
   stage_end(d, 3, ev);
-  ev = stage_begin(d);
+  ev = begin();
   launch_merge(p, nreg, tile_grid, s);
   stage_end(d, 4, ev);
   d->prof.draws += 1;
   d->prof.launches += 10;  // geometry, bin count, 3 scan kernels, tile ranges, bin fill, cover, shade, merge
   d->prof.raster_launches += 1;
   SG_CUDA(d, cudaGetLastError());
-  SG_CUDA(d, cudaMemcpyAsync(d->counters_host, d->counters, sizeof(DrawCounters), cudaMemcpyDeviceToHost, s));
+  SG_CUDA(d, cudaMemcpyAsync(d->counters_host, counters, sizeof(DrawCounters), cudaMemcpyDeviceToHost, s));
   if (stats) {
     SG_CUDA(d, cudaStreamSynchronize(s));
     DrawCounters const& c = *d->counters_host;
+    if (fixed && (c.overflow & 5u)) {
+      char msg[200];
+      std::snprintf(msg, sizeof(msg),
+                    "static scratch exhausted: %u bin entries (room for %u), %u fragment chunks (room for %u)",
+                    c.bin_entries, p.bin_capacity, c.chunk_total, p.chunk_capacity);
+      d->error = msg;
+      return SG_OUT_OF_MEMORY;
+    }
     if (c.overflow & 5u) {
       if (c.overflow & 1u) d->entry_capacity = std::max<uint32_t>(d->entry_capacity * 2, c.bin_entries + c.bin_entries / 4);
       if (c.overflow & 4u)
@@ -668,6 +758,19 @@ int32_t sg_sampler_destroy(sg_device* d, uint32_t h) {
 int32_t sg_draw(sg_device* d, const sg_draw_desc* desc, sg_draw_stats* stats) {
   if (!d || !desc) return SG_INVALID_PARAMETER;
   return draw_impl(d, desc, stats);
+}
+
+int32_t sg_draw_static_scratch(sg_device* d, const sg_draw_desc* desc, sg_draw_stats* stats) {
+  if (!d || !desc) return SG_INVALID_PARAMETER;
+  int cur = -1;
+  SG_CUDA(d, cudaGetDevice(&cur));
+  if (cur != d->ordinal) SG_CUDA(d, cudaSetDevice(d->ordinal));
+  uint8_t* base = static_scratch_address(d->ordinal);
+  if (!base) {
+    d->error = "sg_draw_static_scratch: static scratch address lookup failed";
+    return SG_CUDA_ERROR;
+  }
+  return draw_impl(d, desc, stats, base);
 }
 
 // render_core::clear_color -> surface::fill (render_core.cpp:96-99, surface.cpp:170-275)

@@ -143,6 +143,17 @@ class Device:
             return None
         return {k: getattr(st, k) for k, _ in abi.DrawStats._fields_}
 
+    def draw_static_scratch(self, desc, stats=False):
+        """sg_draw_static_scratch: the same draw with its scratch in the
+        library's static device array (no device allocation)."""
+        st = abi.DrawStats() if stats else None
+        self._check("sg_draw_static_scratch",
+                    self.lib.sg_draw_static_scratch(self.handle, C.byref(desc),
+                                                    C.byref(st) if st is not None else None))
+        if st is None:
+            return None
+        return {k: getattr(st, k) for k, _ in abi.DrawStats._fields_}
+
     def clear_color(self, tex, rgba):
         arr = (C.c_float * 4)(*rgba)
         self._check("sg_clear_color", self.lib.sg_clear_color(self.handle, tex, arr))
