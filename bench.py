@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--size", default="1920x1080",
+                    help="render-target size; smaller sizes are for profiling captures only")
     return ap.parse_args()
 
 
@@ -59,25 +62,42 @@ def workload_config(scene):
 
 
 # ---------------------------------------------------------------------------
-# algorithmic bytes of the raster stage for one frame (every item once)
-def raster_bytes(scene):
+# algorithmic bytes (every item counted once)
+DS_BYTES = 8       # RG32F depth-stencil element
+DEPTH_WORD = 4     # the depth word of it that early-Z reads and writes
+COLOR_BYTES = 4    # RGBA8
+STAGED_REC = 7 * 16  # edge equations, bbox, base and two gradients of the position
+FRAG_REC = 12        # record index, position, coverage per quad
+
+
+def frame_bytes(scene):
+    """Per frame: geometry + sampled texture + framebuffer traffic (clears,
+    depth and colour read-modify-write, resolve)."""
     npx = scene.width * scene.height
     s = scene.samples
-    ds = 8   # RG32F
-    col = 4  # RGBA8
-    fb = 2 * npx * s * ds + 2 * npx * s * col          # depth RMW (early-Z) + colour RMW (blend)
+    geom = sum(v.nbytes for v in scene.buffers.values())
     tex = 0
     for img, mips in scene.textures.values():
-        level0 = img.nbytes
-        tex += level0 * 4 // 3 if mips else level0      # every level sampled at most once
-    rec_bytes = (5 + 3 * 3) * 16                         # triangle record, 2 varyings
-    tris = rec_bytes * scene.triangles
-    return fb + tex + tris
+        tex += img.nbytes * 4 // 3 if mips else img.nbytes
+    fb = (npx * s * (COLOR_BYTES + DS_BYTES)          # clears
+          + 2 * npx * s * DEPTH_WORD                  # depth read-modify-write
+          + 2 * npx * s * COLOR_BYTES                 # colour read-modify-write (blend)
+          + npx * s * COLOR_BYTES + npx * COLOR_BYTES)  # resolve
+    return geom + tex + fb
+
+
+def cover_bytes(scene, stats):
+    """Per frame, k_cover: the depth words read and written once, one staged
+    triangle record per clipped primitive, one fragment record per quad."""
+    npx = scene.width * scene.height
+    cprims = sum(st["cprimitives"] for st in stats)
+    quads = sum(st["ps_invocations"] for st in stats) // 4
+    return 2 * npx * scene.samples * DEPTH_WORD + cprims * STAGED_REC + quads * FRAG_REC
 
 
 def read_traffic():
-    """Per-launch DRAM traffic of k_raster from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_raster_c2_1080p_4x.md")
+    """Per-launch DRAM traffic of k_cover from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_cover_c2_1080p_4x.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -223,10 +243,12 @@ def run_gpu(args):
     torch.cuda.set_stream(stream)
     lib = abi.bind(ctypes.CDLL(pbuild.ensure_built()))
     dev = Device(lib, cuda_device=local, stream=stream.cuda_stream)
-    scene = scenes.c2_scene(seed=SEED + rank)
+    width, height = (int(v) for v in args.size.lower().split("x"))
+    scene = scenes.c2_scene(seed=SEED + rank, width=width, height=height)
     b = scenes.Bound(dev, scene)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
+    frame_stats = b.frame(stats=True)  # pipeline counters of one frame (untimed)
     for _ in range(args.warmup):
         b.frame()
     dev.sync()
@@ -275,26 +297,31 @@ def run_gpu(args):
         if st != abi.SG_OK:
             raise RuntimeError("sg_texture_download failed")
 
-    for _ in range(args.warmup):
-        e2e_frame()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        flush.zero_()
-        e2e_frame()
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_fps = frames / e2e_s
+    e2e_fps = None
+    if not args.no_e2e:
+        for _ in range(args.warmup):
+            e2e_frame()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            e2e_frame()
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e_fps = frames / e2e_s
 
     if rank == 0:
         peak, peak_kind = measured_peak()
-        raster_launch_ms = prof["raster_ms"] / max(1, prof["raster_launches"])
-        bytes_per_launch = raster_bytes(scene) / len(scene.draws)
-        achieved = bytes_per_launch / (raster_launch_ms / 1000.0) / 1e9
+        ndraws = len(scene.draws)
+        cover_launch_ms = prof["cover_ms"] / max(1, prof["raster_launches"])
+        cover_launch_bytes = cover_bytes(scene, frame_stats) / ndraws
+        achieved = cover_launch_bytes / (cover_launch_ms / 1000.0) / 1e9
+        fbytes = frame_bytes(scene)
+        frame_achieved = fbytes / (total_s / args.steps) / 1e9
         cpu = None
         if not args.no_cpu_baseline:
             frames_cpu = 2
@@ -310,18 +337,22 @@ def run_gpu(args):
             "gpix_per_s": fps * scene.width * scene.height / 1e9,
             "gsamples_per_s": fps * scene.width * scene.height * scene.samples / 1e9,
             "mtris_per_s": fps * scene.triangles / 1e6,
-            "stage_ms_per_frame": {"geometry": prof["geometry_ms"] / args.steps,
-                                   "binning": prof["binning_ms"] / args.steps,
-                                   "raster": prof["raster_ms"] / args.steps},
-            "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peak,
+            "stage_ms_per_frame": {k: prof[k + "_ms"] / args.steps
+                                   for k in ("geometry", "binning", "cover", "shade", "merge")},
+            "roofline": {"bound": "hbm", "kernel": "k_cover", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": read_traffic(),
-                         "algorithmic_bytes_per_launch": bytes_per_launch,
-                         "launch_ms": raster_launch_ms},
+                         "traffic": read_traffic() if (width, height) == (1920, 1080) else None,
+                         "algorithmic_bytes_per_launch": cover_launch_bytes,
+                         "launch_ms": cover_launch_ms},
+            "frame_roofline": {"algorithmic_bytes_per_frame": fbytes, "achieved": frame_achieved,
+                               "peak": peak, "unit": "GB/s", "frac": frame_achieved / peak},
+            "pipeline_counters_per_frame": {k: sum(st[k] for st in frame_stats)
+                                            for k in frame_stats[0]},
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_fps, "unit": UNIT,
-                    "h2d_bytes_per_step": int(vb_host.numel() * 4 + ib_host.numel() * 4),
-                    "d2h_bytes_per_step": out_bytes},
+            "e2e": None if e2e_fps is None else {
+                "value": e2e_fps, "unit": UNIT,
+                "h2d_bytes_per_step": int(vb_host.numel() * 4 + ib_host.numel() * 4),
+                "d2h_bytes_per_step": out_bytes},
             "gpu_launches": int(prof["launches"]),
             "clocks": clk.summary(),
         }

@@ -494,6 +494,35 @@ __host__ __device__ constexpr size_t cover_smem(uint32_t samples, bool early_z) 
   return COVER_SMEM_BASE + (early_z ? static_cast<size_t>(QUAD_PX) * QUAD_PX * samples * 4 : 0);
 }
 
+// The sample slots a lane covers in a (triangle, block) pair: slot lane + 32
+// pass of the block's 16 pixels x samples, pixel-major.  Fixed per draw.
+struct LaneSlots {
+  uint32_t bit[2];   // the slot's bit in its half-block coverage word; 0 if unused
+  uint32_t pix[2];   // ix | iy << 2 | sm << 4 | quad << 8 | pixel-in-quad << 10
+  uint32_t zoff[2];  // offset of the slot in the staged depth, relative to the block
+  float mx[2], my[2];  // sample position in the block
+  float ax[2], ay[2];  // sample offset from the pixel centre (aa_z_offset)
+};
+__device__ inline LaneSlots lane_slots(DrawParams const& p, int lane, int zpitch) {
+  LaneSlots ls;
+  uint32_t const S = p.samples;
+#pragma unroll
+  for (int pass = 0; pass < 2; ++pass) {
+    uint32_t slot = lane + 32 * pass;
+    uint32_t i16 = slot / S, sm = slot % S;
+    uint32_t ix = i16 & 3, iy = (i16 >> 2) & 3;
+    uint32_t q = ((iy >> 1) << 1) | (ix >> 1), i = ((iy & 1) << 1) | (ix & 1);
+    ls.bit[pass] = slot < 16 * S ? 1u << (4 * i + sm + 16 * (q & 1)) : 0u;
+    ls.pix[pass] = ix | (iy << 2) | (sm << 4) | (q << 8) | (i << 10);
+    ls.zoff[pass] = (iy * zpitch + ix) * S + sm;
+    ls.mx[pass] = p.sp_x[sm & 3u] + static_cast<float>(ix);
+    ls.my[pass] = p.sp_y[sm & 3u] + static_cast<float>(iy);
+    ls.ax[pass] = p.sp_x[sm & 3u] - 0.5f;
+    ls.ay[pass] = p.sp_y[sm & 3u] - 0.5f;
+  }
+  return ls;
+}
+
 // One (triangle, 4x4 block) pair processed by the whole warp: the block's
 // level-2 classification (rasterizer.cpp:441-571), the per-sample coverage
 // of draw_partial_tile (rasterizer.cpp:298-439) and early-Z
@@ -501,9 +530,9 @@ __host__ __device__ constexpr size_t cover_smem(uint32_t samples, bool early_z) 
 // slot per lane and pass; the quads' masks are assembled with warp
 // reductions and the block's owner lane appends the surviving quads.
 __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool full16, int tile_x0, int tile_y0, int blk,
-                                 int owner, OwnerList& L, uint32_t* ztile, int zx0, int zy0, int zpitch, int lane) {
+                                 int owner, OwnerList& L, uint32_t* ztile, int zx0, int zy0, int zpitch,
+                                 LaneSlots const& ls, int lane) {
   StageView t{st};
-  uint32_t const rec = st->entry >> 1;
   int const bx = blk & 15, by = blk >> 4;
   int const bx_abs = tile_x0 + bx * 4, by_abs = tile_y0 + by * 4;
   float const trr = p.target_w, trb = p.target_h;
@@ -518,7 +547,6 @@ __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool f
     if (static_cast<float>(bx_abs) >= trr || static_cast<float>(by_abs) >= trb) return;
     region_full = c == 2;
   }
-  uint32_t const S = p.samples, nslots = 16 * S;
   uint32_t const W = p.width, H = p.height;
   float const lf = static_cast<float>(bx_abs), tf = static_cast<float>(by_abs);
   float ev[3];
@@ -527,34 +555,28 @@ __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool f
   // coverage: unclipped (uc) and clipped to the target (cv), 4 bits per pixel,
   // quads 0/1 in the low word, 2/3 in the high word
   uint32_t uc_lo = 0, uc_hi = 0, cv_lo = 0, cv_hi = 0;
-  uint32_t slot_bit[2] = {0, 0};
-  bool slot_hi[2] = {false, false};
 #pragma unroll
   for (int pass = 0; pass < 2; ++pass) {
-    uint32_t slot = lane + 32 * pass;
-    if (slot >= nslots) continue;
-    uint32_t i16 = slot / S, sm = slot % S;
-    uint32_t ix = i16 & 3, iy = i16 >> 2;
-    uint32_t q = ((iy >> 1) << 1) | (ix >> 1), i = ((iy & 1) << 1) | (ix & 1);
-    uint32_t bit = 1u << (4 * i + sm + 16 * (q & 1));
-    slot_bit[pass] = bit;
-    slot_hi[pass] = q >= 2;
-    bool in;
-    if (region_full) {
-      in = true;
-    } else {
-      float mx = p.sp_x[sm] + static_cast<float>(ix), my = p.sp_y[sm] + static_cast<float>(iy);
+    uint32_t bit = ls.bit[pass];
+    bool in = region_full;
+    if (!in) {
+      float mx = ls.mx[pass], my = ls.my[pass];
       bool rej = false;
 #pragma unroll
       for (int k = 0; k < 3; ++k) rej = rej || ((mx * e[k].x + my * e[k].y) < ev[k]);
       in = !rej;
     }
-    bool inside = bx_abs + ix < W && by_abs + iy < H;  // EXTENSION: pixels outside the target are not covered
-    if (in) {
-      if (q >= 2) uc_hi |= bit; else uc_lo |= bit;
-      if (inside) {
-        if (q >= 2) cv_hi |= bit; else cv_lo |= bit;
-      }
+    uint32_t pix = ls.pix[pass];
+    bool hi = (pix >> 9) & 1u;
+    // EXTENSION: pixels outside the target are not covered
+    bool inside = bx_abs + (pix & 3u) < W && by_abs + ((pix >> 2) & 3u) < H;
+    uint32_t ub = in ? bit : 0u, cb = in && inside ? bit : 0u;
+    if (hi) {
+      uc_hi |= ub;
+      cv_hi |= cb;
+    } else {
+      uc_lo |= ub;
+      cv_lo |= cb;
     }
   }
   uc_lo = __reduce_or_sync(0xFFFFFFFFu, uc_lo);
@@ -562,7 +584,7 @@ __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool f
   cv_lo = __reduce_or_sync(0xFFFFFFFFu, cv_lo);
   cv_hi = __reduce_or_sync(0xFFFFFFFFu, cv_hi);
   if ((cv_lo | cv_hi) == 0) return;
-  uint32_t const fm = (1u << S) - 1u;
+  uint32_t const fm = (1u << p.samples) - 1u;
   uint32_t const qfull = fm | (fm << 4) | (fm << 8) | (fm << 12);
   // a full region's quads are drawn when their left / top pixel is inside the
   // target (draw_full_tile, rasterizer.cpp:738-742): no quad of this block is
@@ -574,34 +596,32 @@ __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool f
     uint32_t t_lo = 0, t_hi = 0;
     uint32_t cfg_rd = p.read_depth, cfg_wr = p.write_depth;
     bool d24 = p.ds_fmt == SG_FMT_D24S8;
+    uint32_t* zblk = ztile + ((by_abs - zy0) * zpitch + (bx_abs - zx0)) * p.samples;
 #pragma unroll
     for (int pass = 0; pass < 2; ++pass) {
-      uint32_t slot = lane + 32 * pass;
-      if (slot >= nslots) continue;
-      uint32_t bit = slot_bit[pass];
-      bool covered = slot_hi[pass] ? (cv_hi & bit) : (cv_lo & bit);
-      if (!covered) continue;
-      uint32_t i16 = slot / S, sm = slot % S;
-      uint32_t ix = i16 & 3, iy = i16 >> 2;
-      uint32_t q = ((iy >> 1) << 1) | (ix >> 1), i = ((iy & 1) << 1) | (ix & 1);
+      uint32_t bit = ls.bit[pass], pix = ls.pix[pass];
+      bool hi = (pix >> 9) & 1u;
+      if (!((hi ? cv_hi : cv_lo) & bit)) continue;
+      uint32_t q = (pix >> 8) & 3u, i = (pix >> 10) & 3u;
       uint32_t qx = bx_abs + ((q & 1) << 1), qy = by_abs + (q & 2);
       float dx = 0.5f + static_cast<float>(qx) - v0.x;
       float dy = 0.5f + static_cast<float>(qy) - v0.y;
       float z = quad_pos(t, dx, dy, static_cast<int>(i)).z;
-      float nd = S == 1 ? z : ((p.sp_x[sm] - 0.5f) * dz + (p.sp_y[sm] - 0.5f) * dyz) + z;
-      uint32_t* zp = ztile + ((by_abs - zy0 + iy) * zpitch + (bx_abs - zx0 + ix)) * S + sm;
+      float nd = p.samples == 1 ? z : (ls.ax[pass] * dz + ls.ay[pass] * dyz) + z;
+      uint32_t* zp = zblk + ls.zoff[pass];
       uint32_t w = *zp;
       bool pass_z = d24 ? cmpu(p.depth_func, d24_quantize(nd), cfg_rd ? (w & 0xFFFFFFu) : 0u)
                         : cmpf(p.depth_func, nd, cfg_rd ? __uint_as_float(w) : 0.0f);
       if (pass_z) {
         if (cfg_wr) *zp = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
-        if (slot_hi[pass]) t_hi |= bit; else t_lo |= bit;
+        if (hi) t_hi |= bit; else t_lo |= bit;
       }
     }
     tested_lo = __reduce_or_sync(0xFFFFFFFFu, t_lo);
     tested_hi = __reduce_or_sync(0xFFFFFFFFu, t_hi);
   }
   if (lane == owner) {
+    uint32_t const rec = st->entry >> 1;
 #pragma unroll 1
     for (int q = 0; q < 4; ++q) {
       uint32_t tq = ((q < 2 ? tested_lo : tested_hi) >> (16 * (q & 1))) & 0xFFFFu;
@@ -630,11 +650,13 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
   __shared__ uint32_t s_item;
   if (p.counters->overflow & 1u) return;
   int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // lane l < 16 of warp w owns quadrant block lb = 4 l + w (blocks of a warp
-  // are interleaved over the quadrant so that dense rows spread over warps)
-  int const lb = 4 * (lane & 15) + warp;
+  // lane l < 16 of warp w owns the quadrant block (x, y) with (x + y) mod 4 =
+  // w: y = l / 2, so that the blocks along a row, a column or an anti-diagonal
+  // of the quadrant spread over all four warps
+  int const lby = (lane & 15) >> 1, lbx = ((warp - lby) & 3) + 4 * (lane & 1);
+  int const lb = lby * 8 + lbx;
   bool const owns = lane < 16;
-  int const lbx = lb & 7, lby = lb >> 3;
+  LaneSlots const ls = lane_slots(p, lane, QUAD_PX);
   int const nitems = p.tiles_x * p.tiles_y * 4;
   float const trr = p.target_w, trb = p.target_h;
   OwnerList L{NO_CHUNK, NO_CHUNK, 0, 0};
@@ -740,10 +762,10 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
           while (blocks) {
             int l = __ffs(blocks) - 1;
             blocks &= blocks - 1;
-            int olb = 4 * l + warp;
-            int oblk = ((qd >> 1) * 8 + (olb >> 3)) * 16 + (qd & 1) * 8 + (olb & 7);
+            int oy = l >> 1, ox = ((warp - oy) & 3) + 4 * (l & 1);
+            int oblk = ((qd >> 1) * 8 + oy) * 16 + (qd & 1) * 8 + ox;
             pair_warp(p, stage + (w << 5) + b, (fulls >> l) & 1u, tile_x0, tile_y0, oblk, l, L, ztile, qx0, qy0, QUAD_PX,
-                      lane);
+                      ls, lane);
           }
         }
       }
