@@ -488,6 +488,7 @@ constexpr int STAGE_TRIS = 256;  // triangles staged in shared memory per batch
 constexpr int MASK_WORDS = STAGE_TRIS / 32;
 constexpr int COVER_THREADS = 128;  // one CTA per 32x32 quadrant of a tile
 constexpr int QUAD_PX = 32;
+constexpr uint32_t SPLIT_ENTRIES = 320;  // tiles with more bin entries are covered as 16 regions
 constexpr size_t COVER_SMEM_BASE = STAGE_TRIS * sizeof(TriStage) + (64 + 4) * MASK_WORDS * sizeof(uint32_t);
 // plus the staged depth: QUAD_PX * QUAD_PX * samples words (only when early-Z is on)
 __host__ __device__ constexpr size_t cover_smem(uint32_t samples, bool early_z) {
@@ -638,54 +639,79 @@ __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool f
 __device__ inline int tile_x0_of(DrawParams const& p, uint32_t tile) { return static_cast<int>(tile % p.tiles_x) * TILE; }
 __device__ inline int tile_y0_of(DrawParams const& p, uint32_t tile) { return static_cast<int>(tile / p.tiles_x) * TILE; }
 
+// Block owned by lane l < 4 n of warp w in an n x n-block item (n = 8 or 4):
+// the blocks (x, y) with (x + y) mod 4 = w, so that the blocks along a row, a
+// column or an anti-diagonal spread over all four warps.
+__device__ inline void owned_block(int n, int w, int l, int& x, int& y) {
+  if (n == 8) {
+    y = l >> 1;
+    x = ((w - y) & 3) + 4 * (l & 1);
+  } else {
+    y = l;
+    x = (w - y) & 3;
+  }
+}
+
+// Coverage of one draw.  Work items are squares of one tile: its four 32x32
+// quadrants, or, for a tile with more than SPLIT_ENTRIES bin entries, its
+// sixteen 16x16 regions, taken from a dynamic cursor over 16 item slots per
+// tile.  A CTA stages the tile's triangles in batches, classifies them
+// against the item's 16x16 regions and 4x4 blocks (rasterizer.cpp:441-571),
+// and its four warps walk (triangle, block) pairs in primitive order with the
+// item's depth held in shared memory for early-Z.
 __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nreg) {
   extern __shared__ __align__(16) uint8_t smem[];
   TriStage* stage = reinterpret_cast<TriStage*>(smem);
-  // triangle sets of the staged batch (word-major): per 4x4 block of the
-  // quadrant (its 16x16 region partial, block inside the bounding box) and per
-  // 16x16 region of the quadrant (region accepted)
+  // triangle sets of the staged batch (word-major): per 4x4 block of the item
+  // (its 16x16 region partial, block inside the bounding box) and per 16x16
+  // region of the item (region accepted)
   uint32_t* mask4 = reinterpret_cast<uint32_t*>(smem + STAGE_TRIS * sizeof(TriStage));
   uint32_t* mask16 = mask4 + 64 * MASK_WORDS;
   uint32_t* ztile = mask16 + 4 * MASK_WORDS;
   __shared__ uint32_t s_item;
   if (p.counters->overflow & 1u) return;
   int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // lane l < 16 of warp w owns the quadrant block (x, y) with (x + y) mod 4 =
-  // w: y = l / 2, so that the blocks along a row, a column or an anti-diagonal
-  // of the quadrant spread over all four warps
-  int const lby = (lane & 15) >> 1, lbx = ((warp - lby) & 3) + 4 * (lane & 1);
-  int const lb = lby * 8 + lbx;
-  bool const owns = lane < 16;
-  LaneSlots const ls = lane_slots(p, lane, QUAD_PX);
-  int const nitems = p.tiles_x * p.tiles_y * 4;
+  uint32_t const nslots = static_cast<uint32_t>(p.tiles_x * p.tiles_y) * 16;
   float const trr = p.target_w, trb = p.target_h;
+  uint32_t const S = p.samples;
   OwnerList L{NO_CHUNK, NO_CHUNK, 0, 0};
   for (;;) {
     if (tid == 0) s_item = atomicAdd(&p.counters->tile_cursor, 1u);
     __syncthreads();
-    uint32_t item = s_item;
+    uint32_t const item = s_item;
     __syncthreads();
-    if (item >= static_cast<uint32_t>(nitems)) break;
-    uint32_t const tile = item >> 2, qd = item & 3;
-    uint32_t begin = p.tile_begin[tile], end = p.tile_begin[tile + 1];
-    int tile_x0 = tile_x0_of(p, tile), tile_y0 = tile_y0_of(p, tile);
-    int const qx0 = tile_x0 + (qd & 1) * QUAD_PX, qy0 = tile_y0 + (qd >> 1) * QUAD_PX;
-    int const q16x = (qd & 1) * 2, q16y = (qd >> 1) * 2;  // first 16x16 region of the quadrant
-    int const blk = ((qd >> 1) * 8 + lby) * 16 + (qd & 1) * 8 + lbx;  // owned block, tile numbering
-    int const own16 = (lby >> 2) * 2 + (lbx >> 2);                   // its 16x16 region, quadrant numbering
+    if (item >= nslots) break;
+    uint32_t const tile = item >> 4, sub = item & 15;
+    uint32_t const begin = p.tile_begin[tile], end = p.tile_begin[tile + 1];
+    bool const split = end - begin > SPLIT_ENTRIES;
+    if (!split && sub >= 4) continue;
+    int const n = split ? 4 : 8;   // blocks per side
+    int const px = 4 * n;          // pixels per side
+    int const rs = n >> 2;         // 16x16 regions per side
+    int const bx0 = split ? (sub & 3) * 4 : (sub & 1) * 8, by0 = split ? (sub >> 2) * 4 : (sub >> 1) * 8;
+    int const tile_x0 = tile_x0_of(p, tile), tile_y0 = tile_y0_of(p, tile);
+    int const x0 = tile_x0 + bx0 * 4, y0 = tile_y0 + by0 * 4;
+    int const r16x0 = bx0 >> 2, r16y0 = by0 >> 2;  // first 16x16 region of the item
+    bool const owns = lane < (n == 8 ? 16 : 4);
+    int ox = 0, oy = 0;
+    owned_block(n, warp, lane & 15, ox, oy);
+    int const blk = (by0 + oy) * 16 + bx0 + ox;           // owned block, tile numbering
+    int const ib = oy * n + ox;                            // owned block, item numbering
+    int const own16 = (oy >> 2) * rs + (ox >> 2);          // its 16x16 region, item numbering
+    LaneSlots const ls = lane_slots(p, lane, px);
     float const tx0f = static_cast<float>(tile_x0), ty0f = static_cast<float>(tile_y0);
     L.first = L.cur = NO_CHUNK;
     L.count = 0;
     bool const stage_z = p.early_z && begin < end;
-    uint32_t const qw = min(static_cast<uint32_t>(QUAD_PX), p.width - min(p.width, static_cast<uint32_t>(qx0)));
-    uint32_t const qh = min(static_cast<uint32_t>(QUAD_PX), p.height - min(p.height, static_cast<uint32_t>(qy0)));
-    uint32_t const S = p.samples;
+    uint32_t const qw = min(static_cast<uint32_t>(px), p.width - min(p.width, static_cast<uint32_t>(x0)));
+    uint32_t const qh = min(static_cast<uint32_t>(px), p.height - min(p.height, static_cast<uint32_t>(y0)));
+    uint32_t const zrow = px * S;
     if (stage_z) {
-      for (uint32_t i = tid; i < qh * QUAD_PX * S; i += COVER_THREADS) {
-        uint32_t y = i / (QUAD_PX * S), k = i % (QUAD_PX * S);
+      for (uint32_t i = tid; i < qh * zrow; i += COVER_THREADS) {
+        uint32_t y = i / zrow, k = i % zrow;
         if (k >= qw * S) continue;
         uint32_t x = k / S, sm = k % S;
-        ztile[(y * QUAD_PX + x) * S + sm] = *reinterpret_cast<uint32_t const*>(ds_addr(p, qx0 + x, qy0 + y, sm));
+        ztile[i] = *reinterpret_cast<uint32_t const*>(ds_addr(p, x0 + x, y0 + y, sm));
       }
     }
     for (uint32_t bstart = begin; bstart < end; bstart += STAGE_TRIS) {
@@ -693,7 +719,7 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
       __syncthreads();
       for (int i = tid; i < (64 + 4) * MASK_WORDS; i += COVER_THREADS) mask4[i] = 0;
       __syncthreads();
-      // stage the batch and classify each triangle against the quadrant's 16x16 regions
+      // stage the batch and classify each triangle against the item's 16x16 regions
       for (uint32_t i = tid; i < nb; i += COVER_THREADS) {
         uint32_t e = p.bin_entries[bstart + i];
         float4 const* R = p.recs + static_cast<size_t>(e >> 1) * p.rec_stride;
@@ -709,26 +735,25 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
         stage[i] = ts;
         uint32_t bit = 1u << (i & 31), word = i >> 5;
         if (e & 1u) {  // accepted for the whole tile by the binner
-          for (int r = 0; r < 4; ++r) atomicOr(&mask16[word * 4 + r], bit);
+          for (int r = 0; r < rs * rs; ++r) atomicOr(&mask16[word * 4 + r], bit);
           continue;
         }
         float x_min = ts.bbox.x - tx0f, x_max = ts.bbox.y - tx0f, y_min = ts.bbox.z - ty0f, y_max = ts.bbox.w - ty0f;
         float4 ed[3] = {ts.e0, ts.e1, ts.e2};
         LevelParams l1, l2;
         level_params(ed, l1, l2);
-        for (int iy = q16y; iy < q16y + 2; ++iy) {
+        for (int iy = r16y0; iy < r16y0 + rs; ++iy) {
           int m16y = iy * 16;
           if (y_min >= static_cast<float>(m16y + 16) || y_max < static_cast<float>(m16y)) continue;
-          for (int ix = q16x; ix < q16x + 2; ++ix) {
+          for (int ix = r16x0; ix < r16x0 + rs; ++ix) {
             int m16x = ix * 16;
             if (x_min >= static_cast<float>(m16x + 16) || x_max < static_cast<float>(m16x)) continue;
             int c = child_class(ed, l1, tx0f, ty0f, ix, iy);
             if (c == 0) continue;
             // a region whose origin is right of / below the target is skipped
             if (static_cast<float>(tile_x0 + m16x) >= trr || static_cast<float>(tile_y0 + m16y) >= trb) continue;
-            int r16 = (iy - q16y) * 2 + (ix - q16x);
             if (c == 2) {
-              atomicOr(&mask16[word * 4 + r16], bit);
+              atomicOr(&mask16[word * 4 + (iy - r16y0) * rs + (ix - r16x0)], bit);
               continue;
             }
             // partial: the 4x4 children that pass the level-2 bounding-box test
@@ -738,8 +763,7 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
               for (int jx = 0; jx < 4; ++jx) {
                 int m4x = m16x + jx * 4;
                 if (x_min >= static_cast<float>(m4x + 4) || x_max < static_cast<float>(m4x)) continue;
-                int qb = ((iy - q16y) * 4 + jy) * 8 + (ix - q16x) * 4 + jx;  // quadrant block
-                atomicOr(&mask4[word * 64 + qb], bit);
+                atomicOr(&mask4[word * 64 + (iy * 4 + jy - by0) * n + (ix * 4 + jx - bx0)], bit);
               }
             }
           }
@@ -752,7 +776,7 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
       // reference's primitive order.
       for (int w = 0; w < MASK_WORDS; ++w) {
         uint32_t m16 = owns ? mask16[w * 4 + own16] : 0u;
-        uint32_t mine = owns ? (mask4[w * 64 + lb] | m16) : 0u;
+        uint32_t mine = owns ? (mask4[w * 64 + ib] | m16) : 0u;
         uint32_t tris = __reduce_or_sync(0xFFFFFFFFu, mine);
         while (tris) {
           int b = __ffs(tris) - 1;
@@ -762,9 +786,10 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
           while (blocks) {
             int l = __ffs(blocks) - 1;
             blocks &= blocks - 1;
-            int oy = l >> 1, ox = ((warp - oy) & 3) + 4 * (l & 1);
-            int oblk = ((qd >> 1) * 8 + oy) * 16 + (qd & 1) * 8 + ox;
-            pair_warp(p, stage + (w << 5) + b, (fulls >> l) & 1u, tile_x0, tile_y0, oblk, l, L, ztile, qx0, qy0, QUAD_PX,
+            int lx, ly;
+            owned_block(n, warp, l, lx, ly);
+            int oblk = (by0 + ly) * 16 + bx0 + lx;
+            pair_warp(p, stage + (w << 5) + b, (fulls >> l) & 1u, tile_x0, tile_y0, oblk, l, L, ztile, x0, y0, px,
                       ls, lane);
           }
         }
@@ -772,14 +797,14 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
     }
     if (stage_z) {
       __syncthreads();
-      for (uint32_t i = tid; i < qh * QUAD_PX * S; i += COVER_THREADS) {
-        uint32_t y = i / (QUAD_PX * S), k = i % (QUAD_PX * S);
+      for (uint32_t i = tid; i < qh * zrow; i += COVER_THREADS) {
+        uint32_t y = i / zrow, k = i % zrow;
         if (k >= qw * S) continue;
         uint32_t x = k / S, sm = k % S;
-        *reinterpret_cast<uint32_t*>(ds_addr(p, qx0 + x, qy0 + y, sm)) = ztile[(y * QUAD_PX + x) * S + sm];
+        *reinterpret_cast<uint32_t*>(ds_addr(p, x0 + x, y0 + y, sm)) = ztile[i];
       }
     }
-    // close the owned block's list for the tile
+    // close the owned block's list for the item
     if (owns) {
       if (L.cur != NO_CHUNK) {
         p.chunk_next[L.cur] = NO_CHUNK;
