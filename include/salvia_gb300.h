@@ -302,9 +302,10 @@ int32_t sg_draw(sg_device* dev, const sg_draw_desc* desc, sg_draw_stats* stats);
  * or fail against), and frame loops that cannot take the device-wide
  * synchronisation of the cudaFree/cudaMalloc pair an arena grows with.
  *
- * Limits: the draw-sized tables (3 slots per primitive of 4 + 16 * (8 + 3 *
- * num_varyings) bytes, tiles x bin chunks counters, 1 KiB per 64x64 tile)
- * must fit in SG_STATIC_SCRATCH_TABLE_LIMIT; a larger draw is rejected with
+ * Limits: the draw-sized tables (the draw's parameter block, 3 slots per
+ * primitive of 4 + 16 * (8 + 3 * num_varyings) bytes, tiles x bin chunks
+ * counters, 1 KiB per 64x64 tile) must fit in
+ * SG_STATIC_SCRATCH_TABLE_LIMIT; a larger draw is rejected with
  * SG_INVALID_PARAMETER and a message in sg_last_error before any kernel is
  * launched.  Bin entries and fragment chunks share the rest; a draw whose
  * coverage needs more returns SG_OUT_OF_MEMORY (with `stats`; otherwise at
@@ -320,6 +321,79 @@ int32_t sg_draw(sg_device* dev, const sg_draw_desc* desc, sg_draw_stats* stats);
  * must be ordered by the caller; calls through one handle are ordered by
  * its stream. */
 int32_t sg_draw_static_scratch(sg_device* dev, const sg_draw_desc* desc, sg_draw_stats* stats);
+
+/* ---- batched submission --------------------------------------------------
+ * A command list of draws, clears and resolves, possibly over many render
+ * targets (many frames).  Results are exactly those of issuing the commands
+ * one by one through sg_draw / sg_clear_* / sg_resolve (the reference
+ * executes render_core commands in order, render_core.cpp:30-61); the
+ * runtime groups them into passes, each pass one kernel chain over all of
+ * its draws and targets, splitting where order matters: a target cleared,
+ * resolved or sampled between two of its draws, a draw whose depth test runs
+ * before shading (no stencil) after one whose test runs after shading on the
+ * same depth target, or a pass reaching SG_PASS_MAX_PRIMS primitives. */
+enum { SG_CMD_DRAW = 1, SG_CMD_CLEAR_COLOR = 2, SG_CMD_CLEAR_DEPTH_STENCIL = 3, SG_CMD_RESOLVE = 4 };
+#define SG_PASS_MAX_PRIMS (1u << 24)
+
+typedef struct sg_command {
+  uint32_t type;                       /* SG_CMD_* */
+  uint32_t texture;                    /* clear target; resolve source */
+  uint32_t texture2;                   /* resolve destination */
+  uint32_t flags;                      /* SG_CLEAR_DEPTH | SG_CLEAR_STENCIL */
+  float color[4];                      /* clear colour */
+  float depth;
+  uint32_t stencil;
+  const sg_draw_desc* draw;            /* SG_CMD_DRAW */
+} sg_command;
+
+/* Executes `n` commands in order.  `stats` may be NULL, else it holds one
+ * entry per command (zero for non-draw commands) and the call synchronises. */
+int32_t sg_submit(sg_device* dev, const sg_command* cmds, uint32_t n, sg_draw_stats* stats);
+
+/* Recorded command lists: no counterpart in the reference (its async
+ * renderer queues commands to a render thread, async_renderer.cpp:19-104;
+ * here a list becomes one CUDA graph).  sg_graph_create executes the list
+ * once (exactly as sg_submit would, so the targets hold one execution's
+ * results), sizes private scratch for it from that run's counters, and
+ * captures every pass into one CUDA graph with the draw parameters resident
+ * on the device.  sg_graph_launch replays the whole list as one graph
+ * launch on the device's stream; the buffers, textures and samplers the
+ * list names must stay alive and keep their sizes.  Replays of the same
+ * inputs need the same scratch; a replay whose inputs changed so much that
+ * the scratch overflows reports SG_OUT_OF_MEMORY at the next sg_sync. */
+typedef struct sg_graph sg_graph;
+int32_t sg_graph_create(sg_device* dev, const sg_command* cmds, uint32_t n, sg_graph** out_graph);
+int32_t sg_graph_launch(sg_device* dev, sg_graph* graph);
+/* Launches of the graph recorded so far and the passes it holds. */
+int32_t sg_graph_info(sg_device* dev, sg_graph* graph, uint32_t* passes, uint32_t* kernels);
+void sg_graph_destroy(sg_device* dev, sg_graph* graph);
+
+/* ---- scheduling parameters and the autotuner ------------------------------
+ * None of these changes results, only how the work is cut: the coverage
+ * work-item edge (16 or 32 pixels; a 64x64 binning tile is covered as four
+ * 32x32 items or sixteen 16x16 items, the latter also for any tile with more
+ * than `split_entries` bin entries), the minimum triangle slots per binning
+ * warp, the initial bin-entry and fragment capacities, the pixel-shading
+ * quads per warp, and CTAs per SM for the shading and merging kernels. */
+typedef struct sg_tuning {
+  uint32_t cover_item;       /* 16 or 32 */
+  uint32_t split_entries;    /* 32x32 items become 16x16 above this many bin entries */
+  uint32_t bin_chunk;        /* slots per binning warp, power of two >= 256 */
+  uint32_t bin_capacity;     /* initial bin entries */
+  uint32_t frag_chunks;      /* initial fragment chunks (16 quads each) */
+  uint32_t shade_quads_per_warp; /* 8 (4 lanes per quad) */
+  uint32_t shade_ctas_per_sm;
+  uint32_t merge_ctas_per_sm;
+} sg_tuning;
+int32_t sg_get_tuning(sg_device* dev, sg_tuning* out);
+int32_t sg_set_tuning(sg_device* dev, const sg_tuning* tuning);
+/* Times the command list under candidate tunings (CUDA events on the
+ * device's stream, `reps` runs each after one warm-up) and keeps the fastest
+ * in the device; `out` receives it and `best_ms` its time (either may be
+ * NULL).  The targets hold the last run's results, identical for every
+ * candidate. */
+int32_t sg_autotune(sg_device* dev, const sg_command* cmds, uint32_t n, uint32_t reps, sg_tuning* out,
+                    float* best_ms);
 
 /* renderer::clear_color (renderer.h:124). */
 int32_t sg_clear_color(sg_device* dev, uint32_t texture, const float rgba[4]);

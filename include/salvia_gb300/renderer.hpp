@@ -1,0 +1,900 @@
+// renderer.hpp -- C++ renderer facade over the salvia_gb300.h C ABI.
+//
+// Apps written against Salvia's renderer interface
+// (salvia/include/salvia/core/renderer.h:42-147) keep their structure when
+// they include this header instead: the same class names in the same
+// namespaces (salvia::core, salvia::resource), the same factories
+// (create_benchmark_renderer / create_software_renderer), the same state
+// objects (raster_state, depth_stencil_state, sampler, input_layout,
+// viewport), the same draw / draw_index / clear / flush / query calls and
+// the same `result` codes.  Everything forwards to the C ABI, so this header
+// needs no CUDA headers and works with any library that exports the ABI
+// (the GPU library, or the CPU oracle used by the tests).
+//
+// The one structural difference is the shaders.  The reference runs the
+// virtual `shader_prog` of user C++ classes on the CPU (shader.h:159-215);
+// device kernels cannot call host virtuals, so here a cpp_vertex_shader /
+// cpp_pixel_shader / cpp_blend_shader names a compiled device program
+// (`program()`) and carries its constants and samplers, declared exactly as
+// the reference's cpp_shader_impl does (declare_constant, declare_sampler,
+// bind_semantic, set_constant, set_sampler).  Stock classes cover the
+// programs the library ships: the MVP vertex shader, colour / constant /
+// texture pixel shaders and the replace / src-alpha / additive blends.
+//
+// Header-only, C++17.  Link with libsalvia_gb300.so.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "../salvia_gb300.h"
+
+namespace salvia {
+
+// salvia/include/salvia/common/constants.h:9, plus the two codes the GPU adds
+enum class result : uint32_t { ok, failed, out_of_memory, invalid_parameter, timeout, cuda_error };
+
+enum map_mode {
+  map_mode_none = 0, map_read = 1, map_write = 2, map_read_write = 3, map_write_discard = 4,
+  map_write_no_overwrite = 5
+};
+enum primitive_topology { primitive_triangle_list = 2, primitive_triangle_strip = 4 };
+enum cull_mode { cull_none = 0, cull_front = 1, cull_back = 2 };
+enum fill_mode { fill_wireframe = 0, fill_solid = 1 };
+enum address_mode { address_wrap = 0, address_mirror = 1, address_clamp = 2, address_border = 3 };
+enum filter_type { filter_point = 0, filter_linear = 1, filter_anisotropic = 2 };
+enum mip_quality { mip_lo_quality = 0, mip_mi_quality = 1, mip_hi_quality = 2 };
+enum compare_function {
+  compare_function_never = 0, compare_function_less = 1, compare_function_equal = 2,
+  compare_function_less_equal = 3, compare_function_greater = 4, compare_function_not_equal = 5,
+  compare_function_greater_equal = 6, compare_function_always = 7
+};
+enum stencil_op {
+  stencil_op_keep = 1, stencil_op_zero = 2, stencil_op_replace = 3, stencil_op_incr_sat = 4,
+  stencil_op_decr_sat = 5, stencil_op_invert = 6, stencil_op_incr_wrap = 7, stencil_op_decr_wrap = 8
+};
+enum clear_flag { clear_depth = 0x1, clear_stencil = 0x2 };
+enum class async_object_ids : uint32_t {
+  none, event, occlusion, pipeline_statistics, occlusion_predicate, internal_statistics, pipeline_profiles, count
+};
+enum class async_status : uint32_t { error, timeout, ready };
+
+// pixel formats (colors_convertors.h:39-45) and the GPU's three extensions
+enum pixel_format {
+  pixel_format_color_rgba32f = 0, pixel_format_color_rgb32f = 1, pixel_format_color_bgra8 = 2,
+  pixel_format_color_rgba8 = 3, pixel_format_color_r32f = 4, pixel_format_color_rg32f = 5,
+  pixel_format_color_r32i = 6,
+  pixel_format_color_rgba16f = SG_FMT_RGBA16F, pixel_format_depth_d32f = SG_FMT_D32F,
+  pixel_format_depth_d24s8 = SG_FMT_D24S8
+};
+// vertex / index formats (salvia/include/salvia/common/format.h)
+enum format {
+  format_unknown = 0, format_r32g32b32a32_float = 2, format_r32g32b32a32_sint = 4, format_r32g32b32_float = 6,
+  format_r32g32_float = 16, format_r32_float = 41, format_r32_uint = 42, format_r16_uint = 57
+};
+
+inline result to_result(int32_t s) { return static_cast<result>(s); }
+
+}  // namespace salvia
+
+namespace salvia::core {
+
+struct vec4 {
+  float x = 0, y = 0, z = 0, w = 0;
+};
+struct mat44 {  // row-major, m[r][c]; vertices are row vectors (clip = v x M)
+  float m[4][4] = {};
+  static mat44 identity() {
+    mat44 r;
+    for (int i = 0; i < 4; ++i) r.m[i][i] = 1.0f;
+    return r;
+  }
+};
+struct color_rgba32f {
+  float r = 0, g = 0, b = 0, a = 0;
+  color_rgba32f() = default;
+  color_rgba32f(float r_, float g_, float b_, float a_) : r(r_), g(g_), b(b_), a(a_) {}
+};
+
+struct viewport {  // salvia/include/salvia/core/viewport.h
+  float x, y, w, h, minz, maxz;
+};
+
+namespace detail {
+// Owns the C-ABI device; shared by the renderer and every resource it made,
+// so a resource never outlives the device its handle belongs to.
+struct device_ref {
+  sg_device* dev = nullptr;
+  explicit device_ref(sg_device* d) : dev(d) {}
+  ~device_ref() {
+    if (dev) sg_device_destroy(dev);
+  }
+  device_ref(device_ref const&) = delete;
+  device_ref& operator=(device_ref const&) = delete;
+};
+using device_sp = std::shared_ptr<device_ref>;
+}  // namespace detail
+
+}  // namespace salvia::core
+
+namespace salvia::resource {
+
+using salvia::core::color_rgba32f;
+
+// A device buffer (buffer.h).  map/unmap go through a host copy.
+class buffer {
+public:
+  buffer(core::detail::device_sp d, uint32_t h, size_t size) : dev_(std::move(d)), handle_(h), size_(size) {}
+  ~buffer() {
+    if (handle_) sg_buffer_destroy(dev_->dev, handle_);
+  }
+  size_t size() const { return size_; }
+  uint32_t handle() const { return handle_; }
+  // buffer::transfer: copies host bytes into the buffer at `offset`.
+  result transfer(size_t offset, void const* src, size_t sz) {
+    return to_result(sg_buffer_upload(dev_->dev, handle_, offset, src, sz));
+  }
+  result read(size_t offset, void* dst, size_t sz) const {
+    return to_result(sg_buffer_download(dev_->dev, handle_, offset, dst, sz));
+  }
+
+private:
+  core::detail::device_sp dev_;
+  uint32_t handle_;
+  size_t size_;
+};
+using buffer_ptr = std::shared_ptr<buffer>;
+
+class texture;
+// One mip level of a texture (surface.h); render targets name level 0.
+class surface {
+public:
+  surface(std::shared_ptr<texture> const& tex, uint32_t level) : tex_(tex), level_(level) {}
+  std::shared_ptr<texture> get_texture() const { return tex_.lock(); }
+  uint32_t level() const { return level_; }
+  size_t width() const;
+  size_t height() const;
+  size_t sample_count() const;
+  pixel_format get_pixel_format() const;
+  // Raw texels, layout ((y * w + x) * samples + s) * elem (surface.cpp:277-295).
+  result read(std::vector<uint8_t>& out) const;
+  result write(void const* data, size_t size);
+  // surface::resolve (surface.cpp:123-140): box average of the samples into `target`.
+  result resolve(surface& target);
+
+private:
+  std::weak_ptr<texture> tex_;
+  uint32_t level_;
+};
+using surface_ptr = std::shared_ptr<surface>;
+
+class texture : public std::enable_shared_from_this<texture> {
+public:
+  texture(core::detail::device_sp d, uint32_t h) : dev_(std::move(d)), handle_(h) {}
+  ~texture() {
+    if (handle_) sg_texture_destroy(dev_->dev, handle_);
+  }
+  uint32_t handle() const { return handle_; }
+  sg_device* device() const { return dev_->dev; }
+  uint32_t levels() const {
+    uint32_t n = 0;
+    sg_texture_info(dev_->dev, handle_, 0, nullptr, nullptr, nullptr, nullptr, &n);
+    return n;
+  }
+  // texture::subresource (texture.h:17-80)
+  surface_ptr subresource(size_t level) {
+    if (level >= levels()) return nullptr;
+    auto it = surfaces_.find(level);
+    if (it != surfaces_.end()) return it->second;
+    auto s = std::make_shared<surface>(shared_from_this(), static_cast<uint32_t>(level));
+    surfaces_[level] = s;
+    return s;
+  }
+  // texture::gen_mipmap(filter, auto_gen) (texture2d.cpp:25-36)
+  result gen_mipmap(filter_type filter, bool /*auto_gen*/) {
+    surfaces_.clear();
+    return to_result(sg_texture_gen_mipmap(dev_->dev, handle_, static_cast<uint32_t>(filter)));
+  }
+  size_t width(size_t level = 0) const { return info(level, 0); }
+  size_t height(size_t level = 0) const { return info(level, 1); }
+  size_t sample_count() const { return info(0, 2); }
+  pixel_format get_pixel_format() const { return static_cast<pixel_format>(info(0, 3)); }
+
+private:
+  size_t info(size_t level, int what) const {
+    uint32_t v[4] = {0, 0, 0, 0};
+    sg_texture_info(dev_->dev, handle_, static_cast<uint32_t>(level), &v[0], &v[1], &v[2], &v[3], nullptr);
+    return v[what];
+  }
+  core::detail::device_sp dev_;
+  uint32_t handle_;
+  std::map<size_t, surface_ptr> surfaces_;
+};
+using texture_ptr = std::shared_ptr<texture>;
+
+inline size_t surface::width() const { return tex_.lock()->width(level_); }
+inline size_t surface::height() const { return tex_.lock()->height(level_); }
+inline size_t surface::sample_count() const { return tex_.lock()->sample_count(); }
+inline pixel_format surface::get_pixel_format() const { return tex_.lock()->get_pixel_format(); }
+inline result surface::read(std::vector<uint8_t>& out) const {
+  auto t = tex_.lock();
+  if (!t) return result::failed;
+  uint32_t w = 0, h = 0, s = 0, f = 0;
+  sg_texture_info(t->device(), t->handle(), level_, &w, &h, &s, &f, nullptr);
+  size_t esz = f == SG_FMT_RGBA32F ? 16 : f == SG_FMT_RGB32F ? 12 : (f == SG_FMT_RG32F || f == SG_FMT_RGBA16F) ? 8 : 4;
+  out.resize(static_cast<size_t>(w) * h * s * esz);
+  return to_result(sg_texture_download(t->device(), t->handle(), level_, out.data(), out.size()));
+}
+inline result surface::write(void const* data, size_t size) {
+  auto t = tex_.lock();
+  if (!t) return result::failed;
+  return to_result(sg_texture_upload(t->device(), t->handle(), level_, data, size));
+}
+inline result surface::resolve(surface& target) {
+  auto a = tex_.lock();
+  auto b = target.tex_.lock();
+  if (!a || !b || level_ != 0 || target.level_ != 0) return result::invalid_parameter;
+  return to_result(sg_resolve(a->device(), a->handle(), b->handle()));
+}
+
+// sampler_desc (sampler.h:16-45)
+struct sampler_desc {
+  filter_type min_filter = filter_point;
+  filter_type mag_filter = filter_point;
+  filter_type mip_filter = filter_point;
+  mip_quality mip_qual = mip_mi_quality;
+  address_mode addr_mode_u = address_wrap;
+  address_mode addr_mode_v = address_wrap;
+  address_mode addr_mode_w = address_wrap;
+  float mip_lod_bias = 0;
+  uint32_t max_anisotropy = 0;
+  compare_function comparison_func = compare_function_always;
+  color_rgba32f border_color{0, 0, 0, 0};
+  float min_lod = -1e20f;
+  float max_lod = 1e20f;
+};
+
+class sampler {
+public:
+  sampler(core::detail::device_sp d, uint32_t h, sampler_desc const& desc, texture_ptr tex)
+      : dev_(std::move(d)), handle_(h), desc_(desc), tex_(std::move(tex)) {}
+  ~sampler() {
+    if (handle_) sg_sampler_destroy(dev_->dev, handle_);
+  }
+  uint32_t handle() const { return handle_; }
+  sampler_desc const& get_desc() const { return desc_; }
+  texture_ptr const& get_texture() const { return tex_; }
+
+private:
+  core::detail::device_sp dev_;
+  uint32_t handle_;
+  sampler_desc desc_;
+  texture_ptr tex_;
+};
+using sampler_ptr = std::shared_ptr<sampler>;
+
+enum input_classifications { input_per_vertex };
+
+// input_element_desc (input_layout.h:20-47)
+struct input_element_desc {
+  std::string semantic_name;
+  uint32_t semantic_index = 0;
+  format data_format = format_unknown;
+  uint32_t input_slot = 0;
+  uint32_t aligned_byte_offset = 0xFFFFFFFFu;
+  input_classifications slot_class = input_per_vertex;
+  uint32_t instance_data_step_rate = 0;
+  input_element_desc() = default;
+  input_element_desc(char const* name, uint32_t index, format fmt, uint32_t slot, uint32_t offset,
+                     input_classifications cls, uint32_t step)
+      : semantic_name(name), semantic_index(index), data_format(fmt), input_slot(slot),
+        aligned_byte_offset(offset), slot_class(cls), instance_data_step_rate(step) {}
+};
+
+// The elements bound to vertex-shader input registers (renderer::create_input_layout
+// with a cpp_vertex_shader, renderer_impl.cpp; stream_assembler.cpp:26-93).
+class input_layout {
+public:
+  std::vector<sg_vs_input> registers;
+};
+using input_layout_ptr = std::shared_ptr<input_layout>;
+
+}  // namespace salvia::resource
+
+namespace salvia::core {
+
+using resource::buffer_ptr;
+using resource::input_element_desc;
+using resource::input_layout_ptr;
+using resource::sampler_desc;
+using resource::sampler_ptr;
+using resource::surface_ptr;
+using resource::texture_ptr;
+
+// raster_desc / raster_state (raster_state.h:17-68)
+struct raster_desc {
+  fill_mode fm = fill_solid;
+  cull_mode cm = cull_back;
+  bool front_ccw = false;
+  int32_t depth_bias = 0;
+  float depth_bias_clamp = 0;
+  float slope_scaled_depth_bias = 0;
+  bool depth_clip_enable = true;
+  bool scissor_enable = false;
+  bool multisample_enable = true;
+  bool anti_aliased_line_enable = false;
+};
+class raster_state {
+public:
+  explicit raster_state(raster_desc const& d) : desc_(d) {}
+  raster_desc const& get_desc() const { return desc_; }
+
+private:
+  raster_desc desc_;
+};
+using raster_state_ptr = std::shared_ptr<raster_state>;
+
+// depth_stencil_desc / depth_stencil_state (framebuffer.h:20-77)
+struct depth_stencil_op_desc {
+  stencil_op stencil_fail_op = stencil_op_keep;
+  stencil_op stencil_depth_fail_op = stencil_op_keep;
+  stencil_op stencil_pass_op = stencil_op_keep;
+  compare_function stencil_func = compare_function_always;
+};
+struct depth_stencil_desc {
+  bool depth_enable = true;
+  bool depth_write_mask = true;
+  compare_function depth_func = compare_function_less;
+  bool stencil_enable = false;
+  uint8_t stencil_read_mask = 0xFF;
+  uint8_t stencil_write_mask = 0xFF;
+  depth_stencil_op_desc front_face;
+  depth_stencil_op_desc back_face;
+};
+class depth_stencil_state {
+public:
+  explicit depth_stencil_state(depth_stencil_desc const& d) : desc_(d) {}
+  depth_stencil_desc const& get_desc() const { return desc_; }
+
+private:
+  depth_stencil_desc desc_;
+};
+using depth_stencil_state_ptr = std::shared_ptr<depth_stencil_state>;
+
+// ---- shaders ------------------------------------------------------------
+namespace am {  // vs_output::attrib_modifier_type (shader_regs.h:49-55)
+enum { am_linear = SG_AM_LINEAR, am_centroid = SG_AM_CENTROID, am_nointerpolation = SG_AM_NOINTERPOLATION,
+       am_noperspective = SG_AM_NOPERSPECTIVE, am_sample = SG_AM_SAMPLE };
+}
+
+class cpp_shader;
+using cpp_shader_ptr = std::shared_ptr<cpp_shader>;
+
+class cpp_shader {
+public:
+  virtual ~cpp_shader() = default;
+  virtual result set_sampler(std::string const& name, sampler_ptr const& samp) = 0;
+  virtual result set_constant(std::string const& name, void const* pval) = 0;
+  virtual cpp_shader_ptr clone() = 0;
+  // The device program this shader runs (SG_VS_* / SG_PS_* / SG_BS_*).
+  virtual uint32_t program() const = 0;
+};
+
+// cpp_shader_impl (shader.h:86-157): named constants and samplers, and the
+// semantic -> input-register map of a vertex shader.  Constants are packed,
+// in declaration order, into the program's float constant block; samplers,
+// in declaration order, into its sampler slots.
+class cpp_shader_impl : public cpp_shader {
+public:
+  result set_sampler(std::string const& name, sampler_ptr const& samp) override {
+    for (auto& s : samplers_)
+      if (s.first == name) {
+        *s.second = samp;
+        return result::ok;
+      }
+    return result::failed;
+  }
+  result set_constant(std::string const& name, void const* pval) override {
+    for (auto& c : constants_)
+      if (c.name == name) {
+        std::memcpy(c.ptr, pval, c.size);
+        return result::ok;
+      }
+    return result::failed;
+  }
+  template <class T>
+  result declare_constant(std::string const& name, T& var) {
+    static_assert(sizeof(T) % 4 == 0, "shader constants are packed as 32-bit words");
+    constants_.push_back({name, &var, sizeof(T)});
+    return result::ok;
+  }
+  result declare_sampler(std::string const& name, sampler_ptr& var) {
+    samplers_.push_back({name, &var});
+    return result::ok;
+  }
+  void bind_semantic(char const* name, size_t semantic_index, size_t register_index) {
+    regs_[std::string(name) + "#" + std::to_string(semantic_index)] = register_index;
+  }
+  result find_register(char const* name, size_t semantic_index, size_t& index) const {
+    auto it = regs_.find(std::string(name) + "#" + std::to_string(semantic_index));
+    if (it == regs_.end()) return result::failed;
+    index = it->second;
+    return result::ok;
+  }
+  // Fills `s` with the program, constants and samplers of this shader.
+  result pack(sg_shader& s) const {
+    std::memset(&s, 0, sizeof(s));
+    s.program = program();
+    size_t off = 0;
+    for (auto const& c : constants_) {
+      size_t n = c.size / 4;
+      if (off + n > SG_MAX_SHADER_CONSTANTS) return result::invalid_parameter;
+      std::memcpy(&s.constants[off], c.ptr, c.size);
+      off += n;
+    }
+    if (samplers_.size() > SG_MAX_SHADER_SAMPLERS) return result::invalid_parameter;
+    for (size_t i = 0; i < samplers_.size(); ++i) s.samplers[i] = *samplers_[i].second ? (*samplers_[i].second)->handle() : 0;
+    return result::ok;
+  }
+  std::unordered_map<std::string, size_t> const& register_map() const { return regs_; }
+
+  cpp_shader_impl() = default;
+  // Copies re-point the declared constants and samplers at the copy's members
+  // (the offsets of the declared members within the object are kept).
+  cpp_shader_impl(cpp_shader_impl const& o) : regs_(o.regs_) { rebase(o); }
+  cpp_shader_impl& operator=(cpp_shader_impl const& o) {
+    regs_ = o.regs_;
+    rebase(o);
+    return *this;
+  }
+
+private:
+  struct constant {
+    std::string name;
+    void* ptr;
+    size_t size;
+  };
+  void rebase(cpp_shader_impl const& o) {
+    auto const* ob = reinterpret_cast<char const*>(&o);
+    auto* nb = reinterpret_cast<char*>(this);
+    constants_.clear();
+    samplers_.clear();
+    for (auto const& c : o.constants_)
+      constants_.push_back({c.name, nb + (static_cast<char const*>(c.ptr) - ob), c.size});
+    for (auto const& s : o.samplers_)
+      samplers_.push_back({s.first, reinterpret_cast<sampler_ptr*>(nb + (reinterpret_cast<char const*>(s.second) - ob))});
+  }
+  std::vector<constant> constants_;
+  std::vector<std::pair<std::string, sampler_ptr*>> samplers_;
+  std::unordered_map<std::string, size_t> regs_;
+};
+
+// cpp_vertex_shader (shader.h:159-165)
+class cpp_vertex_shader : public cpp_shader_impl {
+public:
+  virtual uint32_t num_output_attributes() const = 0;
+  virtual uint32_t output_attribute_modifiers(uint32_t index) const = 0;
+};
+// cpp_pixel_shader (shader.h:169-205)
+class cpp_pixel_shader : public cpp_shader_impl {};
+// cpp_blend_shader (shader.h:209-215)
+class cpp_blend_shader : public cpp_shader_impl {};
+
+using cpp_vertex_shader_ptr = std::shared_ptr<cpp_vertex_shader>;
+using cpp_pixel_shader_ptr = std::shared_ptr<cpp_pixel_shader>;
+using cpp_blend_shader_ptr = std::shared_ptr<cpp_blend_shader>;
+
+#define SALVIA_GB300_CLONE(cls) \
+  cpp_shader_ptr clone() override { return cpp_shader_ptr(new cls(*this)); }
+
+// ---- stock shaders: the device programs the library ships ---------------
+// out.position = transform(in[0], WorldViewProjMat); out.attr[i] = in[i + 1].
+class transform_vertex_shader : public cpp_vertex_shader {
+public:
+  explicit transform_vertex_shader(uint32_t num_attributes, mat44 const& m = mat44::identity(),
+                                   uint32_t modifiers = am::am_linear)
+      : wvp_(m), nattr_(num_attributes), mods_(modifiers) {
+    declare_constant("WorldViewProjMat", wvp_);
+  }
+  uint32_t program() const override { return SG_VS_TRANSFORM; }
+  uint32_t num_output_attributes() const override { return nattr_; }
+  uint32_t output_attribute_modifiers(uint32_t) const override { return mods_; }
+  SALVIA_GB300_CLONE(transform_vertex_shader)
+
+private:
+  mat44 wvp_;
+  uint32_t nattr_, mods_;
+};
+// out.color[0] = in.attr[0]
+class color_pixel_shader : public cpp_pixel_shader {
+public:
+  uint32_t program() const override { return SG_PS_COLOR; }
+  SALVIA_GB300_CLONE(color_pixel_shader)
+};
+// out.color[0] = Color
+class constant_pixel_shader : public cpp_pixel_shader {
+public:
+  explicit constant_pixel_shader(vec4 const& c = vec4{}) : color_(c) { declare_constant("Color", color_); }
+  uint32_t program() const override { return SG_PS_CONSTANT; }
+  SALVIA_GB300_CLONE(constant_pixel_shader)
+
+private:
+  vec4 color_;
+};
+// out.color[0] = tex2d(Sampler, 0) * in.attr[1]
+class texture_pixel_shader : public cpp_pixel_shader {
+public:
+  explicit texture_pixel_shader(sampler_ptr const& s = nullptr) : samp_(s) { declare_sampler("Sampler", samp_); }
+  uint32_t program() const override { return SG_PS_TEX_MODULATE; }
+  SALVIA_GB300_CLONE(texture_pixel_shader)
+
+private:
+  sampler_ptr samp_;
+};
+// out.color[0] = Sampler.sample_2d_grad(in.attr[0].xy, ddx(0), ddy(0), 0) * in.attr[1]
+class texture_grad_pixel_shader : public cpp_pixel_shader {
+public:
+  explicit texture_grad_pixel_shader(sampler_ptr const& s = nullptr) : samp_(s) { declare_sampler("Sampler", samp_); }
+  uint32_t program() const override { return SG_PS_TEX_GRAD_MODULATE; }
+  SALVIA_GB300_CLONE(texture_grad_pixel_shader)
+
+private:
+  sampler_ptr samp_;
+};
+class replace_blend_shader : public cpp_blend_shader {  // color(0, s) = src
+public:
+  uint32_t program() const override { return SG_BS_REPLACE; }
+  SALVIA_GB300_CLONE(replace_blend_shader)
+};
+class src_alpha_blend_shader : public cpp_blend_shader {  // lerp(dst, src, src.a)
+public:
+  uint32_t program() const override { return SG_BS_LERP_SRC_ALPHA; }
+  SALVIA_GB300_CLONE(src_alpha_blend_shader)
+};
+class additive_blend_shader : public cpp_blend_shader {  // dst + src
+public:
+  uint32_t program() const override { return SG_BS_ADD; }
+  SALVIA_GB300_CLONE(additive_blend_shader)
+};
+
+// ---- queries (async_object.h:90-233) ------------------------------------
+struct pipeline_statistics {
+  uint64_t ia_vertices, ia_primitives, vs_invocations, gs_invocations, gs_primitives, cinvocations, cprimitives,
+      ps_invocations;
+};
+struct internal_statistics {
+  uint64_t backend_input_pixels;
+};
+class async_object {
+public:
+  explicit async_object(async_object_ids id) : id_(id) {}
+  async_object_ids id() const { return id_; }
+  bool running = false;
+  pipeline_statistics stats{};
+  internal_statistics internal{};
+
+private:
+  async_object_ids id_;
+};
+using async_object_ptr = std::shared_ptr<async_object>;
+
+struct mapped_resource {
+  void* data = nullptr;
+  size_t row_pitch = 0, depth_pitch = 0;
+};
+
+// ---- the renderer (renderer.h:42-131) -----------------------------------
+class renderer {
+public:
+  explicit renderer(sg_device* d) : dev_(std::make_shared<detail::device_ref>(d)) {
+    vp_ = viewport{0, 0, 0, 0, 0, 1};
+    rs_ = std::make_shared<raster_state>(raster_desc{});
+    dss_ = std::make_shared<depth_stencil_state>(depth_stencil_desc{});
+  }
+  sg_device* native() const { return dev_->dev; }
+  char const* last_error() const { return sg_last_error(dev_->dev); }
+
+  // creators
+  buffer_ptr create_buffer(size_t size) {
+    uint32_t h = 0;
+    if (sg_buffer_create(dev_->dev, size, &h) != SG_OK) return nullptr;
+    return std::make_shared<resource::buffer>(dev_, h, size);
+  }
+  texture_ptr create_tex2d(size_t width, size_t height, size_t num_samples, pixel_format fmt) {
+    uint32_t h = 0;
+    if (sg_texture_create(dev_->dev, static_cast<uint32_t>(width), static_cast<uint32_t>(height),
+                          static_cast<uint32_t>(num_samples), static_cast<uint32_t>(fmt), &h) != SG_OK)
+      return nullptr;
+    return std::make_shared<resource::texture>(dev_, h);
+  }
+  sampler_ptr create_sampler(sampler_desc const& desc, texture_ptr const& tex) {
+    if (!tex) return nullptr;
+    sg_sampler_desc d{};
+    d.min_filter = desc.min_filter;
+    d.mag_filter = desc.mag_filter;
+    d.mip_filter = desc.mip_filter;
+    d.mip_quality = desc.mip_qual;
+    d.address_u = desc.addr_mode_u;
+    d.address_v = desc.addr_mode_v;
+    d.address_w = desc.addr_mode_w;
+    d.max_anisotropy = desc.max_anisotropy;
+    d.lod_bias = desc.mip_lod_bias;
+    d.border_color[0] = desc.border_color.r;
+    d.border_color[1] = desc.border_color.g;
+    d.border_color[2] = desc.border_color.b;
+    d.border_color[3] = desc.border_color.a;
+    d.min_lod = desc.min_lod;
+    d.max_lod = desc.max_lod;
+    uint32_t h = 0;
+    if (sg_sampler_create(dev_->dev, &d, tex->handle(), &h) != SG_OK) return nullptr;
+    return std::make_shared<resource::sampler>(dev_, h, desc, tex);
+  }
+  async_object_ptr create_query(async_object_ids id) {
+    if (id != async_object_ids::pipeline_statistics && id != async_object_ids::internal_statistics) return nullptr;
+    return std::make_shared<async_object>(id);
+  }
+  // Binds the elements to the shader's input registers by semantic
+  // (renderer::create_input_layout(descs, n, cpp_vertex_shader_ptr)).
+  input_layout_ptr create_input_layout(input_element_desc const* descs, size_t count, cpp_vertex_shader_ptr const& vs) {
+    if (!vs) return nullptr;
+    auto il = std::make_shared<resource::input_layout>();
+    for (size_t i = 0; i < count; ++i) {
+      size_t reg = 0;
+      if (vs->find_register(descs[i].semantic_name.c_str(), descs[i].semantic_index, reg) != result::ok) continue;
+      if (reg >= SG_MAX_VS_INPUTS) return nullptr;
+      if (il->registers.size() <= reg) il->registers.resize(reg + 1, sg_vs_input{SG_SEMANTIC_TEXCOORD, 0,
+                                                                                  SG_VFMT_R32G32B32A32_FLOAT, 0, 0});
+      sg_vs_input& r = il->registers[reg];
+      std::string const& n = descs[i].semantic_name;
+      r.semantic = n == "POSITION" || n == "SV_Position" ? SG_SEMANTIC_POSITION
+                   : n == "COLOR" ? SG_SEMANTIC_COLOR : n == "NORMAL" ? SG_SEMANTIC_NORMAL : SG_SEMANTIC_TEXCOORD;
+      r.semantic_index = descs[i].semantic_index;
+      r.format = descs[i].data_format;
+      r.slot = descs[i].input_slot;
+      r.offset = descs[i].aligned_byte_offset == 0xFFFFFFFFu ? 0 : descs[i].aligned_byte_offset;
+    }
+    return il;
+  }
+
+  // map / unmap (renderer.h:61-63): a host copy, written back on unmap.
+  result map(mapped_resource& mr, buffer_ptr const& buf, map_mode mm) {
+    if (!buf || mapped_buf_) return result::failed;
+    shadow_.assign(buf->size(), 0);
+    if (mm == map_read || mm == map_read_write || mm == map_write_no_overwrite)
+      if (buf->read(0, shadow_.data(), shadow_.size()) != result::ok) return result::failed;
+    mapped_buf_ = buf;
+    mapped_mode_ = mm;
+    mr.data = shadow_.data();
+    mr.row_pitch = mr.depth_pitch = buf->size();
+    return result::ok;
+  }
+  result unmap() {
+    if (!mapped_buf_) return result::failed;
+    result r = result::ok;
+    if (mapped_mode_ != map_read) r = mapped_buf_->transfer(0, shadow_.data(), shadow_.size());
+    mapped_buf_.reset();
+    return r;
+  }
+
+  // state set
+  result set_vertex_buffers(size_t start_slot, size_t count, buffer_ptr const* buffers, size_t const* strides,
+                            size_t const* offsets) {
+    if (start_slot + count > SG_MAX_STREAMS) return result::invalid_parameter;
+    for (size_t i = 0; i < count; ++i) {
+      streams_[start_slot + i] = buffers[i];
+      strides_[start_slot + i] = strides[i];
+      offsets_[start_slot + i] = offsets[i];
+    }
+    return result::ok;
+  }
+  result set_index_buffer(buffer_ptr const& b, format fmt) {
+    if (fmt != format_r16_uint && fmt != format_r32_uint) return result::invalid_parameter;
+    ib_ = b;
+    ib_fmt_ = fmt;
+    return result::ok;
+  }
+  result set_input_layout(input_layout_ptr const& l) {
+    layout_ = l;
+    return result::ok;
+  }
+  result set_vertex_shader(cpp_vertex_shader_ptr const& vs) {
+    vs_ = vs;
+    return result::ok;
+  }
+  result set_pixel_shader(cpp_pixel_shader_ptr const& ps) {
+    ps_ = ps;
+    return result::ok;
+  }
+  result set_blend_shader(cpp_blend_shader_ptr const& bs) {
+    bs_ = bs;
+    return result::ok;
+  }
+  result set_primitive_topology(primitive_topology t) {
+    topo_ = t;
+    return result::ok;
+  }
+  result set_rasterizer_state(raster_state_ptr const& rs) {
+    rs_ = rs ? rs : std::make_shared<raster_state>(raster_desc{});
+    return result::ok;
+  }
+  result set_depth_stencil_state(depth_stencil_state_ptr const& dss, int32_t stencil_ref) {
+    dss_ = dss ? dss : std::make_shared<depth_stencil_state>(depth_stencil_desc{});
+    stencil_ref_ = stencil_ref;
+    return result::ok;
+  }
+  result set_render_targets(size_t color_count, surface_ptr const* colors, surface_ptr const& ds) {
+    if (color_count > 1) return result::failed;  // one colour target, as the blend programs write target 0
+    color_ = color_count ? colors[0] : nullptr;
+    ds_ = ds;
+    return result::ok;
+  }
+  result set_viewport(viewport const& vp) {
+    vp_ = vp;
+    return result::ok;
+  }
+
+  // state get
+  buffer_ptr get_index_buffer() const { return ib_; }
+  format get_index_format() const { return ib_fmt_; }
+  primitive_topology get_primitive_topology() const { return topo_; }
+  cpp_vertex_shader_ptr get_vertex_shader() const { return vs_; }
+  raster_state_ptr get_rasterizer_state() const { return rs_; }
+  cpp_pixel_shader_ptr get_pixel_shader() const { return ps_; }
+  cpp_blend_shader_ptr get_blend_shader() const { return bs_; }
+  viewport get_viewport() const { return vp_; }
+
+  // queries
+  result begin(async_object_ptr const& q) {
+    if (!q || q->running) return result::failed;
+    q->running = true;
+    q->stats = pipeline_statistics{};
+    q->internal = internal_statistics{};
+    queries_.push_back(q);
+    return result::ok;
+  }
+  result end(async_object_ptr const& q) {
+    if (!q || !q->running) return result::failed;
+    q->running = false;
+    for (size_t i = 0; i < queries_.size(); ++i)
+      if (queries_[i] == q) {
+        queries_.erase(queries_.begin() + static_cast<long>(i));
+        break;
+      }
+    return result::ok;
+  }
+  async_status get_data(async_object_ptr const& q, void* data, bool /*do_not_wait*/) {
+    if (!q || q->running) return async_status::error;
+    if (sg_sync(dev_->dev) != SG_OK) return async_status::error;
+    if (q->id() == async_object_ids::pipeline_statistics)
+      std::memcpy(data, &q->stats, sizeof(q->stats));
+    else
+      std::memcpy(data, &q->internal, sizeof(q->internal));
+    return async_status::ready;
+  }
+
+  // render operations
+  result draw(size_t startpos, size_t primcnt) { return submit(false, startpos, primcnt, 0); }
+  result draw_index(size_t startpos, size_t primcnt, int basevert) { return submit(true, startpos, primcnt, basevert); }
+  result clear_color(surface_ptr const& s, color_rgba32f const& c) {
+    if (!s || s->level() != 0) return result::invalid_parameter;
+    float rgba[4] = {c.r, c.g, c.b, c.a};
+    return to_result(sg_clear_color(dev_->dev, s->get_texture()->handle(), rgba));
+  }
+  result clear_depth_stencil(surface_ptr const& s, uint32_t flags, float d, uint32_t st) {
+    if (!s || s->level() != 0) return result::invalid_parameter;
+    return to_result(sg_clear_depth_stencil(dev_->dev, s->get_texture()->handle(), flags, d, st));
+  }
+  result flush() { return to_result(sg_sync(dev_->dev)); }
+
+  // The C-ABI descriptor of a draw under the current state.
+  result build_desc(bool indexed, size_t startpos, size_t primcnt, int basevert, sg_draw_desc& d) const {
+    std::memset(&d, 0, sizeof(d));
+    if (!vs_ || !ps_ || !bs_ || !layout_) return result::failed;
+    d.color_target = color_ ? color_->get_texture()->handle() : 0;
+    d.ds_target = ds_ ? ds_->get_texture()->handle() : 0;
+    d.viewport = sg_viewport{vp_.x, vp_.y, vp_.w, vp_.h, vp_.minz, vp_.maxz};
+    d.topology = topo_;
+    d.indexed = indexed ? 1u : 0u;
+    if (indexed) {
+      if (!ib_) return result::failed;
+      d.index_buffer = ib_->handle();
+      d.index_format = ib_fmt_ == format_r16_uint ? SG_INDEX_U16 : SG_INDEX_U32;
+    }
+    d.start = static_cast<uint32_t>(startpos);
+    d.prim_count = static_cast<uint32_t>(primcnt);
+    d.base_vertex = basevert;
+    uint32_t nstreams = 0;
+    for (uint32_t i = 0; i < SG_MAX_STREAMS; ++i)
+      if (streams_[i]) nstreams = i + 1;
+    d.num_streams = nstreams;
+    for (uint32_t i = 0; i < nstreams; ++i) {
+      if (!streams_[i]) return result::failed;
+      d.streams[i] = sg_vertex_stream{streams_[i]->handle(), static_cast<uint32_t>(strides_[i]),
+                                      static_cast<uint32_t>(offsets_[i])};
+    }
+    d.num_inputs = static_cast<uint32_t>(layout_->registers.size());
+    for (uint32_t i = 0; i < d.num_inputs; ++i) d.inputs[i] = layout_->registers[i];
+    d.num_varyings = vs_->num_output_attributes();
+    if (d.num_varyings > SG_MAX_VARYINGS) return result::invalid_parameter;
+    for (uint32_t i = 0; i < d.num_varyings; ++i) d.varying_modifiers[i] = vs_->output_attribute_modifiers(i);
+    raster_desc const& r = rs_->get_desc();
+    d.raster = sg_raster_desc{static_cast<uint32_t>(r.fm), static_cast<uint32_t>(r.cm), r.front_ccw ? 1u : 0u, 0u};
+    depth_stencil_desc const& s = dss_->get_desc();
+    d.depth_stencil.depth_enable = s.depth_enable;
+    d.depth_stencil.depth_write = s.depth_write_mask;
+    d.depth_stencil.depth_func = s.depth_func;
+    d.depth_stencil.stencil_enable = s.stencil_enable;
+    d.depth_stencil.stencil_read_mask = s.stencil_read_mask;
+    d.depth_stencil.stencil_write_mask = s.stencil_write_mask;
+    d.depth_stencil.front = sg_stencil_face_desc{static_cast<uint32_t>(s.front_face.stencil_fail_op),
+                                                 static_cast<uint32_t>(s.front_face.stencil_depth_fail_op),
+                                                 static_cast<uint32_t>(s.front_face.stencil_pass_op),
+                                                 static_cast<uint32_t>(s.front_face.stencil_func)};
+    d.depth_stencil.back = sg_stencil_face_desc{static_cast<uint32_t>(s.back_face.stencil_fail_op),
+                                                static_cast<uint32_t>(s.back_face.stencil_depth_fail_op),
+                                                static_cast<uint32_t>(s.back_face.stencil_pass_op),
+                                                static_cast<uint32_t>(s.back_face.stencil_func)};
+    d.stencil_ref = stencil_ref_;
+    if (vs_->pack(d.vs) != result::ok || ps_->pack(d.ps) != result::ok || bs_->pack(d.bs) != result::ok)
+      return result::invalid_parameter;
+    return result::ok;
+  }
+
+private:
+  result submit(bool indexed, size_t startpos, size_t primcnt, int basevert) {
+    sg_draw_desc d;
+    result r = build_desc(indexed, startpos, primcnt, basevert, d);
+    if (r != result::ok) return r;
+    if (queries_.empty()) return to_result(sg_draw(dev_->dev, &d, nullptr));
+    sg_draw_stats st{};
+    r = to_result(sg_draw(dev_->dev, &d, &st));
+    for (auto const& q : queries_) {
+      q->stats.ia_primitives += st.ia_primitives;
+      q->stats.ia_vertices += st.ia_primitives * 3;
+      q->stats.cprimitives += st.cprimitives;
+      q->stats.ps_invocations += st.ps_invocations;
+      q->internal.backend_input_pixels += st.backend_input_pixels;
+    }
+    return r;
+  }
+
+  detail::device_sp dev_;
+  buffer_ptr streams_[SG_MAX_STREAMS];
+  size_t strides_[SG_MAX_STREAMS] = {}, offsets_[SG_MAX_STREAMS] = {};
+  buffer_ptr ib_;
+  format ib_fmt_ = format_r16_uint;  // renderer_impl's default (renderer_impl.cpp:269-284)
+  primitive_topology topo_ = primitive_triangle_list;
+  input_layout_ptr layout_;
+  cpp_vertex_shader_ptr vs_;
+  cpp_pixel_shader_ptr ps_;
+  cpp_blend_shader_ptr bs_;
+  raster_state_ptr rs_;
+  depth_stencil_state_ptr dss_;
+  int32_t stencil_ref_ = 0;
+  surface_ptr color_, ds_;
+  viewport vp_;
+  std::vector<async_object_ptr> queries_;
+  buffer_ptr mapped_buf_;
+  map_mode mapped_mode_ = map_mode_none;
+  std::vector<uint8_t> shadow_;
+};
+using renderer_ptr = std::shared_ptr<renderer>;
+
+// Factories (renderer.h:133-134).  Both create a renderer on CUDA device 0 with
+// a stream of its own; commands are stream-ordered, flush() waits for them.
+inline renderer_ptr create_gpu_renderer(int cuda_device = 0, void* cuda_stream = nullptr) {
+  sg_device* d = nullptr;
+  if (sg_device_create(cuda_device, cuda_stream, &d) != SG_OK) return nullptr;
+  return std::make_shared<renderer>(d);
+}
+inline renderer_ptr create_benchmark_renderer() { return create_gpu_renderer(0); }
+inline renderer_ptr create_software_renderer() { return create_gpu_renderer(0); }
+
+}  // namespace salvia::core

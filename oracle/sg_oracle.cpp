@@ -1892,4 +1892,24 @@ int32_t sg_resolve(sg_device* d, uint32_t src, uint32_t dst) {
   return SG_OK;
 }
 
+// The command list of sg_submit, executed one command at a time
+// (render_core::execute in order, render_core.cpp:30-61).
+int32_t sg_submit(sg_device* d, const sg_command* cmds, uint32_t n, sg_draw_stats* stats) {
+  if (!d || (!cmds && n)) return SG_INVALID_PARAMETER;
+  if (stats) std::memset(stats, 0, sizeof(sg_draw_stats) * n);
+  for (uint32_t i = 0; i < n; ++i) {
+    sg_command const& c = cmds[i];
+    int32_t r;
+    switch (c.type) {
+    case SG_CMD_DRAW: r = sg_draw(d, c.draw, stats ? &stats[i] : nullptr); break;
+    case SG_CMD_CLEAR_COLOR: r = sg_clear_color(d, c.texture, c.color); break;
+    case SG_CMD_CLEAR_DEPTH_STENCIL: r = sg_clear_depth_stencil(d, c.texture, c.flags, c.depth, c.stencil); break;
+    case SG_CMD_RESOLVE: r = sg_resolve(d, c.texture, c.texture2); break;
+    default: r = SG_INVALID_PARAMETER; break;
+    }
+    if (r != SG_OK) return r;
+  }
+  return SG_OK;
+}
+
 }  // extern "C"

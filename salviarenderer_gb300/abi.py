@@ -40,6 +40,7 @@ SEMANTIC_POSITION, SEMANTIC_TEXCOORD, SEMANTIC_COLOR, SEMANTIC_NORMAL = 0, 1, 2,
 VS_TRANSFORM, VS_MORPH_DISPLACE = 1, 2
 PS_COLOR, PS_CONSTANT, PS_TEX_MODULATE, PS_TEX_GRAD_MODULATE = 1, 2, 3, 4
 BS_REPLACE, BS_LERP_SRC_ALPHA, BS_ADD = 1, 2, 3
+CMD_DRAW, CMD_CLEAR_COLOR, CMD_CLEAR_DEPTH_STENCIL, CMD_RESOLVE = 1, 2, 3, 4
 
 
 class Viewport(C.Structure):
@@ -111,6 +112,19 @@ class DrawStats(C.Structure):
                 ("ps_invocations", C.c_uint64), ("backend_input_pixels", C.c_uint64)]
 
 
+class Command(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("texture", C.c_uint32), ("texture2", C.c_uint32),
+                ("flags", C.c_uint32), ("color", C.c_float * 4), ("depth", C.c_float),
+                ("stencil", C.c_uint32), ("draw", C.POINTER(DrawDesc))]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("cover_item", C.c_uint32), ("split_entries", C.c_uint32), ("bin_chunk", C.c_uint32),
+                ("bin_capacity", C.c_uint32), ("frag_chunks", C.c_uint32),
+                ("shade_quads_per_warp", C.c_uint32), ("shade_ctas_per_sm", C.c_uint32),
+                ("merge_ctas_per_sm", C.c_uint32)]
+
+
 _u32p = C.POINTER(C.c_uint32)
 
 SIGNATURES = {
@@ -143,11 +157,21 @@ SIGNATURES = {
     "sg_clear_depth_stencil": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,
                                            C.c_uint32]),
     "sg_resolve": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "sg_submit": (C.c_int32, [C.c_void_p, C.POINTER(Command), C.c_uint32, C.POINTER(DrawStats)]),
+    "sg_graph_create": (C.c_int32, [C.c_void_p, C.POINTER(Command), C.c_uint32, C.POINTER(C.c_void_p)]),
+    "sg_graph_launch": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "sg_graph_info": (C.c_int32, [C.c_void_p, C.c_void_p, _u32p, _u32p]),
+    "sg_graph_destroy": (None, [C.c_void_p, C.c_void_p]),
+    "sg_get_tuning": (C.c_int32, [C.c_void_p, C.POINTER(Tuning)]),
+    "sg_set_tuning": (C.c_int32, [C.c_void_p, C.POINTER(Tuning)]),
+    "sg_autotune": (C.c_int32, [C.c_void_p, C.POINTER(Command), C.c_uint32, C.c_uint32,
+                                C.POINTER(Tuning), C.POINTER(C.c_float)]),
 }
 
 # Entry points of the GPU library with no counterpart in the reference (the
 # CPU oracle does not export them).
-PRODUCT_ONLY = {"sg_draw_static_scratch"}
+PRODUCT_ONLY = {"sg_draw_static_scratch", "sg_graph_create", "sg_graph_launch", "sg_graph_info",
+                "sg_graph_destroy", "sg_get_tuning", "sg_set_tuning", "sg_autotune"}
 
 
 def bind(lib, extra=None):

@@ -1,13 +1,15 @@
 // sg_api.cu -- host runtime behind the salvia_gb300.h C ABI.
 //
-// Owns device memory for buffers, textures (all mip levels) and per-draw
-// scratch, translates an sg_draw_desc into a DrawParams block and launches the
-// draw kernel chain on the device's stream.  Mirrors the state handling of
-// renderer_impl / render_core / rasterizer::update / framebuffer::update in
-// the reference (renderer_impl.cpp:159-238, render_core.cpp:44-111,
+// Owns device memory for buffers, textures (all mip levels) and pass
+// scratch; turns commands (draws, clears, resolves) into passes -- many
+// draws over many targets run by one kernel chain -- and launches them on
+// the device's stream.  Mirrors the state handling of renderer_impl /
+// render_core / rasterizer::update / framebuffer::update in the reference
+// (renderer_impl.cpp:159-238, render_core.cpp:30-111,
 // rasterizer.cpp:221-283,1061-1109, framebuffer.cpp:325-425).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -15,34 +17,33 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
 #include "salvia_gb300.h"
 #include "sg_draw.cuh"
+#include "sg_jobs.cuh"
 
 namespace sg {
-void launch_geometry(DrawParams const& p, int nattr, cudaStream_t s);
-void launch_bin(DrawParams const& p, uint32_t nslots, bool fill, cudaStream_t s);
-void launch_scan(uint32_t* data, uint32_t n, uint32_t* sums, DrawCounters* ctr, cudaStream_t s);
-void launch_tile_ranges(DrawParams const& p, uint32_t ntiles, cudaStream_t s);
-void launch_cover(DrawParams const& p, int nreg, uint32_t grid, cudaStream_t s);
-void launch_merge(DrawParams const& p, int nreg, uint32_t grid, cudaStream_t s);
-void launch_shade_0(DrawParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_1(DrawParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_2(DrawParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_3(DrawParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_4(DrawParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_5(DrawParams const& p, uint32_t grid, cudaStream_t s);
+void launch_geometry(PassParams const& p, cudaStream_t s);
+void launch_bin(PassParams const& p, bool fill, cudaStream_t s);
+void launch_scan(uint32_t* data, size_t n, uint32_t* sums, PassCounters* ctr, cudaStream_t s);
+void launch_tile_ranges(PassParams const& p, cudaStream_t s);
+void launch_cover(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
+cudaError_t init_cover();
+void launch_merge(PassParams const& p, uint32_t grid, cudaStream_t s);
+void launch_shade_0(PassParams const& p, uint32_t grid, cudaStream_t s);
+void launch_shade_1(PassParams const& p, uint32_t grid, cudaStream_t s);
+void launch_shade_2(PassParams const& p, uint32_t grid, cudaStream_t s);
+void launch_shade_3(PassParams const& p, uint32_t grid, cudaStream_t s);
+void launch_shade_4(PassParams const& p, uint32_t grid, cudaStream_t s);
+void launch_shade_5(PassParams const& p, uint32_t grid, cudaStream_t s);
 cudaError_t upload_ewa_table_raster_a(float const* tab, cudaStream_t s);
 cudaError_t upload_ewa_table_raster_b(float const* tab, cudaStream_t s);
 cudaError_t upload_ewa_table_raster_c(float const* tab, cudaStream_t s);
 cudaError_t upload_ewa_table_geometry(float const* tab, cudaStream_t s);
-void launch_fill(uint8_t* data, size_t nelem, uint32_t esz, uint4 pattern, cudaStream_t s);
-void launch_clear_ds(uint8_t* data, size_t nelem, uint32_t fmt, uint32_t flags, float depth, uint32_t stencil,
-                     cudaStream_t s);
-void launch_resolve(uint8_t const* src, uint8_t* dst, uint32_t npix, uint32_t samples, uint32_t fmt,
-                    uint32_t dst_fmt, cudaStream_t s);
+uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaStream_t s);
 void launch_mip(uint8_t const* src, uint32_t sw, uint32_t sh, uint8_t* dst, uint32_t dw, uint32_t dh,
                 uint32_t samples, uint32_t fmt, uint32_t filter, cudaStream_t s);
 }  // namespace sg
@@ -123,7 +124,103 @@ uint8_t* static_scratch_address(int ordinal) {
   return addr[ordinal];
 }
 
+// The device memory a pass runs in: parameter blocks, triangle records, bins,
+// fragments, counters.  The device owns one set for immediate submissions;
+// every recorded graph owns its own.
+struct Scratch {
+  Arena params, slot_rec, recs, bin_counts, scan_sums, bin_entries, tile_begin, frag_rec, frag_pos, frag_mask,
+      frag_color, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, sticky;
+  bool pending = false;                // passes ran since the host last read `sticky`
+  uint32_t entry_capacity = 1u << 24;  // bin entries (grows after an overflow)
+  uint32_t chunk_capacity = 1u << 18;  // fragment chunks (grows after an overflow)
+  void release() {
+    for (Arena* a : {&params, &slot_rec, &recs, &bin_counts, &scan_sums, &bin_entries, &tile_begin, &frag_rec,
+                     &frag_pos, &frag_mask, &frag_color, &frag_ps, &chunk_next, &chunk_count, &owner_first,
+                     &counters, &stats, &sticky})
+      a->release();
+  }
+};
+
+// A pass being assembled from commands: translated draw parameters, its
+// targets, and the clears and resolves that run before and after it.
+struct PassPlan {
+  std::vector<DrawParams> draws;
+  std::vector<TargetParams> targets;
+  std::vector<uint32_t> draw_cmd;           // command index of each draw (for statistics)
+  std::vector<SurfaceJob> clears, resolves;
+  std::vector<uint32_t> clear_cmd;
+  // conflict tracking
+  std::map<std::pair<uint32_t, uint32_t>, uint32_t> target_of;  // (colour, ds) -> target index
+  std::set<uint32_t> surfaces;               // textures used as targets by the pass's draws
+  std::set<uint32_t> sampled;                // textures its draws sample
+  std::set<uint32_t> resolved;               // textures its queued resolves read or write
+  std::set<uint32_t> cleared;                // textures its queued clears write
+  std::vector<uint8_t> late_z;               // per target: a draw tests depth after shading
+  std::vector<uint32_t> target_color, target_ds;
+  uint64_t nprims = 0;
+  // derived by finalize()
+  std::vector<uint32_t> draw_prim_base, target_tile_base, chunk_target;
+  uint32_t ntiles = 0, nslots = 0, nchunks = 0, max_samples = 1;
+  uint64_t ncounts = 0, rec_units = 0;
+  bool any_early_z = false;
+  uint32_t na_mask = 0;
+  bool empty() const { return draws.empty() && clears.empty() && resolves.empty(); }
+};
+
+// Device-resident copy of a finalized plan: where its parameter blocks live.
+struct PlanLayout {
+  size_t draws_off, targets_off, dpb_off, ttb_off, ct_off, bytes;
+};
+
+PlanLayout layout_of(PassPlan const& pl) {
+  PlanLayout L{};
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~size_t(255);
+    return o;
+  };
+  L.draws_off = take(pl.draws.size() * sizeof(DrawParams));
+  L.targets_off = take(pl.targets.size() * sizeof(TargetParams));
+  L.dpb_off = take(pl.draw_prim_base.size() * 4);
+  L.ttb_off = take(pl.target_tile_base.size() * 4);
+  L.ct_off = take(pl.chunk_target.size() * 4);
+  L.bytes = off;
+  return L;
+}
+
+void pack_plan(PassPlan const& pl, PlanLayout const& L, std::vector<uint8_t>& out) {
+  out.assign(L.bytes, 0);
+  std::memcpy(out.data() + L.draws_off, pl.draws.data(), pl.draws.size() * sizeof(DrawParams));
+  std::memcpy(out.data() + L.targets_off, pl.targets.data(), pl.targets.size() * sizeof(TargetParams));
+  std::memcpy(out.data() + L.dpb_off, pl.draw_prim_base.data(), pl.draw_prim_base.size() * 4);
+  std::memcpy(out.data() + L.ttb_off, pl.target_tile_base.data(), pl.target_tile_base.size() * 4);
+  std::memcpy(out.data() + L.ct_off, pl.chunk_target.data(), pl.chunk_target.size() * 4);
+}
+
+sg_tuning default_tuning() {
+  sg_tuning t{};
+  t.cover_item = 32;
+  t.split_entries = 320;
+  t.bin_chunk = BIN_CHUNK_MIN;
+  t.bin_capacity = 1u << 24;
+  t.frag_chunks = 1u << 18;
+  t.shade_quads_per_warp = 8;
+  t.shade_ctas_per_sm = 8;
+  t.merge_ctas_per_sm = 3;
+  return t;
+}
+
 }  // namespace
+
+struct sg_graph {
+  Scratch scratch;
+  std::vector<PassPlan> plans;
+  Arena params;                   // every pass's parameter blocks
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint32_t kernels = 0;
+};
 
 struct sg_device {
   int ordinal = 0;
@@ -134,14 +231,15 @@ struct sg_device {
   std::map<uint32_t, Buffer> buffers;
   std::map<uint32_t, Texture> textures;
   std::map<uint32_t, Sampler> samplers;
-  Arena slot_rec, recs, bin_counts, scan_sums, bin_entries, tile_begin, frag_rec, frag_pos, frag_mask, frag_color,
-      frag_ps, chunk_next, chunk_count, owner_first;
-  DrawCounters* counters = nullptr;      // device
-  DrawCounters* counters_host = nullptr; // pinned
-  uint32_t entry_capacity = 1u << 24;    // bin entries (grows after an overflow)
-  uint32_t chunk_capacity = 1u << 18;    // fragment chunks per draw (grows after an overflow)
+  Scratch scratch;
+  PassCounters* counters_host = nullptr;  // pinned: counters of the last pass run with statistics
+  DrawStatsDev* stats_host = nullptr;     // pinned: per-draw statistics of that pass
+  size_t stats_host_cap = 0;
+  unsigned int* sticky_host = nullptr;    // pinned: overflow bits read back at sg_sync
+  unsigned int* static_sticky = nullptr;  // the static scratch's overflow word, when a call used it
+  std::set<sg_graph*> graphs;
+  sg_tuning tuning = default_tuning();
   std::string error;
-  int32_t sticky = SG_OK;
   // profiling: event pairs per stage, summed at sg_profile_read
   bool profiling = false;
   std::vector<cudaEvent_t> event_pool;
@@ -167,13 +265,14 @@ Texture* find_tex(sg_device* d, uint32_t h) {
   return it == d->textures.end() ? nullptr : &it->second;
 }
 
-int32_t build_sampler(sg_device* d, uint32_t handle, dev_sampler& out) {
+int32_t build_sampler(sg_device* d, uint32_t handle, dev_sampler& out, uint32_t* tex_out) {
   std::memset(&out, 0, sizeof(out));
   if (!handle) return SG_OK;
   auto it = d->samplers.find(handle);
   if (it == d->samplers.end()) return SG_INVALID_PARAMETER;
   Texture* t = find_tex(d, it->second.texture);
   if (!t) return SG_INVALID_PARAMETER;
+  *tex_out = it->second.texture;
   sg_sampler_desc const& s = it->second.desc;
   if (s.min_filter > SG_FILTER_LINEAR || s.mag_filter > SG_FILTER_LINEAR || s.mip_filter > SG_FILTER_ANISOTROPIC ||
       s.address_u > SG_ADDRESS_BORDER || s.address_v > SG_ADDRESS_BORDER || s.mip_quality > SG_MIP_HI_QUALITY)
@@ -215,8 +314,8 @@ cudaEvent_t take_event(sg_device* d) {
   return d->event_pool[d->events_used++];
 }
 // Records a stage boundary; returns the begin event (or null when not profiling).
-cudaEvent_t stage_begin(sg_device* d) {
-  if (!d->profiling) return nullptr;
+cudaEvent_t stage_begin(sg_device* d, bool enabled) {
+  if (!d->profiling || !enabled) return nullptr;
   cudaEvent_t e = take_event(d);
   if (e) cudaEventRecord(e, d->stream);
   return e;
@@ -229,62 +328,15 @@ void stage_end(sg_device* d, int stage, cudaEvent_t b) {
   d->marks.push_back({stage, {b, e}});
 }
 
-// Lays the scratch of one draw out in the static array `base`: the draw
-// counters, the tables sized by the draw (records, bin counters, tile tables;
-// at most SG_STATIC_SCRATCH_TABLE_LIMIT bytes) and, in the rest, one quarter
-// for bin entries and three quarters for fragment chunks.
-int32_t carve_static_scratch(sg_device* d, uint8_t* base, DrawParams& p, uint32_t nslots, uint32_t ntiles,
-                             size_t ncounts, void** scan_sums) {
-  size_t off = 0;
-  auto take = [&](size_t bytes) {
-    uint8_t* q = base + off;
-    off += (bytes + 255) & ~size_t(255);
-    return q;
-  };
-  take(sizeof(DrawCounters));
-  p.slot_rec = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(nslots) * 4));
-  p.recs = reinterpret_cast<float4*>(take(static_cast<size_t>(nslots) * p.rec_stride * sizeof(float4)));
-  p.bin_counts = reinterpret_cast<uint32_t*>(take(ncounts * 4));
-  *scan_sums = take((ncounts / 4096 + 2) * 4);
-  p.tile_begin = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(ntiles) + 1) * 4));
-  p.owner_first = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(ntiles) * RASTER_THREADS * 4));
-  if (off > SG_STATIC_SCRATCH_TABLE_LIMIT) {
-    char msg[200];
-    std::snprintf(msg, sizeof(msg),
-                  "sg_draw_static_scratch: the draw's tables need %zu bytes; the static scratch allows %u "
-                  "(%u primitives, %u tiles)",
-                  off, SG_STATIC_SCRATCH_TABLE_LIMIT, nslots / 3, ntiles);
-    d->error = msg;
-    return SG_INVALID_PARAMETER;
-  }
-  size_t rest = SG_STATIC_SCRATCH_BYTES - off;
-  uint32_t entries = static_cast<uint32_t>(rest / 4 / 4);
-  p.bin_entries = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(entries) * 4));
-  p.bin_capacity = entries;
-  // per fragment chunk: FRAG_CHUNK x (record, position, mask, 4 colours, ps flag) + next + count
-  size_t per_chunk = FRAG_CHUNK * (4 + 4 + 4 + 4 * sizeof(float4) + 1) + 8;
-  uint32_t chunks = static_cast<uint32_t>((SG_STATIC_SCRATCH_BYTES - off - 6 * 256) / per_chunk);
-  size_t nfrag = static_cast<size_t>(chunks) * FRAG_CHUNK;
-  p.frag_rec = reinterpret_cast<uint32_t*>(take(nfrag * 4));
-  p.frag_pos = reinterpret_cast<uint32_t*>(take(nfrag * 4));
-  p.frag_mask = reinterpret_cast<uint32_t*>(take(nfrag * 4));
-  p.frag_color = reinterpret_cast<float4*>(take(nfrag * 4 * sizeof(float4)));
-  p.frag_ps = take(nfrag);
-  p.chunk_next = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(chunks) * 4));
-  p.chunk_count = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(chunks) * 4));
-  p.chunk_capacity = chunks;
-  if (off > SG_STATIC_SCRATCH_BYTES) {  // layout arithmetic guard
-    d->error = "sg_draw_static_scratch: scratch layout exceeds the static array";
-    return SG_FAILED;
-  }
-  return SG_OK;
-}
+// ---------------------------------------------------------------------------
+// draw translation (renderer_impl state -> DrawParams)
 
-// `fixed` (sg_draw_static_scratch) is the static scratch array: all per-draw
-// scratch is carved from it and no profiling events are taken; otherwise the
-// device's arenas hold the scratch.
-int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats, uint8_t* fixed = nullptr) {
-  cudaStream_t s = d->stream;
+struct DrawInfo {
+  uint32_t color = 0, ds = 0;       // target textures
+  uint32_t tex[2] = {0, 0};         // sampled textures
+};
+
+int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, DrawInfo& info) {
   if (desc->raster.fill_mode != SG_FILL_SOLID) return SG_INVALID_PARAMETER;
   if (desc->topology != SG_TOPOLOGY_TRIANGLE_LIST && desc->topology != SG_TOPOLOGY_TRIANGLE_STRIP)
     return SG_INVALID_PARAMETER;
@@ -299,8 +351,10 @@ int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats, 
   if (dt && !valid_ds_fmt(dt->fmt)) return SG_FAILED;
   if (ct && dt && (dt->samples != ct->samples || dt->levels[0].w < ct->levels[0].w || dt->levels[0].h < ct->levels[0].h))
     return SG_FAILED;
+  if (desc->prim_count > SG_PASS_MAX_PRIMS) return SG_INVALID_PARAMETER;
+  info.color = desc->color_target;
+  info.ds = desc->ds_target;
 
-  DrawParams p;
   std::memset(&p, 0, sizeof(p));
   // input assembly
   for (uint32_t i = 0; i < desc->num_streams; ++i) {
@@ -344,13 +398,15 @@ int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats, 
   p.bs_prog = desc->bs.program;
   std::memcpy(p.vs_k, desc->vs.constants, sizeof(p.vs_k));
   std::memcpy(p.ps_k, desc->ps.constants, sizeof(p.ps_k));
-  if (int32_t r = build_sampler(d, desc->vs.samplers[0], p.vs_samp)) return r;
-  if (int32_t r = build_sampler(d, desc->ps.samplers[0], p.ps_samp)) return r;
+  if (int32_t r = build_sampler(d, desc->vs.samplers[0], p.vs_samp, &info.tex[0])) return r;
+  if (int32_t r = build_sampler(d, desc->ps.samplers[0], p.ps_samp, &info.tex[1])) return r;
   if (p.vs_prog == SG_VS_MORPH_DISPLACE && !desc->vs.samplers[0]) return SG_INVALID_PARAMETER;
   if ((p.ps_prog == SG_PS_TEX_MODULATE || p.ps_prog == SG_PS_TEX_GRAD_MODULATE) && !desc->ps.samplers[0])
     return SG_INVALID_PARAMETER;
-  int nattr = static_cast<int>(desc->num_varyings);
-  for (int i = 0; i < SG_MAX_VARYINGS; ++i) {
+  uint32_t const nattr = desc->num_varyings;
+  p.nattr = nattr;
+  p.rec_stride = rec_stride_for(static_cast<int>(nattr));
+  for (uint32_t i = 0; i < SG_MAX_VARYINGS; ++i) {
     p.mods[i] = desc->varying_modifiers[i];
     if (i < nattr && (p.mods[i] & SG_AM_CENTROID)) p.has_centroid = 1;
   }
@@ -367,32 +423,9 @@ int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats, 
   p.vp_maxz = vp.maxz;
   p.tiles_x = static_cast<int>(static_cast<size_t>(vp.w + TILE - 1) / TILE);
   p.tiles_y = static_cast<int>(static_cast<size_t>(vp.h + TILE - 1) / TILE);
-  Texture* tt = ct ? ct : dt;
-  p.samples = tt->samples;
-  p.width = tt->levels[0].w;
-  p.height = tt->levels[0].h;
-  p.target_w = static_cast<float>(p.width);
-  p.target_h = static_cast<float>(p.height);
-  static const float pat1[2] = {0.5f, 0.5f};
-  static const float pat2[4] = {0.25f, 0.25f, 0.75f, 0.75f};
-  static const float pat4[8] = {0.375f, 0.125f, 0.875f, 0.375f, 0.125f, 0.625f, 0.625f, 0.875f};
-  float const* pat = p.samples == 1 ? pat1 : p.samples == 2 ? pat2 : pat4;
-  for (uint32_t i = 0; i < p.samples; ++i) {
-    p.sp_x[i] = pat[2 * i];
-    p.sp_y[i] = pat[2 * i + 1];
-  }
   // output merger
-  if (ct) {
-    p.color = ct->levels[0].ptr;
-    p.color_fmt = ct->fmt;
-    p.color_esz = ct->esz;
-  }
   sg_depth_stencil_desc const& ds = desc->depth_stencil;
   if (dt) {
-    p.ds = dt->levels[0].ptr;
-    p.ds_fmt = dt->fmt;
-    p.ds_esz = dt->esz;
-    p.ds_width = dt->levels[0].w;
     if (ds.depth_enable) {
       p.read_depth = ds.depth_func != SG_CMP_NEVER && ds.depth_func != SG_CMP_ALWAYS;
       p.write_depth = ds.depth_write && ds.depth_func != SG_CMP_NEVER;
@@ -408,126 +441,647 @@ int32_t draw_impl(sg_device* d, sg_draw_desc const* desc, sg_draw_stats* stats, 
   p.front_pass = ds.front.pass_op;
   p.back_func = ds.back.func;
   p.back_pass = ds.back.pass_op;
+  Texture* tt = ct ? ct : dt;
+  p.zcfg = zcfg_of(tt->samples, p.read_depth, p.write_depth, dt && dt->fmt == SG_FMT_D24S8, p.early_z && dt,
+                   p.depth_func);
+  return SG_OK;
+}
 
-  // scratch
-  uint32_t nslots = desc->prim_count * 3;
-  uint32_t ntiles = static_cast<uint32_t>(p.tiles_x * p.tiles_y);
-  p.rec_stride = rec_stride_for(nattr);
-  DrawCounters* counters = fixed ? reinterpret_cast<DrawCounters*>(fixed) : d->counters;
-  p.counters = counters;
-  SG_CUDA(d, cudaMemsetAsync(counters, 0, sizeof(DrawCounters), s));
-  if (desc->prim_count == 0 || ntiles == 0) {
-    if (stats) {
-      std::memset(stats, 0, sizeof(*stats));
-      stats->ia_primitives = desc->prim_count;
-    }
-    return SG_OK;
+// Target parameters of a (colour, depth-stencil) pair.
+void fill_target(sg_device* d, uint32_t color, uint32_t ds, TargetParams& T) {
+  std::memset(&T, 0, sizeof(T));
+  Texture* ct = color ? find_tex(d, color) : nullptr;
+  Texture* dt = ds ? find_tex(d, ds) : nullptr;
+  Texture* tt = ct ? ct : dt;
+  T.samples = tt->samples;
+  T.width = tt->levels[0].w;
+  T.height = tt->levels[0].h;
+  T.target_w = static_cast<float>(T.width);
+  T.target_h = static_cast<float>(T.height);
+  static const float pat1[2] = {0.5f, 0.5f};
+  static const float pat2[4] = {0.25f, 0.25f, 0.75f, 0.75f};
+  static const float pat4[8] = {0.375f, 0.125f, 0.875f, 0.375f, 0.125f, 0.625f, 0.625f, 0.875f};
+  float const* pat = T.samples == 1 ? pat1 : T.samples == 2 ? pat2 : pat4;
+  for (uint32_t i = 0; i < T.samples; ++i) {
+    T.sp_x[i] = pat[2 * i];
+    T.sp_y[i] = pat[2 * i + 1];
   }
-  uint32_t chunk = BIN_CHUNK_MIN;
-  uint32_t max_chunks = static_cast<uint32_t>(d->num_sms) * 32;
-  while ((nslots + chunk - 1) / chunk > max_chunks) chunk *= 2;
-  uint32_t nchunks = (nslots + chunk - 1) / chunk;
-  size_t ncounts = static_cast<size_t>(ntiles) * nchunks;
-  void* scan_sums = nullptr;
-  if (fixed) {
-    if (int32_t r = carve_static_scratch(d, fixed, p, nslots, ntiles, ncounts, &scan_sums)) return r;
+  if (ct) {
+    T.color = ct->levels[0].ptr;
+    T.color_fmt = ct->fmt;
+    T.color_esz = ct->esz;
+  }
+  if (dt) {
+    T.ds = dt->levels[0].ptr;
+    T.ds_fmt = dt->fmt;
+    T.ds_esz = dt->esz;
+    T.ds_width = dt->levels[0].w;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pass assembly
+
+// Whether the draw can join the pass; if not, the pass must run first.
+bool draw_fits(PassPlan const& pl, DrawParams const& p, DrawInfo const& info) {
+  if (pl.nprims + p.prim_count > SG_PASS_MAX_PRIMS) return false;
+  for (uint32_t t : info.tex)
+    if (t && (pl.surfaces.count(t) || pl.cleared.count(t) || pl.resolved.count(t))) return false;
+  for (uint32_t s : {info.color, info.ds}) {
+    if (!s) continue;
+    if (pl.sampled.count(s) || pl.resolved.count(s)) return false;
+  }
+  auto it = pl.target_of.find({info.color, info.ds});
+  if (it == pl.target_of.end()) {
+    // a new target may not share a surface with an existing one
+    if ((info.color && pl.surfaces.count(info.color)) || (info.ds && pl.surfaces.count(info.ds))) return false;
+  } else if ((p.zcfg & 128u) && pl.late_z[it->second]) {
+    return false;  // depth tested before shading after a draw that tests after shading
+  }
+  return true;
+}
+
+void add_draw(sg_device* d, PassPlan& pl, DrawParams p, DrawInfo const& info, uint32_t cmd) {
+  auto key = std::make_pair(info.color, info.ds);
+  auto it = pl.target_of.find(key);
+  uint32_t t;
+  if (it == pl.target_of.end()) {
+    t = static_cast<uint32_t>(pl.targets.size());
+    pl.target_of[key] = t;
+    TargetParams T;
+    fill_target(d, info.color, info.ds, T);
+    pl.targets.push_back(T);
+    pl.late_z.push_back(0);
+    if (info.color) pl.surfaces.insert(info.color);
+    if (info.ds) pl.surfaces.insert(info.ds);
   } else {
-  SG_CUDA(d, d->slot_rec.ensure(static_cast<size_t>(nslots) * 4));
-  SG_CUDA(d, d->recs.ensure(static_cast<size_t>(nslots) * p.rec_stride * sizeof(float4)));
-  if (ncounts >= (1u << 31)) return SG_OUT_OF_MEMORY;
-  SG_CUDA(d, d->bin_counts.ensure(ncounts * 4));
-  SG_CUDA(d, d->scan_sums.ensure((ncounts / 4096 + 2) * 4));
-  SG_CUDA(d, d->bin_entries.ensure(static_cast<size_t>(d->entry_capacity) * 4));
-  SG_CUDA(d, d->tile_begin.ensure((static_cast<size_t>(ntiles) + 1) * 4));
-  size_t nfrag = static_cast<size_t>(d->chunk_capacity) * FRAG_CHUNK;
-  SG_CUDA(d, d->frag_rec.ensure(nfrag * 4));
-  SG_CUDA(d, d->frag_pos.ensure(nfrag * 4));
-  SG_CUDA(d, d->frag_mask.ensure(nfrag * 4));
-  SG_CUDA(d, d->frag_color.ensure(nfrag * 4 * sizeof(float4)));
-  SG_CUDA(d, d->frag_ps.ensure(nfrag));
-  SG_CUDA(d, d->chunk_next.ensure(static_cast<size_t>(d->chunk_capacity) * 4));
-  SG_CUDA(d, d->chunk_count.ensure(static_cast<size_t>(d->chunk_capacity) * 4));
-  SG_CUDA(d, d->owner_first.ensure(static_cast<size_t>(ntiles) * RASTER_THREADS * 4));
-  p.slot_rec = static_cast<uint32_t*>(d->slot_rec.ptr);
-  p.recs = static_cast<float4*>(d->recs.ptr);
-  p.bin_counts = static_cast<uint32_t*>(d->bin_counts.ptr);
-  p.bin_entries = static_cast<uint32_t*>(d->bin_entries.ptr);
-  p.tile_begin = static_cast<uint32_t*>(d->tile_begin.ptr);
-  p.bin_capacity = d->entry_capacity;
-  p.frag_rec = static_cast<uint32_t*>(d->frag_rec.ptr);
-  p.frag_pos = static_cast<uint32_t*>(d->frag_pos.ptr);
-  p.frag_mask = static_cast<uint32_t*>(d->frag_mask.ptr);
-  p.frag_color = static_cast<float4*>(d->frag_color.ptr);
-  p.frag_ps = static_cast<uint8_t*>(d->frag_ps.ptr);
-  p.chunk_next = static_cast<uint32_t*>(d->chunk_next.ptr);
-  p.chunk_count = static_cast<uint32_t*>(d->chunk_count.ptr);
-  p.chunk_capacity = d->chunk_capacity;
-  p.owner_first = static_cast<uint32_t*>(d->owner_first.ptr);
-  scan_sums = d->scan_sums.ptr;
+    t = it->second;
   }
-  p.nchunks = nchunks;
-  p.chunk = chunk;
-  uint32_t tile_grid = std::min<uint32_t>(ntiles, static_cast<uint32_t>(d->num_sms) * 3);
-  uint32_t cover_grid = std::min<uint32_t>(ntiles * 4, static_cast<uint32_t>(d->num_sms) * 4);
-  uint32_t shade_grid = static_cast<uint32_t>(d->num_sms) * 8;
-  int const nreg = 1 + nattr;
+  p.target = t;
+  if (!(p.zcfg & 128u) && pl.targets[t].ds) pl.late_z[t] = 1;
+  for (uint32_t x : info.tex)
+    if (x) pl.sampled.insert(x);
+  p.prim_base = static_cast<uint32_t>(pl.nprims);
+  pl.nprims += p.prim_count;
+  pl.draws.push_back(p);
+  pl.draw_cmd.push_back(cmd);
+}
 
-  auto begin = [&]() { return fixed ? nullptr : stage_begin(d); };
-  cudaEvent_t ev = begin();
-  launch_geometry(p, nattr, s);
-  stage_end(d, 0, ev);
-  ev = begin();
-  SG_CUDA(d, cudaMemsetAsync(p.bin_counts, 0, ncounts * 4, s));
-  launch_bin(p, nslots, false, s);
-  launch_scan(p.bin_counts, static_cast<uint32_t>(ncounts), static_cast<uint32_t*>(scan_sums), counters, s);
-  launch_tile_ranges(p, ntiles, s);
-  launch_bin(p, nslots, true, s);
-  stage_end(d, 1, ev);
-  ev = begin();
-  launch_cover(p, nreg, cover_grid, s);
-  stage_end(d, 2, ev);
-  ev = begin();
-  switch (nattr) {
-  case 0: launch_shade_0(p, shade_grid, s); break;
-  case 1: launch_shade_1(p, shade_grid, s); break;
-  case 2: launch_shade_2(p, shade_grid, s); break;
-  case 3: launch_shade_3(p, shade_grid, s); break;
-  case 4: launch_shade_4(p, shade_grid, s); break;
-  default: launch_shade_5(p, shade_grid, s); break;
+// Tile grids, slot ranges and binning chunks of a pass.
+void finalize(PassPlan& pl, sg_device* d) {
+  uint32_t const nt = static_cast<uint32_t>(pl.targets.size());
+  std::vector<uint64_t> slots(nt, 0);
+  for (auto& T : pl.targets) T.tiles_x = T.tiles_y = 0;
+  pl.any_early_z = false;
+  pl.na_mask = 0;
+  pl.max_samples = 1;
+  pl.rec_units = 0;
+  for (auto& p : pl.draws) {
+    TargetParams& T = pl.targets[p.target];
+    T.tiles_x = std::max(T.tiles_x, p.tiles_x);
+    T.tiles_y = std::max(T.tiles_y, p.tiles_y);
+    slots[p.target] += 3ull * p.prim_count;
+    if ((p.zcfg & 128u) && T.ds) T.any_early_z = 1;
+    pl.na_mask |= 1u << p.nattr;
+    pl.rec_units += 3ull * p.prim_count * p.rec_stride;
   }
-  stage_end(d, 3, ev);
-  ev = begin();
-  launch_merge(p, nreg, tile_grid, s);
-  stage_end(d, 4, ev);
-  d->prof.draws += 1;
-  d->prof.launches += 10;  // geometry, bin count, 3 scan kernels, tile ranges, bin fill, cover, shade, merge
-  d->prof.raster_launches += 1;
-  SG_CUDA(d, cudaGetLastError());
-  SG_CUDA(d, cudaMemcpyAsync(d->counters_host, counters, sizeof(DrawCounters), cudaMemcpyDeviceToHost, s));
-  if (stats) {
-    SG_CUDA(d, cudaStreamSynchronize(s));
-    DrawCounters const& c = *d->counters_host;
-    if (fixed && (c.overflow & 5u)) {
-      char msg[200];
-      std::snprintf(msg, sizeof(msg),
-                    "static scratch exhausted: %u bin entries (room for %u), %u fragment chunks (room for %u)",
-                    c.bin_entries, p.bin_capacity, c.chunk_total, p.chunk_capacity);
-      d->error = msg;
-      return SG_OUT_OF_MEMORY;
+  // slot ranges: targets in order, each target's draws in API order
+  std::vector<uint64_t> tslot(nt, 0);
+  uint64_t acc = 0;
+  for (uint32_t t = 0; t < nt; ++t) {
+    tslot[t] = acc;
+    acc += slots[t];
+  }
+  pl.nslots = static_cast<uint32_t>(acc);
+  std::vector<uint64_t> cursor = tslot;
+  for (auto& p : pl.draws) {
+    p.slot_base = static_cast<uint32_t>(cursor[p.target]);
+    cursor[p.target] += 3ull * p.prim_count;
+  }
+  // tiles and binning chunks; counters stay under 32M in total
+  uint32_t const max_chunks = static_cast<uint32_t>(std::max(1, d->num_sms)) * 32;
+  std::vector<uint32_t> chunk(nt);
+  for (uint32_t t = 0; t < nt; ++t) {
+    uint32_t c = std::max<uint32_t>(BIN_CHUNK_MIN, d->tuning.bin_chunk);
+    while ((slots[t] + c - 1) / c > max_chunks) c *= 2;
+    chunk[t] = c;
+  }
+  auto counters_of = [&](uint32_t t) {
+    TargetParams const& T = pl.targets[t];
+    return static_cast<uint64_t>(T.tiles_x) * T.tiles_y * ((slots[t] + chunk[t] - 1) / chunk[t]);
+  };
+  for (;;) {
+    uint64_t total = 0, worst = 0;
+    uint32_t wt = 0;
+    for (uint32_t t = 0; t < nt; ++t) {
+      uint64_t c = counters_of(t);
+      total += c;
+      if (c > worst) {
+        worst = c;
+        wt = t;
+      }
     }
-    if (c.overflow & 5u) {
-      if (c.overflow & 1u) d->entry_capacity = std::max<uint32_t>(d->entry_capacity * 2, c.bin_entries + c.bin_entries / 4);
-      if (c.overflow & 4u)
-        d->chunk_capacity = std::max<uint32_t>(d->chunk_capacity * 2, c.chunk_total + c.chunk_total / 4);
-      d->error = "scratch buffer overflow; capacities raised for later draws";
-      return SG_OUT_OF_MEMORY;
-    }
-    stats->ia_primitives = desc->prim_count;
-    stats->cprimitives = c.cprimitives;
-    stats->ps_invocations = c.ps_invocations;
-    stats->backend_input_pixels = c.backend_input_pixels;
+    if (total <= (1ull << 25) || chunk[wt] >= (1u << 30)) break;
+    chunk[wt] *= 2;
+  }
+  pl.ntiles = pl.nchunks = 0;
+  pl.ncounts = 0;
+  pl.draw_prim_base.clear();
+  pl.target_tile_base.clear();
+  pl.chunk_target.clear();
+  for (uint32_t t = 0; t < nt; ++t) {
+    TargetParams& T = pl.targets[t];
+    T.tile_base = pl.ntiles;
+    pl.target_tile_base.push_back(pl.ntiles);
+    pl.ntiles += static_cast<uint32_t>(T.tiles_x * T.tiles_y);
+    T.slot_base = static_cast<uint32_t>(tslot[t]);
+    T.nslots = static_cast<uint32_t>(slots[t]);
+    T.chunk = chunk[t];
+    T.nchunks = static_cast<uint32_t>((slots[t] + chunk[t] - 1) / chunk[t]);
+    T.chunk_base = pl.nchunks;
+    for (uint32_t c = 0; c < T.nchunks; ++c) pl.chunk_target.push_back(t);
+    pl.nchunks += T.nchunks;
+    T.count_base = pl.ncounts;
+    pl.ncounts += static_cast<uint64_t>(T.tiles_x) * T.tiles_y * T.nchunks;
+    pl.max_samples = std::max(pl.max_samples, T.samples);
+    if (T.any_early_z) pl.any_early_z = true;
+  }
+  for (auto const& p : pl.draws) pl.draw_prim_base.push_back(p.prim_base);
+}
+
+// Where a pass's scratch lives: device arenas, or a fixed region carved here.
+struct ScratchView {
+  uint8_t* params = nullptr;
+  PassParams P{};
+  uint32_t* scan_sums = nullptr;
+};
+
+void bind_params(PassParams& P, uint8_t* params, PlanLayout const& L, PassPlan const& pl) {
+  P.draws = reinterpret_cast<DrawParams const*>(params + L.draws_off);
+  P.targets = reinterpret_cast<TargetParams const*>(params + L.targets_off);
+  P.draw_prim_base = reinterpret_cast<uint32_t const*>(params + L.dpb_off);
+  P.target_tile_base = reinterpret_cast<uint32_t const*>(params + L.ttb_off);
+  P.chunk_target = reinterpret_cast<uint32_t const*>(params + L.ct_off);
+  P.ndraws = static_cast<uint32_t>(pl.draws.size());
+  P.ntargets = static_cast<uint32_t>(pl.targets.size());
+  P.nprims = static_cast<uint32_t>(pl.nprims);
+  P.nslots = pl.nslots;
+  P.ntiles = pl.ntiles;
+  P.nchunks = pl.nchunks;
+}
+
+size_t per_chunk_bytes() { return FRAG_CHUNK * (4 + 4 + 4 + 4 * sizeof(float4) + 1) + 8; }
+
+// Scratch in the device's (or a graph's) arenas.
+int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout const& L, bool own_params,
+                       ScratchView& v) {
+  PassParams& P = v.P;
+  if (pl.rec_units > 0x7FFFFFFFull) return SG_OUT_OF_MEMORY;  // record ids must fit 31 bits
+  if (own_params) SG_CUDA(d, sc.params.ensure(L.bytes));
+  SG_CUDA(d, sc.counters.ensure(sizeof(PassCounters)));
+  if (!sc.sticky.ptr) {
+    SG_CUDA(d, sc.sticky.ensure(sizeof(unsigned int)));
+    SG_CUDA(d, cudaMemset(sc.sticky.ptr, 0, sizeof(unsigned int)));
+  }
+  SG_CUDA(d, sc.stats.ensure(std::max<size_t>(1, pl.draws.size()) * sizeof(DrawStatsDev)));
+  SG_CUDA(d, sc.slot_rec.ensure(static_cast<size_t>(pl.nslots) * 4));
+  SG_CUDA(d, sc.recs.ensure(static_cast<size_t>(pl.rec_units) * sizeof(float4)));
+  SG_CUDA(d, sc.bin_counts.ensure(pl.ncounts * 4));
+  SG_CUDA(d, sc.scan_sums.ensure((pl.ncounts / 4096 + 2) * 4));
+  SG_CUDA(d, sc.bin_entries.ensure(static_cast<size_t>(sc.entry_capacity) * 4));
+  SG_CUDA(d, sc.tile_begin.ensure((static_cast<size_t>(pl.ntiles) + 1) * 4));
+  size_t nfrag = static_cast<size_t>(sc.chunk_capacity) * FRAG_CHUNK;
+  SG_CUDA(d, sc.frag_rec.ensure(nfrag * 4));
+  SG_CUDA(d, sc.frag_pos.ensure(nfrag * 4));
+  SG_CUDA(d, sc.frag_mask.ensure(nfrag * 4));
+  SG_CUDA(d, sc.frag_color.ensure(nfrag * 4 * sizeof(float4)));
+  SG_CUDA(d, sc.frag_ps.ensure(nfrag));
+  SG_CUDA(d, sc.chunk_next.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
+  SG_CUDA(d, sc.chunk_count.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
+  SG_CUDA(d, sc.owner_first.ensure(static_cast<size_t>(pl.ntiles) * RASTER_THREADS * 4));
+  v.params = static_cast<uint8_t*>(sc.params.ptr);
+  P.counters = static_cast<PassCounters*>(sc.counters.ptr);
+  P.sticky = static_cast<unsigned int*>(sc.sticky.ptr);
+  P.draw_stats = static_cast<DrawStatsDev*>(sc.stats.ptr);
+  P.slot_rec = static_cast<uint32_t*>(sc.slot_rec.ptr);
+  P.recs = static_cast<float4*>(sc.recs.ptr);
+  P.rec_capacity = static_cast<uint32_t>(pl.rec_units);
+  P.bin_counts = static_cast<uint32_t*>(sc.bin_counts.ptr);
+  P.bin_entries = static_cast<uint32_t*>(sc.bin_entries.ptr);
+  P.bin_capacity = sc.entry_capacity;
+  P.tile_begin = static_cast<uint32_t*>(sc.tile_begin.ptr);
+  P.frag_rec = static_cast<uint32_t*>(sc.frag_rec.ptr);
+  P.frag_pos = static_cast<uint32_t*>(sc.frag_pos.ptr);
+  P.frag_mask = static_cast<uint32_t*>(sc.frag_mask.ptr);
+  P.frag_color = static_cast<float4*>(sc.frag_color.ptr);
+  P.frag_ps = static_cast<uint8_t*>(sc.frag_ps.ptr);
+  P.chunk_next = static_cast<uint32_t*>(sc.chunk_next.ptr);
+  P.chunk_count = static_cast<uint32_t*>(sc.chunk_count.ptr);
+  P.chunk_capacity = sc.chunk_capacity;
+  P.owner_first = static_cast<uint32_t*>(sc.owner_first.ptr);
+  v.scan_sums = static_cast<uint32_t*>(sc.scan_sums.ptr);
+  return SG_OK;
+}
+
+// Lays the scratch of one pass out in the static array `base`: the counters,
+// the parameter blocks and the tables sized by the draw (records, bin
+// counters, tile tables; at most SG_STATIC_SCRATCH_TABLE_LIMIT bytes) and, in
+// the rest, one quarter for bin entries and three quarters for fragment chunks.
+int32_t scratch_static(sg_device* d, uint8_t* base, PassPlan const& pl, PlanLayout const& L, ScratchView& v) {
+  PassParams& P = v.P;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    uint8_t* q = base + off;
+    off += (bytes + 255) & ~size_t(255);
+    return q;
+  };
+  P.counters = reinterpret_cast<PassCounters*>(take(sizeof(PassCounters)));
+  P.sticky = reinterpret_cast<unsigned int*>(take(sizeof(unsigned int)));
+  P.draw_stats = reinterpret_cast<DrawStatsDev*>(take(pl.draws.size() * sizeof(DrawStatsDev)));
+  v.params = take(L.bytes);
+  P.slot_rec = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(pl.nslots) * 4));
+  P.recs = reinterpret_cast<float4*>(take(static_cast<size_t>(pl.rec_units) * sizeof(float4)));
+  P.rec_capacity = static_cast<uint32_t>(std::min<uint64_t>(pl.rec_units, 0x7FFFFFFFull));
+  P.bin_counts = reinterpret_cast<uint32_t*>(take(pl.ncounts * 4));
+  v.scan_sums = reinterpret_cast<uint32_t*>(take((pl.ncounts / 4096 + 2) * 4));
+  P.tile_begin = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(pl.ntiles) + 1) * 4));
+  P.owner_first = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(pl.ntiles) * RASTER_THREADS * 4));
+  if (off > SG_STATIC_SCRATCH_TABLE_LIMIT) {
+    char msg[200];
+    std::snprintf(msg, sizeof(msg),
+                  "sg_draw_static_scratch: the draw's tables need %zu bytes; the static scratch allows %u "
+                  "(%u primitives, %u tiles)",
+                  off, SG_STATIC_SCRATCH_TABLE_LIMIT, pl.nslots / 3, pl.ntiles);
+    d->error = msg;
+    return SG_INVALID_PARAMETER;
+  }
+  size_t rest = SG_STATIC_SCRATCH_BYTES - off;
+  uint32_t entries = static_cast<uint32_t>(rest / 4 / 4);
+  P.bin_entries = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(entries) * 4));
+  P.bin_capacity = entries;
+  uint32_t chunks = static_cast<uint32_t>((SG_STATIC_SCRATCH_BYTES - off - 6 * 256) / per_chunk_bytes());
+  size_t nfrag = static_cast<size_t>(chunks) * FRAG_CHUNK;
+  P.frag_rec = reinterpret_cast<uint32_t*>(take(nfrag * 4));
+  P.frag_pos = reinterpret_cast<uint32_t*>(take(nfrag * 4));
+  P.frag_mask = reinterpret_cast<uint32_t*>(take(nfrag * 4));
+  P.frag_color = reinterpret_cast<float4*>(take(nfrag * 4 * sizeof(float4)));
+  P.frag_ps = take(nfrag);
+  P.chunk_next = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(chunks) * 4));
+  P.chunk_count = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(chunks) * 4));
+  P.chunk_capacity = chunks;
+  if (off > SG_STATIC_SCRATCH_BYTES) {  // layout arithmetic guard
+    d->error = "sg_draw_static_scratch: scratch layout exceeds the static array";
+    return SG_FAILED;
   }
   return SG_OK;
+}
+
+// Launches the kernel chain of a pass whose scratch is bound in `v`.  With
+// `upload`, the parameter blocks are copied from `packed` first (stream
+// ordered).  Returns the number of kernels launched in `*kernels`.
+int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vector<uint8_t> const* packed,
+                    bool profile, uint32_t* kernels) {
+  cudaStream_t s = d->stream;
+  PassParams P = v.P;
+  P.cover_item = d->tuning.cover_item;
+  P.split_entries = d->tuning.split_entries;
+  uint32_t k = 0;
+  if (!pl.clears.empty()) k += launch_jobs(pl.clears.data(), static_cast<uint32_t>(pl.clears.size()),
+                                           static_cast<uint32_t>(d->num_sms), s);
+  if (!pl.draws.empty()) {
+    if (packed) SG_CUDA(d, cudaMemcpyAsync(v.params, packed->data(), packed->size(), cudaMemcpyHostToDevice, s));
+    SG_CUDA(d, cudaMemsetAsync(P.counters, 0, sizeof(PassCounters), s));
+    SG_CUDA(d, cudaMemsetAsync(P.draw_stats, 0, pl.draws.size() * sizeof(DrawStatsDev), s));
+    if (pl.nprims > 0 && pl.ntiles > 0) {
+      sg_tuning const& tu = d->tuning;
+      uint32_t const sms = static_cast<uint32_t>(d->num_sms);
+      uint32_t merge_grid = std::min<uint32_t>(pl.ntiles, sms * tu.merge_ctas_per_sm);
+      uint32_t cover_grid = std::min<uint32_t>(pl.ntiles * 16, sms * 4);
+      uint32_t shade_grid = sms * tu.shade_ctas_per_sm;
+      cudaEvent_t ev = stage_begin(d, profile);
+      launch_geometry(P, s);
+      stage_end(d, 0, ev);
+      ev = stage_begin(d, profile);
+      SG_CUDA(d, cudaMemsetAsync(P.bin_counts, 0, pl.ncounts * 4, s));
+      launch_bin(P, false, s);
+      launch_scan(P.bin_counts, pl.ncounts, v.scan_sums, P.counters, s);
+      launch_tile_ranges(P, s);
+      launch_bin(P, true, s);
+      stage_end(d, 1, ev);
+      ev = stage_begin(d, profile);
+      launch_cover(P, pl.max_samples, pl.any_early_z, cover_grid, s);
+      stage_end(d, 2, ev);
+      ev = stage_begin(d, profile);
+      for (uint32_t na = 0; na <= SG_MAX_VARYINGS; ++na) {
+        if (!(pl.na_mask & (1u << na))) continue;
+        switch (na) {
+        case 0: launch_shade_0(P, shade_grid, s); break;
+        case 1: launch_shade_1(P, shade_grid, s); break;
+        case 2: launch_shade_2(P, shade_grid, s); break;
+        case 3: launch_shade_3(P, shade_grid, s); break;
+        case 4: launch_shade_4(P, shade_grid, s); break;
+        default: launch_shade_5(P, shade_grid, s); break;
+        }
+        ++k;
+      }
+      stage_end(d, 3, ev);
+      ev = stage_begin(d, profile);
+      launch_merge(P, merge_grid, s);
+      stage_end(d, 4, ev);
+      k += 9;  // geometry, bin count, 3 scan kernels, tile ranges, bin fill, cover, merge
+      d->prof.raster_launches += 1;
+    }
+    d->prof.draws += pl.draws.size();
+  }
+  if (!pl.resolves.empty()) k += launch_jobs(pl.resolves.data(), static_cast<uint32_t>(pl.resolves.size()),
+                                             static_cast<uint32_t>(d->num_sms), s);
+  SG_CUDA(d, cudaGetLastError());
+  *kernels = k;
+  return SG_OK;
+}
+
+// Reads back the counters of the last immediate pass (after a stream sync)
+// and turns an overflow into SG_OUT_OF_MEMORY with raised capacities.
+int32_t check_overflow(sg_device* d, Scratch& sc, PassCounters const& c, bool fixed) {
+  if (!(c.overflow & (OVF_BIN | OVF_FRAG | OVF_REC))) return SG_OK;
+  char msg[256];
+  if (fixed) {
+    std::snprintf(msg, sizeof(msg),
+                  "static scratch exhausted: %u bin entries, %u fragment chunks, %u record units needed",
+                  c.bin_entries, c.chunk_total, c.rec_units);
+  } else {
+    if (c.overflow & OVF_BIN) sc.entry_capacity = std::max<uint32_t>(sc.entry_capacity * 2, c.bin_entries + c.bin_entries / 4);
+    if (c.overflow & OVF_FRAG) sc.chunk_capacity = std::max<uint32_t>(sc.chunk_capacity * 2, c.chunk_total + c.chunk_total / 4);
+    std::snprintf(msg, sizeof(msg), "scratch buffer overflow (bits %u); capacities raised for later passes",
+                  c.overflow);
+  }
+  d->error = msg;
+  return SG_OUT_OF_MEMORY;
+}
+
+// Runs one assembled pass immediately.  `stats` (indexed by command) is
+// filled when given, which synchronises.
+int32_t run_plan(sg_device* d, PassPlan& pl, sg_draw_stats* stats, uint8_t* fixed) {
+  if (pl.empty()) return SG_OK;
+  finalize(pl, d);
+  PlanLayout L = layout_of(pl);
+  std::vector<uint8_t> packed;
+  ScratchView v;
+  if (!pl.draws.empty()) {
+    int32_t r = fixed ? scratch_static(d, fixed, pl, L, v) : scratch_arenas(d, d->scratch, pl, L, true, v);
+    if (r != SG_OK) return r;
+    bind_params(v.P, v.params, L, pl);
+    pack_plan(pl, L, packed);
+  }
+  uint32_t kernels = 0;
+  if (fixed && !pl.draws.empty()) {
+    SG_CUDA(d, cudaMemsetAsync(v.P.sticky, 0, sizeof(unsigned int), d->stream));
+    d->static_sticky = v.P.sticky;
+  }
+  int32_t r = launch_pass(d, pl, v, pl.draws.empty() ? nullptr : &packed, !fixed, &kernels);
+  if (r != SG_OK) return r;
+  d->prof.launches += kernels;
+  if (pl.draws.empty()) return SG_OK;
+  if (!fixed) d->scratch.pending = true;
+  if (!stats) {
+    // the parameter blocks were copied from pageable host memory, which the
+    // copy staged before returning; overflows are reported at sg_sync
+    return SG_OK;
+  }
+  SG_CUDA(d, cudaMemcpyAsync(d->counters_host, v.P.counters, sizeof(PassCounters), cudaMemcpyDeviceToHost, d->stream));
+  if (d->stats_host_cap < pl.draws.size()) {
+    if (d->stats_host) cudaFreeHost(d->stats_host);
+    d->stats_host = nullptr;
+    d->stats_host_cap = 0;
+    SG_CUDA(d, cudaMallocHost(&d->stats_host, pl.draws.size() * sizeof(DrawStatsDev)));
+    d->stats_host_cap = pl.draws.size();
+  }
+  SG_CUDA(d, cudaMemcpyAsync(d->stats_host, v.P.draw_stats, pl.draws.size() * sizeof(DrawStatsDev),
+                             cudaMemcpyDeviceToHost, d->stream));
+  SG_CUDA(d, cudaStreamSynchronize(d->stream));
+  r = check_overflow(d, d->scratch, *d->counters_host, fixed != nullptr);
+  if (r != SG_OK && !fixed) SG_CUDA(d, cudaMemset(v.P.sticky, 0, sizeof(unsigned int)));  // reported here
+  if (r != SG_OK) return r;
+  for (size_t i = 0; i < pl.draws.size(); ++i) {
+    sg_draw_stats& o = stats[pl.draw_cmd[i]];
+    o.ia_primitives = pl.draws[i].prim_count;
+    o.cprimitives = d->stats_host[i].cprimitives;
+    o.ps_invocations = d->stats_host[i].ps_invocations;
+    o.backend_input_pixels = d->stats_host[i].backend_input_pixels;
+  }
+  return SG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// commands -> passes
+
+int32_t make_clear_color_job(sg_device* d, uint32_t h, const float rgba[4], SurfaceJob& j) {
+  Texture* t = find_tex(d, h);
+  if (!t || !rgba || !valid_color_fmt(t->fmt)) return SG_INVALID_PARAMETER;
+  std::memset(&j, 0, sizeof(j));
+  // Convert the colour once on the host with the same rules as the
+  // per-texel conversion (round-half-even, clamp) used by the kernels.
+  uint8_t* pb = reinterpret_cast<uint8_t*>(j.pattern);
+  auto u8 = [](float c) -> uint8_t {
+    float m = c * 255.0f;
+    m = m > 0.0f ? m : 0.0f;
+    m = m < 255.0f ? m : 255.0f;
+    return static_cast<uint8_t>(std::nearbyint(m));
+  };
+  switch (t->fmt) {
+  case SG_FMT_RGBA32F: std::memcpy(pb, rgba, 16); break;
+  case SG_FMT_RGB32F: std::memcpy(pb, rgba, 12); break;
+  case SG_FMT_RG32F: std::memcpy(pb, rgba, 8); break;
+  case SG_FMT_R32F: std::memcpy(pb, rgba, 4); break;
+  case SG_FMT_R32I: {
+    int32_t i = static_cast<int32_t>(rgba[0] + 0.5f);
+    std::memcpy(pb, &i, 4);
+    break;
+  }
+  case SG_FMT_RGBA8: pb[0] = u8(rgba[0]); pb[1] = u8(rgba[1]); pb[2] = u8(rgba[2]); pb[3] = u8(rgba[3]); break;
+  case SG_FMT_BGRA8: pb[0] = u8(rgba[2]); pb[1] = u8(rgba[1]); pb[2] = u8(rgba[0]); pb[3] = u8(rgba[3]); break;
+  case SG_FMT_RGBA16F: {
+    // host-side binary16 conversion, round to nearest even
+    for (int i = 0; i < 4; ++i) {
+      uint32_t x;
+      std::memcpy(&x, &rgba[i], 4);
+      uint32_t sign = (x >> 16) & 0x8000u, exp = (x >> 23) & 0xFFu, man = x & 0x7FFFFFu;
+      uint16_t hv;
+      if (exp == 0xFF) {
+        hv = static_cast<uint16_t>(sign | 0x7C00u | (man ? 0x200u : 0u));
+      } else {
+        int32_t e = static_cast<int32_t>(exp) - 112;
+        if (e >= 31) {
+          hv = static_cast<uint16_t>(sign | 0x7C00u);
+        } else if (e <= 0) {
+          if (e < -10) {
+            hv = static_cast<uint16_t>(sign);
+          } else {
+            man |= 0x800000u;
+            uint32_t sh = static_cast<uint32_t>(14 - e);
+            uint32_t half = man >> sh, rem = man & ((1u << sh) - 1u), mid = 1u << (sh - 1);
+            if (rem > mid || (rem == mid && (half & 1u))) ++half;
+            hv = static_cast<uint16_t>(sign | half);
+          }
+        } else {
+          uint32_t half = (static_cast<uint32_t>(e) << 10) | (man >> 13), rem = man & 0x1FFFu;
+          if (rem > 0x1000u || (rem == 0x1000u && (half & 1u))) ++half;
+          hv = static_cast<uint16_t>(sign | half);
+        }
+      }
+      std::memcpy(pb + 2 * i, &hv, 2);
+    }
+    break;
+  }
+  default: return SG_INVALID_PARAMETER;
+  }
+  Level const& l = t->levels[0];
+  j.kind = JOB_FILL;
+  j.dst = l.ptr;
+  j.n = static_cast<uint64_t>(l.w) * l.h * t->samples;
+  j.esz = t->esz;
+  return SG_OK;
+}
+
+int32_t make_clear_ds_job(sg_device* d, uint32_t h, uint32_t flags, float depth, uint32_t stencil, SurfaceJob& j) {
+  Texture* t = find_tex(d, h);
+  if (!t || !valid_ds_fmt(t->fmt) || flags == 0 || flags > 3) return SG_INVALID_PARAMETER;
+  std::memset(&j, 0, sizeof(j));
+  Level const& l = t->levels[0];
+  j.dst = l.ptr;
+  j.n = static_cast<uint64_t>(l.w) * l.h * t->samples;
+  if (t->fmt == SG_FMT_RG32F && flags == (SG_CLEAR_DEPTH | SG_CLEAR_STENCIL)) {
+    // render_core::clear_depth_stencil fills (depth, bitcast stencil) (render_core.cpp:100-105)
+    j.kind = JOB_FILL;
+    j.esz = 8;
+    std::memcpy(&j.pattern[0], &depth, 4);
+    j.pattern[1] = stencil;
+  } else {
+    j.kind = JOB_CLEAR_DS;
+    j.fmt = t->fmt;
+    j.flags = flags;
+    j.depth = depth;
+    j.stencil = stencil;
+  }
+  return SG_OK;
+}
+
+int32_t make_resolve_job(sg_device* d, uint32_t src, uint32_t dst, SurfaceJob& j) {
+  Texture* a = find_tex(d, src);
+  Texture* b = find_tex(d, dst);
+  if (!a || !b || b->samples != 1 || a->levels[0].w != b->levels[0].w || a->levels[0].h != b->levels[0].h ||
+      !valid_color_fmt(a->fmt) || !valid_color_fmt(b->fmt) || src == dst)
+    return SG_INVALID_PARAMETER;
+  std::memset(&j, 0, sizeof(j));
+  j.kind = JOB_RESOLVE;
+  j.src = a->levels[0].ptr;
+  j.dst = b->levels[0].ptr;
+  j.n = static_cast<uint64_t>(a->levels[0].w) * a->levels[0].h;
+  j.samples = a->samples;
+  j.fmt = a->fmt;
+  j.esz = a->esz;
+  j.dst_fmt = b->fmt;
+  return SG_OK;
+}
+
+// Appends the commands to passes (starting a new pass where order requires)
+// and hands every completed pass to `sink`.
+template <class Sink>
+int32_t plan_commands(sg_device* d, sg_command const* cmds, uint32_t n, Sink&& sink) {
+  PassPlan pl;
+  auto flush = [&]() -> int32_t {
+    if (pl.empty()) return SG_OK;
+    int32_t r = sink(pl);
+    pl = PassPlan();
+    return r;
+  };
+  for (uint32_t i = 0; i < n; ++i) {
+    sg_command const& c = cmds[i];
+    switch (c.type) {
+    case SG_CMD_DRAW: {
+      if (!c.draw) return SG_INVALID_PARAMETER;
+      DrawParams p;
+      DrawInfo info;
+      if (int32_t r = translate_draw(d, c.draw, p, info)) return r;
+      if (!draw_fits(pl, p, info))
+        if (int32_t r = flush()) return r;
+      add_draw(d, pl, p, info, i);
+      break;
+    }
+    case SG_CMD_CLEAR_COLOR:
+    case SG_CMD_CLEAR_DEPTH_STENCIL: {
+      SurfaceJob j;
+      int32_t r = c.type == SG_CMD_CLEAR_COLOR ? make_clear_color_job(d, c.texture, c.color, j)
+                                               : make_clear_ds_job(d, c.texture, c.flags, c.depth, c.stencil, j);
+      if (r) return r;
+      // clears run before the pass's draws: the target may not be drawn,
+      // sampled, resolved or cleared (partially) in it yet
+      if (pl.surfaces.count(c.texture) || pl.sampled.count(c.texture) || pl.resolved.count(c.texture) ||
+          pl.cleared.count(c.texture))
+        if (int32_t rr = flush()) return rr;
+      pl.clears.push_back(j);
+      pl.clear_cmd.push_back(i);
+      pl.cleared.insert(c.texture);
+      break;
+    }
+    case SG_CMD_RESOLVE: {
+      SurfaceJob j;
+      if (int32_t r = make_resolve_job(d, c.texture, c.texture2, j)) return r;
+      // resolves run after the pass's draws: the destination may not be used by it
+      if (pl.surfaces.count(c.texture2) || pl.sampled.count(c.texture2) || pl.resolved.count(c.texture) ||
+          pl.resolved.count(c.texture2) || pl.cleared.count(c.texture2))
+        if (int32_t r = flush()) return r;
+      pl.resolves.push_back(j);
+      pl.resolved.insert(c.texture);
+      pl.resolved.insert(c.texture2);
+      break;
+    }
+    default: return SG_INVALID_PARAMETER;
+    }
+  }
+  return flush();
+}
+
+int32_t submit_impl(sg_device* d, sg_command const* cmds, uint32_t n, sg_draw_stats* stats, uint8_t* fixed) {
+  if (stats) std::memset(stats, 0, sizeof(sg_draw_stats) * n);
+  return plan_commands(d, cmds, n, [&](PassPlan& pl) { return run_plan(d, pl, stats, fixed); });
+}
+
+// After a stream sync: the overflow bits the passes since the last look left
+// in a scratch's sticky word (immediate passes and each graph's).
+int32_t check_sticky(sg_device* d, Scratch& sc, char const* what) {
+  if (!sc.pending || !sc.sticky.ptr) return SG_OK;
+  sc.pending = false;
+  SG_CUDA(d, cudaMemcpy(d->sticky_host, sc.sticky.ptr, sizeof(unsigned int), cudaMemcpyDeviceToHost));
+  unsigned int bits = *d->sticky_host;
+  if (!(bits & (OVF_BIN | OVF_FRAG | OVF_REC))) return SG_OK;
+  SG_CUDA(d, cudaMemset(sc.sticky.ptr, 0, sizeof(unsigned int)));
+  if (&sc == &d->scratch) {
+    PassCounters c{};
+    c.overflow = bits;
+    c.bin_entries = sc.entry_capacity;
+    c.chunk_total = sc.chunk_capacity;
+    return check_overflow(d, sc, c, false);
+  }
+  d->error = what;
+  return SG_OUT_OF_MEMORY;
+}
+
+int32_t check_pending(sg_device* d) {
+  int32_t r = check_sticky(d, d->scratch, "");
+  if (d->static_sticky) {
+    SG_CUDA(d, cudaMemcpy(d->sticky_host, d->static_sticky, sizeof(unsigned int), cudaMemcpyDeviceToHost));
+    d->static_sticky = nullptr;
+    if (*d->sticky_host & (OVF_BIN | OVF_FRAG | OVF_REC)) {
+      d->error = "static scratch exhausted by a draw since the last sync";
+      if (r == SG_OK) r = SG_OUT_OF_MEMORY;
+    }
+  }
+  for (sg_graph* g : d->graphs) {
+    int32_t rg = check_sticky(d, g->scratch, "a recorded graph overflowed its scratch; record it again");
+    if (r == SG_OK) r = rg;
+  }
+  return r;
 }
 
 }  // namespace
@@ -548,9 +1102,10 @@ int32_t sg_device_create(int32_t cuda_device, void* cuda_stream, sg_device** out
     if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess) return SG_CUDA_ERROR;
     d->own_stream = true;
   }
-  if (cudaMalloc(&d->counters, sizeof(DrawCounters)) != cudaSuccess) return SG_OUT_OF_MEMORY;
-  if (cudaMallocHost(&d->counters_host, sizeof(DrawCounters)) != cudaSuccess) return SG_OUT_OF_MEMORY;
-  std::memset(d->counters_host, 0, sizeof(DrawCounters));
+  if (cudaMallocHost(&d->counters_host, sizeof(PassCounters)) != cudaSuccess) return SG_OUT_OF_MEMORY;
+  std::memset(d->counters_host, 0, sizeof(PassCounters));
+  if (cudaMallocHost(&d->sticky_host, sizeof(unsigned int)) != cudaSuccess) return SG_OUT_OF_MEMORY;
+  if (init_cover() != cudaSuccess) return SG_CUDA_ERROR;
   float tab[256];
   make_ewa_table(tab);
   for (auto up : {upload_ewa_table_raster_a, upload_ewa_table_raster_b, upload_ewa_table_raster_c})
@@ -565,15 +1120,14 @@ void sg_device_destroy(sg_device* d) {
   if (!d) return;
   cudaSetDevice(d->ordinal);
   cudaStreamSynchronize(d->stream);
+  for (sg_graph* g : std::vector<sg_graph*>(d->graphs.begin(), d->graphs.end())) sg_graph_destroy(d, g);
   for (auto& b : d->buffers) cudaFree(b.second.ptr);
   for (auto& t : d->textures)
     for (auto& l : t.second.levels) cudaFree(l.ptr);
-  for (Arena* a : {&d->slot_rec, &d->recs, &d->bin_counts, &d->scan_sums, &d->bin_entries, &d->tile_begin,
-                   &d->frag_rec, &d->frag_pos, &d->frag_mask, &d->frag_color, &d->frag_ps, &d->chunk_next,
-                   &d->chunk_count, &d->owner_first})
-    a->release();
-  cudaFree(d->counters);
+  d->scratch.release();
   cudaFreeHost(d->counters_host);
+  cudaFreeHost(d->sticky_host);
+  if (d->stats_host) cudaFreeHost(d->stats_host);
   for (cudaEvent_t e : d->event_pool) cudaEventDestroy(e);
   if (d->own_stream) cudaStreamDestroy(d->stream);
   delete d;
@@ -582,15 +1136,7 @@ void sg_device_destroy(sg_device* d) {
 int32_t sg_sync(sg_device* d) {
   if (!d) return SG_INVALID_PARAMETER;
   SG_CUDA(d, cudaStreamSynchronize(d->stream));
-  DrawCounters& c = *d->counters_host;
-  if (c.overflow & 5u) {
-    if (c.overflow & 1u) d->entry_capacity = std::max<uint32_t>(d->entry_capacity * 2, c.bin_entries + 1024);
-    if (c.overflow & 4u) d->chunk_capacity = std::max<uint32_t>(d->chunk_capacity * 2, c.chunk_total + 1024);
-    c.overflow = 0;
-    d->error = "scratch buffer overflow; capacities raised for later draws";
-    return SG_OUT_OF_MEMORY;
-  }
-  return SG_OK;
+  return check_pending(d);
 }
 
 const char* sg_last_error(sg_device* d) { return d ? d->error.c_str() : ""; }
@@ -706,6 +1252,7 @@ int32_t sg_texture_gen_mipmap(sg_device* d, uint32_t h, uint32_t filter) {
     ++n;
   }
   if (n > static_cast<uint32_t>(SG_MAX_LEVELS)) return SG_INVALID_PARAMETER;
+  SG_CUDA(d, cudaStreamSynchronize(d->stream));
   for (size_t i = 1; i < t->levels.size(); ++i) cudaFree(t->levels[i].ptr);
   t->levels.resize(1);
   for (uint32_t i = 1; i < n; ++i) {
@@ -757,7 +1304,10 @@ int32_t sg_sampler_destroy(sg_device* d, uint32_t h) {
 
 int32_t sg_draw(sg_device* d, const sg_draw_desc* desc, sg_draw_stats* stats) {
   if (!d || !desc) return SG_INVALID_PARAMETER;
-  return draw_impl(d, desc, stats);
+  sg_command c{};
+  c.type = SG_CMD_DRAW;
+  c.draw = desc;
+  return submit_impl(d, &c, 1, stats, nullptr);
 }
 
 int32_t sg_draw_static_scratch(sg_device* d, const sg_draw_desc* desc, sg_draw_stats* stats) {
@@ -770,106 +1320,244 @@ int32_t sg_draw_static_scratch(sg_device* d, const sg_draw_desc* desc, sg_draw_s
     d->error = "sg_draw_static_scratch: static scratch address lookup failed";
     return SG_CUDA_ERROR;
   }
-  return draw_impl(d, desc, stats, base);
+  sg_command c{};
+  c.type = SG_CMD_DRAW;
+  c.draw = desc;
+  return submit_impl(d, &c, 1, stats, base);
+}
+
+int32_t sg_submit(sg_device* d, const sg_command* cmds, uint32_t n, sg_draw_stats* stats) {
+  if (!d || (!cmds && n)) return SG_INVALID_PARAMETER;
+  return submit_impl(d, cmds, n, stats, nullptr);
 }
 
 // render_core::clear_color -> surface::fill (render_core.cpp:96-99, surface.cpp:170-275)
 int32_t sg_clear_color(sg_device* d, uint32_t h, const float rgba[4]) {
-  Texture* t = d ? find_tex(d, h) : nullptr;
-  if (!t || !rgba || !valid_color_fmt(t->fmt)) return SG_INVALID_PARAMETER;
-  // Convert the colour once on the host with the same rules as the
-  // per-texel conversion (round-half-even, clamp) used by the kernels.
-  uint4 pat{0, 0, 0, 0};
-  uint8_t* pb = reinterpret_cast<uint8_t*>(&pat);
-  auto u8 = [](float c) -> uint8_t {
-    float m = c * 255.0f;
-    m = m > 0.0f ? m : 0.0f;
-    m = m < 255.0f ? m : 255.0f;
-    return static_cast<uint8_t>(std::nearbyint(m));
-  };
-  switch (t->fmt) {
-  case SG_FMT_RGBA32F: std::memcpy(pb, rgba, 16); break;
-  case SG_FMT_RGB32F: std::memcpy(pb, rgba, 12); break;
-  case SG_FMT_RG32F: std::memcpy(pb, rgba, 8); break;
-  case SG_FMT_R32F: std::memcpy(pb, rgba, 4); break;
-  case SG_FMT_R32I: {
-    int32_t i = static_cast<int32_t>(rgba[0] + 0.5f);
-    std::memcpy(pb, &i, 4);
-    break;
-  }
-  case SG_FMT_RGBA8: pb[0] = u8(rgba[0]); pb[1] = u8(rgba[1]); pb[2] = u8(rgba[2]); pb[3] = u8(rgba[3]); break;
-  case SG_FMT_BGRA8: pb[0] = u8(rgba[2]); pb[1] = u8(rgba[1]); pb[2] = u8(rgba[0]); pb[3] = u8(rgba[3]); break;
-  case SG_FMT_RGBA16F: {
-    // host-side binary16 conversion, round to nearest even
-    for (int i = 0; i < 4; ++i) {
-      uint32_t x;
-      std::memcpy(&x, &rgba[i], 4);
-      uint32_t sign = (x >> 16) & 0x8000u, exp = (x >> 23) & 0xFFu, man = x & 0x7FFFFFu;
-      uint16_t hv;
-      if (exp == 0xFF) {
-        hv = static_cast<uint16_t>(sign | 0x7C00u | (man ? 0x200u : 0u));
-      } else {
-        int32_t e = static_cast<int32_t>(exp) - 112;
-        if (e >= 31) {
-          hv = static_cast<uint16_t>(sign | 0x7C00u);
-        } else if (e <= 0) {
-          if (e < -10) {
-            hv = static_cast<uint16_t>(sign);
-          } else {
-            man |= 0x800000u;
-            uint32_t sh = static_cast<uint32_t>(14 - e);
-            uint32_t half = man >> sh, rem = man & ((1u << sh) - 1u), mid = 1u << (sh - 1);
-            if (rem > mid || (rem == mid && (half & 1u))) ++half;
-            hv = static_cast<uint16_t>(sign | half);
-          }
-        } else {
-          uint32_t half = (static_cast<uint32_t>(e) << 10) | (man >> 13), rem = man & 0x1FFFu;
-          if (rem > 0x1000u || (rem == 0x1000u && (half & 1u))) ++half;
-          hv = static_cast<uint16_t>(sign | half);
-        }
-      }
-      std::memcpy(pb + 2 * i, &hv, 2);
-    }
-    break;
-  }
-  default: return SG_INVALID_PARAMETER;
-  }
-  Level const& l = t->levels[0];
-  launch_fill(l.ptr, static_cast<size_t>(l.w) * l.h * t->samples, t->esz, pat, d->stream);
-  d->prof.launches += 1;
-  SG_CUDA(d, cudaGetLastError());
-  return SG_OK;
+  if (!d) return SG_INVALID_PARAMETER;
+  sg_command c{};
+  c.type = SG_CMD_CLEAR_COLOR;
+  c.texture = h;
+  if (!rgba) return SG_INVALID_PARAMETER;
+  std::memcpy(c.color, rgba, sizeof(c.color));
+  return submit_impl(d, &c, 1, nullptr, nullptr);
 }
 
 // render_core::clear_depth_stencil (render_core.cpp:100-111)
 int32_t sg_clear_depth_stencil(sg_device* d, uint32_t h, uint32_t flags, float depth, uint32_t stencil) {
-  Texture* t = d ? find_tex(d, h) : nullptr;
-  if (!t || !valid_ds_fmt(t->fmt) || flags == 0 || flags > 3) return SG_INVALID_PARAMETER;
-  Level const& l = t->levels[0];
-  size_t n = static_cast<size_t>(l.w) * l.h * t->samples;
-  if (t->fmt == SG_FMT_RG32F && flags == (SG_CLEAR_DEPTH | SG_CLEAR_STENCIL)) {
-    uint4 pat{0, 0, 0, 0};
-    std::memcpy(&pat.x, &depth, 4);
-    pat.y = stencil;
-    launch_fill(l.ptr, n, 8, pat, d->stream);
-  } else {
-    launch_clear_ds(l.ptr, n, t->fmt, flags, depth, stencil, d->stream);
-  }
-  d->prof.launches += 1;
-  SG_CUDA(d, cudaGetLastError());
-  return SG_OK;
+  if (!d) return SG_INVALID_PARAMETER;
+  sg_command c{};
+  c.type = SG_CMD_CLEAR_DEPTH_STENCIL;
+  c.texture = h;
+  c.flags = flags;
+  c.depth = depth;
+  c.stencil = stencil;
+  return submit_impl(d, &c, 1, nullptr, nullptr);
 }
 
 int32_t sg_resolve(sg_device* d, uint32_t src, uint32_t dst) {
-  Texture* a = d ? find_tex(d, src) : nullptr;
-  Texture* b = d ? find_tex(d, dst) : nullptr;
-  if (!a || !b || b->samples != 1 || a->levels[0].w != b->levels[0].w || a->levels[0].h != b->levels[0].h ||
-      !valid_color_fmt(a->fmt) || !valid_color_fmt(b->fmt))
+  if (!d) return SG_INVALID_PARAMETER;
+  sg_command c{};
+  c.type = SG_CMD_RESOLVE;
+  c.texture = src;
+  c.texture2 = dst;
+  return submit_impl(d, &c, 1, nullptr, nullptr);
+}
+
+// ---- recorded graphs --------------------------------------------------------
+int32_t sg_graph_create(sg_device* d, const sg_command* cmds, uint32_t n, sg_graph** out) {
+  if (!d || !out || (!cmds && n)) return SG_INVALID_PARAMETER;
+  *out = nullptr;
+  auto g = std::make_unique<sg_graph>();
+  // 1. plan the passes
+  int32_t r = plan_commands(d, cmds, n, [&](PassPlan& pl) {
+    finalize(pl, d);
+    g->plans.push_back(pl);
+    return SG_OK;
+  });
+  if (r != SG_OK) return r;
+  // 2. run the list once to learn each pass's needs
+  SG_CUDA(d, cudaStreamSynchronize(d->stream));
+  uint32_t need_entries = 1, need_chunks = 1;
+  for (PassPlan& pl : g->plans) {
+    PassPlan run = pl;
+    for (int attempt = 0;; ++attempt) {
+      std::vector<sg_draw_stats> st(n);
+      r = run_plan(d, run, st.data(), nullptr);
+      if (r == SG_OK) break;
+      if (r != SG_OUT_OF_MEMORY || attempt >= 4) return r;
+      run = pl;  // capacities were raised; the overflowing pass left its targets untouched only on
+                 // bin or record overflow, so a fragment overflow here is reported to the caller
+      if (d->counters_host->overflow & OVF_FRAG) return r;
+    }
+    need_entries = std::max(need_entries, d->counters_host->bin_entries);
+    need_chunks = std::max(need_chunks, d->counters_host->chunk_total);
+  }
+  g->scratch.entry_capacity = need_entries + need_entries / 4 + 1024;
+  g->scratch.chunk_capacity = need_chunks + need_chunks / 4 + 256;
+  // 3. parameter blocks of every pass, resident
+  std::vector<PlanLayout> layouts;
+  size_t total = 0;
+  for (PassPlan const& pl : g->plans) {
+    layouts.push_back(layout_of(pl));
+    total += layouts.back().bytes;
+  }
+  SG_CUDA(d, g->params.ensure(std::max<size_t>(total, 256)));
+  std::vector<ScratchView> views(g->plans.size());
+  size_t off = 0;
+  for (size_t i = 0; i < g->plans.size(); ++i) {
+    PassPlan const& pl = g->plans[i];
+    if (!pl.draws.empty()) {
+      r = scratch_arenas(d, g->scratch, pl, layouts[i], false, views[i]);
+      if (r != SG_OK) return r;
+      views[i].params = static_cast<uint8_t*>(g->params.ptr) + off;
+      bind_params(views[i].P, views[i].params, layouts[i], pl);
+      std::vector<uint8_t> packed;
+      pack_plan(pl, layouts[i], packed);
+      SG_CUDA(d, cudaMemcpy(views[i].params, packed.data(), packed.size(), cudaMemcpyHostToDevice));
+    }
+    off += layouts[i].bytes;
+  }
+  // every pass binds the same (largest) scratch arenas; rebind after all growth
+  for (size_t i = 0; i < g->plans.size(); ++i) {
+    if (g->plans[i].draws.empty()) continue;
+    uint8_t* params = views[i].params;
+    r = scratch_arenas(d, g->scratch, g->plans[i], layouts[i], false, views[i]);
+    if (r != SG_OK) return r;
+    views[i].params = params;
+    bind_params(views[i].P, params, layouts[i], g->plans[i]);
+  }
+  // 4. capture
+  SG_CUDA(d, cudaStreamSynchronize(d->stream));
+  SG_CUDA(d, cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
+  uint32_t kernels = 0;
+  bool saved = d->profiling;
+  d->profiling = false;
+  for (size_t i = 0; i < g->plans.size() && r == SG_OK; ++i) {
+    uint32_t k = 0;
+    r = launch_pass(d, g->plans[i], views[i], nullptr, false, &k);
+    kernels += k;
+  }
+  d->profiling = saved;
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(d->stream, &graph);
+  if (r != SG_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return r;
+  }
+  if (e != cudaSuccess) return cuda_fail(d, e, "cudaStreamEndCapture");
+  g->graph = graph;
+  e = cudaGraphInstantiate(&g->exec, graph, 0);
+  if (e != cudaSuccess) return cuda_fail(d, e, "cudaGraphInstantiate");
+  g->kernels = kernels;
+  *out = g.release();
+  d->graphs.insert(*out);
+  return SG_OK;
+}
+
+int32_t sg_graph_launch(sg_device* d, sg_graph* g) {
+  if (!d || !g || !d->graphs.count(g)) return SG_INVALID_PARAMETER;
+  SG_CUDA(d, cudaGraphLaunch(g->exec, d->stream));
+  g->scratch.pending = true;
+  d->prof.launches += g->kernels;
+  return SG_OK;
+}
+
+int32_t sg_graph_info(sg_device* d, sg_graph* g, uint32_t* passes, uint32_t* kernels) {
+  if (!d || !g || !d->graphs.count(g)) return SG_INVALID_PARAMETER;
+  if (passes) *passes = static_cast<uint32_t>(g->plans.size());
+  if (kernels) *kernels = g->kernels;
+  return SG_OK;
+}
+
+void sg_graph_destroy(sg_device* d, sg_graph* g) {
+  if (!d || !g || !d->graphs.count(g)) return;
+  cudaStreamSynchronize(d->stream);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  g->scratch.release();
+  g->params.release();
+  d->graphs.erase(g);
+  delete g;
+}
+
+// ---- tuning -------------------------------------------------------------------
+int32_t sg_get_tuning(sg_device* d, sg_tuning* out) {
+  if (!d || !out) return SG_INVALID_PARAMETER;
+  *out = d->tuning;
+  return SG_OK;
+}
+
+int32_t sg_set_tuning(sg_device* d, const sg_tuning* t) {
+  if (!d || !t) return SG_INVALID_PARAMETER;
+  if ((t->cover_item != 16 && t->cover_item != 32) || t->bin_chunk < BIN_CHUNK_MIN ||
+      (t->bin_chunk & (t->bin_chunk - 1)) || t->bin_capacity == 0 || t->frag_chunks == 0 ||
+      t->shade_quads_per_warp != 8 || t->shade_ctas_per_sm == 0 || t->shade_ctas_per_sm > 32 ||
+      t->merge_ctas_per_sm == 0 || t->merge_ctas_per_sm > 8)
     return SG_INVALID_PARAMETER;
-  launch_resolve(a->levels[0].ptr, b->levels[0].ptr, a->levels[0].w * a->levels[0].h, a->samples, a->fmt, b->fmt,
-                 d->stream);
-  d->prof.launches += 1;
-  SG_CUDA(d, cudaGetLastError());
+  d->tuning = *t;
+  d->scratch.entry_capacity = std::max(d->scratch.entry_capacity, t->bin_capacity);
+  d->scratch.chunk_capacity = std::max(d->scratch.chunk_capacity, t->frag_chunks);
+  return SG_OK;
+}
+
+int32_t sg_autotune(sg_device* d, const sg_command* cmds, uint32_t n, uint32_t reps, sg_tuning* out,
+                    float* best_ms) {
+  if (!d || (!cmds && n) || reps == 0) return SG_INVALID_PARAMETER;
+  cudaEvent_t e0, e1;
+  SG_CUDA(d, cudaEventCreate(&e0));
+  SG_CUDA(d, cudaEventCreate(&e1));
+  // time of the list under tuning t (one warm-up, then `reps` runs)
+  auto time_of = [&](sg_tuning const& t, float& ms) -> int32_t {
+    d->tuning = t;
+    int32_t r = submit_impl(d, cmds, n, nullptr, nullptr);
+    if (r == SG_OK) r = sg_sync(d);
+    if (r != SG_OK) return r;
+    cudaEventRecord(e0, d->stream);
+    for (uint32_t i = 0; i < reps && r == SG_OK; ++i) r = submit_impl(d, cmds, n, nullptr, nullptr);
+    cudaEventRecord(e1, d->stream);
+    if (r == SG_OK) r = sg_sync(d);
+    if (r != SG_OK) return r;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= static_cast<float>(reps);
+    return SG_OK;
+  };
+  // coordinate descent over the parameters, two sweeps
+  sg_tuning best_t = d->tuning;
+  float best = 0.0f;
+  int32_t r = time_of(best_t, best);
+  for (int sweep = 0; sweep < 2 && r == SG_OK; ++sweep) {
+    for (int param = 0; param < 5 && r == SG_OK; ++param) {
+      std::vector<uint32_t> vals;
+      switch (param) {
+      case 0: vals = {16u, 32u}; break;
+      case 1: vals = {160u, 320u, 640u, 1280u}; break;
+      case 2: vals = {256u, 512u, 1024u, 2048u}; break;
+      case 3: vals = {4u, 8u, 16u}; break;
+      default: vals = {2u, 3u, 6u}; break;
+      }
+      for (uint32_t v : vals) {
+        sg_tuning t = best_t;
+        uint32_t* field = param == 0 ? &t.cover_item : param == 1 ? &t.split_entries : param == 2 ? &t.bin_chunk
+                          : param == 3 ? &t.shade_ctas_per_sm : &t.merge_ctas_per_sm;
+        if (*field == v) continue;
+        if (param == 1 && t.cover_item == 16) continue;  // every item is 16x16 already
+        *field = v;
+        float ms = 0.0f;
+        r = time_of(t, ms);
+        if (r != SG_OK) break;
+        if (ms < best) {
+          best = ms;
+          best_t = t;
+        }
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  d->tuning = best_t;
+  if (r != SG_OK) return r;
+  if (out) *out = best_t;
+  if (best_ms) *best_ms = best;
   return SG_OK;
 }
 

@@ -1,19 +1,15 @@
-// sg_draw.cu -- the draw pipeline as sm_103a kernels.
+// sg_draw.cu -- geometry and binning kernels of a pass.
 //
-//   k_geometry   one thread per input primitive: index fetch, vertex shader,
-//                near/far clipping and culling, viewport transform and
-//                projection, triangle setup -> compact triangle records.
-//   k_bin<count/fill>   one warp per chunk of triangle slots, walking them in
-//                API order: the reference's per-tile trivial reject/accept
-//                test, emitted into per-(tile, chunk) runs so that every
-//                tile list comes out in API order without a sort.
+//   k_geometry   one thread per input primitive of the pass (all draws):
+//                index fetch, vertex shader, near/far clipping and culling,
+//                viewport transform and projection, triangle setup ->
+//                compact triangle records in slot order.
+//   k_bin<count/fill>   one warp per chunk of a target's triangle slots,
+//                walking them in API order: the reference's per-tile trivial
+//                reject/accept test, emitted into per-(tile, chunk) runs so
+//                that every tile list comes out in API order without a sort.
 //   k_scan_*     exclusive scan of the per-(tile, chunk) counts.
-//   k_raster     one CTA per 64x64 tile (dynamically scheduled); each thread
-//                owns a 4x4 pixel block and replays the reference's 64->16->4
-//                classification, quad coverage and early-Z for its block in
-//                primitive order, emitting quad fragments; fragments are
-//                shaded in parallel (4 lanes per quad, derivatives by
-//                shuffle) and merged by their owners in primitive order.
+//   k_tile_ranges  per tile [begin, end) into the bin entries.
 #include <cuda_runtime.h>
 
 #include "sg_draw.cuh"
@@ -29,30 +25,30 @@ struct vtx {
 
 // Reads past the end of a buffer are undefined in the reference; here they
 // read zeros and are counted in fetch_oob.
-__device__ inline uint32_t fetch_index(DrawParams const& p, uint32_t id) {
-  if (!p.index_base) return id + static_cast<uint32_t>(p.base_vertex);
-  if (id >= p.index_count) {
-    atomicAdd(&p.counters->fetch_oob, 1u);
-    return static_cast<uint32_t>(p.base_vertex);
+__device__ inline uint32_t fetch_index(PassParams const& P, DrawParams const& D, uint32_t id) {
+  if (!D.index_base) return id + static_cast<uint32_t>(D.base_vertex);
+  if (id >= D.index_count) {
+    atomicAdd(&P.counters->fetch_oob, 1u);
+    return static_cast<uint32_t>(D.base_vertex);
   }
-  uint32_t v = p.index_stride == 2 ? reinterpret_cast<uint16_t const*>(p.index_base)[id]
-                                   : reinterpret_cast<uint32_t const*>(p.index_base)[id];
-  return v + static_cast<uint32_t>(p.base_vertex);
+  uint32_t v = D.index_stride == 2 ? reinterpret_cast<uint16_t const*>(D.index_base)[id]
+                                   : reinterpret_cast<uint32_t const*>(D.index_base)[id];
+  return v + static_cast<uint32_t>(D.base_vertex);
 }
 
 // stream_assembler::fetch_vertex / get_vec4 (stream_assembler.cpp:26-93)
-__device__ inline v4 fetch_input(DrawParams const& p, int r, uint32_t index) {
-  uint32_t slot = p.in_slot[r];
-  uint64_t off = static_cast<uint64_t>(p.stream_stride[slot]) * index + p.in_off[r];
-  uint32_t n = p.in_fmt[r] == SG_VFMT_R32_FLOAT ? 4 : p.in_fmt[r] == SG_VFMT_R32G32_FLOAT ? 8
-             : p.in_fmt[r] == SG_VFMT_R32G32B32_FLOAT ? 12 : 16;
-  if (off + n > p.stream_bytes[slot] || (off & 3)) {
-    atomicAdd(&p.counters->fetch_oob, 1u);
+__device__ inline v4 fetch_input(PassParams const& P, DrawParams const& D, int r, uint32_t index) {
+  uint32_t slot = D.in_slot[r];
+  uint64_t off = static_cast<uint64_t>(D.stream_stride[slot]) * index + D.in_off[r];
+  uint32_t n = D.in_fmt[r] == SG_VFMT_R32_FLOAT ? 4 : D.in_fmt[r] == SG_VFMT_R32G32_FLOAT ? 8
+             : D.in_fmt[r] == SG_VFMT_R32G32B32_FLOAT ? 12 : 16;
+  if (off + n > D.stream_bytes[slot] || (off & 3)) {
+    atomicAdd(&P.counters->fetch_oob, 1u);
     return mk4(0, 0, 0, 0);
   }
-  float const* f = reinterpret_cast<float const*>(p.stream_base[slot] + off);
-  float dw = p.in_dw[r];
-  switch (p.in_fmt[r]) {
+  float const* f = reinterpret_cast<float const*>(D.stream_base[slot] + off);
+  float dw = D.in_dw[r];
+  switch (D.in_fmt[r]) {
   case SG_VFMT_R32_FLOAT: return mk4(f[0], 0.0f, 0.0f, dw);
   case SG_VFMT_R32G32_FLOAT: return mk4(f[0], f[1], 0.0f, dw);
   case SG_VFMT_R32G32B32_FLOAT: return mk4(f[0], f[1], f[2], dw);
@@ -69,26 +65,26 @@ __device__ inline v4 transform(v4 v, float const* m) {
 }
 
 template <int NA>
-__device__ void run_vs(DrawParams const& p, uint32_t index, vtx<NA>& out) {
+__device__ void run_vs(PassParams const& P, DrawParams const& D, uint32_t index, vtx<NA>& out) {
   v4 in[SG_MAX_VS_INPUTS];
 #pragma unroll
   for (int r = 0; r < SG_MAX_VS_INPUTS; ++r) in[r] = mk4(0, 0, 0, 0);
-  for (int r = 0; r < static_cast<int>(p.num_inputs); ++r) in[r] = fetch_input(p, r, index);
-  switch (p.vs_prog) {
+  for (int r = 0; r < static_cast<int>(D.num_inputs); ++r) in[r] = fetch_input(P, D, r, index);
+  switch (D.vs_prog) {
   case SG_VS_TRANSFORM:
-    out.r[0] = transform(in[0], p.vs_k);
+    out.r[0] = transform(in[0], D.vs_k);
 #pragma unroll
     for (int i = 0; i < NA; ++i) out.r[1 + i] = in[1 + i];
     break;
   case SG_VS_MORPH_DISPLACE: {
-    v4 pp = in[0] + (in[1] - in[0]) * p.vs_k[16];
+    v4 pp = in[0] + (in[1] - in[0]) * D.vs_k[16];
     v4 n = in[2];
-    float h = sample_impl(p.vs_samp, in[3].x, in[3].y, 0.0f, nullptr).x;
-    float hs = h * p.vs_k[17];
+    float h = sample_impl(D.vs_samp, in[3].x, in[3].y, 0.0f, nullptr).x;
+    float hs = h * D.vs_k[17];
     pp.x = pp.x + n.x * hs;
     pp.y = pp.y + n.y * hs;
     pp.z = pp.z + n.z * hs;
-    out.r[0] = transform(pp, p.vs_k);
+    out.r[0] = transform(pp, D.vs_k);
     if constexpr (NA > 0) out.r[1] = in[3];
     if constexpr (NA > 1) out.r[2] = n;
 #pragma unroll
@@ -104,20 +100,20 @@ __device__ void run_vs(DrawParams const& p, uint32_t index, vtx<NA>& out) {
 }
 
 // cull functions (raster_state.cpp:10-32)
-__device__ inline bool cull(DrawParams const& p, float area) {
-  if (p.cull_mode == SG_CULL_NONE) return false;
-  bool cull_ccw = (p.cull_mode == SG_CULL_FRONT) ? (p.front_ccw != 0) : (p.front_ccw == 0);
+__device__ inline bool cull(DrawParams const& D, float area) {
+  if (D.cull_mode == SG_CULL_NONE) return false;
+  bool cull_ccw = (D.cull_mode == SG_CULL_FRONT) ? (D.front_ccw != 0) : (D.front_ccw == 0);
   return cull_ccw ? (area <= 0) : (area >= 0);
 }
 
 // vs_output_op lerp_n (shader.cpp:170-180)
 template <int NA>
-__device__ inline void vtx_lerp(DrawParams const& p, vtx<NA>& out, vtx<NA> const& a, vtx<NA> const& b, float t) {
+__device__ inline void vtx_lerp(DrawParams const& D, vtx<NA>& out, vtx<NA> const& a, vtx<NA> const& b, float t) {
   out.r[0] = a.r[0] + (b.r[0] - a.r[0]) * t;
 #pragma unroll
   for (int i = 0; i < NA; ++i) {
     out.r[1 + i] = a.r[1 + i];
-    if (!(p.mods[i] & SG_AM_NOINTERPOLATION)) out.r[1 + i] = out.r[1 + i] + (b.r[1 + i] - a.r[1 + i]) * t;
+    if (!(D.mods[i] & SG_AM_NOINTERPOLATION)) out.r[1 + i] = out.r[1 + i] + (b.r[1 + i] - a.r[1 + i]) * t;
   }
 }
 
@@ -128,24 +124,23 @@ __device__ inline float clip_d(int plane, v4 q) {  // dot_prod4 with planes (0,0
 
 // viewport_transform + project_n (shader.cpp:499-511, 117-134)
 template <int NA>
-__device__ inline void vp_project(DrawParams const& p, vtx<NA>& v) {
+__device__ inline void vp_project(DrawParams const& D, vtx<NA>& v) {
   v4 q = v.r[0];
   float invw = eq_eps(q.w, 0.0f) ? 1.0f : 1.0f / q.w;
   v4 pos = q * invw;
-  float ox = (p.vp_x + p.vp_w) * 0.5f;
-  float oy = (p.vp_y + p.vp_h) * 0.5f;
-  v.r[0] = mk4((p.vp_w * 0.5f) * pos.x + ox, (p.vp_h * 0.5f) * -pos.y + oy,
-               (p.vp_maxz - p.vp_minz) * pos.z + p.vp_minz, invw);
+  float ox = (D.vp_x + D.vp_w) * 0.5f;
+  float oy = (D.vp_y + D.vp_h) * 0.5f;
+  v.r[0] = mk4((D.vp_w * 0.5f) * pos.x + ox, (D.vp_h * 0.5f) * -pos.y + oy,
+               (D.vp_maxz - D.vp_minz) * pos.z + D.vp_minz, invw);
 #pragma unroll
   for (int i = 0; i < NA; ++i)
-    if (!(p.mods[i] & SG_AM_NOPERSPECTIVE)) v.r[1 + i] = v.r[1 + i] * invw;
+    if (!(D.mods[i] & SG_AM_NOPERSPECTIVE)) v.r[1 + i] = v.r[1 + i] * invw;
 }
 
 // rasterizer::compute_triangle_info (rasterizer.cpp:864-945) + compute_derivative_n
 // (shader.cpp:414-449); writes the record, returns false for zero area.
 template <int NA>
-__device__ bool setup_triangle(DrawParams const& p, vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c,
-                               float4* rec) {
+__device__ bool setup_triangle(uint32_t draw, vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c, float4* rec) {
   vtx<NA> const* verts[3] = {&a, &b, &c};
   double dist[3];
 #pragma unroll
@@ -174,7 +169,7 @@ __device__ bool setup_triangle(DrawParams const& p, vtx<NA> const& a, vtx<NA> co
     rec[i] = make_float4(s.y - e.y, e.x - s.x, e.x * s.y - e.y * s.x, 0.0f);
   }
   rec[3] = bb;
-  rec[4] = make_float4(area > 0.0f ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f);
+  rec[4] = make_float4(area > 0.0f ? 1.0f : 0.0f, __uint_as_float(draw), 0.0f, 0.0f);
   float e01x = e01p.x, e01y = e01p.y, e02x = e02p.x, e02y = e02p.y;
   constexpr int R = 1 + NA;
 #pragma unroll
@@ -196,157 +191,186 @@ __device__ bool setup_triangle(DrawParams const& p, vtx<NA> const& a, vtx<NA> co
 }
 
 template <int NA>
-__device__ void emit_triangle(DrawParams const& p, uint32_t slot, vtx<NA> a, vtx<NA> b, vtx<NA> c,
-                              unsigned long long& ntri) {
+__device__ void emit_triangle(PassParams const& P, DrawParams const& D, uint32_t draw, uint32_t slot, vtx<NA> a,
+                              vtx<NA> b, vtx<NA> c, uint32_t& ntri) {
   ++ntri;
-  vp_project(p, a);
-  vp_project(p, b);
-  vp_project(p, c);
-  alignas(16) float4 rec[rec_stride_for(NA)];
-  bool ok = setup_triangle(p, a, b, c, rec);
+  vp_project(D, a);
+  vp_project(D, b);
+  vp_project(D, c);
+  constexpr uint32_t STRIDE = rec_stride_for(NA);
+  alignas(16) float4 rec[STRIDE];
+  bool ok = setup_triangle(draw, a, b, c, rec);
   uint32_t idx = NO_REC;
   if (ok) {
-    idx = atomicAdd(&p.counters->rec_count, 1u);
-    float4* dst = p.recs + static_cast<size_t>(idx) * p.rec_stride;
+    idx = atomicAdd(&P.counters->rec_units, STRIDE);
+    if (idx > P.rec_capacity - STRIDE || P.rec_capacity < STRIDE) {
+      atomicOr(&P.counters->overflow, OVF_REC);
+      idx = NO_REC;
+    } else {
+      float4* dst = P.recs + idx;
 #pragma unroll
-    for (int i = 0; i < static_cast<int>(rec_stride_for(NA)); ++i) dst[i] = rec[i];
+      for (int i = 0; i < static_cast<int>(STRIDE); ++i) dst[i] = rec[i];
+    }
   }
-  p.slot_rec[slot] = idx;
+  P.slot_rec[slot] = idx;
 }
 
 // clipper::clip_solid_triangle + clip_triangle_to_poly_general (clipper.cpp:43-228)
 template <int NA>
-__global__ void __launch_bounds__(128) k_geometry(DrawParams p) {
-  uint32_t prim = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long ntri = 0;
-  if (prim < p.prim_count) {
-    uint32_t ids[3];
-    if (p.strip) {
-      ids[0] = prim;
-      ids[1] = prim + 1;
-      ids[2] = prim + 2;
-      if (prim & 1) {
-        uint32_t t = ids[0];
-        ids[0] = ids[2];
-        ids[2] = t;
-      }
-    } else {
-      ids[0] = prim * 3;
-      ids[1] = prim * 3 + 1;
-      ids[2] = prim * 3 + 2;
+__device__ void geometry_prim(PassParams const& P, DrawParams const& D, uint32_t draw, uint32_t prim,
+                              uint32_t& ntri) {
+  uint32_t ids[3];
+  if (D.strip) {
+    ids[0] = prim;
+    ids[1] = prim + 1;
+    ids[2] = prim + 2;
+    if (prim & 1) {
+      uint32_t t = ids[0];
+      ids[0] = ids[2];
+      ids[2] = t;
     }
-    vtx<NA> tv[3];
+  } else {
+    ids[0] = prim * 3;
+    ids[1] = prim * 3 + 1;
+    ids[2] = prim * 3 + 2;
+  }
+  vtx<NA> tv[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) run_vs(p, fetch_index(p, ids[i]), tv[i]);
-    uint32_t slot0 = prim * 3;
-    p.slot_rec[slot0 + 1] = NO_REC;
-    p.slot_rec[slot0 + 2] = NO_REC;
-    bool in_frustum = true;
+  for (int i = 0; i < 3; ++i) run_vs(P, D, fetch_index(P, D, ids[i]), tv[i]);
+  uint32_t slot0 = D.slot_base + prim * 3;
+  P.slot_rec[slot0 + 1] = NO_REC;
+  P.slot_rec[slot0 + 2] = NO_REC;
+  bool in_frustum = true;
 #pragma unroll
-    for (int pl = 0; pl < 2; ++pl)
+  for (int pl = 0; pl < 2; ++pl)
 #pragma unroll
-      for (int v = 0; v < 3; ++v)
-        if (clip_d(pl, tv[v].r[0]) < 0) in_frustum = false;
-    if (in_frustum) {
+    for (int v = 0; v < 3; ++v)
+      if (clip_d(pl, tv[v].r[0]) < 0) in_frustum = false;
+  if (in_frustum) {
+    float pv[3][2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      float iw = 1.0f / tv[i].r[0].w;
+      pv[i][0] = tv[i].r[0].x * iw;
+      pv[i][1] = tv[i].r[0].y * iw;
+    }
+    float area = (pv[2][0] - pv[0][0]) * (pv[1][1] - pv[0][1]) - (pv[2][1] - pv[0][1]) * (pv[1][0] - pv[0][0]);
+    bool front = area > 0.0f;
+    if (cull(D, front ? 1.0f : -1.0f)) {
+      P.slot_rec[slot0] = NO_REC;
+    } else if (front) {
+      emit_triangle<NA>(P, D, draw, slot0, tv[0], tv[1], tv[2], ntri);
+    } else {
+      emit_triangle<NA>(P, D, draw, slot0, tv[0], tv[2], tv[1], ntri);
+    }
+    return;
+  }
+  // Sutherland-Hodgman against the near (z >= 0) and far (z <= w) planes.
+  vtx<NA> pool[7];
+  pool[0] = tv[0];
+  pool[1] = tv[1];
+  pool[2] = tv[2];
+  int npool = 3;
+  int poly[2][5];
+  int n[2] = {3, 0};
+  poly[0][0] = 0;
+  poly[0][1] = 1;
+  poly[0][2] = 2;
+  int src = 0, dst = 1;
+  bool is_front = false, culled = false;
+  float d0 = 0.0f, d1 = 0.0f;
+  for (int pl = 0; pl < 2 && !culled; ++pl) {
+    n[dst] = 0;
+    if (n[src] != 0) d0 = clip_d(pl, pool[poly[src][0]].r[0]);
+    for (int i = 0, j = 1; i < n[src]; ++i, ++j) {
+      j %= n[src];
+      d1 = clip_d(pl, pool[poly[src][j]].r[0]);
+      if (d0 >= 0.0f) {
+        poly[dst][n[dst]++] = poly[src][i];
+        if (d1 < 0.0f) {
+          vtx_lerp(D, pool[npool], pool[poly[src][i]], pool[poly[src][j]], d0 / (d0 - d1));
+          poly[dst][n[dst]++] = npool++;
+        }
+      } else if (d1 >= 0.0f) {
+        vtx_lerp(D, pool[npool], pool[poly[src][j]], pool[poly[src][i]], d1 / (d1 - d0));
+        poly[dst][n[dst]++] = npool++;
+      }
+      d0 = d1;
+    }
+    if (pl == 0 && n[dst] >= 3) {
       float pv[3][2];
-#pragma unroll
       for (int i = 0; i < 3; ++i) {
-        float iw = 1.0f / tv[i].r[0].w;
-        pv[i][0] = tv[i].r[0].x * iw;
-        pv[i][1] = tv[i].r[0].y * iw;
+        v4 q = pool[poly[dst][i]].r[0];
+        float inv_abs_w = 1.0f / fabsf(q.w);
+        pv[i][0] = q.x * inv_abs_w;
+        pv[i][1] = q.y * inv_abs_w;
       }
       float area = (pv[2][0] - pv[0][0]) * (pv[1][1] - pv[0][1]) - (pv[2][1] - pv[0][1]) * (pv[1][0] - pv[0][0]);
-      bool front = area > 0.0f;
-      if (cull(p, front ? 1.0f : -1.0f)) {
-        p.slot_rec[slot0] = NO_REC;
-      } else if (front) {
-        emit_triangle<NA>(p, slot0, tv[0], tv[1], tv[2], ntri);
-      } else {
-        emit_triangle<NA>(p, slot0, tv[0], tv[2], tv[1], ntri);
-      }
-    } else {
-      // Sutherland-Hodgman against the near (z >= 0) and far (z <= w) planes.
-      vtx<NA> pool[7];
-      pool[0] = tv[0];
-      pool[1] = tv[1];
-      pool[2] = tv[2];
-      int npool = 3;
-      int poly[2][5];
-      int n[2] = {3, 0};
-      poly[0][0] = 0;
-      poly[0][1] = 1;
-      poly[0][2] = 2;
-      int src = 0, dst = 1;
-      bool is_front = false, culled = false;
-      float d0 = 0.0f, d1 = 0.0f;
-      for (int pl = 0; pl < 2 && !culled; ++pl) {
-        n[dst] = 0;
-        if (n[src] != 0) d0 = clip_d(pl, pool[poly[src][0]].r[0]);
-        for (int i = 0, j = 1; i < n[src]; ++i, ++j) {
-          j %= n[src];
-          d1 = clip_d(pl, pool[poly[src][j]].r[0]);
-          if (d0 >= 0.0f) {
-            poly[dst][n[dst]++] = poly[src][i];
-            if (d1 < 0.0f) {
-              vtx_lerp(p, pool[npool], pool[poly[src][i]], pool[poly[src][j]], d0 / (d0 - d1));
-              poly[dst][n[dst]++] = npool++;
-            }
-          } else if (d1 >= 0.0f) {
-            vtx_lerp(p, pool[npool], pool[poly[src][j]], pool[poly[src][i]], d1 / (d1 - d0));
-            poly[dst][n[dst]++] = npool++;
-          }
-          d0 = d1;
-        }
-        if (pl == 0 && n[dst] >= 3) {
-          float pv[3][2];
-          for (int i = 0; i < 3; ++i) {
-            v4 q = pool[poly[dst][i]].r[0];
-            float inv_abs_w = 1.0f / fabsf(q.w);
-            pv[i][0] = q.x * inv_abs_w;
-            pv[i][1] = q.y * inv_abs_w;
-          }
-          float area = (pv[2][0] - pv[0][0]) * (pv[1][1] - pv[0][1]) - (pv[2][1] - pv[0][1]) * (pv[1][0] - pv[0][0]);
-          is_front = area > 0.0f;
-          if (cull(p, area)) culled = true;
-        }
-        src ^= 1;
-        dst ^= 1;
-      }
-      int nv = culled ? 0 : n[src];
-      p.slot_rec[slot0] = NO_REC;
-      for (int t = 1; t + 1 < nv; ++t) {
-        int ia = poly[src][0], ib = poly[src][is_front ? t : t + 1], ic = poly[src][is_front ? t + 1 : t];
-        emit_triangle<NA>(p, slot0 + (t - 1), pool[ia], pool[ib], pool[ic], ntri);
-      }
+      is_front = area > 0.0f;
+      if (cull(D, area)) culled = true;
+    }
+    src ^= 1;
+    dst ^= 1;
+  }
+  int nv = culled ? 0 : n[src];
+  P.slot_rec[slot0] = NO_REC;
+  for (int t = 1; t + 1 < nv; ++t) {
+    int ia = poly[src][0], ib = poly[src][is_front ? t : t + 1], ic = poly[src][is_front ? t + 1 : t];
+    emit_triangle<NA>(P, D, draw, slot0 + (t - 1), pool[ia], pool[ib], pool[ic], ntri);
+  }
+}
+
+__global__ void __launch_bounds__(128) k_geometry(PassParams P) {
+  uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t ntri = 0, draw = 0xFFFFFFFFu;
+  if (g < P.nprims) {
+    draw = upper_index(P.draw_prim_base, P.ndraws, g);
+    DrawParams const& D = P.draws[draw];
+    uint32_t prim = g - D.prim_base;
+    switch (D.nattr) {
+    case 0: geometry_prim<0>(P, D, draw, prim, ntri); break;
+    case 1: geometry_prim<1>(P, D, draw, prim, ntri); break;
+    case 2: geometry_prim<2>(P, D, draw, prim, ntri); break;
+    case 3: geometry_prim<3>(P, D, draw, prim, ntri); break;
+    case 4: geometry_prim<4>(P, D, draw, prim, ntri); break;
+    default: geometry_prim<5>(P, D, draw, prim, ntri); break;
     }
   }
-  // warp-aggregated counter update
-  for (int o = 16; o > 0; o >>= 1) ntri += __shfl_down_sync(0xFFFFFFFFu, ntri, o);
-  if ((threadIdx.x & 31) == 0 && ntri) atomicAdd(&p.counters->cprimitives, ntri);
+  // per-draw counter, aggregated over the lanes of one draw
+  uint32_t grp = __match_any_sync(0xFFFFFFFFu, draw);
+  uint32_t sum = __reduce_add_sync(grp, ntri);
+  if (draw != 0xFFFFFFFFu && sum && (threadIdx.x & 31) == static_cast<uint32_t>(__ffs(grp) - 1))
+    atomicAdd(&P.draw_stats[draw].cprimitives, static_cast<unsigned long long>(sum));
 }
 
 // ---------------------------------------------------------------------------
 // binning (rasterizer::threaded_dispatch_primitive, rasterizer.cpp:775-862)
 template <bool FILL>
-__global__ void __launch_bounds__(128) k_bin(DrawParams p, uint32_t nslots) {
+__global__ void __launch_bounds__(128) k_bin(PassParams P) {
   uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
-  if (warp >= p.nchunks) return;
-  uint32_t begin = warp * p.chunk, end = min(begin + p.chunk, nslots);
-  int const tx_n = p.tiles_x, ty_n = p.tiles_y;
-  uint32_t* cnt = p.bin_counts;
+  if (warp >= P.nchunks) return;
+  uint32_t const t = P.chunk_target[warp];
+  TargetParams const& T = P.targets[t];
+  uint32_t const c = warp - T.chunk_base, nch = T.nchunks;
+  uint32_t const slot_end = T.slot_base + T.nslots;
+  uint32_t begin = T.slot_base + c * T.chunk, end = min(begin + T.chunk, slot_end);
+  int const tgx = T.tiles_x;
+  uint32_t* cnt = P.bin_counts + T.count_base + c;
   for (uint32_t base = begin; base < end; base += 32) {
     // every lane fetches its own slot's triangle (parallel loads)
     uint32_t slot = base + lane;
-    uint32_t rec = slot < end ? p.slot_rec[slot] : NO_REC;
+    uint32_t rec = slot < end ? P.slot_rec[slot] : NO_REC;
     float4 e0 = make_float4(0, 0, 0, 0), e1 = e0, e2 = e0;
     int sx = 0, sy = 0, ex = 0, ey = 0;
     if (rec != NO_REC) {
-      float4 const* R = p.recs + static_cast<size_t>(rec) * p.rec_stride;
+      float4 const* R = P.recs + rec;
       e0 = R[0];
       e1 = R[1];
       e2 = R[2];
       float4 bb = R[3];
+      DrawParams const& D = P.draws[rec_draw(R)];
+      int const tx_n = D.tiles_x, ty_n = D.tiles_y;
       sx = min(fast_floori(static_cast<double>(smax(0.0f, bb.x) / TILE)), tx_n);
       sy = min(fast_floori(static_cast<double>(smax(0.0f, bb.z) / TILE)), ty_n);
       ex = min(fast_ceili(static_cast<double>(smax(0.0f, bb.y) / TILE)) + 1, tx_n);
@@ -368,13 +392,13 @@ __global__ void __launch_bounds__(128) k_bin(DrawParams p, uint32_t nslots) {
       if (tsx + 1 == tex && tsy + 1 == tey) {
         // single-tile primitive: pushed without the tile tests (rasterizer.cpp:809-811)
         if (lane == 0) {
-          uint32_t* c = cnt + static_cast<size_t>(tsy * tx_n + tsx) * p.nchunks + warp;
+          uint32_t* cc = cnt + static_cast<size_t>(tsy * tgx + tsx) * nch;
           if (FILL) {
-            uint32_t pos = *c;
-            *c = pos + 1;
-            if (pos < p.bin_capacity) p.bin_entries[pos] = r << 1;
+            uint32_t pos = *cc;
+            *cc = pos + 1;
+            if (pos < P.bin_capacity) P.bin_entries[pos] = r << 1;
           } else {
-            atomicAdd(c, 1u);
+            atomicAdd(cc, 1u);
           }
         }
       } else if (tsx < tex && tsy < tey) {
@@ -406,15 +430,15 @@ __global__ void __launch_bounds__(128) k_bin(DrawParams p, uint32_t nslots) {
             acc &= (r2a[k] >= evv);
           }
           if (!rej) {
-            uint32_t* c = cnt + static_cast<size_t>(y * tx_n + x) * p.nchunks + warp;
+            uint32_t* cc = cnt + static_cast<size_t>(y * tgx + x) * nch;
             if (FILL) {
               // the chunk's cursor of this tile: only this warp touches it, and the
               // __syncwarp below orders one step's update before the next step's read
-              uint32_t pos = *c;
-              *c = pos + 1;
-              if (pos < p.bin_capacity) p.bin_entries[pos] = (r << 1) | static_cast<uint32_t>(acc);
+              uint32_t pos = *cc;
+              *cc = pos + 1;
+              if (pos < P.bin_capacity) P.bin_entries[pos] = (r << 1) | static_cast<uint32_t>(acc);
             } else {
-              atomicAdd(c, 1u);
+              atomicAdd(cc, 1u);
             }
           }
         }
@@ -453,7 +477,7 @@ __device__ inline uint32_t block_exclusive_scan(uint32_t v, uint32_t* smem, uint
   return warp_off + x - v;
 }
 
-__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_local(uint32_t* data, uint32_t n, uint32_t* sums) {
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_local(uint32_t* data, size_t n, uint32_t* sums) {
   __shared__ uint32_t smem[32];
   size_t base = static_cast<size_t>(blockIdx.x) * SCAN_BLOCK * SCAN_ITEMS + threadIdx.x * SCAN_ITEMS;
   uint32_t v[SCAN_ITEMS], s = 0;
@@ -472,8 +496,8 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_local(uint32_t* data, uint3
   if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
-// single-block scan of the block sums (nsums <= SCAN_BLOCK * SCAN_ITEMS * many)
-__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_sums(uint32_t* sums, uint32_t nsums, DrawCounters* ctr) {
+// single-block scan of the block sums
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_sums(uint32_t* sums, uint32_t nsums, PassCounters* ctr) {
   __shared__ uint32_t smem[32];
   uint32_t carry = 0;
   for (uint32_t start = 0; start < nsums; start += SCAN_BLOCK * SCAN_ITEMS) {
@@ -496,60 +520,52 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_sums(uint32_t* sums, uint32
   if (threadIdx.x == 0) ctr->bin_entries = carry;
 }
 
-__global__ void k_scan_add(uint32_t* data, uint32_t n, uint32_t const* sums) {
+__global__ void k_scan_add(uint32_t* data, size_t n, uint32_t const* sums) {
   size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n) data[i] += sums[i / (SCAN_BLOCK * SCAN_ITEMS)];
 }
 
 // tile ranges from the scanned counts, and the overflow check
-__global__ void k_tile_ranges(DrawParams p, uint32_t ntiles) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < ntiles) p.tile_begin[t] = p.bin_counts[static_cast<size_t>(t) * p.nchunks];
-  if (t == 0) {
-    p.tile_begin[ntiles] = p.counters->bin_entries;
-    if (p.counters->bin_entries > p.bin_capacity) atomicOr(&p.counters->overflow, 1u);
+__global__ void k_tile_ranges(PassParams P) {
+  uint32_t tile = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tile < P.ntiles) {
+    uint32_t t = upper_index(P.target_tile_base, P.ntargets, tile);
+    TargetParams const& T = P.targets[t];
+    P.tile_begin[tile] = P.bin_counts[T.count_base + static_cast<size_t>(tile - T.tile_base) * T.nchunks];
+  }
+  if (tile == 0) {
+    P.tile_begin[P.ntiles] = P.counters->bin_entries;
+    if (P.counters->bin_entries > P.bin_capacity) atomicOr(&P.counters->overflow, OVF_BIN);
   }
 }
 
 // ---------------------------------------------------------------------------
 // host-side launchers
-template <int NA>
-static void launch_geometry_t(DrawParams const& p, cudaStream_t s) {
-  uint32_t blocks = (p.prim_count + 127) / 128;
-  if (blocks) k_geometry<NA><<<blocks, 128, 0, s>>>(p);
-}
-void launch_geometry(DrawParams const& p, int nattr, cudaStream_t s) {
-  switch (nattr) {
-  case 0: launch_geometry_t<0>(p, s); break;
-  case 1: launch_geometry_t<1>(p, s); break;
-  case 2: launch_geometry_t<2>(p, s); break;
-  case 3: launch_geometry_t<3>(p, s); break;
-  case 4: launch_geometry_t<4>(p, s); break;
-  default: launch_geometry_t<5>(p, s); break;
-  }
+void launch_geometry(PassParams const& P, cudaStream_t s) {
+  uint32_t blocks = (P.nprims + 127) / 128;
+  if (blocks) k_geometry<<<blocks, 128, 0, s>>>(P);
 }
 
-void launch_bin(DrawParams const& p, uint32_t nslots, bool fill, cudaStream_t s) {
-  uint32_t warps = p.nchunks;
-  uint32_t blocks = (warps * 32 + 127) / 128;
+void launch_bin(PassParams const& P, bool fill, cudaStream_t s) {
+  uint32_t blocks = (P.nchunks * 32 + 127) / 128;
   if (!blocks) return;
   if (fill)
-    k_bin<true><<<blocks, 128, 0, s>>>(p, nslots);
+    k_bin<true><<<blocks, 128, 0, s>>>(P);
   else
-    k_bin<false><<<blocks, 128, 0, s>>>(p, nslots);
+    k_bin<false><<<blocks, 128, 0, s>>>(P);
 }
 
 // exclusive scan of `n` counts in place; `sums` needs ceil(n / 4096) entries
-void launch_scan(uint32_t* data, uint32_t n, uint32_t* sums, DrawCounters* ctr, cudaStream_t s) {
-  uint32_t nblocks = (n + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS);
+void launch_scan(uint32_t* data, size_t n, uint32_t* sums, PassCounters* ctr, cudaStream_t s) {
+  size_t nblocks = (n + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS);
   if (nblocks == 0) return;
-  k_scan_local<<<nblocks, SCAN_BLOCK, 0, s>>>(data, n, sums);
-  k_scan_sums<<<1, SCAN_BLOCK, 0, s>>>(sums, nblocks, ctr);
-  k_scan_add<<<(n + 255) / 256, 256, 0, s>>>(data, n, sums);
+  k_scan_local<<<static_cast<uint32_t>(nblocks), SCAN_BLOCK, 0, s>>>(data, n, sums);
+  k_scan_sums<<<1, SCAN_BLOCK, 0, s>>>(sums, static_cast<uint32_t>(nblocks), ctr);
+  k_scan_add<<<static_cast<uint32_t>((n + 255) / 256), 256, 0, s>>>(data, n, sums);
 }
 
-void launch_tile_ranges(DrawParams const& p, uint32_t ntiles, cudaStream_t s) {
-  k_tile_ranges<<<(ntiles + 255) / 256, 256, 0, s>>>(p, ntiles);
+void launch_tile_ranges(PassParams const& P, cudaStream_t s) {
+  k_tile_ranges<<<(P.ntiles + 255) / 256, 256, 0, s>>>(P);
 }
 
 cudaError_t upload_ewa_table_geometry(float const* tab, cudaStream_t s) {

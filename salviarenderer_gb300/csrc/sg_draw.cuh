@@ -1,5 +1,13 @@
-// sg_draw.cuh -- per-draw parameter block and scratch layout shared by the
-// draw kernels (sg_draw.cu) and the host runtime (sg_api.cu).
+// sg_draw.cuh -- parameter blocks and scratch layout of a pass, shared by
+// the pass kernels (sg_draw.cu, sg_raster*.cu) and the host runtime
+// (sg_api.cu).
+//
+// A pass is a list of draws, in API order, over one or more render targets;
+// it runs as one kernel chain (geometry, binning, coverage, shading,
+// merging).  sg_draw submits a pass of one draw; sg_submit and the recorded
+// command graphs put many draws of many frames into one pass.  Results are
+// those of running the draws one by one: every tile list stays in API order
+// and targets never share pixels.
 #pragma once
 
 #include <cstdint>
@@ -9,24 +17,52 @@
 namespace sg {
 
 constexpr int TILE = 64;              // rasterizer.cpp:32 (also the classification tree's root)
-constexpr int RASTER_THREADS = 256;   // one thread per 4x4 block of the 64x64 tile
+constexpr int RASTER_THREADS = 256;   // owners (4x4 blocks) per 64x64 tile
 constexpr int FRAG_CHUNK = 16;        // fragments per chunk of an owner's fragment list
 constexpr uint32_t NO_CHUNK = 0xFFFFFFFFu;
 constexpr int BIN_CHUNK_MIN = 256;    // triangle slots per binning warp (minimum)
 constexpr uint32_t NO_REC = 0xFFFFFFFFu;
 
-struct DrawCounters {
-  unsigned long long cprimitives;
-  unsigned long long ps_invocations;
-  unsigned long long backend_input_pixels;
+// overflow bits of PassCounters::overflow
+constexpr uint32_t OVF_BIN = 1u, OVF_FRAG = 4u, OVF_REC = 8u;
+
+struct PassCounters {
   unsigned int bin_entries;          // entries produced by the count pass
-  unsigned int overflow;             // bit 0: bin entries, bit 1: fragment buffer
-  unsigned int rec_count;            // triangle records allocated
-  unsigned int tile_cursor;          // dynamic tile scheduler
+  unsigned int overflow;             // OVF_* bits
+  unsigned int rec_units;            // float4 units of triangle records allocated
+  unsigned int tile_cursor;          // dynamic item scheduler of the coverage pass
   unsigned int fetch_oob;            // vertex or index reads outside their buffers
   unsigned int chunk_total;          // fragment chunks allocated by the coverage pass
   unsigned int merge_cursor;         // dynamic tile scheduler of the merge pass
-  unsigned int pad[2];
+  unsigned int pad;
+};
+
+// Per-draw pipeline counters (async_object.h:90-175).
+struct DrawStatsDev {
+  unsigned long long cprimitives;
+  unsigned long long ps_invocations;
+  unsigned long long backend_input_pixels;
+  unsigned long long pad;
+};
+
+// One render target (colour and/or depth-stencil surface pair) of a pass.
+struct TargetParams {
+  uint8_t* color;
+  uint8_t* ds;
+  uint32_t color_fmt, color_esz;
+  uint32_t width, height;            // colour target (or depth target) size
+  uint32_t ds_fmt, ds_esz, ds_width;
+  uint32_t samples;
+  int tiles_x, tiles_y;              // tile grid: the largest of the pass's draws on this target
+  uint32_t tile_base;                // global index of the target's first tile
+  float target_w, target_h;
+  float sp_x[4], sp_y[4];            // sample pattern (rasterizer.cpp:1087-1103)
+  uint32_t any_early_z;              // some draw tests depth in the coverage pass
+  // binning: the target's slots are cut into chunks of `chunk` slots, one warp each
+  uint32_t slot_base, nslots;
+  uint32_t chunk_base, nchunks, chunk;
+  uint32_t pad;
+  uint64_t count_base;               // first (tile, chunk) counter of the target
 };
 
 struct DrawParams {
@@ -45,6 +81,10 @@ struct DrawParams {
   int32_t base_vertex;
   uint32_t strip;
   uint32_t prim_count;
+  uint32_t prim_base;           // first global primitive of the draw in the pass
+  uint32_t slot_base;           // first triangle slot (3 per primitive)
+  uint32_t target;              // index into the pass's targets
+  uint32_t nattr, rec_stride;
   // shaders
   uint32_t vs_prog, ps_prog, bs_prog;
   float vs_k[SG_MAX_SHADER_CONSTANTS];
@@ -55,48 +95,77 @@ struct DrawParams {
   // rasterizer state
   uint32_t cull_mode, front_ccw;
   float vp_x, vp_y, vp_w, vp_h, vp_minz, vp_maxz;
-  int tiles_x, tiles_y;
-  float target_w, target_h;
-  uint32_t samples;
-  float sp_x[4], sp_y[4];
+  int tiles_x, tiles_y;         // this draw's tile grid (viewport size / 64)
   // output merger (framebuffer.cpp)
-  uint8_t* color;
-  uint32_t color_fmt, color_esz;
-  uint32_t width, height;       // colour target (or depth target) size
-  uint8_t* ds;
-  uint32_t ds_fmt, ds_esz, ds_width;
   uint32_t early_z, read_depth, write_depth, stencil;
   uint32_t depth_func;
   uint32_t stencil_ref, read_mask, write_mask;
   uint32_t front_func, front_pass, back_func, back_pass;
+  uint32_t zcfg;                // packed early-Z configuration (see zcfg_of)
+};
+
+// samples (bits 0-3), read_depth (4), write_depth (5), D24S8 storage (6),
+// early-Z (7), depth function (bits 8-11)
+__host__ __device__ inline uint32_t zcfg_of(uint32_t samples, uint32_t rd, uint32_t wr, bool d24, uint32_t early_z,
+                                            uint32_t func) {
+  return samples | (rd << 4) | (wr << 5) | (d24 ? 64u : 0u) | (early_z ? 128u : 0u) | (func << 8);
+}
+
+struct PassParams {
+  DrawParams const* draws;
+  TargetParams const* targets;
+  uint32_t const* draw_prim_base;   // per draw, first global primitive (sorted)
+  uint32_t const* target_tile_base; // per target, first global tile (sorted)
+  uint32_t const* chunk_target;     // per binning chunk, its target
+  uint32_t ndraws, ntargets;
+  uint32_t nprims, nslots, ntiles, nchunks;
   // scratch
-  float4* recs;                 // triangle records (rec_stride float4 each)
-  uint32_t rec_stride;
-  uint32_t* slot_rec;           // prim*3+k -> record index or NO_REC
-  uint32_t* bin_counts;         // [tile][chunk] counts, then cursors
+  float4* recs;                 // triangle records, rec id = offset in float4 units
+  uint32_t rec_capacity;        // float4 units
+  uint32_t* slot_rec;           // slot -> record id or NO_REC
+  uint32_t* bin_counts;         // per target [tile][chunk] counts, then cursors
   uint32_t* bin_entries;        // rec << 1 | tile-accept, per tile in API order
-  uint32_t* tile_begin;         // per tile [begin, end) into bin_entries
+  uint32_t* tile_begin;         // per global tile [begin, end) into bin_entries
   uint32_t bin_capacity;
-  uint32_t nchunks, chunk;
+  uint32_t chunk_capacity;
   // Quad fragments, structure of arrays indexed by chunk * FRAG_CHUNK + slot.
   // Each owner (4x4 block) of a tile appends its fragments, in primitive
   // order, to its own list of chunks: owner_first[tile * 256 + owner] is the
   // first chunk, chunk_next links them, chunk_count says how many slots of a
   // chunk are used.
   uint32_t* frag_rec;           // triangle record
-  uint32_t* frag_pos;           // bits 0-11 x/2, 12-23 y/2 (absolute quad), 24 full quad
+  uint32_t* frag_pos;           // bits 0-11 x/2, 12-23 y/2 (absolute quad), 24 full quad, 25-27 varyings
   uint32_t* frag_mask;          // bits 0-15 early-Z-tested samples, 16-31 covered samples
   float4* frag_color;           // 4 pixels per fragment, pixel-shader output
   uint8_t* frag_ps;             // pixel-shader pass mask (4 bits)
   uint32_t* chunk_next;
   uint32_t* chunk_count;
-  uint32_t chunk_capacity;
   uint32_t* owner_first;
-  DrawCounters* counters;
+  PassCounters* counters;
+  DrawStatsDev* draw_stats;     // per draw
+  unsigned int* sticky;         // overflow bits of every pass since the host last looked
+  // coverage work items: 16 or 32 pixels on a side; 32x32 items of a tile with
+  // more than split_entries bin entries become 16x16
+  uint32_t cover_item, split_entries;
 };
 
 // triangle record layout (float4 units): [0..2] edge factors, [3] bbox,
-// [4] (front, 0, 0, 0), then v0, ddx, ddy registers (1 + nattr each).
+// [4] (front, draw index bits, 0, 0), then v0, ddx, ddy registers (1 + nattr each).
 __host__ __device__ constexpr uint32_t rec_stride_for(int nattr) { return 5 + 3 * (1 + nattr); }
+
+__device__ inline uint32_t rec_draw(float4 const* R) { return __float_as_uint(R[4].y); }
+
+// index of the last element of sorted `base[0..n)` that is <= v
+__device__ inline uint32_t upper_index(uint32_t const* base, uint32_t n, uint32_t v) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (base[mid] <= v)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
 
 }  // namespace sg

@@ -1,80 +1,90 @@
-// sg_misc.cu -- clears, MSAA resolve and mip generation.
+// sg_misc.cu -- clears and MSAA resolves (batched as jobs), mip generation.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 
-#include "sg_common.cuh"
+#include "sg_jobs.cuh"
 
 namespace sg {
 
 // surface::fill (surface.cpp:170-275): every texel gets the converted colour.
-// The converted texel (1..16 bytes) is replicated with 4-byte stores when the
-// element size allows, else byte by byte.
-__global__ void k_fill(uint8_t* data, size_t nelem, uint32_t esz, uint4 pattern) {
-  size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
-  uint32_t const* pat = &pattern.x;
-  if (esz % 4 == 0) {
-    uint32_t words = esz / 4;
-    uint32_t* d = reinterpret_cast<uint32_t*>(data);
-    size_t nwords = nelem * words;
-    for (size_t w = i; w < nwords; w += stride) d[w] = pat[w % words];
+// Element sizes that divide 16 bytes are written as 16-byte stores of the
+// replicated texel; 12-byte texels word by word.
+__device__ void fill_job(SurfaceJob const& j, uint32_t part, uint32_t nparts) {
+  size_t const stride = static_cast<size_t>(nparts) * blockDim.x;
+  size_t const i0 = static_cast<size_t>(part) * blockDim.x + threadIdx.x;
+  if (j.esz == 4 || j.esz == 8 || j.esz == 16) {
+    uint4 v;
+    uint32_t* pv = &v.x;
+    for (int k = 0; k < 4; ++k) pv[k] = j.pattern[k % (j.esz / 4)];
+    size_t const nvec = j.n * j.esz / 16, tail_bytes = j.n * j.esz - nvec * 16;
+    uint4* d = reinterpret_cast<uint4*>(j.dst);
+    for (size_t w = i0; w < nvec; w += stride) d[w] = v;
+    uint32_t* t = reinterpret_cast<uint32_t*>(j.dst + nvec * 16);
+    for (size_t w = i0; w < tail_bytes / 4; w += stride) t[w] = pv[w % 4];
   } else {
-    uint8_t const* pb = reinterpret_cast<uint8_t const*>(pat);
-    size_t nbytes = nelem * esz;
-    for (size_t b = i; b < nbytes; b += stride) data[b] = pb[b % esz];
+    uint32_t const words = j.esz / 4;
+    uint32_t* d = reinterpret_cast<uint32_t*>(j.dst);
+    size_t const nwords = j.n * words;
+    for (size_t w = i0; w < nwords; w += stride) d[w] = j.pattern[w % words];
   }
 }
 
 // Depth-stencil clear of one flag (framebuffer::clear_depth_stencil,
 // framebuffer.cpp:616-644) or of D24S8 (extension).
-__global__ void k_clear_ds(uint8_t* data, size_t nelem, uint32_t fmt, uint32_t flags, float depth,
-                           uint32_t stencil) {
-  size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
-  for (; i < nelem; i += stride) {
-    if (fmt == SG_FMT_RG32F) {
-      uint32_t* w = reinterpret_cast<uint32_t*>(data) + 2 * i;
-      if (flags & SG_CLEAR_DEPTH) w[0] = __float_as_uint(depth);
-      if (flags & SG_CLEAR_STENCIL) w[1] = stencil;
-    } else if (fmt == SG_FMT_D32F) {
-      if (flags & SG_CLEAR_DEPTH) reinterpret_cast<float*>(data)[i] = depth;
+__device__ void clear_ds_job(SurfaceJob const& j, uint32_t part, uint32_t nparts) {
+  size_t const stride = static_cast<size_t>(nparts) * blockDim.x;
+  for (size_t i = static_cast<size_t>(part) * blockDim.x + threadIdx.x; i < j.n; i += stride) {
+    if (j.fmt == SG_FMT_RG32F) {
+      uint32_t* w = reinterpret_cast<uint32_t*>(j.dst) + 2 * i;
+      if (j.flags & SG_CLEAR_DEPTH) w[0] = __float_as_uint(j.depth);
+      if (j.flags & SG_CLEAR_STENCIL) w[1] = j.stencil;
+    } else if (j.fmt == SG_FMT_D32F) {
+      if (j.flags & SG_CLEAR_DEPTH) reinterpret_cast<float*>(j.dst)[i] = j.depth;
     } else {
-      uint32_t* w = reinterpret_cast<uint32_t*>(data) + i;
+      uint32_t* w = reinterpret_cast<uint32_t*>(j.dst) + i;
       uint32_t v = *w;
-      if (flags & SG_CLEAR_DEPTH) {
-        float c = fminf(fmaxf(depth, 0.0f), 1.0f) * 16777215.0f;
+      if (j.flags & SG_CLEAR_DEPTH) {
+        float c = fminf(fmaxf(j.depth, 0.0f), 1.0f) * 16777215.0f;
         v = (v & 0xFF000000u) | __float2uint_rn(c);
       }
-      if (flags & SG_CLEAR_STENCIL) v = (v & 0x00FFFFFFu) | ((stencil & 0xFFu) << 24);
+      if (j.flags & SG_CLEAR_STENCIL) v = (v & 0x00FFFFFFu) | ((j.stencil & 0xFFu) << 24);
       *w = v;
     }
   }
 }
 
-// surface::resolve (surface.cpp:123-140): sum of samples in rgba32f, times 1/S.
-__global__ void k_resolve(uint8_t const* src, uint8_t* dst, uint32_t npix, uint32_t samples, uint32_t fmt,
-                          uint32_t dst_fmt) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= npix) return;
-  uint32_t esz = fmt_bytes(fmt);
-  v4 c = mk4(0, 0, 0, 0);
-  for (uint32_t s = 0; s < samples; ++s) c = c + read_texel(fmt, src + (static_cast<size_t>(i) * samples + s) * esz);
-  float inv = 1.0f / static_cast<float>(samples);
-  write_texel(dst_fmt, dst + static_cast<size_t>(i) * fmt_bytes(dst_fmt), c * inv);
+// surface::resolve (surface.cpp:123-140): sum of samples in rgba32f, times
+// 1/S (eflib's operator/= multiplies by the reciprocal).  Four-sample RGBA8
+// reads one 16-byte vector per pixel.
+__device__ void resolve_job(SurfaceJob const& j, uint32_t part, uint32_t nparts) {
+  size_t const stride = static_cast<size_t>(nparts) * blockDim.x;
+  uint32_t const samples = j.samples;
+  float const inv = 1.0f / static_cast<float>(samples);
+  for (size_t i = static_cast<size_t>(part) * blockDim.x + threadIdx.x; i < j.n; i += stride) {
+    v4 c = mk4(0, 0, 0, 0);
+    if (j.fmt == SG_FMT_RGBA8 && samples == 4) {
+      uint4 s = reinterpret_cast<uint4 const*>(j.src)[i];
+      uint32_t w[4] = {s.x, s.y, s.z, s.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        c = c + unorm8_to_f(w[k] & 0xFF, (w[k] >> 8) & 0xFF, (w[k] >> 16) & 0xFF, w[k] >> 24);
+    } else {
+      for (uint32_t s = 0; s < samples; ++s) c = c + read_texel(j.fmt, j.src + (i * samples + s) * j.esz);
+    }
+    write_texel(j.dst_fmt, j.dst + i * fmt_bytes(j.dst_fmt), c * inv);
+  }
 }
 
-// Four-sample RGBA8 resolve, one pixel per thread, 16-byte loads.
-__global__ void k_resolve_rgba8x4(uint4 const* src, uint32_t* dst, uint32_t npix) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= npix) return;
-  uint4 s = src[i];
-  v4 c = mk4(0, 0, 0, 0);
-  uint32_t w[4] = {s.x, s.y, s.z, s.w};
-#pragma unroll
-  for (int k = 0; k < 4; ++k) c = c + unorm8_to_f(w[k] & 0xFF, (w[k] >> 8) & 0xFF, (w[k] >> 16) & 0xFF, w[k] >> 24);
-  c = c * 0.25f;
-  dst[i] = f_to_unorm8(c.x) | (f_to_unorm8(c.y) << 8) | (f_to_unorm8(c.z) << 16) | (f_to_unorm8(c.w) << 24);
+// One launch runs a list of jobs: blockIdx.y selects the job, the x blocks
+// stride over its elements.
+__global__ void __launch_bounds__(256) k_jobs(JobList L) {
+  SurfaceJob const& j = L.jobs[blockIdx.y];
+  switch (j.kind) {
+  case JOB_FILL: fill_job(j, blockIdx.x, gridDim.x); break;
+  case JOB_CLEAR_DS: clear_ds_job(j, blockIdx.x, gridDim.x); break;
+  default: resolve_job(j, blockIdx.x, gridDim.x); break;
+  }
 }
 
 // surface::make_mip_surface (surface.cpp:53-92)
@@ -99,25 +109,26 @@ __global__ void k_mip(uint8_t const* src, uint32_t sw, uint32_t sh, uint8_t* dst
   write_texel(fmt, out, (((c0 + c1) + c2) + c3) * 0.25f);
 }
 
-void launch_fill(uint8_t* data, size_t nelem, uint32_t esz, uint4 pattern, cudaStream_t s) {
-  size_t work = nelem * (esz % 4 == 0 ? esz / 4 : esz);
-  uint32_t blocks = static_cast<uint32_t>(std::min<size_t>((work + 255) / 256, 152 * 16));
-  if (blocks) k_fill<<<blocks, 256, 0, s>>>(data, nelem, esz, pattern);
+// Launches the jobs, JOBS_PER_LAUNCH per launch; returns the launch count.
+uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaStream_t s) {
+  uint32_t launches = 0;
+  for (uint32_t first = 0; first < n; first += JOBS_PER_LAUNCH) {
+    JobList L;
+    L.n = std::min<uint32_t>(JOBS_PER_LAUNCH, n - first);
+    size_t most = 0;
+    for (uint32_t i = 0; i < L.n; ++i) {
+      L.jobs[i] = jobs[first + i];
+      most = std::max<size_t>(most, L.jobs[i].n * (L.jobs[i].kind == JOB_FILL ? L.jobs[i].esz / 4 : 1));
+    }
+    // enough x blocks for the largest job, at most 16 per SM
+    uint32_t bx = static_cast<uint32_t>(std::min<size_t>((most + 1023) / 1024, static_cast<size_t>(num_sms) * 16));
+    bx = std::max<uint32_t>(1, bx);
+    k_jobs<<<dim3(bx, L.n), 256, 0, s>>>(L);
+    ++launches;
+  }
+  return launches;
 }
-void launch_clear_ds(uint8_t* data, size_t nelem, uint32_t fmt, uint32_t flags, float depth, uint32_t stencil,
-                     cudaStream_t s) {
-  uint32_t blocks = static_cast<uint32_t>(std::min<size_t>((nelem + 255) / 256, 152 * 16));
-  if (blocks) k_clear_ds<<<blocks, 256, 0, s>>>(data, nelem, fmt, flags, depth, stencil);
-}
-void launch_resolve(uint8_t const* src, uint8_t* dst, uint32_t npix, uint32_t samples, uint32_t fmt,
-                    uint32_t dst_fmt, cudaStream_t s) {
-  if (!npix) return;
-  if (fmt == SG_FMT_RGBA8 && dst_fmt == SG_FMT_RGBA8 && samples == 4)
-    k_resolve_rgba8x4<<<(npix + 255) / 256, 256, 0, s>>>(reinterpret_cast<uint4 const*>(src),
-                                                          reinterpret_cast<uint32_t*>(dst), npix);
-  else
-    k_resolve<<<(npix + 255) / 256, 256, 0, s>>>(src, dst, npix, samples, fmt, dst_fmt);
-}
+
 void launch_mip(uint8_t const* src, uint32_t sw, uint32_t sh, uint8_t* dst, uint32_t dw, uint32_t dh,
                 uint32_t samples, uint32_t fmt, uint32_t filter, cudaStream_t s) {
   uint32_t n = dw * dh * samples;

@@ -1,15 +1,15 @@
-// sg_raster.cuh -- rasterization, pixel shading and output merging.
+// sg_raster.cuh -- rasterization, pixel shading and output merging of a pass.
 //
-// Three kernels per draw after binning:
-//   k_cover   one CTA per 64x64 tile (dynamically scheduled), 256 threads;
-//             thread t owns the 4x4 pixel block t of the tile and replays,
-//             for its block and in primitive order, the reference's
+// Three kernels per pass after binning:
+//   k_cover   work items are squares of a tile (its four 32x32 quadrants,
+//             or sixteen 16x16 regions for crowded tiles), dynamically
+//             scheduled over every tile of every target; 128 threads.  Each
+//             owned 4x4 block replays, in primitive order, the reference's
 //             64 -> 16 -> 4 -> sample classification, quad coverage and
-//             early-Z.  Surviving quads become fragments, written per round
-//             in owner-major order.
-//   k_shade   every fragment of the draw, 4 lanes per quad (one per pixel):
+//             early-Z.  Surviving quads become fragments in per-owner lists.
+//   k_shade   every fragment of the pass, 4 lanes per quad (one per pixel):
 //             attribute interpolation and the pixel-shader program, with
-//             ddx/ddy from the quad's lanes.
+//             ddx/ddy from the quad's lanes.  One instance per varying count.
 //   k_merge   one CTA per tile; each owner walks its fragments in primitive
 //             order and applies depth-stencil (when early-Z is off) and the
 //             blend program per covered sample.
@@ -22,9 +22,6 @@
 #include "sg_draw.cuh"
 
 namespace sg {
-
-// ---------------------------------------------------------------------------
-// rasterization + pixel shading + output merger
 
 struct TriView {
   float4 const* R;
@@ -86,122 +83,98 @@ struct DSVal {
   uint32_t stencil;
 };
 
-__device__ inline DSVal ds_read(DrawParams const& p, uint8_t const* a) {
+__device__ inline DSVal ds_read(TargetParams const& T, DrawParams const& D, uint8_t const* a) {
   DSVal v{0.0f, 0u, 0u};
-  switch (p.ds_fmt) {
+  switch (T.ds_fmt) {
   case SG_FMT_RG32F:
-    if (p.read_depth) v.depth = *reinterpret_cast<float const*>(a);
-    if (p.stencil) v.stencil = reinterpret_cast<uint32_t const*>(a)[1] & p.read_mask;
+    if (D.read_depth) v.depth = *reinterpret_cast<float const*>(a);
+    if (D.stencil) v.stencil = reinterpret_cast<uint32_t const*>(a)[1] & D.read_mask;
     break;
   case SG_FMT_D32F:
-    if (p.read_depth) v.depth = *reinterpret_cast<float const*>(a);
+    if (D.read_depth) v.depth = *reinterpret_cast<float const*>(a);
     break;
   case SG_FMT_D24S8: {
     uint32_t w = *reinterpret_cast<uint32_t const*>(a);
-    if (p.read_depth) v.q = w & 0xFFFFFFu;
-    if (p.stencil) v.stencil = (w >> 24) & p.read_mask;
+    if (D.read_depth) v.q = w & 0xFFFFFFu;
+    if (D.stencil) v.stencil = (w >> 24) & D.read_mask;
     break;
   }
   default: break;
   }
   return v;
 }
-__device__ inline void ds_write(DrawParams const& p, uint8_t* a, float depth, uint32_t stencil, uint32_t wmask) {
-  switch (p.ds_fmt) {
+__device__ inline void ds_write(TargetParams const& T, DrawParams const& D, uint8_t* a, float depth,
+                                uint32_t stencil, uint32_t wmask) {
+  switch (T.ds_fmt) {
   case SG_FMT_RG32F:
-    if (p.write_depth) *reinterpret_cast<float*>(a) = depth;
-    if (p.stencil) reinterpret_cast<uint32_t*>(a)[1] = stencil & wmask;
+    if (D.write_depth) *reinterpret_cast<float*>(a) = depth;
+    if (D.stencil) reinterpret_cast<uint32_t*>(a)[1] = stencil & wmask;
     break;
   case SG_FMT_D32F:
-    if (p.write_depth) *reinterpret_cast<float*>(a) = depth;
+    if (D.write_depth) *reinterpret_cast<float*>(a) = depth;
     break;
   case SG_FMT_D24S8: {
     uint32_t w = *reinterpret_cast<uint32_t*>(a);
-    if (p.write_depth) w = (w & 0xFF000000u) | d24_quantize(depth);
-    if (p.stencil) w = (w & 0x00FFFFFFu) | ((stencil & wmask & 0xFFu) << 24);
+    if (D.write_depth) w = (w & 0xFF000000u) | d24_quantize(depth);
+    if (D.stencil) w = (w & 0x00FFFFFFu) | ((stencil & wmask & 0xFFu) << 24);
     *reinterpret_cast<uint32_t*>(a) = w;
     break;
   }
   default: break;
   }
 }
-__device__ inline bool depth_pass(DrawParams const& p, float depth, DSVal const& old) {
-  if (p.ds_fmt == SG_FMT_D24S8 && p.read_depth) return cmpu(p.depth_func, d24_quantize(depth), old.q);
-  return cmpf(p.depth_func, depth, old.depth);
+__device__ inline bool depth_pass(TargetParams const& T, DrawParams const& D, float depth, DSVal const& old) {
+  if (T.ds_fmt == SG_FMT_D24S8 && D.read_depth) return cmpu(D.depth_func, d24_quantize(depth), old.q);
+  return cmpf(D.depth_func, depth, old.depth);
 }
-__device__ inline uint8_t* ds_addr(DrawParams const& p, uint32_t x, uint32_t y, uint32_t s) {
-  return p.ds + ((static_cast<size_t>(y) * p.ds_width + x) * p.samples + s) * p.ds_esz;
+__device__ inline uint8_t* ds_addr(TargetParams const& T, uint32_t x, uint32_t y, uint32_t s) {
+  return T.ds + ((static_cast<size_t>(y) * T.ds_width + x) * T.samples + s) * T.ds_esz;
 }
-__device__ inline uint8_t* color_addr(DrawParams const& p, uint32_t x, uint32_t y, uint32_t s) {
-  return p.color + ((static_cast<size_t>(y) * p.width + x) * p.samples + s) * p.color_esz;
+__device__ inline uint8_t* color_addr(TargetParams const& T, uint32_t x, uint32_t y, uint32_t s) {
+  return T.color + ((static_cast<size_t>(y) * T.width + x) * T.samples + s) * T.color_esz;
 }
 
 // cpp_blend_shader programs
-__device__ inline void blend(DrawParams const& p, uint32_t x, uint32_t y, uint32_t s, v4 src) {
-  if (!p.color) return;
-  uint8_t* a = color_addr(p, x, y, s);
-  switch (p.bs_prog) {
+__device__ inline void blend(TargetParams const& T, DrawParams const& D, uint32_t x, uint32_t y, uint32_t s, v4 src) {
+  if (!T.color) return;
+  uint8_t* a = color_addr(T, x, y, s);
+  switch (D.bs_prog) {
   case SG_BS_LERP_SRC_ALPHA: {
-    v4 d = read_texel(p.color_fmt, a);
-    write_texel(p.color_fmt, a, mk4(lerp1(d.x, src.x, src.w), lerp1(d.y, src.y, src.w), lerp1(d.z, src.z, src.w),
+    v4 d = read_texel(T.color_fmt, a);
+    write_texel(T.color_fmt, a, mk4(lerp1(d.x, src.x, src.w), lerp1(d.y, src.y, src.w), lerp1(d.z, src.z, src.w),
                                     lerp1(d.w, src.w, src.w)));
     break;
   }
-  case SG_BS_ADD: write_texel(p.color_fmt, a, read_texel(p.color_fmt, a) + src); break;
-  default: write_texel(p.color_fmt, a, src); break;
+  case SG_BS_ADD: write_texel(T.color_fmt, a, read_texel(T.color_fmt, a) + src); break;
+  default: write_texel(T.color_fmt, a, src); break;
   }
 }
 
 // framebuffer::render_sample (framebuffer.cpp:445-479)
-__device__ inline void render_sample(DrawParams const& p, uint32_t x, uint32_t y, uint32_t s, v4 src, float depth,
-                                     bool front) {
-  if (p.early_z || !p.ds) {
-    blend(p, x, y, s, src);
+__device__ inline void render_sample(TargetParams const& T, DrawParams const& D, uint32_t x, uint32_t y, uint32_t s,
+                                     v4 src, float depth, bool front) {
+  if (D.early_z || !T.ds) {
+    blend(T, D, x, y, s, src);
     return;
   }
-  uint8_t* a = ds_addr(p, x, y, s);
-  DSVal old = ds_read(p, a);
-  bool dp = depth_pass(p, depth, old);
-  uint32_t func = front ? p.front_func : p.back_func;
-  bool sp = p.stencil ? cmpu(func, p.stencil_ref, old.stencil) : true;
+  uint8_t* a = ds_addr(T, x, y, s);
+  DSVal old = ds_read(T, D, a);
+  bool dp = depth_pass(T, D, depth, old);
+  uint32_t func = front ? D.front_func : D.back_func;
+  bool sp = D.stencil ? cmpu(func, D.stencil_ref, old.stencil) : true;
   if (dp && sp) {
-    uint32_t ns = p.stencil ? stencil_op(front ? p.front_pass : p.back_pass, p.stencil_ref, old.stencil) : 0u;
-    blend(p, x, y, s, src);
-    ds_write(p, a, depth, ns, p.write_mask);
+    uint32_t ns = D.stencil ? stencil_op(front ? D.front_pass : D.back_pass, D.stencil_ref, old.stencil) : 0u;
+    blend(T, D, x, y, s, src);
+    ds_write(T, D, a, depth, ns, D.write_mask);
   }
-}
-
-// early_z_test on one pixel (framebuffer.cpp:522-590); returns the passing samples
-__device__ inline uint32_t early_z_px(DrawParams const& p, uint32_t x, uint32_t y, uint32_t m, float depth,
-                                      float const* aa) {
-  if (p.samples == 1) {
-    uint8_t* a = ds_addr(p, x, y, 0);
-    DSVal old = ds_read(p, a);
-    if (depth_pass(p, depth, old)) {
-      ds_write(p, a, depth, 0, 0);
-      return 1;
-    }
-    return 0;
-  }
-  uint32_t out = 0;
-  for (uint32_t s = 0; s < p.samples; ++s) {
-    if (!(m & (1u << s))) continue;
-    uint8_t* a = ds_addr(p, x, y, s);
-    DSVal old = ds_read(p, a);
-    float nd = aa[s] + depth;
-    if (depth_pass(p, nd, old)) {
-      out |= 1u << s;
-      ds_write(p, a, nd, 0, 0);
-    }
-  }
-  return out;
 }
 
 // Coverage-pass copy of a triangle in shared memory: what coverage and early-Z
-// read (edges, bounding box, the position register of v0 / ddx / ddy).
+// read (edges, bounding box, the position register of v0 / ddx / ddy), and
+// the draw's early-Z configuration and varying count.
 struct TriStage {
   float4 bbox, e0, e1, e2, p0, dpx, dpy;
-  uint32_t entry, pad0, pad1, pad2;
+  uint32_t entry, zcfg, nattr, pad;
 };
 struct StageView {
   TriStage const* S;
@@ -211,70 +184,6 @@ struct StageView {
   __device__ v4 ddx(int) const { return mk4(S->dpx.x, S->dpx.y, S->dpx.z, S->dpx.w); }
   __device__ v4 ddy(int) const { return mk4(S->dpy.x, S->dpy.y, S->dpy.z, S->dpy.w); }
 };
-
-// Depth of the tile staged in shared memory for early-Z: one 32-bit word per
-// sample, ((y_in_tile * 64 + x_in_tile) * samples + s).  For RG32F and D32F
-// the word is the float depth, for D24S8 the packed depth-stencil word.
-__device__ inline float zword_depth(DrawParams const& p, uint32_t w) {
-  return p.ds_fmt == SG_FMT_D24S8 ? 0.0f : __uint_as_float(w);
-}
-// early_z_test on one pixel against the staged depth (framebuffer.cpp:522-590)
-__device__ inline uint32_t early_z_px_smem(DrawParams const& p, uint32_t* z, uint32_t m, float depth, float const* aa) {
-  uint32_t out = 0;
-  for (uint32_t s = 0; s < p.samples; ++s) {
-    if (!(m & (1u << s))) continue;
-    float nd = p.samples == 1 ? depth : aa[s] + depth;
-    uint32_t w = z[s];
-    DSVal old{0.0f, 0u, 0u};
-    if (p.read_depth) {
-      if (p.ds_fmt == SG_FMT_D24S8)
-        old.q = w & 0xFFFFFFu;
-      else
-        old.depth = zword_depth(p, w);
-    }
-    if (depth_pass(p, nd, old)) {
-      out |= 1u << s;
-      if (p.write_depth)
-        z[s] = p.ds_fmt == SG_FMT_D24S8 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
-    }
-  }
-  return out;
-}
-
-// early_z_test_quad on the staged depth (framebuffer.cpp:556-614): the four
-// pixels of a quad at z (row stride `row` words), pixel depths zq, per-sample
-// offsets aa.  `cfg` packs samples (bits 0-3), read_depth (4), write_depth (5),
-// D24S8 storage (6) and the depth function (bits 8-11).  Out of line with
-// scalar arguments only, so callers keep their state in registers.
-static __device__ __noinline__ uint64_t early_z_quad(uint32_t* z, uint32_t row, uint64_t mask, float4 zq, float4 aa,
-                                                     uint32_t cfg) {
-  uint32_t const samples = cfg & 15u, func = (cfg >> 8) & 15u;
-  bool const rd = (cfg >> 4) & 1u, wr = (cfg >> 5) & 1u, d24 = (cfg >> 6) & 1u;
-  float const zz[4] = {zq.x, zq.y, zq.z, zq.w};
-  float const off[4] = {aa.x, aa.y, aa.z, aa.w};
-  uint64_t out = 0;
-  for (int i = 0; i < 4; ++i) {
-    uint32_t pm = static_cast<uint32_t>(mask >> (16 * i)) & 0xFFFFu;
-    if (!pm) continue;
-    uint32_t* zp = z + (i >> 1) * row + (i & 1) * samples;
-    for (uint32_t s = 0; s < samples; ++s) {
-      if (!(pm & (1u << s))) continue;
-      float nd = samples == 1 ? zz[i] : off[s] + zz[i];
-      uint32_t w = zp[s];
-      bool pass;
-      if (d24) {
-        pass = cmpu(func, d24_quantize(nd), rd ? (w & 0xFFFFFFu) : 0u);
-      } else {
-        pass = cmpf(func, nd, rd ? __uint_as_float(w) : 0.0f);
-      }
-      if (pass) {
-        out |= 1ull << (16 * i + s);
-        if (wr) zp[s] = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
-      }
-    }
-  }
-  return out;
-}
 
 // step_2d_unproj_pos_quad, one pixel of the quad (shader.cpp:257-287)
 template <class TV>
@@ -297,107 +206,31 @@ __device__ inline uint64_t expand_mask(uint32_t c) {
          (static_cast<uint64_t>((c >> 8) & 0xF) << 32) | (static_cast<uint64_t>((c >> 12) & 0xF) << 48);
 }
 
-
 // An owner's append cursor into its chunked fragment list.
 struct OwnerList {
   uint32_t first, cur, count;  // first chunk, current chunk, slots used in it
-  unsigned long long emitted;
 };
 
-__device__ inline void owner_append(DrawParams const& p, OwnerList& L, uint32_t rec, uint32_t pos, uint32_t mask) {
+__device__ inline void owner_append(PassParams const& P, OwnerList& L, uint32_t rec, uint32_t pos, uint32_t mask) {
   if (L.cur == NO_CHUNK || L.count == FRAG_CHUNK) {
-    uint32_t c = atomicAdd(&p.counters->chunk_total, 1u);
-    if (c >= p.chunk_capacity) {
-      atomicOr(&p.counters->overflow, 4u);
+    uint32_t c = atomicAdd(&P.counters->chunk_total, 1u);
+    if (c >= P.chunk_capacity) {
+      atomicOr(&P.counters->overflow, OVF_FRAG);
       return;
     }
     if (L.cur == NO_CHUNK) {
       L.first = c;
     } else {
-      p.chunk_next[L.cur] = c;
-      p.chunk_count[L.cur] = FRAG_CHUNK;
+      P.chunk_next[L.cur] = c;
+      P.chunk_count[L.cur] = FRAG_CHUNK;
     }
     L.cur = c;
     L.count = 0;
   }
   uint32_t f = L.cur * FRAG_CHUNK + L.count++;
-  p.frag_rec[f] = rec;
-  p.frag_pos[f] = pos;
-  p.frag_mask[f] = mask;
-  ++L.emitted;
-}
-
-// Emits one quad (draw_full_quad / draw_quad up to the pixel shader,
-// rasterizer.cpp:1245-1421) after its early-Z test.
-__device__ inline void emit_quad(DrawParams const& p, StageView const& t, uint32_t rec, uint32_t qx_abs, uint32_t qy_abs,
-                                 uint64_t mask, bool full, float4 aa, OwnerList& L, uint32_t* ztile, int tile_x0,
-                                 int tile_y0) {
-  // EXTENSION: pixels outside the render target are not covered.
-  if (qx_abs + 1 >= p.width || qy_abs + 1 >= p.height) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      if (qx_abs + (i & 1) >= p.width || qy_abs + (i >> 1) >= p.height) {
-        mask &= ~(0xFFFFull << (16 * i));
-        full = false;
-      }
-    }
-    if (mask == 0) return;
-  }
-  uint64_t tested = mask;
-  if (p.early_z) {
-    v4 v0 = t.v0(0);
-    float dx = 0.5f + static_cast<float>(qx_abs) - v0.x;
-    float dy = 0.5f + static_cast<float>(qy_abs) - v0.y;
-    float4 zq = make_float4(quad_pos(t, dx, dy, 0).z, quad_pos(t, dx, dy, 1).z, quad_pos(t, dx, dy, 2).z,
-                            quad_pos(t, dx, dy, 3).z);
-    uint32_t cfg = p.samples | (p.read_depth << 4) | (p.write_depth << 5) |
-                   ((p.ds_fmt == SG_FMT_D24S8) ? 64u : 0u) | (p.depth_func << 8);
-    uint32_t px = qx_abs - tile_x0, py = qy_abs - tile_y0;
-    tested = early_z_quad(ztile + (py * TILE + px) * p.samples, TILE * p.samples, mask, zq, aa, cfg);
-  }
-  if (tested == 0) return;
-  owner_append(p, L, rec, (qx_abs >> 1) | ((qy_abs >> 1) << 12) | (full ? 1u << 24 : 0u),
-               compact_mask(tested) | (compact_mask(mask) << 16));
-}
-
-// The per-sample coverage of one 4x4 block (rasterizer::draw_partial_tile, SSE path,
-// rasterizer.cpp:298-439) followed by the quad emission.
-__device__ inline void partial_block(DrawParams const& p, StageView const& t, uint32_t rec, int left, int top,
-                                     float4 aa, OwnerList& L, uint32_t* ztile, int tile_x0, int tile_y0) {
-  float lf = static_cast<float>(left), tf = static_cast<float>(top);
-  float4 e[3] = {t.edge(0), t.edge(1), t.edge(2)};
-  float ev[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) ev[k] = e[k].z - (lf * e[k].x + tf * e[k].y);
-  // per-pixel sample masks packed four samples per nibble: pixel (ix, iy) of
-  // the block at bit 4 * (iy * 4 + ix) (registers only)
-  uint64_t pm = 0;
-  for (uint32_t s = 0; s < p.samples; ++s) {
-#pragma unroll
-    for (int iy = 0; iy < 4; ++iy) {
-      float my = p.sp_y[s] + static_cast<float>(iy);
-#pragma unroll
-      for (int ix = 0; ix < 4; ++ix) {
-        float mx = p.sp_x[s] + static_cast<float>(ix);
-        bool rej = false;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) rej = rej || ((mx * e[k].x + my * e[k].y) < ev[k]);
-        if (!rej) pm |= 1ull << (4 * (iy * 4 + ix) + s);
-      }
-    }
-  }
-  uint32_t fm = (1u << p.samples) - 1u;
-  uint64_t qfull = static_cast<uint64_t>(fm) | (static_cast<uint64_t>(fm) << 16) |
-                   (static_cast<uint64_t>(fm) << 32) | (static_cast<uint64_t>(fm) << 48);
-#pragma unroll 1
-  for (int q = 0; q < 4; ++q) {
-    int qx = (q & 1) << 1, qy = q & 2;
-    int st = qx | (qy << 2);
-    uint64_t m = ((pm >> (4 * st)) & 0xF) | (((pm >> (4 * (st + 1))) & 0xF) << 16) |
-                 (((pm >> (4 * (st + 4))) & 0xF) << 32) | (((pm >> (4 * (st + 5))) & 0xF) << 48);
-    if (m == 0) continue;
-    emit_quad(p, t, rec, left + qx, top + qy, m, m == qfull, aa, L, ztile, tile_x0, tile_y0);
-  }
+  P.frag_rec[f] = rec;
+  P.frag_pos[f] = pos;
+  P.frag_mask[f] = mask;
 }
 
 // Per-level edge parameters of one triangle: TILE * e, then * 0.25 per level
@@ -433,54 +266,8 @@ __device__ inline int child_class(float4 const* e, LevelParams const& l, float l
   return rej ? 0 : (accf ? 1 : 2);
 }
 
-// One triangle against this thread's 4x4 block.  `full16` says the block's
-// 16x16 region (or the whole tile) was accepted; otherwise the 16x16 region
-// was partial and the block passed the level-2 bounding-box test, and the
-// reference's level-2 edge test decides (rasterizer.cpp:617-773).
-__device__ inline void raster_block(DrawParams const& p, TriStage const* st, bool full16, int tile_x0, int tile_y0,
-                                   int bx, int by, OwnerList& L, uint32_t* ztile) {
-  uint32_t rec = st->entry >> 1;
-  StageView t{st};
-  float const trr = p.target_w, trb = p.target_h;
-  float4 aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  if (p.samples > 1) {
-    float dz = t.ddx(0).z, dyz = t.ddy(0).z;
-    aa.x = (p.sp_x[0] - 0.5f) * dz + (p.sp_y[0] - 0.5f) * dyz;
-    aa.y = (p.sp_x[1] - 0.5f) * dz + (p.sp_y[1] - 0.5f) * dyz;
-    if (p.samples > 2) {
-      aa.z = (p.sp_x[2] - 0.5f) * dz + (p.sp_y[2] - 0.5f) * dyz;
-      aa.w = (p.sp_x[3] - 0.5f) * dz + (p.sp_y[3] - 0.5f) * dyz;
-    }
-  }
-  int const bx_abs = tile_x0 + bx * 4, by_abs = tile_y0 + by * 4;
-  bool draw_all = full16;
-  if (!full16) {
-    float4 e[3] = {t.edge(0), t.edge(1), t.edge(2)};
-    LevelParams l1, l2;
-    level_params(e, l1, l2);
-    int r16x = tile_x0 + (bx >> 2) * 16, r16y = tile_y0 + (by >> 2) * 16;
-    int c = child_class(e, l2, static_cast<float>(r16x), static_cast<float>(r16y), bx & 3, by & 3);
-    if (c == 0) return;
-    if (static_cast<float>(bx_abs) >= trr || static_cast<float>(by_abs) >= trb) return;
-    if (c == 1) {
-      partial_block(p, t, rec, bx_abs, by_abs, aa, L, ztile, tile_x0, tile_y0);
-      return;
-    }
-    draw_all = true;
-  }
-  if (draw_all) {
-    // draw_full_tile over a region containing this block: quads left of the
-    // target's right edge and above its bottom edge (rasterizer.cpp:285-296,738-742)
-    uint32_t fm = (1u << p.samples) - 1u;
-    uint64_t qfull = static_cast<uint64_t>(fm) | (static_cast<uint64_t>(fm) << 16) |
-                     (static_cast<uint64_t>(fm) << 32) | (static_cast<uint64_t>(fm) << 48);
-    uint32_t vr = static_cast<uint32_t>(trr), vb = static_cast<uint32_t>(trb);
-#pragma unroll 1
-    for (int q = 0; q < 4; ++q) {
-      uint32_t qx = bx_abs + ((q & 1) << 1), qy = by_abs + (q & 2);
-      if (qx < vr && qy < vb) emit_quad(p, t, rec, qx, qy, qfull, true, aa, L, ztile, tile_x0, tile_y0);
-    }
-  }
+__device__ inline uint32_t target_of_tile(PassParams const& P, uint32_t tile) {
+  return upper_index(P.target_tile_base, P.ntargets, tile);
 }
 
 #ifdef SG_RASTER_COVER_MERGE  // defined by the one translation unit that owns these kernels
@@ -488,7 +275,6 @@ constexpr int STAGE_TRIS = 256;  // triangles staged in shared memory per batch
 constexpr int MASK_WORDS = STAGE_TRIS / 32;
 constexpr int COVER_THREADS = 128;  // one CTA per 32x32 quadrant of a tile
 constexpr int QUAD_PX = 32;
-constexpr uint32_t SPLIT_ENTRIES = 320;  // tiles with more bin entries are covered as 16 regions
 constexpr size_t COVER_SMEM_BASE = STAGE_TRIS * sizeof(TriStage) + (64 + 4) * MASK_WORDS * sizeof(uint32_t);
 // plus the staged depth: QUAD_PX * QUAD_PX * samples words (only when early-Z is on)
 __host__ __device__ constexpr size_t cover_smem(uint32_t samples, bool early_z) {
@@ -496,7 +282,7 @@ __host__ __device__ constexpr size_t cover_smem(uint32_t samples, bool early_z) 
 }
 
 // The sample slots a lane covers in a (triangle, block) pair: slot lane + 32
-// pass of the block's 16 pixels x samples, pixel-major.  Fixed per draw.
+// pass of the block's 16 pixels x samples, pixel-major.  Fixed per target.
 struct LaneSlots {
   uint32_t bit[2];   // the slot's bit in its half-block coverage word; 0 if unused
   uint32_t pix[2];   // ix | iy << 2 | sm << 4 | quad << 8 | pixel-in-quad << 10
@@ -504,9 +290,9 @@ struct LaneSlots {
   float mx[2], my[2];  // sample position in the block
   float ax[2], ay[2];  // sample offset from the pixel centre (aa_z_offset)
 };
-__device__ inline LaneSlots lane_slots(DrawParams const& p, int lane, int zpitch) {
+__device__ inline LaneSlots lane_slots(TargetParams const& T, int lane, int zpitch) {
   LaneSlots ls;
-  uint32_t const S = p.samples;
+  uint32_t const S = T.samples;
 #pragma unroll
   for (int pass = 0; pass < 2; ++pass) {
     uint32_t slot = lane + 32 * pass;
@@ -516,10 +302,10 @@ __device__ inline LaneSlots lane_slots(DrawParams const& p, int lane, int zpitch
     ls.bit[pass] = slot < 16 * S ? 1u << (4 * i + sm + 16 * (q & 1)) : 0u;
     ls.pix[pass] = ix | (iy << 2) | (sm << 4) | (q << 8) | (i << 10);
     ls.zoff[pass] = (iy * zpitch + ix) * S + sm;
-    ls.mx[pass] = p.sp_x[sm & 3u] + static_cast<float>(ix);
-    ls.my[pass] = p.sp_y[sm & 3u] + static_cast<float>(iy);
-    ls.ax[pass] = p.sp_x[sm & 3u] - 0.5f;
-    ls.ay[pass] = p.sp_y[sm & 3u] - 0.5f;
+    ls.mx[pass] = T.sp_x[sm & 3u] + static_cast<float>(ix);
+    ls.my[pass] = T.sp_y[sm & 3u] + static_cast<float>(iy);
+    ls.ax[pass] = T.sp_x[sm & 3u] - 0.5f;
+    ls.ay[pass] = T.sp_y[sm & 3u] - 0.5f;
   }
   return ls;
 }
@@ -530,13 +316,13 @@ __device__ inline LaneSlots lane_slots(DrawParams const& p, int lane, int zpitch
 // (framebuffer.cpp:522-614) over the block's 16 pixels x samples, one sample
 // slot per lane and pass; the quads' masks are assembled with warp
 // reductions and the block's owner lane appends the surviving quads.
-__device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool full16, int tile_x0, int tile_y0, int blk,
-                                 int owner, OwnerList& L, uint32_t* ztile, int zx0, int zy0, int zpitch,
-                                 LaneSlots const& ls, int lane) {
+__device__ inline void pair_warp(PassParams const& P, TargetParams const& T, TriStage const* st, bool full16,
+                                 int tile_x0, int tile_y0, int blk, int owner, OwnerList& L, uint32_t* ztile, int zx0,
+                                 int zy0, int zpitch, LaneSlots const& ls, int lane) {
   StageView t{st};
   int const bx = blk & 15, by = blk >> 4;
   int const bx_abs = tile_x0 + bx * 4, by_abs = tile_y0 + by * 4;
-  float const trr = p.target_w, trb = p.target_h;
+  float const trr = T.target_w, trb = T.target_h;
   float4 e[3] = {t.edge(0), t.edge(1), t.edge(2)};
   bool region_full = full16;
   if (!full16) {
@@ -548,7 +334,7 @@ __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool f
     if (static_cast<float>(bx_abs) >= trr || static_cast<float>(by_abs) >= trb) return;
     region_full = c == 2;
   }
-  uint32_t const W = p.width, H = p.height;
+  uint32_t const W = T.width, H = T.height;
   float const lf = static_cast<float>(bx_abs), tf = static_cast<float>(by_abs);
   float ev[3];
 #pragma unroll
@@ -585,19 +371,20 @@ __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool f
   cv_lo = __reduce_or_sync(0xFFFFFFFFu, cv_lo);
   cv_hi = __reduce_or_sync(0xFFFFFFFFu, cv_hi);
   if ((cv_lo | cv_hi) == 0) return;
-  uint32_t const fm = (1u << p.samples) - 1u;
+  uint32_t const fm = (1u << T.samples) - 1u;
   uint32_t const qfull = fm | (fm << 4) | (fm << 8) | (fm << 12);
   // a full region's quads are drawn when their left / top pixel is inside the
   // target (draw_full_tile, rasterizer.cpp:738-742): no quad of this block is
   // dropped by that rule once its covered pixels are clipped to the target.
   uint32_t tested_lo = cv_lo, tested_hi = cv_hi;
-  if (p.early_z) {
+  uint32_t const zc = st->zcfg;
+  if (zc & 128u) {  // early-Z: depth test and write now, on the staged depth
     v4 v0 = t.v0(0);
     float dz = t.ddx(0).z, dyz = t.ddy(0).z;
     uint32_t t_lo = 0, t_hi = 0;
-    uint32_t cfg_rd = p.read_depth, cfg_wr = p.write_depth;
-    bool d24 = p.ds_fmt == SG_FMT_D24S8;
-    uint32_t* zblk = ztile + ((by_abs - zy0) * zpitch + (bx_abs - zx0)) * p.samples;
+    uint32_t const func = (zc >> 8) & 15u;
+    bool const rd = (zc >> 4) & 1u, wr = (zc >> 5) & 1u, d24 = (zc >> 6) & 1u;
+    uint32_t* zblk = ztile + ((by_abs - zy0) * zpitch + (bx_abs - zx0)) * T.samples;
 #pragma unroll
     for (int pass = 0; pass < 2; ++pass) {
       uint32_t bit = ls.bit[pass], pix = ls.pix[pass];
@@ -608,13 +395,13 @@ __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool f
       float dx = 0.5f + static_cast<float>(qx) - v0.x;
       float dy = 0.5f + static_cast<float>(qy) - v0.y;
       float z = quad_pos(t, dx, dy, static_cast<int>(i)).z;
-      float nd = p.samples == 1 ? z : (ls.ax[pass] * dz + ls.ay[pass] * dyz) + z;
+      float nd = T.samples == 1 ? z : (ls.ax[pass] * dz + ls.ay[pass] * dyz) + z;
       uint32_t* zp = zblk + ls.zoff[pass];
       uint32_t w = *zp;
-      bool pass_z = d24 ? cmpu(p.depth_func, d24_quantize(nd), cfg_rd ? (w & 0xFFFFFFu) : 0u)
-                        : cmpf(p.depth_func, nd, cfg_rd ? __uint_as_float(w) : 0.0f);
+      bool pass_z = d24 ? cmpu(func, d24_quantize(nd), rd ? (w & 0xFFFFFFu) : 0u)
+                        : cmpf(func, nd, rd ? __uint_as_float(w) : 0.0f);
       if (pass_z) {
-        if (cfg_wr) *zp = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
+        if (wr) *zp = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
         if (hi) t_hi |= bit; else t_lo |= bit;
       }
     }
@@ -623,6 +410,7 @@ __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool f
   }
   if (lane == owner) {
     uint32_t const rec = st->entry >> 1;
+    uint32_t const na = st->nattr << 25;
 #pragma unroll 1
     for (int q = 0; q < 4; ++q) {
       uint32_t tq = ((q < 2 ? tested_lo : tested_hi) >> (16 * (q & 1))) & 0xFFFFu;
@@ -631,13 +419,10 @@ __device__ inline void pair_warp(DrawParams const& p, TriStage const* st, bool f
       uint32_t uq = ((q < 2 ? uc_lo : uc_hi) >> (16 * (q & 1))) & 0xFFFFu;
       bool full = region_full ? cq == qfull : (uq == qfull && cq == uq);
       uint32_t qx = bx_abs + ((q & 1) << 1), qy = by_abs + (q & 2);
-      owner_append(p, L, rec, (qx >> 1) | ((qy >> 1) << 12) | (full ? 1u << 24 : 0u), tq | (cq << 16));
+      owner_append(P, L, rec, (qx >> 1) | ((qy >> 1) << 12) | (full ? 1u << 24 : 0u) | na, tq | (cq << 16));
     }
   }
 }
-
-__device__ inline int tile_x0_of(DrawParams const& p, uint32_t tile) { return static_cast<int>(tile % p.tiles_x) * TILE; }
-__device__ inline int tile_y0_of(DrawParams const& p, uint32_t tile) { return static_cast<int>(tile / p.tiles_x) * TILE; }
 
 // Block owned by lane l < 4 n of warp w in an n x n-block item (n = 8 or 4):
 // the blocks (x, y) with (x + y) mod 4 = w, so that the blocks along a row, a
@@ -652,14 +437,14 @@ __device__ inline void owned_block(int n, int w, int l, int& x, int& y) {
   }
 }
 
-// Coverage of one draw.  Work items are squares of one tile: its four 32x32
-// quadrants, or, for a tile with more than SPLIT_ENTRIES bin entries, its
+// Coverage of one pass.  Work items are squares of one tile: its four 32x32
+// quadrants, or, for a tile with more than P.split_entries bin entries, its
 // sixteen 16x16 regions, taken from a dynamic cursor over 16 item slots per
 // tile.  A CTA stages the tile's triangles in batches, classifies them
 // against the item's 16x16 regions and 4x4 blocks (rasterizer.cpp:441-571),
 // and its four warps walk (triangle, block) pairs in primitive order with the
 // item's depth held in shared memory for early-Z.
-__global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nreg) {
+__global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
   extern __shared__ __align__(16) uint8_t smem[];
   TriStage* stage = reinterpret_cast<TriStage*>(smem);
   // triangle sets of the staged batch (word-major): per 4x4 block of the item
@@ -669,27 +454,27 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
   uint32_t* mask16 = mask4 + 64 * MASK_WORDS;
   uint32_t* ztile = mask16 + 4 * MASK_WORDS;
   __shared__ uint32_t s_item;
-  if (p.counters->overflow & 1u) return;
+  if (P.counters->overflow & (OVF_BIN | OVF_REC)) return;
   int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  uint32_t const nslots = static_cast<uint32_t>(p.tiles_x * p.tiles_y) * 16;
-  float const trr = p.target_w, trb = p.target_h;
-  uint32_t const S = p.samples;
-  OwnerList L{NO_CHUNK, NO_CHUNK, 0, 0};
+  uint32_t const nslots = P.ntiles * 16;
+  OwnerList L{NO_CHUNK, NO_CHUNK, 0};
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(&p.counters->tile_cursor, 1u);
+    if (tid == 0) s_item = atomicAdd(&P.counters->tile_cursor, 1u);
     __syncthreads();
     uint32_t const item = s_item;
     __syncthreads();
     if (item >= nslots) break;
     uint32_t const tile = item >> 4, sub = item & 15;
-    uint32_t const begin = p.tile_begin[tile], end = p.tile_begin[tile + 1];
-    bool const split = end - begin > SPLIT_ENTRIES;
+    uint32_t const begin = P.tile_begin[tile], end = P.tile_begin[tile + 1];
+    bool const split = P.cover_item == 16 || end - begin > P.split_entries;
     if (!split && sub >= 4) continue;
+    TargetParams const& T = P.targets[target_of_tile(P, tile)];
+    uint32_t const ltile = tile - T.tile_base;
     int const n = split ? 4 : 8;   // blocks per side
     int const px = 4 * n;          // pixels per side
     int const rs = n >> 2;         // 16x16 regions per side
     int const bx0 = split ? (sub & 3) * 4 : (sub & 1) * 8, by0 = split ? (sub >> 2) * 4 : (sub >> 1) * 8;
-    int const tile_x0 = tile_x0_of(p, tile), tile_y0 = tile_y0_of(p, tile);
+    int const tile_x0 = static_cast<int>(ltile % T.tiles_x) * TILE, tile_y0 = static_cast<int>(ltile / T.tiles_x) * TILE;
     int const x0 = tile_x0 + bx0 * 4, y0 = tile_y0 + by0 * 4;
     int const r16x0 = bx0 >> 2, r16y0 = by0 >> 2;  // first 16x16 region of the item
     bool const owns = lane < (n == 8 ? 16 : 4);
@@ -698,20 +483,22 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
     int const blk = (by0 + oy) * 16 + bx0 + ox;           // owned block, tile numbering
     int const ib = oy * n + ox;                            // owned block, item numbering
     int const own16 = (oy >> 2) * rs + (ox >> 2);          // its 16x16 region, item numbering
-    LaneSlots const ls = lane_slots(p, lane, px);
+    LaneSlots const ls = lane_slots(T, lane, px);
     float const tx0f = static_cast<float>(tile_x0), ty0f = static_cast<float>(tile_y0);
+    float const trr = T.target_w, trb = T.target_h;
+    uint32_t const S = T.samples;
     L.first = L.cur = NO_CHUNK;
     L.count = 0;
-    bool const stage_z = p.early_z && begin < end;
-    uint32_t const qw = min(static_cast<uint32_t>(px), p.width - min(p.width, static_cast<uint32_t>(x0)));
-    uint32_t const qh = min(static_cast<uint32_t>(px), p.height - min(p.height, static_cast<uint32_t>(y0)));
+    bool const stage_z = T.any_early_z && begin < end;
+    uint32_t const qw = min(static_cast<uint32_t>(px), T.width - min(T.width, static_cast<uint32_t>(x0)));
+    uint32_t const qh = min(static_cast<uint32_t>(px), T.height - min(T.height, static_cast<uint32_t>(y0)));
     uint32_t const zrow = px * S;
     if (stage_z) {
       for (uint32_t i = tid; i < qh * zrow; i += COVER_THREADS) {
         uint32_t y = i / zrow, k = i % zrow;
         if (k >= qw * S) continue;
         uint32_t x = k / S, sm = k % S;
-        ztile[i] = *reinterpret_cast<uint32_t const*>(ds_addr(p, x0 + x, y0 + y, sm));
+        ztile[i] = *reinterpret_cast<uint32_t const*>(ds_addr(T, x0 + x, y0 + y, sm));
       }
     }
     for (uint32_t bstart = begin; bstart < end; bstart += STAGE_TRIS) {
@@ -721,8 +508,10 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
       __syncthreads();
       // stage the batch and classify each triangle against the item's 16x16 regions
       for (uint32_t i = tid; i < nb; i += COVER_THREADS) {
-        uint32_t e = p.bin_entries[bstart + i];
-        float4 const* R = p.recs + static_cast<size_t>(e >> 1) * p.rec_stride;
+        uint32_t e = P.bin_entries[bstart + i];
+        float4 const* R = P.recs + (e >> 1);
+        DrawParams const& D = P.draws[rec_draw(R)];
+        int const nreg = 1 + static_cast<int>(D.nattr);
         TriStage ts;
         ts.e0 = R[0];
         ts.e1 = R[1];
@@ -732,6 +521,9 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
         ts.dpx = R[5 + nreg];
         ts.dpy = R[5 + 2 * nreg];
         ts.entry = e;
+        ts.zcfg = D.zcfg;
+        ts.nattr = D.nattr;
+        ts.pad = 0;
         stage[i] = ts;
         uint32_t bit = 1u << (i & 31), word = i >> 5;
         if (e & 1u) {  // accepted for the whole tile by the binner
@@ -789,8 +581,8 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
             int lx, ly;
             owned_block(n, warp, l, lx, ly);
             int oblk = (by0 + ly) * 16 + bx0 + lx;
-            pair_warp(p, stage + (w << 5) + b, (fulls >> l) & 1u, tile_x0, tile_y0, oblk, l, L, ztile, x0, y0, px,
-                      ls, lane);
+            pair_warp(P, T, stage + (w << 5) + b, (fulls >> l) & 1u, tile_x0, tile_y0, oblk, l, L, ztile, x0, y0,
+                      px, ls, lane);
           }
         }
       }
@@ -801,21 +593,18 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
         uint32_t y = i / zrow, k = i % zrow;
         if (k >= qw * S) continue;
         uint32_t x = k / S, sm = k % S;
-        *reinterpret_cast<uint32_t*>(ds_addr(p, x0 + x, y0 + y, sm)) = ztile[i];
+        *reinterpret_cast<uint32_t*>(ds_addr(T, x0 + x, y0 + y, sm)) = ztile[i];
       }
     }
     // close the owned block's list for the item
     if (owns) {
       if (L.cur != NO_CHUNK) {
-        p.chunk_next[L.cur] = NO_CHUNK;
-        p.chunk_count[L.cur] = L.count;
+        P.chunk_next[L.cur] = NO_CHUNK;
+        P.chunk_count[L.cur] = L.count;
       }
-      p.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + blk] = L.first;
+      P.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + blk] = L.first;
     }
   }
-  unsigned long long ps_inv = 4ull * L.emitted;
-  for (int o = 16; o > 0; o >>= 1) ps_inv += __shfl_down_sync(0xFFFFFFFFu, ps_inv, o);
-  if (lane == 0 && ps_inv) atomicAdd(&p.counters->ps_invocations, ps_inv);
 }
 
 #endif  // SG_RASTER_COVER_MERGE
@@ -824,7 +613,7 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(DrawParams p, int nr
 // (lanes 4k..4k+3 of the warp); tex2d's LOD uses the quad differences
 // (cpp_pixel_shader.cpp:13-31).
 template <int NA>
-__device__ inline v4 run_ps(DrawParams const& p, v4 const* attr, int q) {
+__device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q) {
   v4 a0 = NA > 0 ? attr[0] : mk4(0, 0, 0, 0);
   v4 a1 = NA > 1 ? attr[1 < NA ? 1 : 0] : mk4(0, 0, 0, 0);
   int base = (threadIdx.x & 31) & ~3;
@@ -832,39 +621,46 @@ __device__ inline v4 run_ps(DrawParams const& p, v4 const* attr, int q) {
   float u0 = __shfl_sync(mask, a0.x, base), v0 = __shfl_sync(mask, a0.y, base);
   float u1 = __shfl_sync(mask, a0.x, base + 1), v1 = __shfl_sync(mask, a0.y, base + 1);
   float u2 = __shfl_sync(mask, a0.x, base + 2), v2 = __shfl_sync(mask, a0.y, base + 2);
-  switch (p.ps_prog) {
+  switch (D.ps_prog) {
   case SG_PS_COLOR: return a0;
-  case SG_PS_CONSTANT: return mk4(p.ps_k[0], p.ps_k[1], p.ps_k[2], p.ps_k[3]);
+  case SG_PS_CONSTANT: return mk4(D.ps_k[0], D.ps_k[1], D.ps_k[2], D.ps_k[3]);
   case SG_PS_TEX_MODULATE: {
-    float lod = calc_lod_2d(p.ps_samp, u1 - u0, v1 - v0, u2 - u0, v2 - v0);
-    return mulv(sample_impl(p.ps_samp, a0.x, a0.y, lod, nullptr), a1);
+    float lod = calc_lod_2d(D.ps_samp, u1 - u0, v1 - v0, u2 - u0, v2 - v0);
+    return mulv(sample_impl(D.ps_samp, a0.x, a0.y, lod, nullptr), a1);
   }
   case SG_PS_TEX_GRAD_MODULATE:
-    return mulv(sample_2d_grad(p.ps_samp, a0.x, a0.y, u1 - u0, v1 - v0, u2 - u0, v2 - v0, 0.0f), a1);
+    return mulv(sample_2d_grad(D.ps_samp, a0.x, a0.y, u1 - u0, v1 - v0, u2 - u0, v2 - v0, 0.0f), a1);
   default: return mk4(0, 0, 0, 0);
   }
 }
 
 // Attribute interpolation (step_2d_unproj_attr_n_quad / step_2d_unproj_attr_n
 // with the centroid adjustment, shader.cpp:208-367, rasterizer.cpp:1363-1398)
-// and the pixel shader, for every fragment of the draw.
+// and the pixel shader, for every fragment of the pass whose draw has NA
+// varyings.
 template <int NA>
-__global__ void __launch_bounds__(256) k_shade(DrawParams p) {
-  uint32_t const nfrag = min(p.counters->chunk_total, p.chunk_capacity) * FRAG_CHUNK;
-  if (p.counters->overflow & 5u) return;
+__global__ void __launch_bounds__(256) k_shade(PassParams P) {
+  if (P.counters->overflow & (OVF_BIN | OVF_FRAG | OVF_REC)) return;
+  uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
   int const q = threadIdx.x & 3;
   uint32_t const groups = gridDim.x * (blockDim.x >> 2);
   uint32_t const start = blockIdx.x * (blockDim.x >> 2) + (threadIdx.x >> 2);
   uint32_t const rounds = (nfrag + groups - 1) / groups;
   for (uint32_t it = 0; it < rounds; ++it) {
     uint32_t f = start + it * groups;
-    bool live = f < nfrag && (f % FRAG_CHUNK) < p.chunk_count[f / FRAG_CHUNK];
-    v4 attr[NA > 0 ? NA : 1];
-#pragma unroll
-    for (int i = 0; i < (NA > 0 ? NA : 1); ++i) attr[i] = mk4(0, 0, 0, 0);
+    bool live = f < nfrag && (f % FRAG_CHUNK) < P.chunk_count[f / FRAG_CHUNK];
+    uint32_t pos = live ? P.frag_pos[f] : 0u;
+    live = live && ((pos >> 25) & 7u) == static_cast<uint32_t>(NA);
+    uint32_t draw = 0xFFFFFFFFu;
     if (live) {
-      uint32_t rec = p.frag_rec[f], pos = p.frag_pos[f], masks = p.frag_mask[f];
-      TriView t{p.recs + static_cast<size_t>(rec) * p.rec_stride, 1 + NA};
+      uint32_t rec = P.frag_rec[f], masks = P.frag_mask[f];
+      TriView t{P.recs + rec, 1 + NA};
+      draw = rec_draw(t.R);
+      DrawParams const& D = P.draws[draw];
+      TargetParams const& T = P.targets[D.target];
+      v4 attr[NA > 0 ? NA : 1];
+#pragma unroll
+      for (int i = 0; i < (NA > 0 ? NA : 1); ++i) attr[i] = mk4(0, 0, 0, 0);
       uint32_t qx = (pos & 0xFFFu) << 1, qy = ((pos >> 12) & 0xFFFu) << 1;
       bool full = (pos >> 24) & 1u;
       v4 v0p = t.v0(0);
@@ -872,21 +668,21 @@ __global__ void __launch_bounds__(256) k_shade(DrawParams p) {
       float dy = 0.5f + static_cast<float>(qy) - v0p.y;
       float w = quad_pos(t, dx, dy, q).w;
       float invw = 1.0f / w;
-      bool centroid = !full && p.has_centroid;
+      bool centroid = !full && D.has_centroid;
       float pdx = dx, pdy = dy;
       if (centroid) {
         pdx = dx + static_cast<float>(q & 1);
         pdy = dy + static_cast<float>(q >> 1);
         uint64_t m = expand_mask(masks >> 16);  // coverage before early-Z (rasterizer.cpp:1373)
         uint32_t pm = static_cast<uint32_t>(m >> (16 * q)) & 0xFFFFu;
-        uint32_t fm = (1u << p.samples) - 1u;
+        uint32_t fm = (1u << T.samples) - 1u;
         if (pm != fm && pm != 0) {
           float cx = 0.0f, cy = 0.0f;
           int n = 0;
-          for (uint32_t s = 0; s < p.samples; ++s)
+          for (uint32_t s = 0; s < T.samples; ++s)
             if (pm & (1u << s)) {
-              cx += p.sp_x[s];
-              cy += p.sp_y[s];
+              cx += T.sp_x[s];
+              cy += T.sp_y[s];
               ++n;
             }
           float inv = 1.0f / static_cast<float>(n);
@@ -900,7 +696,7 @@ __global__ void __launch_bounds__(256) k_shade(DrawParams p) {
       for (int i = 0; i < NA; ++i) {
         v4 in = t.v0(1 + i), d0 = t.ddx(1 + i), d1 = t.ddy(1 + i);
         v4 a;
-        if (p.mods[i] & SG_AM_NOINTERPOLATION) {
+        if (D.mods[i] & SG_AM_NOINTERPOLATION) {
           a = in;
         } else if (centroid) {
           a = mk4(in.x + (d0.x * pdx + d1.x * pdy), in.y + (d0.y * pdx + d1.y * pdy), in.z + (d0.z * pdx + d1.z * pdy),
@@ -910,42 +706,47 @@ __global__ void __launch_bounds__(256) k_shade(DrawParams p) {
                        in.w + (d0.w * dx + d1.w * dy));
           a = q == 0 ? a00 : q == 1 ? a00 + d0 : q == 2 ? a00 + d1 : (a00 + d0) + d1;
         }
-        attr[i] = (p.mods[i] & SG_AM_NOPERSPECTIVE) ? a : a * invw;
+        attr[i] = (D.mods[i] & SG_AM_NOPERSPECTIVE) ? a : a * invw;
       }
+      v4 out = run_ps<NA>(D, attr, q);  // all four lanes of a quad take the same path
+      P.frag_color[static_cast<size_t>(f) * 4 + q] = make_float4(out.x, out.y, out.z, out.w);
+      if (q == 0) P.frag_ps[f] = 0xF;  // the stock programs never discard
     }
-    v4 out = run_ps<NA>(p, attr, q);  // all four lanes of a quad take the same path
-    if (live) {
-      p.frag_color[static_cast<size_t>(f) * 4 + q] = make_float4(out.x, out.y, out.z, out.w);
-      if (q == 0) p.frag_ps[f] = 0xF;  // the stock programs never discard
-    }
+    // ps_invocations: 4 per quad, counted per draw (one lane per quad)
+    uint32_t key = q == 0 ? draw : 0xFFFFFFFFu;
+    uint32_t grp = __match_any_sync(0xFFFFFFFFu, key);
+    if (key != 0xFFFFFFFFu && (threadIdx.x & 31) == static_cast<uint32_t>(__ffs(grp) - 1))
+      atomicAdd(&P.draw_stats[key].ps_invocations, 4ull * static_cast<unsigned>(__popc(grp)));
   }
 }
 
 #ifdef SG_RASTER_COVER_MERGE
 // Output merging per tile: owners replay their fragments in primitive order
 // (framebuffer::render_sample_quad, framebuffer.cpp:481-520).
-__global__ void __launch_bounds__(RASTER_THREADS) k_merge(DrawParams p, int nreg) {
+__global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
   __shared__ uint32_t s_tile;
-  if (p.counters->overflow & 5u) return;
-  int const tid = threadIdx.x, lane = tid & 31;
-  int const ntiles = p.tiles_x * p.tiles_y;
+  uint32_t const ovf = P.counters->overflow;  // final: geometry, binning and coverage are done
+  if (blockIdx.x == 0 && threadIdx.x == 0 && ovf) atomicOr(P.sticky, ovf);
+  if (ovf & (OVF_BIN | OVF_FRAG | OVF_REC)) return;
+  int const tid = threadIdx.x;
+  uint32_t cur_draw = 0xFFFFFFFFu;
   unsigned long long backend = 0;
   for (;;) {
-    if (tid == 0) s_tile = atomicAdd(&p.counters->merge_cursor, 1u);
+    if (tid == 0) s_tile = atomicAdd(&P.counters->merge_cursor, 1u);
     __syncthreads();
     uint32_t tile = s_tile;
     __syncthreads();
-    if (tile >= static_cast<uint32_t>(ntiles)) break;
-    uint32_t c = p.tile_begin[tile] == p.tile_begin[tile + 1]
+    if (tile >= P.ntiles) break;
+    uint32_t c = P.tile_begin[tile] == P.tile_begin[tile + 1]
                      ? NO_CHUNK
-                     : p.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + tid];
+                     : P.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + tid];
     while (c != NO_CHUNK) {
-      uint32_t n = p.chunk_count[c];
+      uint32_t n = P.chunk_count[c];
       for (uint32_t k = 0; k < n; ++k) {
         uint32_t f = c * FRAG_CHUNK + k;
-        uint32_t rec = p.frag_rec[f], pos = p.frag_pos[f], masks = p.frag_mask[f];
+        uint32_t rec = P.frag_rec[f], pos = P.frag_pos[f], masks = P.frag_mask[f];
         uint64_t m = expand_mask(masks & 0xFFFFu);
-        uint32_t ps = p.frag_ps[f];
+        uint32_t ps = P.frag_ps[f];
         uint64_t psm = 0;
 #pragma unroll
         for (int i = 0; i < 4; ++i)
@@ -953,50 +754,58 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(DrawParams p, int nreg
         m &= psm;
         bool full = (pos >> 24) & 1u;
         if (full && m == 0) continue;
+        float4 const* R = P.recs + rec;
+        uint32_t const draw = rec_draw(R);
+        if (draw != cur_draw) {
+          if (backend) atomicAdd(&P.draw_stats[cur_draw].backend_input_pixels, backend);
+          backend = 0;
+          cur_draw = draw;
+        }
         backend += 4;
-        TriView t{p.recs + static_cast<size_t>(rec) * p.rec_stride, nreg};
+        DrawParams const& D = P.draws[draw];
+        TargetParams const& T = P.targets[D.target];
+        TriView t{R, 1 + static_cast<int>(D.nattr)};
         uint32_t qx = (pos & 0xFFFu) << 1, qy = ((pos >> 12) & 0xFFFu) << 1;
         bool front = t.front();
         float depth[4] = {0, 0, 0, 0};
         float aa[4] = {0, 0, 0, 0};
-        if (!p.early_z && p.ds) {
+        if (!D.early_z && T.ds) {
           v4 v0p = t.v0(0);
           float dx = 0.5f + static_cast<float>(qx) - v0p.x;
           float dy = 0.5f + static_cast<float>(qy) - v0p.y;
 #pragma unroll
           for (int i = 0; i < 4; ++i) depth[i] = quad_pos(t, dx, dy, i).z;
-          if (p.samples > 1) {
+          if (T.samples > 1) {
             float dz = t.ddx(0).z, dyz = t.ddy(0).z;
-            for (uint32_t s = 0; s < p.samples; ++s) aa[s] = (p.sp_x[s] - 0.5f) * dz + (p.sp_y[s] - 0.5f) * dyz;
+            for (uint32_t s = 0; s < T.samples; ++s) aa[s] = (T.sp_x[s] - 0.5f) * dz + (T.sp_y[s] - 0.5f) * dyz;
           }
         }
         for (int i = 0; i < 4; ++i) {
           uint32_t pm = static_cast<uint32_t>(m >> (16 * i)) & 0xFFFFu;
           if (!pm) continue;
-          float4 c = p.frag_color[static_cast<size_t>(f) * 4 + i];
-          v4 src = mk4(c.x, c.y, c.z, c.w);
+          float4 cc = P.frag_color[static_cast<size_t>(f) * 4 + i];
+          v4 src = mk4(cc.x, cc.y, cc.z, cc.w);
           uint32_t x = qx + (i & 1), y = qy + (i >> 1);
-          if (p.samples == 1) {
-            render_sample(p, x, y, 0, src, depth[i], front);
+          if (T.samples == 1) {
+            render_sample(T, D, x, y, 0, src, depth[i], front);
           } else {
-            for (uint32_t s = 0; s < p.samples; ++s)
-              if (pm & (1u << s)) render_sample(p, x, y, s, src, depth[i] + aa[s], front);
+            for (uint32_t s = 0; s < T.samples; ++s)
+              if (pm & (1u << s)) render_sample(T, D, x, y, s, src, depth[i] + aa[s], front);
           }
         }
       }
-      c = p.chunk_next[c];
+      c = P.chunk_next[c];
     }
   }
-  for (int o = 16; o > 0; o >>= 1) backend += __shfl_down_sync(0xFFFFFFFFu, backend, o);
-  if (lane == 0 && backend) atomicAdd(&p.counters->backend_input_pixels, backend);
+  if (backend) atomicAdd(&P.draw_stats[cur_draw].backend_input_pixels, backend);
 }
 
 #endif  // SG_RASTER_COVER_MERGE
 
 // ---------------------------------------------------------------------------
 template <int NA>
-void launch_shade_t(DrawParams const& p, uint32_t grid, cudaStream_t s) {
-  k_shade<NA><<<grid, 256, 0, s>>>(p);
+void launch_shade_t(PassParams const& P, uint32_t grid, cudaStream_t s) {
+  k_shade<NA><<<grid, 256, 0, s>>>(P);
 }
 
 }  // namespace sg

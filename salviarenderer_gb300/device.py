@@ -154,6 +154,41 @@ class Device:
             return None
         return {k: getattr(st, k) for k, _ in abi.DrawStats._fields_}
 
+    # -- command lists (sg_submit) and recorded graphs --------------------------
+    def submit(self, cmds, stats=False):
+        """Runs a CommandList; with stats, returns one dict per command."""
+        arr = cmds.array()
+        st = (abi.DrawStats * len(cmds))() if stats else None
+        self._check("sg_submit", self.lib.sg_submit(self.handle, arr, len(cmds), st))
+        if st is None:
+            return None
+        return [{k: getattr(x, k) for k, _ in abi.DrawStats._fields_} for x in st]
+
+    def graph_create(self, cmds):
+        g = C.c_void_p()
+        self._check("sg_graph_create",
+                    self.lib.sg_graph_create(self.handle, cmds.array(), len(cmds), C.byref(g)))
+        return Graph(self, g, cmds)
+
+    def get_tuning(self):
+        t = abi.Tuning()
+        self._check("sg_get_tuning", self.lib.sg_get_tuning(self.handle, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in abi.Tuning._fields_}
+
+    def set_tuning(self, **kw):
+        t = abi.Tuning()
+        self._check("sg_get_tuning", self.lib.sg_get_tuning(self.handle, C.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._check("sg_set_tuning", self.lib.sg_set_tuning(self.handle, C.byref(t)))
+
+    def autotune(self, cmds, reps=3):
+        t = abi.Tuning()
+        ms = C.c_float()
+        self._check("sg_autotune", self.lib.sg_autotune(self.handle, cmds.array(), len(cmds), reps,
+                                                        C.byref(t), C.byref(ms)))
+        return {k: getattr(t, k) for k, _ in abi.Tuning._fields_}, ms.value
+
     def clear_color(self, tex, rgba):
         arr = (C.c_float * 4)(*rgba)
         self._check("sg_clear_color", self.lib.sg_clear_color(self.handle, tex, arr))
@@ -164,6 +199,88 @@ class Device:
 
     def resolve(self, src, dst):
         self._check("sg_resolve", self.lib.sg_resolve(self.handle, src, dst))
+
+
+class Graph:
+    """A recorded command list (sg_graph_create); launch() replays it."""
+
+    def __init__(self, dev, handle, cmds):
+        self.dev, self.handle, self._cmds = dev, handle, cmds
+
+    def launch(self):
+        self.dev._check("sg_graph_launch", self.dev.lib.sg_graph_launch(self.dev.handle, self.handle))
+
+    def info(self):
+        p, k = C.c_uint32(), C.c_uint32()
+        self.dev._check("sg_graph_info",
+                        self.dev.lib.sg_graph_info(self.dev.handle, self.handle, C.byref(p), C.byref(k)))
+        return {"passes": p.value, "kernels": k.value}
+
+    def close(self):
+        if self.handle is not None and self.dev.handle is not None:
+            self.dev.lib.sg_graph_destroy(self.dev.handle, self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CommandList:
+    """An sg_command array; keeps the draw descriptors it points at alive."""
+
+    def __init__(self):
+        self._cmds = []
+        self._descs = []
+        self._arr = None
+
+    def __len__(self):
+        return len(self._cmds)
+
+    def draw(self, desc):
+        c = abi.Command()
+        c.type = abi.CMD_DRAW
+        self._descs.append(desc)
+        c.draw = C.pointer(desc)
+        self._cmds.append(c)
+        self._arr = None
+        return self
+
+    def clear_color(self, tex, rgba):
+        c = abi.Command()
+        c.type, c.texture = abi.CMD_CLEAR_COLOR, tex
+        for i, v in enumerate(rgba):
+            c.color[i] = v
+        self._cmds.append(c)
+        self._arr = None
+        return self
+
+    def clear_depth_stencil(self, tex, flags, depth, stencil):
+        c = abi.Command()
+        c.type, c.texture, c.flags, c.depth, c.stencil = abi.CMD_CLEAR_DEPTH_STENCIL, tex, flags, depth, stencil
+        self._cmds.append(c)
+        self._arr = None
+        return self
+
+    def resolve(self, src, dst):
+        c = abi.Command()
+        c.type, c.texture, c.texture2 = abi.CMD_RESOLVE, src, dst
+        self._cmds.append(c)
+        self._arr = None
+        return self
+
+    def extend(self, other):
+        self._cmds += other._cmds
+        self._descs += other._descs
+        self._arr = None
+        return self
+
+    def array(self):
+        if self._arr is None:
+            self._arr = (abi.Command * max(1, len(self._cmds)))(*self._cmds)
+        return self._arr
 
 
 def default_depth_stencil(depth_func=abi.CMP_LESS, depth_enable=1, depth_write=1):

@@ -20,7 +20,7 @@ import math
 import numpy as np
 
 from . import abi
-from .device import default_depth_stencil, make_draw_desc
+from .device import CommandList, default_depth_stencil, make_draw_desc
 
 
 # --------------------------------------------------------------------------
@@ -168,6 +168,20 @@ class Bound:
         self.finish()
         return st
 
+    def commands(self):
+        """The frame (clears, draws, resolve) as one command list."""
+        s = self.scene
+        cl = CommandList()
+        if self.color:
+            cl.clear_color(self.color, s.clear_color)
+        if self.ds:
+            cl.clear_depth_stencil(self.ds, abi.CLEAR_DEPTH | abi.CLEAR_STENCIL, s.clear_depth, s.clear_stencil)
+        for desc in self.descs:
+            cl.draw(desc)
+        if self.resolved:
+            cl.resolve(self.color, self.resolved)
+        return cl
+
     def outputs(self):
         d = self.dev
         out = {}
@@ -180,9 +194,16 @@ class Bound:
         return out
 
 
-def render(dev, scene, stats=False):
+def render(dev, scene, stats=False, batched=False):
+    """Renders one frame: call by call, or (batched) as one command list."""
     b = Bound(dev, scene)
-    st = b.frame(stats)
+    if batched:
+        cl = b.commands()
+        st = dev.submit(cl, stats=stats)
+        if stats:
+            st = [x for x, c in zip(st, cl._cmds) if c.type == abi.CMD_DRAW]
+    else:
+        st = b.frame(stats)
     out = b.outputs()
     if stats:
         out["stats"] = st
