@@ -374,7 +374,10 @@ void sg_graph_destroy(sg_device* dev, sg_graph* graph);
  * 32x32 items or sixteen 16x16 items, the latter also for any tile with more
  * than `split_entries` bin entries), the minimum triangle slots per binning
  * warp, the initial bin-entry and fragment capacities, the pixel-shading
- * quads per warp, and CTAs per SM for the shading and merging kernels. */
+ * quads per warp, CTAs per SM for the shading and merging kernels, and the
+ * threads that cover one 4x4 block: 2 (each half of its samples, walking the
+ * block's triangles in order; 32x32 items) or 32 (a warp per triangle-block
+ * pair, the `cover_item` and `split_entries` choices apply). */
 typedef struct sg_tuning {
   uint32_t cover_item;       /* 16 or 32 */
   uint32_t split_entries;    /* 32x32 items become 16x16 above this many bin entries */
@@ -384,6 +387,7 @@ typedef struct sg_tuning {
   uint32_t shade_quads_per_warp; /* 8 (4 lanes per quad) */
   uint32_t shade_ctas_per_sm;
   uint32_t merge_ctas_per_sm;
+  uint32_t cover_threads_per_block; /* 2 or 32 */
 } sg_tuning;
 int32_t sg_get_tuning(sg_device* dev, sg_tuning* out);
 int32_t sg_set_tuning(sg_device* dev, const sg_tuning* tuning);

@@ -32,6 +32,8 @@ void launch_scan(uint32_t* data, size_t n, uint32_t* sums, PassCounters* ctr, cu
 void launch_tile_ranges(PassParams const& p, cudaStream_t s);
 void launch_cover(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
 cudaError_t init_cover();
+void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
+cudaError_t init_cover2();
 void launch_merge(PassParams const& p, uint32_t grid, cudaStream_t s);
 void launch_shade_0(PassParams const& p, uint32_t grid, cudaStream_t s);
 void launch_shade_1(PassParams const& p, uint32_t grid, cudaStream_t s);
@@ -208,6 +210,7 @@ sg_tuning default_tuning() {
   t.shade_quads_per_warp = 8;
   t.shade_ctas_per_sm = 8;
   t.merge_ctas_per_sm = 3;
+  t.cover_threads_per_block = 2;
   return t;
 }
 
@@ -443,7 +446,7 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   p.back_pass = ds.back.pass_op;
   Texture* tt = ct ? ct : dt;
   p.zcfg = zcfg_of(tt->samples, p.read_depth, p.write_depth, dt && dt->fmt == SG_FMT_D24S8, p.early_z && dt,
-                   p.depth_func);
+                   p.depth_func, p.has_centroid);
   return SG_OK;
 }
 
@@ -769,7 +772,10 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       launch_bin(P, true, s);
       stage_end(d, 1, ev);
       ev = stage_begin(d, profile);
-      launch_cover(P, pl.max_samples, pl.any_early_z, cover_grid, s);
+      if (tu.cover_threads_per_block == 2)
+        launch_cover2(P, pl.max_samples, pl.any_early_z, std::min<uint32_t>(pl.ntiles * 4, sms * 8), s);
+      else
+        launch_cover(P, pl.max_samples, pl.any_early_z, cover_grid, s);
       stage_end(d, 2, ev);
       ev = stage_begin(d, profile);
       for (uint32_t na = 0; na <= SG_MAX_VARYINGS; ++na) {
@@ -1105,7 +1111,7 @@ int32_t sg_device_create(int32_t cuda_device, void* cuda_stream, sg_device** out
   if (cudaMallocHost(&d->counters_host, sizeof(PassCounters)) != cudaSuccess) return SG_OUT_OF_MEMORY;
   std::memset(d->counters_host, 0, sizeof(PassCounters));
   if (cudaMallocHost(&d->sticky_host, sizeof(unsigned int)) != cudaSuccess) return SG_OUT_OF_MEMORY;
-  if (init_cover() != cudaSuccess) return SG_CUDA_ERROR;
+  if (init_cover() != cudaSuccess || init_cover2() != cudaSuccess) return SG_CUDA_ERROR;
   float tab[256];
   make_ewa_table(tab);
   for (auto up : {upload_ewa_table_raster_a, upload_ewa_table_raster_b, upload_ewa_table_raster_c})
@@ -1492,7 +1498,8 @@ int32_t sg_set_tuning(sg_device* d, const sg_tuning* t) {
   if ((t->cover_item != 16 && t->cover_item != 32) || t->bin_chunk < BIN_CHUNK_MIN ||
       (t->bin_chunk & (t->bin_chunk - 1)) || t->bin_capacity == 0 || t->frag_chunks == 0 ||
       t->shade_quads_per_warp != 8 || t->shade_ctas_per_sm == 0 || t->shade_ctas_per_sm > 32 ||
-      t->merge_ctas_per_sm == 0 || t->merge_ctas_per_sm > 8)
+      t->merge_ctas_per_sm == 0 || t->merge_ctas_per_sm > 8 ||
+      (t->cover_threads_per_block != 2 && t->cover_threads_per_block != 32))
     return SG_INVALID_PARAMETER;
   d->tuning = *t;
   d->scratch.entry_capacity = std::max(d->scratch.entry_capacity, t->bin_capacity);
@@ -1526,9 +1533,10 @@ int32_t sg_autotune(sg_device* d, const sg_command* cmds, uint32_t n, uint32_t r
   float best = 0.0f;
   int32_t r = time_of(best_t, best);
   for (int sweep = 0; sweep < 2 && r == SG_OK; ++sweep) {
-    for (int param = 0; param < 5 && r == SG_OK; ++param) {
+    for (int param = 0; param < 6 && r == SG_OK; ++param) {
       std::vector<uint32_t> vals;
       switch (param) {
+      case 5: vals = {2u, 32u}; break;
       case 0: vals = {16u, 32u}; break;
       case 1: vals = {160u, 320u, 640u, 1280u}; break;
       case 2: vals = {256u, 512u, 1024u, 2048u}; break;
@@ -1538,8 +1546,11 @@ int32_t sg_autotune(sg_device* d, const sg_command* cmds, uint32_t n, uint32_t r
       for (uint32_t v : vals) {
         sg_tuning t = best_t;
         uint32_t* field = param == 0 ? &t.cover_item : param == 1 ? &t.split_entries : param == 2 ? &t.bin_chunk
-                          : param == 3 ? &t.shade_ctas_per_sm : &t.merge_ctas_per_sm;
+                          : param == 3 ? &t.shade_ctas_per_sm : param == 4 ? &t.merge_ctas_per_sm
+                          : &t.cover_threads_per_block;
         if (*field == v) continue;
+        // item size and split threshold only shape the warp-per-pair coverage
+        if (param <= 1 && t.cover_threads_per_block != 32) continue;
         if (param == 1 && t.cover_item == 16) continue;  // every item is 16x16 already
         *field = v;
         float ms = 0.0f;

@@ -105,10 +105,11 @@ struct DrawParams {
 };
 
 // samples (bits 0-3), read_depth (4), write_depth (5), D24S8 storage (6),
-// early-Z (7), depth function (bits 8-11)
+// early-Z (7), depth function (bits 8-11), centroid varyings (12)
 __host__ __device__ inline uint32_t zcfg_of(uint32_t samples, uint32_t rd, uint32_t wr, bool d24, uint32_t early_z,
-                                            uint32_t func) {
-  return samples | (rd << 4) | (wr << 5) | (d24 ? 64u : 0u) | (early_z ? 128u : 0u) | (func << 8);
+                                            uint32_t func, uint32_t centroid) {
+  return samples | (rd << 4) | (wr << 5) | (d24 ? 64u : 0u) | (early_z ? 128u : 0u) | (func << 8) |
+         (centroid ? 4096u : 0u);
 }
 
 struct PassParams {
