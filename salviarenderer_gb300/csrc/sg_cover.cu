@@ -1,27 +1,34 @@
-// sg_cover.cu -- coverage and early-Z of a pass, two threads per 4x4 block.
+// sg_cover.cu -- coverage and early-Z of a pass.
 //
 // Work items are the 32x32 quadrants of every tile of every target, taken
-// from a dynamic cursor.  A CTA of 128 threads stages the tile's triangles
-// (its bin list, in API order) in batches and classifies each against the
-// quadrant's 16x16 regions and 4x4 blocks with the reference's level-1 and
-// level-2 trivial reject / accept tests (rasterizer.cpp:441-571), keeping
-// per-block sets of the triangles that reach the block and of those that
-// cover it fully.  Every block is then walked, in primitive order, by its
-// two threads: each tests half of the block's samples (the per-sample edge
-// test of draw_partial_tile, rasterizer.cpp:298-439) and runs early-Z on
-// them against the quadrant's depth staged in shared memory
-// (framebuffer.cpp:522-614).  The pair merges its masks and the block's
-// first thread appends the surviving quads to the block's fragment list.
-// Samples of one block never depend on each other, so the two threads need
-// no ordering beyond walking the same triangle sequence.
+// from a dynamic cursor; a CTA of 128 threads handles one item at a time,
+// two threads per 4x4 block.  For each batch of the tile's triangles (its
+// bin list, in API order) the CTA
+//   1. stages the batch and classifies every triangle against the
+//      quadrant's 16x16 regions and 4x4 blocks with the reference's level-1
+//      and level-2 trivial reject / accept tests (rasterizer.cpp:441-571),
+//      into per-block sets of the triangles reaching the block and of those
+//      covering it fully;
+//   2. drops, per block, the triangles a hierarchical depth test proves
+//      hidden (below);
+//   3. in rounds of up to CV_K triangles per block: computes the per-sample
+//      coverage of every remaining (triangle, block) pair -- the edge test of
+//      draw_partial_tile, rasterizer.cpp:298-439 -- spread evenly over all
+//      threads (coverage does not depend on order), then lets each block's
+//      two threads walk its pairs in primitive order, each running early-Z
+//      (framebuffer.cpp:522-614) on half of the block's samples against the
+//      quadrant's depth staged in shared memory, the first appending the
+//      surviving quads to the block's fragment list.
 //
-// Hierarchical depth cull: each thread keeps the largest and smallest depth
-// stored in its half of the block.  Before testing a triangle it bounds the
-// triangle's depth over the block from the depth plane, widened by a margin
-// that covers the rounding of the reference's per-sample depth expression;
-// when the bound proves every sample fails the depth test, the pair is
-// skipped.  The skipped samples would neither pass nor write, so results are
-// those of testing every sample.
+// Hierarchical depth test: each thread keeps the largest and smallest depth
+// stored in its half of the block.  A triangle's depth over the block is
+// bounded from its depth plane, widened by a margin that covers the rounding
+// of the reference's per-sample depth expression; when the bound proves
+// every sample of both halves fails the depth test, the pair is dropped.
+// Such samples neither pass nor write, so results are those of testing
+// every sample.  The depth range only narrows toward passing values as
+// samples are written, so a drop decided at the start of a batch stays
+// right for the whole batch.
 #include "sg_raster.cuh"
 
 namespace sg {
@@ -30,6 +37,7 @@ constexpr int CV_THREADS = 128;              // 64 blocks x 2 threads
 constexpr int CV_STAGE = 128;                // triangles per staged batch
 constexpr int CV_WORDS = CV_STAGE / 32;
 constexpr int CV_PX = 32;                    // quadrant edge
+constexpr int CV_K = 8;                      // pairs per block per round
 
 struct TriCv {  // what coverage and early-Z read of a triangle
   float4 e0, e1, e2, bbox;
@@ -38,20 +46,32 @@ struct TriCv {  // what coverage and early-Z read of a triangle
   uint32_t entry, zcfg, nattr;
 };
 
-// shared memory: staged triangles, then per word of the batch the sets
-// (one bit per staged triangle): reaching each of the 64 blocks, covering
-// each block fully, covering each 16x16 region fully; then the staged depth
-constexpr size_t cv_smem_base() {
-  return CV_STAGE * sizeof(TriCv) + (64 + 64 + 4) * CV_WORDS * sizeof(uint32_t);
-}
-size_t cv_smem(uint32_t samples, bool early_z) {
-  return cv_smem_base() + (early_z ? static_cast<size_t>(CV_PX) * CV_PX * samples * 4 : 0);
+// Shared memory of one CTA.
+struct CvShared {
+  TriCv stage[CV_STAGE];
+  // per word of the batch, one bit per staged triangle: reaching each block,
+  // covering each block fully, covering each 16x16 region fully
+  uint32_t mask4[CV_WORDS][64], mask4f[CV_WORDS][64], mask16[CV_WORDS][4];
+  // the round's pairs: per block up to CV_K staged-triangle indices (bit 7:
+  // the block is covered fully), their count, the blocks' offsets into the
+  // dense pair numbering, and each pair's coverage (uncut, cut to the target)
+  uint8_t slot[64][CV_K];
+  uint32_t cnt[64], off[65];
+  unsigned long long cov_uc[64][CV_K], cov_cv[64][CV_K];
+  float spx[4], spy[4];
+  uint32_t item;
+};
+// followed by the staged depth: CV_PX * CV_PX * samples words (early-Z only)
+inline size_t cv_smem(uint32_t samples, bool early_z) {
+  return ((sizeof(CvShared) + 15) & ~size_t(15)) + (early_z ? static_cast<size_t>(CV_PX) * CV_PX * samples * 4 : 0);
 }
 
 // This thread's half of a block: samples [s0, s0 + ns) of rows [r0, r0 + nr).
 struct Half {
   uint32_t s0, ns, r0, nr;
   uint32_t inside;  // bit iy * 4 + ix: pixel inside the target
+  uint32_t samples;
+  float ax[2], ay[2];  // offsets of samples s0, s0 + 1 from the pixel centre (aa_z_offset)
 };
 
 // Depth range stored in the thread's half (pixels inside the target only).
@@ -60,7 +80,8 @@ struct ZRange {
   uint32_t qmax, qmin;  // D24 depth bits
 };
 
-__device__ inline void z_range(uint32_t const* zblk, int zrow, uint32_t S, Half const& hf, bool d24, ZRange& r) {
+__device__ inline void z_range(uint32_t const* zblk, int zrow, Half const& hf, bool d24, ZRange& r) {
+  uint32_t const S = hf.samples;
   r.zmax = -INFINITY;
   r.zmin = INFINITY;
   r.qmax = 0;
@@ -117,96 +138,103 @@ __device__ inline bool z_culled(TriCv const& t, int bx_abs, int by_abs, uint32_t
   }
 }
 
-// One (triangle, block) pair, half of the block's samples.  `full`: the
-// block is covered fully (accepted at level 1 or 2).
-__device__ inline void cv_pair(PassParams const& P, TargetParams const& T, TriCv const& t, bool full, int bx_abs,
-                               int by_abs, uint32_t* zblk, int zrow, int h, Half const& hf, ZRange& zr,
-                               OwnerList& L) {
-  uint32_t const S = T.samples;
-  uint32_t const zc = t.zcfg;
-  bool const early = (zc & 128u) != 0;
-  uint32_t const func = (zc >> 8) & 15u;
-  bool const rd = (zc >> 4) & 1u, wr = (zc >> 5) & 1u, d24 = (zc >> 6) & 1u;
-  // masks over the block, 4 bits (samples) per pixel, pixel (ix, iy) at nibble iy * 4 + ix
-  uint64_t uc = 0, cv = 0, tz = 0;
-  // (a culled half contributes no coverage bits: exact only where the quads'
-  // coverage is not read later, i.e. without centroid interpolation)
-  bool const culled = early && !(zc & 4096u) && (rd || func == SG_CMP_NEVER) &&
-                      z_culled(t, bx_abs, by_abs, func, d24, zr);
-  if (!culled) {
+// Whether the pair's half is dropped by the hierarchical depth test.
+__device__ inline bool pair_hidden(TriCv const& t, int bx_abs, int by_abs, bool d24, ZRange const& zr) {
+  uint32_t const zc = t.zcfg, func = (zc >> 8) & 15u;
+  return (zc & 128u) && (((zc >> 4) & 1u) || func == SG_CMP_NEVER) && z_culled(t, bx_abs, by_abs, func, d24, zr);
+}
+
+// Per-sample coverage of a whole 4x4 block (draw_partial_tile's edge test,
+// rasterizer.cpp:298-439): 4 bits (samples) per pixel, pixel (ix, iy) at
+// nibble iy * 4 + ix; `uc` uncut, `cv` cut to the pixels inside the target.
+__device__ inline void block_coverage(TriCv const& t, bool full, int bx_abs, int by_abs, uint32_t S, float const* spx,
+                                      float const* spy, uint32_t inside, uint64_t& uc, uint64_t& cv) {
+  uc = 0;
+  if (full) {
+    uint64_t fm = (1ull << S) - 1ull;
+#pragma unroll
+    for (int p = 0; p < 16; ++p) uc |= fm << (4 * p);
+  } else {
     float4 const e[3] = {t.e0, t.e1, t.e2};
     float const lf = static_cast<float>(bx_abs), tf = static_cast<float>(by_abs);
     float ev[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) ev[k] = e[k].z - (lf * e[k].x + tf * e[k].y);
-    for (uint32_t iy = hf.r0; iy < hf.r0 + hf.nr; ++iy) {
-      for (uint32_t s = hf.s0; s < hf.s0 + hf.ns; ++s) {
-        float const my = T.sp_y[s] + static_cast<float>(iy);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      if (s >= static_cast<int>(S)) break;
+      float const sx = spx[s], sy = spy[s];
+      for (int iy = 0; iy < 4; ++iy) {
+        float const my = sy + static_cast<float>(iy);
 #pragma unroll
         for (int ix = 0; ix < 4; ++ix) {
-          bool in = full;
-          if (!in) {
-            float const mx = T.sp_x[s] + static_cast<float>(ix);
-            bool rej = false;
+          float const mx = sx + static_cast<float>(ix);
+          bool rej = false;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) rej = rej || ((mx * e[k].x + my * e[k].y) < ev[k]);
-            in = !rej;
-          }
-          if (in) {
-            uint64_t bit = 1ull << ((iy * 4 + ix) * 4 + s);
-            uc |= bit;
-            // EXTENSION: pixels outside the target are not covered
-            if ((hf.inside >> (iy * 4 + ix)) & 1u) cv |= bit;
-          }
+          for (int k = 0; k < 3; ++k) rej = rej || ((mx * e[k].x + my * e[k].y) < ev[k]);
+          uc |= static_cast<uint64_t>(!rej) << ((iy * 4 + ix) * 4 + s);
         }
       }
-    }
-    tz = cv;
-    if (early && cv) {  // early-Z: test and write the staged depth now
-      tz = 0;
-      bool wrote = false;
-      for (uint32_t iy = hf.r0; iy < hf.r0 + hf.nr; ++iy) {
-        uint32_t const qy = by_abs + (iy & 2u);
-        float const dy = 0.5f + static_cast<float>(qy) - t.p0y;
-#pragma unroll
-        for (int ixq = 0; ixq < 2; ++ixq) {
-          uint32_t const qx = bx_abs + 2 * ixq;
-          float const dx = 0.5f + static_cast<float>(qx) - t.p0x;
-          // step_2d_unproj_pos_quad's z (shader.cpp:257-287)
-          float const z00 = t.p0z + (t.dzx * dx + t.dzy * dy);
-#pragma unroll
-          for (int i = 0; i < 2; ++i) {
-            uint32_t const ix = 2 * ixq + i;
-            uint32_t const pbits = static_cast<uint32_t>(cv >> ((iy * 4 + ix) * 4)) & 0xFu;
-            if (!pbits) continue;
-            float const z = (iy & 1u) ? (i ? (z00 + t.dzx) + t.dzy : z00 + t.dzy) : (i ? z00 + t.dzx : z00);
-            uint32_t* zp = zblk + iy * zrow + ix * S;
-            for (uint32_t s = hf.s0; s < hf.s0 + hf.ns; ++s) {
-              if (!(pbits & (1u << s))) continue;
-              float const nd = S == 1 ? z : ((T.sp_x[s] - 0.5f) * t.dzx + (T.sp_y[s] - 0.5f) * t.dzy) + z;
-              uint32_t const w = zp[s];
-              bool const pass = d24 ? cmpu(func, d24_quantize(nd), rd ? (w & 0xFFFFFFu) : 0u)
-                                    : cmpf(func, nd, rd ? __uint_as_float(w) : 0.0f);
-              if (pass) {
-                if (wr) {
-                  zp[s] = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
-                  wrote = true;
-                }
-                tz |= 1ull << ((iy * 4 + ix) * 4 + s);
-              }
-            }
-          }
-        }
-      }
-      if (wrote) z_range(zblk, zrow, S, hf, d24, zr);
     }
   }
-  // merge the halves (the pair walks the same triangles, so both lanes are here)
-  uint32_t const lanes = 3u << (threadIdx.x & 30u);
-  uc |= __shfl_xor_sync(lanes, uc, 1);
-  cv |= __shfl_xor_sync(lanes, cv, 1);
-  tz |= __shfl_xor_sync(lanes, tz, 1);
-  if (h != 0 || tz == 0) return;
+  // EXTENSION: pixels outside the target are not covered
+  uint64_t im = 0;
+#pragma unroll
+  for (int p = 0; p < 16; ++p)
+    if ((inside >> p) & 1u) im |= 0xFull << (4 * p);
+  cv = uc & im;
+}
+
+// Early-Z of one pair on this thread's half of the block's samples
+// (framebuffer.cpp:522-614) against the staged depth; returns the passing
+// samples and writes depth on pass.
+__device__ inline uint64_t early_z_half(TriCv const& t, uint64_t cv, int bx_abs, int by_abs, uint32_t* zblk, int zrow,
+                                        Half const& hf, bool& wrote) {
+  uint32_t const S = hf.samples, zc = t.zcfg, func = (zc >> 8) & 15u;
+  bool const rd = (zc >> 4) & 1u, wr = (zc >> 5) & 1u, d24 = (zc >> 6) & 1u;
+  uint64_t tz = 0;
+  for (uint32_t iy = hf.r0; iy < hf.r0 + hf.nr; ++iy) {
+    uint32_t const qy = by_abs + (iy & 2u);
+    float const dy = 0.5f + static_cast<float>(qy) - t.p0y;
+#pragma unroll
+    for (int ixq = 0; ixq < 2; ++ixq) {
+      uint32_t const qx = bx_abs + 2 * ixq;
+      float const dx = 0.5f + static_cast<float>(qx) - t.p0x;
+      // step_2d_unproj_pos_quad's z (shader.cpp:257-287)
+      float const z00 = t.p0z + (t.dzx * dx + t.dzy * dy);
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        uint32_t const ix = 2 * ixq + i;
+        uint32_t const pbits = static_cast<uint32_t>(cv >> ((iy * 4 + ix) * 4)) & 0xFu;
+        if (!pbits) continue;
+        float const z = (iy & 1u) ? (i ? (z00 + t.dzx) + t.dzy : z00 + t.dzy) : (i ? z00 + t.dzx : z00);
+        uint32_t* zp = zblk + iy * zrow + ix * S;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          if (j >= static_cast<int>(hf.ns)) break;
+          uint32_t const s = hf.s0 + j;
+          if (!(pbits & (1u << s))) continue;
+          float const nd = S == 1 ? z : (hf.ax[j] * t.dzx + hf.ay[j] * t.dzy) + z;
+          uint32_t const w = zp[s];
+          bool const pass = d24 ? cmpu(func, d24_quantize(nd), rd ? (w & 0xFFFFFFu) : 0u)
+                                : cmpf(func, nd, rd ? __uint_as_float(w) : 0.0f);
+          if (pass) {
+            if (wr) {
+              zp[s] = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
+              wrote = true;
+            }
+            tz |= 1ull << ((iy * 4 + ix) * 4 + s);
+          }
+        }
+      }
+    }
+  }
+  return tz;
+}
+
+// Appends the block's surviving quads (the first thread of the pair).
+__device__ inline void emit_quads(PassParams const& P, OwnerList& L, TriCv const& t, bool full, int bx_abs,
+                                  int by_abs, uint32_t S, uint64_t uc, uint64_t cv, uint64_t tz) {
   uint32_t const fm = (1u << S) - 1u;
   uint32_t const qfull = fm | (fm << 4) | (fm << 8) | (fm << 12);
   uint32_t const rec = t.entry >> 1, na = t.nattr << 25;
@@ -230,23 +258,97 @@ __device__ inline void cv_pair(PassParams const& P, TargetParams const& T, TriCv
   }
 }
 
-__global__ void __launch_bounds__(CV_THREADS) k_cover2(PassParams P) {
-  extern __shared__ __align__(16) uint8_t smem[];
-  TriCv* stage = reinterpret_cast<TriCv*>(smem);
-  uint32_t* mask4 = reinterpret_cast<uint32_t*>(smem + CV_STAGE * sizeof(TriCv));  // [word][64 blocks]
-  uint32_t* mask4f = mask4 + 64 * CV_WORDS;                                        // [word][64 blocks]
-  uint32_t* mask16 = mask4f + 64 * CV_WORDS;                                       // [word][4 regions]
-  uint32_t* ztile = mask16 + 4 * CV_WORDS;
-  __shared__ uint32_t s_item;
+// Stages a batch of a tile's bin entries and classifies each triangle
+// against the quadrant's regions and blocks (rasterizer.cpp:441-571).
+__device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint32_t bstart, uint32_t nb, int tile_x0,
+                                int tile_y0, int bx0, int by0, CvShared& sh) {
+  float const tx0f = static_cast<float>(tile_x0), ty0f = static_cast<float>(tile_y0);
+  float const trr = T.target_w, trb = T.target_h;
+  for (uint32_t i = threadIdx.x; i < nb; i += CV_THREADS) {
+    uint32_t const e = P.bin_entries[bstart + i];
+    float4 const* R = P.recs + (e >> 1);
+    TriCv ts;
+    ts.e0 = R[0];
+    ts.e1 = R[1];
+    ts.e2 = R[2];
+    ts.bbox = R[3];
+    float4 const r4 = R[4];
+    ts.p0x = ts.e0.w;
+    ts.p0y = ts.e1.w;
+    ts.p0z = ts.e2.w;
+    ts.dzx = r4.x;
+    ts.dzy = r4.y;
+    ts.entry = e;
+    uint32_t const flags = __float_as_uint(r4.w);
+    ts.zcfg = flags & 0x1FFFu;
+    ts.nattr = (flags >> 28) & 7u;
+    sh.stage[i] = ts;
+    uint32_t const bit = 1u << (i & 31), word = i >> 5;
+    if (e & 1u) {  // accepted for the whole tile by the binner
+      for (int r = 0; r < 4; ++r) atomicOr(&sh.mask16[word][r], bit);
+      continue;
+    }
+    float const x_min = ts.bbox.x - tx0f, x_max = ts.bbox.y - tx0f, y_min = ts.bbox.z - ty0f,
+                y_max = ts.bbox.w - ty0f;
+    float4 const ed[3] = {ts.e0, ts.e1, ts.e2};
+    LevelParams l1, l2;
+    level_params(ed, l1, l2);
+    // blocks (tile numbering) the bounding box can reach; the exact
+    // reference tests below decide
+    int const jx_lo = max(bx0, static_cast<int>(floorf(x_min * 0.25f)) - 1);
+    int const jx_hi = min(bx0 + 7, static_cast<int>(floorf(x_max * 0.25f)) + 1);
+    int const jy_lo = max(by0, static_cast<int>(floorf(y_min * 0.25f)) - 1);
+    int const jy_hi = min(by0 + 7, static_cast<int>(floorf(y_max * 0.25f)) + 1);
+    for (int iy = by0 >> 2; iy < (by0 >> 2) + 2; ++iy) {
+      int const m16y = iy * 16;
+      if (y_min >= static_cast<float>(m16y + 16) || y_max < static_cast<float>(m16y)) continue;
+      for (int ix = bx0 >> 2; ix < (bx0 >> 2) + 2; ++ix) {
+        int const m16x = ix * 16;
+        if (x_min >= static_cast<float>(m16x + 16) || x_max < static_cast<float>(m16x)) continue;
+        int const c = child_class(ed, l1, tx0f, ty0f, ix, iy);
+        if (c == 0) continue;
+        // a region whose origin is right of / below the target is skipped
+        if (static_cast<float>(tile_x0 + m16x) >= trr || static_cast<float>(tile_y0 + m16y) >= trb) continue;
+        int const r = (iy - (by0 >> 2)) * 2 + (ix - (bx0 >> 2));
+        if (c == 2) {
+          atomicOr(&sh.mask16[word][r], bit);
+          continue;
+        }
+        // partial: level 2 over the 4x4 children inside the bounding box
+        float const r16xf = static_cast<float>(tile_x0 + m16x), r16yf = static_cast<float>(tile_y0 + m16y);
+        for (int jy = max(0, jy_lo - iy * 4); jy <= min(3, jy_hi - iy * 4); ++jy) {
+          int const m4y = m16y + jy * 4;
+          if (y_min >= static_cast<float>(m4y + 4) || y_max < static_cast<float>(m4y)) continue;
+          if (static_cast<float>(tile_y0 + m4y) >= trb) continue;
+          for (int jx = max(0, jx_lo - ix * 4); jx <= min(3, jx_hi - ix * 4); ++jx) {
+            int const m4x = m16x + jx * 4;
+            if (x_min >= static_cast<float>(m4x + 4) || x_max < static_cast<float>(m4x)) continue;
+            if (static_cast<float>(tile_x0 + m4x) >= trr) continue;
+            int const c2 = child_class(ed, l2, r16xf, r16yf, jx, jy);
+            if (c2 == 0) continue;
+            int const bi = (iy * 4 + jy - by0) * 8 + (ix * 4 + jx - bx0);
+            atomicOr(&sh.mask4[word][bi], bit);
+            if (c2 == 2) atomicOr(&sh.mask4f[word][bi], bit);
+          }
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  CvShared& sh = *reinterpret_cast<CvShared*>(smem_raw);
+  uint32_t* const ztile = reinterpret_cast<uint32_t*>(smem_raw + ((sizeof(CvShared) + 15) & ~size_t(15)));
   if (P.counters->overflow & (OVF_BIN | OVF_REC)) return;
   int const tid = threadIdx.x, h = tid & 1, ib = tid >> 1;  // item block 0..63: (ib & 7, ib >> 3)
   int const ibx = ib & 7, iby = ib >> 3;
   uint32_t const nitems = P.ntiles * 4;
   OwnerList L{NO_CHUNK, NO_CHUNK, 0};
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(&P.counters->tile_cursor, 1u);
+    if (tid == 0) sh.item = atomicAdd(&P.counters->tile_cursor, 1u);
     __syncthreads();
-    uint32_t const item = s_item;
+    uint32_t const item = sh.item;
     __syncthreads();
     if (item >= nitems) break;
     uint32_t const tile = item >> 2, sub = item & 3;
@@ -256,10 +358,12 @@ __global__ void __launch_bounds__(CV_THREADS) k_cover2(PassParams P) {
     int const tile_x0 = static_cast<int>(ltile % T.tiles_x) * TILE, tile_y0 = static_cast<int>(ltile / T.tiles_x) * TILE;
     int const bx0 = (sub & 1) * 8, by0 = (sub >> 1) * 8;  // first block of the quadrant, tile numbering
     int const x0 = tile_x0 + bx0 * 4, y0 = tile_y0 + by0 * 4;
-    float const tx0f = static_cast<float>(tile_x0), ty0f = static_cast<float>(tile_y0);
-    float const trr = T.target_w, trb = T.target_h;
-    uint32_t const S = T.samples;
-    int const bx = bx0 + ibx, by = by0 + iby;        // this thread's block, tile numbering
+    uint32_t const S = T.samples, W = T.width, H = T.height;
+    if (tid < 4) {
+      sh.spx[tid] = T.sp_x[tid];
+      sh.spy[tid] = T.sp_y[tid];
+    }
+    int const bx = bx0 + ibx, by = by0 + iby;  // this thread's block, tile numbering
     int const bx_abs = tile_x0 + bx * 4, by_abs = tile_y0 + by * 4;
     int const own16 = (iby >> 2) * 2 + (ibx >> 2);  // its 16x16 region within the quadrant
     L.first = L.cur = NO_CHUNK;
@@ -269,15 +373,21 @@ __global__ void __launch_bounds__(CV_THREADS) k_cover2(PassParams P) {
     hf.ns = S > 1 ? (S >> 1) : 1;
     hf.r0 = S > 1 ? 0 : 2 * h;
     hf.nr = S > 1 ? 4 : 2;
+    hf.samples = S;
+    for (uint32_t j = 0; j < 2; ++j) {
+      uint32_t const s = min(hf.s0 + j, S - 1);
+      hf.ax[j] = T.sp_x[s] - 0.5f;
+      hf.ay[j] = T.sp_y[s] - 0.5f;
+    }
     hf.inside = 0;
     for (int iy = 0; iy < 4; ++iy)
       for (int ix = 0; ix < 4; ++ix)
-        if (static_cast<uint32_t>(bx_abs + ix) < T.width && static_cast<uint32_t>(by_abs + iy) < T.height)
+        if (static_cast<uint32_t>(bx_abs + ix) < W && static_cast<uint32_t>(by_abs + iy) < H)
           hf.inside |= 1u << (iy * 4 + ix);
     bool const stage_z = T.any_early_z && begin < end;
     bool const d24 = T.ds_fmt == SG_FMT_D24S8;
-    uint32_t const qw = min(static_cast<uint32_t>(CV_PX), T.width - min(T.width, static_cast<uint32_t>(x0)));
-    uint32_t const qh = min(static_cast<uint32_t>(CV_PX), T.height - min(T.height, static_cast<uint32_t>(y0)));
+    uint32_t const qw = min(static_cast<uint32_t>(CV_PX), W - min(W, static_cast<uint32_t>(x0)));
+    uint32_t const qh = min(static_cast<uint32_t>(CV_PX), H - min(H, static_cast<uint32_t>(y0)));
     uint32_t const zrow = CV_PX * S;
     if (stage_z) {
       for (uint32_t i = tid; i < qh * zrow; i += CV_THREADS) {
@@ -291,91 +401,95 @@ __global__ void __launch_bounds__(CV_THREADS) k_cover2(PassParams P) {
     ZRange zr{-INFINITY, INFINITY, 0u, 0xFFFFFFu};
     if (stage_z) {
       __syncthreads();
-      z_range(zblk, static_cast<int>(zrow), S, hf, d24, zr);
+      z_range(zblk, static_cast<int>(zrow), hf, d24, zr);
     }
     for (uint32_t bstart = begin; bstart < end; bstart += CV_STAGE) {
       uint32_t const nb = min(static_cast<uint32_t>(CV_STAGE), end - bstart);
       __syncthreads();
-      for (int i = tid; i < (64 + 64 + 4) * CV_WORDS; i += CV_THREADS) mask4[i] = 0;
+      uint32_t* const masks = &sh.mask4[0][0];
+      for (int i = tid; i < (64 + 64 + 4) * CV_WORDS; i += CV_THREADS) masks[i] = 0;
       __syncthreads();
-      // stage the batch and classify each triangle against the quadrant's regions and blocks
-      for (uint32_t i = tid; i < nb; i += CV_THREADS) {
-        uint32_t const e = P.bin_entries[bstart + i];
-        float4 const* R = P.recs + (e >> 1);
-        DrawParams const& D = P.draws[rec_draw(R)];
-        int const nreg = 1 + static_cast<int>(D.nattr);
-        TriCv ts;
-        ts.e0 = R[0];
-        ts.e1 = R[1];
-        ts.e2 = R[2];
-        ts.bbox = R[3];
-        float4 const p0 = R[5];
-        ts.p0x = p0.x;
-        ts.p0y = p0.y;
-        ts.p0z = p0.z;
-        ts.dzx = R[5 + nreg].z;
-        ts.dzy = R[5 + 2 * nreg].z;
-        ts.entry = e;
-        ts.zcfg = D.zcfg;
-        ts.nattr = D.nattr;
-        stage[i] = ts;
-        uint32_t const bit = 1u << (i & 31), word = i >> 5;
-        if (e & 1u) {  // accepted for the whole tile by the binner
-          for (int r = 0; r < 4; ++r) atomicOr(&mask16[word * 4 + r], bit);
-          continue;
-        }
-        float const x_min = ts.bbox.x - tx0f, x_max = ts.bbox.y - tx0f, y_min = ts.bbox.z - ty0f,
-                    y_max = ts.bbox.w - ty0f;
-        float4 const ed[3] = {ts.e0, ts.e1, ts.e2};
-        LevelParams l1, l2;
-        level_params(ed, l1, l2);
-        for (int iy = by0 >> 2; iy < (by0 >> 2) + 2; ++iy) {
-          int const m16y = iy * 16;
-          if (y_min >= static_cast<float>(m16y + 16) || y_max < static_cast<float>(m16y)) continue;
-          for (int ix = bx0 >> 2; ix < (bx0 >> 2) + 2; ++ix) {
-            int const m16x = ix * 16;
-            if (x_min >= static_cast<float>(m16x + 16) || x_max < static_cast<float>(m16x)) continue;
-            int const c = child_class(ed, l1, tx0f, ty0f, ix, iy);
-            if (c == 0) continue;
-            // a region whose origin is right of / below the target is skipped
-            if (static_cast<float>(tile_x0 + m16x) >= trr || static_cast<float>(tile_y0 + m16y) >= trb) continue;
-            int const r = (iy - (by0 >> 2)) * 2 + (ix - (bx0 >> 2));
-            if (c == 2) {
-              atomicOr(&mask16[word * 4 + r], bit);
-              continue;
-            }
-            // partial: level 2 over the 4x4 children inside the bounding box
-            float const r16xf = static_cast<float>(tile_x0 + m16x), r16yf = static_cast<float>(tile_y0 + m16y);
-            for (int jy = 0; jy < 4; ++jy) {
-              int const m4y = m16y + jy * 4;
-              if (y_min >= static_cast<float>(m4y + 4) || y_max < static_cast<float>(m4y)) continue;
-              if (static_cast<float>(tile_y0 + m4y) >= trb) continue;
-              for (int jx = 0; jx < 4; ++jx) {
-                int const m4x = m16x + jx * 4;
-                if (x_min >= static_cast<float>(m4x + 4) || x_max < static_cast<float>(m4x)) continue;
-                if (static_cast<float>(tile_x0 + m4x) >= trr) continue;
-                int const c2 = child_class(ed, l2, r16xf, r16yf, jx, jy);
-                if (c2 == 0) continue;
-                int const bi = (iy * 4 + jy - by0) * 8 + (ix * 4 + jx - bx0);
-                atomicOr(&mask4[word * 64 + bi], bit);
-                if (c2 == 2) atomicOr(&mask4f[word * 64 + bi], bit);
-              }
-            }
+      cv_stage(P, T, bstart, nb, tile_x0, tile_y0, bx0, by0, sh);
+      __syncthreads();
+      // the block's triangles, without those hidden in both halves
+      uint32_t live[CV_WORDS];
+#pragma unroll
+      for (int w = 0; w < CV_WORDS; ++w) {
+        uint32_t m = sh.mask4[w][ib] | sh.mask16[w][own16];
+        if (stage_z) {
+          uint32_t scan = m;
+          while (scan) {
+            int const b = __ffs(scan) - 1;
+            scan &= scan - 1;
+            if (pair_hidden(sh.stage[(w << 5) + b], bx_abs, by_abs, d24, zr)) m &= ~(1u << b);
           }
         }
+        live[w] = m | __shfl_xor_sync(0xFFFFFFFFu, m, 1);
       }
-      __syncthreads();
-      // every block, by its two threads, walks its triangles in primitive order
-      for (int w = 0; w < CV_WORDS; ++w) {
-        uint32_t const m16 = mask16[w * 4 + own16];
-        uint32_t mine = mask4[w * 64 + ib] | m16;
-        uint32_t const fulls = mask4f[w * 64 + ib] | m16;
-        while (mine) {
-          int const b = __ffs(mine) - 1;
-          mine &= mine - 1;
-          cv_pair(P, T, stage[(w << 5) + b], (fulls >> b) & 1u, bx_abs, by_abs, zblk, static_cast<int>(zrow), h,
-                  hf, zr, L);
+      for (;;) {
+        // this round's pairs: the block's next CV_K triangles in primitive order
+        uint32_t n = 0;
+#pragma unroll
+        for (int w = 0; w < CV_WORDS; ++w) {
+          uint32_t const fulls = sh.mask4f[w][ib] | sh.mask16[w][own16];
+          while (live[w] && n < static_cast<uint32_t>(CV_K)) {
+            int const b = __ffs(live[w]) - 1;
+            live[w] &= live[w] - 1;
+            if (h == 0) sh.slot[ib][n] = static_cast<uint8_t>((w << 5) + b) | static_cast<uint8_t>(((fulls >> b) & 1u) << 7);
+            ++n;
+          }
         }
+        bool more = false;
+#pragma unroll
+        for (int w = 0; w < CV_WORDS; ++w) more = more || live[w] != 0;
+        if (h == 0) sh.cnt[ib] = n;
+        __syncthreads();
+        if (tid < 32) {  // offsets of the blocks in the dense pair numbering
+          uint32_t const c0 = sh.cnt[2 * tid], c1 = sh.cnt[2 * tid + 1];
+          uint32_t incl = c0 + c1;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            uint32_t const y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (tid >= o) incl += y;
+          }
+          uint32_t const excl = incl - (c0 + c1);
+          sh.off[2 * tid] = excl;
+          sh.off[2 * tid + 1] = excl + c0;
+          if (tid == 31) sh.off[64] = incl;
+        }
+        __syncthreads();
+        // coverage of every pair of the round, spread over all threads
+        uint32_t const total = sh.off[64];
+        for (uint32_t d = tid; d < total; d += CV_THREADS) {
+          uint32_t const b = upper_index(sh.off, 64, d), k = d - sh.off[b];
+          uint32_t const e8 = sh.slot[b][k];
+          int const pbx = tile_x0 + (bx0 + static_cast<int>(b & 7)) * 4;
+          int const pby = tile_y0 + (by0 + static_cast<int>(b >> 3)) * 4;
+          uint32_t inside = 0;
+          for (int iy = 0; iy < 4; ++iy)
+            for (int ix = 0; ix < 4; ++ix)
+              if (static_cast<uint32_t>(pbx + ix) < W && static_cast<uint32_t>(pby + iy) < H) inside |= 1u << (iy * 4 + ix);
+          uint64_t uc, cv;
+          block_coverage(sh.stage[e8 & 127u], (e8 >> 7) != 0, pbx, pby, S, sh.spx, sh.spy, inside, uc, cv);
+          sh.cov_uc[b][k] = uc;
+          sh.cov_cv[b][k] = cv;
+        }
+        __syncthreads();
+        // each block's pairs in primitive order: early-Z on this half, then the quads
+        for (uint32_t k = 0; k < n; ++k) {
+          uint32_t const e8 = sh.slot[ib][k];
+          TriCv const& t = sh.stage[e8 & 127u];
+          uint64_t const uc = sh.cov_uc[ib][k], cv = sh.cov_cv[ib][k];
+          uint64_t tz = cv;
+          if ((t.zcfg & 128u) && cv) {
+            bool wrote = false;
+            tz = early_z_half(t, cv, bx_abs, by_abs, zblk, static_cast<int>(zrow), hf, wrote);
+            if (wrote) z_range(zblk, static_cast<int>(zrow), hf, d24, zr);
+          }
+          tz |= __shfl_xor_sync(3u << (tid & 30), tz, 1);
+          if (h == 0 && tz) emit_quads(P, L, t, (e8 >> 7) != 0, bx_abs, by_abs, S, uc, cv, tz);
+        }
+        if (!__syncthreads_or(more)) break;
       }
     }
     if (stage_z) {

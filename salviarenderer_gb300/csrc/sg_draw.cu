@@ -140,7 +140,8 @@ __device__ inline void vp_project(DrawParams const& D, vtx<NA>& v) {
 // rasterizer::compute_triangle_info (rasterizer.cpp:864-945) + compute_derivative_n
 // (shader.cpp:414-449); writes the record, returns false for zero area.
 template <int NA>
-__device__ bool setup_triangle(uint32_t draw, vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c, float4* rec) {
+__device__ bool setup_triangle(uint32_t draw, uint32_t zcfg, vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c,
+                               float4* rec) {
   vtx<NA> const* verts[3] = {&a, &b, &c};
   double dist[3];
 #pragma unroll
@@ -169,7 +170,6 @@ __device__ bool setup_triangle(uint32_t draw, vtx<NA> const& a, vtx<NA> const& b
     rec[i] = make_float4(s.y - e.y, e.x - s.x, e.x * s.y - e.y * s.x, 0.0f);
   }
   rec[3] = bb;
-  rec[4] = make_float4(area > 0.0f ? 1.0f : 0.0f, __uint_as_float(draw), 0.0f, 0.0f);
   float e01x = e01p.x, e01y = e01p.y, e02x = e02p.x, e02y = e02p.y;
   constexpr int R = 1 + NA;
 #pragma unroll
@@ -187,6 +187,13 @@ __device__ bool setup_triangle(uint32_t draw, vtx<NA> const& a, vtx<NA> const& b
     rec[5 + R + i] = make_float4(xd[0], xd[1], xd[2], xd[3]);
     rec[5 + 2 * R + i] = make_float4(yd[0], yd[1], yd[2], yd[3]);
   }
+  // what coverage and early-Z read, in the first five slots: the position
+  // of v0 beside the edge factors, its depth gradients and the draw's flags
+  rec[0].w = v0.r[0].x;
+  rec[1].w = v0.r[0].y;
+  rec[2].w = v0.r[0].z;
+  rec[4] = make_float4(rec[5 + R].z, rec[5 + 2 * R].z, __uint_as_float(draw),
+                       __uint_as_float(rec_flags(area > 0.0f, NA, zcfg)));
   return true;
 }
 
@@ -199,7 +206,7 @@ __device__ void emit_triangle(PassParams const& P, DrawParams const& D, uint32_t
   vp_project(D, c);
   constexpr uint32_t STRIDE = rec_stride_for(NA);
   alignas(16) float4 rec[STRIDE];
-  bool ok = setup_triangle(draw, a, b, c, rec);
+  bool ok = setup_triangle(draw, D.zcfg, a, b, c, rec);
   uint32_t idx = NO_REC;
   if (ok) {
     idx = atomicAdd(&P.counters->rec_units, STRIDE);

@@ -150,11 +150,18 @@ struct PassParams {
   uint32_t cover_item, split_entries;
 };
 
-// triangle record layout (float4 units): [0..2] edge factors, [3] bbox,
-// [4] (front, draw index bits, 0, 0), then v0, ddx, ddy registers (1 + nattr each).
+// triangle record layout (float4 units): [0..2] edge factors (x, y, z) with
+// v0's projected x, y, z in .w, [3] bbox, [4] (ddx.z, ddy.z of the position,
+// draw index bits, flags bits), then v0, ddx, ddy registers (1 + nattr each).
+// Slots 0-4 hold everything coverage and early-Z read.
 __host__ __device__ constexpr uint32_t rec_stride_for(int nattr) { return 5 + 3 * (1 + nattr); }
 
-__device__ inline uint32_t rec_draw(float4 const* R) { return __float_as_uint(R[4].y); }
+// flags: the draw's zcfg (bits 0-12), varying count (28-30), front face (31)
+__host__ __device__ inline uint32_t rec_flags(bool front, uint32_t nattr, uint32_t zcfg) {
+  return (zcfg & 0x1FFFu) | (nattr << 28) | (front ? 0x80000000u : 0u);
+}
+__device__ inline uint32_t rec_draw(float4 const* R) { return __float_as_uint(R[4].z); }
+__device__ inline uint32_t rec_flag_bits(float4 const* R) { return __float_as_uint(R[4].w); }
 
 // index of the last element of sorted `base[0..n)` that is <= v
 __device__ inline uint32_t upper_index(uint32_t const* base, uint32_t n, uint32_t v) {

@@ -28,7 +28,7 @@ struct TriView {
   int nreg;
   __device__ float4 edge(int i) const { return R[i]; }
   __device__ float4 bbox() const { return R[3]; }
-  __device__ bool front() const { return R[4].x != 0.0f; }
+  __device__ bool front() const { return (rec_flag_bits(R) >> 31) != 0u; }
   __device__ v4 v0(int i) const { return ld4(R + 5 + i); }
   __device__ v4 ddx(int i) const { return ld4(R + 5 + nreg + i); }
   __device__ v4 ddy(int i) const { return ld4(R + 5 + 2 * nreg + i); }
