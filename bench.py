@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the 256-frame batched-draw leg")
     ap.add_argument("--size", default="1920x1080",
                     help="render-target size; smaller sizes are for profiling captures only")
     return ap.parse_args()
@@ -239,6 +240,46 @@ def time_steps(stream, flush, steps, fn):
     return sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / 1000.0
 
 
+def measure_uneven(dev, stream, flush, args):
+    """The batched-draw workload: 256 frames of uneven size and triangle
+    count in one command list, plain (clear + one sg_draw per draw, frame by
+    frame) against batched (the list recorded as one CUDA graph)."""
+    from salviarenderer_gb300 import scenes
+    from salviarenderer_gb300.device import SalviaError
+    batch = scenes.UnevenBatch(seed=SEED)
+    b = scenes.BoundUneven(dev, batch)
+    cl = b.commands()
+    for attempt in range(4):  # the first runs size the scratch
+        try:
+            dev.submit(cl, stats=True)
+            dev.sync()
+            break
+        except SalviaError:
+            if attempt == 3:
+                raise
+    steps = max(1, min(args.steps, 3))
+    for _ in range(args.warmup):
+        b.render_plain()
+    dev.sync()
+    plain_s = time_steps(stream, flush, steps, b.render_plain)
+    graph = dev.graph_create(cl)
+    info = graph.info()
+    for _ in range(args.warmup):
+        graph.launch()
+    dev.sync()
+    graph_s = time_steps(stream, flush, steps, graph.launch)
+    dev.sync()
+    graph.close()
+    nf = len(batch.frames)
+    return {"workload": "256 frames, sides {256,512,1024,2048}, 1k-500k triangles log-uniform, RGBA8 + D24S8, "
+                        "1/3 flat, 2/3 textured (1024^2 trilinear), 1/4 with a stencil-mirror pass",
+            "frames": nf, "triangles": batch.triangles, "pixels": batch.pixels,
+            "plain_frames_per_s": nf * steps / plain_s, "batched_frames_per_s": nf * steps / graph_s,
+            "batched_gpix_per_s": batch.pixels * steps / graph_s / 1e9,
+            "batched_over_plain": plain_s / graph_s, "graph_passes": info["passes"],
+            "graph_kernels": info["kernels"], "steps": steps}
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -332,6 +373,7 @@ def run_gpu(args):
         barrier()
         e2e_fps = frames / max_over_ranks(time.perf_counter() - t0)
     dev.sync()
+    uneven = None if args.no_uneven else measure_uneven(dev, stream, flush, args)
 
     if rank == 0:
         peak, peak_kind = measured_peak()
@@ -374,6 +416,7 @@ def run_gpu(args):
                 "value": e2e_fps, "unit": UNIT,
                 "h2d_bytes_per_step": int(vb_host.numel() * 4 + ib_host.numel() * 4),
                 "d2h_bytes_per_step": out_bytes},
+            "uneven_batch": uneven,
             "gpu_launches": int(ginfo["kernels"]) * args.steps,
             "clocks": clk.summary(),
         }

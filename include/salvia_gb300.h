@@ -331,9 +331,11 @@ int32_t sg_draw_static_scratch(sg_device* dev, const sg_draw_desc* desc, sg_draw
  * its draws and targets, splitting where order matters: a target cleared,
  * resolved or sampled between two of its draws, a draw whose depth test runs
  * before shading (no stencil) after one whose test runs after shading on the
- * same depth target, or a pass reaching SG_PASS_MAX_PRIMS primitives. */
+ * same depth target, or a pass reaching SG_PASS_MAX_PRIMS primitives or
+ * SG_PASS_MAX_SAMPLES target samples. */
 enum { SG_CMD_DRAW = 1, SG_CMD_CLEAR_COLOR = 2, SG_CMD_CLEAR_DEPTH_STENCIL = 3, SG_CMD_RESOLVE = 4 };
 #define SG_PASS_MAX_PRIMS (1u << 24)
+#define SG_PASS_MAX_SAMPLES (1ull << 26)
 
 typedef struct sg_command {
   uint32_t type;                       /* SG_CMD_* */

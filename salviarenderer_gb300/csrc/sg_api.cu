@@ -160,6 +160,7 @@ struct PassPlan {
   std::vector<uint8_t> late_z;               // per target: a draw tests depth after shading
   std::vector<uint32_t> target_color, target_ds;
   uint64_t nprims = 0;
+  uint64_t samples = 0;                      // target samples of the pass's targets
   // derived by finalize()
   std::vector<uint32_t> draw_prim_base, target_tile_base, chunk_target;
   uint32_t ntiles = 0, nslots = 0, nchunks = 0, max_samples = 1;
@@ -486,8 +487,13 @@ void fill_target(sg_device* d, uint32_t color, uint32_t ds, TargetParams& T) {
 // pass assembly
 
 // Whether the draw can join the pass; if not, the pass must run first.
-bool draw_fits(PassPlan const& pl, DrawParams const& p, DrawInfo const& info) {
+bool draw_fits(sg_device* d, PassPlan const& pl, DrawParams const& p, DrawInfo const& info) {
   if (pl.nprims + p.prim_count > SG_PASS_MAX_PRIMS) return false;
+  if (!pl.draws.empty() && !pl.target_of.count({info.color, info.ds})) {
+    Texture* t = find_tex(d, info.color ? info.color : info.ds);
+    uint64_t const smp = static_cast<uint64_t>(t->levels[0].w) * t->levels[0].h * t->samples;
+    if (pl.samples + smp > SG_PASS_MAX_SAMPLES) return false;
+  }
   for (uint32_t t : info.tex)
     if (t && (pl.surfaces.count(t) || pl.cleared.count(t) || pl.resolved.count(t))) return false;
   for (uint32_t s : {info.color, info.ds}) {
@@ -515,6 +521,7 @@ void add_draw(sg_device* d, PassPlan& pl, DrawParams p, DrawInfo const& info, ui
     fill_target(d, info.color, info.ds, T);
     pl.targets.push_back(T);
     pl.late_z.push_back(0);
+    pl.samples += static_cast<uint64_t>(T.width) * T.height * T.samples;
     if (info.color) pl.surfaces.insert(info.color);
     if (info.ds) pl.surfaces.insert(info.ds);
   } else {
@@ -653,6 +660,9 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.scan_sums.ensure((pl.ncounts / 4096 + 2) * 4));
   SG_CUDA(d, sc.bin_entries.ensure(static_cast<size_t>(sc.entry_capacity) * 4));
   SG_CUDA(d, sc.tile_begin.ensure((static_cast<size_t>(pl.ntiles) + 1) * 4));
+  // fragment room for at least two quads per pixel quad of the pass's targets
+  uint64_t const want_chunks = pl.samples / 4 * 2 / FRAG_CHUNK + 1024;
+  if (want_chunks > sc.chunk_capacity) sc.chunk_capacity = static_cast<uint32_t>(std::min<uint64_t>(want_chunks, 1u << 30));
   size_t nfrag = static_cast<size_t>(sc.chunk_capacity) * FRAG_CHUNK;
   SG_CUDA(d, sc.frag_rec.ensure(nfrag * 4));
   SG_CUDA(d, sc.frag_pos.ensure(nfrag * 4));
@@ -1009,7 +1019,7 @@ int32_t plan_commands(sg_device* d, sg_command const* cmds, uint32_t n, Sink&& s
       DrawParams p;
       DrawInfo info;
       if (int32_t r = translate_draw(d, c.draw, p, info)) return r;
-      if (!draw_fits(pl, p, info))
+      if (!draw_fits(d, pl, p, info))
         if (int32_t r = flush()) return r;
       add_draw(d, pl, p, info, i);
       break;

@@ -430,3 +430,155 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
             dd["base_vertex"] = base_vertex + first * (3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else 1)
         s.draws.append(dd)
     return s
+
+
+# --------------------------------------------------------------------------
+def random_small_tris(rng, n, extent):
+    """n independent clip-space triangles: each one's vertices lie in a box
+    of half-size `extent` around a uniform centre in [-1,1]^2, at a depth
+    uniform in [0.05, 0.95] (w = 1).  Returns (3n, 12) float32: position,
+    texcoord (u, v spanning [0, 4] over the screen), colour."""
+    c = rng.uniform(-1.0, 1.0, size=(n, 1, 2))
+    p = c + rng.uniform(-extent, extent, size=(n, 3, 2))
+    z = rng.uniform(0.05, 0.95, size=(n, 1, 1)) + rng.uniform(-0.02, 0.02, size=(n, 3, 1))
+    v = np.zeros((n, 3, 12), dtype=np.float64)
+    v[:, :, 0:2] = p
+    v[:, :, 2:3] = z
+    v[:, :, 3] = 1.0
+    v[:, :, 4:6] = (p + 1.0) * 2.0
+    v[:, :, 8:11] = rng.uniform(0.0, 1.0, size=(n, 3, 3))
+    v[:, :, 11] = 1.0
+    return v.reshape(-1, 12).astype(np.float32)
+
+
+class UnevenBatch:
+    """Many independent frames of uneven size and triangle count, each with
+    its own RGBA8 + D24S8 targets (the batched-draw workload).
+
+    Frame i: side length drawn uniformly from `sizes`; triangle count
+    log-uniform in `tri_range`; every third frame flat-coloured (a constant
+    colour per frame), the others textured (one shared value-noise texture,
+    trilinear, modulated by the vertex colour); every fourth frame adds the
+    stencil-mirror pass (a quad written with stencil REPLACE, then a quarter
+    of the frame's triangles reflected and drawn with stencil EQUAL).
+    Triangles are small random clip-space triangles sized so that the
+    expected depth complexity is about three (random_small_tris).
+    """
+
+    def __init__(self, seed=20261204, nframes=256, sizes=(256, 512, 1024, 2048), tri_range=(1000, 500000),
+                 tex_size=1024):
+        rng = np.random.default_rng(seed)
+        self.tex = to_rgba8(value_noise(rng, tex_size))
+        self.frames = []
+        chunks = []
+        base = 0
+        for i in range(nframes):
+            size = int(sizes[rng.integers(len(sizes))])
+            n = int(round(math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1])))))
+            extent = min(0.5, math.sqrt(40.0 / n))
+            chunks.append(random_small_tris(rng, n, extent))
+            self.frames.append(dict(size=size, ntris=n, base=base, flat=(i % 3 == 0), mirror=(i % 4 == 3),
+                                    color=tuple(float(x) for x in rng.uniform(0.2, 1.0, size=3)) + (1.0,)))
+            base += 3 * n
+        self.vb = np.concatenate(chunks)
+        self.quad = np.array([[-0.5, -0.5, 0.5, 1, 0, 0, 0, 0, 0.3, 0.3, 0.9, 1],
+                              [0.5, -0.5, 0.5, 1, 0, 0, 0, 0, 0.3, 0.3, 0.9, 1],
+                              [-0.5, 0.5, 0.5, 1, 0, 0, 0, 0, 0.3, 0.3, 0.9, 1],
+                              [0.5, 0.5, 0.5, 1, 0, 0, 0, 0, 0.3, 0.3, 0.9, 1]], dtype=np.float32)
+        self.quad_ib = np.array([0, 2, 1, 1, 2, 3], dtype=np.uint16)
+
+    @property
+    def triangles(self):
+        return sum(f["ntris"] + (f["ntris"] // 4 + 2 if f["mirror"] else 0) for f in self.frames)
+
+    @property
+    def pixels(self):
+        return sum(f["size"] * f["size"] for f in self.frames)
+
+
+class BoundUneven:
+    """An UnevenBatch's resources on one device, its draws and command lists."""
+
+    def __init__(self, dev, batch):
+        self.dev, self.batch = dev, batch
+        self.vb = dev.buffer(batch.vb)
+        self.quad = dev.buffer(batch.quad)
+        self.quad_ib = dev.buffer(batch.quad_ib)
+        t = dev.texture(batch.tex.shape[1], batch.tex.shape[0], 1, abi.FMT_RGBA8)
+        dev.texture_upload(t, batch.tex)
+        dev.gen_mipmap(t, abi.FILTER_LINEAR)
+        self.tex = t
+        self.samp = dev.sampler(t, min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+                                mip_filter=abi.FILTER_LINEAR)
+        ident = np.identity(4, dtype=np.float32)
+        mirror = np.diag([-1.0, 1.0, 1.0, 1.0]).astype(np.float32)
+        ds_write = default_depth_stencil()
+        ds_write.stencil_enable, ds_write.depth_write = 1, 0
+        ds_test = default_depth_stencil()
+        ds_test.stencil_enable = 1
+        for face in (ds_write.front, ds_write.back):
+            face.func, face.pass_op = abi.CMP_ALWAYS, abi.SOP_REPLACE
+        for face in (ds_test.front, ds_test.back):
+            face.func, face.pass_op = abi.CMP_EQUAL, abi.SOP_KEEP
+        self.targets, self.descs = [], []
+        for f in batch.frames:
+            s = f["size"]
+            color = dev.texture(s, s, 1, abi.FMT_RGBA8)
+            ds = dev.texture(s, s, 1, abi.FMT_D24S8)
+            self.targets.append((color, ds))
+            vp = (0, 0, s, s, 0.0, 1.0)
+            common = dict(viewport=vp, color_target=color, ds_target=ds, inputs=GRID_INPUTS)
+            stream = [(self.vb, 48, 4 * 12 * f["base"])]
+            if f["flat"]:
+                main = make_draw_desc(prim_count=f["ntris"], streams=stream, num_varyings=0,
+                                      vs=dict(program=abi.VS_TRANSFORM, constants=ident),
+                                      ps=dict(program=abi.PS_CONSTANT, constants=f["color"]),
+                                      bs=dict(program=abi.BS_REPLACE), **common)
+            else:
+                main = make_draw_desc(prim_count=f["ntris"], streams=stream, num_varyings=2,
+                                      varying_modifiers=[abi.AM_LINEAR, abi.AM_LINEAR],
+                                      vs=dict(program=abi.VS_TRANSFORM, constants=ident),
+                                      ps=dict(program=abi.PS_TEX_MODULATE, samplers=[self.samp]),
+                                      bs=dict(program=abi.BS_REPLACE), **common)
+            draws = [main]
+            if f["mirror"]:
+                draws.append(make_draw_desc(prim_count=2, streams=[(self.quad, 48, 0)], index_buffer=self.quad_ib,
+                                            index_format=abi.INDEX_U16, num_varyings=1,
+                                            varying_modifiers=[abi.AM_LINEAR], depth_stencil=ds_write,
+                                            stencil_ref=1, vs=dict(program=abi.VS_TRANSFORM, constants=ident),
+                                            ps=dict(program=abi.PS_COLOR), bs=dict(program=abi.BS_REPLACE),
+                                            **dict(common, inputs=COLOR_FIRST_INPUTS)))
+                draws.append(make_draw_desc(prim_count=f["ntris"] // 4, streams=stream, num_varyings=1,
+                                            varying_modifiers=[abi.AM_LINEAR], depth_stencil=ds_test,
+                                            stencil_ref=1, vs=dict(program=abi.VS_TRANSFORM, constants=mirror),
+                                            ps=dict(program=abi.PS_COLOR), bs=dict(program=abi.BS_REPLACE),
+                                            **dict(common, inputs=COLOR_FIRST_INPUTS)))
+            self.descs.append(draws)
+
+    def frame_commands(self, i, cl=None):
+        cl = cl if cl is not None else CommandList()
+        color, ds = self.targets[i]
+        cl.clear_color(color, (0.1, 0.1, 0.1, 1.0))
+        cl.clear_depth_stencil(ds, abi.CLEAR_DEPTH | abi.CLEAR_STENCIL, 1.0, 0)
+        for d in self.descs[i]:
+            cl.draw(d)
+        return cl
+
+    def commands(self):
+        """Every frame as one command list."""
+        cl = CommandList()
+        for i in range(len(self.descs)):
+            self.frame_commands(i, cl)
+        return cl
+
+    def render_plain(self):
+        """Every frame call by call: clears, then one sg_draw per draw."""
+        for i, (color, ds) in enumerate(self.targets):
+            self.dev.clear_color(color, (0.1, 0.1, 0.1, 1.0))
+            self.dev.clear_depth_stencil(ds, abi.CLEAR_DEPTH | abi.CLEAR_STENCIL, 1.0, 0)
+            for d in self.descs[i]:
+                self.dev.draw(d)
+
+    def outputs(self, i):
+        color, ds = self.targets[i]
+        return {"color": self.dev.texture_download(color), "depth_stencil": self.dev.texture_download(ds)}
