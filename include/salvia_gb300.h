@@ -122,7 +122,14 @@ enum {
   SG_PS_TEX_MODULATE = 3,
   /* out.color[0] = sampler0.sample_2d_grad(in.attr[0].xy, ddx(0).xy,
    * ddy(0).xy, 0) * in.attr[1]  (sampler.cpp:854-873; the anisotropic path). */
-  SG_PS_TEX_GRAD_MODULATE = 4
+  SG_PS_TEX_GRAD_MODULATE = 4,
+  /* No counterpart in the reference: SG_PS_TEX_GRAD_MODULATE with the
+   * anisotropic lookup approximated by the learned filter named in the
+   * shader's `learned_filter` (sg_af_model_id) where it applies -- a minified
+   * lookup of an anisotropic sampler with more than 4 and at most
+   * constants[1] probes -- and where the filter's confidence is at least
+   * constants[0]; every other lookup runs the plain sampler. */
+  SG_PS_TEX_GRAD_LEARNED = 5
 };
 enum {
   SG_BS_REPLACE = 1,        /* color(0, s) = in.color[0] */
@@ -182,7 +189,7 @@ typedef struct sg_vs_input {           /* input_element_desc (input_layout.h:20-
 typedef struct sg_shader {
   uint32_t program;                    /* SG_VS_* / SG_PS_* / SG_BS_* */
   uint32_t samplers[SG_MAX_SHADER_SAMPLERS];
-  uint32_t reserved;
+  uint32_t learned_filter;             /* SG_PS_TEX_GRAD_LEARNED: sg_af_model_id, else 0 */
   float constants[SG_MAX_SHADER_CONSTANTS];
 } sg_shader;
 
@@ -235,6 +242,8 @@ typedef struct sg_profile_data {
   uint64_t draws;
   uint64_t launches;          /* kernels launched (all stages, clears, resolves) */
   uint64_t raster_launches;
+  uint64_t af_lookups;        /* lookups the learned filter took */
+  uint64_t af_fallbacks;      /* of those, the ones it sent back to the plain sampler */
 } sg_profile_data;
 
 /* ---- device (create_benchmark_renderer, renderer.h:133-134) --------------- */
@@ -400,6 +409,69 @@ int32_t sg_set_tuning(sg_device* dev, const sg_tuning* tuning);
  * candidate. */
 int32_t sg_autotune(sg_device* dev, const sg_command* cmds, uint32_t n, uint32_t reps, sg_tuning* out,
                     float* best_ms);
+
+/* ---- learned anisotropic filter --------------------------------------------
+ * No counterpart in the reference.  A small MLP (24 inputs -> 64 -> 64 -> 5,
+ * GELU in its tanh form, BF16 weights and activations, FP32 accumulate on the
+ * tensor cores) that predicts sampler::sample_2d_grad's anisotropic result
+ * and a confidence from the texel-space derivatives, the anisotropy measures
+ * of calc_anisotropic_info and four bilinear taps along the major axis
+ * (sampler.cpp:730-760,875-958).  Features, in order: the two derivatives in
+ * texels divided by the longer one's length (4), the probes' mip level / 8,
+ * log2 of the longer derivative's length / 8, the probe count / 16, log2 of
+ * the anisotropy ratio / 4, and the RGBA of bilinear taps at the probes'
+ * level at -3/8, -1/8, 1/8 and 3/8 of the probe span (16).  The predicted
+ * colour is 0.25 * ((tap0 + tap1) + (tap2 + tap3)) (float32) plus the
+ * network's first four outputs; the confidence is the sigmoid of the fifth.
+ * Parameters are fp32 masters in the order W1 [64 x 24], b1 [64],
+ * W2 [64 x 64], b2 [64], W3 [5 x 64], b3 [5] (W[out][in]). */
+#define SG_AF_FEATURES 24
+#define SG_AF_OUTPUTS 5
+#define SG_AF_PARAMS 6085
+typedef struct sg_af_model sg_af_model;
+/* Uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights from `seed`, zero biases. */
+int32_t sg_af_model_create(sg_device* dev, uint64_t seed, sg_af_model** out_model);
+/* Destroy recorded graphs that draw with the model before the model. */
+void sg_af_model_destroy(sg_device* dev, sg_af_model* model);
+/* The id a pixel shader names the model by (sg_shader.learned_filter). */
+uint32_t sg_af_model_id(const sg_af_model* model);
+int32_t sg_af_model_get_params(sg_device* dev, sg_af_model* model, float* params /* SG_AF_PARAMS */);
+int32_t sg_af_model_set_params(sg_device* dev, sg_af_model* model, const float* params);
+/* Inference on the tensor cores: `features` n x 24 (the network reads them
+ * rounded to BF16), `out` n x 5 (predicted RGBA, confidence in [0, 1]). */
+int32_t sg_af_model_forward(sg_device* dev, sg_af_model* model, const float* features, uint32_t n, float* out);
+/* Draws n random anisotropic lookups on the samplers (lookup i on sampler
+ * i mod num_samplers: uniform position, minor axis 2^U(0, 7) texels, ratio
+ * U(2.5, 16), major axis at a uniform angle) and writes their features
+ * (n x 24) and the plain sampler's result as the target (n x 4 RGBA). */
+int32_t sg_af_sample(sg_device* dev, const uint32_t* samplers, uint32_t num_samplers, uint32_t n, uint64_t seed,
+                     float* features, float* targets);
+/* One forward and backward pass on the tensor cores over n samples: `grads`
+ * (SG_AF_PARAMS) receives the gradient of the mean loss, `loss` the mean
+ * loss.  Loss of one sample: the squared error of the predicted colour plus
+ * the binary cross-entropy of the confidence against
+ * exp(-32 * max |colour error|).  The parameters do not change. */
+int32_t sg_af_model_gradients(sg_device* dev, sg_af_model* model, const float* features, const float* targets,
+                              uint32_t n, float* grads, float* loss);
+typedef struct sg_af_train_desc {
+  const uint32_t* samplers; /* training textures (sampler handles) */
+  uint32_t num_samplers;
+  uint32_t samples;         /* training set size, drawn once as sg_af_sample does */
+  uint32_t batch;           /* samples per Adam step */
+  uint32_t epochs;
+  float lr;                 /* Adam step size (beta1 0.9, beta2 0.999, eps 1e-8) */
+  uint64_t seed;
+} sg_af_train_desc;
+typedef struct sg_af_report {
+  float first_loss;         /* mean loss of the first and last batches */
+  float last_loss;
+  uint32_t steps;
+  float train_ms;           /* device time of the steps (CUDA events) */
+} sg_af_report;
+/* Trains the model on the device: the training set is sampled from the plain
+ * anisotropic sampler, then each step is a tensor-core forward and backward
+ * pass over one batch and an Adam update of the fp32 masters. */
+int32_t sg_af_model_train(sg_device* dev, sg_af_model* model, const sg_af_train_desc* desc, sg_af_report* report);
 
 /* renderer::clear_color (renderer.h:124). */
 int32_t sg_clear_color(sg_device* dev, uint32_t texture, const float rgba[4]);

@@ -1318,7 +1318,8 @@ bool run_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, float& lod_cac
     out = mulv(t, in.r[2]);
     return true;
   }
-  case SG_PS_TEX_GRAD_MODULATE: {
+  case SG_PS_TEX_GRAD_MODULATE:
+  case SG_PS_TEX_GRAD_LEARNED: {  // the oracle of the learned filter is the plain lookup it approximates
     vec4 dx = sub(quad[1].r[1], quad[0].r[1]);
     vec4 dy = sub(quad[2].r[1], quad[0].r[1]);
     vec4 t = sample_2d_grad(*c.ps_samp, in.r[1][0], in.r[1][1], dx[0], dx[1], dy[0], dy[1], 0.0f);

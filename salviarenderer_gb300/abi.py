@@ -38,7 +38,7 @@ AM_LINEAR, AM_CENTROID, AM_NOINTERPOLATION, AM_NOPERSPECTIVE, AM_SAMPLE = 1, 2, 
 SEMANTIC_POSITION, SEMANTIC_TEXCOORD, SEMANTIC_COLOR, SEMANTIC_NORMAL = 0, 1, 2, 3
 
 VS_TRANSFORM, VS_MORPH_DISPLACE = 1, 2
-PS_COLOR, PS_CONSTANT, PS_TEX_MODULATE, PS_TEX_GRAD_MODULATE = 1, 2, 3, 4
+PS_COLOR, PS_CONSTANT, PS_TEX_MODULATE, PS_TEX_GRAD_MODULATE, PS_TEX_GRAD_LEARNED = 1, 2, 3, 4, 5
 BS_REPLACE, BS_LERP_SRC_ALPHA, BS_ADD = 1, 2, 3
 CMD_DRAW, CMD_CLEAR_COLOR, CMD_CLEAR_DEPTH_STENCIL, CMD_RESOLVE = 1, 2, 3, 4
 
@@ -85,7 +85,7 @@ class VSInput(C.Structure):
 
 class Shader(C.Structure):
     _fields_ = [("program", C.c_uint32), ("samplers", C.c_uint32 * SG_MAX_SHADER_SAMPLERS),
-                ("reserved", C.c_uint32), ("constants", C.c_float * SG_MAX_SHADER_CONSTANTS)]
+                ("learned_filter", C.c_uint32), ("constants", C.c_float * SG_MAX_SHADER_CONSTANTS)]
 
 
 class DrawDesc(C.Structure):
@@ -104,7 +104,8 @@ class DrawDesc(C.Structure):
 class ProfileData(C.Structure):
     _fields_ = [("geometry_ms", C.c_double), ("binning_ms", C.c_double), ("raster_ms", C.c_double),
                 ("cover_ms", C.c_double), ("shade_ms", C.c_double), ("merge_ms", C.c_double),
-                ("draws", C.c_uint64), ("launches", C.c_uint64), ("raster_launches", C.c_uint64)]
+                ("draws", C.c_uint64), ("launches", C.c_uint64), ("raster_launches", C.c_uint64),
+                ("af_lookups", C.c_uint64), ("af_fallbacks", C.c_uint64)]
 
 
 class DrawStats(C.Structure):
@@ -126,6 +127,18 @@ class Tuning(C.Structure):
 
 
 _u32p = C.POINTER(C.c_uint32)
+
+class AfTrainDesc(C.Structure):
+    """sg_af_train_desc"""
+    _fields_ = [("samplers", _u32p), ("num_samplers", C.c_uint32), ("samples", C.c_uint32),
+                ("batch", C.c_uint32), ("epochs", C.c_uint32), ("lr", C.c_float), ("seed", C.c_uint64)]
+
+
+class AfReport(C.Structure):
+    """sg_af_report"""
+    _fields_ = [("first_loss", C.c_float), ("last_loss", C.c_float), ("steps", C.c_uint32),
+                ("train_ms", C.c_float)]
+
 
 SIGNATURES = {
     "sg_device_create": (C.c_int32, [C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
@@ -166,12 +179,27 @@ SIGNATURES = {
     "sg_set_tuning": (C.c_int32, [C.c_void_p, C.POINTER(Tuning)]),
     "sg_autotune": (C.c_int32, [C.c_void_p, C.POINTER(Command), C.c_uint32, C.c_uint32,
                                 C.POINTER(Tuning), C.POINTER(C.c_float)]),
+    "sg_af_model_create": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "sg_af_model_destroy": (None, [C.c_void_p, C.c_void_p]),
+    "sg_af_model_id": (C.c_uint32, [C.c_void_p]),
+    "sg_af_model_get_params": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
+    "sg_af_model_set_params": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
+    "sg_af_model_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_float), C.c_uint32,
+                                        C.POINTER(C.c_float)]),
+    "sg_af_sample": (C.c_int32, [C.c_void_p, _u32p, C.c_uint32, C.c_uint32, C.c_uint64,
+                                 C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "sg_af_model_gradients": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                          C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "sg_af_model_train": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(AfTrainDesc), C.POINTER(AfReport)]),
 }
+
+AF_FEATURES, AF_OUTPUTS, AF_PARAMS = 24, 5, 6085
 
 # Entry points of the GPU library with no counterpart in the reference (the
 # CPU oracle does not export them).
 PRODUCT_ONLY = {"sg_draw_static_scratch", "sg_graph_create", "sg_graph_launch", "sg_graph_info",
                 "sg_graph_destroy", "sg_get_tuning", "sg_set_tuning", "sg_autotune"}
+PRODUCT_ONLY |= {name for name in SIGNATURES if name.startswith("sg_af_")}
 
 
 def bind(lib, extra=None):

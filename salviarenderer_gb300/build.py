@@ -2,7 +2,7 @@
 
     python -m salviarenderer_gb300.build
 
-nvcc compiles the three translation units in parallel with
+nvcc compiles the translation units in parallel with
 -gencode arch=compute_103a,code=sm_103a, -fmad=false (no contraction of a
 multiply and an add into an FMA, which the bit-exact float semantics need)
 and -lineinfo, then links them into salviarenderer_gb300/_lib/.
@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT, "libsalvia_gb300.so")
 SOURCES = ["sg_raster_a.cu", "sg_raster_b.cu", "sg_raster_c.cu", "sg_cover.cu", "sg_draw.cu", "sg_misc.cu",
-           "sg_api.cu"]
+           "sg_api.cu", "sg_learned.cu", "sg_af_api.cu", "sg_af_data.cu", "sg_af_filter.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

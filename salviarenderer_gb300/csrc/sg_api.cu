@@ -24,6 +24,7 @@
 #include "salvia_gb300.h"
 #include "sg_draw.cuh"
 #include "sg_jobs.cuh"
+#include "sg_learned.cuh"
 
 namespace sg {
 void launch_geometry(PassParams const& p, cudaStream_t s);
@@ -45,6 +46,11 @@ cudaError_t upload_ewa_table_raster_a(float const* tab, cudaStream_t s);
 cudaError_t upload_ewa_table_raster_b(float const* tab, cudaStream_t s);
 cudaError_t upload_ewa_table_raster_c(float const* tab, cudaStream_t s);
 cudaError_t upload_ewa_table_geometry(float const* tab, cudaStream_t s);
+cudaError_t upload_ewa_table_af(float const* tab, cudaStream_t s);
+cudaError_t upload_ewa_table_filter(float const* tab, cudaStream_t s);
+void launch_af_pass(PassParams const& P, AfModelDev const& M, uint32_t num_sms, cudaStream_t s);
+void launch_shade_learned(uint32_t na, PassParams const& P, uint32_t grid, cudaStream_t s);
+void launch_af_count(PassParams const& P, unsigned long long* acc, cudaStream_t s);
 uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaStream_t s);
 void launch_mip(uint8_t const* src, uint32_t sw, uint32_t sh, uint8_t* dst, uint32_t dw, uint32_t dh,
                 uint32_t samples, uint32_t fmt, uint32_t filter, cudaStream_t s);
@@ -131,14 +137,14 @@ uint8_t* static_scratch_address(int ordinal) {
 // every recorded graph owns its own.
 struct Scratch {
   Arena params, slot_rec, recs, bin_counts, scan_sums, bin_entries, tile_begin, frag_rec, frag_pos, frag_mask,
-      frag_color, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, sticky;
+      frag_color, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, sticky, af_lookups, af_fallback;
   bool pending = false;                // passes ran since the host last read `sticky`
   uint32_t entry_capacity = 1u << 24;  // bin entries (grows after an overflow)
   uint32_t chunk_capacity = 1u << 18;  // fragment chunks (grows after an overflow)
   void release() {
     for (Arena* a : {&params, &slot_rec, &recs, &bin_counts, &scan_sums, &bin_entries, &tile_begin, &frag_rec,
                      &frag_pos, &frag_mask, &frag_color, &frag_ps, &chunk_next, &chunk_count, &owner_first,
-                     &counters, &stats, &sticky})
+                     &counters, &stats, &sticky, &af_lookups, &af_fallback})
       a->release();
   }
 };
@@ -161,6 +167,8 @@ struct PassPlan {
   std::vector<uint32_t> target_color, target_ds;
   uint64_t nprims = 0;
   uint64_t samples = 0;                      // target samples of the pass's targets
+  uint32_t af_model = 0;                     // the learned filter its draws use (one per pass), 0 = none
+  AfModelDev af{};
   // derived by finalize()
   std::vector<uint32_t> draw_prim_base, target_tile_base, chunk_target;
   uint32_t ntiles = 0, nslots = 0, nchunks = 0, max_samples = 1;
@@ -242,6 +250,7 @@ struct sg_device {
   unsigned int* sticky_host = nullptr;    // pinned: overflow bits read back at sg_sync
   unsigned int* static_sticky = nullptr;  // the static scratch's overflow word, when a call used it
   std::set<sg_graph*> graphs;
+  std::map<uint32_t, AfModelDev> af_models;  // learned filters by id
   sg_tuning tuning = default_tuning();
   std::string error;
   // profiling: event pairs per stage, summed at sg_profile_read
@@ -250,6 +259,7 @@ struct sg_device {
   size_t events_used = 0;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;  // (stage, begin, end)
   sg_profile_data prof{};
+  unsigned long long* prof_af = nullptr;   // device: learned-filter lookups and fallbacks while profiling
 };
 
 namespace {
@@ -338,6 +348,7 @@ void stage_end(sg_device* d, int stage, cudaEvent_t b) {
 struct DrawInfo {
   uint32_t color = 0, ds = 0;       // target textures
   uint32_t tex[2] = {0, 0};         // sampled textures
+  uint32_t af_model = 0;            // learned filter of an SG_PS_TEX_GRAD_LEARNED draw
 };
 
 int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, DrawInfo& info) {
@@ -405,10 +416,18 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   if (int32_t r = build_sampler(d, desc->vs.samplers[0], p.vs_samp, &info.tex[0])) return r;
   if (int32_t r = build_sampler(d, desc->ps.samplers[0], p.ps_samp, &info.tex[1])) return r;
   if (p.vs_prog == SG_VS_MORPH_DISPLACE && !desc->vs.samplers[0]) return SG_INVALID_PARAMETER;
-  if ((p.ps_prog == SG_PS_TEX_MODULATE || p.ps_prog == SG_PS_TEX_GRAD_MODULATE) && !desc->ps.samplers[0])
+  if ((p.ps_prog == SG_PS_TEX_MODULATE || p.ps_prog == SG_PS_TEX_GRAD_MODULATE ||
+       p.ps_prog == SG_PS_TEX_GRAD_LEARNED) && !desc->ps.samplers[0])
     return SG_INVALID_PARAMETER;
+  if (p.ps_prog == SG_PS_TEX_GRAD_LEARNED) {
+    if (!d->af_models.count(desc->ps.learned_filter)) return SG_INVALID_PARAMETER;
+    info.af_model = desc->ps.learned_filter;
+  }
   uint32_t const nattr = desc->num_varyings;
   p.nattr = nattr;
+  // learned-filter draws modulate by attribute 1; with fewer varyings the
+  // result is zero either way and the plain instance shades them
+  p.shade_class = nattr + ((p.ps_prog == SG_PS_TEX_GRAD_LEARNED && nattr >= 2) ? 8u : 0u);
   p.rec_stride = rec_stride_for(static_cast<int>(nattr));
   for (uint32_t i = 0; i < SG_MAX_VARYINGS; ++i) {
     p.mods[i] = desc->varying_modifiers[i];
@@ -500,6 +519,7 @@ bool draw_fits(sg_device* d, PassPlan const& pl, DrawParams const& p, DrawInfo c
     if (!s) continue;
     if (pl.sampled.count(s) || pl.resolved.count(s)) return false;
   }
+  if (info.af_model && pl.af_model && info.af_model != pl.af_model) return false;
   auto it = pl.target_of.find({info.color, info.ds});
   if (it == pl.target_of.end()) {
     // a new target may not share a surface with an existing one
@@ -531,6 +551,10 @@ void add_draw(sg_device* d, PassPlan& pl, DrawParams p, DrawInfo const& info, ui
   if (!(p.zcfg & 128u) && pl.targets[t].ds) pl.late_z[t] = 1;
   for (uint32_t x : info.tex)
     if (x) pl.sampled.insert(x);
+  if (info.af_model) {
+    pl.af_model = info.af_model;
+    pl.af = d->af_models.at(info.af_model);
+  }
   p.prim_base = static_cast<uint32_t>(pl.nprims);
   pl.nprims += p.prim_count;
   pl.draws.push_back(p);
@@ -552,7 +576,7 @@ void finalize(PassPlan& pl, sg_device* d) {
     T.tiles_y = std::max(T.tiles_y, p.tiles_y);
     slots[p.target] += 3ull * p.prim_count;
     if ((p.zcfg & 128u) && T.ds) T.any_early_z = 1;
-    pl.na_mask |= 1u << p.nattr;
+    pl.na_mask |= 1u << p.shade_class;
     pl.rec_units += 3ull * p.prim_count * p.rec_stride;
   }
   // slot ranges: targets in order, each target's draws in API order
@@ -672,6 +696,18 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.chunk_next.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.chunk_count.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.owner_first.ensure(static_cast<size_t>(pl.ntiles) * RASTER_THREADS * 4));
+  // learned-filter lookups: room for every pixel the fragment buffer holds
+  // (fragment pixel indices must fit 32 bits; past 2^30 pixels the pass's
+  // learned-filter draws run on the plain sampler)
+  P.af_capacity = 0;
+  if (pl.af_model && nfrag * 4 <= (1ull << 30)) {
+    uint32_t const cap = static_cast<uint32_t>(nfrag * 4);
+    SG_CUDA(d, sc.af_lookups.ensure(static_cast<size_t>(cap) * AF_LOOKUP_UNITS * sizeof(float4)));
+    SG_CUDA(d, sc.af_fallback.ensure(static_cast<size_t>(cap) * 4));
+    P.af_lookups = static_cast<float4*>(sc.af_lookups.ptr);
+    P.af_fallback = static_cast<uint32_t*>(sc.af_fallback.ptr);
+    P.af_capacity = cap;
+  }
   v.params = static_cast<uint8_t*>(sc.params.ptr);
   P.counters = static_cast<PassCounters*>(sc.counters.ptr);
   P.sticky = static_cast<unsigned int*>(sc.sticky.ptr);
@@ -742,6 +778,7 @@ int32_t scratch_static(sg_device* d, uint8_t* base, PassPlan const& pl, PlanLayo
   P.chunk_next = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(chunks) * 4));
   P.chunk_count = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(chunks) * 4));
   P.chunk_capacity = chunks;
+  P.af_capacity = 0;  // learned-filter draws run on the plain sampler here
   if (off > SG_STATIC_SCRATCH_BYTES) {  // layout arithmetic guard
     d->error = "sg_draw_static_scratch: scratch layout exceeds the static array";
     return SG_FAILED;
@@ -788,17 +825,23 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
         launch_cover(P, pl.max_samples, pl.any_early_z, cover_grid, s);
       stage_end(d, 2, ev);
       ev = stage_begin(d, profile);
-      for (uint32_t na = 0; na <= SG_MAX_VARYINGS; ++na) {
-        if (!(pl.na_mask & (1u << na))) continue;
-        switch (na) {
+      for (uint32_t cls = 0; cls < 16; ++cls) {  // shade classes: varyings, plus 8 for learned-filter draws
+        if (!(pl.na_mask & (1u << cls))) continue;
+        switch (cls) {
         case 0: launch_shade_0(P, shade_grid, s); break;
         case 1: launch_shade_1(P, shade_grid, s); break;
         case 2: launch_shade_2(P, shade_grid, s); break;
         case 3: launch_shade_3(P, shade_grid, s); break;
         case 4: launch_shade_4(P, shade_grid, s); break;
-        default: launch_shade_5(P, shade_grid, s); break;
+        case 5: launch_shade_5(P, shade_grid, s); break;
+        default: launch_shade_learned(cls - 8, P, shade_grid, s); break;
         }
         ++k;
+      }
+      if (pl.af_model && P.af_capacity) {
+        launch_af_pass(P, pl.af, sms, s);
+        k += 2;
+        if (profile && d->profiling && d->prof_af) launch_af_count(P, d->prof_af, s);
       }
       stage_end(d, 3, ev);
       ev = stage_begin(d, profile);
@@ -1070,8 +1113,12 @@ int32_t check_sticky(sg_device* d, Scratch& sc, char const* what) {
   sc.pending = false;
   SG_CUDA(d, cudaMemcpy(d->sticky_host, sc.sticky.ptr, sizeof(unsigned int), cudaMemcpyDeviceToHost));
   unsigned int bits = *d->sticky_host;
-  if (!(bits & (OVF_BIN | OVF_FRAG | OVF_REC))) return SG_OK;
+  if (!(bits & (OVF_BIN | OVF_FRAG | OVF_REC | OVF_AF_TIMEOUT))) return SG_OK;
   SG_CUDA(d, cudaMemset(sc.sticky.ptr, 0, sizeof(unsigned int)));
+  if (!(bits & (OVF_BIN | OVF_FRAG | OVF_REC))) {
+    d->error = "learned filter: a tensor-core wait timed out";
+    return SG_TIMEOUT;
+  }
   if (&sc == &d->scratch) {
     PassCounters c{};
     c.overflow = bits;
@@ -1127,6 +1174,8 @@ int32_t sg_device_create(int32_t cuda_device, void* cuda_stream, sg_device** out
   for (auto up : {upload_ewa_table_raster_a, upload_ewa_table_raster_b, upload_ewa_table_raster_c})
     if (up(tab, d->stream) != cudaSuccess) return SG_CUDA_ERROR;
   if (upload_ewa_table_geometry(tab, d->stream) != cudaSuccess) return SG_CUDA_ERROR;
+  if (upload_ewa_table_af(tab, d->stream) != cudaSuccess) return SG_CUDA_ERROR;
+  if (upload_ewa_table_filter(tab, d->stream) != cudaSuccess) return SG_CUDA_ERROR;
   if (cudaStreamSynchronize(d->stream) != cudaSuccess) return SG_CUDA_ERROR;
   *out = d.release();
   return SG_OK;
@@ -1144,6 +1193,7 @@ void sg_device_destroy(sg_device* d) {
   cudaFreeHost(d->counters_host);
   cudaFreeHost(d->sticky_host);
   if (d->stats_host) cudaFreeHost(d->stats_host);
+  if (d->prof_af) cudaFree(d->prof_af);
   for (cudaEvent_t e : d->event_pool) cudaEventDestroy(e);
   if (d->own_stream) cudaStreamDestroy(d->stream);
   delete d;
@@ -1164,6 +1214,8 @@ int32_t sg_profile_enable(sg_device* d, int32_t enable) {
   d->marks.clear();
   d->events_used = 0;
   d->prof = sg_profile_data{};
+  if (!d->prof_af) SG_CUDA(d, cudaMalloc(&d->prof_af, 2 * sizeof(unsigned long long)));
+  SG_CUDA(d, cudaMemset(d->prof_af, 0, 2 * sizeof(unsigned long long)));
   return SG_OK;
 }
 
@@ -1183,6 +1235,12 @@ int32_t sg_profile_read(sg_device* d, sg_profile_data* out) {
   out->shade_ms = acc[3];
   out->merge_ms = acc[4];
   out->raster_ms = acc[2] + acc[3] + acc[4];
+  if (d->prof_af) {
+    unsigned long long af[2];
+    SG_CUDA(d, cudaMemcpy(af, d->prof_af, sizeof(af), cudaMemcpyDeviceToHost));
+    out->af_lookups = af[0];
+    out->af_fallbacks = af[1];
+  }
   return SG_OK;
 }
 
@@ -1583,3 +1641,20 @@ int32_t sg_autotune(sg_device* d, const sg_command* cmds, uint32_t n, uint32_t r
 }
 
 }  // extern "C"
+
+// Device internals for the learned-filter runtime (sg_af_api.cu).
+namespace sg {
+cudaStream_t device_stream(sg_device* d) { return d->stream; }
+int device_sms(sg_device* d) { return d->num_sms; }
+void device_set_error(sg_device* d, char const* msg) { d->error = msg; }
+int32_t device_sampler(sg_device* d, uint32_t handle, dev_sampler& out) {
+  uint32_t tex = 0;
+  return build_sampler(d, handle, out, &tex);
+}
+uint32_t device_register_af(sg_device* d, AfModelDev const& m) {
+  uint32_t const id = d->next++;
+  d->af_models[id] = m;
+  return id;
+}
+void device_unregister_af(sg_device* d, uint32_t id) { d->af_models.erase(id); }
+}  // namespace sg

@@ -140,7 +140,7 @@ __device__ inline void vp_project(DrawParams const& D, vtx<NA>& v) {
 // rasterizer::compute_triangle_info (rasterizer.cpp:864-945) + compute_derivative_n
 // (shader.cpp:414-449); writes the record, returns false for zero area.
 template <int NA>
-__device__ bool setup_triangle(uint32_t draw, uint32_t zcfg, vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c,
+__device__ bool setup_triangle(uint32_t draw, uint32_t zcfg, uint32_t shade_class, vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c,
                                float4* rec) {
   vtx<NA> const* verts[3] = {&a, &b, &c};
   double dist[3];
@@ -193,7 +193,7 @@ __device__ bool setup_triangle(uint32_t draw, uint32_t zcfg, vtx<NA> const& a, v
   rec[1].w = v0.r[0].y;
   rec[2].w = v0.r[0].z;
   rec[4] = make_float4(rec[5 + R].z, rec[5 + 2 * R].z, __uint_as_float(draw),
-                       __uint_as_float(rec_flags(area > 0.0f, NA, zcfg)));
+                       __uint_as_float(rec_flags(area > 0.0f, shade_class, zcfg)));
   return true;
 }
 
@@ -206,7 +206,7 @@ __device__ void emit_triangle(PassParams const& P, DrawParams const& D, uint32_t
   vp_project(D, c);
   constexpr uint32_t STRIDE = rec_stride_for(NA);
   alignas(16) float4 rec[STRIDE];
-  bool ok = setup_triangle(draw, D.zcfg, a, b, c, rec);
+  bool ok = setup_triangle(draw, D.zcfg, D.shade_class, a, b, c, rec);
   uint32_t idx = NO_REC;
   if (ok) {
     idx = atomicAdd(&P.counters->rec_units, STRIDE);

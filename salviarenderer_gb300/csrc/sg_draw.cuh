@@ -25,6 +25,7 @@ constexpr uint32_t NO_REC = 0xFFFFFFFFu;
 
 // overflow bits of PassCounters::overflow
 constexpr uint32_t OVF_BIN = 1u, OVF_FRAG = 4u, OVF_REC = 8u;
+constexpr uint32_t OVF_AF_TIMEOUT = 16u;  // a tensor-core wait of the learned filter gave up
 
 struct PassCounters {
   unsigned int bin_entries;          // entries produced by the count pass
@@ -34,6 +35,8 @@ struct PassCounters {
   unsigned int fetch_oob;            // vertex or index reads outside their buffers
   unsigned int chunk_total;          // fragment chunks allocated by the coverage pass
   unsigned int merge_cursor;         // dynamic tile scheduler of the merge pass
+  unsigned int af_lookups;           // lookups queued for the learned filter
+  unsigned int af_fallbacks;         // of those, lookups sent back to the plain sampler
   unsigned int pad;
 };
 
@@ -85,6 +88,7 @@ struct DrawParams {
   uint32_t slot_base;           // first triangle slot (3 per primitive)
   uint32_t target;              // index into the pass's targets
   uint32_t nattr, rec_stride;
+  uint32_t shade_class;         // nattr, plus 8 for learned-filter draws: which k_shade instance runs it
   // shaders
   uint32_t vs_prog, ps_prog, bs_prog;
   float vs_k[SG_MAX_SHADER_CONSTANTS];
@@ -135,7 +139,7 @@ struct PassParams {
   // first chunk, chunk_next links them, chunk_count says how many slots of a
   // chunk are used.
   uint32_t* frag_rec;           // triangle record
-  uint32_t* frag_pos;           // bits 0-11 x/2, 12-23 y/2 (absolute quad), 24 full quad, 25-27 varyings
+  uint32_t* frag_pos;           // bits 0-11 x/2, 12-23 y/2 (absolute quad), 24 full quad, 25-28 shade class
   uint32_t* frag_mask;          // bits 0-15 early-Z-tested samples, 16-31 covered samples
   float4* frag_color;           // 4 pixels per fragment, pixel-shader output
   uint8_t* frag_ps;             // pixel-shader pass mask (4 bits)
@@ -148,7 +152,17 @@ struct PassParams {
   // coverage work items: 16 or 32 pixels on a side; 32x32 items of a tile with
   // more than split_entries bin entries become 16x16
   uint32_t cover_item, split_entries;
+  // learned anisotropic filter: k_shade queues the lookups it applies to
+  // (AF_LOOKUP_UNITS float4 each) for k_af_filter, which sends the ones it
+  // is not confident about to k_af_fallback through af_fallback
+  float4* af_lookups;
+  uint32_t* af_fallback;
+  uint32_t af_capacity;         // lookups; 0 runs every lookup on the plain sampler
 };
+
+// A queued learned-filter lookup: (u, v, ddx.u, ddx.v), (ddy.u, ddy.v,
+// fragment pixel index bits, draw index bits), the colour it modulates.
+constexpr uint32_t AF_LOOKUP_UNITS = 3;
 
 // triangle record layout (float4 units): [0..2] edge factors (x, y, z) with
 // v0's projected x, y, z in .w, [3] bbox, [4] (ddx.z, ddy.z of the position,
@@ -156,9 +170,9 @@ struct PassParams {
 // Slots 0-4 hold everything coverage and early-Z read.
 __host__ __device__ constexpr uint32_t rec_stride_for(int nattr) { return 5 + 3 * (1 + nattr); }
 
-// flags: the draw's zcfg (bits 0-12), varying count (28-30), front face (31)
-__host__ __device__ inline uint32_t rec_flags(bool front, uint32_t nattr, uint32_t zcfg) {
-  return (zcfg & 0x1FFFu) | (nattr << 28) | (front ? 0x80000000u : 0u);
+// flags: the draw's zcfg (bits 0-12), shade class (27-30), front face (31)
+__host__ __device__ inline uint32_t rec_flags(bool front, uint32_t shade_class, uint32_t zcfg) {
+  return (zcfg & 0x1FFFu) | (shade_class << 27) | (front ? 0x80000000u : 0u);
 }
 __device__ inline uint32_t rec_draw(float4 const* R) { return __float_as_uint(R[4].z); }
 __device__ inline uint32_t rec_flag_bits(float4 const* R) { return __float_as_uint(R[4].w); }

@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
         ts.dpy = R[5 + 2 * nreg];
         ts.entry = e;
         ts.zcfg = D.zcfg;
-        ts.nattr = D.nattr;
+        ts.nattr = D.shade_class;
         ts.pad = 0;
         stage[i] = ts;
         uint32_t bit = 1u << (i & 31), word = i >> 5;
@@ -629,17 +629,20 @@ __device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q) {
     return mulv(sample_impl(D.ps_samp, a0.x, a0.y, lod, nullptr), a1);
   }
   case SG_PS_TEX_GRAD_MODULATE:
+  case SG_PS_TEX_GRAD_LEARNED:  // the lookups the learned filter does not take
     return mulv(sample_2d_grad(D.ps_samp, a0.x, a0.y, u1 - u0, v1 - v0, u2 - u0, v2 - v0, 0.0f), a1);
   default: return mk4(0, 0, 0, 0);
   }
 }
 
+
 // Attribute interpolation (step_2d_unproj_attr_n_quad / step_2d_unproj_attr_n
 // with the centroid adjustment, shader.cpp:208-367, rasterizer.cpp:1363-1398)
 // and the pixel shader, for every fragment of the pass whose draw has NA
-// varyings.
-template <int NA>
-__global__ void __launch_bounds__(256) k_shade(PassParams P) {
+// varyings.  The LEARNED instances take the SG_PS_TEX_GRAD_LEARNED draws
+// (shade class 8 + NA) and queue the lookups the learned filter applies to.
+template <int NA, bool LEARNED>
+__global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
   if (P.counters->overflow & (OVF_BIN | OVF_FRAG | OVF_REC)) return;
   uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
   int const q = threadIdx.x & 3;
@@ -650,8 +653,19 @@ __global__ void __launch_bounds__(256) k_shade(PassParams P) {
     uint32_t f = start + it * groups;
     bool live = f < nfrag && (f % FRAG_CHUNK) < P.chunk_count[f / FRAG_CHUNK];
     uint32_t pos = live ? P.frag_pos[f] : 0u;
-    live = live && ((pos >> 25) & 7u) == static_cast<uint32_t>(NA);
+    live = live && ((pos >> 25) & 15u) == static_cast<uint32_t>(NA + (LEARNED ? 8 : 0));
     uint32_t draw = 0xFFFFFFFFu;
+    // learned-filter draws queue every pixel: reserve the warp's queue slots
+    uint32_t af_idx = 0;
+    if (LEARNED && P.af_capacity) {
+      unsigned const want = __ballot_sync(0xFFFFFFFFu, live);
+      if (want) {
+        int const lane = threadIdx.x & 31, leader = __ffs(want) - 1;
+        uint32_t first = 0;
+        if (lane == leader) first = atomicAdd(&P.counters->af_lookups, static_cast<unsigned>(__popc(want)));
+        af_idx = __shfl_sync(0xFFFFFFFFu, first, leader) + __popc(want & ((1u << lane) - 1u));
+      }
+    }
     if (live) {
       uint32_t rec = P.frag_rec[f], masks = P.frag_mask[f];
       TriView t{P.recs + rec, 1 + NA};
@@ -708,8 +722,26 @@ __global__ void __launch_bounds__(256) k_shade(PassParams P) {
         }
         attr[i] = (D.mods[i] & SG_AM_NOPERSPECTIVE) ? a : a * invw;
       }
-      v4 out = run_ps<NA>(D, attr, q);  // all four lanes of a quad take the same path
-      P.frag_color[static_cast<size_t>(f) * 4 + q] = make_float4(out.x, out.y, out.z, out.w);
+      if (LEARNED && P.af_capacity) {
+        // the lookup, with the quad's derivatives as run_ps takes them, for
+        // the filter pass (which runs the network or the plain sampler)
+        int const base = (threadIdx.x & 31) & ~3;
+        unsigned const qm = 0xFu << base;
+        v4 const a0 = attr[0];
+        float const u0 = __shfl_sync(qm, a0.x, base), v0 = __shfl_sync(qm, a0.y, base);
+        float const u1 = __shfl_sync(qm, a0.x, base + 1), v1 = __shfl_sync(qm, a0.y, base + 1);
+        float const u2 = __shfl_sync(qm, a0.x, base + 2), v2 = __shfl_sync(qm, a0.y, base + 2);
+        v4 const m = NA > 1 ? attr[NA > 1 ? 1 : 0] : mk4(0, 0, 0, 0);
+        if (af_idx < P.af_capacity) {  // always: the queue holds every pixel of the pass
+          float4* r = P.af_lookups + static_cast<size_t>(af_idx) * AF_LOOKUP_UNITS;
+          r[0] = make_float4(a0.x, a0.y, u1 - u0, v1 - v0);
+          r[1] = make_float4(u2 - u0, v2 - v0, __uint_as_float(f * 4 + q), __uint_as_float(draw));
+          r[2] = make_float4(m.x, m.y, m.z, m.w);
+        }
+      } else {
+        v4 out = run_ps<NA>(D, attr, q);  // all four lanes of a quad take the same path
+        P.frag_color[static_cast<size_t>(f) * 4 + q] = make_float4(out.x, out.y, out.z, out.w);
+      }
       if (q == 0) P.frag_ps[f] = 0xF;  // the stock programs never discard
     }
     // ps_invocations: 4 per quad, counted per draw (one lane per quad)
@@ -805,7 +837,11 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
 // ---------------------------------------------------------------------------
 template <int NA>
 void launch_shade_t(PassParams const& P, uint32_t grid, cudaStream_t s) {
-  k_shade<NA><<<grid, 256, 0, s>>>(P);
+  k_shade<NA, false><<<grid, 256, 0, s>>>(P);
+}
+template <int NA>
+void launch_shade_learned_t(PassParams const& P, uint32_t grid, cudaStream_t s) {
+  k_shade<NA, true><<<grid, 256, 0, s>>>(P);
 }
 
 }  // namespace sg

@@ -189,6 +189,18 @@ class Device:
                                                         C.byref(t), C.byref(ms)))
         return {k: getattr(t, k) for k, _ in abi.Tuning._fields_}, ms.value
 
+    def af_sample(self, samplers, n, seed=1):
+        """Random anisotropic lookups (sg_af_sample): features n x 24 and the
+        plain sampler's RGBA n x 4."""
+        hs = (C.c_uint32 * len(samplers))(*samplers)
+        f = np.empty((n, abi.AF_FEATURES), dtype=np.float32)
+        y = np.empty((n, 4), dtype=np.float32)
+        fp = C.POINTER(C.c_float)
+        self._check("sg_af_sample", self.lib.sg_af_sample(self.handle, C.cast(hs, C.POINTER(C.c_uint32)),
+                                                          len(samplers), n, seed, f.ctypes.data_as(fp),
+                                                          y.ctypes.data_as(fp)))
+        return f, y
+
     def clear_color(self, tex, rgba):
         arr = (C.c_float * 4)(*rgba)
         self._check("sg_clear_color", self.lib.sg_clear_color(self.handle, tex, arr))
@@ -199,6 +211,82 @@ class Device:
 
     def resolve(self, src, dst):
         self._check("sg_resolve", self.lib.sg_resolve(self.handle, src, dst))
+
+
+class AfModel:
+    """The learned anisotropic filter's MLP on one device (sg_af_model_*)."""
+
+    def __init__(self, dev, seed=1):
+        self.dev = dev
+        h = C.c_void_p()
+        dev._check("sg_af_model_create", dev.lib.sg_af_model_create(dev.handle, seed, C.byref(h)))
+        self.handle = h
+
+    def params(self):
+        p = np.empty(abi.AF_PARAMS, dtype=np.float32)
+        self.dev._check("sg_af_model_get_params",
+                        self.dev.lib.sg_af_model_get_params(self.dev.handle, self.handle,
+                                                            p.ctypes.data_as(C.POINTER(C.c_float))))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == abi.AF_PARAMS
+        self.dev._check("sg_af_model_set_params",
+                        self.dev.lib.sg_af_model_set_params(self.dev.handle, self.handle,
+                                                            p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def forward(self, features):
+        x = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, abi.AF_FEATURES)
+        out = np.empty((x.shape[0], abi.AF_OUTPUTS), dtype=np.float32)
+        self.dev._check("sg_af_model_forward",
+                        self.dev.lib.sg_af_model_forward(self.dev.handle, self.handle,
+                                                         x.ctypes.data_as(C.POINTER(C.c_float)), x.shape[0],
+                                                         out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def gradients(self, features, targets):
+        """Gradient of the mean loss over the samples (sg_af_model_gradients)
+        and the mean loss."""
+        x = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, abi.AF_FEATURES)
+        y = np.ascontiguousarray(targets, dtype=np.float32).reshape(-1, 4)
+        assert x.shape[0] == y.shape[0]
+        g = np.empty(abi.AF_PARAMS, dtype=np.float32)
+        loss = C.c_float()
+        fp = C.POINTER(C.c_float)
+        self.dev._check("sg_af_model_gradients",
+                        self.dev.lib.sg_af_model_gradients(self.dev.handle, self.handle, x.ctypes.data_as(fp),
+                                                           y.ctypes.data_as(fp), x.shape[0], g.ctypes.data_as(fp),
+                                                           C.byref(loss)))
+        return g, loss.value
+
+    def train(self, samplers, samples, batch=4096, epochs=1, lr=2e-3, seed=1):
+        """Trains on lookups of the plain sampler (sg_af_model_train); returns
+        the report as a dict."""
+        hs = (C.c_uint32 * len(samplers))(*samplers)
+        desc = abi.AfTrainDesc(samplers=C.cast(hs, C.POINTER(C.c_uint32)), num_samplers=len(samplers),
+                               samples=samples, batch=batch, epochs=epochs, lr=lr, seed=seed)
+        rep = abi.AfReport()
+        self.dev._check("sg_af_model_train",
+                        self.dev.lib.sg_af_model_train(self.dev.handle, self.handle, C.byref(desc), C.byref(rep)))
+        return {"first_loss": rep.first_loss, "last_loss": rep.last_loss, "steps": rep.steps,
+                "train_ms": rep.train_ms}
+
+    @property
+    def id(self):
+        """The id pixel shaders name the model by (sg_shader.learned_filter)."""
+        return self.dev.lib.sg_af_model_id(self.handle)
+
+    def close(self):
+        if self.handle is not None and self.dev.handle is not None:
+            self.dev.lib.sg_af_model_destroy(self.dev.handle, self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Graph:
@@ -333,4 +421,5 @@ def make_draw_desc(**kw):
             sh.samplers[i] = s
         for i, v in enumerate(np.asarray(spec.get("constants", ()), dtype=np.float32).ravel()):
             sh.constants[i] = float(v)
+        sh.learned_filter = spec.get("learned_filter", 0)
     return d

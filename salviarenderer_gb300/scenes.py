@@ -109,8 +109,9 @@ class Scene:
 class Bound:
     """Device handles of a scene's resources on one backend."""
 
-    def __init__(self, dev, scene):
+    def __init__(self, dev, scene, af_model=None):
         self.dev, self.scene = dev, scene
+        self.af_model = af_model
         self.buf = {k: dev.buffer(v) for k, v in scene.buffers.items()}
         self.tex = {}
         for k, (img, mips) in scene.textures.items():
@@ -131,6 +132,9 @@ class Bound:
     def _shader(self, spec):
         spec = dict(spec)
         spec["samplers"] = [self.samp[n] for n in spec.get("samplers", ())]
+        if spec.get("learned_filter") == "model":
+            # the CPU oracle renders learned-filter draws with the plain sampler
+            spec["learned_filter"] = self.af_model.id if self.af_model is not None else 0
         return spec
 
     def _desc(self, d):
@@ -194,9 +198,9 @@ class Bound:
         return out
 
 
-def render(dev, scene, stats=False, batched=False):
+def render(dev, scene, stats=False, batched=False, af_model=None):
     """Renders one frame: call by call, or (batched) as one command list."""
-    b = Bound(dev, scene)
+    b = Bound(dev, scene, af_model)
     if batched:
         cl = b.commands()
         st = dev.submit(cl, stats=stats)
@@ -281,8 +285,13 @@ COLOR_FIRST_INPUTS = [(abi.SEMANTIC_POSITION, 0, abi.VFMT_R32G32B32A32_FLOAT, 0,
 
 
 def c2_scene(seed=20261204, width=1920, height=1080, samples=4, grid=317, tex_size=2048,
-             ndraws=8, ds_fmt=abi.FMT_RG32F, max_aniso=16, af_draws=True):
-    """Textured, filtered, alpha-blended height-field grid (the 1080p 4x workload)."""
+             ndraws=8, ds_fmt=abi.FMT_RG32F, max_aniso=16, af_draws=True, learned=None, af_stride=2):
+    """Textured, filtered, alpha-blended height-field grid (the 1080p 4x workload).
+
+    Every other draw (every af_stride-th) samples anisotropically
+    (sample_2d_grad); with
+    `learned` = (confidence threshold, largest probe count) those draws run
+    SG_PS_TEX_GRAD_LEARNED with the model the scene is bound with."""
     rng = np.random.default_rng(seed)
     verts, idx = grid_mesh(rng, grid)
     tex = to_rgba8(value_noise(rng, tex_size))
@@ -305,7 +314,7 @@ def c2_scene(seed=20261204, width=1920, height=1080, samples=4, grid=317, tex_si
     ntris = idx.size // 3
     bounds = np.linspace(0, ntris, ndraws + 1).astype(np.int64)
     for i in range(ndraws):
-        aniso = af_draws and (i % 2 == 1)
+        aniso = af_draws and (i % af_stride == af_stride - 1)
         s.draws.append(dict(
             viewport=(0, 0, width, height, 0.0, 1.0),
             start=int(bounds[i] * 3), prim_count=int(bounds[i + 1] - bounds[i]),
@@ -313,8 +322,10 @@ def c2_scene(seed=20261204, width=1920, height=1080, samples=4, grid=317, tex_si
             streams=[("vb", 48, 0)], inputs=GRID_INPUTS,
             num_varyings=2, varying_modifiers=[abi.AM_LINEAR, abi.AM_LINEAR],
             vs=dict(program=abi.VS_TRANSFORM, constants=mvp),
-            ps=dict(program=abi.PS_TEX_GRAD_MODULATE if aniso else abi.PS_TEX_MODULATE,
-                    samplers=["aniso" if aniso else "trilinear"]),
+            ps=(dict(program=abi.PS_TEX_GRAD_LEARNED, samplers=["aniso"], learned_filter="model",
+                     constants=list(learned)) if aniso and learned is not None else
+                dict(program=abi.PS_TEX_GRAD_MODULATE if aniso else abi.PS_TEX_MODULATE,
+                     samplers=["aniso" if aniso else "trilinear"])),
             bs=dict(program=abi.BS_LERP_SRC_ALPHA)))
     s.clear_color = (0.1, 0.2, 0.3, 1.0)
     s.mvp = mvp
@@ -582,3 +593,39 @@ class BoundUneven:
     def outputs(self, i):
         color, ds = self.targets[i]
         return {"color": self.dev.texture_download(color), "depth_stencil": self.dev.texture_download(ds)}
+
+
+# --------------------------------------------------------------------------
+def af_training_images(seed=20261204, size=512):
+    """The learned anisotropic filter's training textures (RGBA8, size^2):
+    two value-noise fields, checkerboards of periods 2, 8 and 32 texels in
+    random colours and sinusoidal gratings at three frequencies and angles."""
+    rng = np.random.default_rng(seed)
+    imgs = [value_noise(rng, size), value_noise(rng, size, octaves=9)]
+    y, x = np.mgrid[0:size, 0:size]
+    for period in (2, 8, 32):
+        a, b = rng.uniform(0, 1, 4), rng.uniform(0, 1, 4)
+        m = (((x // period) + (y // period)) & 1).astype(np.float64)[..., None]
+        imgs.append(a * (1 - m) + b * m)
+    for cycles, ang in ((4, 0.3), (32, 1.1), (96, 2.2)):
+        k = 2 * np.pi * cycles / size
+        ph = rng.uniform(0, 2 * np.pi, 4)
+        t = (x * np.cos(ang) + y * np.sin(ang)) * k
+        imgs.append(0.5 + 0.5 * np.sin(t[..., None] + ph))
+    return [to_rgba8(i) for i in imgs]
+
+
+class AfTextures:
+    """The training (or evaluation) textures bound on a device with mip
+    chains and anisotropic samplers (16 probes at most)."""
+
+    def __init__(self, dev, images, max_aniso=16):
+        self.dev = dev
+        self.textures, self.samplers = [], []
+        for img in images:
+            t = dev.texture(img.shape[1], img.shape[0], 1, abi.FMT_RGBA8)
+            dev.texture_upload(t, img)
+            dev.gen_mipmap(t, abi.FILTER_LINEAR)
+            self.textures.append(t)
+            self.samplers.append(dev.sampler(t, min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+                                             mip_filter=abi.FILTER_ANISOTROPIC, max_anisotropy=max_aniso))
