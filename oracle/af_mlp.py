@@ -3,10 +3,10 @@
 ORACLE / TEST INFRASTRUCTURE: only tests/ load this module.  It restates the
 network the GPU kernels run -- 24 -> 64 -> 64 -> 5, GELU (tanh form), RGBA plus a
 confidence logit -- and its training loss and gradients, in float64.  With
-`bf16=True` it rounds the operands the GPU feeds to its tensor cores (inputs,
-weights, hidden activations, backward activations) to BF16 first, so forward
-outputs can be compared closely; gradients are compared against the exact
-float64 ones at a stated tolerance.
+`bf16_ops=True` it rounds the operands the GPU feeds to its tensor cores
+(inputs, weights, hidden activations) to BF16 and evaluates GELU in BF16
+steps as the GPU does, so forward outputs can be compared closely; gradients
+are compared against the exact float64 ones at a stated tolerance.
 
 Parameter layout (fp32 masters, W[out][in]): W1 [64 x 24], b1 [64],
 W2 [64 x 64], b2 [64], W3 [5 x 64], b3 [5].
@@ -60,6 +60,18 @@ def gelu(x):
     return 0.5 * x * (1.0 + np.tanh(x * (K0 + K1 * x * x)))
 
 
+def gelu_bf16(x):
+    """The GPU's forward GELU, step by step in BF16 arithmetic (each product
+    or fused multiply-add rounded once; tanh in float64 where the GPU's
+    tanh.approx differs by about one BF16 step)."""
+    k0, k1 = bf16(np.float32(K0)), bf16(np.float32(K1))
+    x = bf16(x)
+    u = bf16(x * bf16(bf16(x * x) * k1 + k0))
+    t = bf16(np.tanh(u))
+    h = bf16(x * 0.5)
+    return bf16(h * t + h)
+
+
 def gelu_grad(x):
     t = np.tanh(x * (K0 + K1 * x * x))
     return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * (K0 + 3.0 * K1 * x * x)
@@ -79,11 +91,12 @@ def forward(params, x, bf16_ops=False):
     P = unpack(params)
     r = bf16 if bf16_ops else (lambda v: np.asarray(v, dtype=np.float64))
     skip = tap_mean(x)
+    act = gelu_bf16 if bf16_ops else gelu
     x = r(x)
     h1p = x @ r(P["W1"]).T + P["b1"]
-    h1 = gelu(h1p)
+    h1 = act(h1p)
     h2p = r(h1) @ r(P["W2"]).T + P["b2"]
-    h2 = gelu(h2p)
+    h2 = act(h2p)
     o = r(h2) @ r(P["W3"]).T + P["b3"]
     out = o.copy()
     out[:, :4] += skip

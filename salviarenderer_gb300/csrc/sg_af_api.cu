@@ -17,7 +17,7 @@ namespace sg {
 cudaStream_t device_stream(sg_device* d);
 int device_sms(sg_device* d);
 void device_set_error(sg_device* d, char const* msg);
-int32_t device_sampler(sg_device* d, uint32_t handle, dev_sampler& out);
+int32_t device_af_sampler(sg_device* d, uint32_t handle, dev_sampler& out);
 uint32_t device_register_af(sg_device* d, AfModelDev const& m);
 void device_unregister_af(sg_device* d, uint32_t id);
 void launch_af_pack(AfModelDev const& M, cudaStream_t s);
@@ -114,7 +114,7 @@ int32_t upload_samplers(sg_device* d, uint32_t const* handles, uint32_t n, DevSa
   std::vector<dev_sampler> h(n);
   for (uint32_t i = 0; i < n; ++i) {
     if (!handles[i]) return SG_INVALID_PARAMETER;
-    if (int32_t r = device_sampler(d, handles[i], h[i])) return r;
+    if (int32_t r = device_af_sampler(d, handles[i], h[i])) return r;
   }
   AF_CUDA(d, out.buf.alloc(n));
   AF_CUDA(d, cudaMemcpyAsync(out.buf.p, h.data(), n * sizeof(dev_sampler), cudaMemcpyHostToDevice, device_stream(d)));

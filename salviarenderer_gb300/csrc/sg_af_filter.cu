@@ -1,21 +1,19 @@
-// sg_af_filter.cu -- the learned anisotropic filter inside a pass: the
-// lookups k_shade queued for SG_PS_TEX_GRAD_LEARNED draws are filtered here,
-// between shading and output merging.
+// sg_af_filter.cu -- the learned anisotropic filter inside a pass, between
+// shading and output merging.  k_shade's learned instances (compiled here)
+// queue each lookup of an SG_PS_TEX_GRAD_LEARNED draw either for the network
+// -- with its 24 features already formed, the four taps filtered by the
+// texture units -- or for the plain sampler.
 //
-//   k_af_filter    128 lookups per tile: each thread decides whether the
-//                  network applies to its lookup (a minified lookup of an
-//                  anisotropic sampler with more than 4 probes -- fewer cost
-//                  no more than the network's own four taps -- and at most
-//                  the draw's constants[1]) and forms its 24 features (four
-//                  bilinear taps along the major axis); the three layers run
-//                  on tcgen05.mma with the accumulators in tensor memory, and
-//                  the epilogue writes the modulated prediction into the
-//                  fragment's colour -- or, for a lookup the network does not
-//                  apply to or whose confidence is below the draw's
-//                  constants[0], queues it for the plain sampler.
+//   k_af_filter    128 queued lookups per tile: the feature rows go to shared
+//                  memory, the three layers run on tcgen05.mma with the
+//                  accumulators in tensor memory, and the epilogue writes the
+//                  modulated prediction (tap mean + network) into the
+//                  fragment's colour -- or, below the draw's confidence
+//                  threshold (constants[0]), queues the lookup for the plain
+//                  sampler.
 //   k_af_fallback  the plain anisotropic sampler (sampler::sample_2d_grad,
-//                  sampler.cpp:854-873) for the queued lookups.
-// The k_shade instances of those draws are compiled here too.
+//                  sampler.cpp:854-873) for the network's rejects and for the
+//                  lookups k_shade queued for it.
 #include <cuda_runtime.h>
 
 #include "sg_af_mma.cuh"
@@ -23,21 +21,25 @@
 
 namespace sg {
 
+// One activation tile serves both hidden layers: layer 2's MMA has read h1
+// by the time its epilogue writes h2 over it.
 struct FilterSmem {
   uint8_t w1[AF_H * AF_K1 * 2], w2[AF_H * AF_H * 2], w3[AF_N3 * AF_H * 2];
-  uint8_t x[AF_TILE * AF_K1 * 2], h1[AF_TILE * AF_H * 2], h2[AF_TILE * AF_H * 2];
+  uint8_t x[AF_TILE * AF_K1 * 2], h[AF_TILE * AF_H * 2];
   float b1[AF_H], b2[AF_H], b3[AF_N3];
   uint64_t bar;
   uint32_t tmem;
 };
-constexpr uint32_t FILTER_CTAS_PER_SM = 4;   // 4 x 128 tensor-memory columns = all 512
-constexpr uint32_t FILTER_TMEM_COLS = 128;    // layer 1 and 3 at column 0, layer 2 at 64
+constexpr uint32_t FILTER_CTAS_PER_SM = 5;  // 39 KB of shared memory each
+// Every layer's accumulator at column 0: each epilogue has read the previous
+// one (tcgen05.wait::ld) before the barrier that precedes the next MMA.
+constexpr uint32_t FILTER_TMEM_COLS = 64;
 
 __device__ inline bool unorm_format(uint32_t fmt) { return fmt == SG_FMT_RGBA8 || fmt == SG_FMT_BGRA8; }
 
 __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassParams P, AfModelDev M) {
   if (P.counters->overflow & (OVF_BIN | OVF_FRAG | OVF_REC)) return;
-  uint32_t const n = min(P.counters->af_lookups, P.af_capacity);
+  uint32_t const n = min(P.counters->af_lookups, P.af_net_capacity);
   if (blockIdx.x * AF_TILE >= n) return;  // no tile for this CTA: no tensor memory either
   extern __shared__ __align__(128) uint8_t smem_raw[];
   FilterSmem& s = *reinterpret_cast<FilterSmem*>(smem_raw);
@@ -61,37 +63,18 @@ __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassP
   for (uint32_t t0 = blockIdx.x * AF_TILE; t0 < n && ok; t0 += gridDim.x * AF_TILE) {
     uint32_t const row = t0 + tid;
     bool const valid = row < n;
-    float f[AF_F];
-    float4 r1 = make_float4(0, 0, 0, 0), mod = make_float4(0, 0, 0, 0);
-    float skip[4] = {0, 0, 0, 0};
-    uint32_t draw = 0;
-    bool take = false;
+    // the lookup's feature row (formed by k_shade) into the A tile
+    float4 skip = make_float4(0, 0, 0, 0), r1 = make_float4(0, 0, 0, 0), mod = make_float4(0, 0, 0, 0);
+    float4 const* L = P.af_net + static_cast<size_t>(row) * AF_NET_UNITS;
+    uint4 const* X = reinterpret_cast<uint4 const*>(L);
+#pragma unroll
+    for (int j = 0; j < AF_K1 / 8; ++j)
+      *reinterpret_cast<uint4*>(s.x + tile_off(tid, 8 * j, AF_K1)) = valid ? X[j] : make_uint4(0, 0, 0, 0);
     if (valid) {
-      float4 const* L = P.af_lookups + static_cast<size_t>(row) * AF_LOOKUP_UNITS;
-      float4 const r0 = L[0];
-      r1 = L[1];
-      mod = L[2];
-      draw = __float_as_uint(r1.w);
-      DrawParams const& D = P.draws[draw];
-      dev_sampler const& S = D.ps_samp;
-      if (S.mip_filter == SG_FILTER_ANISOTROPIC && S.max_anisotropy > 1) {
-        af_info af;
-        af_features(S, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, f, af);
-        take = af.lod >= 0.0f && af.probe_count > 4.0f && af.probe_count <= D.ps_k[1];
-      }
+      skip = L[4];
+      r1 = L[6];
+      mod = L[7];
     }
-    if (take) {
-#pragma unroll
-      for (int c = 0; c < 4; ++c) skip[c] = af_skip(f, c);
-    } else {
-#pragma unroll
-      for (int k = 0; k < AF_F; ++k) f[k] = 0.0f;
-    }
-    float fz[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    put8(s.x, tid, 0, AF_K1, f);
-    put8(s.x, tid, 8, AF_K1, f + 8);
-    put8(s.x, tid, 16, AF_K1, f + 16);
-    put8(s.x, tid, 24, AF_K1, fz);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -100,37 +83,32 @@ __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassP
 #pragma unroll
     for (int c = 0; c < AF_H; c += 16) {
       tmem_ld16(lane_addr(tm, c), v);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = gelu(v[i] + s.b1[c + i]);
-      put8(s.h1, tid, c, AF_H, v);
-      put8(s.h1, tid, c + 8, AF_H, v + 8);
+      gelu_row16(s.h, tid, c, AF_H, v, s.b1 + c);
     }
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
-    ok = ok && layer_mma(tm + 64, s.h1, s.w2, AF_H, AF_H, 0, &s.bar, phase);
+    ok = ok && layer_mma(tm, s.h, s.w2, AF_H, AF_H, 0, &s.bar, phase);
 #pragma unroll
     for (int c = 0; c < AF_H; c += 16) {
-      tmem_ld16(lane_addr(tm, 64 + c), v);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = gelu(v[i] + s.b2[c + i]);
-      put8(s.h2, tid, c, AF_H, v);
-      put8(s.h2, tid, c + 8, AF_H, v + 8);
+      tmem_ld16(lane_addr(tm, c), v);
+      gelu_row16(s.h, tid, c, AF_H, v, s.b2 + c);
     }
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
-    ok = ok && layer_mma(tm, s.h2, s.w3, AF_H, AF_N3, 0, &s.bar, phase);
+    ok = ok && layer_mma(tm, s.h, s.w3, AF_H, AF_N3, 0, &s.bar, phase);
     tmem_ld16(lane_addr(tm, 0), v);
-    bool fallback = valid && ok && !take;
-    if (take && ok) {
-      DrawParams const& D = P.draws[draw];
+    bool fallback = false;
+    if (valid && ok) {
+      DrawParams const& D = P.draws[__float_as_uint(r1.w)];
       float const conf = 1.0f / (1.0f + expf(-(v[4] + s.b3[4])));
       if (conf >= D.ps_k[0]) {
         float c[4];
 #pragma unroll
+        float const k4[4] = {skip.x, skip.y, skip.z, skip.w};
         for (int i = 0; i < 4; ++i) {
-          c[i] = skip[i] + (v[i] + s.b3[i]);
+          c[i] = k4[i] + (v[i] + s.b3[i]);
           if (unorm_format(D.ps_samp.fmt)) c[i] = fminf(fmaxf(c[i], 0.0f), 1.0f);
         }
         P.frag_color[__float_as_uint(r1.z)] = make_float4(c[0] * mod.x, c[1] * mod.y, c[2] * mod.z, c[3] * mod.w);
@@ -159,9 +137,13 @@ __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassP
 
 __global__ void __launch_bounds__(256) k_af_fallback(PassParams P) {
   if (P.counters->overflow & (OVF_BIN | OVF_FRAG | OVF_REC)) return;
-  uint32_t const n = P.counters->af_fallbacks;  // at most the lookups filtered, which fit the queue
+  // the network's rejects (af_fallback into af_net), then the lookups
+  // k_shade queued for the plain sampler (af_plain)
+  uint32_t const nf = P.counters->af_fallbacks;
+  uint32_t const n = nf + min(P.counters->af_plain, P.af_capacity);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 const* L = P.af_lookups + static_cast<size_t>(P.af_fallback[i]) * AF_LOOKUP_UNITS;
+    float4 const* L = i < nf ? P.af_net + static_cast<size_t>(P.af_fallback[i]) * AF_NET_UNITS + 5
+                             : P.af_plain + static_cast<size_t>(i - nf) * AF_PLAIN_UNITS;
     float4 const r0 = L[0], r1 = L[1], m = L[2];
     DrawParams const& D = P.draws[__float_as_uint(r1.w)];
     v4 const t = sample_2d_grad(D.ps_samp, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, 0.0f);
@@ -182,7 +164,7 @@ void launch_af_pass(PassParams const& P, AfModelDev const& M, uint32_t num_sms, 
 // Adds the pass's learned-filter counts to the device's profile totals.
 __global__ void k_af_count(PassParams P, unsigned long long* acc) {
   if (P.counters->overflow & (OVF_BIN | OVF_FRAG | OVF_REC)) return;
-  acc[0] += min(P.counters->af_lookups, P.af_capacity);
+  acc[0] += min(P.counters->af_lookups, P.af_net_capacity);
   acc[1] += P.counters->af_fallbacks;
 }
 void launch_af_count(PassParams const& P, unsigned long long* acc, cudaStream_t s) { k_af_count<<<1, 1, 0, s>>>(P, acc); }

@@ -10,8 +10,8 @@ namespace sg {
 
 // GELU in its tanh form (Hendrycks and Gimpel, "Gaussian Error Linear Units",
 // 2016): 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), with the hardware
-// tanh (tanh.approx.f32, about 2^-11 relative error) -- the activations are
-// rounded to BF16 (2^-9) for the next layer in any case.
+// tanh (tanh.approx).  The forward pass evaluates it in packed BF16
+// (gelu_bf16x2); the backward pass takes its derivative in FP32.
 constexpr float GELU_K0 = 0.7978845608028654f;            // sqrt(2 / pi)
 constexpr float GELU_K1 = 0.7978845608028654f * 0.044715f;
 __device__ inline float tanh_hw(float x) {
@@ -19,15 +19,42 @@ __device__ inline float tanh_hw(float x) {
   asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
-__device__ inline float gelu(float x) {
-  float const t = tanh_hw(x * (GELU_K0 + GELU_K1 * (x * x)));
-  float const h = 0.5f * x;
-  return h + h * t;
-}
 __device__ inline float gelu_grad(float x) {
   float const x2 = x * x;
   float const t = tanh_hw(x * (GELU_K0 + GELU_K1 * x2));
   return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * (GELU_K0 + 3.0f * GELU_K1 * x2);
+}
+
+// GELU of two pre-activations, evaluated in packed BF16 arithmetic (the
+// activations are BF16 operands of the next layer): returns the BF16 pair
+// as the low and high halves of a 32-bit word.
+__device__ inline uint32_t gelu_bf16x2(float a, float b) {
+  __nv_bfloat162 const x = __floats2bfloat162_rn(a, b);
+  __nv_bfloat162 const k0 = __float2bfloat162_rn(GELU_K0), k1 = __float2bfloat162_rn(GELU_K1);
+  __nv_bfloat162 const u = __hmul2(x, __hfma2(__hmul2(x, x), k1, k0));
+  uint32_t t;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(*reinterpret_cast<uint32_t const*>(&u)));
+  __nv_bfloat162 const h = __hmul2(x, __float2bfloat162_rn(0.5f));
+  __nv_bfloat162 const g = __hfma2(h, *reinterpret_cast<__nv_bfloat162 const*>(&t), h);
+  return *reinterpret_cast<uint32_t const*>(&g);
+}
+
+// GELU of 16 pre-activations v + bias into a row of a K-major tile (columns
+// k .. k + 15); `out` (optional) receives the activations as floats.
+__device__ inline void gelu_row16(uint8_t* tile, uint32_t row, uint32_t k, uint32_t K, float const* v,
+                                  float const* bias, float* out = nullptr) {
+  uint32_t w[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) w[i] = gelu_bf16x2(v[2 * i] + bias[2 * i], v[2 * i + 1] + bias[2 * i + 1]);
+  *reinterpret_cast<uint4*>(tile + tile_off(row, k, K)) = make_uint4(w[0], w[1], w[2], w[3]);
+  *reinterpret_cast<uint4*>(tile + tile_off(row, k + 8, K)) = make_uint4(w[4], w[5], w[6], w[7]);
+  if (out) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      out[2 * i] = __uint_as_float(w[i] << 16);
+      out[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
+    }
+  }
 }
 
 // Copies `bytes` (multiple of 16) from global to shared memory.

@@ -67,6 +67,10 @@ struct Level {
 struct Texture {
   uint32_t samples = 1, fmt = 0, esz = 0;
   std::vector<Level> levels;
+  // the learned filter's texture-unit copies of the levels (made on first
+  // use, refreshed by every pass that samples them, dropped with the levels)
+  std::vector<cudaArray_t> af_arrays;
+  uint32_t af_gen = 0;
 };
 struct Buffer {
   uint8_t* ptr = nullptr;
@@ -75,6 +79,8 @@ struct Buffer {
 struct Sampler {
   sg_sampler_desc desc{};
   uint32_t texture = 0;
+  std::vector<cudaTextureObject_t> af_objs;  // one per level of the texture's af_arrays
+  uint32_t af_gen = 0xFFFFFFFFu;              // the arrays' generation the objects were made for
 };
 
 // Grow-only device arena.
@@ -137,14 +143,15 @@ uint8_t* static_scratch_address(int ordinal) {
 // every recorded graph owns its own.
 struct Scratch {
   Arena params, slot_rec, recs, bin_counts, scan_sums, bin_entries, tile_begin, frag_rec, frag_pos, frag_mask,
-      frag_color, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, sticky, af_lookups, af_fallback;
+      frag_color, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, sticky, af_net, af_plain,
+      af_fallback;
   bool pending = false;                // passes ran since the host last read `sticky`
   uint32_t entry_capacity = 1u << 24;  // bin entries (grows after an overflow)
   uint32_t chunk_capacity = 1u << 18;  // fragment chunks (grows after an overflow)
   void release() {
     for (Arena* a : {&params, &slot_rec, &recs, &bin_counts, &scan_sums, &bin_entries, &tile_begin, &frag_rec,
                      &frag_pos, &frag_mask, &frag_color, &frag_ps, &chunk_next, &chunk_count, &owner_first,
-                     &counters, &stats, &sticky, &af_lookups, &af_fallback})
+                     &counters, &stats, &sticky, &af_net, &af_plain, &af_fallback})
       a->release();
   }
 };
@@ -165,6 +172,7 @@ struct PassPlan {
   std::set<uint32_t> cleared;                // textures its queued clears write
   std::vector<uint8_t> late_z;               // per target: a draw tests depth after shading
   std::vector<uint32_t> target_color, target_ds;
+  std::set<uint32_t> af_textures;            // textures its learned-filter draws take feature taps from
   uint64_t nprims = 0;
   uint64_t samples = 0;                      // target samples of the pass's targets
   uint32_t af_model = 0;                     // the learned filter its draws use (one per pass), 0 = none
@@ -313,6 +321,100 @@ int32_t build_sampler(sg_device* d, uint32_t handle, dev_sampler& out, uint32_t*
   return SG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// texture-unit copies for the learned filter's feature taps
+
+// The channel layout of a four-channel format the texture units filter.
+bool af_channel(uint32_t fmt, cudaChannelFormatDesc& c, cudaTextureReadMode& mode) {
+  mode = cudaReadModeElementType;
+  switch (fmt) {
+  case SG_FMT_RGBA8:
+  case SG_FMT_BGRA8:
+    c = cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsigned);
+    mode = cudaReadModeNormalizedFloat;
+    return true;
+  case SG_FMT_RGBA32F: c = cudaCreateChannelDesc(32, 32, 32, 32, cudaChannelFormatKindFloat); return true;
+  case SG_FMT_RGBA16F: c = cudaCreateChannelDescHalf4(); return true;
+  default: return false;
+  }
+}
+void af_release_objects(Sampler& s) {
+  for (cudaTextureObject_t o : s.af_objs)
+    if (o) cudaDestroyTextureObject(o);
+  s.af_objs.clear();
+  s.af_gen = 0xFFFFFFFFu;
+}
+// Drops a texture's copies (its samplers remake their objects on next use).
+void af_release_arrays(Texture& t) {
+  for (cudaArray_t a : t.af_arrays)
+    if (a) cudaFreeArray(a);
+  t.af_arrays.clear();
+  ++t.af_gen;
+}
+cudaTextureAddressMode af_address(uint32_t m) {
+  switch (m) {
+  case SG_ADDRESS_MIRROR: return cudaAddressModeMirror;
+  case SG_ADDRESS_CLAMP: return cudaAddressModeClamp;
+  case SG_ADDRESS_BORDER: return cudaAddressModeBorder;
+  default: return cudaAddressModeWrap;
+  }
+}
+// Makes the texture-unit copies of a sampler's texture and the sampler's
+// texture objects (one per level) and records them in `ds`; formats the
+// texture units do not filter as four channels get none.  The copies' data
+// is written by af_refresh.
+int32_t af_prepare(sg_device* d, uint32_t handle, dev_sampler& ds) {
+  for (auto& o : ds.af_tex) o = 0;
+  auto it = d->samplers.find(handle);
+  if (it == d->samplers.end()) return SG_INVALID_PARAMETER;
+  Sampler& smp = it->second;
+  Texture* t = find_tex(d, smp.texture);
+  cudaChannelFormatDesc ch;
+  cudaTextureReadMode mode;
+  if (!t || t->samples != 1 || !af_channel(t->fmt, ch, mode)) return SG_OK;
+  if (t->af_arrays.size() != t->levels.size()) {
+    af_release_arrays(*t);
+    for (Level const& l : t->levels) {
+      cudaArray_t a = nullptr;
+      SG_CUDA(d, cudaMallocArray(&a, &ch, l.w, l.h));
+      t->af_arrays.push_back(a);
+    }
+  }
+  if (smp.af_gen != t->af_gen) {
+    af_release_objects(smp);
+    for (cudaArray_t a : t->af_arrays) {
+      cudaResourceDesc rd{};
+      rd.resType = cudaResourceTypeArray;
+      rd.res.array.array = a;
+      cudaTextureDesc td{};
+      td.addressMode[0] = af_address(smp.desc.address_u);
+      td.addressMode[1] = af_address(smp.desc.address_v);
+      td.filterMode = cudaFilterModeLinear;
+      td.readMode = mode;
+      td.normalizedCoords = 1;
+      for (int i = 0; i < 4; ++i) td.borderColor[i] = smp.desc.border_color[i];
+      cudaTextureObject_t o = 0;
+      SG_CUDA(d, cudaCreateTextureObject(&o, &rd, &td, nullptr));
+      smp.af_objs.push_back(o);
+    }
+    smp.af_gen = t->af_gen;
+  }
+  for (size_t i = 0; i < smp.af_objs.size() && i < static_cast<size_t>(SG_MAX_LEVELS); ++i) ds.af_tex[i] = smp.af_objs[i];
+  return SG_OK;
+}
+// Copies a texture's levels into its texture-unit copies, stream-ordered.
+int32_t af_refresh(sg_device* d, uint32_t tex) {
+  Texture* t = find_tex(d, tex);
+  if (!t || t->af_arrays.size() != t->levels.size()) return SG_OK;
+  for (size_t i = 0; i < t->levels.size(); ++i) {
+    Level const& l = t->levels[i];
+    size_t const row = static_cast<size_t>(l.w) * t->esz;
+    SG_CUDA(d, cudaMemcpy2DToArrayAsync(t->af_arrays[i], 0, 0, l.ptr, row, row, l.h, cudaMemcpyDeviceToDevice,
+                                        d->stream));
+  }
+  return SG_OK;
+}
+
 bool valid_color_fmt(uint32_t f) {
   return f == SG_FMT_RGBA32F || f == SG_FMT_RGB32F || f == SG_FMT_BGRA8 || f == SG_FMT_RGBA8 || f == SG_FMT_R32F ||
          f == SG_FMT_RG32F || f == SG_FMT_R32I || f == SG_FMT_RGBA16F;
@@ -349,6 +451,7 @@ struct DrawInfo {
   uint32_t color = 0, ds = 0;       // target textures
   uint32_t tex[2] = {0, 0};         // sampled textures
   uint32_t af_model = 0;            // learned filter of an SG_PS_TEX_GRAD_LEARNED draw
+  uint32_t af_texture = 0;          // the texture its feature taps read
 };
 
 int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, DrawInfo& info) {
@@ -422,6 +525,8 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   if (p.ps_prog == SG_PS_TEX_GRAD_LEARNED) {
     if (!d->af_models.count(desc->ps.learned_filter)) return SG_INVALID_PARAMETER;
     info.af_model = desc->ps.learned_filter;
+    info.af_texture = info.tex[1];
+    if (int32_t r = af_prepare(d, desc->ps.samplers[0], p.ps_samp)) return r;
   }
   uint32_t const nattr = desc->num_varyings;
   p.nattr = nattr;
@@ -554,6 +659,7 @@ void add_draw(sg_device* d, PassPlan& pl, DrawParams p, DrawInfo const& info, ui
   if (info.af_model) {
     pl.af_model = info.af_model;
     pl.af = d->af_models.at(info.af_model);
+    pl.af_textures.insert(info.af_texture);
   }
   p.prim_base = static_cast<uint32_t>(pl.nprims);
   pl.nprims += p.prim_count;
@@ -696,16 +802,21 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.chunk_next.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.chunk_count.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.owner_first.ensure(static_cast<size_t>(pl.ntiles) * RASTER_THREADS * 4));
-  // learned-filter lookups: room for every pixel the fragment buffer holds
-  // (fragment pixel indices must fit 32 bits; past 2^30 pixels the pass's
-  // learned-filter draws run on the plain sampler)
+  // learned-filter lookups: the plain queue has room for every pixel the
+  // fragment buffer holds (fragment pixel indices must fit 32 bits; past
+  // 2^30 pixels the pass's learned-filter draws run on the plain shading
+  // instances), the network's for 2^22 lookups at most (more go plain)
   P.af_capacity = 0;
   if (pl.af_model && nfrag * 4 <= (1ull << 30)) {
     uint32_t const cap = static_cast<uint32_t>(nfrag * 4);
-    SG_CUDA(d, sc.af_lookups.ensure(static_cast<size_t>(cap) * AF_LOOKUP_UNITS * sizeof(float4)));
-    SG_CUDA(d, sc.af_fallback.ensure(static_cast<size_t>(cap) * 4));
-    P.af_lookups = static_cast<float4*>(sc.af_lookups.ptr);
+    uint32_t const net = std::min<uint32_t>(cap, 1u << 22);
+    SG_CUDA(d, sc.af_plain.ensure(static_cast<size_t>(cap) * AF_PLAIN_UNITS * sizeof(float4)));
+    SG_CUDA(d, sc.af_net.ensure(static_cast<size_t>(net) * AF_NET_UNITS * sizeof(float4)));
+    SG_CUDA(d, sc.af_fallback.ensure(static_cast<size_t>(net) * 4));
+    P.af_plain = static_cast<float4*>(sc.af_plain.ptr);
+    P.af_net = static_cast<float4*>(sc.af_net.ptr);
     P.af_fallback = static_cast<uint32_t*>(sc.af_fallback.ptr);
+    P.af_net_capacity = net;
     P.af_capacity = cap;
   }
   v.params = static_cast<uint8_t*>(sc.params.ptr);
@@ -800,6 +911,9 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
                                            static_cast<uint32_t>(d->num_sms), s);
   if (!pl.draws.empty()) {
     if (packed) SG_CUDA(d, cudaMemcpyAsync(v.params, packed->data(), packed->size(), cudaMemcpyHostToDevice, s));
+    if (P.af_capacity)  // the texture-unit copies the filter's feature taps read, current as of this pass
+      for (uint32_t t : pl.af_textures)
+        if (int32_t r = af_refresh(d, t)) return r;
     SG_CUDA(d, cudaMemsetAsync(P.counters, 0, sizeof(PassCounters), s));
     SG_CUDA(d, cudaMemsetAsync(P.draw_stats, 0, pl.draws.size() * sizeof(DrawStatsDev), s));
     if (pl.nprims > 0 && pl.ntiles > 0) {
@@ -825,8 +939,12 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
         launch_cover(P, pl.max_samples, pl.any_early_z, cover_grid, s);
       stage_end(d, 2, ev);
       ev = stage_begin(d, profile);
-      for (uint32_t cls = 0; cls < 16; ++cls) {  // shade classes: varyings, plus 8 for learned-filter draws
-        if (!(pl.na_mask & (1u << cls))) continue;
+      // shade classes: varyings, plus 8 for learned-filter draws (which the
+      // plain instances shade when the pass has no lookup queue)
+      uint32_t classes = pl.na_mask;
+      if (!P.af_capacity) classes = (classes & 0xFFu) | (classes >> 8);
+      for (uint32_t cls = 0; cls < 16; ++cls) {
+        if (!(classes & (1u << cls))) continue;
         switch (cls) {
         case 0: launch_shade_0(P, shade_grid, s); break;
         case 1: launch_shade_1(P, shade_grid, s); break;
@@ -1186,9 +1304,12 @@ void sg_device_destroy(sg_device* d) {
   cudaSetDevice(d->ordinal);
   cudaStreamSynchronize(d->stream);
   for (sg_graph* g : std::vector<sg_graph*>(d->graphs.begin(), d->graphs.end())) sg_graph_destroy(d, g);
+  for (auto& sm : d->samplers) af_release_objects(sm.second);
   for (auto& b : d->buffers) cudaFree(b.second.ptr);
-  for (auto& t : d->textures)
+  for (auto& t : d->textures) {
+    af_release_arrays(t.second);
     for (auto& l : t.second.levels) cudaFree(l.ptr);
+  }
   d->scratch.release();
   cudaFreeHost(d->counters_host);
   cudaFreeHost(d->sticky_host);
@@ -1327,6 +1448,7 @@ int32_t sg_texture_gen_mipmap(sg_device* d, uint32_t h, uint32_t filter) {
   }
   if (n > static_cast<uint32_t>(SG_MAX_LEVELS)) return SG_INVALID_PARAMETER;
   SG_CUDA(d, cudaStreamSynchronize(d->stream));
+  af_release_arrays(*t);
   for (size_t i = 1; i < t->levels.size(); ++i) cudaFree(t->levels[i].ptr);
   t->levels.resize(1);
   for (uint32_t i = 1; i < n; ++i) {
@@ -1357,6 +1479,7 @@ int32_t sg_texture_destroy(sg_device* d, uint32_t h) {
   Texture* t = d ? find_tex(d, h) : nullptr;
   if (!t) return SG_INVALID_PARAMETER;
   cudaStreamSynchronize(d->stream);
+  af_release_arrays(*t);
   for (auto& l : t->levels) cudaFree(l.ptr);
   d->textures.erase(h);
   return SG_OK;
@@ -1372,7 +1495,12 @@ int32_t sg_sampler_create(sg_device* d, const sg_sampler_desc* desc, uint32_t te
   return SG_OK;
 }
 int32_t sg_sampler_destroy(sg_device* d, uint32_t h) {
-  if (!d || !d->samplers.erase(h)) return SG_INVALID_PARAMETER;
+  if (!d) return SG_INVALID_PARAMETER;
+  auto it = d->samplers.find(h);
+  if (it == d->samplers.end()) return SG_INVALID_PARAMETER;
+  cudaStreamSynchronize(d->stream);
+  af_release_objects(it->second);
+  d->samplers.erase(it);
   return SG_OK;
 }
 
@@ -1650,6 +1778,14 @@ void device_set_error(sg_device* d, char const* msg) { d->error = msg; }
 int32_t device_sampler(sg_device* d, uint32_t handle, dev_sampler& out) {
   uint32_t tex = 0;
   return build_sampler(d, handle, out, &tex);
+}
+// The sampler as the learned filter's sample generator reads it: with its
+// texture-unit copies, refreshed on the device's stream.
+int32_t device_af_sampler(sg_device* d, uint32_t handle, dev_sampler& out) {
+  uint32_t tex = 0;
+  if (int32_t r = build_sampler(d, handle, out, &tex)) return r;
+  if (int32_t r = af_prepare(d, handle, out)) return r;
+  return af_refresh(d, tex);
 }
 uint32_t device_register_af(sg_device* d, AfModelDev const& m) {
   uint32_t const id = d->next++;

@@ -263,6 +263,9 @@ struct dev_sampler {
   float border[4];
   uint32_t width, height;  // texture size (level 0)
   dev_level lv[SG_MAX_LEVELS];
+  // texture-unit copies of the levels (bilinear, the sampler's addressing),
+  // for the learned filter's feature taps; 0 where the format has none
+  unsigned long long af_tex[SG_MAX_LEVELS];
 };
 
 // EWA weight table (sampler.cpp:636-678), uploaded at device creation by the

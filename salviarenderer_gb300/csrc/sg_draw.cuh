@@ -35,9 +35,9 @@ struct PassCounters {
   unsigned int fetch_oob;            // vertex or index reads outside their buffers
   unsigned int chunk_total;          // fragment chunks allocated by the coverage pass
   unsigned int merge_cursor;         // dynamic tile scheduler of the merge pass
-  unsigned int af_lookups;           // lookups queued for the learned filter
+  unsigned int af_lookups;           // lookups queued for the learned filter's network
   unsigned int af_fallbacks;         // of those, lookups sent back to the plain sampler
-  unsigned int pad;
+  unsigned int af_plain;             // lookups of learned-filter draws queued for the plain sampler
 };
 
 // Per-draw pipeline counters (async_object.h:90-175).
@@ -152,17 +152,26 @@ struct PassParams {
   // coverage work items: 16 or 32 pixels on a side; 32x32 items of a tile with
   // more than split_entries bin entries become 16x16
   uint32_t cover_item, split_entries;
-  // learned anisotropic filter: k_shade queues the lookups it applies to
-  // (AF_LOOKUP_UNITS float4 each) for k_af_filter, which sends the ones it
-  // is not confident about to k_af_fallback through af_fallback
-  float4* af_lookups;
+  // learned anisotropic filter: k_shade queues the lookups of learned-filter
+  // draws, those the network takes in af_net (with their features, for
+  // k_af_filter), the others in af_plain (for k_af_fallback); k_af_filter
+  // sends the ones it is not confident about to k_af_fallback through
+  // af_fallback (indices into af_net)
+  float4* af_net;
+  float4* af_plain;
   uint32_t* af_fallback;
-  uint32_t af_capacity;         // lookups; 0 runs every lookup on the plain sampler
+  uint32_t af_net_capacity;     // records of af_net (and entries of af_fallback)
+  uint32_t af_capacity;         // records of af_plain: every pixel of the pass; 0 = no queues, the plain
+                                // shading instances take the learned-filter draws
 };
 
-// A queued learned-filter lookup: (u, v, ddx.u, ddx.v), (ddy.u, ddy.v,
+// A lookup for the plain sampler: (u, v, ddx.u, ddx.v), (ddy.u, ddy.v,
 // fragment pixel index bits, draw index bits), the colour it modulates.
-constexpr uint32_t AF_LOOKUP_UNITS = 3;
+constexpr uint32_t AF_PLAIN_UNITS = 3;
+// A lookup for the network: its feature row as the tensor cores read it
+// (32 BF16, 24 features and 8 zeros), the tap mean the prediction adds, then
+// the three units of the plain record (for a fallback).
+constexpr uint32_t AF_NET_UNITS = 8;
 
 // triangle record layout (float4 units): [0..2] edge factors (x, y, z) with
 // v0's projected x, y, z in .w, [3] bbox, [4] (ddx.z, ddy.z of the position,

@@ -85,10 +85,7 @@ __global__ void __launch_bounds__(AF_TILE, 1) k_af_infer(AfModelDev M, uint16_t 
 #pragma unroll
     for (int c = 0; c < AF_H; c += 16) {
       tmem_ld16(lane_addr(tm, c), v);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = gelu(v[i] + s.b1[c + i]);
-      put8(s.h1, tid, c, AF_H, v);
-      put8(s.h1, tid, c + 8, AF_H, v + 8);
+      gelu_row16(s.h1, tid, c, AF_H, v, s.b1 + c);
     }
     fence_async_smem();
     tc_fence_before();
@@ -97,10 +94,7 @@ __global__ void __launch_bounds__(AF_TILE, 1) k_af_infer(AfModelDev M, uint16_t 
 #pragma unroll
     for (int c = 0; c < AF_H; c += 16) {
       tmem_ld16(lane_addr(tm, 64 + c), v);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = gelu(v[i] + s.b2[c + i]);
-      put8(s.h2, tid, c, AF_H, v);
-      put8(s.h2, tid, c + 8, AF_H, v + 8);
+      gelu_row16(s.h2, tid, c, AF_H, v, s.b2 + c);
     }
     fence_async_smem();
     tc_fence_before();
@@ -216,13 +210,9 @@ __global__ void __launch_bounds__(AF_TILE, 1) k_af_train(AfModelDev M, uint16_t 
 #pragma unroll
     for (int c = 0; c < AF_H; c += 16) {
       tmem_ld16(lane_addr(tm, TM_D1 + c), v);
+      gelu_row16(s.h1, tid, c, AF_H, v, s.b1 + c, v);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        v[i] = gelu(v[i] + s.b1[c + i]);
-        put_t(s.a1, c + i, tid, v[i]);
-      }
-      put8(s.h1, tid, c, AF_H, v);
-      put8(s.h1, tid, c + 8, AF_H, v + 8);
+      for (int i = 0; i < 16; ++i) put_t(s.a1, c + i, tid, v[i]);
     }
     fence_async_smem();
     tc_fence_before();
@@ -231,13 +221,9 @@ __global__ void __launch_bounds__(AF_TILE, 1) k_af_train(AfModelDev M, uint16_t 
 #pragma unroll
     for (int c = 0; c < AF_H; c += 16) {
       tmem_ld16(lane_addr(tm, TM_D2 + c), v);
+      gelu_row16(s.h2, tid, c, AF_H, v, s.b2 + c, v);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        v[i] = gelu(v[i] + s.b2[c + i]);
-        put_t(s.a1, 64 + c + i, tid, v[i]);
-      }
-      put8(s.h2, tid, c, AF_H, v);
-      put8(s.h2, tid, c + 8, AF_H, v + 8);
+      for (int i = 0; i < 16; ++i) put_t(s.a1, 64 + c + i, tid, v[i]);
     }
     fence_async_smem();
     tc_fence_before();

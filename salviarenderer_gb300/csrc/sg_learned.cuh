@@ -39,10 +39,11 @@ constexpr int AF_IMG_W1 = 0, AF_IMG_W2 = AF_IMG_W1 + AF_H * AF_K1 * 2, AF_IMG_W3
 //   6     probe count / 16
 //   7     log2 of the anisotropy ratio (long / minor) / 4
 //   8-23  RGBA of four bilinear taps at the probes' level, along the major
-//         axis at -3/8, -1/8, 1/8, 3/8 of the probe span
-__device__ inline void af_features(dev_sampler const& s, float u, float v, float dxu, float dxv, float dyu, float dyv,
-                                   float* f, af_info& af) {
-  calc_af(s, dxu, dxv, dyu, dyv, 0.0f, af);
+//         axis at -3/8, -1/8, 1/8, 3/8 of the probe span, filtered by the
+//         texture units where the format allows (dev_sampler::af_tex)
+// With the anisotropy measures `af` already computed (calc_af, bias 0).
+__device__ inline void af_features_from(dev_sampler const& s, float u, float v, float dxu, float dxv, float dyu,
+                                        float dyv, af_info const& af, float* f) {
   float const fw = static_cast<float>(s.width), fh = static_cast<float>(s.height);
   float const tx0 = dxu * fw, tx1 = dxv * fh, ty0 = dyu * fw, ty1 = dyv * fh;
   float const lx = sqrtf(tx0 * tx0 + tx1 * tx1), ly = sqrtf(ty0 * ty0 + ty1 * ty1);
@@ -61,15 +62,29 @@ __device__ inline void af_features(dev_sampler const& s, float u, float v, float
   int const min_lod = s.nlevels - 1;
   int const lvl = lo < 0 ? 0 : (lo > min_lod ? min_lod : lo);
   float const span = fmaxf(af.probe_count - 1.0f, 0.0f);
+  unsigned long long const obj = s.af_tex[lvl];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     float const t = (static_cast<float>(k) - 1.5f) * 0.25f * span;
-    v4 const c = sample_surface(s, lvl, u + af.du * t, v + af.dv * t, SG_FILTER_LINEAR);
+    float const tu = u + af.du * t, tv = v + af.dv * t;
+    float4 c;
+    if (obj) {  // the texture units' bilinear filter (features need not match the sampler bit for bit)
+      c = tex2D<float4>(obj, tu, tv);
+      if (s.fmt == SG_FMT_BGRA8) c = make_float4(c.z, c.y, c.x, c.w);
+    } else {
+      v4 const p = sample_surface(s, lvl, tu, tv, SG_FILTER_LINEAR);
+      c = make_float4(p.x, p.y, p.z, p.w);
+    }
     f[8 + 4 * k] = c.x;
     f[9 + 4 * k] = c.y;
     f[10 + 4 * k] = c.z;
     f[11 + 4 * k] = c.w;
   }
+}
+__device__ inline void af_features(dev_sampler const& s, float u, float v, float dxu, float dxv, float dyu, float dyv,
+                                   float* f, af_info& af) {
+  calc_af(s, dxu, dxv, dyu, dyv, 0.0f, af);
+  af_features_from(s, u, v, dxu, dxv, dyu, dyv, af, f);
 }
 
 // The filter's prediction is this mean of the four taps plus the network's

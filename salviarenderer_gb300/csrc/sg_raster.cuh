@@ -17,9 +17,11 @@
 // two varying counts each so the translation units compile in parallel.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "sg_draw.cuh"
+#include "sg_learned.cuh"
 
 namespace sg {
 
@@ -636,6 +638,17 @@ __device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q) {
 }
 
 
+// Whether the learned filter takes an SG_PS_TEX_GRAD_LEARNED lookup: a
+// minified lookup of an anisotropic sampler whose probe count is above
+// max(4, constants[2]) -- below that the plain sampler costs no more than the
+// network -- and at most constants[1].
+__device__ inline bool af_takes(DrawParams const& D, float dxu, float dxv, float dyu, float dyv, af_info& af) {
+  dev_sampler const& s = D.ps_samp;
+  if (s.mip_filter != SG_FILTER_ANISOTROPIC || s.max_anisotropy <= 1) return false;
+  calc_af(s, dxu, dxv, dyu, dyv, 0.0f, af);
+  return af.lod >= 0.0f && af.probe_count > fmaxf(4.0f, D.ps_k[2]) && af.probe_count <= D.ps_k[1];
+}
+
 // Attribute interpolation (step_2d_unproj_attr_n_quad / step_2d_unproj_attr_n
 // with the centroid adjustment, shader.cpp:208-367, rasterizer.cpp:1363-1398)
 // and the pixel shader, for every fragment of the pass whose draw has NA
@@ -649,23 +662,22 @@ __global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
   uint32_t const groups = gridDim.x * (blockDim.x >> 2);
   uint32_t const start = blockIdx.x * (blockDim.x >> 2) + (threadIdx.x >> 2);
   uint32_t const rounds = (nfrag + groups - 1) / groups;
+  // learned instances: each thread's network record (feature row and tap
+  // mean) waits here, unit-major, until the warp has its queue slots
+  __shared__ uint4 s_net[LEARNED ? 5 * 256 : 1];
   for (uint32_t it = 0; it < rounds; ++it) {
     uint32_t f = start + it * groups;
     bool live = f < nfrag && (f % FRAG_CHUNK) < P.chunk_count[f / FRAG_CHUNK];
     uint32_t pos = live ? P.frag_pos[f] : 0u;
-    live = live && ((pos >> 25) & 15u) == static_cast<uint32_t>(NA + (LEARNED ? 8 : 0));
+    // shade class: NA varyings, plus 8 for learned-filter draws; without a
+    // lookup queue the plain instances shade those draws too
+    uint32_t const cls = (pos >> 25) & 15u;
+    live = live && (LEARNED ? cls == NA + 8u : (cls == NA || (!P.af_capacity && cls == NA + 8u)));
     uint32_t draw = 0xFFFFFFFFu;
-    // learned-filter draws queue every pixel: reserve the warp's queue slots
-    uint32_t af_idx = 0;
-    if (LEARNED && P.af_capacity) {
-      unsigned const want = __ballot_sync(0xFFFFFFFFu, live);
-      if (want) {
-        int const lane = threadIdx.x & 31, leader = __ffs(want) - 1;
-        uint32_t first = 0;
-        if (lane == leader) first = atomicAdd(&P.counters->af_lookups, static_cast<unsigned>(__popc(want)));
-        af_idx = __shfl_sync(0xFFFFFFFFu, first, leader) + __popc(want & ((1u << lane) - 1u));
-      }
-    }
+    // learned instances: the pixel's lookup, for the network's queue (af_net)
+    // or for the plain sampler's (af_plain)
+    bool af_net = false, af_plain = false;
+    float4 af_r0, af_r1, af_r2;
     if (live) {
       uint32_t rec = P.frag_rec[f], masks = P.frag_mask[f];
       TriView t{P.recs + rec, 1 + NA};
@@ -722,27 +734,83 @@ __global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
         }
         attr[i] = (D.mods[i] & SG_AM_NOPERSPECTIVE) ? a : a * invw;
       }
-      if (LEARNED && P.af_capacity) {
-        // the lookup, with the quad's derivatives as run_ps takes them, for
-        // the filter pass (which runs the network or the plain sampler)
+      if constexpr (LEARNED) {
+        // the lookup, with the quad's derivatives as run_ps takes them (the
+        // same for its four lanes, so a quad goes to one queue whole)
         int const base = (threadIdx.x & 31) & ~3;
         unsigned const qm = 0xFu << base;
         v4 const a0 = attr[0];
         float const u0 = __shfl_sync(qm, a0.x, base), v0 = __shfl_sync(qm, a0.y, base);
         float const u1 = __shfl_sync(qm, a0.x, base + 1), v1 = __shfl_sync(qm, a0.y, base + 1);
         float const u2 = __shfl_sync(qm, a0.x, base + 2), v2 = __shfl_sync(qm, a0.y, base + 2);
-        v4 const m = NA > 1 ? attr[NA > 1 ? 1 : 0] : mk4(0, 0, 0, 0);
-        if (af_idx < P.af_capacity) {  // always: the queue holds every pixel of the pass
-          float4* r = P.af_lookups + static_cast<size_t>(af_idx) * AF_LOOKUP_UNITS;
-          r[0] = make_float4(a0.x, a0.y, u1 - u0, v1 - v0);
-          r[1] = make_float4(u2 - u0, v2 - v0, __uint_as_float(f * 4 + q), __uint_as_float(draw));
-          r[2] = make_float4(m.x, m.y, m.z, m.w);
+        af_info af;
+        af_net = af_takes(D, u1 - u0, v1 - v0, u2 - u0, v2 - v0, af);
+        af_plain = !af_net;
+        if (af_net) {  // the network's features: taps by the texture units, BF16 for the tensor cores
+          float fe[AF_F];
+          af_features_from(D.ps_samp, a0.x, a0.y, u1 - u0, v1 - v0, u2 - u0, v2 - v0, af, fe);
+          uint32_t w[16];
+#pragma unroll
+          for (int i = 0; i < 12; ++i)
+            w[i] = static_cast<uint32_t>(__bfloat16_as_ushort(__float2bfloat16_rn(fe[2 * i]))) |
+                   (static_cast<uint32_t>(__bfloat16_as_ushort(__float2bfloat16_rn(fe[2 * i + 1]))) << 16);
+#pragma unroll
+          for (int i = 12; i < 16; ++i) w[i] = 0u;
+          if constexpr (LEARNED) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              s_net[i * 256 + threadIdx.x] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
+            s_net[4 * 256 + threadIdx.x] = make_uint4(__float_as_uint(af_skip(fe, 0)), __float_as_uint(af_skip(fe, 1)),
+                                                      __float_as_uint(af_skip(fe, 2)), __float_as_uint(af_skip(fe, 3)));
+          }
         }
+        af_r0 = make_float4(a0.x, a0.y, u1 - u0, v1 - v0);
+        af_r1 = make_float4(u2 - u0, v2 - v0, __uint_as_float(f * 4 + q), __uint_as_float(draw));
+        v4 const m = NA > 1 ? attr[NA > 1 ? 1 : 0] : mk4(0, 0, 0, 0);
+        af_r2 = make_float4(m.x, m.y, m.z, m.w);
       } else {
         v4 out = run_ps<NA>(D, attr, q);  // all four lanes of a quad take the same path
         P.frag_color[static_cast<size_t>(f) * 4 + q] = make_float4(out.x, out.y, out.z, out.w);
       }
       if (q == 0) P.frag_ps[f] = 0xF;  // the stock programs never discard
+    }
+    if constexpr (LEARNED) {
+      // queue the lookups, one atomic per warp and queue; lookups past the
+      // network queue's end go to the plain queue, which holds every pixel
+      int const lane = threadIdx.x & 31;
+      unsigned const want_net = __ballot_sync(0xFFFFFFFFu, af_net);
+      if (want_net) {
+        int const leader = __ffs(want_net) - 1;
+        uint32_t first = 0;
+        if (lane == leader) first = atomicAdd(&P.counters->af_lookups, static_cast<unsigned>(__popc(want_net)));
+        uint32_t const k = __shfl_sync(0xFFFFFFFFu, first, leader) + __popc(want_net & ((1u << lane) - 1u));
+        if (af_net) {
+          if (k < P.af_net_capacity) {
+            uint4* x = reinterpret_cast<uint4*>(P.af_net + static_cast<size_t>(k) * AF_NET_UNITS);
+#pragma unroll
+            for (int i = 0; i < 5; ++i) x[i] = s_net[i * 256 + threadIdx.x];
+            float4* r = P.af_net + static_cast<size_t>(k) * AF_NET_UNITS + 4;
+            r[1] = af_r0;
+            r[2] = af_r1;
+            r[3] = af_r2;
+          } else {
+            af_plain = true;
+          }
+        }
+      }
+      unsigned const want_plain = __ballot_sync(0xFFFFFFFFu, af_plain);
+      if (want_plain) {
+        int const leader = __ffs(want_plain) - 1;
+        uint32_t first = 0;
+        if (lane == leader) first = atomicAdd(&P.counters->af_plain, static_cast<unsigned>(__popc(want_plain)));
+        uint32_t const k = __shfl_sync(0xFFFFFFFFu, first, leader) + __popc(want_plain & ((1u << lane) - 1u));
+        if (af_plain && k < P.af_capacity) {  // always below
+          float4* r = P.af_plain + static_cast<size_t>(k) * AF_PLAIN_UNITS;
+          r[0] = af_r0;
+          r[1] = af_r1;
+          r[2] = af_r2;
+        }
+      }
     }
     // ps_invocations: 4 per quad, counted per draw (one lane per quad)
     uint32_t key = q == 0 ? draw : 0xFFFFFFFFu;

@@ -90,8 +90,8 @@ def test_training_beats_tap_average(gdev):
     from salviarenderer_gb300.device import AfModel
     tex = scenes.AfTextures(gdev, scenes.af_training_images(size=256))
     m = AfModel(gdev, seed=3)
-    rep = m.train(tex.samplers, samples=1 << 19, batch=4096, epochs=4, lr=3e-3, seed=5)
-    assert rep["steps"] == 512
+    rep = m.train(tex.samplers, samples=1 << 20, batch=8192, epochs=8, lr=2e-3, seed=5)
+    assert rep["steps"] == 1024
     assert rep["last_loss"] < rep["first_loss"], rep
     f, y = gdev.af_sample(tex.samplers, 1 << 16, seed=99)
     assert np.all(np.isfinite(f)) and np.all((y >= 0) & (y <= 1))
