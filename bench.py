@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-uneven", action="store_true", help="skip the 256-frame batched-draw leg")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-filter leg")
     ap.add_argument("--size", default="1920x1080",
                     help="render-target size; smaller sizes are for profiling captures only")
     return ap.parse_args()
@@ -280,6 +281,82 @@ def measure_uneven(dev, stream, flush, args):
             "graph_kernels": info["kernels"], "steps": steps}
 
 
+AF_MLP_FLOPS = 2 * (32 * 64 + 64 * 64 + 64 * 16)  # per lookup, as the tensor cores run the padded layers
+AF_TRAIN_FLOPS = AF_MLP_FLOPS + 2 * (16 * 64 + 64 * 64) + 2 * 128 * (80 + 64 + 80)  # fwd + bwd + weight grads
+
+
+def measure_learned(dev, stream, flush, args, width, height):
+    """The learned anisotropic filter: trained on the device from the plain
+    16x sampler over 4096 procedural 512^2 textures (20M samples), then the
+    1080p frame rendered with its anisotropic draws on the learned filter
+    against the plain sampler: frames/s (recorded graphs), PSNR and largest
+    error of the resolved image, and the anisotropic pixels' shading
+    throughput on the same frame with every draw anisotropic."""
+    import numpy as np
+    from salviarenderer_gb300 import abi, scenes
+    from salviarenderer_gb300.device import AfModel
+    t0 = time.perf_counter()
+    train = scenes.AfTextures(dev, count=4096, size=512, seed=SEED)
+    dev.sync()
+    make_s = time.perf_counter() - t0
+    model = AfModel(dev, seed=SEED)
+    rep = model.train(train.samplers, samples=20_000_000, batch=8192, epochs=2, lr=2e-3, seed=SEED)
+    learned = (0.5, 16.0, 0.0)  # confidence threshold, probe range (0, 16]
+    steps = max(1, min(args.steps, 10))
+
+    def frame(stride, lrn):
+        b = scenes.Bound(dev, scenes.c2_scene(seed=SEED, width=width, height=height, learned=lrn,
+                                              af_stride=stride), model if lrn else None)
+        cl = b.commands()
+        st = [x for x, c in zip(dev.submit(cl, stats=True), cl._cmds) if c.type == abi.CMD_DRAW]
+        img = b.outputs()["resolved"]
+        g = dev.graph_create(cl)
+        for _ in range(args.warmup):
+            g.launch()
+        dev.sync()
+        sec = time_steps(stream, flush, steps, g.launch)
+        g.close()
+        dev.profile_enable(True)
+        dev.profile_read()
+        for _ in range(steps):
+            dev.submit(cl)
+        dev.sync()
+        prof = dev.profile_read()
+        dev.profile_enable(False)
+        af_pixels = sum(x["ps_invocations"] for i, x in enumerate(st) if i % stride == stride - 1)
+        return {"fps": steps / sec, "img": img, "shade_ms": prof["shade_ms"] / steps,
+                "lookups": prof["af_lookups"] / steps, "fallbacks": prof["af_fallbacks"] / steps,
+                "af_pixels": af_pixels}
+
+    def psnr(a, b):
+        d = a.astype(np.float64) / 255.0 - b.astype(np.float64) / 255.0
+        mse = float((d * d).mean())
+        return float("inf") if mse == 0 else 10.0 * math.log10(1.0 / mse)
+
+    out = {"training": {"textures": 4096, "texture_size": 512, "make_textures_s": make_s,
+                        "samples": 20_000_000, "batch": 8192, "epochs": 2, "steps": rep["steps"],
+                        "first_loss": rep["first_loss"], "last_loss": rep["last_loss"],
+                        "train_ms": rep["train_ms"],
+                        "samples_per_s": 40_000_000 / (rep["train_ms"] / 1000.0),
+                        "tensor_tflops": 40_000_000 * AF_TRAIN_FLOPS / (rep["train_ms"] / 1000.0) / 1e12},
+           "filter": {"confidence_threshold": learned[0], "probe_range": [learned[2], learned[1]]}}
+    for stride, key in ((2, "c2_frame"), (1, "all_af_frame")):
+        p, l = frame(stride, None), frame(stride, learned)
+        err = int(np.abs(l["img"].astype(np.int16) - p["img"].astype(np.int16)).max())
+        out[key] = {
+            "af_draws": "every other draw" if stride == 2 else "all 8 draws",
+            "plain_frames_per_s": p["fps"], "learned_frames_per_s": l["fps"],
+            "learned_over_plain": l["fps"] / p["fps"],
+            "psnr_db": psnr(l["img"], p["img"]), "max_abs_error_lsb": err,
+            "af_pixels": p["af_pixels"], "network_lookups": l["lookups"],
+            "fallback_rate": l["fallbacks"] / max(1.0, l["lookups"]),
+            "shade_ms": {"plain": p["shade_ms"], "learned": l["shade_ms"]},
+            "af_gpix_per_s_shade_stage": {"plain": p["af_pixels"] / p["shade_ms"] / 1e6,
+                                          "learned": p["af_pixels"] / l["shade_ms"] / 1e6}}
+    model.close()
+    return out
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -374,6 +451,7 @@ def run_gpu(args):
         e2e_fps = frames / max_over_ranks(time.perf_counter() - t0)
     dev.sync()
     uneven = None if args.no_uneven else measure_uneven(dev, stream, flush, args)
+    learned = None if args.no_learned else measure_learned(dev, stream, flush, args, width, height)
 
     if rank == 0:
         peak, peak_kind = measured_peak()
@@ -417,6 +495,7 @@ def run_gpu(args):
                 "h2d_bytes_per_step": int(vb_host.numel() * 4 + ib_host.numel() * 4),
                 "d2h_bytes_per_step": out_bytes},
             "uneven_batch": uneven,
+            "learned_filter": learned,
             "gpu_launches": int(ginfo["kernels"]) * args.steps,
             "clocks": clk.summary(),
         }

@@ -126,7 +126,7 @@ enum {
   /* No counterpart in the reference: SG_PS_TEX_GRAD_MODULATE with the
    * anisotropic lookup approximated by the learned filter named in the
    * shader's `learned_filter` (sg_af_model_id) where it applies -- a minified
-   * lookup of an anisotropic sampler with more than 4 and at most
+   * lookup of an anisotropic sampler with more than constants[2] and at most
    * constants[1] probes -- and where the filter's confidence is at least
    * constants[0]; every other lookup runs the plain sampler. */
   SG_PS_TEX_GRAD_LEARNED = 5
@@ -453,6 +453,14 @@ int32_t sg_af_sample(sg_device* dev, const uint32_t* samplers, uint32_t num_samp
  * exp(-32 * max |colour error|).  The parameters do not change. */
 int32_t sg_af_model_gradients(sg_device* dev, sg_af_model* model, const float* features, const float* targets,
                               uint32_t n, float* grads, float* loss);
+/* Creates `count` tileable RGBA8 textures of size x size (a power of two,
+ * 16-4096) with full box-filtered mip chains, filled on the device from
+ * `seed`: texture i is value noise (4-8 octaves from 2, 4 or 8 cells) when
+ * i mod 3 == 0, a two-colour checkerboard with a period of 2-64 texels when
+ * i mod 3 == 1, and an RGBA sinusoidal grating at a random orientation with
+ * a period of 2-64 texels when i mod 3 == 2.  The handles go to
+ * `out_textures` (count entries); they are ordinary textures. */
+int32_t sg_af_make_textures(sg_device* dev, uint32_t count, uint32_t size, uint64_t seed, uint32_t* out_textures);
 typedef struct sg_af_train_desc {
   const uint32_t* samplers; /* training textures (sampler handles) */
   uint32_t num_samplers;

@@ -190,6 +190,7 @@ SIGNATURES = {
                                  C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "sg_af_model_gradients": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                           C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "sg_af_make_textures": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, _u32p]),
     "sg_af_model_train": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(AfTrainDesc), C.POINTER(AfReport)]),
 }
 

@@ -19,6 +19,8 @@ int device_sms(sg_device* d);
 void device_set_error(sg_device* d, char const* msg);
 int32_t device_af_sampler(sg_device* d, uint32_t handle, dev_sampler& out);
 uint32_t device_register_af(sg_device* d, AfModelDev const& m);
+uint8_t* device_texture_data(sg_device* d, uint32_t tex);
+void launch_af_pattern(uint8_t* dst, uint32_t size, uint64_t seed, uint32_t index, cudaStream_t s);
 void device_unregister_af(sg_device* d, uint32_t id);
 void launch_af_pack(AfModelDev const& M, cudaStream_t s);
 cudaError_t launch_af_infer(AfModelDev const& M, uint16_t const* X, float4 const* skip, uint32_t n, float* out,
@@ -273,6 +275,19 @@ int32_t sg_af_model_gradients(sg_device* d, sg_af_model* m, const float* feature
   AF_CUDA(d, cudaStreamSynchronize(s));
   if (loss) *loss = l / static_cast<float>(n);
   return check_status(d, m);
+}
+
+int32_t sg_af_make_textures(sg_device* d, uint32_t count, uint32_t size, uint64_t seed, uint32_t* out) {
+  if (!d || !out || count == 0 || size < 16 || size > 4096 || (size & (size - 1))) return SG_INVALID_PARAMETER;
+  for (uint32_t i = 0; i < count; ++i) {
+    uint32_t h = 0;
+    if (int32_t r = sg_texture_create(d, size, size, 1, SG_FMT_RGBA8, &h)) return r;
+    out[i] = h;
+    launch_af_pattern(device_texture_data(d, h), size, seed, i, device_stream(d));
+    AF_CUDA(d, cudaGetLastError());
+    if (int32_t r = sg_texture_gen_mipmap(d, h, SG_FILTER_LINEAR)) return r;
+  }
+  return SG_OK;
 }
 
 int32_t sg_af_model_train(sg_device* d, sg_af_model* m, const sg_af_train_desc* t, sg_af_report* rep) {

@@ -67,6 +67,65 @@ void launch_af_samples(dev_sampler const* samplers, uint32_t ntex, uint32_t n, u
   if (n) k_af_samples<<<(n + 127) / 128, 128, 0, s>>>(samplers, ntex, n, first, seed, X, Y, features_f32, residual);
 }
 
+// ---------------------------------------------------------------------------
+// Procedural training textures (RGBA8, size x size, tileable): kind 0 value
+// noise, 1 checkerboard, 2 sinusoidal grating; the parameters come from a
+// hash of (seed, texture index).
+
+__device__ inline float lattice(uint64_t key, int x, int y, int c) {
+  uint64_t const h = hash64(key ^ (static_cast<uint64_t>(x) * 0x9E3779B1ull) ^ (static_cast<uint64_t>(y) << 32) ^
+                            (static_cast<uint64_t>(c) << 58));
+  return static_cast<float>((h >> 40) * (1.0 / 16777216.0));
+}
+
+__global__ void k_af_pattern(uint8_t* dst, uint32_t size, uint64_t seed, uint32_t index) {
+  uint32_t const x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= size) return;
+  uint64_t st = hash64(seed * 0x100000001B3ull + index);
+  uint32_t const kind = index % 3u;
+  float rgba[4];
+  if (kind == 0) {  // value noise: octaves of a smoothstep-interpolated random lattice, tileable
+    int const base = 2 << (hash64(st + 1) % 3);           // 2, 4 or 8 cells
+    int const octaves = 4 + static_cast<int>(hash64(st + 2) % 5);
+    for (int c = 0; c < 4; ++c) {
+      float v = 0.0f, amp = 1.0f, sum = 0.0f;
+      for (int o = 0; o < octaves; ++o) {
+        int const cells = base << o;
+        if (cells > static_cast<int>(size)) break;
+        float const fx = (static_cast<float>(x) + 0.5f) * cells / size, fy = (static_cast<float>(y) + 0.5f) * cells / size;
+        int const ix = static_cast<int>(floorf(fx)), iy = static_cast<int>(floorf(fy));
+        float tx = fx - ix, ty = fy - iy;
+        tx = tx * tx * (3.0f - 2.0f * tx);
+        ty = ty * ty * (3.0f - 2.0f * ty);
+        uint64_t const key = st * 31 + o;
+        int const x0 = ix % cells, x1 = (ix + 1) % cells, y0 = iy % cells, y1 = (iy + 1) % cells;
+        float const a = lattice(key, x0, y0, c), b = lattice(key, x1, y0, c);
+        float const d = lattice(key, x0, y1, c), e = lattice(key, x1, y1, c);
+        v += amp * ((a + (b - a) * tx) + ((d + (e - d) * tx) - (a + (b - a) * tx)) * ty);
+        sum += amp;
+        amp *= 0.5f;
+      }
+      rgba[c] = v / sum;
+    }
+  } else if (kind == 1) {  // checkerboard, period 2-64 texels, two random colours
+    uint32_t const period = 2u << (hash64(st + 3) % 6);
+    bool const odd = (((x / period) + (y / period)) & 1u) != 0u;
+    for (int c = 0; c < 4; ++c) rgba[c] = lattice(st, odd ? 1 : 0, 7, c);
+  } else {  // sinusoidal grating at a random orientation, period 2-64 texels, tileable
+    float const ang = 6.2831853f * lattice(st, 3, 3, 0);
+    float const k = static_cast<float>(size) / exp2f(1.0f + 5.0f * lattice(st, 4, 4, 0));  // cycles per texture
+    float const kx = rintf(k * cosf(ang)), ky = rintf(k * sinf(ang));
+    float const t = 6.2831853f * (kx * static_cast<float>(x) + ky * static_cast<float>(y)) / static_cast<float>(size);
+    for (int c = 0; c < 4; ++c) rgba[c] = 0.5f + 0.5f * sinf(t + 6.2831853f * lattice(st, 5, 5, c));
+  }
+  uint8_t* p = dst + (static_cast<size_t>(y) * size + x) * 4;
+  for (int c = 0; c < 4; ++c) p[c] = static_cast<uint8_t>(fminf(fmaxf(rintf(rgba[c] * 255.0f), 0.0f), 255.0f));
+}
+
+void launch_af_pattern(uint8_t* dst, uint32_t size, uint64_t seed, uint32_t index, cudaStream_t s) {
+  k_af_pattern<<<dim3((size + 127) / 128, size), 128, 0, s>>>(dst, size, seed, index);
+}
+
 // The EWA table of this translation unit's sampler.
 cudaError_t upload_ewa_table_af(float const* tab, cudaStream_t s) {
   return cudaMemcpyToSymbolAsync(c_ewa, tab, 256 * sizeof(float), 0, cudaMemcpyHostToDevice, s);

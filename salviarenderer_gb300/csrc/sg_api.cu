@@ -148,6 +148,7 @@ struct Scratch {
   bool pending = false;                // passes ran since the host last read `sticky`
   uint32_t entry_capacity = 1u << 24;  // bin entries (grows after an overflow)
   uint32_t chunk_capacity = 1u << 18;  // fragment chunks (grows after an overflow)
+  uint32_t af_capacity = 0;            // learned-filter plain-queue records (grows after an overflow)
   void release() {
     for (Arena* a : {&params, &slot_rec, &recs, &bin_counts, &scan_sums, &bin_entries, &tile_begin, &frag_rec,
                      &frag_pos, &frag_mask, &frag_color, &frag_ps, &chunk_next, &chunk_count, &owner_first,
@@ -802,14 +803,18 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.chunk_next.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.chunk_count.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.owner_first.ensure(static_cast<size_t>(pl.ntiles) * RASTER_THREADS * 4));
-  // learned-filter lookups: the plain queue has room for every pixel the
-  // fragment buffer holds (fragment pixel indices must fit 32 bits; past
-  // 2^30 pixels the pass's learned-filter draws run on the plain shading
-  // instances), the network's for 2^22 lookups at most (more go plain)
+  // learned-filter lookups: the plain queue has room for the pixels of twice
+  // the pass's target quads (as the fragment buffer; a pass that queues more
+  // reports OVF_AF_QUEUE and the room grows), the network's for 2^23 lookups
+  // at most (more go plain); with a fragment buffer past 2^30 pixels the
+  // pass's learned-filter draws run on the plain shading instances
   P.af_capacity = 0;
-  if (pl.af_model && nfrag * 4 <= (1ull << 30)) {
-    uint32_t const cap = static_cast<uint32_t>(nfrag * 4);
-    uint32_t const net = std::min<uint32_t>(cap, 1u << 22);
+  if (pl.af_model && nfrag * 4 <= 0xFFFFFFFFull) {  // queued fragment pixel indices are 32-bit
+    // this pass's pixels at twice its targets' quads (the fragment rule above)
+    uint64_t const want = (pl.samples / 4 * 2 + 1024ull * FRAG_CHUNK) * 4;
+    if (want > sc.af_capacity) sc.af_capacity = static_cast<uint32_t>(std::min<uint64_t>(want, 1u << 30));
+    uint32_t const cap = sc.af_capacity;
+    uint32_t const net = std::min<uint32_t>(cap, 1u << 23);
     SG_CUDA(d, sc.af_plain.ensure(static_cast<size_t>(cap) * AF_PLAIN_UNITS * sizeof(float4)));
     SG_CUDA(d, sc.af_net.ensure(static_cast<size_t>(net) * AF_NET_UNITS * sizeof(float4)));
     SG_CUDA(d, sc.af_fallback.ensure(static_cast<size_t>(net) * 4));
@@ -980,7 +985,7 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
 // Reads back the counters of the last immediate pass (after a stream sync)
 // and turns an overflow into SG_OUT_OF_MEMORY with raised capacities.
 int32_t check_overflow(sg_device* d, Scratch& sc, PassCounters const& c, bool fixed) {
-  if (!(c.overflow & (OVF_BIN | OVF_FRAG | OVF_REC))) return SG_OK;
+  if (!(c.overflow & OVF_FATAL)) return SG_OK;
   char msg[256];
   if (fixed) {
     std::snprintf(msg, sizeof(msg),
@@ -989,6 +994,10 @@ int32_t check_overflow(sg_device* d, Scratch& sc, PassCounters const& c, bool fi
   } else {
     if (c.overflow & OVF_BIN) sc.entry_capacity = std::max<uint32_t>(sc.entry_capacity * 2, c.bin_entries + c.bin_entries / 4);
     if (c.overflow & OVF_FRAG) sc.chunk_capacity = std::max<uint32_t>(sc.chunk_capacity * 2, c.chunk_total + c.chunk_total / 4);
+    if (c.overflow & OVF_AF_QUEUE)
+      sc.af_capacity = static_cast<uint32_t>(std::min<uint64_t>(std::max<uint64_t>(2ull * sc.af_capacity,
+                                                                                   c.af_plain + c.af_plain / 4),
+                                                                1u << 30));
     std::snprintf(msg, sizeof(msg), "scratch buffer overflow (bits %u); capacities raised for later passes",
                   c.overflow);
   }
@@ -1231,9 +1240,9 @@ int32_t check_sticky(sg_device* d, Scratch& sc, char const* what) {
   sc.pending = false;
   SG_CUDA(d, cudaMemcpy(d->sticky_host, sc.sticky.ptr, sizeof(unsigned int), cudaMemcpyDeviceToHost));
   unsigned int bits = *d->sticky_host;
-  if (!(bits & (OVF_BIN | OVF_FRAG | OVF_REC | OVF_AF_TIMEOUT))) return SG_OK;
+  if (!(bits & (OVF_FATAL | OVF_AF_TIMEOUT))) return SG_OK;
   SG_CUDA(d, cudaMemset(sc.sticky.ptr, 0, sizeof(unsigned int)));
-  if (!(bits & (OVF_BIN | OVF_FRAG | OVF_REC))) {
+  if (!(bits & OVF_FATAL)) {
     d->error = "learned filter: a tensor-core wait timed out";
     return SG_TIMEOUT;
   }
@@ -1242,6 +1251,7 @@ int32_t check_sticky(sg_device* d, Scratch& sc, char const* what) {
     c.overflow = bits;
     c.bin_entries = sc.entry_capacity;
     c.chunk_total = sc.chunk_capacity;
+    c.af_plain = sc.af_capacity;
     return check_overflow(d, sc, c, false);
   }
   d->error = what;
@@ -1253,7 +1263,7 @@ int32_t check_pending(sg_device* d) {
   if (d->static_sticky) {
     SG_CUDA(d, cudaMemcpy(d->sticky_host, d->static_sticky, sizeof(unsigned int), cudaMemcpyDeviceToHost));
     d->static_sticky = nullptr;
-    if (*d->sticky_host & (OVF_BIN | OVF_FRAG | OVF_REC)) {
+    if (*d->sticky_host & OVF_FATAL) {
       d->error = "static scratch exhausted by a draw since the last sync";
       if (r == SG_OK) r = SG_OUT_OF_MEMORY;
     }
@@ -1793,4 +1803,8 @@ uint32_t device_register_af(sg_device* d, AfModelDev const& m) {
   return id;
 }
 void device_unregister_af(sg_device* d, uint32_t id) { d->af_models.erase(id); }
+uint8_t* device_texture_data(sg_device* d, uint32_t tex) {
+  Texture* t = find_tex(d, tex);
+  return t ? t->levels[0].ptr : nullptr;
+}
 }  // namespace sg

@@ -26,6 +26,10 @@ constexpr uint32_t NO_REC = 0xFFFFFFFFu;
 // overflow bits of PassCounters::overflow
 constexpr uint32_t OVF_BIN = 1u, OVF_FRAG = 4u, OVF_REC = 8u;
 constexpr uint32_t OVF_AF_TIMEOUT = 16u;  // a tensor-core wait of the learned filter gave up
+constexpr uint32_t OVF_AF_QUEUE = 32u;    // the learned filter's lookup queue was full
+// overflows that leave the pass's result incomplete (the host raises the
+// capacity and reports SG_OUT_OF_MEMORY)
+constexpr uint32_t OVF_FATAL = OVF_BIN | OVF_FRAG | OVF_REC | OVF_AF_QUEUE;
 
 struct PassCounters {
   unsigned int bin_entries;          // entries produced by the count pass

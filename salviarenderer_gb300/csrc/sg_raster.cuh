@@ -640,13 +640,12 @@ __device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q) {
 
 // Whether the learned filter takes an SG_PS_TEX_GRAD_LEARNED lookup: a
 // minified lookup of an anisotropic sampler whose probe count is above
-// max(4, constants[2]) -- below that the plain sampler costs no more than the
-// network -- and at most constants[1].
+// constants[2] and at most constants[1].
 __device__ inline bool af_takes(DrawParams const& D, float dxu, float dxv, float dyu, float dyv, af_info& af) {
   dev_sampler const& s = D.ps_samp;
   if (s.mip_filter != SG_FILTER_ANISOTROPIC || s.max_anisotropy <= 1) return false;
   calc_af(s, dxu, dxv, dyu, dyv, 0.0f, af);
-  return af.lod >= 0.0f && af.probe_count > fmaxf(4.0f, D.ps_k[2]) && af.probe_count <= D.ps_k[1];
+  return af.lod >= 0.0f && af.probe_count > D.ps_k[2] && af.probe_count <= D.ps_k[1];
 }
 
 // Attribute interpolation (step_2d_unproj_attr_n_quad / step_2d_unproj_attr_n
@@ -656,7 +655,7 @@ __device__ inline bool af_takes(DrawParams const& D, float dxu, float dxv, float
 // (shade class 8 + NA) and queue the lookups the learned filter applies to.
 template <int NA, bool LEARNED>
 __global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
-  if (P.counters->overflow & (OVF_BIN | OVF_FRAG | OVF_REC)) return;
+  if (P.counters->overflow & OVF_FATAL) return;
   uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
   int const q = threadIdx.x & 3;
   uint32_t const groups = gridDim.x * (blockDim.x >> 2);
@@ -776,7 +775,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
     }
     if constexpr (LEARNED) {
       // queue the lookups, one atomic per warp and queue; lookups past the
-      // network queue's end go to the plain queue, which holds every pixel
+      // network queue's end go to the plain queue (sized for the pass's
+      // fragments; past its end the pass reports OVF_AF_QUEUE)
       int const lane = threadIdx.x & 31;
       unsigned const want_net = __ballot_sync(0xFFFFFFFFu, af_net);
       if (want_net) {
@@ -804,11 +804,15 @@ __global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
         uint32_t first = 0;
         if (lane == leader) first = atomicAdd(&P.counters->af_plain, static_cast<unsigned>(__popc(want_plain)));
         uint32_t const k = __shfl_sync(0xFFFFFFFFu, first, leader) + __popc(want_plain & ((1u << lane) - 1u));
-        if (af_plain && k < P.af_capacity) {  // always below
-          float4* r = P.af_plain + static_cast<size_t>(k) * AF_PLAIN_UNITS;
-          r[0] = af_r0;
-          r[1] = af_r1;
-          r[2] = af_r2;
+        if (af_plain) {
+          if (k < P.af_capacity) {
+            float4* r = P.af_plain + static_cast<size_t>(k) * AF_PLAIN_UNITS;
+            r[0] = af_r0;
+            r[1] = af_r1;
+            r[2] = af_r2;
+          } else {
+            atomicOr(&P.counters->overflow, OVF_AF_QUEUE);
+          }
         }
       }
     }
@@ -827,7 +831,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
   __shared__ uint32_t s_tile;
   uint32_t const ovf = P.counters->overflow;  // final: geometry, binning and coverage are done
   if (blockIdx.x == 0 && threadIdx.x == 0 && ovf) atomicOr(P.sticky, ovf);
-  if (ovf & (OVF_BIN | OVF_FRAG | OVF_REC)) return;
+  if (ovf & OVF_FATAL) return;
   int const tid = threadIdx.x;
   uint32_t cur_draw = 0xFFFFFFFFu;
   unsigned long long backend = 0;

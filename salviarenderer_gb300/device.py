@@ -189,6 +189,15 @@ class Device:
                                                         C.byref(t), C.byref(ms)))
         return {k: getattr(t, k) for k, _ in abi.Tuning._fields_}, ms.value
 
+    def af_make_textures(self, count, size=512, seed=1):
+        """sg_af_make_textures: the learned filter's procedural training
+        textures; returns their handles."""
+        out = (C.c_uint32 * count)()
+        self._check("sg_af_make_textures", self.lib.sg_af_make_textures(self.handle, count, size, seed, out))
+        for h in out:
+            self._textures[h] = (size, size, 1, abi.FMT_RGBA8)
+        return list(out)
+
     def af_sample(self, samplers, n, seed=1):
         """Random anisotropic lookups (sg_af_sample): features n x 24 and the
         plain sampler's RGBA n x 4."""

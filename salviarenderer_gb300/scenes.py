@@ -617,15 +617,20 @@ def af_training_images(seed=20261204, size=512):
 
 class AfTextures:
     """The training (or evaluation) textures bound on a device with mip
-    chains and anisotropic samplers (16 probes at most)."""
+    chains and anisotropic samplers (16 probes at most): from host images,
+    or (images=None) `count` procedural textures made on the device
+    (sg_af_make_textures)."""
 
-    def __init__(self, dev, images, max_aniso=16):
+    def __init__(self, dev, images=None, max_aniso=16, count=0, size=512, seed=1):
         self.dev = dev
         self.textures, self.samplers = [], []
-        for img in images:
+        if images is None:
+            self.textures = dev.af_make_textures(count, size, seed)
+        for img in images or ():
             t = dev.texture(img.shape[1], img.shape[0], 1, abi.FMT_RGBA8)
             dev.texture_upload(t, img)
             dev.gen_mipmap(t, abi.FILTER_LINEAR)
             self.textures.append(t)
-            self.samplers.append(dev.sampler(t, min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
-                                             mip_filter=abi.FILTER_ANISOTROPIC, max_anisotropy=max_aniso))
+        self.samplers = [dev.sampler(t, min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+                                     mip_filter=abi.FILTER_ANISOTROPIC, max_anisotropy=max_aniso)
+                         for t in self.textures]

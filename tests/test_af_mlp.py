@@ -83,17 +83,18 @@ def test_gradients_match_reference(gdev, n):
 
 def test_training_beats_tap_average(gdev):
     """Training on the plain anisotropic sampler lowers the loss, and the
-    trained network predicts held-out lookups (other seed) better than the
-    method it refines: the mean of its four bilinear taps along the major
-    axis (features 8-23)."""
+    trained network predicts lookups on held-out textures (another seed)
+    better than the method it refines: the mean of its four bilinear taps
+    along the major axis (features 8-23)."""
     from salviarenderer_gb300 import scenes
     from salviarenderer_gb300.device import AfModel
-    tex = scenes.AfTextures(gdev, scenes.af_training_images(size=256))
+    tex = scenes.AfTextures(gdev, count=192, size=256, seed=1)
+    held = scenes.AfTextures(gdev, count=48, size=256, seed=2)
     m = AfModel(gdev, seed=3)
-    rep = m.train(tex.samplers, samples=1 << 20, batch=8192, epochs=8, lr=2e-3, seed=5)
-    assert rep["steps"] == 1024
+    rep = m.train(tex.samplers, samples=1 << 21, batch=8192, epochs=2, lr=2e-3, seed=5)
+    assert rep["steps"] == 512
     assert rep["last_loss"] < rep["first_loss"], rep
-    f, y = gdev.af_sample(tex.samplers, 1 << 16, seed=99)
+    f, y = gdev.af_sample(held.samplers, 1 << 16, seed=99)
     assert np.all(np.isfinite(f)) and np.all((y >= 0) & (y <= 1))
     out = m.forward(f)
     mse_learned = float(np.mean((out[:, :4] - y) ** 2))

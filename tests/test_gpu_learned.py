@@ -33,9 +33,9 @@ def odev(oracle_lib):
 
 @pytest.fixture(scope="module")
 def model(gdev):
-    tex = scenes.AfTextures(gdev, scenes.af_training_images(size=256))
+    tex = scenes.AfTextures(gdev, count=256, size=256, seed=1)
     m = AfModel(gdev, seed=3)
-    m.train(tex.samplers, samples=1 << 20, batch=8192, epochs=8, lr=2e-3, seed=5)
+    m.train(tex.samplers, samples=4_000_000, batch=8192, epochs=2, lr=2e-3, seed=5)
     return m
 
 
