@@ -385,6 +385,8 @@ public:
   virtual cpp_shader_ptr clone() = 0;
   // The device program this shader runs (SG_VS_* / SG_PS_* / SG_BS_*).
   virtual uint32_t program() const = 0;
+  // The learned filter an SG_PS_TEX_GRAD_LEARNED program uses (sg_af_model_id), else 0.
+  virtual uint32_t learned_filter() const { return 0; }
 };
 
 // cpp_shader_impl (shader.h:86-157): named constants and samplers, and the
@@ -432,6 +434,7 @@ public:
   result pack(sg_shader& s) const {
     std::memset(&s, 0, sizeof(s));
     s.program = program();
+    s.learned_filter = learned_filter();
     size_t off = 0;
     for (auto const& c : constants_) {
       size_t n = c.size / 4;
@@ -548,6 +551,29 @@ public:
 private:
   sampler_ptr samp_;
 };
+// No counterpart in the reference: texture_grad_pixel_shader with the
+// anisotropic lookup on a learned filter (SG_PS_TEX_GRAD_LEARNED) where its
+// probe count lies in (MinProbes, MaxProbes] and its confidence reaches
+// ConfidenceThreshold; the plain sampler everywhere else.
+class learned_texture_grad_pixel_shader : public cpp_pixel_shader {
+public:
+  learned_texture_grad_pixel_shader(sampler_ptr const& s, uint32_t filter_id, float confidence_threshold = 0.5f,
+                                    float max_probes = 16.0f, float min_probes = 0.0f)
+      : samp_(s), filter_(filter_id), thr_(confidence_threshold), max_(max_probes), min_(min_probes) {
+    declare_sampler("Sampler", samp_);
+    declare_constant("ConfidenceThreshold", thr_);
+    declare_constant("MaxProbes", max_);
+    declare_constant("MinProbes", min_);
+  }
+  uint32_t program() const override { return SG_PS_TEX_GRAD_LEARNED; }
+  uint32_t learned_filter() const override { return filter_; }
+  SALVIA_GB300_CLONE(learned_texture_grad_pixel_shader)
+
+private:
+  sampler_ptr samp_;
+  uint32_t filter_;
+  float thr_, max_, min_;
+};
 class replace_blend_shader : public cpp_blend_shader {  // color(0, s) = src
 public:
   uint32_t program() const override { return SG_BS_REPLACE; }
@@ -591,6 +617,42 @@ struct mapped_resource {
 };
 
 // ---- the renderer (renderer.h:42-131) -----------------------------------
+// No counterpart in the reference: a learned anisotropic filter (sg_af_model)
+// owned by a renderer's device.  Train it on the device from the plain
+// sampler, then hand id() to learned_texture_grad_pixel_shader.
+class learned_filter {
+public:
+  learned_filter(detail::device_sp d, sg_af_model* m) : dev_(std::move(d)), model_(m) {}
+  ~learned_filter() {
+    if (model_) sg_af_model_destroy(dev_->dev, model_);
+  }
+  learned_filter(learned_filter const&) = delete;
+  learned_filter& operator=(learned_filter const&) = delete;
+  uint32_t id() const { return sg_af_model_id(model_); }
+  sg_af_model* native() const { return model_; }
+  // Trains on lookups of the plain anisotropic sampler over the samplers'
+  // textures (sg_af_model_train).
+  result train(std::vector<sampler_ptr> const& samplers, uint32_t samples, uint32_t batch = 8192, uint32_t epochs = 2,
+               float lr = 2e-3f, uint64_t seed = 1, sg_af_report* report = nullptr) {
+    std::vector<uint32_t> h;
+    for (auto const& sp : samplers) h.push_back(sp ? sp->handle() : 0u);
+    sg_af_train_desc t{};
+    t.samplers = h.data();
+    t.num_samplers = static_cast<uint32_t>(h.size());
+    t.samples = samples;
+    t.batch = batch;
+    t.epochs = epochs;
+    t.lr = lr;
+    t.seed = seed;
+    return to_result(sg_af_model_train(dev_->dev, model_, &t, report));
+  }
+
+private:
+  detail::device_sp dev_;
+  sg_af_model* model_ = nullptr;
+};
+using learned_filter_ptr = std::shared_ptr<learned_filter>;
+
 class renderer {
 public:
   explicit renderer(sg_device* d) : dev_(std::make_shared<detail::device_ref>(d)) {
@@ -635,6 +697,13 @@ public:
     uint32_t h = 0;
     if (sg_sampler_create(dev_->dev, &d, tex->handle(), &h) != SG_OK) return nullptr;
     return std::make_shared<resource::sampler>(dev_, h, desc, tex);
+  }
+  // No counterpart in the reference: a learned anisotropic filter on this
+  // renderer's device (sg_af_model_create), untrained.
+  learned_filter_ptr create_learned_filter(uint64_t seed = 1) {
+    sg_af_model* m = nullptr;
+    if (sg_af_model_create(dev_->dev, seed, &m) != SG_OK) return nullptr;
+    return std::make_shared<learned_filter>(dev_, m);
   }
   async_object_ptr create_query(async_object_ids id) {
     if (id != async_object_ids::pipeline_statistics && id != async_object_ids::internal_statistics) return nullptr;
