@@ -634,3 +634,106 @@ class AfTextures:
         self.samplers = [dev.sampler(t, min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
                                      mip_filter=abi.FILTER_ANISOTROPIC, max_anisotropy=max_aniso)
                          for t in self.textures]
+
+
+# --------------------------------------------------------------------------
+def icosphere(subdiv):
+    """Unit icosphere: 20 * 4^subdiv triangles (5,120 at 4, 2,562 vertices).
+    Returns (positions (V, 3) float64, faces (F, 3) int64)."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+         (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    faces = list(f)
+    for _ in range(subdiv):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                mid[key] = len(verts) - 1
+            return mid[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.array(verts), np.array(faces, dtype=np.int64)
+
+
+MORPH_INPUTS = [(abi.SEMANTIC_POSITION, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 0),   # in[0]: base position
+                (abi.SEMANTIC_POSITION, 1, abi.VFMT_R32G32B32A32_FLOAT, 1, 0),   # in[1]: morph target
+                (abi.SEMANTIC_NORMAL, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 16),    # in[2]: normal
+                (abi.SEMANTIC_TEXCOORD, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 32)]  # in[3]: (u, v)
+
+
+def c5_scene(seed=20261204, width=3840, height=2160, samples=4, instances=1000, subdiv=4, tex_size=2048,
+             hmap_size=1024, max_aniso=8, additive=0.1, learned=None):
+    """Large instanced scene (the 4K workload): `instances` draws of a
+    subdivided icosphere (5,120 triangles at subdiv 4), each with a seeded
+    world transform (translation uniform in a 100-unit box, scale in
+    [0.5, 3]) and morph weight (uniform in [0, 1]); the vertex shader blends
+    two position streams and displaces along the normal by a vertex-texture
+    fetch from an R32F height map (SG_VS_MORPH_DISPLACE); the pixel shader
+    samples a 2048^2 RGBA8 texture at 8x anisotropy (the learned filter with
+    `learned` = (threshold, max probes, min probes)) modulated by the normal;
+    RGBA16F colour, 4x MSAA, D32F depth LESS; `additive` of the instances
+    blend additively, the rest replace."""
+    rng = np.random.default_rng(seed)
+    p0, faces = icosphere(subdiv)
+    nv = p0.shape[0]
+    uv = np.stack([np.arctan2(p0[:, 2], p0[:, 0]) / (2 * math.pi) + 0.5, np.arcsin(np.clip(p0[:, 1], -1, 1)) / math.pi + 0.5],
+                  axis=1)
+    p1 = p0 * rng.uniform(0.8, 1.25, size=(nv, 1))
+    vb0 = np.zeros((nv, 12), dtype=np.float32)
+    vb0[:, 0:3], vb0[:, 3] = p0, 1.0
+    vb0[:, 4:7] = p0
+    vb0[:, 8:10] = uv * 4.0
+    vb1 = np.zeros((nv, 4), dtype=np.float32)
+    vb1[:, 0:3], vb1[:, 3] = p1, 1.0
+    hmap = value_noise(rng, hmap_size, octaves=5, channels=1)[:, :, 0].astype(np.float32)
+    tex = to_rgba8(value_noise(rng, tex_size))
+    eye = np.array([50.0, 52.0, -25.0])
+    view = look_at_lh(eye, [50.0, 50.0, 50.0], [0.0, 1.0, 0.0])
+    proj = perspective_fov_lh(math.radians(60.0), width / height, 0.5, 400.0)
+    vp = (view @ proj)
+    s = Scene("c5", width, height, samples, color_fmt=abi.FMT_RGBA16F, ds_fmt=abi.FMT_D32F)
+    s.buffers["vb0"] = vb0
+    s.buffers["vb1"] = vb1
+    s.buffers["ib"] = faces.reshape(-1).astype(np.uint32)
+    s.textures["hmap"] = (hmap, False)
+    s.textures["tex"] = (tex, True)
+    s.samplers["height"] = ("hmap", dict(min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+                                         mip_filter=abi.FILTER_POINT))
+    s.samplers["aniso"] = ("tex", dict(min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+                                       mip_filter=abi.FILTER_ANISOTROPIC, max_anisotropy=max_aniso))
+    ds = default_depth_stencil(depth_func=abi.CMP_LESS)
+    t = rng.uniform(0.0, 100.0, size=(instances, 3))
+    sc = rng.uniform(0.5, 3.0, size=instances)
+    w = rng.uniform(0.0, 1.0, size=instances)
+    add = rng.uniform(0.0, 1.0, size=instances) < additive
+    for i in range(instances):
+        world = np.diag([sc[i], sc[i], sc[i], 1.0])
+        world[3, 0:3] = t[i]
+        k = np.zeros(18, dtype=np.float32)
+        k[0:16] = (world @ vp).astype(np.float32).ravel()
+        k[16] = w[i]
+        k[17] = 0.15
+        ps = (dict(program=abi.PS_TEX_GRAD_LEARNED, samplers=["aniso"], learned_filter="model",
+                   constants=list(learned)) if learned is not None else
+              dict(program=abi.PS_TEX_GRAD_MODULATE, samplers=["aniso"]))
+        s.draws.append(dict(
+            viewport=(0, 0, width, height, 0.0, 1.0), prim_count=faces.shape[0],
+            index_buffer="ib", index_format=abi.INDEX_U32,
+            streams=[("vb0", 48, 0), ("vb1", 16, 0)], inputs=MORPH_INPUTS,
+            num_varyings=2, varying_modifiers=[abi.AM_LINEAR, abi.AM_LINEAR], depth_stencil=ds,
+            vs=dict(program=abi.VS_MORPH_DISPLACE, constants=k, samplers=["height"]),
+            ps=ps, bs=dict(program=abi.BS_ADD if add[i] else abi.BS_REPLACE)))
+    s.clear_color = (0.02, 0.02, 0.05, 1.0)
+    return s

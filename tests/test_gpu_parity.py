@@ -91,3 +91,15 @@ def test_repeat_is_deterministic(gdev):
     b = scenes.render(gdev, s)
     for k in a:
         assert np.array_equal(a[k], b[k])
+
+
+@pytest.mark.parametrize("instances,subdiv", [(200, 3), (40, 4)])
+def test_c5_instanced_small(gdev, odev, instances, subdiv):
+    """The 4K instanced workload's state at a small size: icosphere
+    instances as draws, two position streams blended by a morph weight,
+    normal displacement by a vertex-texture fetch from an R32F height map
+    (SG_VS_MORPH_DISPLACE), 8x anisotropic sampling, RGBA16F colour with 4x
+    MSAA, D32F depth, additive blending on a tenth of the instances."""
+    s = scenes.c5_scene(seed=5 + subdiv, width=480, height=270, instances=instances, subdiv=subdiv,
+                        tex_size=256, hmap_size=128)
+    compare(gdev, odev, s)
