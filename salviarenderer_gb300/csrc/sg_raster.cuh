@@ -825,25 +825,28 @@ __global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
 }
 
 #ifdef SG_RASTER_COVER_MERGE
-// Output merging per tile: owners replay their fragments in primitive order
+// Output merging: owners replay their fragments in primitive order
 // (framebuffer::render_sample_quad, framebuffer.cpp:481-520).
+// Work is handed out per warp -- 32 owners of a tile at a time, from a
+// device-wide cursor -- so tiles of very different cost spread over the SMs.
 __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
-  __shared__ uint32_t s_tile;
   uint32_t const ovf = P.counters->overflow;  // final: geometry, binning and coverage are done
   if (blockIdx.x == 0 && threadIdx.x == 0 && ovf) atomicOr(P.sticky, ovf);
   if (ovf & OVF_FATAL) return;
-  int const tid = threadIdx.x;
+  int const lane = threadIdx.x & 31;
+  uint32_t const groups = RASTER_THREADS / 32;  // owner groups per tile
   uint32_t cur_draw = 0xFFFFFFFFu;
   unsigned long long backend = 0;
   for (;;) {
-    if (tid == 0) s_tile = atomicAdd(&P.counters->merge_cursor, 1u);
-    __syncthreads();
-    uint32_t tile = s_tile;
-    __syncthreads();
+    uint32_t unit = 0;
+    if (lane == 0) unit = atomicAdd(&P.counters->merge_cursor, 1u);
+    unit = __shfl_sync(0xFFFFFFFFu, unit, 0);
+    uint32_t const tile = unit / groups;
     if (tile >= P.ntiles) break;
+    uint32_t const owner = (unit % groups) * 32 + lane;
     uint32_t c = P.tile_begin[tile] == P.tile_begin[tile + 1]
                      ? NO_CHUNK
-                     : P.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + tid];
+                     : P.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + owner];
     while (c != NO_CHUNK) {
       uint32_t n = P.chunk_count[c];
       for (uint32_t k = 0; k < n; ++k) {
