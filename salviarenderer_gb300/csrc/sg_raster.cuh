@@ -152,6 +152,38 @@ __device__ inline void blend(TargetParams const& T, DrawParams const& D, uint32_
   }
 }
 
+// The 4-byte colour formats as words (read_texel / write_texel, the same
+// conversions), and the blend programs on a decoded value.
+__device__ inline v4 decode_word(uint32_t fmt, uint32_t u) {
+  switch (fmt) {
+  case SG_FMT_BGRA8: return unorm8_to_f((u >> 16) & 0xFF, (u >> 8) & 0xFF, u & 0xFF, u >> 24);
+  case SG_FMT_RGBA8: return unorm8_to_f(u & 0xFF, (u >> 8) & 0xFF, (u >> 16) & 0xFF, u >> 24);
+  case SG_FMT_R32F: return mk4(__uint_as_float(u), 0.0f, 0.0f, 0.0f);
+  case SG_FMT_R32I: return mk4(static_cast<float>(static_cast<int32_t>(u)), 0.0f, 0.0f, 0.0f);
+  default: return mk4(0, 0, 0, 0);
+  }
+}
+__device__ inline uint32_t encode_word(uint32_t fmt, v4 c) {
+  switch (fmt) {
+  case SG_FMT_BGRA8: return f_to_unorm8(c.z) | (f_to_unorm8(c.y) << 8) | (f_to_unorm8(c.x) << 16) | (f_to_unorm8(c.w) << 24);
+  case SG_FMT_RGBA8: return f_to_unorm8(c.x) | (f_to_unorm8(c.y) << 8) | (f_to_unorm8(c.z) << 16) | (f_to_unorm8(c.w) << 24);
+  case SG_FMT_R32F: return __float_as_uint(c.x);
+  case SG_FMT_R32I: return static_cast<uint32_t>(static_cast<int32_t>(c.x + 0.5f));
+  default: return 0u;
+  }
+}
+__device__ inline uint32_t blend_word(uint32_t fmt, uint32_t bs_prog, uint32_t dst, v4 src) {
+  switch (bs_prog) {
+  case SG_BS_LERP_SRC_ALPHA: {
+    v4 d = decode_word(fmt, dst);
+    return encode_word(fmt, mk4(lerp1(d.x, src.x, src.w), lerp1(d.y, src.y, src.w), lerp1(d.z, src.z, src.w),
+                                lerp1(d.w, src.w, src.w)));
+  }
+  case SG_BS_ADD: return encode_word(fmt, decode_word(fmt, dst) + src);
+  default: return encode_word(fmt, src);
+  }
+}
+
 // framebuffer::render_sample (framebuffer.cpp:445-479)
 __device__ inline void render_sample(TargetParams const& T, DrawParams const& D, uint32_t x, uint32_t y, uint32_t s,
                                      v4 src, float depth, bool front) {
@@ -886,6 +918,32 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
             float dz = t.ddx(0).z, dyz = t.ddy(0).z;
             for (uint32_t s = 0; s < T.samples; ++s) aa[s] = (T.sp_x[s] - 0.5f) * dz + (T.sp_y[s] - 0.5f) * dyz;
           }
+        }
+        if ((D.early_z || !T.ds) && T.color && T.color_esz == 4 && T.samples == 4) {
+          // colour only, four 4-byte samples per pixel: each covered pixel's
+          // samples are read, blended and written as one 16-byte word
+          uint4 w[4];
+          float4 cc[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if ((m >> (16 * i)) & 0xFu) {
+              uint32_t x = qx + (i & 1), y = qy + (i >> 1);
+              w[i] = *reinterpret_cast<uint4 const*>(color_addr(T, x, y, 0));
+              cc[i] = P.frag_color[static_cast<size_t>(f) * 4 + i];
+            }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            uint32_t const pm = static_cast<uint32_t>(m >> (16 * i)) & 0xFu;
+            if (!pm) continue;
+            v4 const src = mk4(cc[i].x, cc[i].y, cc[i].z, cc[i].w);
+            if (pm & 1u) w[i].x = blend_word(T.color_fmt, D.bs_prog, w[i].x, src);
+            if (pm & 2u) w[i].y = blend_word(T.color_fmt, D.bs_prog, w[i].y, src);
+            if (pm & 4u) w[i].z = blend_word(T.color_fmt, D.bs_prog, w[i].z, src);
+            if (pm & 8u) w[i].w = blend_word(T.color_fmt, D.bs_prog, w[i].w, src);
+            uint32_t x = qx + (i & 1), y = qy + (i >> 1);
+            *reinterpret_cast<uint4*>(color_addr(T, x, y, 0)) = w[i];
+          }
+          continue;
         }
         for (int i = 0; i < 4; ++i) {
           uint32_t pm = static_cast<uint32_t>(m >> (16 * i)) & 0xFFFFu;
