@@ -31,6 +31,7 @@ void launch_geometry(PassParams const& p, cudaStream_t s);
 void launch_bin(PassParams const& p, bool fill, cudaStream_t s);
 void launch_scan(uint32_t* data, size_t n, uint32_t* sums, PassCounters* ctr, cudaStream_t s);
 void launch_tile_ranges(PassParams const& p, cudaStream_t s);
+cudaError_t launch_tile_order(PassParams const& P, uint32_t* counts, cudaStream_t s);
 void launch_cover(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
 cudaError_t init_cover();
 void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
@@ -144,7 +145,7 @@ uint8_t* static_scratch_address(int ordinal) {
 struct Scratch {
   Arena params, slot_rec, recs, bin_counts, scan_sums, bin_entries, tile_begin, frag_rec, frag_pos, frag_mask,
       frag_color, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, sticky, af_net, af_plain,
-      af_fallback;
+      af_fallback, tile_order;
   bool pending = false;                // passes ran since the host last read `sticky`
   uint32_t entry_capacity = 1u << 24;  // bin entries (grows after an overflow)
   uint32_t chunk_capacity = 1u << 18;  // fragment chunks (grows after an overflow)
@@ -152,7 +153,7 @@ struct Scratch {
   void release() {
     for (Arena* a : {&params, &slot_rec, &recs, &bin_counts, &scan_sums, &bin_entries, &tile_begin, &frag_rec,
                      &frag_pos, &frag_mask, &frag_color, &frag_ps, &chunk_next, &chunk_count, &owner_first,
-                     &counters, &stats, &sticky, &af_net, &af_plain, &af_fallback})
+                     &counters, &stats, &sticky, &af_net, &af_plain, &af_fallback, &tile_order})
       a->release();
   }
 };
@@ -791,6 +792,7 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.scan_sums.ensure((pl.ncounts / 4096 + 2) * 4));
   SG_CUDA(d, sc.bin_entries.ensure(static_cast<size_t>(sc.entry_capacity) * 4));
   SG_CUDA(d, sc.tile_begin.ensure((static_cast<size_t>(pl.ntiles) + 1) * 4));
+  SG_CUDA(d, sc.tile_order.ensure((static_cast<size_t>(pl.ntiles) + 64) * 4));
   // fragment room for at least two quads per pixel quad of the pass's targets
   uint64_t const want_chunks = pl.samples / 4 * 2 / FRAG_CHUNK + 1024;
   if (want_chunks > sc.chunk_capacity) sc.chunk_capacity = static_cast<uint32_t>(std::min<uint64_t>(want_chunks, 1u << 30));
@@ -835,6 +837,7 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   P.bin_entries = static_cast<uint32_t*>(sc.bin_entries.ptr);
   P.bin_capacity = sc.entry_capacity;
   P.tile_begin = static_cast<uint32_t*>(sc.tile_begin.ptr);
+  P.tile_order = static_cast<uint32_t*>(sc.tile_order.ptr);
   P.frag_rec = static_cast<uint32_t*>(sc.frag_rec.ptr);
   P.frag_pos = static_cast<uint32_t*>(sc.frag_pos.ptr);
   P.frag_mask = static_cast<uint32_t*>(sc.frag_mask.ptr);
@@ -935,6 +938,7 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       launch_bin(P, false, s);
       launch_scan(P.bin_counts, pl.ncounts, v.scan_sums, P.counters, s);
       launch_tile_ranges(P, s);
+      if (P.tile_order) SG_CUDA(d, launch_tile_order(P, P.tile_order + pl.ntiles, s));
       launch_bin(P, true, s);
       stage_end(d, 1, ev);
       ev = stage_begin(d, profile);
@@ -970,7 +974,7 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       ev = stage_begin(d, profile);
       launch_merge(P, merge_grid, s);
       stage_end(d, 4, ev);
-      k += 9;  // geometry, bin count, 3 scan kernels, tile ranges, bin fill, cover, merge
+      k += P.tile_order ? 11 : 9;  // geometry, bin count, 3 scans, tile ranges (+ 2 order), bin fill, cover, merge
       d->prof.raster_launches += 1;
     }
     d->prof.draws += pl.draws.size();

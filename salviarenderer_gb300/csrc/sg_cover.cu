@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
     uint32_t const item = sh.item;
     __syncthreads();
     if (item >= nitems) break;
-    uint32_t const tile = item >> 2, sub = item & 3;
+    uint32_t const tile = P.tile_order ? P.tile_order[item >> 2] : item >> 2, sub = item & 3;
     uint32_t const begin = P.tile_begin[tile], end = P.tile_begin[tile + 1];
     TargetParams const& T = P.targets[target_of_tile(P, tile)];
     uint32_t const ltile = tile - T.tile_base;

@@ -546,6 +546,25 @@ __global__ void k_tile_ranges(PassParams P) {
   }
 }
 
+// Longest-first order of the tiles for the coverage and merge passes, whose
+// dynamic schedulers then start the costly tiles first: tiles by descending
+// log2 of their bin entries (the order inside a bucket is free -- no result
+// depends on the order tiles are taken in).  counts[0..31] count the
+// buckets (phase 0), counts[32..63] are the buckets' cursors (phase 1).
+__global__ void k_tile_order(PassParams P, uint32_t* counts, uint32_t phase) {
+  uint32_t const tile = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tile >= P.ntiles) return;
+  uint32_t const entries = P.tile_begin[tile + 1] - P.tile_begin[tile];
+  uint32_t const b = 31u - static_cast<uint32_t>(__clz(entries | 1u));
+  if (phase == 0) {
+    atomicAdd(&counts[b], 1u);
+    return;
+  }
+  uint32_t base = 0;
+  for (uint32_t k = b + 1; k < 32; ++k) base += counts[k];
+  P.tile_order[base + atomicAdd(&counts[32 + b], 1u)] = tile;
+}
+
 // ---------------------------------------------------------------------------
 // host-side launchers
 void launch_geometry(PassParams const& P, cudaStream_t s) {
@@ -573,6 +592,15 @@ void launch_scan(uint32_t* data, size_t n, uint32_t* sums, PassCounters* ctr, cu
 
 void launch_tile_ranges(PassParams const& P, cudaStream_t s) {
   k_tile_ranges<<<(P.ntiles + 255) / 256, 256, 0, s>>>(P);
+}
+// P.tile_order (ntiles) and `counts` (64 words, zeroed here) in scratch.
+cudaError_t launch_tile_order(PassParams const& P, uint32_t* counts, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(counts, 0, 64 * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  uint32_t const blocks = (P.ntiles + 255) / 256;
+  k_tile_order<<<blocks, 256, 0, s>>>(P, counts, 0u);
+  k_tile_order<<<blocks, 256, 0, s>>>(P, counts, 1u);
+  return cudaGetLastError();
 }
 
 cudaError_t upload_ewa_table_geometry(float const* tab, cudaStream_t s) {

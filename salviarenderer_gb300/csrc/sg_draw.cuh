@@ -135,6 +135,7 @@ struct PassParams {
   uint32_t* bin_counts;         // per target [tile][chunk] counts, then cursors
   uint32_t* bin_entries;        // rec << 1 | tile-accept, per tile in API order
   uint32_t* tile_begin;         // per global tile [begin, end) into bin_entries
+  uint32_t* tile_order;         // the tiles, costliest first (k_tile_order); null: index order
   uint32_t bin_capacity;
   uint32_t chunk_capacity;
   // Quad fragments, structure of arrays indexed by chunk * FRAG_CHUNK + slot.

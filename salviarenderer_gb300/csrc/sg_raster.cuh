@@ -873,8 +873,8 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
     uint32_t unit = 0;
     if (lane == 0) unit = atomicAdd(&P.counters->merge_cursor, 1u);
     unit = __shfl_sync(0xFFFFFFFFu, unit, 0);
-    uint32_t const tile = unit / groups;
-    if (tile >= P.ntiles) break;
+    if (unit / groups >= P.ntiles) break;
+    uint32_t const tile = P.tile_order ? P.tile_order[unit / groups] : unit / groups;
     uint32_t const owner = (unit % groups) * 32 + lane;
     uint32_t c = P.tile_begin[tile] == P.tile_begin[tile + 1]
                      ? NO_CHUNK
