@@ -435,8 +435,10 @@ def run_gpu(args):
             x = float(t.item())
         return x
 
-    # pipeline counters of one frame (untimed)
+    # pipeline counters of one frame (untimed), then the autotuner's pick of
+    # the scheduling parameters for this frame (sg_autotune; untimed)
     frame_stats = [st for st, c in zip(dev.submit(cl, stats=True), cl._cmds) if c.type == abi.CMD_DRAW]
+    tuning, _ = dev.autotune(cl, reps=3)
 
     # plain path: one sg_draw (one kernel chain) per draw, as the reference's API is called
     for _ in range(args.warmup):
@@ -537,6 +539,7 @@ def run_gpu(args):
                 "value": e2e_fps, "unit": UNIT,
                 "h2d_bytes_per_step": int(vb_host.numel() * 4 + ib_host.numel() * 4),
                 "d2h_bytes_per_step": out_bytes},
+            "tuning": tuning,
             "uneven_batch": uneven,
             "learned_filter": learned,
             "gpu_launches": int(ginfo["kernels"]) * args.steps,

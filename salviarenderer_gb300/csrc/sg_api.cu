@@ -227,8 +227,8 @@ sg_tuning default_tuning() {
   t.bin_capacity = 1u << 24;
   t.frag_chunks = 1u << 18;
   t.shade_quads_per_warp = 8;
-  t.shade_ctas_per_sm = 8;
-  t.merge_ctas_per_sm = 3;
+  t.shade_ctas_per_sm = 16;
+  t.merge_ctas_per_sm = 6;
   t.cover_threads_per_block = 2;
   return t;
 }
