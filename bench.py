@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-uneven", action="store_true", help="skip the 256-frame batched-draw leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-filter leg")
+    ap.add_argument("--no-autotune", action="store_true", help="time under the default scheduling parameters")
     ap.add_argument("--size", default="1920x1080",
                     help="render-target size; smaller sizes are for profiling captures only")
     return ap.parse_args()
@@ -438,7 +439,7 @@ def run_gpu(args):
     # pipeline counters of one frame (untimed), then the autotuner's pick of
     # the scheduling parameters for this frame (sg_autotune; untimed)
     frame_stats = [st for st, c in zip(dev.submit(cl, stats=True), cl._cmds) if c.type == abi.CMD_DRAW]
-    tuning, _ = dev.autotune(cl, reps=3)
+    tuning = dev.get_tuning() if args.no_autotune else dev.autotune(cl, reps=3)[0]
 
     # plain path: one sg_draw (one kernel chain) per draw, as the reference's API is called
     for _ in range(args.warmup):

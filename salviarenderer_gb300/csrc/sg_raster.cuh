@@ -879,13 +879,37 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
     uint32_t c = P.tile_begin[tile] == P.tile_begin[tile + 1]
                      ? NO_CHUNK
                      : P.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + owner];
+    // the next fragment's header and record flags are read a fragment ahead
+    // (they are read-only here), overlapping their latency with the blend
+    uint32_t n = c != NO_CHUNK ? __ldg(&P.chunk_count[c]) : 0u, k = 0;
+    uint32_t h_rec = 0, h_pos = 0, h_mask = 0, h_ps = 0, h_draw = 0;
+    if (n) {
+      uint32_t const f0 = c * FRAG_CHUNK;
+      h_rec = __ldg(&P.frag_rec[f0]);
+      h_pos = __ldg(&P.frag_pos[f0]);
+      h_mask = __ldg(&P.frag_mask[f0]);
+      h_ps = __ldg(&P.frag_ps[f0]);
+      h_draw = __float_as_uint(__ldg(&P.recs[h_rec + 4].z));
+    }
     while (c != NO_CHUNK) {
-      uint32_t n = P.chunk_count[c];
-      for (uint32_t k = 0; k < n; ++k) {
-        uint32_t f = c * FRAG_CHUNK + k;
-        uint32_t rec = P.frag_rec[f], pos = P.frag_pos[f], masks = P.frag_mask[f];
+      {
+        uint32_t const f = c * FRAG_CHUNK + k;
+        uint32_t const rec = h_rec, pos = h_pos, masks = h_mask, ps = h_ps, rdraw = h_draw;
+        // advance to the next fragment and start its loads
+        if (++k == n) {
+          c = __ldg(&P.chunk_next[c]);
+          k = 0;
+          n = c != NO_CHUNK ? __ldg(&P.chunk_count[c]) : 0u;
+        }
+        if (c != NO_CHUNK && k < n) {
+          uint32_t const fn = c * FRAG_CHUNK + k;
+          h_rec = __ldg(&P.frag_rec[fn]);
+          h_pos = __ldg(&P.frag_pos[fn]);
+          h_mask = __ldg(&P.frag_mask[fn]);
+          h_ps = __ldg(&P.frag_ps[fn]);
+          h_draw = __float_as_uint(__ldg(&P.recs[h_rec + 4].z));
+        }
         uint64_t m = expand_mask(masks & 0xFFFFu);
-        uint32_t ps = P.frag_ps[f];
         uint64_t psm = 0;
 #pragma unroll
         for (int i = 0; i < 4; ++i)
@@ -894,7 +918,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
         bool full = (pos >> 24) & 1u;
         if (full && m == 0) continue;
         float4 const* R = P.recs + rec;
-        uint32_t const draw = rec_draw(R);
+        uint32_t const draw = rdraw;
         if (draw != cur_draw) {
           if (backend) atomicAdd(&P.draw_stats[cur_draw].backend_input_pixels, backend);
           backend = 0;
@@ -959,7 +983,6 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
           }
         }
       }
-      c = P.chunk_next[c];
     }
   }
   if (backend) atomicAdd(&P.draw_stats[cur_draw].backend_input_pixels, backend);
