@@ -100,7 +100,7 @@ def cover_bytes(scene, stats):
 
 def read_traffic():
     """Per-launch DRAM traffic of k_cover2 from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_cover2_c2_1080p_4x.md")
+    path = os.path.join(ROOT, "profiles", "pass_kernels_c2_1080p_4x.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
