@@ -37,7 +37,7 @@ constexpr int CV_THREADS = 128;              // 64 blocks x 2 threads
 constexpr int CV_STAGE = 128;                // triangles per staged batch
 constexpr int CV_WORDS = CV_STAGE / 32;
 constexpr int CV_PX = 32;                    // quadrant edge
-constexpr int CV_K = 8;                      // pairs per block per round
+constexpr int CV_K = 12;                     // pairs per block per round
 
 struct TriCv {  // what coverage and early-Z read of a triangle
   float4 e0, e1, e2, bbox;
