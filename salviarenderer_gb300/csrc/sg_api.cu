@@ -32,6 +32,7 @@ void launch_bin(PassParams const& p, bool fill, cudaStream_t s);
 void launch_scan(uint32_t* data, size_t n, uint32_t* sums, PassCounters* ctr, cudaStream_t s);
 void launch_tile_ranges(PassParams const& p, cudaStream_t s);
 cudaError_t launch_tile_order(PassParams const& P, uint32_t* counts, cudaStream_t s);
+cudaError_t launch_frag_classes(PassParams const& P, uint32_t num_sms, cudaStream_t s);
 void launch_cover(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
 cudaError_t init_cover();
 void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
@@ -145,7 +146,7 @@ uint8_t* static_scratch_address(int ordinal) {
 struct Scratch {
   Arena params, slot_rec, recs, bin_counts, scan_sums, bin_entries, tile_begin, frag_rec, frag_pos, frag_mask,
       frag_color, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, sticky, af_net, af_plain,
-      af_fallback, tile_order;
+      af_fallback, tile_order, frag_list;
   bool pending = false;                // passes ran since the host last read `sticky`
   uint32_t entry_capacity = 1u << 24;  // bin entries (grows after an overflow)
   uint32_t chunk_capacity = 1u << 18;  // fragment chunks (grows after an overflow)
@@ -153,7 +154,7 @@ struct Scratch {
   void release() {
     for (Arena* a : {&params, &slot_rec, &recs, &bin_counts, &scan_sums, &bin_entries, &tile_begin, &frag_rec,
                      &frag_pos, &frag_mask, &frag_color, &frag_ps, &chunk_next, &chunk_count, &owner_first,
-                     &counters, &stats, &sticky, &af_net, &af_plain, &af_fallback, &tile_order})
+                     &counters, &stats, &sticky, &af_net, &af_plain, &af_fallback, &tile_order, &frag_list})
       a->release();
   }
 };
@@ -802,6 +803,7 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.frag_mask.ensure(nfrag * 4));
   SG_CUDA(d, sc.frag_color.ensure(nfrag * 4 * sizeof(float4)));
   SG_CUDA(d, sc.frag_ps.ensure(nfrag));
+  SG_CUDA(d, sc.frag_list.ensure((nfrag + 32) * 4));
   SG_CUDA(d, sc.chunk_next.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.chunk_count.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.owner_first.ensure(static_cast<size_t>(pl.ntiles) * RASTER_THREADS * 4));
@@ -843,6 +845,8 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   P.frag_mask = static_cast<uint32_t*>(sc.frag_mask.ptr);
   P.frag_color = static_cast<float4*>(sc.frag_color.ptr);
   P.frag_ps = static_cast<uint8_t*>(sc.frag_ps.ptr);
+  P.frag_list = static_cast<uint32_t*>(sc.frag_list.ptr);
+  P.class_counts = P.frag_list + nfrag;
   P.chunk_next = static_cast<uint32_t*>(sc.chunk_next.ptr);
   P.chunk_count = static_cast<uint32_t*>(sc.chunk_count.ptr);
   P.chunk_capacity = sc.chunk_capacity;
@@ -948,6 +952,10 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
         launch_cover(P, pl.max_samples, pl.any_early_z, cover_grid, s);
       stage_end(d, 2, ev);
       ev = stage_begin(d, profile);
+      if (P.frag_list) {
+        SG_CUDA(d, launch_frag_classes(P, sms, s));
+        k += 2;
+      }
       // shade classes: varyings, plus 8 for learned-filter draws (which the
       // plain instances shade when the pass has no lookup queue)
       uint32_t classes = pl.na_mask;

@@ -565,6 +565,41 @@ __global__ void k_tile_order(PassParams P, uint32_t* counts, uint32_t phase) {
   P.tile_order[base + atomicAdd(&counts[32 + b], 1u)] = tile;
 }
 
+// The pass's fragments grouped by shade class, so each shading instance
+// walks only its own (order inside a class is free: every fragment's colour
+// has its own slot).  Phase 0 counts the classes, phase 1 scatters the
+// fragment indices; one atomic per warp and class.
+__global__ void k_frag_classes(PassParams P, uint32_t phase) {
+  if (P.counters->overflow & OVF_FATAL) return;
+  uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
+  uint32_t base[16];
+  if (phase == 1) {
+    uint32_t acc = 0;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      base[c] = acc;
+      acc += P.class_counts[c];
+    }
+  }
+  int const lane = threadIdx.x & 31;
+  uint32_t const stride = gridDim.x * blockDim.x;
+  uint32_t const rounds = (nfrag + stride - 1) / stride;
+  for (uint32_t it = 0; it < rounds; ++it) {
+    uint32_t const f = blockIdx.x * blockDim.x + threadIdx.x + it * stride;
+    bool const live = f < nfrag && (f % FRAG_CHUNK) < P.chunk_count[f / FRAG_CHUNK];
+    uint32_t const cls = live ? (P.frag_pos[f] >> 25) & 15u : 16u;
+    unsigned const same = __match_any_sync(0xFFFFFFFFu, cls);
+    int const leader = __ffs(same) - 1;
+    if (!live) continue;
+    uint32_t first = 0;
+    if (lane == leader)
+      first = atomicAdd(&P.class_counts[(phase == 0 ? 0u : 16u) + cls], static_cast<unsigned>(__popc(same)));
+    if (phase == 0) continue;
+    first = __shfl_sync(same, first, leader);
+    P.frag_list[base[cls] + first + __popc(same & ((1u << lane) - 1u))] = f;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host-side launchers
 void launch_geometry(PassParams const& P, cudaStream_t s) {
@@ -593,6 +628,15 @@ void launch_scan(uint32_t* data, size_t n, uint32_t* sums, PassCounters* ctr, cu
 void launch_tile_ranges(PassParams const& P, cudaStream_t s) {
   k_tile_ranges<<<(P.ntiles + 255) / 256, 256, 0, s>>>(P);
 }
+// P.frag_list / P.class_counts (zeroed here) in scratch.
+cudaError_t launch_frag_classes(PassParams const& P, uint32_t num_sms, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(P.class_counts, 0, 32 * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  k_frag_classes<<<num_sms * 4, 256, 0, s>>>(P, 0u);
+  k_frag_classes<<<num_sms * 4, 256, 0, s>>>(P, 1u);
+  return cudaGetLastError();
+}
+
 // P.tile_order (ntiles) and `counts` (64 words, zeroed here) in scratch.
 cudaError_t launch_tile_order(PassParams const& P, uint32_t* counts, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(counts, 0, 64 * sizeof(uint32_t), s);

@@ -136,6 +136,11 @@ struct PassParams {
   uint32_t* bin_entries;        // rec << 1 | tile-accept, per tile in API order
   uint32_t* tile_begin;         // per global tile [begin, end) into bin_entries
   uint32_t* tile_order;         // the tiles, costliest first (k_tile_order); null: index order
+  // the pass's fragments by shade class (k_frag_classes): frag_list holds
+  // the fragment indices of class 0, then class 1, ...; class_counts[0..15]
+  // the classes' sizes, [16..31] the fill cursors.  Null: walk every slot.
+  uint32_t* frag_list;
+  uint32_t* class_counts;
   uint32_t bin_capacity;
   uint32_t chunk_capacity;
   // Quad fragments, structure of arrays indexed by chunk * FRAG_CHUNK + slot.

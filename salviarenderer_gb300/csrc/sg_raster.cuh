@@ -692,18 +692,40 @@ __global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
   int const q = threadIdx.x & 3;
   uint32_t const groups = gridDim.x * (blockDim.x >> 2);
   uint32_t const start = blockIdx.x * (blockDim.x >> 2) + (threadIdx.x >> 2);
-  uint32_t const rounds = (nfrag + groups - 1) / groups;
+  // this instance's shade classes: NA varyings, plus 8 for learned-filter
+  // draws; without a lookup queue the plain instances shade those draws too.
+  // With the class lists, only their fragments are walked; else every slot.
+  uint32_t const cls_a = LEARNED ? NA + 8u : NA;
+  bool const with_b = !LEARNED && !P.af_capacity;
+  uint32_t base_a = 0, n_a = 0, base_b = 0, n_b = 0;
+  if (P.frag_list) {
+    uint32_t acc = 0;
+    for (uint32_t c = 0; c < 16; ++c) {
+      uint32_t const k = P.class_counts[c];
+      if (c == cls_a) base_a = acc, n_a = k;
+      if (with_b && c == NA + 8u) base_b = acc, n_b = k;
+      acc += k;
+    }
+  }
+  uint32_t const total = P.frag_list ? n_a + n_b : nfrag;
+  uint32_t const rounds = (total + groups - 1) / groups;
   // learned instances: each thread's network record (feature row and tap
   // mean) waits here, unit-major, until the warp has its queue slots
   __shared__ uint4 s_net[LEARNED ? 5 * 256 : 1];
   for (uint32_t it = 0; it < rounds; ++it) {
-    uint32_t f = start + it * groups;
-    bool live = f < nfrag && (f % FRAG_CHUNK) < P.chunk_count[f / FRAG_CHUNK];
+    uint32_t const idx = start + it * groups;
+    uint32_t f;
+    bool live;
+    if (P.frag_list) {
+      live = idx < total;
+      f = live ? P.frag_list[idx < n_a ? base_a + idx : base_b + (idx - n_a)] : 0u;
+    } else {
+      f = idx;
+      live = f < nfrag && (f % FRAG_CHUNK) < P.chunk_count[f / FRAG_CHUNK];
+    }
     uint32_t pos = live ? P.frag_pos[f] : 0u;
-    // shade class: NA varyings, plus 8 for learned-filter draws; without a
-    // lookup queue the plain instances shade those draws too
     uint32_t const cls = (pos >> 25) & 15u;
-    live = live && (LEARNED ? cls == NA + 8u : (cls == NA || (!P.af_capacity && cls == NA + 8u)));
+    live = live && (cls == cls_a || (with_b && cls == NA + 8u));
     uint32_t draw = 0xFFFFFFFFu;
     // learned instances: the pixel's lookup, for the network's queue (af_net)
     // or for the plain sampler's (af_plain)
