@@ -21,14 +21,14 @@
 //      surviving quads to the block's fragment list.
 //
 // Hierarchical depth test: each thread keeps the largest and smallest depth
-// stored in its half of the block.  A triangle's depth over the block is
-// bounded from its depth plane, widened by a margin that covers the rounding
-// of the reference's per-sample depth expression; when the bound proves
-// every sample of both halves fails the depth test, the pair is dropped.
-// Such samples neither pass nor write, so results are those of testing
-// every sample.  The depth range only narrows toward passing values as
-// samples are written, so a drop decided at the start of a batch stays
-// right for the whole batch.
+// stored in its half of the block, recomputed at the start of each batch
+// after writes.  A triangle's depth over the block is bounded from its depth
+// plane, widened by a margin that covers the rounding of the reference's
+// per-sample depth expression; when the bound proves every sample of both
+// halves fails the depth test, the pair is dropped.  Such samples neither
+// pass nor write, so results are those of testing every sample.  The depth
+// range only narrows toward passing values as samples are written, so a drop
+// decided at the start of a batch stays right for the whole batch.
 #include "sg_raster.cuh"
 
 namespace sg {
@@ -399,12 +399,14 @@ __global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
     }
     uint32_t* const zblk = ztile + (iby * 4 * zrow) + ibx * 4 * S;
     ZRange zr{-INFINITY, INFINITY, 0u, 0xFFFFFFu};
-    if (stage_z) {
-      __syncthreads();
-      z_range(zblk, static_cast<int>(zrow), hf, d24, zr);
-    }
+    bool z_dirty = stage_z;  // the half's depth range is recomputed before a batch's culling when stale
+    if (stage_z) __syncthreads();
     for (uint32_t bstart = begin; bstart < end; bstart += CV_STAGE) {
       uint32_t const nb = min(static_cast<uint32_t>(CV_STAGE), end - bstart);
+      if (z_dirty) {
+        z_range(zblk, static_cast<int>(zrow), hf, d24, zr);
+        z_dirty = false;
+      }
       __syncthreads();
       uint32_t* const masks = &sh.mask4[0][0];
       for (int i = tid; i < (64 + 64 + 4) * CV_WORDS; i += CV_THREADS) masks[i] = 0;
@@ -484,7 +486,7 @@ __global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
           if ((t.zcfg & 128u) && cv) {
             bool wrote = false;
             tz = early_z_half(t, cv, bx_abs, by_abs, zblk, static_cast<int>(zrow), hf, wrote);
-            if (wrote) z_range(zblk, static_cast<int>(zrow), hf, d24, zr);
+            z_dirty = z_dirty || wrote;
           }
           tz |= __shfl_xor_sync(3u << (tid & 30), tz, 1);
           if (h == 0 && tz) emit_quads(P, L, t, (e8 >> 7) != 0, bx_abs, by_abs, S, uc, cv, tz);
