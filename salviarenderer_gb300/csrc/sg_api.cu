@@ -806,7 +806,7 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.frag_list.ensure((nfrag + 32) * 4));
   SG_CUDA(d, sc.chunk_next.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.chunk_count.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
-  SG_CUDA(d, sc.owner_first.ensure(static_cast<size_t>(pl.ntiles) * RASTER_THREADS * 4));
+  SG_CUDA(d, sc.owner_first.ensure(static_cast<size_t>(pl.ntiles) * QUAD_OWNERS * 4));
   // learned-filter lookups: the plain queue has room for the pixels of twice
   // the pass's target quads (as the fragment buffer; a pass that queues more
   // reports OVF_AF_QUEUE and the room grows), the network's for 2^23 lookups
@@ -877,7 +877,7 @@ int32_t scratch_static(sg_device* d, uint8_t* base, PassPlan const& pl, PlanLayo
   P.bin_counts = reinterpret_cast<uint32_t*>(take(pl.ncounts * 4));
   v.scan_sums = reinterpret_cast<uint32_t*>(take((pl.ncounts / 4096 + 2) * 4));
   P.tile_begin = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(pl.ntiles) + 1) * 4));
-  P.owner_first = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(pl.ntiles) * RASTER_THREADS * 4));
+  P.owner_first = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(pl.ntiles) * QUAD_OWNERS * 4));
   if (off > SG_STATIC_SCRATCH_TABLE_LIMIT) {
     char msg[200];
     std::snprintf(msg, sizeof(msg),

@@ -1,8 +1,8 @@
 // sg_cover.cu -- coverage and early-Z of a pass.
 //
 // Work items are the 32x32 quadrants of every tile of every target, taken
-// from a dynamic cursor; a CTA of 128 threads handles one item at a time,
-// two threads per 4x4 block.  For each batch of the tile's triangles (its
+// from a dynamic cursor; a CTA of 256 threads handles one item at a time,
+// four threads per 4x4 block, one per 2x2 quad.  For each batch of the tile's triangles (its
 // bin list, in API order) the CTA
 //   1. stages the batch and classifies every triangle against the
 //      quadrant's 16x16 regions and 4x4 blocks with the reference's level-1
@@ -14,26 +14,28 @@
 //   3. in rounds of up to CV_K triangles per block: computes the per-sample
 //      coverage of every remaining (triangle, block) pair -- the edge test of
 //      draw_partial_tile, rasterizer.cpp:298-439 -- spread evenly over all
-//      threads (coverage does not depend on order), then lets each block's
-//      two threads walk its pairs in primitive order, each running early-Z
-//      (framebuffer.cpp:522-614) on half of the block's samples against the
-//      quadrant's depth staged in shared memory, the first appending the
-//      surviving quads to the block's fragment list.
+//      threads (coverage does not depend on order), then lets each of the
+//      block's four threads walk its pairs in primitive order on its quad:
+//      early-Z (framebuffer.cpp:522-614) on the quad's samples against the
+//      quadrant's depth staged in shared memory, and the surviving quad
+//      appended to that quad's own fragment list.  Quads are disjoint, so
+//      the four walks need no synchronisation.
 //
-// Hierarchical depth test: each thread keeps the largest and smallest depth
-// stored in its half of the block, recomputed at the start of each batch
+// Hierarchical depth test: the block's four threads keep the largest and
+// smallest depth stored in the block, recomputed at the start of each batch
 // after writes.  A triangle's depth over the block is bounded from its depth
 // plane, widened by a margin that covers the rounding of the reference's
-// per-sample depth expression; when the bound proves every sample of both
-// halves fails the depth test, the pair is dropped.  Such samples neither
-// pass nor write, so results are those of testing every sample.  The depth
-// range only narrows toward passing values as samples are written, so a drop
-// decided at the start of a batch stays right for the whole batch.
+// per-sample depth expression; when the bound proves every sample of the
+// block fails the depth test, the pair is dropped (the four threads test a
+// quarter of the block's triangles each).  Such samples neither pass nor
+// write, so results are those of testing every sample.  The depth range only
+// narrows toward passing values as samples are written, so a drop decided at
+// the start of a batch stays right for the whole batch.
 #include "sg_raster.cuh"
 
 namespace sg {
 
-constexpr int CV_THREADS = 128;              // 64 blocks x 2 threads
+constexpr int CV_THREADS = 256;              // 64 blocks x 4 quads
 constexpr int CV_STAGE = 128;                // triangles per staged batch
 constexpr int CV_WORDS = CV_STAGE / 32;
 constexpr int CV_PX = 32;                    // quadrant edge
@@ -66,45 +68,45 @@ inline size_t cv_smem(uint32_t samples, bool early_z) {
   return ((sizeof(CvShared) + 15) & ~size_t(15)) + (early_z ? static_cast<size_t>(CV_PX) * CV_PX * samples * 4 : 0);
 }
 
-// This thread's half of a block: samples [s0, s0 + ns) of rows [r0, r0 + nr).
-struct Half {
-  uint32_t s0, ns, r0, nr;
-  uint32_t inside;  // bit iy * 4 + ix: pixel inside the target
+// This thread's quad: pixel i at (x + (i & 1), y + (i >> 1)).
+struct Quad {
+  int x, y;         // target coordinates of its top-left pixel
+  uint32_t inside;  // bit i: pixel i inside the target
   uint32_t samples;
-  float ax[2], ay[2];  // offsets of samples s0, s0 + 1 from the pixel centre (aa_z_offset)
+  float ax[4], ay[4];  // offsets of the samples from the pixel centre (aa_z_offset)
 };
 
-// Depth range stored in the thread's half (pixels inside the target only).
+// Depth range stored in a quad or block (pixels inside the target only).
 struct ZRange {
   float zmax, zmin;
   uint32_t qmax, qmin;  // D24 depth bits
 };
 
-__device__ inline void z_range(uint32_t const* zblk, int zrow, Half const& hf, bool d24, ZRange& r) {
-  uint32_t const S = hf.samples;
+__device__ inline void z_range(uint32_t const* zq, int zrow, Quad const& qd, bool d24, ZRange& r) {
+  uint32_t const S = qd.samples;
   r.zmax = -INFINITY;
   r.zmin = INFINITY;
   r.qmax = 0;
   r.qmin = 0xFFFFFFu;
-  for (uint32_t iy = hf.r0; iy < hf.r0 + hf.nr; ++iy)
 #pragma unroll
-    for (int ix = 0; ix < 4; ++ix) {
-      if (!((hf.inside >> (iy * 4 + ix)) & 1u)) continue;
-      uint32_t const* zp = zblk + iy * zrow + ix * S;
-      for (uint32_t s = hf.s0; s < hf.s0 + hf.ns; ++s) {
-        uint32_t w = zp[s];
-        if (d24) {
-          r.qmax = max(r.qmax, w & 0xFFFFFFu);
-          r.qmin = min(r.qmin, w & 0xFFFFFFu);
-        } else {
-          r.zmax = fmaxf(r.zmax, __uint_as_float(w));
-          r.zmin = fminf(r.zmin, __uint_as_float(w));
-        }
+  for (int i = 0; i < 4; ++i) {
+    if (!((qd.inside >> i) & 1u)) continue;
+    uint32_t const* zp = zq + (i >> 1) * zrow + (i & 1) * S;
+    for (uint32_t s = 0; s < S; ++s) {
+      uint32_t w = zp[s];
+      if (d24) {
+        r.qmax = max(r.qmax, w & 0xFFFFFFu);
+        r.qmin = min(r.qmin, w & 0xFFFFFFu);
+      } else {
+        r.zmax = fmaxf(r.zmax, __uint_as_float(w));
+        r.zmin = fminf(r.zmin, __uint_as_float(w));
       }
     }
+  }
 }
 
-// Whether every sample of the block fails `func` against the stored range.
+// Whether every sample of the 4x4 block at (bx_abs, by_abs) fails `func` against the
+// stored range.
 __device__ inline bool z_culled(TriCv const& t, int bx_abs, int by_abs, uint32_t func, bool d24, ZRange const& r) {
   if (func == SG_CMP_NEVER) return true;
   if (func != SG_CMP_LESS && func != SG_CMP_LESS_EQUAL && func != SG_CMP_GREATER && func != SG_CMP_GREATER_EQUAL)
@@ -138,10 +140,10 @@ __device__ inline bool z_culled(TriCv const& t, int bx_abs, int by_abs, uint32_t
   }
 }
 
-// Whether the pair's half is dropped by the hierarchical depth test.
-__device__ inline bool pair_hidden(TriCv const& t, int bx_abs, int by_abs, bool d24, ZRange const& zr) {
+// Whether the hierarchical depth test drops the pair on the block at (bx, by).
+__device__ inline bool pair_hidden(TriCv const& t, int bx, int by, bool d24, ZRange const& zr) {
   uint32_t const zc = t.zcfg, func = (zc >> 8) & 15u;
-  return (zc & 128u) && (((zc >> 4) & 1u) || func == SG_CMP_NEVER) && z_culled(t, bx_abs, by_abs, func, d24, zr);
+  return (zc & 128u) && (((zc >> 4) & 1u) || func == SG_CMP_NEVER) && z_culled(t, bx, by, func, d24, zr);
 }
 
 // Per-sample coverage of a whole 4x4 block (draw_partial_tile's edge test,
@@ -185,86 +187,60 @@ __device__ inline void block_coverage(TriCv const& t, bool full, int bx_abs, int
   cv = uc & im;
 }
 
-// Early-Z of one pair on this thread's half of the block's samples
-// (framebuffer.cpp:522-614) against the staged depth; returns the passing
-// samples and writes depth on pass.
-__device__ inline uint64_t early_z_half(TriCv const& t, uint64_t cv, int bx_abs, int by_abs, uint32_t* zblk, int zrow,
-                                        Half const& hf, bool& wrote) {
-  uint32_t const S = hf.samples, zc = t.zcfg, func = (zc >> 8) & 15u;
+// A quad's 16 coverage bits (4 per pixel i, in quad order) out of a block's
+// 64 (4 per pixel, nibble iy * 4 + ix); the quad's top-left pixel is block
+// pixel (qx, qy).
+__device__ inline uint32_t quad_bits(uint64_t m, int qx, int qy) {
+  return (static_cast<uint32_t>(m >> ((qy * 4 + qx) * 4)) & 0xFFu) |
+         ((static_cast<uint32_t>(m >> ((qy * 4 + 4 + qx) * 4)) & 0xFFu) << 8);
+}
+
+// Early-Z of one pair on this thread's quad (framebuffer.cpp:522-614)
+// against the staged depth: returns the passing samples of the covered ones
+// `cq` and writes depth on pass.
+__device__ inline uint32_t early_z_quad(TriCv const& t, uint32_t cq, uint32_t* zq, int zrow, Quad const& qd,
+                                        bool& wrote) {
+  uint32_t const S = qd.samples, zc = t.zcfg, func = (zc >> 8) & 15u;
   bool const rd = (zc >> 4) & 1u, wr = (zc >> 5) & 1u, d24 = (zc >> 6) & 1u;
-  uint64_t tz = 0;
-  for (uint32_t iy = hf.r0; iy < hf.r0 + hf.nr; ++iy) {
-    uint32_t const qy = by_abs + (iy & 2u);
-    float const dy = 0.5f + static_cast<float>(qy) - t.p0y;
+  // step_2d_unproj_pos_quad's z (shader.cpp:257-287)
+  float const dx = 0.5f + static_cast<float>(qd.x) - t.p0x;
+  float const dy = 0.5f + static_cast<float>(qd.y) - t.p0y;
+  float const z00 = t.p0z + (t.dzx * dx + t.dzy * dy);
+  uint32_t tz = 0;
 #pragma unroll
-    for (int ixq = 0; ixq < 2; ++ixq) {
-      uint32_t const qx = bx_abs + 2 * ixq;
-      float const dx = 0.5f + static_cast<float>(qx) - t.p0x;
-      // step_2d_unproj_pos_quad's z (shader.cpp:257-287)
-      float const z00 = t.p0z + (t.dzx * dx + t.dzy * dy);
+  for (int i = 0; i < 4; ++i) {
+    uint32_t const pbits = (cq >> (4 * i)) & 0xFu;
+    if (!pbits) continue;
+    float const z = (i & 2) ? ((i & 1) ? (z00 + t.dzx) + t.dzy : z00 + t.dzy) : ((i & 1) ? z00 + t.dzx : z00);
+    uint32_t* zp = zq + (i >> 1) * zrow + (i & 1) * S;
 #pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        uint32_t const ix = 2 * ixq + i;
-        uint32_t const pbits = static_cast<uint32_t>(cv >> ((iy * 4 + ix) * 4)) & 0xFu;
-        if (!pbits) continue;
-        float const z = (iy & 1u) ? (i ? (z00 + t.dzx) + t.dzy : z00 + t.dzy) : (i ? z00 + t.dzx : z00);
-        uint32_t* zp = zblk + iy * zrow + ix * S;
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-          if (j >= static_cast<int>(hf.ns)) break;
-          uint32_t const s = hf.s0 + j;
-          if (!(pbits & (1u << s))) continue;
-          float const nd = S == 1 ? z : (hf.ax[j] * t.dzx + hf.ay[j] * t.dzy) + z;
-          uint32_t const w = zp[s];
-          bool const pass = d24 ? cmpu(func, d24_quantize(nd), rd ? (w & 0xFFFFFFu) : 0u)
-                                : cmpf(func, nd, rd ? __uint_as_float(w) : 0.0f);
-          if (pass) {
-            if (wr) {
-              zp[s] = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
-              wrote = true;
-            }
-            tz |= 1ull << ((iy * 4 + ix) * 4 + s);
-          }
+    for (int s = 0; s < 4; ++s) {
+      if (!(pbits & (1u << s))) continue;  // coverage holds samples below S only
+      float const nd = S == 1 ? z : (qd.ax[s] * t.dzx + qd.ay[s] * t.dzy) + z;
+      uint32_t const w = zp[s];
+      bool const pass = d24 ? cmpu(func, d24_quantize(nd), rd ? (w & 0xFFFFFFu) : 0u)
+                            : cmpf(func, nd, rd ? __uint_as_float(w) : 0.0f);
+      if (pass) {
+        if (wr) {
+          zp[s] = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
+          wrote = true;
         }
+        tz |= 1u << (4 * i + s);
       }
     }
   }
   return tz;
 }
 
-// Appends the block's surviving quads (the first thread of the pair).
-__device__ inline void emit_quads(PassParams const& P, OwnerList& L, TriCv const& t, bool full, int bx_abs,
-                                  int by_abs, uint32_t S, uint64_t uc, uint64_t cv, uint64_t tz) {
-  uint32_t const fm = (1u << S) - 1u;
-  uint32_t const qfull = fm | (fm << 4) | (fm << 8) | (fm << 12);
-  uint32_t const rec = t.entry >> 1, na = t.nattr << 25;
-#pragma unroll 1
-  for (int q = 0; q < 4; ++q) {
-    int const qx = (q & 1) * 2, qy = (q >> 1) * 2;
-    // quad pixel i at (qx + (i & 1), qy + (i >> 1)), packed 4 bits per pixel
-    auto quad = [&](uint64_t m) {
-      uint32_t r = 0;
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-        r |= (static_cast<uint32_t>(m >> (((qy + (i >> 1)) * 4 + qx + (i & 1)) * 4)) & 0xFu) << (4 * i);
-      return r;
-    };
-    uint32_t const tq = quad(tz);
-    if (!tq) continue;
-    uint32_t const cq = quad(cv), uq = quad(uc);
-    bool const fullq = full ? cq == qfull : (uq == qfull && cq == uq);
-    uint32_t const ax = bx_abs + qx, ay = by_abs + qy;
-    owner_append(P, L, rec, (ax >> 1) | ((ay >> 1) << 12) | (fullq ? 1u << 24 : 0u) | na, tq | (cq << 16));
-  }
-}
-
 // Stages a batch of a tile's bin entries and classifies each triangle
-// against the quadrant's regions and blocks (rasterizer.cpp:441-571).
+// against the quadrant's regions and blocks (rasterizer.cpp:441-571); two
+// threads per triangle, one per row of 16x16 regions.
 __device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint32_t bstart, uint32_t nb, int tile_x0,
                                 int tile_y0, int bx0, int by0, CvShared& sh) {
   float const tx0f = static_cast<float>(tile_x0), ty0f = static_cast<float>(tile_y0);
   float const trr = T.target_w, trb = T.target_h;
-  for (uint32_t i = threadIdx.x; i < nb; i += CV_THREADS) {
+  for (uint32_t j = threadIdx.x; j < 2 * nb; j += CV_THREADS) {
+    uint32_t const i = j >> 1, row = j & 1;
     uint32_t const e = P.bin_entries[bstart + i];
     float4 const* R = P.recs + (e >> 1);
     TriCv ts;
@@ -282,10 +258,11 @@ __device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint
     uint32_t const flags = __float_as_uint(r4.w);
     ts.zcfg = flags & 0x1FFFu;
     ts.nattr = (flags >> 27) & 15u;  // shade class
-    sh.stage[i] = ts;
+    if (row == 0) sh.stage[i] = ts;
     uint32_t const bit = 1u << (i & 31), word = i >> 5;
     if (e & 1u) {  // accepted for the whole tile by the binner
-      for (int r = 0; r < 4; ++r) atomicOr(&sh.mask16[word][r], bit);
+      atomicOr(&sh.mask16[word][2 * row], bit);
+      atomicOr(&sh.mask16[word][2 * row + 1], bit);
       continue;
     }
     float const x_min = ts.bbox.x - tx0f, x_max = ts.bbox.y - tx0f, y_min = ts.bbox.z - ty0f,
@@ -299,7 +276,8 @@ __device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint
     int const jx_hi = min(bx0 + 7, static_cast<int>(floorf(x_max * 0.25f)) + 1);
     int const jy_lo = max(by0, static_cast<int>(floorf(y_min * 0.25f)) - 1);
     int const jy_hi = min(by0 + 7, static_cast<int>(floorf(y_max * 0.25f)) + 1);
-    for (int iy = by0 >> 2; iy < (by0 >> 2) + 2; ++iy) {
+    {
+      int const iy = (by0 >> 2) + static_cast<int>(row);
       int const m16y = iy * 16;
       if (y_min >= static_cast<float>(m16y + 16) || y_max < static_cast<float>(m16y)) continue;
       for (int ix = bx0 >> 2; ix < (bx0 >> 2) + 2; ++ix) {
@@ -336,13 +314,15 @@ __device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint
   }
 }
 
-__global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
+__global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   CvShared& sh = *reinterpret_cast<CvShared*>(smem_raw);
   uint32_t* const ztile = reinterpret_cast<uint32_t*>(smem_raw + ((sizeof(CvShared) + 15) & ~size_t(15)));
   if (P.counters->overflow & (OVF_BIN | OVF_REC)) return;
-  int const tid = threadIdx.x, h = tid & 1, ib = tid >> 1;  // item block 0..63: (ib & 7, ib >> 3)
-  int const ibx = ib & 7, iby = ib >> 3;
+  // item block ib = 0..63 at (ib & 7, ib >> 3); this thread's quad q of it
+  // has its top-left pixel at block pixel (qx0, qy0)
+  int const tid = threadIdx.x, q = tid & 3, ib = tid >> 2;
+  int const ibx = ib & 7, iby = ib >> 3, qx0 = (q & 1) * 2, qy0 = (q >> 1) * 2;
   uint32_t const nitems = P.ntiles * 4;
   OwnerList L{NO_CHUNK, NO_CHUNK, 0};
   for (;;) {
@@ -364,26 +344,23 @@ __global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
       sh.spy[tid] = T.sp_y[tid];
     }
     int const bx = bx0 + ibx, by = by0 + iby;  // this thread's block, tile numbering
-    int const bx_abs = tile_x0 + bx * 4, by_abs = tile_y0 + by * 4;
     int const own16 = (iby >> 2) * 2 + (ibx >> 2);  // its 16x16 region within the quadrant
     L.first = L.cur = NO_CHUNK;
     L.count = 0;
-    Half hf;
-    hf.s0 = S > 1 ? h * (S >> 1) : 0;
-    hf.ns = S > 1 ? (S >> 1) : 1;
-    hf.r0 = S > 1 ? 0 : 2 * h;
-    hf.nr = S > 1 ? 4 : 2;
-    hf.samples = S;
-    for (uint32_t j = 0; j < 2; ++j) {
-      uint32_t const s = min(hf.s0 + j, S - 1);
-      hf.ax[j] = T.sp_x[s] - 0.5f;
-      hf.ay[j] = T.sp_y[s] - 0.5f;
+    Quad qd;
+    qd.x = tile_x0 + bx * 4 + qx0;
+    qd.y = tile_y0 + by * 4 + qy0;
+    qd.samples = S;
+#pragma unroll
+    for (uint32_t s = 0; s < 4; ++s) {
+      uint32_t const sm = min(s, S - 1);
+      qd.ax[s] = T.sp_x[sm] - 0.5f;
+      qd.ay[s] = T.sp_y[sm] - 0.5f;
     }
-    hf.inside = 0;
-    for (int iy = 0; iy < 4; ++iy)
-      for (int ix = 0; ix < 4; ++ix)
-        if (static_cast<uint32_t>(bx_abs + ix) < W && static_cast<uint32_t>(by_abs + iy) < H)
-          hf.inside |= 1u << (iy * 4 + ix);
+    qd.inside = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (static_cast<uint32_t>(qd.x + (i & 1)) < W && static_cast<uint32_t>(qd.y + (i >> 1)) < H) qd.inside |= 1u << i;
     bool const stage_z = T.any_early_z && begin < end;
     bool const d24 = T.ds_fmt == SG_FMT_D24S8;
     uint32_t const qw = min(static_cast<uint32_t>(CV_PX), W - min(W, static_cast<uint32_t>(x0)));
@@ -397,14 +374,21 @@ __global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
         ztile[i] = *reinterpret_cast<uint32_t const*>(ds_addr(T, x0 + x, y0 + y, sm));
       }
     }
-    uint32_t* const zblk = ztile + (iby * 4 * zrow) + ibx * 4 * S;
-    ZRange zr{-INFINITY, INFINITY, 0u, 0xFFFFFFu};
-    bool z_dirty = stage_z;  // the half's depth range is recomputed before a batch's culling when stale
+    uint32_t* const zq = ztile + (iby * 4 + qy0) * zrow + (ibx * 4 + qx0) * S;
+    ZRange zr{-INFINITY, INFINITY, 0u, 0xFFFFFFu};  // the block's
+    bool z_dirty = stage_z;  // the depth range is recomputed before a batch's culling when stale
     if (stage_z) __syncthreads();
     for (uint32_t bstart = begin; bstart < end; bstart += CV_STAGE) {
       uint32_t const nb = min(static_cast<uint32_t>(CV_STAGE), end - bstart);
-      if (z_dirty) {
-        z_range(zblk, static_cast<int>(zrow), hf, d24, zr);
+      if (__any_sync(0xFFFFFFFFu, z_dirty)) {  // the block's range: its four quads' ranges combined
+        z_range(zq, static_cast<int>(zrow), qd, d24, zr);
+#pragma unroll
+        for (int o = 1; o < 4; o <<= 1) {
+          zr.zmax = fmaxf(zr.zmax, __shfl_xor_sync(0xFFFFFFFFu, zr.zmax, o));
+          zr.zmin = fminf(zr.zmin, __shfl_xor_sync(0xFFFFFFFFu, zr.zmin, o));
+          zr.qmax = max(zr.qmax, __shfl_xor_sync(0xFFFFFFFFu, zr.qmax, o));
+          zr.qmin = min(zr.qmin, __shfl_xor_sync(0xFFFFFFFFu, zr.qmin, o));
+        }
         z_dirty = false;
       }
       __syncthreads();
@@ -413,20 +397,24 @@ __global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
       __syncthreads();
       cv_stage(P, T, bstart, nb, tile_x0, tile_y0, bx0, by0, sh);
       __syncthreads();
-      // the block's triangles, without those hidden in both halves
+      // the block's triangles without the hidden ones; the block's four
+      // threads test every fourth triangle each
       uint32_t live[CV_WORDS];
 #pragma unroll
       for (int w = 0; w < CV_WORDS; ++w) {
-        uint32_t m = sh.mask4[w][ib] | sh.mask16[w][own16];
+        uint32_t const m = sh.mask4[w][ib] | sh.mask16[w][own16];
+        uint32_t hid = 0;
         if (stage_z) {
-          uint32_t scan = m;
+          uint32_t scan = m & (0x11111111u << q);
           while (scan) {
             int const b = __ffs(scan) - 1;
             scan &= scan - 1;
-            if (pair_hidden(sh.stage[(w << 5) + b], bx_abs, by_abs, d24, zr)) m &= ~(1u << b);
+            if (pair_hidden(sh.stage[(w << 5) + b], qd.x - qx0, qd.y - qy0, d24, zr)) hid |= 1u << b;
           }
+          hid |= __shfl_xor_sync(0xFFFFFFFFu, hid, 1);
+          hid |= __shfl_xor_sync(0xFFFFFFFFu, hid, 2);
         }
-        live[w] = m | __shfl_xor_sync(0xFFFFFFFFu, m, 1);
+        live[w] = m & ~hid;
       }
       for (;;) {
         // this round's pairs: the block's next CV_K triangles in primitive order
@@ -437,14 +425,14 @@ __global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
           while (live[w] && n < static_cast<uint32_t>(CV_K)) {
             int const b = __ffs(live[w]) - 1;
             live[w] &= live[w] - 1;
-            if (h == 0) sh.slot[ib][n] = static_cast<uint8_t>((w << 5) + b) | static_cast<uint8_t>(((fulls >> b) & 1u) << 7);
+            if (q == 0) sh.slot[ib][n] = static_cast<uint8_t>((w << 5) + b) | static_cast<uint8_t>(((fulls >> b) & 1u) << 7);
             ++n;
           }
         }
         bool more = false;
 #pragma unroll
         for (int w = 0; w < CV_WORDS; ++w) more = more || live[w] != 0;
-        if (h == 0) sh.cnt[ib] = n;
+        if (q == 0) sh.cnt[ib] = n;
         __syncthreads();
         if (tid < 32) {  // offsets of the blocks in the dense pair numbering
           uint32_t const c0 = sh.cnt[2 * tid], c1 = sh.cnt[2 * tid + 1];
@@ -477,19 +465,27 @@ __global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
           sh.cov_cv[b][k] = cv;
         }
         __syncthreads();
-        // each block's pairs in primitive order: early-Z on this half, then the quads
+        // the block's pairs in primitive order on this thread's quad: early-Z,
+        // then the surviving quad into the quad's fragment list
+        uint32_t const fm = (1u << S) - 1u, qfull = fm | (fm << 4) | (fm << 8) | (fm << 12);
         for (uint32_t k = 0; k < n; ++k) {
-          uint32_t const e8 = sh.slot[ib][k];
-          TriCv const& t = sh.stage[e8 & 127u];
-          uint64_t const uc = sh.cov_uc[ib][k], cv = sh.cov_cv[ib][k];
-          uint64_t tz = cv;
-          if ((t.zcfg & 128u) && cv) {
+          uint32_t const e8 = sh.slot[ib][k], idx = e8 & 127u;
+          uint32_t const cq = quad_bits(sh.cov_cv[ib][k], qx0, qy0);
+          if (!cq) continue;
+          TriCv const& t = sh.stage[idx];
+          uint32_t tq = cq;
+          if (t.zcfg & 128u) {
             bool wrote = false;
-            tz = early_z_half(t, cv, bx_abs, by_abs, zblk, static_cast<int>(zrow), hf, wrote);
+            tq = early_z_quad(t, cq, zq, static_cast<int>(zrow), qd, wrote);
             z_dirty = z_dirty || wrote;
           }
-          tz |= __shfl_xor_sync(3u << (tid & 30), tz, 1);
-          if (h == 0 && tz) emit_quads(P, L, t, (e8 >> 7) != 0, bx_abs, by_abs, S, uc, cv, tz);
+          if (!tq) continue;
+          uint32_t const uq = quad_bits(sh.cov_uc[ib][k], qx0, qy0);
+          bool const fullq = (e8 >> 7) ? cq == qfull : (uq == qfull && cq == uq);
+          owner_append(P, L, t.entry >> 1,
+                       (static_cast<uint32_t>(qd.x) >> 1) | ((static_cast<uint32_t>(qd.y) >> 1) << 12) |
+                           (fullq ? 1u << 24 : 0u) | (t.nattr << 25),
+                       tq | (cq << 16));
         }
         if (!__syncthreads_or(more)) break;
       }
@@ -503,14 +499,12 @@ __global__ void __launch_bounds__(CV_THREADS, 4) k_cover2(PassParams P) {
         *reinterpret_cast<uint32_t*>(ds_addr(T, x0 + x, y0 + y, sm)) = ztile[i];
       }
     }
-    // close the block's list for the item
-    if (h == 0) {
-      if (L.cur != NO_CHUNK) {
-        P.chunk_next[L.cur] = NO_CHUNK;
-        P.chunk_count[L.cur] = L.count;
-      }
-      P.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + by * 16 + bx] = L.first;
+    // close the quad's list for the item
+    if (L.cur != NO_CHUNK) {
+      P.chunk_next[L.cur] = NO_CHUNK;
+      P.chunk_count[L.cur] = L.count;
     }
+    P.owner_first[static_cast<size_t>(tile) * QUAD_OWNERS + (by * 2 + (q >> 1)) * 32 + bx * 2 + (q & 1)] = L.first;
   }
 }
 

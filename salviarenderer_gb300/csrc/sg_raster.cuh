@@ -6,7 +6,10 @@
 //             scheduled over every tile of every target; 128 threads.  Each
 //             owned 4x4 block replays, in primitive order, the reference's
 //             64 -> 16 -> 4 -> sample classification, quad coverage and
-//             early-Z.  Surviving quads become fragments in per-owner lists.
+//             early-Z.  Surviving quads become fragments in per-owner lists
+//             (an owner per 2x2 quad of the tile; this kernel fills the list
+//             of each block's top-left quad).  sg_cover.cu's k_cover2 is the
+//             default coverage kernel.
 //   k_shade   every fragment of the pass, 4 lanes per quad (one per pixel):
 //             attribute interpolation and the pixel-shader program, with
 //             ddx/ddy from the quad's lanes.  One instance per varying count.
@@ -636,7 +639,13 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
         P.chunk_next[L.cur] = NO_CHUNK;
         P.chunk_count[L.cur] = L.count;
       }
-      P.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + blk] = L.first;
+      // the block's whole list goes to the owner of its top-left quad; the
+      // block's other quads have none
+      uint32_t* const of = P.owner_first + static_cast<size_t>(tile) * QUAD_OWNERS + (blk >> 4) * 64 + (blk & 15) * 2;
+      of[0] = L.first;
+      of[1] = NO_CHUNK;
+      of[32] = NO_CHUNK;
+      of[33] = NO_CHUNK;
     }
   }
 }
@@ -888,7 +897,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
   if (blockIdx.x == 0 && threadIdx.x == 0 && ovf) atomicOr(P.sticky, ovf);
   if (ovf & OVF_FATAL) return;
   int const lane = threadIdx.x & 31;
-  uint32_t const groups = RASTER_THREADS / 32;  // owner groups per tile
+  uint32_t const groups = QUAD_OWNERS / 32;  // owner groups per tile
   uint32_t cur_draw = 0xFFFFFFFFu;
   unsigned long long backend = 0;
   for (;;) {
@@ -900,7 +909,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
     uint32_t const owner = (unit % groups) * 32 + lane;
     uint32_t c = P.tile_begin[tile] == P.tile_begin[tile + 1]
                      ? NO_CHUNK
-                     : P.owner_first[static_cast<size_t>(tile) * RASTER_THREADS + owner];
+                     : P.owner_first[static_cast<size_t>(tile) * QUAD_OWNERS + owner];
     // the next fragment's header and record flags are read a fragment ahead
     // (they are read-only here), overlapping their latency with the blend
     uint32_t n = c != NO_CHUNK ? __ldg(&P.chunk_count[c]) : 0u, k = 0;
