@@ -4,7 +4,9 @@
 // from a dynamic cursor; a CTA of 256 threads handles one item at a time,
 // four threads per 4x4 block, one per 2x2 quad.  For each batch of the tile's triangles (its
 // bin list, in API order) the CTA
-//   1. stages the batch and classifies every triangle against the
+//   1. stages the batch -- the next CV_STAGE of the tile's triangles whose
+//      bounding box reaches the quadrant, compacted in order from the bin
+//      list -- and classifies every staged triangle against the
 //      quadrant's 16x16 regions and 4x4 blocks with the reference's level-1
 //      and level-2 trivial reject / accept tests (rasterizer.cpp:441-571),
 //      into per-block sets of the triangles reaching the block and of those
@@ -62,6 +64,10 @@ struct CvShared {
   unsigned long long cov_uc[64][CV_K], cov_cv[64][CV_K];
   float spx[4], spy[4];
   uint32_t item;
+  // the batch's bin entries, and the fill's per-warp counts and resume point
+  uint32_t cand[CV_STAGE];
+  uint32_t wcnt[CV_THREADS / 32];
+  uint32_t next;
 };
 // followed by the staged depth: CV_PX * CV_PX * samples words (early-Z only)
 inline size_t cv_smem(uint32_t samples, bool early_z) {
@@ -232,16 +238,64 @@ __device__ inline uint32_t early_z_quad(TriCv const& t, uint32_t cq, uint32_t* z
   return tz;
 }
 
-// Stages a batch of a tile's bin entries and classifies each triangle
-// against the quadrant's regions and blocks (rasterizer.cpp:441-571); two
-// threads per triangle, one per row of 16x16 regions.
-__device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint32_t bstart, uint32_t nb, int tile_x0,
-                                int tile_y0, int bx0, int by0, CvShared& sh) {
+// Fills the batch: from bin entry `bpos` on, the entries whose triangle's
+// bounding box reaches the quadrant (x in [qx0, qx0 + 32), y in [qy0,
+// qy0 + 32) of the tile), in order, at most CV_STAGE of them.  A triangle
+// whose box misses the quadrant misses every one of its regions, so the
+// classification below would give it no bit.  Returns the batch's size and
+// advances `bpos` past the last entry taken (or examined).
+__device__ inline uint32_t cv_fill(PassParams const& P, uint32_t& bpos, uint32_t end, int tile_x0, int tile_y0,
+                                   int qx0, int qy0, CvShared& sh) {
+  float const tx0f = static_cast<float>(tile_x0), ty0f = static_cast<float>(tile_y0);
+  float const xs = static_cast<float>(qx0), xe = xs + CV_PX, ys = static_cast<float>(qy0), ye = ys + CV_PX;
+  int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  uint32_t nst = 0;
+  for (;;) {
+    uint32_t const cand = bpos + tid;
+    uint32_t e = 0;
+    bool reach = false;
+    if (cand < end) {
+      e = P.bin_entries[cand];
+      reach = (e & 1u) != 0;  // accepted for the whole tile by the binner
+      if (!reach) {
+        float4 const bb = P.recs[(e >> 1) + 3];
+        reach = !(bb.x - tx0f >= xe || bb.y - tx0f < xs || bb.z - ty0f >= ye || bb.w - ty0f < ys);
+      }
+    }
+    uint32_t const bal = __ballot_sync(0xFFFFFFFFu, reach);
+    if (lane == 0) sh.wcnt[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t excl = __popc(bal & ((1u << lane) - 1u)), total = 0;
+#pragma unroll
+    for (int w = 0; w < CV_THREADS / 32; ++w) {
+      uint32_t const c = sh.wcnt[w];
+      excl += w < warp ? c : 0u;
+      total += c;
+    }
+    uint32_t const room = CV_STAGE - nst;
+    if (reach && excl < room) sh.cand[nst + excl] = e;
+    if (reach && excl == room) sh.next = cand;
+    __syncthreads();
+    if (total > room) {
+      bpos = sh.next;
+      return CV_STAGE;
+    }
+    nst += total;
+    bpos = min(bpos + CV_THREADS, end);
+    if (nst == CV_STAGE || bpos >= end) return nst;
+  }
+}
+
+// Stages the batch's triangles and classifies each against the quadrant's
+// regions and blocks (rasterizer.cpp:441-571); two threads per triangle, one
+// per row of 16x16 regions.
+__device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint32_t nb, int tile_x0, int tile_y0,
+                                int bx0, int by0, CvShared& sh) {
   float const tx0f = static_cast<float>(tile_x0), ty0f = static_cast<float>(tile_y0);
   float const trr = T.target_w, trb = T.target_h;
   for (uint32_t j = threadIdx.x; j < 2 * nb; j += CV_THREADS) {
     uint32_t const i = j >> 1, row = j & 1;
-    uint32_t const e = P.bin_entries[bstart + i];
+    uint32_t const e = sh.cand[i];
     float4 const* R = P.recs + (e >> 1);
     TriCv ts;
     ts.e0 = R[0];
@@ -378,8 +432,7 @@ __global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
     ZRange zr{-INFINITY, INFINITY, 0u, 0xFFFFFFu};  // the block's
     bool z_dirty = stage_z;  // the depth range is recomputed before a batch's culling when stale
     if (stage_z) __syncthreads();
-    for (uint32_t bstart = begin; bstart < end; bstart += CV_STAGE) {
-      uint32_t const nb = min(static_cast<uint32_t>(CV_STAGE), end - bstart);
+    for (uint32_t bpos = begin; bpos < end;) {
       if (__any_sync(0xFFFFFFFFu, z_dirty)) {  // the block's range: its four quads' ranges combined
         z_range(zq, static_cast<int>(zrow), qd, d24, zr);
 #pragma unroll
@@ -394,8 +447,9 @@ __global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
       __syncthreads();
       uint32_t* const masks = &sh.mask4[0][0];
       for (int i = tid; i < (64 + 64 + 4) * CV_WORDS; i += CV_THREADS) masks[i] = 0;
-      __syncthreads();
-      cv_stage(P, T, bstart, nb, tile_x0, tile_y0, bx0, by0, sh);
+      uint32_t const nb = cv_fill(P, bpos, end, tile_x0, tile_y0, bx0 * 4, by0 * 4, sh);
+      if (nb == 0) break;
+      cv_stage(P, T, nb, tile_x0, tile_y0, bx0, by0, sh);
       __syncthreads();
       // the block's triangles without the hidden ones; the block's four
       // threads test every fourth triangle each
