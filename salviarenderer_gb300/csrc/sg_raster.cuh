@@ -39,29 +39,17 @@ struct TriView {
   __device__ v4 ddy(int i) const { return ld4(R + 5 + 2 * nreg + i); }
 };
 
+// Compare functions: SG_CMP_* are the reference's values (LESS 1, EQUAL 2,
+// GREATER 4 and their unions), so a function passes when the bit of the
+// operands' ordering is set.  Unordered float operands (NaN) pass NOT_EQUAL
+// and ALWAYS only, as `a != b` and `true` do; values above ALWAYS pass.
+// Branch-free: the function is data, and a switch per sample diverges.
 __device__ inline bool cmpf(uint32_t f, float a, float b) {
-  switch (f) {
-  case SG_CMP_NEVER: return false;
-  case SG_CMP_LESS: return a < b;
-  case SG_CMP_EQUAL: return a == b;
-  case SG_CMP_LESS_EQUAL: return a <= b;
-  case SG_CMP_GREATER: return a > b;
-  case SG_CMP_NOT_EQUAL: return a != b;
-  case SG_CMP_GREATER_EQUAL: return a >= b;
-  default: return true;
-  }
+  bool const lt = a < b, eq = a == b, gt = a > b;
+  return ((f & 1u) && lt) || ((f & 2u) && eq) || ((f & 4u) && gt) || ((f & 5u) == 5u && !(lt || eq || gt)) || f > 7u;
 }
 __device__ inline bool cmpu(uint32_t f, uint32_t a, uint32_t b) {
-  switch (f) {
-  case SG_CMP_NEVER: return false;
-  case SG_CMP_LESS: return a < b;
-  case SG_CMP_EQUAL: return a == b;
-  case SG_CMP_LESS_EQUAL: return a <= b;
-  case SG_CMP_GREATER: return a > b;
-  case SG_CMP_NOT_EQUAL: return a != b;
-  case SG_CMP_GREATER_EQUAL: return a >= b;
-  default: return true;
-  }
+  return ((f & 1u) && a < b) || ((f & 2u) && a == b) || ((f & 4u) && a > b) || f > 7u;
 }
 __device__ inline uint32_t stencil_op(uint32_t op, uint32_t ref, uint32_t cur) {  // framebuffer.cpp:136-166
   switch (op) {

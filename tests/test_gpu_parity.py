@@ -70,6 +70,16 @@ def test_depth_extension_formats(gdev, odev, fmt):
     compare(gdev, odev, scenes.c1_scene(width=128, height=128, ntris=400, samples=4, ds_fmt=fmt, seed=31))
 
 
+@pytest.mark.parametrize("ds_fmt", [abi.FMT_RG32F, abi.FMT_D24S8])
+@pytest.mark.parametrize("func", range(8))
+def test_every_depth_function(gdev, odev, func, ds_fmt):
+    """Each SG_CMP_* depth function (NEVER .. ALWAYS) over three overlapping
+    draws, early-Z path, both depth formats; the clear depth sits at the
+    scene's median depth so that every function passes and fails somewhere."""
+    compare(gdev, odev, scenes.feature_scene(seed=50 + func, samples=4, ntris=160, draws=3, depth_func=func,
+                                             clear_depth=0.96, ds_fmt=ds_fmt, blend=abi.BS_LERP_SRC_ALPHA))
+
+
 def test_rgba16f_target(gdev, odev):
     compare(gdev, odev, scenes.feature_scene(seed=41, color_fmt=abi.FMT_RGBA16F, blend=abi.BS_LERP_SRC_ALPHA,
                                              samples=4))
