@@ -200,21 +200,25 @@ __device__ inline v4 lerp4(v4 c0, v4 c1, v4 c2, v4 c3, float tx, float ty) {
   return mk4(r[0], r[1], r[2], r[3]);
 }
 
+// lerp_2d of 8-bit RGBA / BGRA texels (colors.h:340-489)
+__device__ inline v4 lerp_2d_unorm8(bool rgba, uint8_t const* a, uint8_t const* b, uint8_t const* c,
+                                    uint8_t const* d, float tx, float ty) {
+  auto ld = [&](uint8_t const* p) {
+    uint32_t u = *reinterpret_cast<uint32_t const*>(p);
+    float x = static_cast<float>(u & 0xFF), y = static_cast<float>((u >> 8) & 0xFF),
+          z = static_cast<float>((u >> 16) & 0xFF), w = static_cast<float>(u >> 24);
+    return rgba ? mk4(x, y, z, w) : mk4(z, y, x, w);
+  };
+  v4 r = lerp4(ld(a), ld(b), ld(c), ld(d), tx, ty);
+  return r * (1.0f / 255);
+}
+
 // lerp_2d per format (colors.h:340-489)
 __device__ inline v4 lerp_2d(uint32_t fmt, uint8_t const* a, uint8_t const* b, uint8_t const* c,
                              uint8_t const* d, float tx, float ty) {
   switch (fmt) {
   case SG_FMT_RGBA8:
-  case SG_FMT_BGRA8: {
-    auto ld = [&](uint8_t const* p) {
-      uint32_t u = *reinterpret_cast<uint32_t const*>(p);
-      float x = static_cast<float>(u & 0xFF), y = static_cast<float>((u >> 8) & 0xFF),
-            z = static_cast<float>((u >> 16) & 0xFF), w = static_cast<float>(u >> 24);
-      return fmt == SG_FMT_RGBA8 ? mk4(x, y, z, w) : mk4(z, y, x, w);
-    };
-    v4 r = lerp4(ld(a), ld(b), ld(c), ld(d), tx, ty);
-    return r * (1.0f / 255);
-  }
+  case SG_FMT_BGRA8: return lerp_2d_unorm8(fmt == SG_FMT_RGBA8, a, b, c, d, tx, ty);
   case SG_FMT_RGB32F: {
     v4 c0 = read_texel(fmt, a), c1 = read_texel(fmt, b), c2 = read_texel(fmt, c),
        c3 = read_texel(fmt, d);
@@ -539,23 +543,54 @@ __device__ inline void calc_af(dev_sampler const& s, float dxu, float dxv, float
   }
 }
 
+// Whether the sampler's texels are 8-bit RGBA / BGRA and both axes wrap:
+// the state whose linear lookups take surface_bilinear_wrap8.
+__device__ inline bool wrap8_state(dev_sampler const& s) {
+  return (s.fmt == SG_FMT_RGBA8 || s.fmt == SG_FMT_BGRA8) && s.address_u == SG_ADDRESS_WRAP &&
+         s.address_v == SG_ADDRESS_WRAP;
+}
+
+// sample_surface's linear filter for that state, inline: the same
+// addressing and interpolation steps without the per-lookup dispatch on
+// filter, address mode and format.
+__device__ __forceinline__ v4 surface_bilinear_wrap8(dev_sampler const& s, int level, float x, float y) {
+  dev_level const lv = s.lv[level];
+  int const w = lv.w, h = lv.h;
+  int x0, x1, y0, y1;
+  float tx, ty;
+  wrap_linear(x, w, x0, x1, tx);
+  wrap_linear(y, h, y0, y1, ty);
+  bool const ok = x0 >= 0 && x1 >= 0 && y0 >= 0 && y1 >= 0 && x0 < w && x1 < w && y0 < h && y1 < h;
+  if (!ok) return sample_surface(s, level, x, y, SG_FILTER_LINEAR);
+  auto texel = [&](int xx, int yy) -> uint8_t const* { return lv.data + (static_cast<size_t>(yy) * w + xx) * 4; };
+  return lerp_2d_unorm8(s.fmt == SG_FMT_RGBA8, texel(x0, y0), texel(x1, y0), texel(x0, y1), texel(x1, y1), tx, ty);
+}
+
+// One surface lookup of sample_impl; WRAP8: the sampler is in wrap8_state.
+template <bool WRAP8>
+__device__ __forceinline__ v4 surface_lookup(dev_sampler const& s, int level, float x, float y, uint32_t filter) {
+  if (WRAP8 && filter == SG_FILTER_LINEAR) return surface_bilinear_wrap8(s, level, x, y);
+  return sample_surface(s, level, x, y, filter);
+}
+
 // sampler::sample_impl<false> (sampler.cpp:680-764)
-static __device__ __noinline__ v4 sample_impl(dev_sampler const& s, float cx, float cy, float miplevel, af_info const* af) {
+template <bool WRAP8>
+__device__ __forceinline__ v4 sample_impl_t(dev_sampler const& s, float cx, float cy, float miplevel, af_info const* af) {
   int max_lod = 0, min_lod = s.nlevels - 1;
   bool is_mag = (s.mip_filter == SG_FILTER_POINT) ? (miplevel < 0.5f) : (miplevel < 0.0f);
-  if (is_mag) return sample_surface(s, max_lod, cx, cy, s.mag_filter);
+  if (is_mag) return surface_lookup<WRAP8>(s, max_lod, cx, cy, s.mag_filter);
   if (s.mip_filter == SG_FILTER_POINT) {
     int ml = fast_floori(0.5 + static_cast<double>(miplevel));
     ml = iclamp(ml, max_lod, min_lod);
-    return sample_surface(s, ml, cx, cy, s.min_filter);
+    return surface_lookup<WRAP8>(s, ml, cx, cy, s.min_filter);
   }
   if (s.mip_filter == SG_FILTER_LINEAR) {
     int lo = fast_floori(static_cast<double>(miplevel));
     int hi = lo + 1;
     float frac = miplevel - static_cast<float>(lo);
     int lc = iclamp(lo, max_lod, min_lod), hc = iclamp(hi, max_lod, min_lod);
-    v4 c0 = sample_surface(s, lc, cx, cy, s.min_filter);
-    v4 c1 = sample_surface(s, hc, cx, cy, s.min_filter);
+    v4 c0 = surface_lookup<WRAP8>(s, lc, cx, cy, s.min_filter);
+    v4 c1 = surface_lookup<WRAP8>(s, hc, cx, cy, s.min_filter);
     return mk4(lerp1(c0.x, c1.x, frac), lerp1(c0.y, c1.y, frac), lerp1(c0.z, c1.z, frac), lerp1(c0.w, c1.w, frac));
   }
   float start = -0.5f * (af->probe_count - 1.0f);
@@ -568,7 +603,7 @@ static __device__ __noinline__ v4 sample_impl(dev_sampler const& s, float cx, fl
   float wsum = 0.0f;
   int pc = static_cast<int>(af->probe_count);
   for (int i = -pc + 1; i < pc; i += 2) {
-    v4 c0 = sample_surface(s, lvl, sx, sy, s.min_filter);
+    v4 c0 = surface_lookup<WRAP8>(s, lvl, sx, sy, s.min_filter);
     int widx = static_cast<int>(static_cast<float>(i * i) * af->weight_D);
     float w = c_ewa[widx < 0 ? 0 : (widx > 255 ? 255 : widx)];
     color = color + c0 * w;
@@ -578,6 +613,9 @@ static __device__ __noinline__ v4 sample_impl(dev_sampler const& s, float cx, fl
   }
   float inv = 1.0f / wsum;
   return color * inv;
+}
+static __device__ __noinline__ v4 sample_impl(dev_sampler const& s, float cx, float cy, float miplevel, af_info const* af) {
+  return wrap8_state(s) ? sample_impl_t<true>(s, cx, cy, miplevel, af) : sample_impl_t<false>(s, cx, cy, miplevel, af);
 }
 
 __device__ inline float calc_lod_2d(dev_sampler const& s, float dxu, float dxv, float dyu, float dyv) {

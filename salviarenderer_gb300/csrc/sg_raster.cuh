@@ -974,18 +974,26 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
               w[i] = *reinterpret_cast<uint4 const*>(color_addr(T, x, y, 0));
               cc[i] = P.frag_color[static_cast<size_t>(f) * 4 + i];
             }
+          // the blend with the format and program as constants for the
+          // common state (RGBA8, source-alpha lerp), else as data
+          auto blend_quad = [&](uint32_t fmt, uint32_t bs) {
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            uint32_t const pm = static_cast<uint32_t>(m >> (16 * i)) & 0xFu;
-            if (!pm) continue;
-            v4 const src = mk4(cc[i].x, cc[i].y, cc[i].z, cc[i].w);
-            if (pm & 1u) w[i].x = blend_word(T.color_fmt, D.bs_prog, w[i].x, src);
-            if (pm & 2u) w[i].y = blend_word(T.color_fmt, D.bs_prog, w[i].y, src);
-            if (pm & 4u) w[i].z = blend_word(T.color_fmt, D.bs_prog, w[i].z, src);
-            if (pm & 8u) w[i].w = blend_word(T.color_fmt, D.bs_prog, w[i].w, src);
-            uint32_t x = qx + (i & 1), y = qy + (i >> 1);
-            *reinterpret_cast<uint4*>(color_addr(T, x, y, 0)) = w[i];
-          }
+            for (int i = 0; i < 4; ++i) {
+              uint32_t const pm = static_cast<uint32_t>(m >> (16 * i)) & 0xFu;
+              if (!pm) continue;
+              v4 const src = mk4(cc[i].x, cc[i].y, cc[i].z, cc[i].w);
+              if (pm & 1u) w[i].x = blend_word(fmt, bs, w[i].x, src);
+              if (pm & 2u) w[i].y = blend_word(fmt, bs, w[i].y, src);
+              if (pm & 4u) w[i].z = blend_word(fmt, bs, w[i].z, src);
+              if (pm & 8u) w[i].w = blend_word(fmt, bs, w[i].w, src);
+              uint32_t x = qx + (i & 1), y = qy + (i >> 1);
+              *reinterpret_cast<uint4*>(color_addr(T, x, y, 0)) = w[i];
+            }
+          };
+          if (T.color_fmt == SG_FMT_RGBA8 && D.bs_prog == SG_BS_LERP_SRC_ALPHA)
+            blend_quad(SG_FMT_RGBA8, SG_BS_LERP_SRC_ALPHA);
+          else
+            blend_quad(T.color_fmt, D.bs_prog);
           continue;
         }
         for (int i = 0; i < 4; ++i) {
