@@ -536,6 +536,7 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   // learned-filter draws modulate by attribute 1; with fewer varyings the
   // result is zero either way and the plain instance shades them
   p.shade_class = nattr + ((p.ps_prog == SG_PS_TEX_GRAD_LEARNED && nattr >= 2) ? 8u : 0u);
+  p.shade_key = p.shade_class * 8u + (p.ps_prog & 7u);
   p.rec_stride = rec_stride_for(static_cast<int>(nattr));
   for (uint32_t i = 0; i < SG_MAX_VARYINGS; ++i) {
     p.mods[i] = desc->varying_modifiers[i];
@@ -803,7 +804,7 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.frag_mask.ensure(nfrag * 4));
   SG_CUDA(d, sc.frag_color.ensure(nfrag * 4 * sizeof(float4)));
   SG_CUDA(d, sc.frag_ps.ensure(nfrag));
-  SG_CUDA(d, sc.frag_list.ensure((nfrag + 32) * 4));
+  SG_CUDA(d, sc.frag_list.ensure((nfrag + 256) * 4));
   SG_CUDA(d, sc.chunk_next.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.chunk_count.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.owner_first.ensure(static_cast<size_t>(pl.ntiles) * QUAD_OWNERS * 4));

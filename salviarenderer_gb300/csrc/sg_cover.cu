@@ -311,7 +311,7 @@ __device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint
     ts.entry = e;
     uint32_t const flags = __float_as_uint(r4.w);
     ts.zcfg = flags & 0x1FFFu;
-    ts.nattr = (flags >> 27) & 15u;  // shade class
+    ts.nattr = (flags >> 24) & 127u;  // shade key
     if (row == 0) sh.stage[i] = ts;
     uint32_t const bit = 1u << (i & 31), word = i >> 5;
     if (e & 1u) {  // accepted for the whole tile by the binner

@@ -140,7 +140,7 @@ __device__ inline void vp_project(DrawParams const& D, vtx<NA>& v) {
 // rasterizer::compute_triangle_info (rasterizer.cpp:864-945) + compute_derivative_n
 // (shader.cpp:414-449); writes the record, returns false for zero area.
 template <int NA>
-__device__ bool setup_triangle(uint32_t draw, uint32_t zcfg, uint32_t shade_class, vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c,
+__device__ bool setup_triangle(uint32_t draw, uint32_t zcfg, uint32_t shade_key, vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c,
                                float4* rec) {
   vtx<NA> const* verts[3] = {&a, &b, &c};
   double dist[3];
@@ -193,7 +193,7 @@ __device__ bool setup_triangle(uint32_t draw, uint32_t zcfg, uint32_t shade_clas
   rec[1].w = v0.r[0].y;
   rec[2].w = v0.r[0].z;
   rec[4] = make_float4(rec[5 + R].z, rec[5 + 2 * R].z, __uint_as_float(draw),
-                       __uint_as_float(rec_flags(area > 0.0f, shade_class, zcfg)));
+                       __uint_as_float(rec_flags(area > 0.0f, shade_key, zcfg)));
   return true;
 }
 
@@ -206,7 +206,7 @@ __device__ void emit_triangle(PassParams const& P, DrawParams const& D, uint32_t
   vp_project(D, c);
   constexpr uint32_t STRIDE = rec_stride_for(NA);
   alignas(16) float4 rec[STRIDE];
-  bool ok = setup_triangle(draw, D.zcfg, D.shade_class, a, b, c, rec);
+  bool ok = setup_triangle(draw, D.zcfg, D.shade_key, a, b, c, rec);
   uint32_t idx = NO_REC;
   if (ok) {
     idx = atomicAdd(&P.counters->rec_units, STRIDE);
@@ -565,21 +565,32 @@ __global__ void k_tile_order(PassParams P, uint32_t* counts, uint32_t phase) {
   P.tile_order[base + atomicAdd(&counts[32 + b], 1u)] = tile;
 }
 
-// The pass's fragments grouped by shade class, so each shading instance
-// walks only its own (order inside a class is free: every fragment's colour
-// has its own slot).  Phase 0 counts the classes, phase 1 scatters the
-// fragment indices; one atomic per warp and class.
-__global__ void k_frag_classes(PassParams P, uint32_t phase) {
+// The pass's fragments grouped by shade key -- shade class, then pixel-shader
+// program -- so each shading instance walks only its own class, and its
+// warps run one program (order is free: every fragment's colour has its own
+// slot).  Phase 0 counts the keys, phase 1 scatters the fragment indices;
+// one atomic per warp and key.
+__global__ void __launch_bounds__(256) k_frag_classes(PassParams P, uint32_t phase) {
+  __shared__ uint32_t base[128];
   if (P.counters->overflow & OVF_FATAL) return;
   uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
-  uint32_t base[16];
-  if (phase == 1) {
-    uint32_t acc = 0;
+  if (phase == 1) {  // exclusive scan of the 128 key sizes
+    if (threadIdx.x < 32) {
+      uint32_t const* c = P.class_counts + 4 * threadIdx.x;
+      uint32_t const c0 = c[0], c1 = c[1], c2 = c[2], c3 = c[3];
+      uint32_t incl = c0 + c1 + c2 + c3;
 #pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      base[c] = acc;
-      acc += P.class_counts[c];
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t const y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (static_cast<int>(threadIdx.x) >= o) incl += y;
+      }
+      uint32_t const excl = incl - (c0 + c1 + c2 + c3);
+      base[4 * threadIdx.x] = excl;
+      base[4 * threadIdx.x + 1] = excl + c0;
+      base[4 * threadIdx.x + 2] = excl + c0 + c1;
+      base[4 * threadIdx.x + 3] = excl + c0 + c1 + c2;
     }
+    __syncthreads();
   }
   int const lane = threadIdx.x & 31;
   uint32_t const stride = gridDim.x * blockDim.x;
@@ -587,13 +598,13 @@ __global__ void k_frag_classes(PassParams P, uint32_t phase) {
   for (uint32_t it = 0; it < rounds; ++it) {
     uint32_t const f = blockIdx.x * blockDim.x + threadIdx.x + it * stride;
     bool const live = f < nfrag && (f % FRAG_CHUNK) < P.chunk_count[f / FRAG_CHUNK];
-    uint32_t const cls = live ? (P.frag_pos[f] >> 25) & 15u : 16u;
+    uint32_t const cls = live ? P.frag_pos[f] >> 25 : 128u;  // the shade key
     unsigned const same = __match_any_sync(0xFFFFFFFFu, cls);
     int const leader = __ffs(same) - 1;
     if (!live) continue;
     uint32_t first = 0;
     if (lane == leader)
-      first = atomicAdd(&P.class_counts[(phase == 0 ? 0u : 16u) + cls], static_cast<unsigned>(__popc(same)));
+      first = atomicAdd(&P.class_counts[(phase == 0 ? 0u : 128u) + cls], static_cast<unsigned>(__popc(same)));
     if (phase == 0) continue;
     first = __shfl_sync(same, first, leader);
     P.frag_list[base[cls] + first + __popc(same & ((1u << lane) - 1u))] = f;
@@ -630,7 +641,7 @@ void launch_tile_ranges(PassParams const& P, cudaStream_t s) {
 }
 // P.frag_list / P.class_counts (zeroed here) in scratch.
 cudaError_t launch_frag_classes(PassParams const& P, uint32_t num_sms, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(P.class_counts, 0, 32 * sizeof(uint32_t), s);
+  cudaError_t e = cudaMemsetAsync(P.class_counts, 0, 256 * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
   k_frag_classes<<<num_sms * 4, 256, 0, s>>>(P, 0u);
   k_frag_classes<<<num_sms * 4, 256, 0, s>>>(P, 1u);

@@ -94,6 +94,7 @@ struct DrawParams {
   uint32_t target;              // index into the pass's targets
   uint32_t nattr, rec_stride;
   uint32_t shade_class;         // nattr, plus 8 for learned-filter draws: which k_shade instance runs it
+  uint32_t shade_key;           // shade_class * 8 + the pixel-shader program: fragments are shaded grouped by it
   // shaders
   uint32_t vs_prog, ps_prog, bs_prog;
   float vs_k[SG_MAX_SHADER_CONSTANTS];
@@ -137,9 +138,9 @@ struct PassParams {
   uint32_t* bin_entries;        // rec << 1 | tile-accept, per tile in API order
   uint32_t* tile_begin;         // per global tile [begin, end) into bin_entries
   uint32_t* tile_order;         // the tiles, costliest first (k_tile_order); null: index order
-  // the pass's fragments by shade class (k_frag_classes): frag_list holds
-  // the fragment indices of class 0, then class 1, ...; class_counts[0..15]
-  // the classes' sizes, [16..31] the fill cursors.  Null: walk every slot.
+  // the pass's fragments by shade key (k_frag_classes): frag_list holds the
+  // fragment indices of key 0, then key 1, ...; class_counts[0..127] the
+  // keys' sizes, [128..255] the fill cursors.  Null: walk every slot.
   uint32_t* frag_list;
   uint32_t* class_counts;
   uint32_t bin_capacity;
@@ -150,7 +151,7 @@ struct PassParams {
   // first chunk, chunk_next links them, chunk_count says how many slots of a
   // chunk are used.
   uint32_t* frag_rec;           // triangle record
-  uint32_t* frag_pos;           // bits 0-11 x/2, 12-23 y/2 (absolute quad), 24 full quad, 25-28 shade class
+  uint32_t* frag_pos;           // bits 0-11 x/2, 12-23 y/2 (absolute quad), 24 full quad, 25-31 shade key
   uint32_t* frag_mask;          // bits 0-15 early-Z-tested samples, 16-31 covered samples
   float4* frag_color;           // 4 pixels per fragment, pixel-shader output
   uint8_t* frag_ps;             // pixel-shader pass mask (4 bits)
@@ -190,10 +191,14 @@ constexpr uint32_t AF_NET_UNITS = 8;
 // Slots 0-4 hold everything coverage and early-Z read.
 __host__ __device__ constexpr uint32_t rec_stride_for(int nattr) { return 5 + 3 * (1 + nattr); }
 
-// flags: the draw's zcfg (bits 0-12), shade class (27-30), front face (31)
-__host__ __device__ inline uint32_t rec_flags(bool front, uint32_t shade_class, uint32_t zcfg) {
-  return (zcfg & 0x1FFFu) | (shade_class << 27) | (front ? 0x80000000u : 0u);
+// flags: the draw's zcfg (bits 0-12), shade key (24-30: shade class in
+// 27-30, pixel-shader program in 24-26), front face (31)
+__host__ __device__ inline uint32_t rec_flags(bool front, uint32_t shade_key, uint32_t zcfg) {
+  return (zcfg & 0x1FFFu) | ((shade_key & 127u) << 24) | (front ? 0x80000000u : 0u);
 }
+// a fragment's position word: x / 2 (bits 0-11), y / 2 (12-23), fully
+// covered (24), shade key (25-31: shade class in 28-31)
+__device__ inline uint32_t frag_class(uint32_t pos) { return pos >> 28; }
 __device__ inline uint32_t rec_draw(float4 const* R) { return __float_as_uint(R[4].z); }
 __device__ inline uint32_t rec_flag_bits(float4 const* R) { return __float_as_uint(R[4].w); }
 

@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
         ts.dpy = R[5 + 2 * nreg];
         ts.entry = e;
         ts.zcfg = D.zcfg;
-        ts.nattr = D.shade_class;
+        ts.nattr = D.shade_key;
         ts.pad = 0;
         stage[i] = ts;
         uint32_t bit = 1u << (i & 31), word = i >> 5;
@@ -696,12 +696,12 @@ __global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
   bool const with_b = !LEARNED && !P.af_capacity;
   uint32_t base_a = 0, n_a = 0, base_b = 0, n_b = 0;
   if (P.frag_list) {
-    uint32_t acc = 0;
-    for (uint32_t c = 0; c < 16; ++c) {
-      uint32_t const k = P.class_counts[c];
-      if (c == cls_a) base_a = acc, n_a = k;
-      if (with_b && c == NA + 8u) base_b = acc, n_b = k;
-      acc += k;
+    for (uint32_t key = 0; key < 128; ++key) {  // class c: keys [8c, 8c + 8)
+      uint32_t const k = P.class_counts[key], c = key >> 3;
+      if (c < cls_a) base_a += k;
+      if (c == cls_a) n_a += k;
+      if (c < NA + 8u) base_b += k;
+      if (with_b && c == NA + 8u) n_b += k;
     }
   }
   uint32_t const total = P.frag_list ? n_a + n_b : nfrag;
@@ -721,7 +721,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
       live = f < nfrag && (f % FRAG_CHUNK) < P.chunk_count[f / FRAG_CHUNK];
     }
     uint32_t pos = live ? P.frag_pos[f] : 0u;
-    uint32_t const cls = (pos >> 25) & 15u;
+    uint32_t const cls = frag_class(pos);
     live = live && (cls == cls_a || (with_b && cls == NA + 8u));
     uint32_t draw = 0xFFFFFFFFu;
     // learned instances: the pixel's lookup, for the network's queue (af_net)
