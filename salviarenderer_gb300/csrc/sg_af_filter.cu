@@ -60,20 +60,42 @@ __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassP
   uint32_t const tm = s.tmem;
   uint32_t phase = 0;
   bool ok = true;
-  for (uint32_t t0 = blockIdx.x * AF_TILE; t0 < n && ok; t0 += gridDim.x * AF_TILE) {
+  uint32_t const stride = gridDim.x * AF_TILE;
+  // a tile's records (feature row, tap mean, pixel and draw, modulation) are
+  // read one tile ahead: they arrive while the previous tile's layers run
+  uint4 nx[AF_K1 / 8];
+  float4 nskip, nr1, nmod;
+  auto fetch = [&](uint32_t t) {
+    uint32_t const r = t + tid;
+#pragma unroll
+    for (int j = 0; j < AF_K1 / 8; ++j) nx[j] = make_uint4(0, 0, 0, 0);
+    nskip = nr1 = nmod = make_float4(0, 0, 0, 0);
+    if (r < n) {
+      float4 const* L = P.af_net + static_cast<size_t>(r) * AF_NET_UNITS;
+      uint4 const* X = reinterpret_cast<uint4 const*>(L);
+#pragma unroll
+      for (int j = 0; j < AF_K1 / 8; ++j) nx[j] = X[j];
+      nskip = L[4];
+      nr1 = L[6];
+      nmod = L[7];
+    }
+  };
+  fetch(blockIdx.x * AF_TILE);
+  for (uint32_t t0 = blockIdx.x * AF_TILE; t0 < n && ok; t0 += stride) {
     uint32_t const row = t0 + tid;
     bool const valid = row < n;
     // the lookup's feature row (formed by k_shade) into the A tile
-    float4 skip = make_float4(0, 0, 0, 0), r1 = make_float4(0, 0, 0, 0), mod = make_float4(0, 0, 0, 0);
-    float4 const* L = P.af_net + static_cast<size_t>(row) * AF_NET_UNITS;
-    uint4 const* X = reinterpret_cast<uint4 const*>(L);
 #pragma unroll
-    for (int j = 0; j < AF_K1 / 8; ++j)
-      *reinterpret_cast<uint4*>(s.x + tile_off(tid, 8 * j, AF_K1)) = valid ? X[j] : make_uint4(0, 0, 0, 0);
+    for (int j = 0; j < AF_K1 / 8; ++j) *reinterpret_cast<uint4*>(s.x + tile_off(tid, 8 * j, AF_K1)) = nx[j];
+    float4 const skip = nskip, r1 = nr1, mod = nmod;
+    if (t0 + stride < n) fetch(t0 + stride);
+    // the draw's confidence threshold and texel format, read before the layers
+    float thr = 0.0f;
+    bool unorm = false;
     if (valid) {
-      skip = L[4];
-      r1 = L[6];
-      mod = L[7];
+      DrawParams const& D = P.draws[__float_as_uint(r1.w)];
+      thr = D.ps_k[0];
+      unorm = unorm_format(D.ps_samp.fmt);
     }
     fence_async_smem();
     tc_fence_before();
@@ -101,15 +123,14 @@ __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassP
     tmem_ld16(lane_addr(tm, 0), v);
     bool fallback = false;
     if (valid && ok) {
-      DrawParams const& D = P.draws[__float_as_uint(r1.w)];
       float const conf = 1.0f / (1.0f + expf(-(v[4] + s.b3[4])));
-      if (conf >= D.ps_k[0]) {
+      if (conf >= thr) {
         float c[4];
-#pragma unroll
         float const k4[4] = {skip.x, skip.y, skip.z, skip.w};
+#pragma unroll
         for (int i = 0; i < 4; ++i) {
           c[i] = k4[i] + (v[i] + s.b3[i]);
-          if (unorm_format(D.ps_samp.fmt)) c[i] = fminf(fmaxf(c[i], 0.0f), 1.0f);
+          if (unorm) c[i] = fminf(fmaxf(c[i], 0.0f), 1.0f);
         }
         P.frag_color[__float_as_uint(r1.z)] = make_float4(c[0] * mod.x, c[1] * mod.y, c[2] * mod.z, c[3] * mod.w);
       } else {
