@@ -681,9 +681,11 @@ __device__ inline bool af_takes(DrawParams const& D, float dxu, float dxv, float
 // with the centroid adjustment, shader.cpp:208-367, rasterizer.cpp:1363-1398)
 // and the pixel shader, for every fragment of the pass whose draw has NA
 // varyings.  The LEARNED instances take the SG_PS_TEX_GRAD_LEARNED draws
-// (shade class 8 + NA) and queue the lookups the learned filter applies to.
+// (shade class 8 + NA) and queue the lookups the learned filter applies to;
+// they wait mostly on texture taps and queue atomics, so they run 4 CTAs per
+// SM (64 registers) where the plain instances run 3.
 template <int NA, bool LEARNED>
-__global__ void __launch_bounds__(256, 3) k_shade(PassParams P) {
+__global__ void __launch_bounds__(256, LEARNED ? 4 : 3) k_shade(PassParams P) {
   if (P.counters->overflow & OVF_FATAL) return;
   uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
   int const q = threadIdx.x & 3;
