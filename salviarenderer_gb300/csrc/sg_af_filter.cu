@@ -22,15 +22,18 @@
 namespace sg {
 
 // One activation tile serves both hidden layers: layer 2's MMA has read h1
-// by the time its epilogue writes h2 over it.
+// by the time its epilogue writes h2 over it.  `rec` receives a tile's
+// queue records by one bulk copy, issued for the next tile as soon as the
+// threads have taken the current one out.
 struct FilterSmem {
+  float4 rec[AF_TILE * AF_NET_UNITS];
   uint8_t w1[AF_H * AF_K1 * 2], w2[AF_H * AF_H * 2], w3[AF_N3 * AF_H * 2];
   uint8_t x[AF_TILE * AF_K1 * 2], h[AF_TILE * AF_H * 2];
   float b1[AF_H], b2[AF_H], b3[AF_N3];
-  uint64_t bar;
+  uint64_t bar, lbar;
   uint32_t tmem;
 };
-constexpr uint32_t FILTER_CTAS_PER_SM = 5;  // 39 KB of shared memory each
+constexpr uint32_t FILTER_CTAS_PER_SM = 4;  // 55 KB of shared memory each
 // Every layer's accumulator at column 0: each epilogue has read the previous
 // one (tcgen05.wait::ld) before the barrier that precedes the next MMA.
 constexpr uint32_t FILTER_TMEM_COLS = 64;
@@ -44,8 +47,19 @@ __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassP
   extern __shared__ __align__(128) uint8_t smem_raw[];
   FilterSmem& s = *reinterpret_cast<FilterSmem*>(smem_raw);
   uint32_t const tid = threadIdx.x;
+  uint32_t const stride = gridDim.x * AF_TILE;
+  // thread 0: the records of the tile at `t` into s.rec
+  auto issue = [&](uint32_t t) {
+    uint32_t const bytes = min(static_cast<uint32_t>(AF_TILE), n - t) * AF_NET_UNITS * static_cast<uint32_t>(sizeof(float4));
+    mbar_expect_tx(&s.lbar, bytes);
+    bulk_g2s(s.rec, P.af_net + static_cast<size_t>(t) * AF_NET_UNITS, bytes, &s.lbar);
+  };
   if (tid < 32) tmem_alloc(&s.tmem, FILTER_TMEM_COLS);
-  if (tid == 0) mbar_init(&s.bar, 1);
+  if (tid == 0) {
+    mbar_init(&s.bar, 1);
+    mbar_init(&s.lbar, 1);
+    issue(blockIdx.x * AF_TILE);
+  }
   copy16(s.w1, M.img + AF_IMG_W1, sizeof(s.w1));
   copy16(s.w2, M.img + AF_IMG_W2, sizeof(s.w2));
   copy16(s.w3, M.img + AF_IMG_W3, sizeof(s.w3));
@@ -58,37 +72,43 @@ __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassP
   __syncthreads();
   tc_fence_after();
   uint32_t const tm = s.tmem;
-  uint32_t phase = 0;
-  bool ok = true;
-  uint32_t const stride = gridDim.x * AF_TILE;
-  // a tile's records (feature row, tap mean, pixel and draw, modulation) are
-  // read one tile ahead: they arrive while the previous tile's layers run
-  uint4 nx[AF_K1 / 8];
-  float4 nskip, nr1, nmod;
-  auto fetch = [&](uint32_t t) {
-    uint32_t const r = t + tid;
-#pragma unroll
-    for (int j = 0; j < AF_K1 / 8; ++j) nx[j] = make_uint4(0, 0, 0, 0);
-    nskip = nr1 = nmod = make_float4(0, 0, 0, 0);
-    if (r < n) {
-      float4 const* L = P.af_net + static_cast<size_t>(r) * AF_NET_UNITS;
-      uint4 const* X = reinterpret_cast<uint4 const*>(L);
-#pragma unroll
-      for (int j = 0; j < AF_K1 / 8; ++j) nx[j] = X[j];
-      nskip = L[4];
-      nr1 = L[6];
-      nmod = L[7];
-    }
-  };
-  fetch(blockIdx.x * AF_TILE);
+  uint32_t phase = 0, lphase = 0;
+  bool ok = true, inflight = true;  // inflight: a bulk copy into s.rec not yet waited for
   for (uint32_t t0 = blockIdx.x * AF_TILE; t0 < n && ok; t0 += stride) {
     uint32_t const row = t0 + tid;
     bool const valid = row < n;
-    // the lookup's feature row (formed by k_shade) into the A tile
+    if (__syncthreads_or(!mbar_wait(&s.lbar, lphase))) {  // the CTA leaves together
+      ok = false;
+      break;
+    }
+    lphase ^= 1u;
+    inflight = false;
+    // this row's record: the feature row into the A tile, the tap mean,
+    // pixel and draw, and modulation into registers (units read in an order
+    // rotated by row, so that the threads of a warp hit distinct banks)
+    float4 skip = make_float4(0, 0, 0, 0), r1 = skip, mod = skip;
 #pragma unroll
-    for (int j = 0; j < AF_K1 / 8; ++j) *reinterpret_cast<uint4*>(s.x + tile_off(tid, 8 * j, AF_K1)) = nx[j];
-    float4 const skip = nskip, r1 = nr1, mod = nmod;
-    if (t0 + stride < n) fetch(t0 + stride);
+    for (uint32_t j = 0; j < AF_NET_UNITS; ++j) {
+      uint32_t const u = (j + tid) & (AF_NET_UNITS - 1);
+      if (u == 5) continue;  // the plain sampler's coordinates: for the fallback only
+      float4 const v = valid ? s.rec[tid * AF_NET_UNITS + u] : make_float4(0, 0, 0, 0);
+      if (u < AF_K1 / 8)
+        *reinterpret_cast<float4*>(s.x + tile_off(tid, 8 * u, AF_K1)) = v;
+      else if (u == 4)
+        skip = v;
+      else if (u == 6)
+        r1 = v;
+      else
+        mod = v;
+    }
+    __syncthreads();  // s.rec is free: the next tile's records come in during this tile's layers
+    if (t0 + stride < n) {
+      if (tid == 0) {
+        fence_async_smem();
+        issue(t0 + stride);
+      }
+      inflight = true;
+    }
     // the draw's confidence threshold and texel format, read before the layers
     float thr = 0.0f;
     bool unorm = false;
@@ -150,6 +170,8 @@ __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassP
     __syncthreads();
   }
   if (!ok && tid == 0) atomicOr(&P.counters->overflow, OVF_AF_TIMEOUT);
+  // a copy still in flight (after a timeout) lands before the CTA ends
+  if (inflight) mbar_wait(&s.lbar, lphase);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();

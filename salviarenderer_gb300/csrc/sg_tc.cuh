@@ -68,6 +68,20 @@ __device__ inline bool mbar_wait(uint64_t* bar, uint32_t phase) {
   return true;
 }
 
+// ---- bulk copies (untiled TMA) --------------------------------------------------
+// This thread's arrival on `bar`, which then also waits for `bytes` of copies.
+__device__ inline void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Copies `bytes` (a multiple of 16; both addresses 16-byte aligned) from
+// global memory into this CTA's shared memory, completing on `bar`.
+__device__ inline void bulk_g2s(void* dst, void const* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
 // ---- tensor memory -------------------------------------------------------------
 // Allocates `ncols` columns (power of two, >= 32); one whole warp calls it.
 __device__ inline void tmem_alloc(uint32_t* slot, uint32_t ncols) {
