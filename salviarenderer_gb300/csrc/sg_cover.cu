@@ -58,7 +58,8 @@ struct CvShared {
   uint32_t mask4[CV_WORDS][64], mask4f[CV_WORDS][64], mask16[CV_WORDS][4];
   // the round's pairs: per block up to CV_K staged-triangle indices (bit 7:
   // the block is covered fully), their count, the blocks' offsets into the
-  // dense pair numbering, and each pair's coverage (uncut, cut to the target)
+  // dense pair numbering, and each pair's coverage (uncut, cut to the
+  // target; quad-major, so quad q's 16 bits are its 16-bit word q)
   uint8_t slot[64][CV_K];
   uint32_t cnt[64], off[65];
   unsigned long long cov_uc[64][CV_K], cov_cv[64][CV_K];
@@ -152,9 +153,14 @@ __device__ inline bool pair_hidden(TriCv const& t, int bx, int by, bool d24, ZRa
   return (zc & 128u) && (((zc >> 4) & 1u) || func == SG_CMP_NEVER) && z_culled(t, bx, by, func, d24, zr);
 }
 
+// Nibble of block pixel (ix, iy) in a quad-major block mask: quad
+// q = (iy / 2) * 2 + ix / 2, then pixel i = (iy % 2) * 2 + ix % 2 of the quad.
+__host__ __device__ constexpr int qnib(int ix, int iy) { return ((iy >> 1) * 2 + (ix >> 1)) * 4 + (iy & 1) * 2 + (ix & 1); }
+
 // Per-sample coverage of a whole 4x4 block (draw_partial_tile's edge test,
 // rasterizer.cpp:298-439): 4 bits (samples) per pixel, pixel (ix, iy) at
-// nibble iy * 4 + ix; `uc` uncut, `cv` cut to the pixels inside the target.
+// nibble qnib(ix, iy); `uc` uncut, `cv` cut to the pixels inside the target
+// (`inside`: bit qnib(ix, iy)).
 __device__ inline void block_coverage(TriCv const& t, bool full, int bx_abs, int by_abs, uint32_t S, float const* spx,
                                       float const* spy, uint32_t inside, uint64_t& uc, uint64_t& cv) {
   uc = 0;
@@ -172,6 +178,7 @@ __device__ inline void block_coverage(TriCv const& t, bool full, int bx_abs, int
     for (int s = 0; s < 4; ++s) {
       if (s >= static_cast<int>(S)) break;
       float const sx = spx[s], sy = spy[s];
+#pragma unroll
       for (int iy = 0; iy < 4; ++iy) {
         float const my = sy + static_cast<float>(iy);
 #pragma unroll
@@ -180,7 +187,7 @@ __device__ inline void block_coverage(TriCv const& t, bool full, int bx_abs, int
           bool rej = false;
 #pragma unroll
           for (int k = 0; k < 3; ++k) rej = rej || ((mx * e[k].x + my * e[k].y) < ev[k]);
-          uc |= static_cast<uint64_t>(!rej) << ((iy * 4 + ix) * 4 + s);
+          uc |= static_cast<uint64_t>(!rej) << (qnib(ix, iy) * 4 + s);
         }
       }
     }
@@ -193,12 +200,10 @@ __device__ inline void block_coverage(TriCv const& t, bool full, int bx_abs, int
   cv = uc & im;
 }
 
-// A quad's 16 coverage bits (4 per pixel i, in quad order) out of a block's
-// 64 (4 per pixel, nibble iy * 4 + ix); the quad's top-left pixel is block
-// pixel (qx, qy).
-__device__ inline uint32_t quad_bits(uint64_t m, int qx, int qy) {
-  return (static_cast<uint32_t>(m >> ((qy * 4 + qx) * 4)) & 0xFFu) |
-         ((static_cast<uint32_t>(m >> ((qy * 4 + 4 + qx) * 4)) & 0xFFu) << 8);
+// Quad q's 16 coverage bits (4 per pixel i, in quad order) of a quad-major
+// block mask in shared memory.
+__device__ inline uint32_t quad_bits(unsigned long long const& m, int q) {
+  return reinterpret_cast<uint16_t const*>(&m)[q];
 }
 
 // Early-Z of one pair on this thread's quad (framebuffer.cpp:522-614)
@@ -512,7 +517,7 @@ __global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
           uint32_t inside = 0;
           for (int iy = 0; iy < 4; ++iy)
             for (int ix = 0; ix < 4; ++ix)
-              if (static_cast<uint32_t>(pbx + ix) < W && static_cast<uint32_t>(pby + iy) < H) inside |= 1u << (iy * 4 + ix);
+              if (static_cast<uint32_t>(pbx + ix) < W && static_cast<uint32_t>(pby + iy) < H) inside |= 1u << qnib(ix, iy);
           uint64_t uc, cv;
           block_coverage(sh.stage[e8 & 127u], (e8 >> 7) != 0, pbx, pby, S, sh.spx, sh.spy, inside, uc, cv);
           sh.cov_uc[b][k] = uc;
@@ -524,7 +529,7 @@ __global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
         uint32_t const fm = (1u << S) - 1u, qfull = fm | (fm << 4) | (fm << 8) | (fm << 12);
         for (uint32_t k = 0; k < n; ++k) {
           uint32_t const e8 = sh.slot[ib][k], idx = e8 & 127u;
-          uint32_t const cq = quad_bits(sh.cov_cv[ib][k], qx0, qy0);
+          uint32_t const cq = quad_bits(sh.cov_cv[ib][k], q);
           if (!cq) continue;
           TriCv const& t = sh.stage[idx];
           uint32_t tq = cq;
@@ -534,7 +539,7 @@ __global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
             z_dirty = z_dirty || wrote;
           }
           if (!tq) continue;
-          uint32_t const uq = quad_bits(sh.cov_uc[ib][k], qx0, qy0);
+          uint32_t const uq = quad_bits(sh.cov_uc[ib][k], q);
           bool const fullq = (e8 >> 7) ? cq == qfull : (uq == qfull && cq == uq);
           owner_append(P, L, t.entry >> 1,
                        (static_cast<uint32_t>(qd.x) >> 1) | ((static_cast<uint32_t>(qd.y) >> 1) << 12) |
