@@ -209,10 +209,14 @@ __device__ inline uint32_t quad_bits(unsigned long long const& m, int q) {
 // Early-Z of one pair on this thread's quad (framebuffer.cpp:522-614)
 // against the staged depth: returns the passing samples of the covered ones
 // `cq` and writes depth on pass.
+// FUNC: the depth function when known at compile time (LESS or LESS_EQUAL,
+// which read depth), else -1 and it and the depth format are read from
+// the draw's configuration per sample.
+template <int FUNC, bool D24>
 __device__ inline uint32_t early_z_quad(TriCv const& t, uint32_t cq, uint32_t* zq, int zrow, Quad const& qd,
                                         bool& wrote) {
   uint32_t const S = qd.samples, zc = t.zcfg, func = (zc >> 8) & 15u;
-  bool const rd = (zc >> 4) & 1u, wr = (zc >> 5) & 1u, d24 = (zc >> 6) & 1u;
+  bool const rd = (zc >> 4) & 1u, wr = (zc >> 5) & 1u, d24 = FUNC < 0 ? ((zc >> 6) & 1u) != 0 : D24;
   // step_2d_unproj_pos_quad's z (shader.cpp:257-287)
   float const dx = 0.5f + static_cast<float>(qd.x) - t.p0x;
   float const dy = 0.5f + static_cast<float>(qd.y) - t.p0y;
@@ -229,8 +233,14 @@ __device__ inline uint32_t early_z_quad(TriCv const& t, uint32_t cq, uint32_t* z
       if (!(pbits & (1u << s))) continue;  // coverage holds samples below S only
       float const nd = S == 1 ? z : (qd.ax[s] * t.dzx + qd.ay[s] * t.dzy) + z;
       uint32_t const w = zp[s];
-      bool const pass = d24 ? cmpu(func, d24_quantize(nd), rd ? (w & 0xFFFFFFu) : 0u)
-                            : cmpf(func, nd, rd ? __uint_as_float(w) : 0.0f);
+      bool pass;
+      if constexpr (FUNC == SG_CMP_LESS)
+        pass = D24 ? d24_quantize(nd) < (w & 0xFFFFFFu) : nd < __uint_as_float(w);
+      else if constexpr (FUNC == SG_CMP_LESS_EQUAL)
+        pass = D24 ? d24_quantize(nd) <= (w & 0xFFFFFFu) : nd <= __uint_as_float(w);
+      else
+        pass = d24 ? cmpu(func, d24_quantize(nd), rd ? (w & 0xFFFFFFu) : 0u)
+                   : cmpf(func, nd, rd ? __uint_as_float(w) : 0.0f);
       if (pass) {
         if (wr) {
           zp[s] = d24 ? ((w & 0xFF000000u) | d24_quantize(nd)) : __float_as_uint(nd);
@@ -535,7 +545,18 @@ __global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
           uint32_t tq = cq;
           if (t.zcfg & 128u) {
             bool wrote = false;
-            tq = early_z_quad(t, cq, zq, static_cast<int>(zrow), qd, wrote);
+            // the common depth functions with the compare as code, not data
+            uint32_t const zc = t.zcfg, func = (zc >> 8) & 15u;
+            bool const d24z = (zc >> 6) & 1u;
+            int const zr_ = static_cast<int>(zrow);
+            if (func == SG_CMP_LESS)
+              tq = d24z ? early_z_quad<SG_CMP_LESS, true>(t, cq, zq, zr_, qd, wrote)
+                        : early_z_quad<SG_CMP_LESS, false>(t, cq, zq, zr_, qd, wrote);
+            else if (func == SG_CMP_LESS_EQUAL)
+              tq = d24z ? early_z_quad<SG_CMP_LESS_EQUAL, true>(t, cq, zq, zr_, qd, wrote)
+                        : early_z_quad<SG_CMP_LESS_EQUAL, false>(t, cq, zq, zr_, qd, wrote);
+            else
+              tq = early_z_quad<-1, false>(t, cq, zq, zr_, qd, wrote);
             z_dirty = z_dirty || wrote;
           }
           if (!tq) continue;
