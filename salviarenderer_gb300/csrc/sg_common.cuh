@@ -277,6 +277,14 @@ struct dev_sampler {
 static __constant__ float c_ewa[256];
 
 // addressers, SSE paths (sampler.cpp:19-393)
+// a / fs for a texture size fs (a positive integer below 2^24): by a power
+// of two the quotient is exact either way, so it is the product with the
+// reciprocal (an exponent change) -- the same float without a division.
+__device__ inline float div_by_size(float a, float fs) {
+  uint32_t const b = __float_as_uint(fs);
+  if ((b & 0x7FFFFFu) == 0u) return a * __uint_as_float(0x7F000000u - b);
+  return a / fs;
+}
 __device__ inline void wrap_linear(float coord, int size, int& lo, int& hi, float& frac) {
   float c0 = coord - static_cast<float>(cvtt(coord));
   float fs = static_cast<float>(size);
@@ -287,7 +295,7 @@ __device__ inline void wrap_linear(float coord, int size, int& lo, int& hi, floa
   frac = c0 - ip;
   float big = fs * 8192.0f;
   float a0 = (ip + 0.0f) + big, a1 = (ip + 1.0f) + big;
-  float d0 = static_cast<float>(cvtt(a0 / fs)), d1 = static_cast<float>(cvtt(a1 / fs));
+  float d0 = static_cast<float>(cvtt(div_by_size(a0, fs))), d1 = static_cast<float>(cvtt(div_by_size(a1, fs)));
   lo = cvtt(a0 - d0 * fs);
   hi = cvtt(a1 - d1 * fs);
 }
@@ -335,7 +343,7 @@ __device__ inline int wrap_point(float coord, int size) {
   float ip = static_cast<float>(cvtt(c));
   if (ip > c) ip = ip - 1.0f;
   float a = ip + fs * 8192.0f;
-  float dv = static_cast<float>(cvtt(a / fs));
+  float dv = static_cast<float>(cvtt(div_by_size(a, fs)));
   return cvtt(a - dv * fs);
 }
 __device__ inline int mirror_point(float coord, int size) {

@@ -80,6 +80,17 @@ def test_every_depth_function(gdev, odev, func, ds_fmt):
                                              clear_depth=0.96, ds_fmt=ds_fmt, blend=abi.BS_LERP_SRC_ALPHA))
 
 
+@pytest.mark.parametrize("ps,tex_size", [(abi.PS_TEX_GRAD_MODULATE, 100), (abi.PS_TEX_MODULATE, 72),
+                                         (abi.PS_TEX_GRAD_MODULATE, 128)])
+def test_texture_sizes(gdev, odev, ps, tex_size):
+    """Wrapped lookups on textures whose sizes (and mip levels) are and are
+    not powers of two: the addressing divides by the level size either as a
+    quotient or, for powers of two, as the exact product."""
+    sampler = cases.AF16 if ps == abi.PS_TEX_GRAD_MODULATE else cases.TRILINEAR
+    compare(gdev, odev, scenes.feature_scene(seed=61, ps=ps, sampler=sampler, tex_size=tex_size, samples=4,
+                                             uv_scale=5.0))
+
+
 def test_rgba16f_target(gdev, odev):
     compare(gdev, odev, scenes.feature_scene(seed=41, color_fmt=abi.FMT_RGBA16F, blend=abi.BS_LERP_SRC_ALPHA,
                                              samples=4))
