@@ -1,9 +1,10 @@
 // sg_cover.cu -- coverage and early-Z of a pass.
 //
 // Work items are the 32x32 quadrants of every tile of every target, taken
-// from a dynamic cursor; a CTA of 256 threads handles one item at a time,
-// four threads per 4x4 block, one per 2x2 quad.  For each batch of the tile's triangles (its
-// bin list, in API order) the CTA
+// from a dynamic cursor (costliest tiles first); a CTA of 256 threads
+// handles one item at a time, four threads per 4x4 block, one per 2x2 quad.
+// For each batch of the tile's triangles (its bin list, in API order) the
+// CTA
 //   1. stages the batch -- the next CV_STAGE of the tile's triangles whose
 //      bounding box reaches the quadrant, compacted in order from the bin
 //      list -- and classifies every staged triangle against the
@@ -21,7 +22,9 @@
 //      early-Z (framebuffer.cpp:522-614) on the quad's samples against the
 //      quadrant's depth staged in shared memory, and the surviving quad
 //      appended to that quad's own fragment list.  Quads are disjoint, so
-//      the four walks need no synchronisation.
+//      the four walks need no synchronisation.  The common depth functions
+//      (LESS, LESS_EQUAL on float or D24 storage) run as compiled compares,
+//      chosen once per pair; the others go through the general compare.
 //
 // Hierarchical depth test: the block's four threads keep the largest and
 // smallest depth stored in the block, recomputed at the start of each batch
@@ -47,7 +50,7 @@ struct TriCv {  // what coverage and early-Z read of a triangle
   float4 e0, e1, e2, bbox;
   float p0x, p0y, p0z, dzx;
   float dzy;
-  uint32_t entry, zcfg, nattr;
+  uint32_t entry, zcfg, shade_key;  // shade class * 8 + pixel-shader program
 };
 
 // Shared memory of one CTA.
@@ -326,7 +329,7 @@ __device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint
     ts.entry = e;
     uint32_t const flags = __float_as_uint(r4.w);
     ts.zcfg = flags & 0x1FFFu;
-    ts.nattr = (flags >> 24) & 127u;  // shade key
+    ts.shade_key = (flags >> 24) & 127u;
     if (row == 0) sh.stage[i] = ts;
     uint32_t const bit = 1u << (i & 31), word = i >> 5;
     if (e & 1u) {  // accepted for the whole tile by the binner
@@ -564,7 +567,7 @@ __global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
           bool const fullq = (e8 >> 7) ? cq == qfull : (uq == qfull && cq == uq);
           owner_append(P, L, t.entry >> 1,
                        (static_cast<uint32_t>(qd.x) >> 1) | ((static_cast<uint32_t>(qd.y) >> 1) << 12) |
-                           (fullq ? 1u << 24 : 0u) | (t.nattr << 25),
+                           (fullq ? 1u << 24 : 0u) | (t.shade_key << 25),
                        tq | (cq << 16));
         }
         if (!__syncthreads_or(more)) break;

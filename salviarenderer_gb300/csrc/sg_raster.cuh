@@ -196,10 +196,10 @@ __device__ inline void render_sample(TargetParams const& T, DrawParams const& D,
 
 // Coverage-pass copy of a triangle in shared memory: what coverage and early-Z
 // read (edges, bounding box, the position register of v0 / ddx / ddy), and
-// the draw's early-Z configuration and varying count.
+// the draw's early-Z configuration and shade key.
 struct TriStage {
   float4 bbox, e0, e1, e2, p0, dpx, dpy;
-  uint32_t entry, zcfg, nattr, pad;
+  uint32_t entry, zcfg, shade_key, pad;
 };
 struct StageView {
   TriStage const* S;
@@ -435,7 +435,7 @@ __device__ inline void pair_warp(PassParams const& P, TargetParams const& T, Tri
   }
   if (lane == owner) {
     uint32_t const rec = st->entry >> 1;
-    uint32_t const na = st->nattr << 25;
+    uint32_t const na = st->shade_key << 25;
 #pragma unroll 1
     for (int q = 0; q < 4; ++q) {
       uint32_t tq = ((q < 2 ? tested_lo : tested_hi) >> (16 * (q & 1))) & 0xFFFFu;
@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
         ts.dpy = R[5 + 2 * nreg];
         ts.entry = e;
         ts.zcfg = D.zcfg;
-        ts.nattr = D.shade_key;
+        ts.shade_key = D.shade_key;
         ts.pad = 0;
         stage[i] = ts;
         uint32_t bit = 1u << (i & 31), word = i >> 5;
