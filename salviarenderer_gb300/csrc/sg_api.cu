@@ -178,6 +178,7 @@ struct PassPlan {
   std::set<uint32_t> af_textures;            // textures its learned-filter draws take feature taps from
   uint64_t nprims = 0;
   uint64_t samples = 0;                      // target samples of the pass's targets
+  uint64_t quads = 0;                        // 2x2 quads of the pass's targets (fragment-list owners)
   uint32_t af_model = 0;                     // the learned filter its draws use (one per pass), 0 = none
   AfModelDev af{};
   // derived by finalize()
@@ -651,6 +652,7 @@ void add_draw(sg_device* d, PassPlan& pl, DrawParams p, DrawInfo const& info, ui
     pl.targets.push_back(T);
     pl.late_z.push_back(0);
     pl.samples += static_cast<uint64_t>(T.width) * T.height * T.samples;
+    pl.quads += static_cast<uint64_t>((T.width + 1) / 2) * ((T.height + 1) / 2);
     if (info.color) pl.surfaces.insert(info.color);
     if (info.ds) pl.surfaces.insert(info.ds);
   } else {
@@ -795,8 +797,9 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.bin_entries.ensure(static_cast<size_t>(sc.entry_capacity) * 4));
   SG_CUDA(d, sc.tile_begin.ensure((static_cast<size_t>(pl.ntiles) + 1) * 4));
   SG_CUDA(d, sc.tile_order.ensure((static_cast<size_t>(pl.ntiles) + 64) * 4));
-  // fragment room for at least two quads per pixel quad of the pass's targets
-  uint64_t const want_chunks = pl.samples / 4 * 2 / FRAG_CHUNK + 1024;
+  // fragment room: a chunk for every quad owner of the pass's targets, and
+  // chunks for two quads per sample quad
+  uint64_t const want_chunks = pl.quads + pl.samples / 4 * 2 / FRAG_CHUNK + 1024;
   if (want_chunks > sc.chunk_capacity) sc.chunk_capacity = static_cast<uint32_t>(std::min<uint64_t>(want_chunks, 1u << 30));
   size_t nfrag = static_cast<size_t>(sc.chunk_capacity) * FRAG_CHUNK;
   SG_CUDA(d, sc.frag_rec.ensure(nfrag * 4));

@@ -124,3 +124,24 @@ def test_c5_instanced_small(gdev, odev, instances, subdiv):
     s = scenes.c5_scene(seed=5 + subdiv, width=480, height=270, instances=instances, subdiv=subdiv,
                         tex_size=256, hmap_size=128)
     compare(gdev, odev, s)
+
+
+def test_first_full_screen_draw_fits(odev):
+    """A fresh device's first pass has fragment room for every 2x2 quad of a
+    fully covered 1x target (one fragment list per quad): a full-screen quad
+    at 1920x1080 renders on the first call, and matches the oracle."""
+    s = scenes.Scene("fullscreen", 1920, 1080, 1)
+    quad = np.array([[-1, -1, 0.5, 1], [1, -1, 0.5, 1], [1, 1, 0.5, 1],
+                     [-1, -1, 0.5, 1], [1, 1, 0.5, 1], [-1, 1, 0.5, 1]], dtype=np.float32)
+    col = np.tile(np.array([[0.25, 0.5, 0.75, 1.0]], dtype=np.float32), (6, 1))
+    s.buffers["vb"] = np.concatenate([quad, col], axis=1).astype(np.float32)
+    s.draws.append(dict(viewport=(0, 0, 1920, 1080, 0.0, 1.0), prim_count=2, streams=[("vb", 32, 0)],
+                        inputs=scenes.VS_POS_COLOR_INPUTS, num_varyings=1, varying_modifiers=[abi.AM_LINEAR],
+                        vs=dict(program=abi.VS_TRANSFORM, constants=np.eye(4, dtype=np.float32)),
+                        ps=dict(program=abi.PS_COLOR), bs=dict(program=abi.BS_REPLACE)))
+    fresh = Device(abi.bind(ctypes.CDLL(pbuild.ensure_built())), cuda_device=0)
+    got = scenes.render(fresh, s, stats=True)
+    assert got["stats"][0]["ps_invocations"] >= 1920 * 1080  # quads on the diagonal shade twice
+    want = scenes.render(odev, s, stats=True)
+    assert got["stats"] == want["stats"]
+    assert np.array_equal(got["color"], want["color"])
