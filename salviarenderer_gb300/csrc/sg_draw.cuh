@@ -146,10 +146,10 @@ struct PassParams {
   uint32_t bin_capacity;
   uint32_t chunk_capacity;
   // Quad fragments, structure of arrays indexed by chunk * FRAG_CHUNK + slot.
-  // Each owner (4x4 block) of a tile appends its fragments, in primitive
-  // order, to its own list of chunks: owner_first[tile * 256 + owner] is the
-  // first chunk, chunk_next links them, chunk_count says how many slots of a
-  // chunk are used.
+  // Each owner (2x2 quad) of a tile appends its fragments, in primitive
+  // order, to its own list of chunks: owner_first[tile * QUAD_OWNERS + owner]
+  // is the first chunk, chunk_next links them, chunk_count says how many
+  // slots of a chunk are used.
   uint32_t* frag_rec;           // triangle record
   uint32_t* frag_pos;           // bits 0-11 x/2, 12-23 y/2 (absolute quad), 24 full quad, 25-31 shade key
   uint32_t* frag_mask;          // bits 0-15 early-Z-tested samples, 16-31 covered samples

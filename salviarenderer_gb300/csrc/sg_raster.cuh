@@ -12,10 +12,13 @@
 //             default coverage kernel.
 //   k_shade   every fragment of the pass, 4 lanes per quad (one per pixel):
 //             attribute interpolation and the pixel-shader program, with
-//             ddx/ddy from the quad's lanes.  One instance per varying count.
-//   k_merge   one CTA per tile; each owner walks its fragments in primitive
-//             order and applies depth-stencil (when early-Z is off) and the
-//             blend program per covered sample.
+//             ddx/ddy from the quad's lanes.  One instance per varying count
+//             (and learned-filter instances), walking the fragment lists
+//             k_frag_classes groups by shade class and program.
+//   k_merge   warps take 32 owners of a tile at a time from a device-wide
+//             cursor; each owner walks its fragments in primitive order and
+//             applies depth-stencil (when early-Z is off) and the blend
+//             program per covered sample.
 // Included by sg_raster_a.cu / _b.cu / _c.cu, which instantiate k_shade for
 // two varying counts each so the translation units compile in parallel.
 #pragma once
