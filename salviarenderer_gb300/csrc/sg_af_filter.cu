@@ -195,13 +195,14 @@ __global__ void __launch_bounds__(256) k_af_fallback(PassParams P) {
 }
 
 void launch_af_pass(PassParams const& P, AfModelDev const& M, uint32_t num_sms, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_af_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sizeof(FilterSmem)));
-    attr = true;
-  }
   k_af_filter<<<num_sms * FILTER_CTAS_PER_SM, AF_TILE, sizeof(FilterSmem), s>>>(P, M);
   k_af_fallback<<<num_sms * 4, 256, 0, s>>>(P);
+}
+
+// k_af_filter's shared-memory limit on the current device.
+cudaError_t init_af_filter() {
+  return cudaFuncSetAttribute(k_af_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(sizeof(FilterSmem)));
 }
 
 // Adds the pass's learned-filter counts to the device's profile totals.

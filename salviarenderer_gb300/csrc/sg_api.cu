@@ -37,6 +37,8 @@ void launch_cover(PassParams const& p, uint32_t max_samples, bool early_z, uint3
 cudaError_t init_cover();
 void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
 cudaError_t init_cover2();
+cudaError_t init_learned();
+cudaError_t init_af_filter();
 void launch_merge(PassParams const& p, uint32_t grid, cudaStream_t s);
 void launch_shade_0(PassParams const& p, uint32_t grid, cudaStream_t s);
 void launch_shade_1(PassParams const& p, uint32_t grid, cudaStream_t s);
@@ -1312,7 +1314,9 @@ int32_t sg_device_create(int32_t cuda_device, void* cuda_stream, sg_device** out
   if (cudaMallocHost(&d->counters_host, sizeof(PassCounters)) != cudaSuccess) return SG_OUT_OF_MEMORY;
   std::memset(d->counters_host, 0, sizeof(PassCounters));
   if (cudaMallocHost(&d->sticky_host, sizeof(unsigned int)) != cudaSuccess) return SG_OUT_OF_MEMORY;
-  if (init_cover() != cudaSuccess || init_cover2() != cudaSuccess) return SG_CUDA_ERROR;
+  if (init_cover() != cudaSuccess || init_cover2() != cudaSuccess || init_learned() != cudaSuccess ||
+      init_af_filter() != cudaSuccess)
+    return SG_CUDA_ERROR;
   float tab[256];
   make_ewa_table(tab);
   for (auto up : {upload_ewa_table_raster_a, upload_ewa_table_raster_b, upload_ewa_table_raster_c})

@@ -359,17 +359,20 @@ __global__ void k_af_adam(AfModelDev M, float lr, float beta1, float beta2, floa
 
 cudaError_t launch_af_train(AfModelDev const& M, uint16_t const* X, float4 const* Y, uint32_t n, float inv_batch,
                             float* loss_out, unsigned int* status, uint32_t num_sms, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_af_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(sizeof(TrainSmem)));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
   uint32_t tiles = (n + AF_TILE - 1) / AF_TILE;
   uint32_t grid = tiles < num_sms ? tiles : num_sms;
   if (grid) k_af_train<<<grid, AF_TILE, sizeof(TrainSmem), s>>>(M, X, Y, n, inv_batch, loss_out, status);
   return cudaGetLastError();
+}
+
+// The training and inference kernels' shared-memory limits, set on the
+// current device (function attributes are per device).
+cudaError_t init_learned() {
+  cudaError_t e = cudaFuncSetAttribute(k_af_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sizeof(TrainSmem)));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_af_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(sizeof(InferSmem)));
 }
 
 void launch_af_adam(AfModelDev const& M, float lr, uint32_t step, cudaStream_t s) {
@@ -382,13 +385,6 @@ void launch_af_pack(AfModelDev const& M, cudaStream_t s) { k_af_pack<<<1, 256, 0
 
 cudaError_t launch_af_infer(AfModelDev const& M, uint16_t const* X, float4 const* skip, uint32_t n, float* out,
                             unsigned int* status, uint32_t num_sms, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_af_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(sizeof(InferSmem)));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
   uint32_t tiles = (n + AF_TILE - 1) / AF_TILE;
   uint32_t grid = tiles < num_sms ? tiles : num_sms;
   if (grid) k_af_infer<<<grid, AF_TILE, sizeof(InferSmem), s>>>(M, X, skip, n, out, status);
