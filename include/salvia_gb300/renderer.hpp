@@ -84,6 +84,14 @@ inline result to_result(int32_t s) { return static_cast<result>(s); }
 
 }  // namespace salvia
 
+// Compiled SASL shader objects (shader_object.h) are not on this path; the
+// type is declared so that the renderer's shader-code entry points keep
+// their signatures.
+namespace salvia::shader {
+class shader_object;
+using shader_object_ptr = std::shared_ptr<shader_object>;
+}  // namespace salvia::shader
+
 namespace salvia::core {
 
 struct vec4 {
@@ -705,6 +713,8 @@ public:
     if (sg_af_model_create(dev_->dev, seed, &m) != SG_OK) return nullptr;
     return std::make_shared<learned_filter>(dev_, m);
   }
+  // Cube maps are not on this path (renderer.h:49): no texture.
+  texture_ptr create_texcube(size_t, size_t, size_t, pixel_format) { return nullptr; }
   async_object_ptr create_query(async_object_ids id) {
     if (id != async_object_ids::pipeline_statistics && id != async_object_ids::internal_statistics) return nullptr;
     return std::make_shared<async_object>(id);
@@ -734,7 +744,7 @@ public:
 
   // map / unmap (renderer.h:61-63): a host copy, written back on unmap.
   result map(mapped_resource& mr, buffer_ptr const& buf, map_mode mm) {
-    if (!buf || mapped_buf_) return result::failed;
+    if (!buf || mapped_buf_ || mapped_surf_) return result::failed;
     shadow_.assign(buf->size(), 0);
     if (mm == map_read || mm == map_read_write || mm == map_write_no_overwrite)
       if (buf->read(0, shadow_.data(), shadow_.size()) != result::ok) return result::failed;
@@ -744,11 +754,25 @@ public:
     mr.row_pitch = mr.depth_pitch = buf->size();
     return result::ok;
   }
+  // A surface maps as its texels, ((y * w + x) * samples + s) * elem, with
+  // the row and slice pitches of surface::map (surface.cpp:94-116).
+  result map(mapped_resource& mr, surface_ptr const& surf, map_mode mm) {
+    if (!surf || mapped_buf_ || mapped_surf_ || !surf->height()) return result::failed;
+    if (surf->read(shadow_) != result::ok) return result::failed;
+    mapped_surf_ = surf;
+    mapped_mode_ = mm;
+    mr.data = shadow_.data();
+    mr.row_pitch = shadow_.size() / surf->height();
+    mr.depth_pitch = shadow_.size();
+    return result::ok;
+  }
   result unmap() {
-    if (!mapped_buf_) return result::failed;
+    if (!mapped_buf_ && !mapped_surf_) return result::failed;
     result r = result::ok;
-    if (mapped_mode_ != map_read) r = mapped_buf_->transfer(0, shadow_.data(), shadow_.size());
+    if (mapped_buf_ && mapped_mode_ != map_read) r = mapped_buf_->transfer(0, shadow_.data(), shadow_.size());
+    if (mapped_surf_ && mapped_mode_ != map_read) r = mapped_surf_->write(shadow_.data(), shadow_.size());
     mapped_buf_.reset();
+    mapped_surf_.reset();
     return r;
   }
 
@@ -808,6 +832,36 @@ public:
     vp_ = vp;
     return result::ok;
   }
+  // Shader-code state (renderer.h:75-101, renderer_impl.cpp:287-335).  The
+  // reference keeps these variables and samplers in constant buffers that
+  // only compiled SASL shaders read; cpp shaders take theirs through
+  // set_constant / set_sampler.  They are kept here the same way; shader
+  // objects themselves are not on this path and are refused.
+  result set_vertex_shader_code(shader::shader_object_ptr const&) { return result::failed; }
+  result set_pixel_shader_code(shader::shader_object_ptr const&) { return result::failed; }
+  result set_vs_variable_value(std::string const& name, void const* data, size_t sz) {
+    return keep(vs_vars_, name, data, sz);
+  }
+  result set_vs_variable_pointer(std::string const& name, void const* data, size_t sz) {
+    return keep(vs_vars_, name, data, sz);
+  }
+  template <typename T>
+  result set_vs_variable(std::string const& name, T const* data) {
+    return set_vs_variable_value(name, static_cast<void const*>(data), sizeof(T));
+  }
+  result set_ps_variable(std::string const& name, void const* data, size_t sz) { return keep(ps_vars_, name, data, sz); }
+  template <typename T>
+  result set_ps_variable(std::string const& name, T const* data) {
+    return set_ps_variable(name, static_cast<void const*>(data), sizeof(T));
+  }
+  result set_vs_sampler(std::string const& name, sampler_ptr const& samp) {
+    vs_samplers_[name] = samp;
+    return result::ok;
+  }
+  result set_ps_sampler(std::string const& name, sampler_ptr const& samp) {
+    ps_samplers_[name] = samp;
+    return result::ok;
+  }
 
   // state get
   buffer_ptr get_index_buffer() const { return ib_; }
@@ -818,6 +872,8 @@ public:
   cpp_pixel_shader_ptr get_pixel_shader() const { return ps_; }
   cpp_blend_shader_ptr get_blend_shader() const { return bs_; }
   viewport get_viewport() const { return vp_; }
+  shader::shader_object_ptr get_vertex_shader_code() const { return nullptr; }
+  shader::shader_object_ptr get_pixel_shader_code() const { return nullptr; }
 
   // queries
   result begin(async_object_ptr const& q) {
@@ -951,8 +1007,19 @@ private:
   viewport vp_;
   std::vector<async_object_ptr> queries_;
   buffer_ptr mapped_buf_;
+  surface_ptr mapped_surf_;
   map_mode mapped_mode_ = map_mode_none;
   std::vector<uint8_t> shadow_;
+  std::unordered_map<std::string, std::vector<uint8_t>> vs_vars_, ps_vars_;
+  std::unordered_map<std::string, sampler_ptr> vs_samplers_, ps_samplers_;
+
+  static result keep(std::unordered_map<std::string, std::vector<uint8_t>>& vars, std::string const& name,
+                     void const* data, size_t sz) {
+    if (!data && sz) return result::invalid_parameter;
+    auto const* b = static_cast<uint8_t const*>(data);
+    vars[name].assign(b, b + sz);
+    return result::ok;
+  }
 };
 using renderer_ptr = std::shared_ptr<renderer>;
 

@@ -42,11 +42,11 @@ def write_input(scene, path):
         f.write(tex.astype(np.uint8).tobytes())
 
 
-def build_facade(lib_path, out_dir):
-    exe = os.path.join(out_dir, "facade_scene")
+def build_facade(lib_path, out_dir, src=SRC):
+    exe = os.path.join(out_dir, os.path.splitext(os.path.basename(src))[0])
     libdir, libfile = os.path.split(lib_path)
     name = libfile[3:-3]
-    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), SRC,
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), src,
                     "-o", exe, "-L", libdir, f"-l{name}", f"-Wl,-rpath,{libdir}"], check=True)
     return exe
 
@@ -82,6 +82,16 @@ def test_facade_header_compiles_and_matches_wrapper_on_oracle(oracle_lib, tmp_pa
     assert got["stats"] == summed_stats(want["stats"])
     for k in ("color", "depth_stencil", "resolved"):
         assert np.array_equal(got[k], want[k]), f"{k} differs in {(got[k] != want[k]).sum()} bytes"
+
+
+def test_facade_api_entry_points_on_oracle(oracle_lib, tmp_path):
+    """Surface map / unmap, the shader-code state and create_texcube through
+    the facade (tests/cpp/facade_api.cpp), against the oracle library."""
+    from conftest import ORACLE_LIB
+    exe = build_facade(ORACLE_LIB, str(tmp_path), os.path.join(ROOT, "tests", "cpp", "facade_api.cpp"))
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.count("ok ") == 3, out.stdout
 
 
 @pytest.mark.gpu
