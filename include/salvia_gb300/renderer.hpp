@@ -719,6 +719,11 @@ public:
     if (id != async_object_ids::pipeline_statistics && id != async_object_ids::internal_statistics) return nullptr;
     return std::make_shared<async_object>(id);
   }
+  // The SASL overload (renderer.h:52-54): compiled shader objects are not on
+  // this path, so there is no layout.
+  input_layout_ptr create_input_layout(input_element_desc const*, size_t, shader::shader_object_ptr const&) {
+    return nullptr;
+  }
   // Binds the elements to the shader's input registers by semantic
   // (renderer::create_input_layout(descs, n, cpp_vertex_shader_ptr)).
   input_layout_ptr create_input_layout(input_element_desc const* descs, size_t count, cpp_vertex_shader_ptr const& vs) {

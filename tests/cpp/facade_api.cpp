@@ -60,6 +60,8 @@ int main() {
   if (r->set_vertex_shader_code(nullptr) != salvia::result::failed) return fail("set_vertex_shader_code");
   if (r->set_pixel_shader_code(nullptr) != salvia::result::failed) return fail("set_pixel_shader_code");
   if (r->get_vertex_shader_code() || r->get_pixel_shader_code()) return fail("shader code getters");
+  input_element_desc el{};
+  if (r->create_input_layout(&el, 1, salvia::shader::shader_object_ptr())) return fail("SASL input layout");
   std::printf("ok shader-code state\n");
 
   if (r->create_texcube(8, 8, 1, pixel_format_color_rgba8)) return fail("create_texcube");
