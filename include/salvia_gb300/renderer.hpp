@@ -171,6 +171,10 @@ public:
   size_t height() const;
   size_t sample_count() const;
   pixel_format get_pixel_format() const;
+  // bytes per row of texels (surface.h:48)
+  size_t pitch() const { return width() * sample_count() * elem_size(); }
+  // bytes per sample of the surface's format
+  size_t elem_size() const;
   // Raw texels, layout ((y * w + x) * samples + s) * elem (surface.cpp:277-295).
   result read(std::vector<uint8_t>& out) const;
   result write(void const* data, size_t size);
@@ -231,13 +235,16 @@ inline size_t surface::width() const { return tex_.lock()->width(level_); }
 inline size_t surface::height() const { return tex_.lock()->height(level_); }
 inline size_t surface::sample_count() const { return tex_.lock()->sample_count(); }
 inline pixel_format surface::get_pixel_format() const { return tex_.lock()->get_pixel_format(); }
+inline size_t surface::elem_size() const {
+  uint32_t const f = static_cast<uint32_t>(get_pixel_format());
+  return f == SG_FMT_RGBA32F ? 16 : f == SG_FMT_RGB32F ? 12 : (f == SG_FMT_RG32F || f == SG_FMT_RGBA16F) ? 8 : 4;
+}
 inline result surface::read(std::vector<uint8_t>& out) const {
   auto t = tex_.lock();
   if (!t) return result::failed;
   uint32_t w = 0, h = 0, s = 0, f = 0;
   sg_texture_info(t->device(), t->handle(), level_, &w, &h, &s, &f, nullptr);
-  size_t esz = f == SG_FMT_RGBA32F ? 16 : f == SG_FMT_RGB32F ? 12 : (f == SG_FMT_RG32F || f == SG_FMT_RGBA16F) ? 8 : 4;
-  out.resize(static_cast<size_t>(w) * h * s * esz);
+  out.resize(static_cast<size_t>(w) * h * s * elem_size());
   return to_result(sg_texture_download(t->device(), t->handle(), level_, out.data(), out.size()));
 }
 inline result surface::write(void const* data, size_t size) {

@@ -28,7 +28,8 @@ int main() {
   surface_ptr surf = tex->subresource(0);
   mapped_resource mr;
   if (r->map(mr, surf, map_write) != salvia::result::ok) return fail("map surface for writing");
-  if (mr.row_pitch != 5 * 2 * 4 || mr.depth_pitch != 3 * mr.row_pitch) return fail("surface pitches");
+  if (mr.row_pitch != 5 * 2 * 4 || mr.depth_pitch != 3 * mr.row_pitch || surf->pitch() != mr.row_pitch)
+    return fail("surface pitches");
   auto* bytes = static_cast<unsigned char*>(mr.data);
   for (size_t i = 0; i < mr.depth_pitch; ++i) bytes[i] = static_cast<unsigned char>(i * 7 + 3);
   mapped_resource other;
