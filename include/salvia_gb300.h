@@ -158,8 +158,8 @@ typedef struct sg_depth_stencil_desc { /* framebuffer.h:35-52 */
   uint32_t depth_write;
   uint32_t depth_func;
   uint32_t stencil_enable;
-  uint32_t stencil_read_mask;
-  uint32_t stencil_write_mask;
+  uint32_t stencil_read_mask;          /* low 8 bits used (uint8_t in the reference) */
+  uint32_t stencil_write_mask;         /* low 8 bits used */
   sg_stencil_face_desc front, back;
 } sg_depth_stencil_desc;
 
@@ -205,7 +205,7 @@ typedef struct sg_draw_desc {
   uint32_t index_format;
   uint32_t start;
   uint32_t prim_count;
-  int32_t base_vertex;
+  int32_t base_vertex;                 /* draw_index only: draw() has none (renderer_impl.cpp:337-344) */
   uint32_t num_streams;
   sg_vertex_stream streams[SG_MAX_STREAMS];
   uint32_t num_inputs;

@@ -896,7 +896,8 @@ void fetch_indexes(draw_ctx const& c, uint32_t prim, uint32_t out[3]) {
       out[i] = v + static_cast<uint32_t>(d.base_vertex);
     }
   } else {
-    for (int i = 0; i < 3; ++i) out[i] = ids[i] + static_cast<uint32_t>(d.base_vertex);
+    // renderer_impl::draw sets base_vertex = 0 (renderer_impl.cpp:337-344)
+    for (int i = 0; i < 3; ++i) out[i] = ids[i];
   }
 }
 
@@ -1154,7 +1155,7 @@ void ds_read(draw_ctx const& c, ds_rw const& f, size_t x, size_t y, size_t s, fl
   stencil = 0;
   q = 0;
   uint8_t const* p = c.ds->addr(x, y, s);
-  uint32_t rm = c.d->depth_stencil.stencil_read_mask;
+  uint32_t rm = c.d->depth_stencil.stencil_read_mask & 0xFFu;  // uint8_t in depth_stencil_desc
   switch (c.ds->fmt) {
   case SG_FMT_RG32F:
     if (f.read_depth) std::memcpy(&depth, p, 4);
@@ -1243,13 +1244,13 @@ void render_sample(rasterizer_state& rs, size_t x, size_t y, size_t s, vec4 cons
   uint32_t old_q, old_stencil;
   ds_read(c, rs.f, x, y, s, old_depth, old_q, old_stencil);
   bool dpass = depth_test(c, rs.f, depth, old_depth, old_q);
-  uint32_t ref = rs.f.stencil ? (static_cast<uint32_t>(c.d->stencil_ref) & d.stencil_read_mask) : 0;
+  uint32_t ref = rs.f.stencil ? (static_cast<uint32_t>(c.d->stencil_ref) & d.stencil_read_mask & 0xFFu) : 0;
   sg_stencil_face_desc const& face = front ? d.front : d.back;
   bool spass = rs.f.stencil ? cmpu(face.func, ref, old_stencil) : true;
   if (dpass && spass) {
     uint32_t ns = rs.f.stencil ? sop(face.pass_op, ref, old_stencil) : 0;
     blend(c, x, y, s, src);
-    ds_write(c, rs.f, x, y, s, depth, ns, d.stencil_write_mask);
+    ds_write(c, rs.f, x, y, s, depth, ns, d.stencil_write_mask & 0xFFu);
   }
 }
 

@@ -513,7 +513,8 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
     p.index_base = it->second.ptr + first;
     p.index_count = (it->second.size - first) / p.index_stride;
   }
-  p.base_vertex = desc->base_vertex;
+  // draw() has no base vertex (renderer_impl.cpp:337-344)
+  p.base_vertex = desc->indexed ? desc->base_vertex : 0;
   p.strip = desc->topology == SG_TOPOLOGY_TRIANGLE_STRIP;
   p.prim_count = desc->prim_count;
   // shaders
@@ -569,9 +570,10 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
     p.early_z = !ds.stencil_enable;
   }
   p.depth_func = ds.depth_enable ? ds.depth_func : SG_CMP_ALWAYS;
-  p.read_mask = ds.stencil_read_mask;
-  p.write_mask = ds.stencil_write_mask;
-  p.stencil_ref = p.stencil ? (static_cast<uint32_t>(desc->stencil_ref) & ds.stencil_read_mask) : 0u;
+  // the masks are 8-bit fields of depth_stencil_desc (framebuffer.h:35-52)
+  p.read_mask = ds.stencil_read_mask & 0xFFu;
+  p.write_mask = ds.stencil_write_mask & 0xFFu;
+  p.stencil_ref = p.stencil ? (static_cast<uint32_t>(desc->stencil_ref) & p.read_mask) : 0u;
   p.front_func = ds.front.func;
   p.front_pass = ds.front.pass_op;
   p.back_func = ds.back.func;

@@ -376,6 +376,42 @@ def stencil_mirror_scene(seed=7, width=128, height=128, samples=1, ntris=40):
     return s
 
 
+def stencil_ops_scene(front, back, seed=1, width=96, height=80, samples=1, ntris=90, draws=3,
+                      ref=0x5A, read_mask=0xFF, write_mask=0xFF, clear_stencil=0x80, ds_fmt=abi.FMT_RG32F,
+                      depth_func=abi.CMP_LESS):
+    """Stencil state on both faces: `front` and `back` are (func, pass_op)
+    pairs; random clip-space triangles of both windings (no culling), depth
+    tested late (stencil on), drawn in `draws` draws so the stencil values
+    accumulate over overlapping triangles.  Exercises
+    depth_stencil_state::stencil_test / stencil_operation and the read and
+    write masks (framebuffer.cpp:136-166,252-256,336,470-478)."""
+    rng = np.random.default_rng(seed)
+    s = Scene("stencil_ops", width, height, samples, ds_fmt=ds_fmt)
+    s.clear_stencil = clear_stencil
+    s.clear_color = (0.1, 0.1, 0.1, 1.0)
+    pos = rng.uniform(-1.0, 1.0, size=(ntris * 3, 4))
+    pos[:, 2] = rng.uniform(0.05, 0.95, size=ntris * 3)
+    pos[:, 3] = 1.0
+    col = rng.uniform(0.0, 1.0, size=(ntris * 3, 4))
+    s.buffers["geo"] = np.concatenate([pos, col], axis=1).astype(np.float32)
+    dsd = default_depth_stencil(depth_func=depth_func)
+    dsd.stencil_enable = 1
+    dsd.stencil_read_mask, dsd.stencil_write_mask = read_mask, write_mask
+    for face, (func, op) in ((dsd.front, front), (dsd.back, back)):
+        face.func, face.pass_op = func, op
+        # the reference never applies these (framebuffer.cpp:470-478)
+        face.fail_op, face.depth_fail_op = abi.SOP_INVERT, abi.SOP_ZERO
+    ident = np.identity(4, dtype=np.float32)
+    bounds = np.linspace(0, ntris, draws + 1).astype(np.int64)
+    for i in range(draws):
+        s.draws.append(dict(viewport=(0, 0, width, height, 0.0, 1.0), prim_count=int(bounds[i + 1] - bounds[i]),
+                            streams=[("geo", 32, 32 * 3 * int(bounds[i]))],
+                            inputs=VS_POS_COLOR_INPUTS, num_varyings=1, depth_stencil=dsd, stencil_ref=ref,
+                            vs=dict(program=abi.VS_TRANSFORM, constants=ident),
+                            ps=dict(program=abi.PS_COLOR), bs=dict(program=abi.BS_REPLACE)))
+    return s
+
+
 def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=abi.TOPOLOGY_TRIANGLE_LIST,
                   index_format=None, base_vertex=0, cull=abi.CULL_NONE, front_ccw=0,
                   depth_func=abi.CMP_LESS, depth_write=1, depth_enable=1, blend=abi.BS_REPLACE,
@@ -436,9 +472,12 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
             dd.update(index_buffer="ib", index_format=index_format,
                       start=first * (3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else 1))
         else:
-            # draw(start, count) ignores `start` in the reference
-            # (index_fetcher.cpp:96-100); split draws use base_vertex instead.
-            dd["base_vertex"] = base_vertex + first * (3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else 1)
+            # draw(start, count) ignores `start` and has no base vertex in the
+            # reference (renderer_impl.cpp:337-344, index_fetcher.cpp:104-107):
+            # split draws start at a vertex-stream offset instead.
+            first_vertex = base_vertex + first * (3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else 1)
+            dd["streams"] = [("vb", 48, 48 * first_vertex)]
+            dd["base_vertex"] = 0
         s.draws.append(dd)
     return s
 

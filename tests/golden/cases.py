@@ -75,3 +75,44 @@ CASES = {
     "stencil_mirror_1x": lambda: scenes.stencil_mirror_scene(),
     "stencil_mirror_4x": lambda: scenes.stencil_mirror_scene(samples=4, seed=8),
 }
+
+# Stencil state (framebuffer.cpp:136-166,252-256,336,470-478).  The
+# reference's clipper hands every triangle to the rasterizer in one winding
+# (clipper.cpp:75-89), so the rasterizer's front_face (rasterizer.cpp:915) is
+# the same for all of them and only the back-face state is ever applied; each
+# case puts a different state on the front face to show it stays unused.
+# Cases: every stencil op (back face; incr_sat cleared next to its 0xFF clamp,
+# decr_sat next to zero, where the reference keeps the wrapped value and the
+# write mask cuts it); every stencil function, with a reference value and
+# clear that let some samples pass and then stop passing; read and write
+# masks, one case over a 32-bit cleared stencil word; 4x MSAA.
+SOPS = [abi.SOP_KEEP, abi.SOP_ZERO, abi.SOP_REPLACE, abi.SOP_INCR_SAT, abi.SOP_DECR_SAT, abi.SOP_INVERT,
+        abi.SOP_INCR_WRAP, abi.SOP_DECR_WRAP]
+SOP_NAMES = ["keep", "zero", "replace", "incr_sat", "decr_sat", "invert", "incr_wrap", "decr_wrap"]
+S = scenes.stencil_ops_scene
+for _i, _op in enumerate(SOPS):
+    _clear = {abi.SOP_INCR_SAT: 0xFE, abi.SOP_DECR_SAT: 0x01}.get(_op, 0x80)
+    CASES[f"stencil_op_{SOP_NAMES[_i]}"] = (
+        lambda i=_i, op=_op, clear=_clear: S((abi.CMP_ALWAYS, SOPS[(i + 3) % 8]), (abi.CMP_ALWAYS, op),
+                                             seed=40 + i, clear_stencil=clear))
+CASES.update({
+    "stencil_func_less": lambda: S((abi.CMP_GREATER, abi.SOP_DECR_WRAP), (abi.CMP_LESS, abi.SOP_INCR_WRAP),
+                                   seed=50, ref=0x7F),
+    "stencil_func_greater": lambda: S((abi.CMP_LESS, abi.SOP_INCR_WRAP), (abi.CMP_GREATER, abi.SOP_DECR_WRAP),
+                                      seed=51, ref=0x81),
+    "stencil_func_lequal": lambda: S((abi.CMP_ALWAYS, abi.SOP_ZERO), (abi.CMP_LESS_EQUAL, abi.SOP_DECR_WRAP),
+                                     seed=52, ref=0x7F),
+    "stencil_func_gequal": lambda: S((abi.CMP_ALWAYS, abi.SOP_ZERO), (abi.CMP_GREATER_EQUAL, abi.SOP_INCR_WRAP),
+                                     seed=53, ref=0x81),
+    "stencil_func_equal": lambda: S((abi.CMP_NEVER, abi.SOP_ZERO), (abi.CMP_EQUAL, abi.SOP_INVERT),
+                                    seed=54, ref=0x80),
+    "stencil_func_notequal": lambda: S((abi.CMP_ALWAYS, abi.SOP_INVERT), (abi.CMP_NOT_EQUAL, abi.SOP_REPLACE),
+                                       seed=55, ref=0x81),
+    "stencil_func_never": lambda: S((abi.CMP_ALWAYS, abi.SOP_REPLACE), (abi.CMP_NEVER, abi.SOP_REPLACE), seed=56),
+    "stencil_masks_0f_f0": lambda: S((abi.CMP_ALWAYS, abi.SOP_ZERO), (abi.CMP_EQUAL, abi.SOP_INVERT),
+                                     seed=57, ref=0x35, read_mask=0x0F, write_mask=0xF0, clear_stencil=0xA5),
+    "stencil_masks_3c_3f": lambda: S((abi.CMP_ALWAYS, abi.SOP_ZERO), (abi.CMP_LESS_EQUAL, abi.SOP_INCR_WRAP),
+                                     seed=58, ref=0x10, read_mask=0x3C, write_mask=0x3F, clear_stencil=0x12345678),
+    "stencil_4x_equal_invert": lambda: S((abi.CMP_ALWAYS, abi.SOP_ZERO), (abi.CMP_EQUAL, abi.SOP_INVERT),
+                                         seed=59, samples=4, ref=0x80),
+})

@@ -6,6 +6,7 @@ bit-for-bit: colour, depth-stencil, the MSAA resolve and the pipeline
 counters (input primitives, primitives after clipping/culling, pixel-shader
 invocations, back-end input pixels).
 """
+import json
 import os
 
 import numpy as np
@@ -44,3 +45,19 @@ def test_oracle_mipchain_matches_reference(odev):
     assert odev.levels(t) == len(g.files)
     for i in range(odev.levels(t)):
         np.testing.assert_array_equal(odev.texture_download(t, i), g[f"level{i}"])
+
+
+@pytest.mark.parametrize("name", ["c1_512_10k", "c2_1080p_4x"])
+def test_oracle_full_size_matches_reference(odev, name):
+    """The full-size C1 frame and the benchmark's own 1080p 4x MSAA frame:
+    the restatement's outputs and counters hash to the digests of the
+    reference renderer's (tests/golden/full_size_digests.json)."""
+    from make_golden import FULL_SIZE, output_digests
+    with open(os.path.join(GOLDEN, "full_size_digests.json")) as fh:
+        want = json.load(fh)[name]
+    s = FULL_SIZE[name]()
+    assert scene_digest(s) == want["scene"], "scene generator drifted from the digests"
+    got = output_digests(scenes.render(odev, s, stats=True))
+    assert got["stats_total"] == want["stats_total"]
+    for k, v in got.items():
+        assert v == want[k], f"{name}: {k} differs from the reference"
