@@ -247,18 +247,10 @@ def measure_uneven(dev, stream, flush, args):
     count in one command list, plain (clear + one sg_draw per draw, frame by
     frame) against batched (the list recorded as one CUDA graph)."""
     from salviarenderer_gb300 import scenes
-    from salviarenderer_gb300.device import SalviaError
     batch = scenes.UnevenBatch(seed=SEED)
     b = scenes.BoundUneven(dev, batch)
     cl = b.commands()
-    for attempt in range(4):  # the first runs size the scratch
-        try:
-            dev.submit(cl, stats=True)
-            dev.sync()
-            break
-        except SalviaError:
-            if attempt == 3:
-                raise
+    dev.submit(cl, stats=True)  # sizes the scratch
     steps = max(1, min(args.steps, 3))
     for _ in range(args.warmup):
         b.render_plain()
@@ -368,7 +360,6 @@ def measure_c5(dev, stream, flush, args, model):
     learned filter; frames/s of each as a recorded graph."""
     import numpy as np
     from salviarenderer_gb300 import scenes
-    from salviarenderer_gb300.device import SalviaError
     steps = max(1, min(args.steps, 5))
     out = {"workload": "3840x2160 RGBA16F 4xMSAA D32F, 1000 instances x 5120 triangles, morph + R32F "
                        "vertex-texture displacement, 2048^2 RGBA8 8x AF, 10% additive"}
@@ -376,14 +367,8 @@ def measure_c5(dev, stream, flush, args, model):
     for key, lrn in (("plain", None), ("learned", (0.5, 16.0, 0.0))):
         b = scenes.Bound(dev, scenes.c5_scene(seed=SEED, learned=lrn), model if lrn else None)
         cl = b.commands()
-        for attempt in range(4):  # the first runs size the scratch
-            try:
-                dev.submit(cl)
-                dev.sync()
-                break
-            except SalviaError:
-                if attempt == 3:
-                    raise
+        dev.submit(cl)
+        dev.sync()
         imgs[key] = np.frombuffer(b.outputs()["resolved"], dtype=np.float16).astype(np.float32)
         g = dev.graph_create(cl)
         for _ in range(args.warmup):

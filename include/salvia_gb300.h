@@ -224,6 +224,19 @@ typedef struct sg_draw_stats {
   uint64_t cprimitives;                /* triangles after clipping and culling */
   uint64_t ps_invocations;             /* pixel-shader invocations, helpers included */
   uint64_t backend_input_pixels;       /* pixels of quads that reached the output merger */
+  /* vertices the input assembler fetched: three per primitive for lists and
+   * strips alike, as the reference's vertex cache counts them
+   * (default_vertex_cache.cpp:363) */
+  uint64_t ia_vertices;
+  /* vertex-shader executions: here one per primitive corner (no vertex
+   * reuse across primitives), counted on the device.  The reference counts
+   * the misses of its per-thread vertex caches (default_vertex_cache.cpp:
+   * 354-400), which depends on how its worker threads split the draw, so
+   * this counter is not compared with it. */
+  uint64_t vs_invocations;
+  /* primitives that entered the clipper: every input primitive
+   * (geom_setup_engine.cpp:108-123) */
+  uint64_t cinvocations;
 } sg_draw_stats;
 
 /* Per-stage device time and launch counts, accumulated while profiling is

@@ -27,6 +27,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <memory>
 #include <string>
@@ -116,16 +117,108 @@ struct viewport {  // salvia/include/salvia/core/viewport.h
 };
 
 namespace detail {
+// What a running query adds up (pipeline_statistics and internal_statistics,
+// async_object.h:90-175).
+struct query_counters {
+  uint64_t ia_vertices = 0, ia_primitives = 0, vs_invocations = 0, cinvocations = 0, cprimitives = 0,
+           ps_invocations = 0, backend_input_pixels = 0;
+};
+
 // Owns the C-ABI device; shared by the renderer and every resource it made,
 // so a resource never outlives the device its handle belongs to.
+//
+// It also holds the renderer's queued commands.  The reference's renderer
+// executes each call as it comes (the synchronous renderer) or queues it for
+// a render thread (async_renderer.cpp:19-104); here draws, clears and
+// resolves are queued and go to the device as one command list (sg_submit,
+// which runs them exactly as one-by-one calls would, many draws per kernel
+// chain) when something needs their results or changes what they read:
+// flush() and get_data() on the renderer, any read, write, mip generation,
+// resolve or destruction of a resource, or a full queue.  Errors of queued
+// commands are therefore reported by the call that submits them.
 struct device_ref {
   sg_device* dev = nullptr;
   explicit device_ref(sg_device* d) : dev(d) {}
   ~device_ref() {
-    if (dev) sg_device_destroy(dev);
+    if (dev) {
+      flush();
+      sg_device_destroy(dev);
+    }
   }
   device_ref(device_ref const&) = delete;
   device_ref& operator=(device_ref const&) = delete;
+
+  static constexpr size_t max_queued = 1024;
+
+  void queue_draw(sg_draw_desc const& d, std::vector<std::shared_ptr<query_counters>> const& queries) {
+    descs_.push_back(d);
+    sg_command c{};
+    c.type = SG_CMD_DRAW;
+    c.draw = &descs_.back();
+    push(c, queries);
+  }
+  void queue_clear_color(uint32_t tex, float const rgba[4]) {
+    sg_command c{};
+    c.type = SG_CMD_CLEAR_COLOR;
+    c.texture = tex;
+    std::memcpy(c.color, rgba, sizeof(c.color));
+    push(c, {});
+  }
+  void queue_clear_depth_stencil(uint32_t tex, uint32_t flags, float depth, uint32_t stencil) {
+    sg_command c{};
+    c.type = SG_CMD_CLEAR_DEPTH_STENCIL;
+    c.texture = tex;
+    c.flags = flags;
+    c.depth = depth;
+    c.stencil = stencil;
+    push(c, {});
+  }
+  void queue_resolve(uint32_t src, uint32_t dst) {
+    sg_command c{};
+    c.type = SG_CMD_RESOLVE;
+    c.texture = src;
+    c.texture2 = dst;
+    push(c, {});
+  }
+  // Submits the queue; the queries of its draws get their counters.
+  int32_t flush() {
+    if (cmds_.empty()) return pending_;
+    bool counted = false;
+    for (auto const& q : queries_) counted = counted || !q.empty();
+    std::vector<sg_draw_stats> st(counted ? cmds_.size() : 0);
+    int32_t r = sg_submit(dev, cmds_.data(), static_cast<uint32_t>(cmds_.size()), counted ? st.data() : nullptr);
+    if (r == SG_OK && counted)
+      for (size_t i = 0; i < cmds_.size(); ++i)
+        for (auto const& q : queries_[i]) {
+          q->ia_vertices += st[i].ia_vertices;
+          q->ia_primitives += st[i].ia_primitives;
+          q->vs_invocations += st[i].vs_invocations;
+          q->cinvocations += st[i].cinvocations;
+          q->cprimitives += st[i].cprimitives;
+          q->ps_invocations += st[i].ps_invocations;
+          q->backend_input_pixels += st[i].backend_input_pixels;
+        }
+    cmds_.clear();
+    descs_.clear();
+    queries_.clear();
+    if (pending_ != SG_OK) r = pending_;
+    pending_ = SG_OK;
+    return r;
+  }
+
+private:
+  void push(sg_command const& c, std::vector<std::shared_ptr<query_counters>> const& q) {
+    cmds_.push_back(c);
+    queries_.push_back(q);
+    if (cmds_.size() >= max_queued) {
+      int32_t r = flush();
+      if (r != SG_OK) pending_ = r;  // reported by the next submitting call
+    }
+  }
+  std::deque<sg_draw_desc> descs_;  // stable addresses for cmds_[i].draw
+  std::vector<sg_command> cmds_;
+  std::vector<std::vector<std::shared_ptr<query_counters>>> queries_;
+  int32_t pending_ = SG_OK;
 };
 using device_sp = std::shared_ptr<device_ref>;
 }  // namespace detail
@@ -141,15 +234,21 @@ class buffer {
 public:
   buffer(core::detail::device_sp d, uint32_t h, size_t size) : dev_(std::move(d)), handle_(h), size_(size) {}
   ~buffer() {
-    if (handle_) sg_buffer_destroy(dev_->dev, handle_);
+    if (handle_) {
+      dev_->flush();
+      sg_buffer_destroy(dev_->dev, handle_);
+    }
   }
   size_t size() const { return size_; }
   uint32_t handle() const { return handle_; }
-  // buffer::transfer: copies host bytes into the buffer at `offset`.
+  // buffer::transfer: copies host bytes into the buffer at `offset` (after
+  // the queued commands that read it).
   result transfer(size_t offset, void const* src, size_t sz) {
+    if (result r = to_result(dev_->flush()); r != result::ok) return r;
     return to_result(sg_buffer_upload(dev_->dev, handle_, offset, src, sz));
   }
   result read(size_t offset, void* dst, size_t sz) const {
+    if (result r = to_result(dev_->flush()); r != result::ok) return r;
     return to_result(sg_buffer_download(dev_->dev, handle_, offset, dst, sz));
   }
 
@@ -191,10 +290,14 @@ class texture : public std::enable_shared_from_this<texture> {
 public:
   texture(core::detail::device_sp d, uint32_t h) : dev_(std::move(d)), handle_(h) {}
   ~texture() {
-    if (handle_) sg_texture_destroy(dev_->dev, handle_);
+    if (handle_) {
+      dev_->flush();
+      sg_texture_destroy(dev_->dev, handle_);
+    }
   }
   uint32_t handle() const { return handle_; }
   sg_device* device() const { return dev_->dev; }
+  core::detail::device_ref& device_ref() const { return *dev_; }
   uint32_t levels() const {
     uint32_t n = 0;
     sg_texture_info(dev_->dev, handle_, 0, nullptr, nullptr, nullptr, nullptr, &n);
@@ -211,6 +314,7 @@ public:
   }
   // texture::gen_mipmap(filter, auto_gen) (texture2d.cpp:25-36)
   result gen_mipmap(filter_type filter, bool /*auto_gen*/) {
+    if (result r = to_result(dev_->flush()); r != result::ok) return r;
     surfaces_.clear();
     return to_result(sg_texture_gen_mipmap(dev_->dev, handle_, static_cast<uint32_t>(filter)));
   }
@@ -242,6 +346,7 @@ inline size_t surface::elem_size() const {
 inline result surface::read(std::vector<uint8_t>& out) const {
   auto t = tex_.lock();
   if (!t) return result::failed;
+  if (result r = to_result(t->device_ref().flush()); r != result::ok) return r;
   uint32_t w = 0, h = 0, s = 0, f = 0;
   sg_texture_info(t->device(), t->handle(), level_, &w, &h, &s, &f, nullptr);
   out.resize(static_cast<size_t>(w) * h * s * elem_size());
@@ -250,13 +355,17 @@ inline result surface::read(std::vector<uint8_t>& out) const {
 inline result surface::write(void const* data, size_t size) {
   auto t = tex_.lock();
   if (!t) return result::failed;
+  if (result r = to_result(t->device_ref().flush()); r != result::ok) return r;
   return to_result(sg_texture_upload(t->device(), t->handle(), level_, data, size));
 }
+// Queued with the renderer's commands (it runs after the draws before it).
 inline result surface::resolve(surface& target) {
   auto a = tex_.lock();
   auto b = target.tex_.lock();
-  if (!a || !b || level_ != 0 || target.level_ != 0) return result::invalid_parameter;
-  return to_result(sg_resolve(a->device(), a->handle(), b->handle()));
+  if (!a || !b || level_ != 0 || target.level_ != 0 || a.get() == b.get()) return result::invalid_parameter;
+  if (b->sample_count() != 1 || a->width() != b->width() || a->height() != b->height()) return result::invalid_parameter;
+  a->device_ref().queue_resolve(a->handle(), b->handle());
+  return result::ok;
 }
 
 // sampler_desc (sampler.h:16-45)
@@ -618,8 +727,8 @@ public:
   explicit async_object(async_object_ids id) : id_(id) {}
   async_object_ids id() const { return id_; }
   bool running = false;
-  pipeline_statistics stats{};
-  internal_statistics internal{};
+  // added up by the queued draws issued while the query runs
+  std::shared_ptr<detail::query_counters> counters = std::make_shared<detail::query_counters>();
 
 private:
   async_object_ids id_;
@@ -891,8 +1000,7 @@ public:
   result begin(async_object_ptr const& q) {
     if (!q || q->running) return result::failed;
     q->running = true;
-    q->stats = pipeline_statistics{};
-    q->internal = internal_statistics{};
+    q->counters = std::make_shared<detail::query_counters>();  // draws still queued keep the old one
     queries_.push_back(q);
     return result::ok;
   }
@@ -906,29 +1014,48 @@ public:
       }
     return result::ok;
   }
+  // Submits the queued commands a query counts and waits for them.
   async_status get_data(async_object_ptr const& q, void* data, bool /*do_not_wait*/) {
     if (!q || q->running) return async_status::error;
-    if (sg_sync(dev_->dev) != SG_OK) return async_status::error;
-    if (q->id() == async_object_ids::pipeline_statistics)
-      std::memcpy(data, &q->stats, sizeof(q->stats));
-    else
-      std::memcpy(data, &q->internal, sizeof(q->internal));
+    if (dev_->flush() != SG_OK || sg_sync(dev_->dev) != SG_OK) return async_status::error;
+    detail::query_counters const& c = *q->counters;
+    if (q->id() == async_object_ids::pipeline_statistics) {
+      pipeline_statistics s{};
+      s.ia_vertices = c.ia_vertices;
+      s.ia_primitives = c.ia_primitives;
+      s.vs_invocations = c.vs_invocations;
+      s.cinvocations = c.cinvocations;
+      s.cprimitives = c.cprimitives;
+      s.ps_invocations = c.ps_invocations;
+      std::memcpy(data, &s, sizeof(s));
+    } else {
+      internal_statistics s{c.backend_input_pixels};
+      std::memcpy(data, &s, sizeof(s));
+    }
     return async_status::ready;
   }
 
-  // render operations
+  // render operations: queued (see detail::device_ref), submitted together
   result draw(size_t startpos, size_t primcnt) { return submit(false, startpos, primcnt, 0); }
   result draw_index(size_t startpos, size_t primcnt, int basevert) { return submit(true, startpos, primcnt, basevert); }
   result clear_color(surface_ptr const& s, color_rgba32f const& c) {
     if (!s || s->level() != 0) return result::invalid_parameter;
     float rgba[4] = {c.r, c.g, c.b, c.a};
-    return to_result(sg_clear_color(dev_->dev, s->get_texture()->handle(), rgba));
+    dev_->queue_clear_color(s->get_texture()->handle(), rgba);
+    return result::ok;
   }
   result clear_depth_stencil(surface_ptr const& s, uint32_t flags, float d, uint32_t st) {
     if (!s || s->level() != 0) return result::invalid_parameter;
-    return to_result(sg_clear_depth_stencil(dev_->dev, s->get_texture()->handle(), flags, d, st));
+    if (flags == 0 || flags > (clear_depth | clear_stencil)) return result::invalid_parameter;
+    dev_->queue_clear_depth_stencil(s->get_texture()->handle(), flags, d, st);
+    return result::ok;
   }
-  result flush() { return to_result(sg_sync(dev_->dev)); }
+  // renderer::flush (renderer.h:128): submits the queued commands and waits for them
+  result flush() {
+    int32_t r = dev_->flush();
+    int32_t s = sg_sync(dev_->dev);
+    return to_result(r != SG_OK ? r : s);
+  }
 
   // The C-ABI descriptor of a draw under the current state.
   result build_desc(bool indexed, size_t startpos, size_t primcnt, int basevert, sg_draw_desc& d) const {
@@ -989,17 +1116,10 @@ private:
     sg_draw_desc d;
     result r = build_desc(indexed, startpos, primcnt, basevert, d);
     if (r != result::ok) return r;
-    if (queries_.empty()) return to_result(sg_draw(dev_->dev, &d, nullptr));
-    sg_draw_stats st{};
-    r = to_result(sg_draw(dev_->dev, &d, &st));
-    for (auto const& q : queries_) {
-      q->stats.ia_primitives += st.ia_primitives;
-      q->stats.ia_vertices += st.ia_primitives * 3;
-      q->stats.cprimitives += st.cprimitives;
-      q->stats.ps_invocations += st.ps_invocations;
-      q->internal.backend_input_pixels += st.backend_input_pixels;
-    }
-    return r;
+    std::vector<std::shared_ptr<detail::query_counters>> qs;
+    for (auto const& q : queries_) qs.push_back(q->counters);
+    dev_->queue_draw(d, qs);
+    return result::ok;
   }
 
   detail::device_sp dev_;

@@ -372,6 +372,9 @@ int32_t sg_draw(sg_device* d, const sg_draw_desc* desc, sg_draw_stats* stats) {
     stats->cprimitives = ps_stat.cprimitives;
     stats->ps_invocations = ps_stat.ps_invocations;
     stats->backend_input_pixels = in_stat.backend_input_pixels;
+    stats->ia_vertices = ps_stat.ia_vertices;
+    stats->vs_invocations = ps_stat.vs_invocations;
+    stats->cinvocations = ps_stat.cinvocations;
   }
   r->flush();
   return rv == result::ok ? SG_OK : SG_FAILED;

@@ -1632,6 +1632,11 @@ int32_t do_draw(device_state* dev, sg_draw_desc const* d, sg_draw_stats* stats_o
   // early-Z enable (framebuffer.cpp:424)
   c.early_z = c.ds != nullptr && !d->depth_stencil.stencil_enable;
   c.stats.ia_primitives = d->prim_count;
+  c.stats.ia_vertices = 3ull * d->prim_count;  // three per fetched primitive (default_vertex_cache.cpp:363)
+  c.stats.cinvocations = d->prim_count;        // every primitive enters the clipper (geom_setup_engine.cpp:108-123)
+  // the GPU path's count (one run per primitive corner); the reference's
+  // depends on its worker threads' vertex caches and is not compared
+  c.stats.vs_invocations = 3ull * d->prim_count;
 
   // Vertex processing: the vertex shader is a pure function of the index,
   // so one result per distinct index stands for the reference's caches.

@@ -110,7 +110,14 @@ class ProfileData(C.Structure):
 
 class DrawStats(C.Structure):
     _fields_ = [("ia_primitives", C.c_uint64), ("cprimitives", C.c_uint64),
-                ("ps_invocations", C.c_uint64), ("backend_input_pixels", C.c_uint64)]
+                ("ps_invocations", C.c_uint64), ("backend_input_pixels", C.c_uint64),
+                ("ia_vertices", C.c_uint64), ("vs_invocations", C.c_uint64), ("cinvocations", C.c_uint64)]
+
+
+# counters whose values the reference renderer fixes (vs_invocations depends
+# on its worker threads' vertex caches)
+REFERENCE_STATS = ("ia_primitives", "cprimitives", "ps_invocations", "backend_input_pixels", "ia_vertices",
+                   "cinvocations")
 
 
 class Command(C.Structure):

@@ -15,6 +15,7 @@
 
 namespace sg {
 cudaStream_t device_stream(sg_device* d);
+int32_t device_settle(sg_device* d);
 int device_sms(sg_device* d);
 void device_set_error(sg_device* d, char const* msg);
 int32_t device_af_sampler(sg_device* d, uint32_t handle, dev_sampler& out);
@@ -175,6 +176,7 @@ uint32_t sg_af_model_id(const sg_af_model* m) { return m ? m->id : 0u; }
 
 void sg_af_model_destroy(sg_device* d, sg_af_model* m) {
   if (!m) return;
+  if (d) device_settle(d);  // a replay of logged passes reads the model
   if (d && m->id) device_unregister_af(d, m->id);
   if (d) cudaStreamSynchronize(device_stream(d));
   cudaFree(m->m.params);
@@ -196,6 +198,7 @@ int32_t sg_af_model_get_params(sg_device* d, sg_af_model* m, float* params) {
 
 int32_t sg_af_model_set_params(sg_device* d, sg_af_model* m, const float* params) {
   if (!d || !m || !params) return SG_INVALID_PARAMETER;
+  if (int32_t r = device_settle(d)) return r;
   cudaStream_t s = device_stream(d);
   AF_CUDA(d, cudaMemcpyAsync(m->m.params, params, AF_PARAMS * sizeof(float), cudaMemcpyHostToDevice, s));
   launch_af_pack(m->m, s);
@@ -294,6 +297,7 @@ int32_t sg_af_model_train(sg_device* d, sg_af_model* m, const sg_af_train_desc* 
   if (!d || !m || !t || !t->samplers || t->num_samplers == 0 || t->samples == 0 || t->batch == 0 ||
       t->epochs == 0 || !(t->lr > 0.0f))
     return SG_INVALID_PARAMETER;
+  if (int32_t r = device_settle(d)) return r;
   cudaStream_t s = device_stream(d);
   DevSamplers ds;
   if (int32_t r = upload_samplers(d, t->samplers, t->num_samplers, ds)) return r;

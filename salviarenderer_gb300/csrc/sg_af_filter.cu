@@ -41,7 +41,7 @@ constexpr uint32_t FILTER_TMEM_COLS = 64;
 __device__ inline bool unorm_format(uint32_t fmt) { return fmt == SG_FMT_RGBA8 || fmt == SG_FMT_BGRA8; }
 
 __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassParams P, AfModelDev M) {
-  if (P.counters->overflow & OVF_FATAL) return;
+  if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
   uint32_t const n = min(P.counters->af_lookups, P.af_net_capacity);
   if (blockIdx.x * AF_TILE >= n) return;  // no tile for this CTA: no tensor memory either
   extern __shared__ __align__(128) uint8_t smem_raw[];
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassP
 }
 
 __global__ void __launch_bounds__(256) k_af_fallback(PassParams P) {
-  if (P.counters->overflow & OVF_FATAL) return;
+  if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
   // the network's rejects (af_fallback into af_net), then the lookups
   // k_shade queued for the plain sampler (af_plain)
   uint32_t const nf = P.counters->af_fallbacks;
@@ -207,7 +207,7 @@ cudaError_t init_af_filter() {
 
 // Adds the pass's learned-filter counts to the device's profile totals.
 __global__ void k_af_count(PassParams P, unsigned long long* acc) {
-  if (P.counters->overflow & OVF_FATAL) return;
+  if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
   acc[0] += min(P.counters->af_lookups, P.af_net_capacity);
   acc[1] += P.counters->af_fallbacks;
 }

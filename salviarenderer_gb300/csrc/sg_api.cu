@@ -37,6 +37,7 @@ void launch_cover(PassParams const& p, uint32_t max_samples, bool early_z, uint3
 cudaError_t init_cover();
 void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
 cudaError_t init_cover2();
+void launch_cover_rollback(PassParams const& p, uint32_t grid, cudaStream_t s);
 cudaError_t init_learned();
 cudaError_t init_af_filter();
 void launch_merge(PassParams const& p, uint32_t grid, cudaStream_t s);
@@ -55,7 +56,8 @@ cudaError_t upload_ewa_table_filter(float const* tab, cudaStream_t s);
 void launch_af_pass(PassParams const& P, AfModelDev const& M, uint32_t num_sms, cudaStream_t s);
 void launch_shade_learned(uint32_t na, PassParams const& P, uint32_t grid, cudaStream_t s);
 void launch_af_count(PassParams const& P, unsigned long long* acc, cudaStream_t s);
-uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaStream_t s);
+uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaStream_t s, unsigned int* status,
+                     bool count_pass);
 void launch_mip(uint8_t const* src, uint32_t sw, uint32_t sh, uint8_t* dst, uint32_t dw, uint32_t dh,
                 uint32_t samples, uint32_t fmt, uint32_t filter, cudaStream_t s);
 }  // namespace sg
@@ -147,16 +149,15 @@ uint8_t* static_scratch_address(int ordinal) {
 // every recorded graph owns its own.
 struct Scratch {
   Arena params, slot_rec, recs, bin_counts, scan_sums, bin_entries, tile_begin, frag_rec, frag_pos, frag_mask,
-      frag_color, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, sticky, af_net, af_plain,
+      frag_color, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, zbackup, af_net, af_plain,
       af_fallback, tile_order, frag_list;
-  bool pending = false;                // passes ran since the host last read `sticky`
   uint32_t entry_capacity = 1u << 24;  // bin entries (grows after an overflow)
   uint32_t chunk_capacity = 1u << 18;  // fragment chunks (grows after an overflow)
   uint32_t af_capacity = 0;            // learned-filter plain-queue records (grows after an overflow)
   void release() {
     for (Arena* a : {&params, &slot_rec, &recs, &bin_counts, &scan_sums, &bin_entries, &tile_begin, &frag_rec,
                      &frag_pos, &frag_mask, &frag_color, &frag_ps, &chunk_next, &chunk_count, &owner_first,
-                     &counters, &stats, &sticky, &af_net, &af_plain, &af_fallback, &tile_order, &frag_list})
+                     &counters, &stats, &zbackup, &af_net, &af_plain, &af_fallback, &tile_order, &frag_list})
       a->release();
   }
 };
@@ -242,11 +243,27 @@ sg_tuning default_tuning() {
 struct sg_graph {
   Scratch scratch;
   std::vector<PassPlan> plans;
+  std::vector<uint32_t> plan_kernels;  // kernels each pass launches (a pass with none is not logged)
   Arena params;                   // every pass's parameter blocks
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   uint32_t kernels = 0;
 };
+
+namespace {
+// A pass launched since the host last read the device's status words: an
+// immediate pass (its plan), a pass of a recorded graph, or a static-scratch
+// draw.  When a pass overflows, it and every pass after it did nothing on
+// the device (pass_gated), and the host runs them again from this log.
+struct LogEntry {
+  PassPlan plan;              // immediate passes
+  sg_graph* graph = nullptr;  // graph passes: graph->plans[pass]
+  uint32_t pass = 0;
+  bool fixed = false;         // runs in the static scratch
+};
+// Passes logged before the host looks at the status words unasked.
+constexpr size_t LOG_LIMIT = 4096;
+}  // namespace
 
 struct sg_device {
   int ordinal = 0;
@@ -261,8 +278,12 @@ struct sg_device {
   PassCounters* counters_host = nullptr;  // pinned: counters of the last pass run with statistics
   DrawStatsDev* stats_host = nullptr;     // pinned: per-draw statistics of that pass
   size_t stats_host_cap = 0;
-  unsigned int* sticky_host = nullptr;    // pinned: overflow bits read back at sg_sync
-  unsigned int* static_sticky = nullptr;  // the static scratch's overflow word, when a call used it
+  unsigned int* status = nullptr;         // device: the status words every pass shares (PassParams::sticky)
+  unsigned int* status_host = nullptr;    // pinned: their copy when the host looks
+  uint8_t* static_base = nullptr;         // this device's g_static_scratch (looked up at creation)
+  std::vector<LogEntry> log;              // passes launched since the host last looked
+  unsigned int done_base = 0;             // the completed-pass count when the host last looked
+  int32_t pending = 0;                    // an error of earlier work, reported at the next sg_sync
   std::set<sg_graph*> graphs;
   std::map<uint32_t, AfModelDev> af_models;  // learned filters by id
   sg_tuning tuning = default_tuning();
@@ -789,10 +810,6 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   if (pl.rec_units > 0x7FFFFFFFull) return SG_OUT_OF_MEMORY;  // record ids must fit 31 bits
   if (own_params) SG_CUDA(d, sc.params.ensure(L.bytes));
   SG_CUDA(d, sc.counters.ensure(sizeof(PassCounters)));
-  if (!sc.sticky.ptr) {
-    SG_CUDA(d, sc.sticky.ensure(sizeof(unsigned int)));
-    SG_CUDA(d, cudaMemset(sc.sticky.ptr, 0, sizeof(unsigned int)));
-  }
   SG_CUDA(d, sc.stats.ensure(std::max<size_t>(1, pl.draws.size()) * sizeof(DrawStatsDev)));
   SG_CUDA(d, sc.slot_rec.ensure(static_cast<size_t>(pl.nslots) * 4));
   SG_CUDA(d, sc.recs.ensure(static_cast<size_t>(pl.rec_units) * sizeof(float4)));
@@ -815,6 +832,13 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.chunk_next.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.chunk_count.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
   SG_CUDA(d, sc.owner_first.ensure(static_cast<size_t>(pl.ntiles) * QUAD_OWNERS * 4));
+  // pre-images of the depth the coverage pass writes back (early-Z only)
+  P.zbackup = nullptr;
+  P.zbackup_tile_words = TILE * TILE * pl.max_samples;
+  if (pl.any_early_z) {
+    SG_CUDA(d, sc.zbackup.ensure(static_cast<size_t>(pl.ntiles) * P.zbackup_tile_words * 4));
+    P.zbackup = static_cast<uint32_t*>(sc.zbackup.ptr);
+  }
   // learned-filter lookups: the plain queue has room for the pixels of twice
   // the pass's target quads (as the fragment buffer; a pass that queues more
   // reports OVF_AF_QUEUE and the room grows), the network's for 2^23 lookups
@@ -838,7 +862,7 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   }
   v.params = static_cast<uint8_t*>(sc.params.ptr);
   P.counters = static_cast<PassCounters*>(sc.counters.ptr);
-  P.sticky = static_cast<unsigned int*>(sc.sticky.ptr);
+  P.sticky = d->status;
   P.draw_stats = static_cast<DrawStatsDev*>(sc.stats.ptr);
   P.slot_rec = static_cast<uint32_t*>(sc.slot_rec.ptr);
   P.recs = static_cast<float4*>(sc.recs.ptr);
@@ -876,7 +900,7 @@ int32_t scratch_static(sg_device* d, uint8_t* base, PassPlan const& pl, PlanLayo
     return q;
   };
   P.counters = reinterpret_cast<PassCounters*>(take(sizeof(PassCounters)));
-  P.sticky = reinterpret_cast<unsigned int*>(take(sizeof(unsigned int)));
+  P.sticky = d->status;  // allocated with the device
   P.draw_stats = reinterpret_cast<DrawStatsDev*>(take(pl.draws.size() * sizeof(DrawStatsDev)));
   v.params = take(L.bytes);
   P.slot_rec = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(pl.nslots) * 4));
@@ -886,6 +910,10 @@ int32_t scratch_static(sg_device* d, uint8_t* base, PassPlan const& pl, PlanLayo
   v.scan_sums = reinterpret_cast<uint32_t*>(take((pl.ncounts / 4096 + 2) * 4));
   P.tile_begin = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(pl.ntiles) + 1) * 4));
   P.owner_first = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(pl.ntiles) * QUAD_OWNERS * 4));
+  P.zbackup_tile_words = TILE * TILE * pl.max_samples;
+  P.zbackup = pl.any_early_z ? reinterpret_cast<uint32_t*>(take(static_cast<size_t>(pl.ntiles) *
+                                                                 P.zbackup_tile_words * 4))
+                             : nullptr;
   if (off > SG_STATIC_SCRATCH_TABLE_LIMIT) {
     char msg[200];
     std::snprintf(msg, sizeof(msg),
@@ -919,16 +947,21 @@ int32_t scratch_static(sg_device* d, uint8_t* base, PassPlan const& pl, PlanLayo
 
 // Launches the kernel chain of a pass whose scratch is bound in `v`.  With
 // `upload`, the parameter blocks are copied from `packed` first (stream
-// ordered).  Returns the number of kernels launched in `*kernels`.
+// ordered).  Returns the number of kernels launched in `*kernels`.  The
+// pass's last kernel counts it as completed in the device's status words
+// (none when the pass launches no kernel).
 int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vector<uint8_t> const* packed,
                     bool profile, uint32_t* kernels) {
   cudaStream_t s = d->stream;
   PassParams P = v.P;
   P.cover_item = d->tuning.cover_item;
   P.split_entries = d->tuning.split_entries;
+  bool const raster = !pl.draws.empty() && pl.nprims > 0 && pl.ntiles > 0;
+  P.count_pass = raster && pl.resolves.empty() ? 1u : 0u;
   uint32_t k = 0;
   if (!pl.clears.empty()) k += launch_jobs(pl.clears.data(), static_cast<uint32_t>(pl.clears.size()),
-                                           static_cast<uint32_t>(d->num_sms), s);
+                                           static_cast<uint32_t>(d->num_sms), s, d->status,
+                                           !raster && pl.resolves.empty());
   if (!pl.draws.empty()) {
     if (packed) SG_CUDA(d, cudaMemcpyAsync(v.params, packed->data(), packed->size(), cudaMemcpyHostToDevice, s));
     if (P.af_capacity)  // the texture-unit copies the filter's feature taps read, current as of this pass
@@ -988,6 +1021,10 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       }
       stage_end(d, 3, ev);
       ev = stage_begin(d, profile);
+      if (P.zbackup) {  // undoes the coverage pass's depth writes if the pass overflowed
+        launch_cover_rollback(P, std::min<uint32_t>(pl.ntiles, sms * 8), s);
+        ++k;
+      }
       launch_merge(P, merge_grid, s);
       stage_end(d, 4, ev);
       k += P.tile_order ? 11 : 9;  // geometry, bin count, 3 scans, tile ranges (+ 2 order), bin fill, cover, merge
@@ -996,20 +1033,21 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
     d->prof.draws += pl.draws.size();
   }
   if (!pl.resolves.empty()) k += launch_jobs(pl.resolves.data(), static_cast<uint32_t>(pl.resolves.size()),
-                                             static_cast<uint32_t>(d->num_sms), s);
+                                             static_cast<uint32_t>(d->num_sms), s, d->status, true);
   SG_CUDA(d, cudaGetLastError());
   *kernels = k;
   return SG_OK;
 }
 
-// Reads back the counters of the last immediate pass (after a stream sync)
-// and turns an overflow into SG_OUT_OF_MEMORY with raised capacities.
-int32_t check_overflow(sg_device* d, Scratch& sc, PassCounters const& c, bool fixed) {
-  if (!(c.overflow & OVF_FATAL)) return SG_OK;
+// Raises the scratch capacities an overflow (bits of PassCounters) showed
+// too small, from the pass's counters, and describes it in the device's
+// error text.  With a fixed (static) scratch nothing can grow.
+void grow_after_overflow(sg_device* d, Scratch& sc, PassCounters const& c, bool fixed) {
   char msg[256];
   if (fixed) {
     std::snprintf(msg, sizeof(msg),
-                  "static scratch exhausted: %u bin entries, %u fragment chunks, %u record units needed",
+                  "static scratch exhausted: %u bin entries, %u fragment chunks, %u record units needed; the draw "
+                  "was not drawn and its targets are untouched",
                   c.bin_entries, c.chunk_total, c.rec_units);
   } else {
     if (c.overflow & OVF_BIN) sc.entry_capacity = std::max<uint32_t>(sc.entry_capacity * 2, c.bin_entries + c.bin_entries / 4);
@@ -1018,64 +1056,175 @@ int32_t check_overflow(sg_device* d, Scratch& sc, PassCounters const& c, bool fi
       sc.af_capacity = static_cast<uint32_t>(std::min<uint64_t>(std::max<uint64_t>(2ull * sc.af_capacity,
                                                                                    c.af_plain + c.af_plain / 4),
                                                                 1u << 30));
-    std::snprintf(msg, sizeof(msg), "scratch buffer overflow (bits %u); capacities raised for later passes",
-                  c.overflow);
+    std::snprintf(msg, sizeof(msg), "scratch overflow (bits %u): capacities raised", c.overflow);
   }
   d->error = msg;
-  return SG_OUT_OF_MEMORY;
 }
 
-// Runs one assembled pass immediately.  `stats` (indexed by command) is
-// filled when given, which synchronises.
-int32_t run_plan(sg_device* d, PassPlan& pl, sg_draw_stats* stats, uint8_t* fixed) {
+// Queues the copy of the status words to the host (read by read_status once
+// the stream has been synchronised).
+int32_t queue_status(sg_device* d) {
+  SG_CUDA(d, cudaMemcpyAsync(d->status_host, d->status, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                             d->stream));
+  return SG_OK;
+}
+// The status words as queue_status copied them: the overflow bits, and the
+// passes completed since the host last looked.  Overflow bits are cleared on
+// the device (the completed-pass count runs on).
+int32_t read_status(sg_device* d, unsigned int& bits, unsigned int& done) {
+  bits = d->status_host[0];
+  done = d->status_host[1] - d->done_base;
+  d->done_base = d->status_host[1];
+  if (bits) SG_CUDA(d, cudaMemsetAsync(d->status, 0, sizeof(unsigned int), d->stream));
+  return SG_OK;
+}
+
+// Runs one assembled pass.  Without `sync` the pass is queued on the stream
+// and logged (so the host can run it again if it or an earlier pass
+// overflows).  With `sync` (and always when `stats`, indexed by command,
+// is given) the call waits for it: an overflow of the pass left its targets
+// untouched (the coverage pass's depth writes are rolled back, nothing is
+// merged), so the capacities are raised and the pass is run again; a
+// static-scratch pass cannot grow and returns SG_OUT_OF_MEMORY, not drawn.
+// The caller has handled earlier passes first (settle).
+int32_t run_plan(sg_device* d, PassPlan& pl, sg_draw_stats* stats, uint8_t* fixed, bool sync) {
   if (pl.empty()) return SG_OK;
   finalize(pl, d);
-  PlanLayout L = layout_of(pl);
-  std::vector<uint8_t> packed;
-  ScratchView v;
-  if (!pl.draws.empty()) {
-    int32_t r = fixed ? scratch_static(d, fixed, pl, L, v) : scratch_arenas(d, d->scratch, pl, L, true, v);
+  sync = sync || stats != nullptr;
+  for (int attempt = 0;; ++attempt) {
+    PlanLayout L = layout_of(pl);
+    std::vector<uint8_t> packed;
+    ScratchView v;
+    if (!pl.draws.empty()) {
+      int32_t r = fixed ? scratch_static(d, fixed, pl, L, v) : scratch_arenas(d, d->scratch, pl, L, true, v);
+      if (r != SG_OK) return r;
+      bind_params(v.P, v.params, L, pl);
+      pack_plan(pl, L, packed);
+    }
+    uint32_t kernels = 0;
+    int32_t r = launch_pass(d, pl, v, pl.draws.empty() ? nullptr : &packed, !fixed, &kernels);
     if (r != SG_OK) return r;
-    bind_params(v.P, v.params, L, pl);
-    pack_plan(pl, L, packed);
-  }
-  uint32_t kernels = 0;
-  if (fixed && !pl.draws.empty()) {
-    SG_CUDA(d, cudaMemsetAsync(v.P.sticky, 0, sizeof(unsigned int), d->stream));
-    d->static_sticky = v.P.sticky;
-  }
-  int32_t r = launch_pass(d, pl, v, pl.draws.empty() ? nullptr : &packed, !fixed, &kernels);
-  if (r != SG_OK) return r;
-  d->prof.launches += kernels;
-  if (pl.draws.empty()) return SG_OK;
-  if (!fixed) d->scratch.pending = true;
-  if (!stats) {
-    // the parameter blocks were copied from pageable host memory, which the
-    // copy staged before returning; overflows are reported at sg_sync
+    d->prof.launches += kernels;
+    if (!sync) {
+      // the parameter blocks were copied from pageable host memory, which the
+      // copy staged before returning
+      if (kernels) {
+        LogEntry e;
+        e.plan = std::move(pl);
+        e.fixed = fixed != nullptr;
+        d->log.push_back(std::move(e));
+      }
+      return SG_OK;
+    }
+    bool const counted = !pl.draws.empty();
+    if (counted) {
+      SG_CUDA(d, cudaMemcpyAsync(d->counters_host, v.P.counters, sizeof(PassCounters), cudaMemcpyDeviceToHost,
+                                 d->stream));
+      if (stats) {
+        if (d->stats_host_cap < pl.draws.size()) {  // (one entry is allocated with the device)
+          if (d->stats_host) cudaFreeHost(d->stats_host);
+          d->stats_host = nullptr;
+          d->stats_host_cap = 0;
+          SG_CUDA(d, cudaMallocHost(&d->stats_host, pl.draws.size() * sizeof(DrawStatsDev)));
+          d->stats_host_cap = pl.draws.size();
+        }
+        SG_CUDA(d, cudaMemcpyAsync(d->stats_host, v.P.draw_stats, pl.draws.size() * sizeof(DrawStatsDev),
+                                   cudaMemcpyDeviceToHost, d->stream));
+      }
+    }
+    if (int32_t rs = queue_status(d)) return rs;
+    SG_CUDA(d, cudaStreamSynchronize(d->stream));
+    unsigned int bits = 0, done = 0;
+    if (int32_t rs = read_status(d, bits, done)) return rs;
+    if (bits & OVF_FATAL) {
+      PassCounters c = counted ? *d->counters_host : PassCounters{};
+      c.overflow |= bits;
+      grow_after_overflow(d, d->scratch, c, fixed != nullptr);
+      if (fixed || attempt >= 8) return SG_OUT_OF_MEMORY;
+      continue;
+    }
+    if (bits & OVF_AF_TIMEOUT) {
+      d->error = "learned filter: a tensor-core wait timed out";
+      return SG_TIMEOUT;
+    }
+    if (stats)
+      for (size_t i = 0; i < pl.draws.size(); ++i) {
+        sg_draw_stats& o = stats[pl.draw_cmd[i]];
+        o.ia_primitives = pl.draws[i].prim_count;
+        o.cprimitives = d->stats_host[i].cprimitives;
+        o.ps_invocations = d->stats_host[i].ps_invocations;
+        o.backend_input_pixels = d->stats_host[i].backend_input_pixels;
+        o.ia_vertices = 3ull * pl.draws[i].prim_count;  // default_vertex_cache.cpp:363
+        o.vs_invocations = d->stats_host[i].vs_invocations;
+        o.cinvocations = pl.draws[i].prim_count;        // geom_setup_engine.cpp:108-123
+      }
     return SG_OK;
   }
-  SG_CUDA(d, cudaMemcpyAsync(d->counters_host, v.P.counters, sizeof(PassCounters), cudaMemcpyDeviceToHost, d->stream));
-  if (d->stats_host_cap < pl.draws.size()) {
-    if (d->stats_host) cudaFreeHost(d->stats_host);
-    d->stats_host = nullptr;
-    d->stats_host_cap = 0;
-    SG_CUDA(d, cudaMallocHost(&d->stats_host, pl.draws.size() * sizeof(DrawStatsDev)));
-    d->stats_host_cap = pl.draws.size();
+}
+
+void graph_regrow(sg_device* d, sg_graph* g);
+
+// Waits for the logged passes and reads the status words.  If a pass
+// overflowed, it and every pass after it did nothing (pass_gated); they run
+// again now, each waited for and grown until it fits, and every recorded
+// graph among them gets larger scratch.  Returns an error of the work since
+// the last look (an SG_OUT_OF_MEMORY of a static-scratch draw that did not
+// fit, SG_TIMEOUT of the learned filter), once.
+// `queued`: the caller has queued the status copy and synchronised.
+int32_t settle(sg_device* d, bool queued = false) {
+  int32_t r = d->pending;
+  d->pending = SG_OK;
+  if (d->log.empty()) return r;
+  if (!queued) {
+    if (int32_t rs = queue_status(d)) return rs;
+    SG_CUDA(d, cudaStreamSynchronize(d->stream));
   }
-  SG_CUDA(d, cudaMemcpyAsync(d->stats_host, v.P.draw_stats, pl.draws.size() * sizeof(DrawStatsDev),
-                             cudaMemcpyDeviceToHost, d->stream));
-  SG_CUDA(d, cudaStreamSynchronize(d->stream));
-  r = check_overflow(d, d->scratch, *d->counters_host, fixed != nullptr);
-  if (r != SG_OK && !fixed) SG_CUDA(d, cudaMemset(v.P.sticky, 0, sizeof(unsigned int)));  // reported here
-  if (r != SG_OK) return r;
-  for (size_t i = 0; i < pl.draws.size(); ++i) {
-    sg_draw_stats& o = stats[pl.draw_cmd[i]];
-    o.ia_primitives = pl.draws[i].prim_count;
-    o.cprimitives = d->stats_host[i].cprimitives;
-    o.ps_invocations = d->stats_host[i].ps_invocations;
-    o.backend_input_pixels = d->stats_host[i].backend_input_pixels;
+  unsigned int bits = 0, done = 0;
+  if (int32_t rs = read_status(d, bits, done)) return rs;
+  std::vector<LogEntry> entries = std::move(d->log);
+  d->log.clear();
+  if ((bits & OVF_AF_TIMEOUT) && r == SG_OK) {
+    d->error = "learned filter: a tensor-core wait timed out";
+    r = SG_TIMEOUT;
   }
+  if (!(bits & OVF_FATAL)) return r;
+  std::set<sg_graph*> regrow;
+  std::string err;
+  for (size_t i = std::min<size_t>(done, entries.size()); i < entries.size(); ++i) {
+    LogEntry& e = entries[i];
+    PassPlan pl = e.graph ? e.graph->plans[e.pass] : std::move(e.plan);
+    if (e.graph) regrow.insert(e.graph);
+    int32_t ri = run_plan(d, pl, nullptr, e.fixed ? d->static_base : nullptr, true);
+    if (ri != SG_OK && r == SG_OK) {
+      r = ri;
+      err = d->error;
+    }
+  }
+  for (sg_graph* g : regrow) graph_regrow(d, g);
+  if (r != SG_OK) d->error = err.empty() ? d->error : err;
+  return r;
+}
+
+// Settles before a call changes what logged passes read or write (uploads,
+// mip generation, destruction): a replay must see the inputs the passes
+// were issued with.  An error of that work is kept for sg_sync.
+int32_t settle_before_change(sg_device* d) {
+  if (d->log.empty()) return SG_OK;
+  int32_t r = settle(d);
+  if (r == SG_CUDA_ERROR) return r;
+  d->pending = r;
   return SG_OK;
+}
+
+// Waits for the logged passes when the log is long; keeps an error for sg_sync.
+int32_t settle_if_long(sg_device* d) {
+  if (d->log.size() < LOG_LIMIT) return SG_OK;
+  int32_t r = settle(d);
+  if (r != SG_OK && r != SG_CUDA_ERROR) {
+    d->pending = r;
+    return SG_OK;
+  }
+  return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -1249,50 +1398,118 @@ int32_t plan_commands(sg_device* d, sg_command const* cmds, uint32_t n, Sink&& s
 }
 
 int32_t submit_impl(sg_device* d, sg_command const* cmds, uint32_t n, sg_draw_stats* stats, uint8_t* fixed) {
-  if (stats) std::memset(stats, 0, sizeof(sg_draw_stats) * n);
-  return plan_commands(d, cmds, n, [&](PassPlan& pl) { return run_plan(d, pl, stats, fixed); });
+  if (stats) {
+    std::memset(stats, 0, sizeof(sg_draw_stats) * n);
+    // statistics wait for this list's passes: the earlier ones come first
+    int32_t r = settle(d);
+    if (r == SG_CUDA_ERROR) return r;
+    d->pending = r;
+  }
+  int32_t r = plan_commands(d, cmds, n, [&](PassPlan& pl) { return run_plan(d, pl, stats, fixed, false); });
+  if (r != SG_OK) return r;
+  return stats ? SG_OK : settle_if_long(d);
 }
 
-// After a stream sync: the overflow bits the passes since the last look left
-// in a scratch's sticky word (immediate passes and each graph's).
-int32_t check_sticky(sg_device* d, Scratch& sc, char const* what) {
-  if (!sc.pending || !sc.sticky.ptr) return SG_OK;
-  sc.pending = false;
-  SG_CUDA(d, cudaMemcpy(d->sticky_host, sc.sticky.ptr, sizeof(unsigned int), cudaMemcpyDeviceToHost));
-  unsigned int bits = *d->sticky_host;
-  if (!(bits & (OVF_FATAL | OVF_AF_TIMEOUT))) return SG_OK;
-  SG_CUDA(d, cudaMemset(sc.sticky.ptr, 0, sizeof(unsigned int)));
-  if (!(bits & OVF_FATAL)) {
-    d->error = "learned filter: a tensor-core wait timed out";
-    return SG_TIMEOUT;
+// Sizes a graph's private scratch for its passes (capacities in
+// g->scratch), uploads every pass's parameter blocks and captures all passes
+// into one CUDA graph.
+int32_t graph_build(sg_device* d, sg_graph* g) {
+  std::vector<PlanLayout> layouts;
+  size_t total = 0;
+  for (PassPlan const& pl : g->plans) {
+    layouts.push_back(layout_of(pl));
+    total += layouts.back().bytes;
   }
-  if (&sc == &d->scratch) {
-    PassCounters c{};
-    c.overflow = bits;
-    c.bin_entries = sc.entry_capacity;
-    c.chunk_total = sc.chunk_capacity;
-    c.af_plain = sc.af_capacity;
-    return check_overflow(d, sc, c, false);
-  }
-  d->error = what;
-  return SG_OUT_OF_MEMORY;
-}
-
-int32_t check_pending(sg_device* d) {
-  int32_t r = check_sticky(d, d->scratch, "");
-  if (d->static_sticky) {
-    SG_CUDA(d, cudaMemcpy(d->sticky_host, d->static_sticky, sizeof(unsigned int), cudaMemcpyDeviceToHost));
-    d->static_sticky = nullptr;
-    if (*d->sticky_host & OVF_FATAL) {
-      d->error = "static scratch exhausted by a draw since the last sync";
-      if (r == SG_OK) r = SG_OUT_OF_MEMORY;
+  SG_CUDA(d, g->params.ensure(std::max<size_t>(total, 256)));
+  std::vector<ScratchView> views(g->plans.size());
+  size_t off = 0;
+  int32_t r = SG_OK;
+  for (size_t i = 0; i < g->plans.size(); ++i) {
+    PassPlan const& pl = g->plans[i];
+    if (!pl.draws.empty()) {
+      r = scratch_arenas(d, g->scratch, pl, layouts[i], false, views[i]);
+      if (r != SG_OK) return r;
+      views[i].params = static_cast<uint8_t*>(g->params.ptr) + off;
+      bind_params(views[i].P, views[i].params, layouts[i], pl);
+      std::vector<uint8_t> packed;
+      pack_plan(pl, layouts[i], packed);
+      SG_CUDA(d, cudaMemcpy(views[i].params, packed.data(), packed.size(), cudaMemcpyHostToDevice));
     }
+    off += layouts[i].bytes;
   }
-  for (sg_graph* g : d->graphs) {
-    int32_t rg = check_sticky(d, g->scratch, "a recorded graph overflowed its scratch; record it again");
-    if (r == SG_OK) r = rg;
+  // every pass binds the same (largest) scratch arenas; rebind after all growth
+  for (size_t i = 0; i < g->plans.size(); ++i) {
+    if (g->plans[i].draws.empty()) continue;
+    uint8_t* params = views[i].params;
+    r = scratch_arenas(d, g->scratch, g->plans[i], layouts[i], false, views[i]);
+    if (r != SG_OK) return r;
+    views[i].params = params;
+    bind_params(views[i].P, params, layouts[i], g->plans[i]);
   }
-  return r;
+  SG_CUDA(d, cudaStreamSynchronize(d->stream));
+  SG_CUDA(d, cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
+  uint32_t kernels = 0;
+  bool saved = d->profiling;
+  d->profiling = false;
+  g->plan_kernels.assign(g->plans.size(), 0);
+  for (size_t i = 0; i < g->plans.size() && r == SG_OK; ++i) {
+    uint32_t k = 0;
+    r = launch_pass(d, g->plans[i], views[i], nullptr, false, &k);
+    g->plan_kernels[i] = k;
+    kernels += k;
+  }
+  d->profiling = saved;
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(d->stream, &graph);
+  if (r != SG_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return r;
+  }
+  if (e != cudaSuccess) return cuda_fail(d, e, "cudaStreamEndCapture");
+  g->graph = graph;
+  e = cudaGraphInstantiate(&g->exec, graph, 0);
+  if (e != cudaSuccess) return cuda_fail(d, e, "cudaGraphInstantiate");
+  g->kernels = kernels;
+  return SG_OK;
+}
+
+// After a replay of a graph's overflowing passes (which grew the device's
+// own capacities to fit them): the graph's scratch takes at least those
+// capacities and the graph is recorded again.
+void graph_regrow(sg_device* d, sg_graph* g) {
+  cudaStreamSynchronize(d->stream);
+  g->scratch.entry_capacity = std::max(g->scratch.entry_capacity, d->scratch.entry_capacity);
+  g->scratch.chunk_capacity = std::max(g->scratch.chunk_capacity, d->scratch.chunk_capacity);
+  g->scratch.af_capacity = std::max(g->scratch.af_capacity, d->scratch.af_capacity);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  g->exec = nullptr;
+  g->graph = nullptr;
+  if (graph_build(d, g) != SG_OK) {  // sg_graph_launch reports the graph unusable
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    g->exec = nullptr;
+  }
+}
+
+// A device-to-host copy after the logged passes: the status words travel
+// with it (one synchronisation); if a pass overflowed, the passes run again
+// and the copy is repeated.
+int32_t download(sg_device* d, void* dst, void const* src, size_t size) {
+  bool const logged = !d->log.empty();
+  SG_CUDA(d, cudaMemcpyAsync(dst, src, size, cudaMemcpyDeviceToHost, d->stream));
+  if (logged)
+    if (int32_t r = queue_status(d)) return r;
+  SG_CUDA(d, cudaStreamSynchronize(d->stream));
+  if (!logged) return SG_OK;
+  bool const overflowed = (d->status_host[0] & OVF_FATAL) != 0u;
+  int32_t r = settle(d, true);
+  if (r == SG_CUDA_ERROR) return r;
+  d->pending = r;
+  if (overflowed) {
+    SG_CUDA(d, cudaMemcpyAsync(dst, src, size, cudaMemcpyDeviceToHost, d->stream));
+    SG_CUDA(d, cudaStreamSynchronize(d->stream));
+  }
+  return SG_OK;
 }
 
 }  // namespace
@@ -1315,7 +1532,14 @@ int32_t sg_device_create(int32_t cuda_device, void* cuda_stream, sg_device** out
   }
   if (cudaMallocHost(&d->counters_host, sizeof(PassCounters)) != cudaSuccess) return SG_OUT_OF_MEMORY;
   std::memset(d->counters_host, 0, sizeof(PassCounters));
-  if (cudaMallocHost(&d->sticky_host, sizeof(unsigned int)) != cudaSuccess) return SG_OUT_OF_MEMORY;
+  if (cudaMallocHost(&d->status_host, 2 * sizeof(unsigned int)) != cudaSuccess) return SG_OUT_OF_MEMORY;
+  // statistics of a one-draw pass never allocate (the static-scratch entry point)
+  if (cudaMallocHost(&d->stats_host, sizeof(DrawStatsDev)) != cudaSuccess) return SG_OUT_OF_MEMORY;
+  d->stats_host_cap = 1;
+  if (cudaMalloc(&d->status, 2 * sizeof(unsigned int)) != cudaSuccess) return SG_OUT_OF_MEMORY;
+  if (cudaMemset(d->status, 0, 2 * sizeof(unsigned int)) != cudaSuccess) return SG_CUDA_ERROR;
+  // the static scratch's address on this device, which is current here
+  d->static_base = static_scratch_address(cuda_device);
   if (init_cover() != cudaSuccess || init_cover2() != cudaSuccess || init_learned() != cudaSuccess ||
       init_af_filter() != cudaSuccess)
     return SG_CUDA_ERROR;
@@ -1344,7 +1568,8 @@ void sg_device_destroy(sg_device* d) {
   }
   d->scratch.release();
   cudaFreeHost(d->counters_host);
-  cudaFreeHost(d->sticky_host);
+  cudaFreeHost(d->status_host);
+  if (d->status) cudaFree(d->status);
   if (d->stats_host) cudaFreeHost(d->stats_host);
   if (d->prof_af) cudaFree(d->prof_af);
   for (cudaEvent_t e : d->event_pool) cudaEventDestroy(e);
@@ -1355,7 +1580,7 @@ void sg_device_destroy(sg_device* d) {
 int32_t sg_sync(sg_device* d) {
   if (!d) return SG_INVALID_PARAMETER;
   SG_CUDA(d, cudaStreamSynchronize(d->stream));
-  return check_pending(d);
+  return settle(d);
 }
 
 const char* sg_last_error(sg_device* d) { return d ? d->error.c_str() : ""; }
@@ -1410,6 +1635,7 @@ int32_t sg_buffer_upload(sg_device* d, uint32_t h, size_t off, const void* src, 
   if (!d) return SG_INVALID_PARAMETER;
   auto it = d->buffers.find(h);
   if (it == d->buffers.end() || off + size > it->second.size || (!src && size)) return SG_INVALID_PARAMETER;
+  if (int32_t r = settle_before_change(d)) return r;
   SG_CUDA(d, cudaMemcpyAsync(it->second.ptr + off, src, size, cudaMemcpyHostToDevice, d->stream));
   SG_CUDA(d, cudaStreamSynchronize(d->stream));
   return SG_OK;
@@ -1418,14 +1644,13 @@ int32_t sg_buffer_download(sg_device* d, uint32_t h, size_t off, void* dst, size
   if (!d) return SG_INVALID_PARAMETER;
   auto it = d->buffers.find(h);
   if (it == d->buffers.end() || off + size > it->second.size || (!dst && size)) return SG_INVALID_PARAMETER;
-  SG_CUDA(d, cudaMemcpyAsync(dst, it->second.ptr + off, size, cudaMemcpyDeviceToHost, d->stream));
-  SG_CUDA(d, cudaStreamSynchronize(d->stream));
-  return SG_OK;
+  return download(d, dst, it->second.ptr + off, size);
 }
 int32_t sg_buffer_destroy(sg_device* d, uint32_t h) {
   if (!d) return SG_INVALID_PARAMETER;
   auto it = d->buffers.find(h);
   if (it == d->buffers.end()) return SG_INVALID_PARAMETER;
+  if (int32_t r = settle_before_change(d)) return r;
   cudaStreamSynchronize(d->stream);
   cudaFree(it->second.ptr);
   d->buffers.erase(it);
@@ -1456,6 +1681,7 @@ int32_t sg_texture_upload(sg_device* d, uint32_t h, uint32_t level, const void* 
   if (!t || level >= t->levels.size() || !src) return SG_INVALID_PARAMETER;
   Level const& l = t->levels[level];
   if (size != static_cast<size_t>(l.w) * l.h * t->samples * t->esz) return SG_INVALID_PARAMETER;
+  if (int32_t r = settle_before_change(d)) return r;
   SG_CUDA(d, cudaMemcpyAsync(l.ptr, src, size, cudaMemcpyHostToDevice, d->stream));
   SG_CUDA(d, cudaStreamSynchronize(d->stream));
   return SG_OK;
@@ -1465,9 +1691,7 @@ int32_t sg_texture_download(sg_device* d, uint32_t h, uint32_t level, void* dst,
   if (!t || level >= t->levels.size() || !dst) return SG_INVALID_PARAMETER;
   Level const& l = t->levels[level];
   if (size != static_cast<size_t>(l.w) * l.h * t->samples * t->esz) return SG_INVALID_PARAMETER;
-  SG_CUDA(d, cudaMemcpyAsync(dst, l.ptr, size, cudaMemcpyDeviceToHost, d->stream));
-  SG_CUDA(d, cudaStreamSynchronize(d->stream));
-  return SG_OK;
+  return download(d, dst, l.ptr, size);
 }
 // texture_2d::gen_mipmap(filter, true) (texture2d.cpp:25-36, texture.h:26-36)
 int32_t sg_texture_gen_mipmap(sg_device* d, uint32_t h, uint32_t filter) {
@@ -1479,6 +1703,7 @@ int32_t sg_texture_gen_mipmap(sg_device* d, uint32_t h, uint32_t filter) {
     ++n;
   }
   if (n > static_cast<uint32_t>(SG_MAX_LEVELS)) return SG_INVALID_PARAMETER;
+  if (int32_t r = settle_before_change(d)) return r;
   SG_CUDA(d, cudaStreamSynchronize(d->stream));
   af_release_arrays(*t);
   for (size_t i = 1; i < t->levels.size(); ++i) cudaFree(t->levels[i].ptr);
@@ -1510,6 +1735,7 @@ int32_t sg_texture_info(sg_device* d, uint32_t h, uint32_t level, uint32_t* w, u
 int32_t sg_texture_destroy(sg_device* d, uint32_t h) {
   Texture* t = d ? find_tex(d, h) : nullptr;
   if (!t) return SG_INVALID_PARAMETER;
+  if (int32_t r = settle_before_change(d)) return r;
   cudaStreamSynchronize(d->stream);
   af_release_arrays(*t);
   for (auto& l : t->levels) cudaFree(l.ptr);
@@ -1530,6 +1756,7 @@ int32_t sg_sampler_destroy(sg_device* d, uint32_t h) {
   if (!d) return SG_INVALID_PARAMETER;
   auto it = d->samplers.find(h);
   if (it == d->samplers.end()) return SG_INVALID_PARAMETER;
+  if (int32_t r = settle_before_change(d)) return r;
   cudaStreamSynchronize(d->stream);
   af_release_objects(it->second);
   d->samplers.erase(it);
@@ -1546,18 +1773,14 @@ int32_t sg_draw(sg_device* d, const sg_draw_desc* desc, sg_draw_stats* stats) {
 
 int32_t sg_draw_static_scratch(sg_device* d, const sg_draw_desc* desc, sg_draw_stats* stats) {
   if (!d || !desc) return SG_INVALID_PARAMETER;
-  int cur = -1;
-  SG_CUDA(d, cudaGetDevice(&cur));
-  if (cur != d->ordinal) SG_CUDA(d, cudaSetDevice(d->ordinal));
-  uint8_t* base = static_scratch_address(d->ordinal);
-  if (!base) {
-    d->error = "sg_draw_static_scratch: static scratch address lookup failed";
+  if (!d->static_base) {
+    d->error = "sg_draw_static_scratch: the static scratch's address could not be looked up on this device";
     return SG_CUDA_ERROR;
   }
   sg_command c{};
   c.type = SG_CMD_DRAW;
   c.draw = desc;
-  return submit_impl(d, &c, 1, stats, base);
+  return submit_impl(d, &c, 1, stats, d->static_base);
 }
 
 int32_t sg_submit(sg_device* d, const sg_command* cmds, uint32_t n, sg_draw_stats* stats) {
@@ -1609,80 +1832,26 @@ int32_t sg_graph_create(sg_device* d, const sg_command* cmds, uint32_t n, sg_gra
     return SG_OK;
   });
   if (r != SG_OK) return r;
-  // 2. run the list once to learn each pass's needs
-  SG_CUDA(d, cudaStreamSynchronize(d->stream));
-  uint32_t need_entries = 1, need_chunks = 1;
+  // 2. run the list once (each pass waited for, grown until it fits) to
+  //    learn each pass's needs
+  r = settle(d);
+  if (r == SG_CUDA_ERROR) return r;
+  d->pending = r;
+  uint32_t need_entries = 1, need_chunks = 1, need_af = 0;
   for (PassPlan& pl : g->plans) {
     PassPlan run = pl;
-    for (int attempt = 0;; ++attempt) {
-      std::vector<sg_draw_stats> st(n);
-      r = run_plan(d, run, st.data(), nullptr);
-      if (r == SG_OK) break;
-      if (r != SG_OUT_OF_MEMORY || attempt >= 4) return r;
-      run = pl;  // capacities were raised; the overflowing pass left its targets untouched only on
-                 // bin or record overflow, so a fragment overflow here is reported to the caller
-      if (d->counters_host->overflow & OVF_FRAG) return r;
-    }
+    std::vector<sg_draw_stats> st(n);
+    r = run_plan(d, run, st.data(), nullptr, true);
+    if (r != SG_OK) return r;
     need_entries = std::max(need_entries, d->counters_host->bin_entries);
     need_chunks = std::max(need_chunks, d->counters_host->chunk_total);
+    need_af = std::max(need_af, d->counters_host->af_plain);
   }
   g->scratch.entry_capacity = need_entries + need_entries / 4 + 1024;
   g->scratch.chunk_capacity = need_chunks + need_chunks / 4 + 256;
-  // 3. parameter blocks of every pass, resident
-  std::vector<PlanLayout> layouts;
-  size_t total = 0;
-  for (PassPlan const& pl : g->plans) {
-    layouts.push_back(layout_of(pl));
-    total += layouts.back().bytes;
-  }
-  SG_CUDA(d, g->params.ensure(std::max<size_t>(total, 256)));
-  std::vector<ScratchView> views(g->plans.size());
-  size_t off = 0;
-  for (size_t i = 0; i < g->plans.size(); ++i) {
-    PassPlan const& pl = g->plans[i];
-    if (!pl.draws.empty()) {
-      r = scratch_arenas(d, g->scratch, pl, layouts[i], false, views[i]);
-      if (r != SG_OK) return r;
-      views[i].params = static_cast<uint8_t*>(g->params.ptr) + off;
-      bind_params(views[i].P, views[i].params, layouts[i], pl);
-      std::vector<uint8_t> packed;
-      pack_plan(pl, layouts[i], packed);
-      SG_CUDA(d, cudaMemcpy(views[i].params, packed.data(), packed.size(), cudaMemcpyHostToDevice));
-    }
-    off += layouts[i].bytes;
-  }
-  // every pass binds the same (largest) scratch arenas; rebind after all growth
-  for (size_t i = 0; i < g->plans.size(); ++i) {
-    if (g->plans[i].draws.empty()) continue;
-    uint8_t* params = views[i].params;
-    r = scratch_arenas(d, g->scratch, g->plans[i], layouts[i], false, views[i]);
-    if (r != SG_OK) return r;
-    views[i].params = params;
-    bind_params(views[i].P, params, layouts[i], g->plans[i]);
-  }
-  // 4. capture
-  SG_CUDA(d, cudaStreamSynchronize(d->stream));
-  SG_CUDA(d, cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
-  uint32_t kernels = 0;
-  bool saved = d->profiling;
-  d->profiling = false;
-  for (size_t i = 0; i < g->plans.size() && r == SG_OK; ++i) {
-    uint32_t k = 0;
-    r = launch_pass(d, g->plans[i], views[i], nullptr, false, &k);
-    kernels += k;
-  }
-  d->profiling = saved;
-  cudaGraph_t graph = nullptr;
-  cudaError_t e = cudaStreamEndCapture(d->stream, &graph);
-  if (r != SG_OK) {
-    if (graph) cudaGraphDestroy(graph);
-    return r;
-  }
-  if (e != cudaSuccess) return cuda_fail(d, e, "cudaStreamEndCapture");
-  g->graph = graph;
-  e = cudaGraphInstantiate(&g->exec, graph, 0);
-  if (e != cudaSuccess) return cuda_fail(d, e, "cudaGraphInstantiate");
-  g->kernels = kernels;
+  g->scratch.af_capacity = need_af ? std::min<uint32_t>(need_af + need_af / 4 + 1024, 1u << 30) : 0u;
+  r = graph_build(d, g.get());
+  if (r != SG_OK) return r;
   *out = g.release();
   d->graphs.insert(*out);
   return SG_OK;
@@ -1690,10 +1859,20 @@ int32_t sg_graph_create(sg_device* d, const sg_command* cmds, uint32_t n, sg_gra
 
 int32_t sg_graph_launch(sg_device* d, sg_graph* g) {
   if (!d || !g || !d->graphs.count(g)) return SG_INVALID_PARAMETER;
+  if (!g->exec) {
+    d->error = "sg_graph_launch: the graph could not be recorded again after an overflow";
+    return SG_FAILED;
+  }
   SG_CUDA(d, cudaGraphLaunch(g->exec, d->stream));
-  g->scratch.pending = true;
+  for (uint32_t k = 0; k < g->plans.size(); ++k)
+    if (g->plan_kernels[k]) {
+      LogEntry e;
+      e.graph = g;
+      e.pass = k;
+      d->log.push_back(std::move(e));
+    }
   d->prof.launches += g->kernels;
-  return SG_OK;
+  return settle_if_long(d);
 }
 
 int32_t sg_graph_info(sg_device* d, sg_graph* g, uint32_t* passes, uint32_t* kernels) {
@@ -1705,6 +1884,7 @@ int32_t sg_graph_info(sg_device* d, sg_graph* g, uint32_t* passes, uint32_t* ker
 
 void sg_graph_destroy(sg_device* d, sg_graph* g) {
   if (!d || !g || !d->graphs.count(g)) return;
+  settle_before_change(d);  // (a replay reads the graph's plans)
   cudaStreamSynchronize(d->stream);
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
@@ -1729,9 +1909,11 @@ int32_t sg_set_tuning(sg_device* d, const sg_tuning* t) {
       t->merge_ctas_per_sm == 0 || t->merge_ctas_per_sm > 8 ||
       (t->cover_threads_per_block != 2 && t->cover_threads_per_block != 32))
     return SG_INVALID_PARAMETER;
+  // a changed initial capacity is where the next passes start from (they
+  // grow again on overflow)
+  if (t->bin_capacity != d->tuning.bin_capacity) d->scratch.entry_capacity = t->bin_capacity;
+  if (t->frag_chunks != d->tuning.frag_chunks) d->scratch.chunk_capacity = t->frag_chunks;
   d->tuning = *t;
-  d->scratch.entry_capacity = std::max(d->scratch.entry_capacity, t->bin_capacity);
-  d->scratch.chunk_capacity = std::max(d->scratch.chunk_capacity, t->frag_chunks);
   return SG_OK;
 }
 
@@ -1805,6 +1987,8 @@ int32_t sg_autotune(sg_device* d, const sg_command* cmds, uint32_t n, uint32_t r
 // Device internals for the learned-filter runtime (sg_af_api.cu).
 namespace sg {
 cudaStream_t device_stream(sg_device* d) { return d->stream; }
+// Before a change to what logged passes read (a learned filter's weights).
+int32_t device_settle(sg_device* d) { return settle_before_change(d); }
 int device_sms(sg_device* d) { return d->num_sms; }
 void device_set_error(sg_device* d, char const* msg) { d->error = msg; }
 int32_t device_sampler(sg_device* d, uint32_t handle, dev_sampler& out) {

@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   CvShared& sh = *reinterpret_cast<CvShared*>(smem_raw);
   uint32_t* const ztile = reinterpret_cast<uint32_t*>(smem_raw + ((sizeof(CvShared) + 15) & ~size_t(15)));
-  if (P.counters->overflow & (OVF_BIN | OVF_REC)) return;
+  if ((P.counters->overflow & (OVF_BIN | OVF_REC)) || pass_gated(P)) return;
   // item block ib = 0..63 at (ib & 7, ib >> 3); this thread's quad q of it
   // has its top-left pixel at block pixel (qx0, qy0)
   int const tid = threadIdx.x, q = tid & 3, ib = tid >> 2;
@@ -439,11 +439,17 @@ __global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
     uint32_t const qh = min(static_cast<uint32_t>(CV_PX), H - min(H, static_cast<uint32_t>(y0)));
     uint32_t const zrow = CV_PX * S;
     if (stage_z) {
+      // the quadrant's depth, and its pre-image for k_cover_rollback
+      uint32_t* const zb = P.zbackup ? P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words +
+                                           (static_cast<size_t>(by0) * 4 * TILE + bx0 * 4) * S
+                                     : nullptr;
       for (uint32_t i = tid; i < qh * zrow; i += CV_THREADS) {
         uint32_t y = i / zrow, k = i % zrow;
         if (k >= qw * S) continue;
         uint32_t x = k / S, sm = k % S;
-        ztile[i] = *reinterpret_cast<uint32_t const*>(ds_addr(T, x0 + x, y0 + y, sm));
+        uint32_t const v = *reinterpret_cast<uint32_t const*>(ds_addr(T, x0 + x, y0 + y, sm));
+        ztile[i] = v;
+        if (zb) zb[static_cast<size_t>(y) * TILE * S + k] = v;
       }
     }
     uint32_t* const zq = ztile + (iby * 4 + qy0) * zrow + (ibx * 4 + qx0) * S;
@@ -589,6 +595,37 @@ __global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
     }
     P.owner_first[static_cast<size_t>(tile) * QUAD_OWNERS + (by * 2 + (q >> 1)) * 32 + bx * 2 + (q & 1)] = L.first;
   }
+}
+
+// Undoes the coverage pass's depth write-back when the pass overflowed after
+// it (fragments, or the learned filter's lookup queue): every tile the
+// coverage pass staged gets its pre-image back from P.zbackup, so the pass
+// leaves its targets as it found them and the host can run it again.  (A
+// pass that overflowed its bins or records skipped the coverage pass.)
+__global__ void __launch_bounds__(256) k_cover_rollback(PassParams P) {
+  if (pass_gated(P)) return;
+  uint32_t const ovf = P.counters->overflow;
+  if (!(ovf & (OVF_FRAG | OVF_AF_QUEUE)) || (ovf & (OVF_BIN | OVF_REC))) return;
+  for (uint32_t tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
+    if (P.tile_begin[tile] == P.tile_begin[tile + 1]) continue;
+    TargetParams const& T = P.targets[target_of_tile(P, tile)];
+    if (!T.any_early_z) continue;
+    uint32_t const ltile = tile - T.tile_base, S = T.samples;
+    uint32_t const tx0 = (ltile % static_cast<uint32_t>(T.tiles_x)) * TILE;
+    uint32_t const ty0 = (ltile / static_cast<uint32_t>(T.tiles_x)) * TILE;
+    uint32_t const tw = min(static_cast<uint32_t>(TILE), T.width - min(T.width, tx0));
+    uint32_t const th = min(static_cast<uint32_t>(TILE), T.height - min(T.height, ty0));
+    uint32_t const* zb = P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words;
+    for (uint32_t i = threadIdx.x; i < th * TILE * S; i += blockDim.x) {
+      uint32_t const y = i / (TILE * S), k = i % (TILE * S), x = k / S, sm = k % S;
+      if (x >= tw) continue;
+      *reinterpret_cast<uint32_t*>(ds_addr(T, tx0 + x, ty0 + y, sm)) = zb[i];
+    }
+  }
+}
+
+void launch_cover_rollback(PassParams const& p, uint32_t grid, cudaStream_t s) {
+  k_cover_rollback<<<grid, 256, 0, s>>>(p);
 }
 
 void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s) {

@@ -328,6 +328,7 @@ __device__ void geometry_prim(PassParams const& P, DrawParams const& D, uint32_t
 }
 
 __global__ void __launch_bounds__(128) k_geometry(PassParams P) {
+  if (pass_gated(P)) return;
   uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t ntri = 0, draw = 0xFFFFFFFFu;
   if (g < P.nprims) {
@@ -343,11 +344,15 @@ __global__ void __launch_bounds__(128) k_geometry(PassParams P) {
     default: geometry_prim<5>(P, D, draw, prim, ntri); break;
     }
   }
-  // per-draw counter, aggregated over the lanes of one draw
+  // per-draw counters, aggregated over the lanes of one draw: clipped
+  // triangles, and vertex-shader runs (one per corner of every primitive)
   uint32_t grp = __match_any_sync(0xFFFFFFFFu, draw);
   uint32_t sum = __reduce_add_sync(grp, ntri);
-  if (draw != 0xFFFFFFFFu && sum && (threadIdx.x & 31) == static_cast<uint32_t>(__ffs(grp) - 1))
-    atomicAdd(&P.draw_stats[draw].cprimitives, static_cast<unsigned long long>(sum));
+  uint32_t const leader = static_cast<uint32_t>(__ffs(grp) - 1);
+  if (draw != 0xFFFFFFFFu && (threadIdx.x & 31) == leader) {
+    if (sum) atomicAdd(&P.draw_stats[draw].cprimitives, static_cast<unsigned long long>(sum));
+    atomicAdd(&P.draw_stats[draw].vs_invocations, 3ull * static_cast<unsigned>(__popc(grp)));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -356,7 +361,7 @@ template <bool FILL>
 __global__ void __launch_bounds__(128) k_bin(PassParams P) {
   uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
-  if (warp >= P.nchunks) return;
+  if (warp >= P.nchunks || pass_gated(P)) return;
   uint32_t const t = P.chunk_target[warp];
   TargetParams const& T = P.targets[t];
   uint32_t const c = warp - T.chunk_base, nch = T.nchunks;
@@ -534,6 +539,7 @@ __global__ void k_scan_add(uint32_t* data, size_t n, uint32_t const* sums) {
 
 // tile ranges from the scanned counts, and the overflow check
 __global__ void k_tile_ranges(PassParams P) {
+  if (pass_gated(P)) return;
   uint32_t tile = blockIdx.x * blockDim.x + threadIdx.x;
   if (tile < P.ntiles) {
     uint32_t t = upper_index(P.target_tile_base, P.ntargets, tile);
@@ -553,7 +559,7 @@ __global__ void k_tile_ranges(PassParams P) {
 // buckets (phase 0), counts[32..63] are the buckets' cursors (phase 1).
 __global__ void k_tile_order(PassParams P, uint32_t* counts, uint32_t phase) {
   uint32_t const tile = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tile >= P.ntiles) return;
+  if (tile >= P.ntiles || pass_gated(P)) return;
   uint32_t const entries = P.tile_begin[tile + 1] - P.tile_begin[tile];
   uint32_t const b = 31u - static_cast<uint32_t>(__clz(entries | 1u));
   if (phase == 0) {
@@ -572,7 +578,7 @@ __global__ void k_tile_order(PassParams P, uint32_t* counts, uint32_t phase) {
 // one atomic per warp and key.
 __global__ void __launch_bounds__(256) k_frag_classes(PassParams P, uint32_t phase) {
   __shared__ uint32_t base[128];
-  if (P.counters->overflow & OVF_FATAL) return;
+  if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
   uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
   if (phase == 1) {  // exclusive scan of the 128 key sizes
     if (threadIdx.x < 32) {

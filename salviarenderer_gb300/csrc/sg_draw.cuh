@@ -50,7 +50,7 @@ struct DrawStatsDev {
   unsigned long long cprimitives;
   unsigned long long ps_invocations;
   unsigned long long backend_input_pixels;
-  unsigned long long pad;
+  unsigned long long vs_invocations;
 };
 
 // One render target (colour and/or depth-stencil surface pair) of a pass.
@@ -160,7 +160,22 @@ struct PassParams {
   uint32_t* owner_first;
   PassCounters* counters;
   DrawStatsDev* draw_stats;     // per draw
-  unsigned int* sticky;         // overflow bits of every pass since the host last looked
+  // The device's status words, shared by every pass on the device (direct
+  // calls, recorded graphs, the static-scratch entry point): [0] the
+  // overflow bits of every pass since the host last looked -- a fatal bit
+  // there makes every later pass a no-op (pass_gated) until the host has
+  // replayed the failed pass and those after it; [1] the passes completed
+  // since then (counted by the pass's last kernel, when count_pass is set).
+  unsigned int* sticky;
+  uint32_t count_pass;
+  // Pre-images of the depth words the coverage pass stages and writes back
+  // (early-Z), tile-major: tile t's pixel (x, y) sample s at
+  // zbackup[t * zbackup_tile_words + (y * 64 + x) * samples + s], tile-local
+  // x, y.  When the pass overflows after the coverage pass has written depth
+  // back, k_cover_rollback restores them, so an overflowing pass leaves its
+  // targets as it found them.  Null when no draw of the pass tests early.
+  uint32_t* zbackup;
+  uint32_t zbackup_tile_words;
   // coverage work items: 16 or 32 pixels on a side; 32x32 items of a tile with
   // more than split_entries bin entries become 16x16
   uint32_t cover_item, split_entries;
@@ -201,6 +216,10 @@ __host__ __device__ inline uint32_t rec_flags(bool front, uint32_t shade_key, ui
 __device__ inline uint32_t frag_class(uint32_t pos) { return pos >> 28; }
 __device__ inline uint32_t rec_draw(float4 const* R) { return __float_as_uint(R[4].z); }
 __device__ inline uint32_t rec_flag_bits(float4 const* R) { return __float_as_uint(R[4].w); }
+
+// Whether an earlier pass on the device overflowed and this one must do
+// nothing: the host replays it once the overflow is handled.
+__device__ inline bool pass_gated(PassParams const& P) { return (*P.sticky & OVF_FATAL) != 0u; }
 
 // index of the last element of sorted `base[0..n)` that is <= v
 __device__ inline uint32_t upper_index(uint32_t const* base, uint32_t n, uint32_t v) {

@@ -25,7 +25,8 @@ struct SurfaceJob {
 constexpr uint32_t JOBS_PER_LAUNCH = 32;
 struct JobList {
   uint32_t n;
-  uint32_t pad;
+  uint32_t count_pass;         // this launch completes its pass: count it in status[1]
+  unsigned int* status;        // the device's status words (PassParams::sticky)
   SurfaceJob jobs[JOBS_PER_LAUNCH];
 };
 

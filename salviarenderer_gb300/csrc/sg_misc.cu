@@ -3,6 +3,7 @@
 
 #include <algorithm>
 
+#include "sg_draw.cuh"
 #include "sg_jobs.cuh"
 
 namespace sg {
@@ -79,6 +80,10 @@ __device__ void resolve_job(SurfaceJob const& j, uint32_t part, uint32_t nparts)
 // One launch runs a list of jobs: blockIdx.y selects the job, the x blocks
 // stride over its elements.
 __global__ void __launch_bounds__(256) k_jobs(JobList L) {
+  if (L.status) {  // a job of a pass: nothing after an overflow the host has not handled yet
+    if (L.status[0] & OVF_FATAL) return;
+    if (L.count_pass && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(&L.status[1], 1u);
+  }
   SurfaceJob const& j = L.jobs[blockIdx.y];
   switch (j.kind) {
   case JOB_FILL: fill_job(j, blockIdx.x, gridDim.x); break;
@@ -110,11 +115,16 @@ __global__ void k_mip(uint8_t const* src, uint32_t sw, uint32_t sh, uint8_t* dst
 }
 
 // Launches the jobs, JOBS_PER_LAUNCH per launch; returns the launch count.
-uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaStream_t s) {
+// With `status`, the jobs belong to a pass (see JobList); `count_pass` makes
+// the last launch count the pass as completed.
+uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaStream_t s, unsigned int* status,
+                     bool count_pass) {
   uint32_t launches = 0;
   for (uint32_t first = 0; first < n; first += JOBS_PER_LAUNCH) {
     JobList L;
     L.n = std::min<uint32_t>(JOBS_PER_LAUNCH, n - first);
+    L.status = status;
+    L.count_pass = count_pass && first + JOBS_PER_LAUNCH >= n ? 1u : 0u;
     size_t most = 0;
     for (uint32_t i = 0; i < L.n; ++i) {
       L.jobs[i] = jobs[first + i];

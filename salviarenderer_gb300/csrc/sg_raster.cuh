@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
   uint32_t* mask16 = mask4 + 64 * MASK_WORDS;
   uint32_t* ztile = mask16 + 4 * MASK_WORDS;
   __shared__ uint32_t s_item;
-  if (P.counters->overflow & (OVF_BIN | OVF_REC)) return;
+  if ((P.counters->overflow & (OVF_BIN | OVF_REC)) || pass_gated(P)) return;
   int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   uint32_t const nslots = P.ntiles * 16;
   OwnerList L{NO_CHUNK, NO_CHUNK, 0};
@@ -522,11 +522,17 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
     uint32_t const qh = min(static_cast<uint32_t>(px), T.height - min(T.height, static_cast<uint32_t>(y0)));
     uint32_t const zrow = px * S;
     if (stage_z) {
+      // the item's depth, and its pre-image for k_cover_rollback
+      uint32_t* const zb = P.zbackup ? P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words +
+                                           (static_cast<size_t>(by0) * 4 * TILE + bx0 * 4) * S
+                                     : nullptr;
       for (uint32_t i = tid; i < qh * zrow; i += COVER_THREADS) {
         uint32_t y = i / zrow, k = i % zrow;
         if (k >= qw * S) continue;
         uint32_t x = k / S, sm = k % S;
-        ztile[i] = *reinterpret_cast<uint32_t const*>(ds_addr(T, x0 + x, y0 + y, sm));
+        uint32_t const v = *reinterpret_cast<uint32_t const*>(ds_addr(T, x0 + x, y0 + y, sm));
+        ztile[i] = v;
+        if (zb) zb[static_cast<size_t>(y) * TILE * S + k] = v;
       }
     }
     for (uint32_t bstart = begin; bstart < end; bstart += STAGE_TRIS) {
@@ -689,7 +695,7 @@ __device__ inline bool af_takes(DrawParams const& D, float dxu, float dxv, float
 // SM (64 registers) where the plain instances run 3.
 template <int NA, bool LEARNED>
 __global__ void __launch_bounds__(256, LEARNED ? 4 : 3) k_shade(PassParams P) {
-  if (P.counters->overflow & OVF_FATAL) return;
+  if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
   uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
   int const q = threadIdx.x & 3;
   uint32_t const groups = gridDim.x * (blockDim.x >> 2);
@@ -886,8 +892,12 @@ __global__ void __launch_bounds__(256, LEARNED ? 4 : 3) k_shade(PassParams P) {
 // Work is handed out per warp -- 32 owners of a tile at a time, from a
 // device-wide cursor -- so tiles of very different cost spread over the SMs.
 __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
-  uint32_t const ovf = P.counters->overflow;  // final: geometry, binning and coverage are done
-  if (blockIdx.x == 0 && threadIdx.x == 0 && ovf) atomicOr(P.sticky, ovf);
+  if (pass_gated(P)) return;
+  uint32_t const ovf = P.counters->overflow;  // final: geometry, binning, coverage and shading are done
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (ovf) atomicOr(P.sticky, ovf);
+    if (P.count_pass && !(ovf & OVF_FATAL)) atomicAdd(P.sticky + 1, 1u);
+  }
   if (ovf & OVF_FATAL) return;
   int const lane = threadIdx.x & 31;
   uint32_t const groups = QUAD_OWNERS / 32;  // owner groups per tile

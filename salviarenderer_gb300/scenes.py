@@ -412,6 +412,48 @@ def stencil_ops_scene(front, back, seed=1, width=96, height=80, samples=1, ntris
     return s
 
 
+def overdraw_scene(seed=1, width=256, height=256, samples=1, ntris=60, draws=3, textured=False, learned=None,
+                   depth_func=abi.CMP_ALWAYS):
+    """Heavy overdraw: large clip-space triangles (vertices in [-3, 3]^2,
+    most of them covering most of the target), depth function ALWAYS so that
+    every covered quad of every triangle reaches the output merger, blended
+    with source alpha.  Textured draws sample a 64^2 value-noise texture with
+    16x anisotropy (with `learned` = (threshold, max probes, min probes) on
+    the learned filter).  Sized to overrun a fresh device's fragment room and
+    lookup queue in one pass."""
+    rng = np.random.default_rng(seed)
+    s = Scene("overdraw", width, height, samples)
+    s.clear_color = (0.2, 0.1, 0.3, 1.0)
+    pos = rng.uniform(-3.0, 3.0, size=(ntris * 3, 4))
+    pos[:, 2] = rng.uniform(0.05, 0.95, size=ntris * 3)
+    pos[:, 3] = 1.0
+    uv = rng.uniform(-4.0, 4.0, size=(ntris * 3, 4))
+    uv[:, 2:] = 0.0
+    col = rng.uniform(0.0, 1.0, size=(ntris * 3, 4))
+    col[:, 3] = rng.uniform(0.1, 0.4, size=ntris * 3)
+    s.buffers["vb"] = np.concatenate([pos, uv, col], axis=1).astype(np.float32)
+    if textured:
+        s.textures["tex"] = (to_rgba8(value_noise(rng, 64, octaves=4)), True)
+        s.samplers["aniso"] = ("tex", dict(min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+                                           mip_filter=abi.FILTER_ANISOTROPIC, max_anisotropy=16))
+        ps = (dict(program=abi.PS_TEX_GRAD_LEARNED, samplers=["aniso"], learned_filter="model",
+                   constants=list(learned)) if learned is not None else
+              dict(program=abi.PS_TEX_GRAD_MODULATE, samplers=["aniso"]))
+    else:
+        ps = dict(program=abi.PS_COLOR)
+    dsd = default_depth_stencil(depth_func=depth_func)
+    ident = np.identity(4, dtype=np.float32)
+    bounds = np.linspace(0, ntris, draws + 1).astype(np.int64)
+    for i in range(draws):
+        s.draws.append(dict(viewport=(0, 0, width, height, 0.0, 1.0), prim_count=int(bounds[i + 1] - bounds[i]),
+                            streams=[("vb", 48, 48 * 3 * int(bounds[i]))],
+                            inputs=GRID_INPUTS if textured else COLOR_FIRST_INPUTS, num_varyings=2,
+                            varying_modifiers=[abi.AM_LINEAR, abi.AM_LINEAR], depth_stencil=dsd,
+                            vs=dict(program=abi.VS_TRANSFORM, constants=ident), ps=ps,
+                            bs=dict(program=abi.BS_LERP_SRC_ALPHA)))
+    return s
+
+
 def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=abi.TOPOLOGY_TRIANGLE_LIST,
                   index_format=None, base_vertex=0, cull=abi.CULL_NONE, front_ccw=0,
                   depth_func=abi.CMP_LESS, depth_write=1, depth_enable=1, blend=abi.BS_REPLACE,

@@ -154,8 +154,9 @@ int main(int argc, char** argv) {
     resolved_tex->subresource(0)->read(bytes);
     std::fwrite(bytes.data(), 1, bytes.size(), o);
   }
-  uint64_t st[4] = {ps.ia_primitives, ps.cprimitives, ps.ps_invocations, is.backend_input_pixels};
-  std::fwrite(st, 8, 4, o);
+  uint64_t st[7] = {ps.ia_primitives, ps.cprimitives, ps.ps_invocations, is.backend_input_pixels,
+                    ps.ia_vertices, ps.vs_invocations, ps.cinvocations};
+  std::fwrite(st, 8, 7, o);
   std::fclose(o);
   return 0;
 }

@@ -62,7 +62,7 @@ FULL_SIZE = {
 def output_digests(out):
     """sha256 of each output array and of the per-draw counters."""
     d = {k: hashlib.sha256(np.ascontiguousarray(v).tobytes()).hexdigest() for k, v in out.items() if k != "stats"}
-    stats = np.array([[st[k] for k, _ in abi.DrawStats._fields_] for st in out["stats"]], dtype=np.uint64)
+    stats = np.array([[st[k] for k in abi.REFERENCE_STATS] for st in out["stats"]], dtype=np.uint64)
     d["stats"] = hashlib.sha256(stats.tobytes()).hexdigest()
     d["stats_total"] = stats.sum(axis=0).tolist()
     return d
@@ -91,8 +91,7 @@ def main():
             continue
         s = build()
         out = scenes.render(dev, s, stats=True)
-        stats = np.array([[st[k] for k, _ in abi.DrawStats._fields_] for st in out.pop("stats")],
-                         dtype=np.uint64)
+        stats = np.array([[st[k] for k in abi.REFERENCE_STATS] for st in out.pop("stats")], dtype=np.uint64)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), digest=scene_digest(s),
                             stats=stats, **out)
         print(name, {k: v.shape for k, v in out.items()}, stats.sum(axis=0).tolist())

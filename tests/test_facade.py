@@ -64,13 +64,14 @@ def run_facade(exe, scene, tmp):
     for k, sz in sizes:
         res[k] = np.frombuffer(raw[off:off + sz], np.uint8)
         off += sz
-    res["stats"] = struct.unpack("<4Q", raw[off:off + 32])
+    res["stats"] = struct.unpack("<7Q", raw[off:off + 56])
     return res
 
 
 def summed_stats(stats):
     return tuple(sum(st[k] for st in stats) for k in
-                 ("ia_primitives", "cprimitives", "ps_invocations", "backend_input_pixels"))
+                 ("ia_primitives", "cprimitives", "ps_invocations", "backend_input_pixels", "ia_vertices",
+                  "vs_invocations", "cinvocations"))
 
 
 def test_facade_header_compiles_and_matches_wrapper_on_oracle(oracle_lib, tmp_path):
