@@ -129,7 +129,23 @@ enum {
    * lookup of an anisotropic sampler with more than constants[2] and at most
    * constants[1] probes -- and where the filter's confidence is at least
    * constants[0]; every other lookup runs the plain sampler. */
-  SG_PS_TEX_GRAD_LEARNED = 5
+  SG_PS_TEX_GRAD_LEARNED = 5,
+  /* out.color[0] = tex2dlod(sampler0, 0) * in.attr[1]: the lookup at
+   * (attr[0].x, attr[0].y) with attr[0].w as the mip level, sampler::sample
+   * (cpp_pixel_shader.cpp:33-40). */
+  SG_PS_TEX_LOD_MODULATE = 6,
+  /* out.color[0] = tex2dproj(sampler0, 0) * in.attr[1]: attr[0] divided by
+   * its w and mapped from [-1, 1] to [0, 1], with the derivatives of that
+   * projection across the quad (cpp_pixel_shader.cpp:42-60). */
+  SG_PS_TEX_PROJ_MODULATE = 7,
+  /* out.color[0] = c = tex2d(sampler0, 0) * in.attr[1]; discard
+   * (shader_prog returns false) when c.a < constants[0] -- the alpha-test
+   * pattern.  As in the reference, a quad keeps pixel 0 when pixel 0 or
+   * pixel 2 passes and pixels 1-3 when pixel 1 or pixel 3 passes (the pass
+   * mask is built from int shifts, cpp_pixel_shader.cpp:62-74); a pixel that
+   * is not kept is neither blended nor depth-tested late, and with early-Z
+   * its depth was already written (rasterizer.cpp:1245-1421). */
+  SG_PS_TEX_ALPHA_TEST = 8
 };
 enum {
   SG_BS_REPLACE = 1,        /* color(0, s) = in.color[0] */

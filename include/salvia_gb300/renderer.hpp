@@ -675,6 +675,40 @@ public:
 private:
   sampler_ptr samp_;
 };
+// tex2dlod(Sampler, 0) * in.attr[1]: the level is attr[0].w (cpp_pixel_shader.cpp:33-40).
+class texture_lod_pixel_shader : public cpp_pixel_shader {
+public:
+  explicit texture_lod_pixel_shader(sampler_ptr const& s = nullptr) : samp_(s) { declare_sampler("Sampler", samp_); }
+  uint32_t program() const override { return SG_PS_TEX_LOD_MODULATE; }
+  SALVIA_GB300_CLONE(texture_lod_pixel_shader)
+
+private:
+  sampler_ptr samp_;
+};
+// tex2dproj(Sampler, 0) * in.attr[1] (cpp_pixel_shader.cpp:42-60).
+class texture_proj_pixel_shader : public cpp_pixel_shader {
+public:
+  explicit texture_proj_pixel_shader(sampler_ptr const& s = nullptr) : samp_(s) { declare_sampler("Sampler", samp_); }
+  uint32_t program() const override { return SG_PS_TEX_PROJ_MODULATE; }
+  SALVIA_GB300_CLONE(texture_proj_pixel_shader)
+
+private:
+  sampler_ptr samp_;
+};
+// Alpha test: tex2d(Sampler, 0) * in.attr[1], discarded below the "AlphaRef" alpha.
+class alpha_test_pixel_shader : public cpp_pixel_shader {
+public:
+  explicit alpha_test_pixel_shader(float alpha_ref = 0.5f, sampler_ptr const& s = nullptr) : ref_(alpha_ref), samp_(s) {
+    declare_constant("AlphaRef", ref_);
+    declare_sampler("Sampler", samp_);
+  }
+  uint32_t program() const override { return SG_PS_TEX_ALPHA_TEST; }
+  SALVIA_GB300_CLONE(alpha_test_pixel_shader)
+
+private:
+  float ref_;
+  sampler_ptr samp_;
+};
 // No counterpart in the reference: texture_grad_pixel_shader with the
 // anisotropic lookup on a learned filter (SG_PS_TEX_GRAD_LEARNED) where its
 // probe count lies in (MinProbes, MaxProbes] and its confidence reaches

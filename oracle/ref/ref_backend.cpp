@@ -133,6 +133,13 @@ public:
       out.color[0] = c.get_vec4() * in.attribute(1);
       return true;
     }
+    case SG_PS_TEX_LOD_MODULATE: out.color[0] = tex2dlod(*samp, 0).get_vec4() * in.attribute(1); return true;
+    case SG_PS_TEX_PROJ_MODULATE: out.color[0] = tex2dproj(*samp, 0).get_vec4() * in.attribute(1); return true;
+    case SG_PS_TEX_ALPHA_TEST: {
+      vec4 c = tex2d(*samp, 0).get_vec4() * in.attribute(1);
+      out.color[0] = c;
+      return !(c[3] < prog.constants[0]);
+    }
     default: out.color[0] = vec4(0, 0, 0, 0); return true;
     }
   }

@@ -1327,16 +1327,52 @@ bool run_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, float& lod_cac
     out = mulv(t, in.r[2]);
     return true;
   }
+  case SG_PS_TEX_LOD_MODULATE: {  // tex2dlod: sampler::sample(x, y, w) (cpp_pixel_shader.cpp:33-40)
+    vec4 t = sample_impl(*c.ps_samp, in.r[1][0], in.r[1][1], in.r[1][3], nullptr);
+    out = mulv(t, in.r[2]);
+    return true;
+  }
+  case SG_PS_TEX_PROJ_MODULATE: {  // tex2dproj (cpp_pixel_shader.cpp:42-60)
+    vec4 const& a = in.r[1];
+    vec4 nx = add(a, sub(quad[1].r[1], quad[0].r[1]));
+    vec4 ny = add(a, sub(quad[2].r[1], quad[0].r[1]));
+    auto proj = [](vec4 const& v, int k) { return (v[k] / v[3] + 1.0f) * 0.5f; };
+    float px = proj(a, 0), py = proj(a, 1);
+    vec4 t = sample_2d_grad(*c.ps_samp, px, py, proj(nx, 0) - px, proj(nx, 1) - py, proj(ny, 0) - px,
+                            proj(ny, 1) - py, 0.0f);
+    out = mulv(t, in.r[2]);
+    return true;
+  }
+  case SG_PS_TEX_ALPHA_TEST: {  // tex2d * attr[1]; discarded below constants[0] alpha
+    if (!have_lod) {
+      vec4 dx = sub(quad[1].r[1], quad[0].r[1]);
+      vec4 dy = sub(quad[2].r[1], quad[0].r[1]);
+      lod_cache = calc_lod_2d(*c.ps_samp, dx[0], dx[1], dy[0], dy[1]);
+      have_lod = true;
+    }
+    out = mulv(sample_impl(*c.ps_samp, in.r[1][0], in.r[1][1], lod_cache, nullptr), in.r[2]);
+    return !(out[3] < s.constants[0]);
+  }
   default: out = mk(0, 0, 0, 0); return true;
   }
 }
 
-uint64_t execute_ps(draw_ctx const& c, vso const* quad, vec4* out) {  // cpp_pixel_shader::execute
-  uint64_t mask = 0;
+// cpp_pixel_shader::execute (cpp_pixel_shader.cpp:62-74).  The reference
+// builds the quad's pass mask as `(passed ? 0xFFFF : 0) << (i * 16)` with an
+// int left operand: the shift of pixel 1 gives the negative int 0xFFFF0000,
+// which sign-extends into the 64-bit mask and sets pixels 1-3, and the
+// shifts of pixels 2 and 3 by 32 and 48 bits act as shifts by 0 and 16 (the
+// 32-bit shift count wraps).  So pixel 0 is kept when pixel 0 or pixel 2
+// passes, and pixels 1-3 are all kept when pixel 1 or pixel 3 passes; with
+// no discard every pixel is kept.
+uint64_t execute_ps(draw_ctx const& c, vso const* quad, vec4* out) {
+  bool pass[4];
   float lod = 0;
   bool have = false;
-  for (int i = 0; i < 4; ++i)
-    mask |= static_cast<uint64_t>(run_ps(c, quad, i, out[i], lod, have) ? 0xFFFF : 0) << (i * 16);
+  for (int i = 0; i < 4; ++i) pass[i] = run_ps(c, quad, i, out[i], lod, have);
+  uint64_t mask = 0;
+  if (pass[0] || pass[2]) mask |= 0xFFFFull;
+  if (pass[1] || pass[3]) mask |= 0xFFFFFFFFFFFF0000ull;
   return mask;
 }
 

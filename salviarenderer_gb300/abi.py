@@ -39,6 +39,9 @@ SEMANTIC_POSITION, SEMANTIC_TEXCOORD, SEMANTIC_COLOR, SEMANTIC_NORMAL = 0, 1, 2,
 
 VS_TRANSFORM, VS_MORPH_DISPLACE = 1, 2
 PS_COLOR, PS_CONSTANT, PS_TEX_MODULATE, PS_TEX_GRAD_MODULATE, PS_TEX_GRAD_LEARNED = 1, 2, 3, 4, 5
+PS_TEX_LOD_MODULATE, PS_TEX_PROJ_MODULATE, PS_TEX_ALPHA_TEST = 6, 7, 8
+TEXTURED_PS = (PS_TEX_MODULATE, PS_TEX_GRAD_MODULATE, PS_TEX_GRAD_LEARNED, PS_TEX_LOD_MODULATE, PS_TEX_PROJ_MODULATE,
+               PS_TEX_ALPHA_TEST)
 BS_REPLACE, BS_LERP_SRC_ALPHA, BS_ADD = 1, 2, 3
 CMD_DRAW, CMD_CLEAR_COLOR, CMD_CLEAR_DEPTH_STENCIL, CMD_RESOLVE = 1, 2, 3, 4
 

@@ -547,9 +547,10 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   if (int32_t r = build_sampler(d, desc->vs.samplers[0], p.vs_samp, &info.tex[0])) return r;
   if (int32_t r = build_sampler(d, desc->ps.samplers[0], p.ps_samp, &info.tex[1])) return r;
   if (p.vs_prog == SG_VS_MORPH_DISPLACE && !desc->vs.samplers[0]) return SG_INVALID_PARAMETER;
-  if ((p.ps_prog == SG_PS_TEX_MODULATE || p.ps_prog == SG_PS_TEX_GRAD_MODULATE ||
-       p.ps_prog == SG_PS_TEX_GRAD_LEARNED) && !desc->ps.samplers[0])
+  if (p.vs_prog < SG_VS_TRANSFORM || p.vs_prog > SG_VS_MORPH_DISPLACE || p.ps_prog < SG_PS_COLOR ||
+      p.ps_prog > SG_PS_TEX_ALPHA_TEST || p.bs_prog < SG_BS_REPLACE || p.bs_prog > SG_BS_ADD)
     return SG_INVALID_PARAMETER;
+  if (p.ps_prog != SG_PS_COLOR && p.ps_prog != SG_PS_CONSTANT && !desc->ps.samplers[0]) return SG_INVALID_PARAMETER;
   if (p.ps_prog == SG_PS_TEX_GRAD_LEARNED) {
     if (!d->af_models.count(desc->ps.learned_filter)) return SG_INVALID_PARAMETER;
     info.af_model = desc->ps.learned_filter;

@@ -650,10 +650,11 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
 #endif  // SG_RASTER_COVER_MERGE
 
 // cpp_pixel_shader programs for one pixel `q` of a quad shaded by four lanes
-// (lanes 4k..4k+3 of the warp); tex2d's LOD uses the quad differences
-// (cpp_pixel_shader.cpp:13-31).
+// (lanes 4k..4k+3 of the warp); ddx / ddy are the quad differences and
+// tex2d's LOD uses them (cpp_pixel_shader.cpp:13-31).  `keep` is the
+// program's return value: false discards the pixel.
 template <int NA>
-__device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q) {
+__device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q, bool& keep) {
   v4 a0 = NA > 0 ? attr[0] : mk4(0, 0, 0, 0);
   v4 a1 = NA > 1 ? attr[1 < NA ? 1 : 0] : mk4(0, 0, 0, 0);
   int base = (threadIdx.x & 31) & ~3;
@@ -661,6 +662,7 @@ __device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q) {
   float u0 = __shfl_sync(mask, a0.x, base), v0 = __shfl_sync(mask, a0.y, base);
   float u1 = __shfl_sync(mask, a0.x, base + 1), v1 = __shfl_sync(mask, a0.y, base + 1);
   float u2 = __shfl_sync(mask, a0.x, base + 2), v2 = __shfl_sync(mask, a0.y, base + 2);
+  keep = true;
   switch (D.ps_prog) {
   case SG_PS_COLOR: return a0;
   case SG_PS_CONSTANT: return mk4(D.ps_k[0], D.ps_k[1], D.ps_k[2], D.ps_k[3]);
@@ -671,6 +673,25 @@ __device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q) {
   case SG_PS_TEX_GRAD_MODULATE:
   case SG_PS_TEX_GRAD_LEARNED:  // the lookups the learned filter does not take
     return mulv(sample_2d_grad(D.ps_samp, a0.x, a0.y, u1 - u0, v1 - v0, u2 - u0, v2 - v0, 0.0f), a1);
+  case SG_PS_TEX_LOD_MODULATE:  // tex2dlod(s, 0) = s.sample(x, y, w) (cpp_pixel_shader.cpp:33-40)
+    return mulv(sample_impl(D.ps_samp, a0.x, a0.y, a0.w, nullptr), a1);
+  case SG_PS_TEX_PROJ_MODULATE: {  // tex2dproj(s, 0) (cpp_pixel_shader.cpp:42-60)
+    float const w0 = __shfl_sync(mask, a0.w, base), w1 = __shfl_sync(mask, a0.w, base + 1),
+                w2 = __shfl_sync(mask, a0.w, base + 2);
+    // this pixel's attribute, and it stepped by ddx and by ddy
+    float const nxx = a0.x + (u1 - u0), nxy = a0.y + (v1 - v0), nxw = a0.w + (w1 - w0);
+    float const nyx = a0.x + (u2 - u0), nyy = a0.y + (v2 - v0), nyw = a0.w + (w2 - w0);
+    float const px = (a0.x / a0.w + 1.0f) * 0.5f, py = (a0.y / a0.w + 1.0f) * 0.5f;
+    float const qxx = (nxx / nxw + 1.0f) * 0.5f, qxy = (nxy / nxw + 1.0f) * 0.5f;
+    float const qyx = (nyx / nyw + 1.0f) * 0.5f, qyy = (nyy / nyw + 1.0f) * 0.5f;
+    return mulv(sample_2d_grad(D.ps_samp, px, py, qxx - px, qxy - py, qyx - px, qyy - py, 0.0f), a1);
+  }
+  case SG_PS_TEX_ALPHA_TEST: {  // tex2d * attr[1], discarded below constants[0] alpha
+    float lod = calc_lod_2d(D.ps_samp, u1 - u0, v1 - v0, u2 - u0, v2 - v0);
+    v4 const c = mulv(sample_impl(D.ps_samp, a0.x, a0.y, lod, nullptr), a1);
+    keep = !(c.w < D.ps_k[0]);
+    return c;
+  }
   default: return mk4(0, 0, 0, 0);
   }
 }
@@ -829,11 +850,20 @@ __global__ void __launch_bounds__(256, LEARNED ? 4 : 3) k_shade(PassParams P) {
         af_r1 = make_float4(u2 - u0, v2 - v0, __uint_as_float(f * 4 + q), __uint_as_float(draw));
         v4 const m = NA > 1 ? attr[NA > 1 ? 1 : 0] : mk4(0, 0, 0, 0);
         af_r2 = make_float4(m.x, m.y, m.z, m.w);
+        if (q == 0) P.frag_ps[f] = 0xF;  // the learned filter's lookups never discard
       } else {
-        v4 out = run_ps<NA>(D, attr, q);  // all four lanes of a quad take the same path
+        bool keep = true;
+        v4 out = run_ps<NA>(D, attr, q, keep);  // all four lanes of a quad take the same path
         P.frag_color[static_cast<size_t>(f) * 4 + q] = make_float4(out.x, out.y, out.z, out.w);
+        // the quad's pass mask as cpp_pixel_shader::execute builds it
+        // (cpp_pixel_shader.cpp:62-74): from int shifts of 0xFFFF by 16 i, so
+        // pixel 0 is kept when pixel 0 or 2 passes and pixels 1-3 when pixel
+        // 1 or 3 passes (a negative int sign-extends, a 32-bit shift count wraps)
+        int const qb = (threadIdx.x & 31) & ~3;
+        uint32_t const passed = (__ballot_sync(0xFu << qb, keep) >> qb) & 0xFu;
+        uint32_t const kept = ((passed & 5u) ? 1u : 0u) | ((passed & 10u) ? 14u : 0u);
+        if (q == 0) P.frag_ps[f] = static_cast<uint8_t>(kept);
       }
-      if (q == 0) P.frag_ps[f] = 0xF;  // the stock programs never discard
     }
     if constexpr (LEARNED) {
       // queue the lookups, one atomic per warp and queue; lookups past the

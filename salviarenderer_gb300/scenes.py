@@ -459,7 +459,7 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
                   depth_func=abi.CMP_LESS, depth_write=1, depth_enable=1, blend=abi.BS_REPLACE,
                   ps=abi.PS_COLOR, sampler=None, modifiers=(abi.AM_LINEAR, abi.AM_LINEAR),
                   color_fmt=abi.FMT_RGBA8, ds_fmt=abi.FMT_RG32F, tex_size=64, uv_scale=3.0,
-                  eye_dist=(2.2, 3.2), draws=1, clear_depth=1.0):
+                  eye_dist=(2.2, 3.2), draws=1, clear_depth=1.0, uv_w=None, ps_constants=None, stencil=None):
     """A small scene that exercises one combination of pipeline state.
 
     Vertices carry position, a (u, v) pair and an RGBA colour.  Strips and
@@ -473,6 +473,8 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
     pos[:, 3] = 1.0
     uv = rng.uniform(-uv_scale, uv_scale, size=(npool, 4))
     uv[:, 2:] = 0.0
+    if uv_w is not None:  # a fourth texture coordinate: the mip level of tex2dlod, the w of tex2dproj
+        uv[:, 3] = rng.uniform(*uv_w, size=npool)
     col = rng.uniform(0.0, 1.0, size=(npool, 4))
     col[:, 3] = rng.uniform(0.25, 1.0, size=npool)
     pad = np.zeros((base_vertex, 12), dtype=np.float32)
@@ -490,11 +492,15 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
     if index_format is not None:
         idx = rng.integers(0, npool, size=nv)
         s.buffers["ib"] = idx.astype(np.uint16 if index_format == abi.INDEX_U16 else np.uint32)
-    if ps in (abi.PS_TEX_MODULATE, abi.PS_TEX_GRAD_MODULATE):
+    if ps in abi.TEXTURED_PS:
         s.textures["tex"] = (to_rgba8(value_noise(rng, tex_size, octaves=4)), True)
         s.samplers["s0"] = ("tex", dict(sampler or {}))
     dsd = default_depth_stencil(depth_func=depth_func, depth_enable=depth_enable,
                                 depth_write=depth_write)
+    if stencil is not None:  # (func, pass_op, ref) on both faces: late depth test
+        dsd.stencil_enable = 1
+        for face in (dsd.front, dsd.back):
+            face.func, face.pass_op = stencil[0], stencil[1]
     bounds = np.linspace(0, ntris, draws + 1).astype(np.int64)
     for i in range(draws):
         count = int(bounds[i + 1] - bounds[i])
@@ -506,9 +512,10 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
                   inputs=COLOR_FIRST_INPUTS if ps in (abi.PS_COLOR, abi.PS_CONSTANT) else GRID_INPUTS,
                   num_varyings=len(modifiers), varying_modifiers=list(modifiers),
                   cull_mode=cull, front_ccw=front_ccw, depth_stencil=dsd,
-                  base_vertex=base_vertex,
+                  base_vertex=base_vertex, stencil_ref=stencil[2] if stencil is not None else 0,
                   vs=dict(program=abi.VS_TRANSFORM, constants=mvp),
-                  ps=dict(program=ps, samplers=["s0"] if "s0" in s.samplers else []),
+                  ps=dict(program=ps, samplers=["s0"] if "s0" in s.samplers else [],
+                          constants=list(ps_constants or [])),
                   bs=dict(program=blend))
         if index_format is not None:
             dd.update(index_buffer="ib", index_format=index_format,

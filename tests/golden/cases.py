@@ -67,6 +67,23 @@ CASES = {
                                      blend=abi.BS_LERP_SRC_ALPHA, uv_scale=6.0),
     "tex_grad_af8_4x": lambda: F(seed=20, ps=abi.PS_TEX_GRAD_MODULATE, sampler=AF8, samples=4),
     "tex_grad_trilinear": lambda: F(seed=21, ps=abi.PS_TEX_GRAD_MODULATE, sampler=TRILINEAR),
+    # pixel-shader paths (cpp_pixel_shader.cpp:33-74): tex2dlod (the level
+    # from attribute w), tex2dproj (w-divided coordinates, projected
+    # derivatives), discard (alpha test) with early depth -- discarded pixels
+    # keep the depth they wrote -- and with late depth (stencil on)
+    "ps_tex2dlod_trilinear": lambda: F(seed=22, ps=abi.PS_TEX_LOD_MODULATE, sampler=TRILINEAR, uv_w=(0.0, 5.0)),
+    "ps_tex2dlod_point_4x": lambda: F(seed=23, ps=abi.PS_TEX_LOD_MODULATE, sampler=POINT, uv_w=(-1.0, 6.0),
+                                      samples=4),
+    "ps_tex2dproj_af16": lambda: F(seed=24, ps=abi.PS_TEX_PROJ_MODULATE, sampler=AF16, uv_w=(0.5, 2.0)),
+    "ps_tex2dproj_trilinear_4x": lambda: F(seed=25, ps=abi.PS_TEX_PROJ_MODULATE, sampler=TRILINEAR,
+                                           uv_w=(0.6, 1.8), samples=4, blend=abi.BS_LERP_SRC_ALPHA),
+    "ps_discard_early_z": lambda: F(seed=26, ps=abi.PS_TEX_ALPHA_TEST, sampler=TRILINEAR, ps_constants=[0.45],
+                                    ntris=200),
+    "ps_discard_early_z_4x_blend": lambda: F(seed=27, ps=abi.PS_TEX_ALPHA_TEST, sampler=TRILINEAR,
+                                             ps_constants=[0.5], samples=4, blend=abi.BS_LERP_SRC_ALPHA),
+    "ps_discard_late_z_stencil": lambda: F(seed=28, ps=abi.PS_TEX_ALPHA_TEST, sampler=TRILINEAR,
+                                           ps_constants=[0.45], ntris=200,
+                                           stencil=(abi.CMP_ALWAYS, abi.SOP_INCR_WRAP, 0)),
     # C2 pattern (textured grid, trilinear + 16x AF, src-alpha blend)
     "c2_160x96_4x": lambda: scenes.c2_scene(width=160, height=96, grid=33, tex_size=128, ndraws=4),
     "c2_128x72_1x": lambda: scenes.c2_scene(width=128, height=72, grid=25, tex_size=64, samples=1,
