@@ -47,6 +47,9 @@ enum {
 #define SG_MAX_RT_SIZE 8192   /* MAX_RENDER_TARGET_WIDTH/HEIGHT */
 #define SG_MAX_SHADER_CONSTANTS 48
 #define SG_MAX_SHADER_SAMPLERS 2
+/* colour targets of one draw: set_render_targets takes fewer than
+ * MAX_RENDER_TARGETS = 8 (renderer_impl.cpp:159-238) */
+#define SG_MAX_COLOR_TARGETS 7
 
 /* ---- enumerations (reference numeric values) ----------------------------- */
 /* primitive_topology (constants.h:44-52) */
@@ -145,12 +148,16 @@ enum {
    * mask is built from int shifts, cpp_pixel_shader.cpp:62-74); a pixel that
    * is not kept is neither blended nor depth-tested late, and with early-Z
    * its depth was already written (rasterizer.cpp:1245-1421). */
-  SG_PS_TEX_ALPHA_TEST = 8
+  SG_PS_TEX_ALPHA_TEST = 8,
+  /* out.color[i] = in.attr[i] for every varying i (one colour per bound
+   * target); colours a program does not write are zero. */
+  SG_PS_COLOR_MRT = 9
 };
 enum {
   SG_BS_REPLACE = 1,        /* color(0, s) = in.color[0] */
   SG_BS_LERP_SRC_ALPHA = 2, /* color(0, s) = lerp(dst, src, src.a) (TextureAndBlending.cpp:168-176) */
-  SG_BS_ADD = 3             /* color(0, s) = dst + src */
+  SG_BS_ADD = 3,            /* color(0, s) = dst + src */
+  SG_BS_REPLACE_ALL = 4     /* color(i, s) = in.color[i] for every bound colour target i */
 };
 
 /* ---- descriptors ------------------------------------------------------------ */
@@ -232,6 +239,11 @@ typedef struct sg_draw_desc {
   sg_depth_stencil_desc depth_stencil;
   int32_t stencil_ref;
   sg_shader vs, ps, bs;
+  /* colour targets 1..6 after color_target (0 = none, from the first 0 on):
+   * the draw renders into every one; the render area is the smallest of
+   * their sizes, as in renderer_impl::set_render_targets, and all have the
+   * sample count of color_target */
+  uint32_t more_color_targets[SG_MAX_COLOR_TARGETS - 1];
 } sg_draw_desc;
 
 /* Pipeline counters of one draw (async_object.h:90-175). */

@@ -24,6 +24,7 @@
 // Header-only, C++17.  Link with libsalvia_gb300.so.
 #pragma once
 
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -640,6 +641,12 @@ private:
   uint32_t nattr_, mods_;
 };
 // out.color[0] = in.attr[0]
+// out.color[i] = in.attr[i]: one colour per bound target (SG_PS_COLOR_MRT).
+class color_mrt_pixel_shader : public cpp_pixel_shader {
+public:
+  uint32_t program() const override { return SG_PS_COLOR_MRT; }
+  SALVIA_GB300_CLONE(color_mrt_pixel_shader)
+};
 class color_pixel_shader : public cpp_pixel_shader {
 public:
   uint32_t program() const override { return SG_PS_COLOR; }
@@ -741,6 +748,11 @@ class src_alpha_blend_shader : public cpp_blend_shader {  // lerp(dst, src, src.
 public:
   uint32_t program() const override { return SG_BS_LERP_SRC_ALPHA; }
   SALVIA_GB300_CLONE(src_alpha_blend_shader)
+};
+class replace_all_blend_shader : public cpp_blend_shader {  // color(i, s) = in.color[i], every target
+public:
+  uint32_t program() const override { return SG_BS_REPLACE_ALL; }
+  SALVIA_GB300_CLONE(replace_all_blend_shader)
 };
 class additive_blend_shader : public cpp_blend_shader {  // dst + src
 public:
@@ -977,9 +989,25 @@ public:
     stencil_ref_ = stencil_ref;
     return result::ok;
   }
+  // renderer_impl::set_render_targets (renderer_impl.cpp:159-238): fewer
+  // than MAX_RENDER_TARGETS colour targets of one sample count, level-0
+  // surfaces here; the depth-stencil target covers the smallest of them.
   result set_render_targets(size_t color_count, surface_ptr const* colors, surface_ptr const& ds) {
-    if (color_count > 1) return result::failed;  // one colour target, as the blend programs write target 0
-    color_ = color_count ? colors[0] : nullptr;
+    colors_.clear();
+    ds_.reset();
+    if (color_count > SG_MAX_COLOR_TARGETS) return result::failed;
+    if ((color_count == 0 || colors == nullptr) && !ds) return result::failed;
+    size_t samples = 0, w = static_cast<size_t>(-1), h = static_cast<size_t>(-1);
+    for (size_t i = 0; i < color_count && colors; ++i) {
+      if (!colors[i] || colors[i]->level() != 0) return result::failed;
+      if (samples == 0) samples = colors[i]->sample_count();
+      if (colors[i]->sample_count() != samples) return result::failed;
+      w = std::min(w, colors[i]->width());
+      h = std::min(h, colors[i]->height());
+    }
+    if (ds && color_count && (ds->sample_count() != samples || ds->width() < w || ds->height() < h))
+      return result::failed;
+    if (colors) colors_.assign(colors, colors + color_count);
     ds_ = ds;
     return result::ok;
   }
@@ -1095,7 +1123,8 @@ public:
   result build_desc(bool indexed, size_t startpos, size_t primcnt, int basevert, sg_draw_desc& d) const {
     std::memset(&d, 0, sizeof(d));
     if (!vs_ || !ps_ || !bs_ || !layout_) return result::failed;
-    d.color_target = color_ ? color_->get_texture()->handle() : 0;
+    d.color_target = colors_.empty() ? 0 : colors_[0]->get_texture()->handle();
+    for (size_t i = 1; i < colors_.size(); ++i) d.more_color_targets[i - 1] = colors_[i]->get_texture()->handle();
     d.ds_target = ds_ ? ds_->get_texture()->handle() : 0;
     d.viewport = sg_viewport{vp_.x, vp_.y, vp_.w, vp_.h, vp_.minz, vp_.maxz};
     d.topology = topo_;
@@ -1169,7 +1198,8 @@ private:
   raster_state_ptr rs_;
   depth_stencil_state_ptr dss_;
   int32_t stencil_ref_ = 0;
-  surface_ptr color_, ds_;
+  std::vector<surface_ptr> colors_;
+  surface_ptr ds_;
   viewport vp_;
   std::vector<async_object_ptr> queries_;
   buffer_ptr mapped_buf_;

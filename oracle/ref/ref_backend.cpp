@@ -113,9 +113,13 @@ public:
 
   ref_ps(sg_shader const& p, sampler_ptr const& s) : prog(p), samp(s) {}
 
+  uint32_t nattr = 0;
   bool shader_prog(vs_output const& in, ps_output& out) override {
     switch (prog.program) {
     case SG_PS_COLOR: out.color[0] = in.attribute(0); return true;
+    case SG_PS_COLOR_MRT:
+      for (uint32_t i = 0; i < SG_MAX_COLOR_TARGETS; ++i) out.color[i] = i < nattr ? in.attribute(i) : vec4(0, 0, 0, 0);
+      return true;
     case SG_PS_CONSTANT:
       out.color[0] = vec4(prog.constants[0], prog.constants[1], prog.constants[2], prog.constants[3]);
       return true;
@@ -149,9 +153,13 @@ public:
 class ref_bs : public cpp_blend_shader {
 public:
   uint32_t program;
+  uint32_t ncolor = 1;
   explicit ref_bs(uint32_t p) : program(p) {}
   bool shader_prog(size_t sample, pixel_accessor& inout, ps_output const& in) override {
     switch (program) {
+    case SG_BS_REPLACE_ALL:
+      for (uint32_t i = 0; i < ncolor; ++i) inout.color(i, sample, color_rgba32f(in.color[i]));
+      break;
     case SG_BS_LERP_SRC_ALPHA: {
       color_rgba32f dst = inout.color(0, sample);
       color_rgba32f src(in.color[0]);
@@ -350,10 +358,16 @@ int32_t sg_draw(sg_device* d, const sg_draw_desc* desc, sg_draw_stats* stats) {
   dsd.back_face.stencil_func = static_cast<compare_function>(s.back.func);
   r->set_depth_stencil_state(std::make_shared<depth_stencil_state>(dsd), desc->stencil_ref);
 
-  surface_ptr color = desc->color_target ? d->textures[desc->color_target]->subresource(0)
-                                         : surface_ptr();
+  std::vector<surface_ptr> colors;
+  if (desc->color_target) {
+    colors.push_back(d->textures[desc->color_target]->subresource(0));
+    for (uint32_t i = 0; i + 1 < SG_MAX_COLOR_TARGETS && desc->more_color_targets[i]; ++i)
+      colors.push_back(d->textures[desc->more_color_targets[i]]->subresource(0));
+  }
+  ps->nattr = desc->num_varyings;
+  bs->ncolor = static_cast<uint32_t>(std::max<size_t>(1, colors.size()));
   surface_ptr ds = desc->ds_target ? d->textures[desc->ds_target]->subresource(0) : surface_ptr();
-  if (r->set_render_targets(color ? 1 : 0, color ? &color : nullptr, ds) != result::ok)
+  if (r->set_render_targets(colors.size(), colors.empty() ? nullptr : colors.data(), ds) != result::ok)
     return SG_FAILED;
   viewport vp{desc->viewport.x, desc->viewport.y, desc->viewport.w,
               desc->viewport.h, desc->viewport.minz, desc->viewport.maxz};

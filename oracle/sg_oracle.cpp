@@ -791,6 +791,8 @@ struct draw_ctx {
   device_state* dev;
   sg_draw_desc const* d;
   surface* color = nullptr;
+  surface* more[SG_MAX_COLOR_TARGETS - 1] = {};  // colour targets 1..
+  uint32_t nmore = 0;
   surface* ds = nullptr;
   uint32_t nattr = 0;
   uint32_t mods[SG_MAX_VARYINGS];
@@ -1216,9 +1218,14 @@ struct rasterizer_state {
 };
 
 // cpp_blend_shader programs (shader.h:209-215)
-void blend(draw_ctx const& c, size_t x, size_t y, size_t s, vec4 const& src) {
+// `more`: the pixel's colours 1.. (SG_MAX_COLOR_TARGETS - 1 of them)
+void blend(draw_ctx const& c, size_t x, size_t y, size_t s, vec4 const& src, vec4 const* more) {
   if (!c.color) return;
   switch (c.d->bs.program) {
+  case SG_BS_REPLACE_ALL:  // color(i, s) = in.color[i] for every bound target
+    c.color->set(x, y, s, src);
+    for (uint32_t i = 0; i < c.nmore; ++i) c.more[i]->set(x, y, s, more[i]);
+    break;
   case SG_BS_LERP_SRC_ALPHA: {
     vec4 dst = c.color->get(x, y, s);
     vec4 r;
@@ -1233,10 +1240,10 @@ void blend(draw_ctx const& c, size_t x, size_t y, size_t s, vec4 const& src) {
 
 // framebuffer::render_sample (framebuffer.cpp:445-479)
 void render_sample(rasterizer_state& rs, size_t x, size_t y, size_t s, vec4 const& src,
-                   float depth, bool front) {
+                   float depth, bool front, vec4 const* more) {
   draw_ctx const& c = *rs.c;
   if (c.early_z || !c.ds) {  // EXTENSION: without a depth-stencil target every sample passes
-    blend(c, x, y, s, src);
+    blend(c, x, y, s, src, more);
     return;
   }
   sg_depth_stencil_desc const& d = c.d->depth_stencil;
@@ -1249,7 +1256,7 @@ void render_sample(rasterizer_state& rs, size_t x, size_t y, size_t s, vec4 cons
   bool spass = rs.f.stencil ? cmpu(face.func, ref, old_stencil) : true;
   if (dpass && spass) {
     uint32_t ns = rs.f.stencil ? sop(face.pass_op, ref, old_stencil) : 0;
-    blend(c, x, y, s, src);
+    blend(c, x, y, s, src, more);
     ds_write(c, rs.f, x, y, s, depth, ns, d.stencil_write_mask & 0xFFu);
   }
 }
@@ -1284,7 +1291,8 @@ uint64_t early_z_px(rasterizer_state& rs, size_t x, size_t y, uint32_t px_mask, 
 
 // framebuffer::render_sample_quad (framebuffer.cpp:481-520)
 void render_sample_quad(rasterizer_state& rs, size_t x, size_t y, uint64_t mask, vec4 const* col,
-                        float const* depth, bool front, float const* aa) {
+                        vec4 const (*more)[SG_MAX_COLOR_TARGETS - 1], float const* depth, bool front,
+                        float const* aa) {
   draw_ctx const& c = *rs.c;
   for (int i = 0; i < 4; ++i) {
     size_t px = x + (i & 1), py = y + ((i & 2) >> 1);
@@ -1292,21 +1300,27 @@ void render_sample_quad(rasterizer_state& rs, size_t x, size_t y, uint64_t mask,
     mask >>= 16;
     if (m == 0) continue;
     if (c.samples == 1) {
-      render_sample(rs, px, py, 0, col[i], depth[i], front);
+      render_sample(rs, px, py, 0, col[i], depth[i], front, more[i]);
     } else {
       for (uint32_t s = 0; s < c.samples; ++s)
-        if (m & (1u << s)) render_sample(rs, px, py, s, col[i], depth[i] + aa[s], front);
+        if (m & (1u << s)) render_sample(rs, px, py, s, col[i], depth[i] + aa[s], front, more[i]);
     }
   }
 }
 
 // cpp_pixel_shader programs; tex2d's LOD is computed once per quad from
 // the quad's attribute differences (cpp_pixel_shader.cpp:13-31).
-bool run_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, float& lod_cache, bool& have_lod) {
+// `more` receives out.color[1..] (zero unless the program writes them).
+bool run_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, vec4* more, float& lod_cache, bool& have_lod) {
   sg_shader const& s = c.d->ps;
   vso const& in = quad[i];
+  for (uint32_t k = 0; k + 1 < SG_MAX_COLOR_TARGETS; ++k) more[k] = mk(0, 0, 0, 0);
   switch (s.program) {
   case SG_PS_COLOR: out = in.r[1]; return true;
+  case SG_PS_COLOR_MRT:  // out.color[k] = in.attr[k]
+    out = in.r[1];
+    for (uint32_t k = 1; k < c.nattr && k < SG_MAX_COLOR_TARGETS; ++k) more[k - 1] = in.r[1 + k];
+    return true;
   case SG_PS_CONSTANT: out = mk(s.constants[0], s.constants[1], s.constants[2], s.constants[3]); return true;
   case SG_PS_TEX_MODULATE: {
     if (!have_lod) {
@@ -1365,11 +1379,11 @@ bool run_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, float& lod_cac
 // 32-bit shift count wraps).  So pixel 0 is kept when pixel 0 or pixel 2
 // passes, and pixels 1-3 are all kept when pixel 1 or pixel 3 passes; with
 // no discard every pixel is kept.
-uint64_t execute_ps(draw_ctx const& c, vso const* quad, vec4* out) {
+uint64_t execute_ps(draw_ctx const& c, vso const* quad, vec4* out, vec4 (*more)[SG_MAX_COLOR_TARGETS - 1]) {
   bool pass[4];
   float lod = 0;
   bool have = false;
-  for (int i = 0; i < 4; ++i) pass[i] = run_ps(c, quad, i, out[i], lod, have);
+  for (int i = 0; i < 4; ++i) pass[i] = run_ps(c, quad, i, out[i], more[i], lod, have);
   uint64_t mask = 0;
   if (pass[0] || pass[2]) mask |= 0xFFFFull;
   if (pass[1] || pass[3]) mask |= 0xFFFFFFFFFFFF0000ull;
@@ -1479,10 +1493,11 @@ void draw_quad(rasterizer_state& rs, tri_info const& ti, uint32_t left, uint32_t
   }
   rs.st->ps_invocations += 4;
   vec4 col[4];
-  tested &= execute_ps(c, px, col);
+  vec4 colm[4][SG_MAX_COLOR_TARGETS - 1];
+  tested &= execute_ps(c, px, col, colm);
   if (full && tested == 0) return;  // draw_full_quad checks the PS-masked value
   rs.st->backend_input_pixels += 4;
-  render_sample_quad(rs, left, top, tested, col, depth, ti.front, aa);
+  render_sample_quad(rs, left, top, tested, col, colm, depth, ti.front, aa);
 }
 
 // rasterizer::draw_partial_tile (rasterizer.cpp:298-439), SSE path
@@ -1630,6 +1645,11 @@ int32_t do_draw(device_state* dev, sg_draw_desc const* d, sg_draw_stats* stats_o
     auto it = dev->textures.find(d->color_target);
     if (it == dev->textures.end()) return SG_INVALID_PARAMETER;
     c.color = it->second->levels[0].get();
+    for (uint32_t i = 0; i + 1 < SG_MAX_COLOR_TARGETS && d->more_color_targets[i]; ++i) {
+      auto mt = dev->textures.find(d->more_color_targets[i]);
+      if (mt == dev->textures.end()) return SG_INVALID_PARAMETER;
+      c.more[c.nmore++] = mt->second->levels[0].get();
+    }
   }
   if (d->ds_target) {
     auto it = dev->textures.find(d->ds_target);
@@ -1641,7 +1661,12 @@ int32_t do_draw(device_state* dev, sg_draw_desc const* d, sg_draw_stats* stats_o
   c.target_w = c.color ? static_cast<float>(c.color->w) : static_cast<float>(c.ds->w);
   c.target_h = c.color ? static_cast<float>(c.color->h) : static_cast<float>(c.ds->h);
   c.samples = c.color ? c.color->samples : c.ds->samples;
-  if (c.ds && c.color && (c.ds->samples != c.samples || c.ds->w < c.color->w || c.ds->h < c.color->h))
+  for (uint32_t i = 0; i < c.nmore; ++i) {  // the smallest colour target; one sample count
+    if (c.more[i]->samples != c.samples) return SG_FAILED;
+    c.target_w = std::min(c.target_w, static_cast<float>(c.more[i]->w));
+    c.target_h = std::min(c.target_h, static_cast<float>(c.more[i]->h));
+  }
+  if (c.ds && c.color && (c.ds->samples != c.samples || c.ds->w < c.target_w || c.ds->h < c.target_h))
     return SG_FAILED;
   if (c.samples != 1 && c.samples != 2 && c.samples != 4) return SG_INVALID_PARAMETER;
   if (d->vs.samplers[0]) c.vs_samp = &dev->samplers.at(d->vs.samplers[0]);

@@ -39,10 +39,11 @@ SEMANTIC_POSITION, SEMANTIC_TEXCOORD, SEMANTIC_COLOR, SEMANTIC_NORMAL = 0, 1, 2,
 
 VS_TRANSFORM, VS_MORPH_DISPLACE = 1, 2
 PS_COLOR, PS_CONSTANT, PS_TEX_MODULATE, PS_TEX_GRAD_MODULATE, PS_TEX_GRAD_LEARNED = 1, 2, 3, 4, 5
-PS_TEX_LOD_MODULATE, PS_TEX_PROJ_MODULATE, PS_TEX_ALPHA_TEST = 6, 7, 8
+PS_TEX_LOD_MODULATE, PS_TEX_PROJ_MODULATE, PS_TEX_ALPHA_TEST, PS_COLOR_MRT = 6, 7, 8, 9
 TEXTURED_PS = (PS_TEX_MODULATE, PS_TEX_GRAD_MODULATE, PS_TEX_GRAD_LEARNED, PS_TEX_LOD_MODULATE, PS_TEX_PROJ_MODULATE,
                PS_TEX_ALPHA_TEST)
-BS_REPLACE, BS_LERP_SRC_ALPHA, BS_ADD = 1, 2, 3
+BS_REPLACE, BS_LERP_SRC_ALPHA, BS_ADD, BS_REPLACE_ALL = 1, 2, 3, 4
+MAX_COLOR_TARGETS = 7
 CMD_DRAW, CMD_CLEAR_COLOR, CMD_CLEAR_DEPTH_STENCIL, CMD_RESOLVE = 1, 2, 3, 4
 
 
@@ -101,7 +102,8 @@ class DrawDesc(C.Structure):
                 ("num_varyings", C.c_uint32),
                 ("varying_modifiers", C.c_uint32 * SG_MAX_VARYINGS),
                 ("raster", RasterDesc), ("depth_stencil", DepthStencilDesc),
-                ("stencil_ref", C.c_int32), ("vs", Shader), ("ps", Shader), ("bs", Shader)]
+                ("stencil_ref", C.c_int32), ("vs", Shader), ("ps", Shader), ("bs", Shader),
+                ("more_color_targets", C.c_uint32 * 6)]
 
 
 class ProfileData(C.Structure):

@@ -149,14 +149,15 @@ uint8_t* static_scratch_address(int ordinal) {
 // every recorded graph owns its own.
 struct Scratch {
   Arena params, slot_rec, recs, bin_counts, scan_sums, bin_entries, tile_begin, frag_rec, frag_pos, frag_mask,
-      frag_color, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, zbackup, af_net, af_plain,
-      af_fallback, tile_order, frag_list;
+      frag_color, frag_color_more, frag_ps, chunk_next, chunk_count, owner_first, counters, stats, zbackup, af_net,
+      af_plain, af_fallback, tile_order, frag_list;
   uint32_t entry_capacity = 1u << 24;  // bin entries (grows after an overflow)
   uint32_t chunk_capacity = 1u << 18;  // fragment chunks (grows after an overflow)
   uint32_t af_capacity = 0;            // learned-filter plain-queue records (grows after an overflow)
   void release() {
     for (Arena* a : {&params, &slot_rec, &recs, &bin_counts, &scan_sums, &bin_entries, &tile_begin, &frag_rec,
-                     &frag_pos, &frag_mask, &frag_color, &frag_ps, &chunk_next, &chunk_count, &owner_first,
+                     &frag_pos, &frag_mask, &frag_color, &frag_color_more, &frag_ps, &chunk_next, &chunk_count,
+                     &owner_first,
                      &counters, &stats, &zbackup, &af_net, &af_plain, &af_fallback, &tile_order, &frag_list})
       a->release();
   }
@@ -171,13 +172,13 @@ struct PassPlan {
   std::vector<SurfaceJob> clears, resolves;
   std::vector<uint32_t> clear_cmd;
   // conflict tracking
-  std::map<std::pair<uint32_t, uint32_t>, uint32_t> target_of;  // (colour, ds) -> target index
+  std::map<std::vector<uint32_t>, uint32_t> target_of;  // (colours..., ds) -> target index
   std::set<uint32_t> surfaces;               // textures used as targets by the pass's draws
   std::set<uint32_t> sampled;                // textures its draws sample
   std::set<uint32_t> resolved;               // textures its queued resolves read or write
   std::set<uint32_t> cleared;                // textures its queued clears write
   std::vector<uint8_t> late_z;               // per target: a draw tests depth after shading
-  std::vector<uint32_t> target_color, target_ds;
+  uint32_t more_colors = 0;                  // most colour targets after the first of any of its targets
   std::set<uint32_t> af_textures;            // textures its learned-filter draws take feature taps from
   uint64_t nprims = 0;
   uint64_t samples = 0;                      // target samples of the pass's targets
@@ -475,7 +476,15 @@ void stage_end(sg_device* d, int stage, cudaEvent_t b) {
 // draw translation (renderer_impl state -> DrawParams)
 
 struct DrawInfo {
-  uint32_t color = 0, ds = 0;       // target textures
+  uint32_t color = 0, ds = 0;       // target textures: colour target 0, depth-stencil
+  uint32_t more[SG_MAX_COLOR_TARGETS - 1] = {};  // colour targets 1.. (0 = none)
+  uint32_t nmore = 0;
+  std::vector<uint32_t> key() const {  // the target's identity in a pass
+    std::vector<uint32_t> k{color};
+    k.insert(k.end(), more, more + nmore);
+    k.push_back(ds);
+    return k;
+  }
   uint32_t tex[2] = {0, 0};         // sampled textures
   uint32_t af_model = 0;            // learned filter of an SG_PS_TEX_GRAD_LEARNED draw
   uint32_t af_texture = 0;          // the texture its feature taps read
@@ -494,7 +503,19 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   if (!ct && !dt) return SG_FAILED;  // renderer_impl::set_render_targets
   if (ct && !valid_color_fmt(ct->fmt)) return SG_INVALID_PARAMETER;
   if (dt && !valid_ds_fmt(dt->fmt)) return SG_FAILED;
-  if (ct && dt && (dt->samples != ct->samples || dt->levels[0].w < ct->levels[0].w || dt->levels[0].h < ct->levels[0].h))
+  // further colour targets: same sample count; the render area is the
+  // smallest colour target (renderer_impl.cpp:159-238)
+  uint32_t area_w = ct ? ct->levels[0].w : 0, area_h = ct ? ct->levels[0].h : 0;
+  info.nmore = 0;
+  for (uint32_t i = 0; ct && i < SG_MAX_COLOR_TARGETS - 1 && desc->more_color_targets[i]; ++i) {
+    Texture* mt = find_tex(d, desc->more_color_targets[i]);
+    if (!mt || !valid_color_fmt(mt->fmt)) return SG_INVALID_PARAMETER;
+    if (mt->samples != ct->samples) return SG_FAILED;
+    area_w = std::min(area_w, mt->levels[0].w);
+    area_h = std::min(area_h, mt->levels[0].h);
+    info.more[info.nmore++] = desc->more_color_targets[i];
+  }
+  if (ct && dt && (dt->samples != ct->samples || dt->levels[0].w < area_w || dt->levels[0].h < area_h))
     return SG_FAILED;
   if (desc->prim_count > SG_PASS_MAX_PRIMS) return SG_INVALID_PARAMETER;
   info.color = desc->color_target;
@@ -548,9 +569,11 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   if (int32_t r = build_sampler(d, desc->ps.samplers[0], p.ps_samp, &info.tex[1])) return r;
   if (p.vs_prog == SG_VS_MORPH_DISPLACE && !desc->vs.samplers[0]) return SG_INVALID_PARAMETER;
   if (p.vs_prog < SG_VS_TRANSFORM || p.vs_prog > SG_VS_MORPH_DISPLACE || p.ps_prog < SG_PS_COLOR ||
-      p.ps_prog > SG_PS_TEX_ALPHA_TEST || p.bs_prog < SG_BS_REPLACE || p.bs_prog > SG_BS_ADD)
+      p.ps_prog > SG_PS_COLOR_MRT || p.bs_prog < SG_BS_REPLACE || p.bs_prog > SG_BS_REPLACE_ALL)
     return SG_INVALID_PARAMETER;
-  if (p.ps_prog != SG_PS_COLOR && p.ps_prog != SG_PS_CONSTANT && !desc->ps.samplers[0]) return SG_INVALID_PARAMETER;
+  if (p.ps_prog != SG_PS_COLOR && p.ps_prog != SG_PS_CONSTANT && p.ps_prog != SG_PS_COLOR_MRT &&
+      !desc->ps.samplers[0])
+    return SG_INVALID_PARAMETER;
   if (p.ps_prog == SG_PS_TEX_GRAD_LEARNED) {
     if (!d->af_models.count(desc->ps.learned_filter)) return SG_INVALID_PARAMETER;
     info.af_model = desc->ps.learned_filter;
@@ -606,17 +629,15 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   return SG_OK;
 }
 
-// Target parameters of a (colour, depth-stencil) pair.
-void fill_target(sg_device* d, uint32_t color, uint32_t ds, TargetParams& T) {
+// Target parameters of a set of colour targets and a depth-stencil target.
+void fill_target(sg_device* d, DrawInfo const& info, TargetParams& T) {
   std::memset(&T, 0, sizeof(T));
-  Texture* ct = color ? find_tex(d, color) : nullptr;
-  Texture* dt = ds ? find_tex(d, ds) : nullptr;
+  Texture* ct = info.color ? find_tex(d, info.color) : nullptr;
+  Texture* dt = info.ds ? find_tex(d, info.ds) : nullptr;
   Texture* tt = ct ? ct : dt;
   T.samples = tt->samples;
   T.width = tt->levels[0].w;
   T.height = tt->levels[0].h;
-  T.target_w = static_cast<float>(T.width);
-  T.target_h = static_cast<float>(T.height);
   static const float pat1[2] = {0.5f, 0.5f};
   static const float pat2[4] = {0.25f, 0.25f, 0.75f, 0.75f};
   static const float pat4[8] = {0.375f, 0.125f, 0.875f, 0.375f, 0.125f, 0.625f, 0.625f, 0.875f};
@@ -629,7 +650,20 @@ void fill_target(sg_device* d, uint32_t color, uint32_t ds, TargetParams& T) {
     T.color = ct->levels[0].ptr;
     T.color_fmt = ct->fmt;
     T.color_esz = ct->esz;
+    T.color_stride = ct->levels[0].w;
+    for (uint32_t i = 0; i < info.nmore; ++i) {
+      Texture* mt = find_tex(d, info.more[i]);
+      T.more_color[i] = mt->levels[0].ptr;
+      T.more_fmt[i] = mt->fmt;
+      T.more_esz[i] = mt->esz;
+      T.more_stride[i] = mt->levels[0].w;
+      T.width = std::min(T.width, mt->levels[0].w);
+      T.height = std::min(T.height, mt->levels[0].h);
+    }
+    T.nmore = info.nmore;
   }
+  T.target_w = static_cast<float>(T.width);
+  T.target_h = static_cast<float>(T.height);
   if (dt) {
     T.ds = dt->levels[0].ptr;
     T.ds_fmt = dt->fmt;
@@ -644,22 +678,24 @@ void fill_target(sg_device* d, uint32_t color, uint32_t ds, TargetParams& T) {
 // Whether the draw can join the pass; if not, the pass must run first.
 bool draw_fits(sg_device* d, PassPlan const& pl, DrawParams const& p, DrawInfo const& info) {
   if (pl.nprims + p.prim_count > SG_PASS_MAX_PRIMS) return false;
-  if (!pl.draws.empty() && !pl.target_of.count({info.color, info.ds})) {
+  if (!pl.draws.empty() && !pl.target_of.count(info.key())) {
     Texture* t = find_tex(d, info.color ? info.color : info.ds);
     uint64_t const smp = static_cast<uint64_t>(t->levels[0].w) * t->levels[0].h * t->samples;
     if (pl.samples + smp > SG_PASS_MAX_SAMPLES) return false;
   }
   for (uint32_t t : info.tex)
     if (t && (pl.surfaces.count(t) || pl.cleared.count(t) || pl.resolved.count(t))) return false;
-  for (uint32_t s : {info.color, info.ds}) {
+  std::vector<uint32_t> const key = info.key();
+  for (uint32_t s : key) {
     if (!s) continue;
     if (pl.sampled.count(s) || pl.resolved.count(s)) return false;
   }
   if (info.af_model && pl.af_model && info.af_model != pl.af_model) return false;
-  auto it = pl.target_of.find({info.color, info.ds});
+  auto it = pl.target_of.find(key);
   if (it == pl.target_of.end()) {
     // a new target may not share a surface with an existing one
-    if ((info.color && pl.surfaces.count(info.color)) || (info.ds && pl.surfaces.count(info.ds))) return false;
+    for (uint32_t s : key)
+      if (s && pl.surfaces.count(s)) return false;
   } else if ((p.zcfg & 128u) && pl.late_z[it->second]) {
     return false;  // depth tested before shading after a draw that tests after shading
   }
@@ -667,20 +703,21 @@ bool draw_fits(sg_device* d, PassPlan const& pl, DrawParams const& p, DrawInfo c
 }
 
 void add_draw(sg_device* d, PassPlan& pl, DrawParams p, DrawInfo const& info, uint32_t cmd) {
-  auto key = std::make_pair(info.color, info.ds);
+  auto key = info.key();
   auto it = pl.target_of.find(key);
   uint32_t t;
   if (it == pl.target_of.end()) {
     t = static_cast<uint32_t>(pl.targets.size());
     pl.target_of[key] = t;
     TargetParams T;
-    fill_target(d, info.color, info.ds, T);
+    fill_target(d, info, T);
     pl.targets.push_back(T);
     pl.late_z.push_back(0);
     pl.samples += static_cast<uint64_t>(T.width) * T.height * T.samples;
     pl.quads += static_cast<uint64_t>((T.width + 1) / 2) * ((T.height + 1) / 2);
-    if (info.color) pl.surfaces.insert(info.color);
-    if (info.ds) pl.surfaces.insert(info.ds);
+    for (uint32_t x : key)
+      if (x) pl.surfaces.insert(x);
+    pl.more_colors = std::max(pl.more_colors, T.nmore);
   } else {
     t = it->second;
   }
@@ -802,7 +839,11 @@ void bind_params(PassParams& P, uint8_t* params, PlanLayout const& L, PassPlan c
   P.nchunks = pl.nchunks;
 }
 
-size_t per_chunk_bytes() { return FRAG_CHUNK * (4 + 4 + 4 + 4 * sizeof(float4) + 1) + 8; }
+// bytes of one fragment chunk: record, position, masks, four pixel colours
+// (and four per further colour target), pass mask; the chunk's link and count
+size_t per_chunk_bytes(uint32_t more_colors) {
+  return FRAG_CHUNK * (4 + 4 + 4 + 4 * sizeof(float4) * (1 + more_colors) + 1) + 8;
+}
 
 // Scratch in the device's (or a graph's) arenas.
 int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout const& L, bool own_params,
@@ -828,6 +869,12 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.frag_pos.ensure(nfrag * 4));
   SG_CUDA(d, sc.frag_mask.ensure(nfrag * 4));
   SG_CUDA(d, sc.frag_color.ensure(nfrag * 4 * sizeof(float4)));
+  P.more_colors = pl.more_colors;
+  P.frag_color_more = nullptr;
+  if (pl.more_colors) {
+    SG_CUDA(d, sc.frag_color_more.ensure(nfrag * 4 * pl.more_colors * sizeof(float4)));
+    P.frag_color_more = static_cast<float4*>(sc.frag_color_more.ptr);
+  }
   SG_CUDA(d, sc.frag_ps.ensure(nfrag));
   SG_CUDA(d, sc.frag_list.ensure((nfrag + 256) * 4));
   SG_CUDA(d, sc.chunk_next.ensure(static_cast<size_t>(sc.chunk_capacity) * 4));
@@ -928,12 +975,15 @@ int32_t scratch_static(sg_device* d, uint8_t* base, PassPlan const& pl, PlanLayo
   uint32_t entries = static_cast<uint32_t>(rest / 4 / 4);
   P.bin_entries = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(entries) * 4));
   P.bin_capacity = entries;
-  uint32_t chunks = static_cast<uint32_t>((SG_STATIC_SCRATCH_BYTES - off - 6 * 256) / per_chunk_bytes());
+  uint32_t chunks = static_cast<uint32_t>((SG_STATIC_SCRATCH_BYTES - off - 7 * 256) / per_chunk_bytes(pl.more_colors));
   size_t nfrag = static_cast<size_t>(chunks) * FRAG_CHUNK;
   P.frag_rec = reinterpret_cast<uint32_t*>(take(nfrag * 4));
   P.frag_pos = reinterpret_cast<uint32_t*>(take(nfrag * 4));
   P.frag_mask = reinterpret_cast<uint32_t*>(take(nfrag * 4));
   P.frag_color = reinterpret_cast<float4*>(take(nfrag * 4 * sizeof(float4)));
+  P.more_colors = pl.more_colors;
+  P.frag_color_more = pl.more_colors ? reinterpret_cast<float4*>(take(nfrag * 4 * pl.more_colors * sizeof(float4)))
+                                     : nullptr;
   P.frag_ps = take(nfrag);
   P.chunk_next = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(chunks) * 4));
   P.chunk_count = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(chunks) * 4));

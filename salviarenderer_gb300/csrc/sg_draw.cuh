@@ -58,7 +58,14 @@ struct TargetParams {
   uint8_t* color;
   uint8_t* ds;
   uint32_t color_fmt, color_esz;
-  uint32_t width, height;            // colour target (or depth target) size
+  uint32_t color_stride;             // texels per row of colour target 0
+  // colour targets after the first (renderer_impl::set_render_targets with
+  // several); each with its own format and row length
+  uint32_t nmore;
+  uint8_t* more_color[SG_MAX_COLOR_TARGETS - 1];
+  uint32_t more_fmt[SG_MAX_COLOR_TARGETS - 1], more_esz[SG_MAX_COLOR_TARGETS - 1];
+  uint32_t more_stride[SG_MAX_COLOR_TARGETS - 1];
+  uint32_t width, height;            // render area: the smallest colour target (or the depth target)
   uint32_t ds_fmt, ds_esz, ds_width;
   uint32_t samples;
   int tiles_x, tiles_y;              // tile grid: the largest of the pass's draws on this target
@@ -153,7 +160,11 @@ struct PassParams {
   uint32_t* frag_rec;           // triangle record
   uint32_t* frag_pos;           // bits 0-11 x/2, 12-23 y/2 (absolute quad), 24 full quad, 25-31 shade key
   uint32_t* frag_mask;          // bits 0-15 early-Z-tested samples, 16-31 covered samples
-  float4* frag_color;           // 4 pixels per fragment, pixel-shader output
+  float4* frag_color;           // 4 pixels per fragment, pixel-shader output (colour 0)
+  // the pixel-shader colours 1..more_colors of every pixel, for passes whose
+  // targets have several colour targets ((f * 4 + pixel) * more_colors + i - 1)
+  float4* frag_color_more;
+  uint32_t more_colors;
   uint8_t* frag_ps;             // pixel-shader pass mask (4 bits)
   uint32_t* chunk_next;
   uint32_t* chunk_count;

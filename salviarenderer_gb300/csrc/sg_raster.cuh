@@ -127,13 +127,24 @@ __device__ inline uint8_t* ds_addr(TargetParams const& T, uint32_t x, uint32_t y
   return T.ds + ((static_cast<size_t>(y) * T.ds_width + x) * T.samples + s) * T.ds_esz;
 }
 __device__ inline uint8_t* color_addr(TargetParams const& T, uint32_t x, uint32_t y, uint32_t s) {
-  return T.color + ((static_cast<size_t>(y) * T.width + x) * T.samples + s) * T.color_esz;
+  return T.color + ((static_cast<size_t>(y) * T.color_stride + x) * T.samples + s) * T.color_esz;
 }
 
-// cpp_blend_shader programs
-__device__ inline void blend(TargetParams const& T, DrawParams const& D, uint32_t x, uint32_t y, uint32_t s, v4 src) {
+// cpp_blend_shader programs; `more` holds the pixel's colours 1.. (or null)
+__device__ inline void blend(TargetParams const& T, DrawParams const& D, uint32_t x, uint32_t y, uint32_t s, v4 src,
+                             float4 const* more) {
   if (!T.color) return;
   uint8_t* a = color_addr(T, x, y, s);
+  if (D.bs_prog == SG_BS_REPLACE_ALL) {  // color(i, s) = in.color[i] for every bound target
+    write_texel(T.color_fmt, a, src);
+    for (uint32_t i = 0; i < T.nmore; ++i) {
+      float4 const c = more ? more[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      write_texel(T.more_fmt[i],
+                  T.more_color[i] + ((static_cast<size_t>(y) * T.more_stride[i] + x) * T.samples + s) * T.more_esz[i],
+                  mk4(c.x, c.y, c.z, c.w));
+    }
+    return;
+  }
   switch (D.bs_prog) {
   case SG_BS_LERP_SRC_ALPHA: {
     v4 d = read_texel(T.color_fmt, a);
@@ -180,9 +191,9 @@ __device__ inline uint32_t blend_word(uint32_t fmt, uint32_t bs_prog, uint32_t d
 
 // framebuffer::render_sample (framebuffer.cpp:445-479)
 __device__ inline void render_sample(TargetParams const& T, DrawParams const& D, uint32_t x, uint32_t y, uint32_t s,
-                                     v4 src, float depth, bool front) {
+                                     v4 src, float depth, bool front, float4 const* more) {
   if (D.early_z || !T.ds) {
-    blend(T, D, x, y, s, src);
+    blend(T, D, x, y, s, src, more);
     return;
   }
   uint8_t* a = ds_addr(T, x, y, s);
@@ -192,7 +203,7 @@ __device__ inline void render_sample(TargetParams const& T, DrawParams const& D,
   bool sp = D.stencil ? cmpu(func, D.stencil_ref, old.stencil) : true;
   if (dp && sp) {
     uint32_t ns = D.stencil ? stencil_op(front ? D.front_pass : D.back_pass, D.stencil_ref, old.stencil) : 0u;
-    blend(T, D, x, y, s, src);
+    blend(T, D, x, y, s, src, more);
     ds_write(T, D, a, depth, ns, D.write_mask);
   }
 }
@@ -664,7 +675,8 @@ __device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q, bool& ke
   float u2 = __shfl_sync(mask, a0.x, base + 2), v2 = __shfl_sync(mask, a0.y, base + 2);
   keep = true;
   switch (D.ps_prog) {
-  case SG_PS_COLOR: return a0;
+  case SG_PS_COLOR:
+  case SG_PS_COLOR_MRT: return a0;  // (its other colours: k_shade)
   case SG_PS_CONSTANT: return mk4(D.ps_k[0], D.ps_k[1], D.ps_k[2], D.ps_k[3]);
   case SG_PS_TEX_MODULATE: {
     float lod = calc_lod_2d(D.ps_samp, u1 - u0, v1 - v0, u2 - u0, v2 - v0);
@@ -851,10 +863,21 @@ __global__ void __launch_bounds__(256, LEARNED ? 4 : 3) k_shade(PassParams P) {
         v4 const m = NA > 1 ? attr[NA > 1 ? 1 : 0] : mk4(0, 0, 0, 0);
         af_r2 = make_float4(m.x, m.y, m.z, m.w);
         if (q == 0) P.frag_ps[f] = 0xF;  // the learned filter's lookups never discard
+        if (P.frag_color_more)  // colours the program does not write are zero
+          for (uint32_t i = 0; i < P.more_colors; ++i)
+            P.frag_color_more[(static_cast<size_t>(f) * 4 + q) * P.more_colors + i] = make_float4(0, 0, 0, 0);
       } else {
         bool keep = true;
         v4 out = run_ps<NA>(D, attr, q, keep);  // all four lanes of a quad take the same path
         P.frag_color[static_cast<size_t>(f) * 4 + q] = make_float4(out.x, out.y, out.z, out.w);
+        if (P.frag_color_more)  // colours 1..: attributes 1.. of SG_PS_COLOR_MRT, else zero
+          for (uint32_t i = 0; i < P.more_colors; ++i) {
+            v4 c = mk4(0, 0, 0, 0);
+#pragma unroll
+            for (int k = 1; k < NA; ++k)
+              if (D.ps_prog == SG_PS_COLOR_MRT && static_cast<uint32_t>(k) == i + 1) c = attr[k];
+            P.frag_color_more[(static_cast<size_t>(f) * 4 + q) * P.more_colors + i] = make_float4(c.x, c.y, c.z, c.w);
+          }
         // the quad's pass mask as cpp_pixel_shader::execute builds it
         // (cpp_pixel_shader.cpp:62-74): from int shifts of 0xFFFF by 16 i, so
         // pixel 0 is kept when pixel 0 or 2 passes and pixels 1-3 when pixel
@@ -1007,7 +1030,8 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
             for (uint32_t s = 0; s < T.samples; ++s) aa[s] = (T.sp_x[s] - 0.5f) * dz + (T.sp_y[s] - 0.5f) * dyz;
           }
         }
-        if ((D.early_z || !T.ds) && T.color && T.color_esz == 4 && T.samples == 4) {
+        if ((D.early_z || !T.ds) && T.color && T.color_esz == 4 && T.samples == 4 &&
+            (T.nmore == 0 || D.bs_prog != SG_BS_REPLACE_ALL)) {
           // colour only, four 4-byte samples per pixel: each covered pixel's
           // samples are read, blended and written as one 16-byte word
           uint4 w[4];
@@ -1046,12 +1070,14 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
           if (!pm) continue;
           float4 cc = P.frag_color[static_cast<size_t>(f) * 4 + i];
           v4 src = mk4(cc.x, cc.y, cc.z, cc.w);
+          float4 const* more =
+              P.frag_color_more ? P.frag_color_more + (static_cast<size_t>(f) * 4 + i) * P.more_colors : nullptr;
           uint32_t x = qx + (i & 1), y = qy + (i >> 1);
           if (T.samples == 1) {
-            render_sample(T, D, x, y, 0, src, depth[i], front);
+            render_sample(T, D, x, y, 0, src, depth[i], front, more);
           } else {
             for (uint32_t s = 0; s < T.samples; ++s)
-              if (pm & (1u << s)) render_sample(T, D, x, y, s, src, depth[i] + aa[s], front);
+              if (pm & (1u << s)) render_sample(T, D, x, y, s, src, depth[i] + aa[s], front, more);
           }
         }
       }

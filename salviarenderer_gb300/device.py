@@ -403,6 +403,8 @@ def make_draw_desc(**kw):
     vp = kw["viewport"]
     d.viewport = abi.Viewport(*vp)
     d.color_target = kw.get("color_target", 0)
+    for i, t in enumerate(kw.get("more_color_targets", ())):
+        d.more_color_targets[i] = t
     d.ds_target = kw.get("ds_target", 0)
     d.indexed = 1 if kw.get("index_buffer") else 0
     d.index_buffer = kw.get("index_buffer", 0)

@@ -100,6 +100,7 @@ class Scene:
         self.clear_depth = 1.0
         self.clear_stencil = 0
         self.resolve = samples > 1
+        self.more_colors = []   # colour targets 1..: (format, width, height)
 
     @property
     def triangles(self):
@@ -127,6 +128,7 @@ class Bound:
         self.color = dev.texture(s.width, s.height, s.samples, s.color_fmt) if s.color_fmt is not None else 0
         self.ds = dev.texture(s.width, s.height, s.samples, s.ds_fmt) if s.ds_fmt is not None else 0
         self.resolved = dev.texture(s.width, s.height, 1, s.color_fmt) if (s.resolve and self.color) else 0
+        self.more = [dev.texture(w, h, s.samples, fmt) for fmt, w, h in s.more_colors]
         self.descs = [self._desc(d) for d in scene.draws]
 
     def _shader(self, spec):
@@ -143,6 +145,7 @@ class Bound:
         if d.get("index_buffer"):
             kw["index_buffer"] = self.buf[d["index_buffer"]]
         kw["color_target"] = self.color
+        kw["more_color_targets"] = self.more
         kw["ds_target"] = self.ds
         for n in ("vs", "ps", "bs"):
             kw[n] = self._shader(d[n])
@@ -152,6 +155,8 @@ class Bound:
         s = self.scene
         if self.color:
             self.dev.clear_color(self.color, s.clear_color)
+        for t in self.more:
+            self.dev.clear_color(t, s.clear_color)
         if self.ds:
             self.dev.clear_depth_stencil(self.ds, abi.CLEAR_DEPTH | abi.CLEAR_STENCIL,
                                          s.clear_depth, s.clear_stencil)
@@ -178,6 +183,8 @@ class Bound:
         cl = CommandList()
         if self.color:
             cl.clear_color(self.color, s.clear_color)
+        for t in self.more:
+            cl.clear_color(t, s.clear_color)
         if self.ds:
             cl.clear_depth_stencil(self.ds, abi.CLEAR_DEPTH | abi.CLEAR_STENCIL, s.clear_depth, s.clear_stencil)
         for desc in self.descs:
@@ -195,6 +202,8 @@ class Bound:
             out["depth_stencil"] = d.texture_download(self.ds)
         if self.resolved:
             out["resolved"] = d.texture_download(self.resolved)
+        for i, t in enumerate(self.more):
+            out[f"color{i + 1}"] = d.texture_download(t)
         return out
 
 
@@ -409,6 +418,40 @@ def stencil_ops_scene(front, back, seed=1, width=96, height=80, samples=1, ntris
                             inputs=VS_POS_COLOR_INPUTS, num_varyings=1, depth_stencil=dsd, stencil_ref=ref,
                             vs=dict(program=abi.VS_TRANSFORM, constants=ident),
                             ps=dict(program=abi.PS_COLOR), bs=dict(program=abi.BS_REPLACE)))
+    return s
+
+
+def mrt_scene(seed=1, width=96, height=80, samples=1, ntris=120, more=((abi.FMT_RGBA32F, 112, 80),),
+              ds_fmt=abi.FMT_RG32F):
+    """Several colour targets (renderer_impl::set_render_targets with more
+    than one): random clip-space triangles whose pixel shader writes one
+    colour per target (SG_PS_COLOR_MRT, colour i = attribute i) and whose
+    blend shader writes every target (SG_BS_REPLACE_ALL); then a draw that
+    writes only target 0 (source-alpha blend), leaving the others.  `more`
+    lists targets 1.. as (format, width, height); the render area is the
+    smallest target."""
+    rng = np.random.default_rng(seed)
+    s = Scene("mrt", width, height, samples, ds_fmt=ds_fmt)
+    s.more_colors = list(more)
+    s.clear_color = (0.1, 0.2, 0.3, 0.4)
+    nt = 1 + len(more)
+    pos = rng.uniform(-1.0, 1.0, size=(ntris * 3, 4))
+    pos[:, 2] = rng.uniform(0.05, 0.95, size=ntris * 3)
+    pos[:, 3] = 1.0
+    cols = rng.uniform(0.0, 1.0, size=(ntris * 3, 4 * nt))
+    s.buffers["vb"] = np.concatenate([pos, cols], axis=1).astype(np.float32)
+    stride = 16 * (1 + nt)
+    inputs = [(abi.SEMANTIC_POSITION, 0, abi.VFMT_R32G32B32A32_FLOAT, 0, 0)] + \
+             [(abi.SEMANTIC_COLOR, i, abi.VFMT_R32G32B32A32_FLOAT, 0, 16 * (1 + i)) for i in range(nt)]
+    ident = np.identity(4, dtype=np.float32)
+    half = ntris * 2 // 3
+    for first, count, ps, bs in ((0, half, abi.PS_COLOR_MRT, abi.BS_REPLACE_ALL),
+                                 (half, ntris - half, abi.PS_COLOR, abi.BS_LERP_SRC_ALPHA)):
+        s.draws.append(dict(viewport=(0, 0, width, height, 0.0, 1.0), prim_count=count,
+                            streams=[("vb", stride, stride * 3 * first)], inputs=inputs, num_varyings=nt,
+                            varying_modifiers=[abi.AM_LINEAR] * nt,
+                            vs=dict(program=abi.VS_TRANSFORM, constants=ident), ps=dict(program=ps),
+                            bs=dict(program=bs)))
     return s
 
 

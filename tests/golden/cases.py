@@ -84,6 +84,12 @@ CASES = {
     "ps_discard_late_z_stencil": lambda: F(seed=28, ps=abi.PS_TEX_ALPHA_TEST, sampler=TRILINEAR,
                                            ps_constants=[0.45], ntris=200,
                                            stencil=(abi.CMP_ALWAYS, abi.SOP_INCR_WRAP, 0)),
+    # several colour targets (renderer_impl.cpp:159-238): of other formats and
+    # sizes (the render area is the smallest), a blend writing all of them
+    "mrt_3_targets": lambda: scenes.mrt_scene(seed=60, more=((abi.FMT_RGBA32F, 112, 80), (abi.FMT_BGRA8, 96, 72))),
+    "mrt_4x_5_targets": lambda: scenes.mrt_scene(seed=61, samples=4, ntris=80,
+                                                 more=((abi.FMT_RGBA8, 96, 80), (abi.FMT_RGBA32F, 96, 80),
+                                                       (abi.FMT_RGBA8, 100, 90), (abi.FMT_BGRA8, 96, 80))),
     # C2 pattern (textured grid, trilinear + 16x AF, src-alpha blend)
     "c2_160x96_4x": lambda: scenes.c2_scene(width=160, height=96, grid=33, tex_size=128, ndraws=4),
     "c2_128x72_1x": lambda: scenes.c2_scene(width=128, height=72, grid=25, tex_size=64, samples=1,

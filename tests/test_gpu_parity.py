@@ -48,6 +48,8 @@ def compare(gdev, odev, scene):
     for k in ("color", "resolved"):
         if k in want:
             assert_color_close(got[k], want[k], scene.color_fmt, k)
+    for i, (fmt, _, _) in enumerate(scene.more_colors):  # colour targets 1..
+        assert_color_close(got[f"color{i + 1}"], want[f"color{i + 1}"], fmt, f"color{i + 1}")
     return got, want
 
 
