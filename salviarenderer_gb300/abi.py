@@ -135,7 +135,8 @@ class Tuning(C.Structure):
     _fields_ = [("cover_item", C.c_uint32), ("split_entries", C.c_uint32), ("bin_chunk", C.c_uint32),
                 ("bin_capacity", C.c_uint32), ("frag_chunks", C.c_uint32),
                 ("shade_quads_per_warp", C.c_uint32), ("shade_ctas_per_sm", C.c_uint32),
-                ("merge_ctas_per_sm", C.c_uint32), ("cover_threads_per_block", C.c_uint32)]
+                ("merge_ctas_per_sm", C.c_uint32), ("cover_threads_per_block", C.c_uint32),
+                ("cover_ctas_per_sm", C.c_uint32), ("shade_resident", C.c_uint32)]
 
 
 _u32p = C.POINTER(C.c_uint32)

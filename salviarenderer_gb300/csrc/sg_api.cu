@@ -35,18 +35,19 @@ cudaError_t launch_tile_order(PassParams const& P, uint32_t* counts, cudaStream_
 cudaError_t launch_frag_classes(PassParams const& P, uint32_t num_sms, cudaStream_t s);
 void launch_cover(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
 cudaError_t init_cover();
-void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
+void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t ctas_per_sm, uint32_t grid,
+                   cudaStream_t s);
 cudaError_t init_cover2();
 void launch_cover_rollback(PassParams const& p, uint32_t grid, cudaStream_t s);
 cudaError_t init_learned();
 cudaError_t init_af_filter();
 void launch_merge(PassParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_0(PassParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_1(PassParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_2(PassParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_3(PassParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_4(PassParams const& p, uint32_t grid, cudaStream_t s);
-void launch_shade_5(PassParams const& p, uint32_t grid, cudaStream_t s);
+void launch_shade_0(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
+void launch_shade_1(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
+void launch_shade_2(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
+void launch_shade_3(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
+void launch_shade_4(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
+void launch_shade_5(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
 cudaError_t upload_ewa_table_raster_a(float const* tab, cudaStream_t s);
 cudaError_t upload_ewa_table_raster_b(float const* tab, cudaStream_t s);
 cudaError_t upload_ewa_table_raster_c(float const* tab, cudaStream_t s);
@@ -233,9 +234,11 @@ sg_tuning default_tuning() {
   t.bin_capacity = 1u << 24;
   t.frag_chunks = 1u << 18;
   t.shade_quads_per_warp = 8;
-  t.shade_ctas_per_sm = 16;
+  t.shade_ctas_per_sm = 8;
   t.merge_ctas_per_sm = 6;
   t.cover_threads_per_block = 2;
+  t.cover_ctas_per_sm = 4;
+  t.shade_resident = 4;
   return t;
 }
 
@@ -1039,7 +1042,8 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       stage_end(d, 1, ev);
       ev = stage_begin(d, profile);
       if (tu.cover_threads_per_block == 2)
-        launch_cover2(P, pl.max_samples, pl.any_early_z, std::min<uint32_t>(pl.ntiles * 4, sms * 8), s);
+        launch_cover2(P, pl.max_samples, pl.any_early_z, tu.cover_ctas_per_sm, std::min<uint32_t>(pl.ntiles * 4, sms * 8),
+                      s);
       else
         launch_cover(P, pl.max_samples, pl.any_early_z, cover_grid, s);
       stage_end(d, 2, ev);
@@ -1055,12 +1059,12 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       for (uint32_t cls = 0; cls < 16; ++cls) {
         if (!(classes & (1u << cls))) continue;
         switch (cls) {
-        case 0: launch_shade_0(P, shade_grid, s); break;
-        case 1: launch_shade_1(P, shade_grid, s); break;
-        case 2: launch_shade_2(P, shade_grid, s); break;
-        case 3: launch_shade_3(P, shade_grid, s); break;
-        case 4: launch_shade_4(P, shade_grid, s); break;
-        case 5: launch_shade_5(P, shade_grid, s); break;
+        case 0: launch_shade_0(P, shade_grid, tu.shade_resident, s); break;
+        case 1: launch_shade_1(P, shade_grid, tu.shade_resident, s); break;
+        case 2: launch_shade_2(P, shade_grid, tu.shade_resident, s); break;
+        case 3: launch_shade_3(P, shade_grid, tu.shade_resident, s); break;
+        case 4: launch_shade_4(P, shade_grid, tu.shade_resident, s); break;
+        case 5: launch_shade_5(P, shade_grid, tu.shade_resident, s); break;
         default: launch_shade_learned(cls - 8, P, shade_grid, s); break;
         }
         ++k;
@@ -1958,7 +1962,8 @@ int32_t sg_set_tuning(sg_device* d, const sg_tuning* t) {
       (t->bin_chunk & (t->bin_chunk - 1)) || t->bin_capacity == 0 || t->frag_chunks == 0 ||
       t->shade_quads_per_warp != 8 || t->shade_ctas_per_sm == 0 || t->shade_ctas_per_sm > 32 ||
       t->merge_ctas_per_sm == 0 || t->merge_ctas_per_sm > 8 ||
-      (t->cover_threads_per_block != 2 && t->cover_threads_per_block != 32))
+      (t->cover_threads_per_block != 2 && t->cover_threads_per_block != 32) ||
+      (t->cover_ctas_per_sm != 3 && t->cover_ctas_per_sm != 4) || (t->shade_resident != 3 && t->shade_resident != 4))
     return SG_INVALID_PARAMETER;
   // a changed initial capacity is where the next passes start from (they
   // grow again on overflow)
@@ -1994,10 +1999,12 @@ int32_t sg_autotune(sg_device* d, const sg_command* cmds, uint32_t n, uint32_t r
   float best = 0.0f;
   int32_t r = time_of(best_t, best);
   for (int sweep = 0; sweep < 2 && r == SG_OK; ++sweep) {
-    for (int param = 0; param < 6 && r == SG_OK; ++param) {
+    for (int param = 0; param < 8 && r == SG_OK; ++param) {
       std::vector<uint32_t> vals;
       switch (param) {
       case 5: vals = {2u, 32u}; break;
+      case 6:
+      case 7: vals = {3u, 4u}; break;
       case 0: vals = {16u, 32u}; break;
       case 1: vals = {160u, 320u, 640u, 1280u}; break;
       case 2: vals = {256u, 512u, 1024u, 2048u}; break;
@@ -2008,10 +2015,13 @@ int32_t sg_autotune(sg_device* d, const sg_command* cmds, uint32_t n, uint32_t r
         sg_tuning t = best_t;
         uint32_t* field = param == 0 ? &t.cover_item : param == 1 ? &t.split_entries : param == 2 ? &t.bin_chunk
                           : param == 3 ? &t.shade_ctas_per_sm : param == 4 ? &t.merge_ctas_per_sm
-                          : &t.cover_threads_per_block;
+                          : param == 5 ? &t.cover_threads_per_block : param == 6 ? &t.cover_ctas_per_sm
+                          : &t.shade_resident;
         if (*field == v) continue;
-        // item size and split threshold only shape the warp-per-pair coverage
+        // item size and split threshold only shape the warp-per-pair coverage,
+        // the CTAs per SM only the 2-thread one
         if (param <= 1 && t.cover_threads_per_block != 32) continue;
+        if (param == 6 && t.cover_threads_per_block != 2) continue;
         if (param == 1 && t.cover_item == 16) continue;  // every item is 16x16 already
         *field = v;
         float ms = 0.0f;

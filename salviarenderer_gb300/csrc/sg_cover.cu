@@ -386,7 +386,9 @@ __device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint
   }
 }
 
-__global__ void __launch_bounds__(CV_THREADS, 3) k_cover2(PassParams P) {
+// MINB: CTAs per SM the register budget is cut for (3: 80 registers, 4: 64)
+template <int MINB>
+__global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   CvShared& sh = *reinterpret_cast<CvShared*>(smem_raw);
   uint32_t* const ztile = reinterpret_cast<uint32_t*>(smem_raw + ((sizeof(CvShared) + 15) & ~size_t(15)));
@@ -628,13 +630,26 @@ void launch_cover_rollback(PassParams const& p, uint32_t grid, cudaStream_t s) {
   k_cover_rollback<<<grid, 256, 0, s>>>(p);
 }
 
-void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s) {
-  k_cover2<<<grid, CV_THREADS, cv_smem(max_samples, early_z), s>>>(p);
+void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t ctas_per_sm, uint32_t grid,
+                   cudaStream_t s) {
+  if (ctas_per_sm >= 4)
+    k_cover2<4><<<grid, CV_THREADS, cv_smem(max_samples, early_z), s>>>(p);
+  else
+    k_cover2<3><<<grid, CV_THREADS, cv_smem(max_samples, early_z), s>>>(p);
 }
 
+// Per device (function attributes are per device): the largest dynamic
+// shared memory an item needs, and the shared-memory carveout at its
+// maximum so that four items' tables fit on an SM.
 cudaError_t init_cover2() {
-  return cudaFuncSetAttribute(k_cover2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(cv_smem(4, true)));
+  for (auto fn : {k_cover2<3>, k_cover2<4>}) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(cv_smem(4, true)));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace sg

@@ -726,8 +726,8 @@ __device__ inline bool af_takes(DrawParams const& D, float dxu, float dxv, float
 // (shade class 8 + NA) and queue the lookups the learned filter applies to;
 // they wait mostly on texture taps and queue atomics, so they run 4 CTAs per
 // SM (64 registers) where the plain instances run 3.
-template <int NA, bool LEARNED>
-__global__ void __launch_bounds__(256, LEARNED ? 4 : 3) k_shade(PassParams P) {
+template <int NA, bool LEARNED, int MINB = (LEARNED ? 4 : 3)>
+__global__ void __launch_bounds__(256, MINB) k_shade(PassParams P) {
   if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
   uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
   int const q = threadIdx.x & 3;
@@ -1089,9 +1089,13 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
 #endif  // SG_RASTER_COVER_MERGE
 
 // ---------------------------------------------------------------------------
+// `resident`: CTAs per SM the plain instances' registers are cut for (3 or 4)
 template <int NA>
-void launch_shade_t(PassParams const& P, uint32_t grid, cudaStream_t s) {
-  k_shade<NA, false><<<grid, 256, 0, s>>>(P);
+void launch_shade_t(PassParams const& P, uint32_t grid, uint32_t resident, cudaStream_t s) {
+  if (resident >= 4)
+    k_shade<NA, false, 4><<<grid, 256, 0, s>>>(P);
+  else
+    k_shade<NA, false, 3><<<grid, 256, 0, s>>>(P);
 }
 template <int NA>
 void launch_shade_learned_t(PassParams const& P, uint32_t grid, cudaStream_t s) {

@@ -3,8 +3,12 @@
 
 namespace sg {
 
-void launch_shade_2(PassParams const& p, uint32_t grid, cudaStream_t s) { launch_shade_t<2>(p, grid, s); }
-void launch_shade_3(PassParams const& p, uint32_t grid, cudaStream_t s) { launch_shade_t<3>(p, grid, s); }
+void launch_shade_2(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s) {
+  launch_shade_t<2>(p, grid, resident, s);
+}
+void launch_shade_3(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s) {
+  launch_shade_t<3>(p, grid, resident, s);
+}
 
 // The EWA table of this translation unit's sampler (each translation unit
 // has its own copy of the __constant__ table).

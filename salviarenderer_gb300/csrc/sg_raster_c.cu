@@ -3,8 +3,12 @@
 
 namespace sg {
 
-void launch_shade_4(PassParams const& p, uint32_t grid, cudaStream_t s) { launch_shade_t<4>(p, grid, s); }
-void launch_shade_5(PassParams const& p, uint32_t grid, cudaStream_t s) { launch_shade_t<5>(p, grid, s); }
+void launch_shade_4(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s) {
+  launch_shade_t<4>(p, grid, resident, s);
+}
+void launch_shade_5(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s) {
+  launch_shade_t<5>(p, grid, resident, s);
+}
 
 // The EWA table of this translation unit's sampler (each translation unit
 // has its own copy of the __constant__ table).
