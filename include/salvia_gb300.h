@@ -160,6 +160,76 @@ enum {
   SG_BS_REPLACE_ALL = 4     /* color(i, s) = in.color[i] for every bound colour target i */
 };
 
+/* ---- user shader programs ----------------------------------------------------
+ * The reference's applications write shader bodies as C++ classes
+ * (cpp_pixel_shader / cpp_blend_shader, shader.h:159-215).  Here a shader
+ * body is a class compiled by the application with nvcc against
+ * <salvia_gb300/device_shader.cuh> and exported by SALVIA_GB300_PIXEL_SHADER
+ * or SALVIA_GB300_BLEND_SHADER as an sg_shader_module: the pass kernels
+ * instantiated for the class (device code in the application's own module),
+ * and the same body compiled for the host, which CPU backends of this ABI
+ * run.  sg_shader_register gives the module a program id (at least
+ * SG_USER_PROGRAM_BASE) that draws name in sg_shader.program, beside the
+ * stock SG_PS_* / SG_BS_* programs.  Pixel shaders read sampler slot 0 and
+ * the pixel shader's constants; blend shaders the blend shader's constants.
+ * A pass holds draws of at most 8 user pixel shaders and one user blend
+ * shader (more split the pass). */
+#define SG_SHADER_ABI_VERSION 1
+#define SG_USER_PROGRAM_BASE 64
+enum { SG_STAGE_PIXEL = 1, SG_STAGE_BLEND = 2 };
+
+/* What a host backend hands a pixel-shader body for one pixel of a quad
+ * (cpp_pixel_shader::execute, cpp_pixel_shader.cpp:62-74): the pixel's
+ * interpolated registers and the backend's own cpp_pixel_shader helpers
+ * (cpp_pixel_shader.cpp:13-60; `reg` is a varying index, the lookups use
+ * sampler slot 0 of the draw's pixel shader). */
+typedef struct sg_host_ps_io {
+  float attr[SG_MAX_VARYINGS][4];      /* vs_output::attribute(i) */
+  float position[4];
+  uint32_t front_face;
+  uint32_t num_varyings;
+  const float* constants;              /* the pixel shader's SG_MAX_SHADER_CONSTANTS */
+  void* backend;
+  void (*ddx)(void* backend, uint32_t reg, float out[4]);
+  void (*ddy)(void* backend, uint32_t reg, float out[4]);
+  void (*tex2d)(void* backend, uint32_t reg, float out[4]);
+  void (*tex2dlod)(void* backend, uint32_t reg, float out[4]);
+  void (*tex2dproj)(void* backend, uint32_t reg, float out[4]);
+  void (*sample)(void* backend, float u, float v, float lod, float out[4]);  /* sampler::sample */
+  void (*sample_grad)(void* backend, float u, float v, float dxu, float dxv, float dyu, float dyv,
+                      float out[4]);   /* sampler::sample_2d_grad */
+  float color[SG_MAX_COLOR_TARGETS][4]; /* out: ps_output::color */
+} sg_host_ps_io;
+
+/* What a host backend hands a blend-shader body for one sample
+ * (cpp_blend_shader::execute, shader.cpp:524-526). */
+typedef struct sg_host_bs_io {
+  uint32_t sample;
+  float in_color[SG_MAX_COLOR_TARGETS][4]; /* ps_output::color */
+  const float* constants;              /* the blend shader's SG_MAX_SHADER_CONSTANTS */
+  void* backend;
+  /* pixel_accessor::color(target, sample) and color(target, sample, c) */
+  void (*get)(void* backend, uint32_t target, uint32_t sample, float out[4]);
+  void (*set)(void* backend, uint32_t target, uint32_t sample, const float c[4]);
+} sg_host_bs_io;
+
+typedef struct sg_shader_module {
+  uint32_t abi_version;                /* SG_SHADER_ABI_VERSION */
+  uint32_t stage;                      /* SG_STAGE_PIXEL or SG_STAGE_BLEND */
+  const char* name;
+  /* Called by a GPU device at registration, its CUDA device current:
+   * prepares the module's kernels there (the sampler's weight table of
+   * 256 floats, shared-memory limits); 0 on success. */
+  int32_t (*device_init)(const float* ewa_table, void* cuda_stream);
+  /* Launches the module's kernel for one pass: `pass` is the library's pass
+   * parameter block (opaque here), `key` the shade key of the module's
+   * fragments (pixel stage) or 0 (blend stage: the pass's merge). */
+  void (*device_launch)(const void* pass, uint32_t key, uint32_t grid, void* cuda_stream);
+  /* The body compiled for the host: shader_prog's result (0 discards). */
+  int32_t (*host_ps)(sg_host_ps_io* io);
+  int32_t (*host_bs)(sg_host_bs_io* io);
+} sg_shader_module;
+
 /* ---- descriptors ------------------------------------------------------------ */
 typedef struct sg_viewport {           /* salvia/include/salvia/core/viewport.h */
   float x, y, w, h, minz, maxz;
@@ -523,6 +593,11 @@ typedef struct sg_af_report {
  * anisotropic sampler, then each step is a tensor-core forward and backward
  * pass over one batch and an Adam update of the fp32 masters. */
 int32_t sg_af_model_train(sg_device* dev, sg_af_model* model, const sg_af_train_desc* desc, sg_af_report* report);
+
+/* Registers a user shader module on the device (see sg_shader_module) and
+ * returns its program id; the module must outlive the device.  The same
+ * module registered twice gets the same id. */
+int32_t sg_shader_register(sg_device* dev, const sg_shader_module* module, uint32_t* out_program);
 
 /* renderer::clear_color (renderer.h:124). */
 int32_t sg_clear_color(sg_device* dev, uint32_t texture, const float rgba[4]);

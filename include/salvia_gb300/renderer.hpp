@@ -739,6 +739,26 @@ private:
   uint32_t filter_;
   float thr_, max_, min_;
 };
+// A user pixel or blend shader (a registered module's program id); its
+// constants and sampler are declared by a subclass as for any cpp shader.
+class module_pixel_shader : public cpp_pixel_shader {
+public:
+  explicit module_pixel_shader(uint32_t program_id) : prog_(program_id) {}
+  uint32_t program() const override { return prog_; }
+  SALVIA_GB300_CLONE(module_pixel_shader)
+
+private:
+  uint32_t prog_;
+};
+class module_blend_shader : public cpp_blend_shader {
+public:
+  explicit module_blend_shader(uint32_t program_id) : prog_(program_id) {}
+  uint32_t program() const override { return prog_; }
+  SALVIA_GB300_CLONE(module_blend_shader)
+
+private:
+  uint32_t prog_;
+};
 class replace_blend_shader : public cpp_blend_shader {  // color(0, s) = src
 public:
   uint32_t program() const override { return SG_BS_REPLACE; }
@@ -874,6 +894,14 @@ public:
     sg_af_model* m = nullptr;
     if (sg_af_model_create(dev_->dev, seed, &m) != SG_OK) return nullptr;
     return std::make_shared<learned_filter>(dev_, m);
+  }
+  // No counterpart in the reference: makes a user shader module
+  // (salvia_gb300/device_shader.cuh) a program of this renderer's device; a
+  // cpp_pixel_shader / cpp_blend_shader subclass returns the id from
+  // program() (module_pixel_shader / module_blend_shader do).  0 on failure.
+  uint32_t register_shader(sg_shader_module const* m) {
+    uint32_t id = 0;
+    return sg_shader_register(dev_->dev, m, &id) == SG_OK ? id : 0u;
   }
   // Cube maps are not on this path (renderer.h:49): no texture.
   texture_ptr create_texcube(size_t, size_t, size_t, pixel_format) { return nullptr; }

@@ -114,7 +114,57 @@ public:
   ref_ps(sg_shader const& p, sampler_ptr const& s) : prog(p), samp(s) {}
 
   uint32_t nattr = 0;
+  sg_shader_module const* user = nullptr;  // a user pixel shader's module
+
+  // the reference's own cpp_pixel_shader helpers, for a user body's host io
+  static void put(vec4 const& v, float out[4]) {
+    for (int k = 0; k < 4; ++k) out[k] = v[k];
+  }
+  static void io_ddx(void* b, uint32_t reg, float out[4]) { put(static_cast<ref_ps*>(b)->ddx(reg), out); }
+  static void io_ddy(void* b, uint32_t reg, float out[4]) { put(static_cast<ref_ps*>(b)->ddy(reg), out); }
+  static void io_tex2d(void* b, uint32_t reg, float out[4]) {
+    auto* p = static_cast<ref_ps*>(b);
+    put(p->tex2d(*p->samp, reg).get_vec4(), out);
+  }
+  static void io_tex2dlod(void* b, uint32_t reg, float out[4]) {
+    auto* p = static_cast<ref_ps*>(b);
+    put(p->tex2dlod(*p->samp, reg).get_vec4(), out);
+  }
+  static void io_tex2dproj(void* b, uint32_t reg, float out[4]) {
+    auto* p = static_cast<ref_ps*>(b);
+    put(p->tex2dproj(*p->samp, reg).get_vec4(), out);
+  }
+  static void io_sample(void* b, float u, float v, float lod, float out[4]) {
+    put(static_cast<ref_ps*>(b)->samp->sample(u, v, lod).get_vec4(), out);
+  }
+  static void io_sample_grad(void* b, float u, float v, float dxu, float dxv, float dyu, float dyv, float out[4]) {
+    put(static_cast<ref_ps*>(b)->samp->sample_2d_grad(vec2(u, v), vec2(dxu, dxv), vec2(dyu, dyv), 0.0f).get_vec4(),
+        out);
+  }
+  bool run_user(vs_output const& in, ps_output& out) {
+    sg_host_ps_io io{};
+    for (uint32_t a = 0; a < SG_MAX_VARYINGS && a < nattr; ++a)
+      for (int k = 0; k < 4; ++k) io.attr[a][k] = in.attribute(a)[k];
+    for (int k = 0; k < 4; ++k) io.position[k] = in.position()[k];
+    io.front_face = front_face() ? 1u : 0u;
+    io.num_varyings = nattr;
+    io.constants = prog.constants;
+    io.backend = this;
+    io.ddx = io_ddx;
+    io.ddy = io_ddy;
+    io.tex2d = io_tex2d;
+    io.tex2dlod = io_tex2dlod;
+    io.tex2dproj = io_tex2dproj;
+    io.sample = io_sample;
+    io.sample_grad = io_sample_grad;
+    bool const keep = user->host_ps(&io) != 0;
+    for (uint32_t i = 0; i < SG_MAX_COLOR_TARGETS; ++i)
+      out.color[i] = vec4(io.color[i][0], io.color[i][1], io.color[i][2], io.color[i][3]);
+    return keep;
+  }
+
   bool shader_prog(vs_output const& in, ps_output& out) override {
+    if (user) return run_user(in, out);
     switch (prog.program) {
     case SG_PS_COLOR: out.color[0] = in.attribute(0); return true;
     case SG_PS_COLOR_MRT:
@@ -154,8 +204,29 @@ class ref_bs : public cpp_blend_shader {
 public:
   uint32_t program;
   uint32_t ncolor = 1;
+  sg_shader_module const* user = nullptr;  // a user blend shader's module
+  float constants[SG_MAX_SHADER_CONSTANTS] = {};
   explicit ref_bs(uint32_t p) : program(p) {}
+  static void io_get(void* b, uint32_t t, uint32_t s, float out[4]) {
+    color_rgba32f c = static_cast<pixel_accessor*>(b)->color(t, s);
+    vec4 v = c.get_vec4();
+    for (int k = 0; k < 4; ++k) out[k] = v[k];
+  }
+  static void io_set(void* b, uint32_t t, uint32_t s, const float c[4]) {
+    static_cast<pixel_accessor*>(b)->color(t, s, color_rgba32f(c[0], c[1], c[2], c[3]));
+  }
   bool shader_prog(size_t sample, pixel_accessor& inout, ps_output const& in) override {
+    if (user) {  // the user body on the reference's pixel_accessor
+      sg_host_bs_io io{};
+      io.sample = static_cast<uint32_t>(sample);
+      for (uint32_t i = 0; i < SG_MAX_COLOR_TARGETS; ++i)
+        for (int k = 0; k < 4; ++k) io.in_color[i][k] = in.color[i][k];
+      io.constants = constants;
+      io.backend = &inout;
+      io.get = io_get;
+      io.set = io_set;
+      return user->host_bs(&io) != 0;
+    }
     switch (program) {
     case SG_BS_REPLACE_ALL:
       for (uint32_t i = 0; i < ncolor; ++i) inout.color(i, sample, color_rgba32f(in.color[i]));
@@ -186,9 +257,25 @@ struct sg_device {
   std::map<uint32_t, buffer_ptr> buffers;
   std::map<uint32_t, texture_ptr> textures;
   std::map<uint32_t, sampler_ptr> samplers;
+  std::vector<sg_shader_module const*> user_shaders;  // program SG_USER_PROGRAM_BASE + i
 };
 
 extern "C" {
+
+int32_t sg_shader_register(sg_device* d, const sg_shader_module* m, uint32_t* out) {
+  if (!d || !m || !out || m->abi_version != SG_SHADER_ABI_VERSION ||
+      (m->stage == SG_STAGE_PIXEL && !m->host_ps) || (m->stage == SG_STAGE_BLEND && !m->host_bs) ||
+      (m->stage != SG_STAGE_PIXEL && m->stage != SG_STAGE_BLEND))
+    return SG_INVALID_PARAMETER;
+  for (size_t i = 0; i < d->user_shaders.size(); ++i)
+    if (d->user_shaders[i] == m) {
+      *out = SG_USER_PROGRAM_BASE + static_cast<uint32_t>(i);
+      return SG_OK;
+    }
+  d->user_shaders.push_back(m);
+  *out = SG_USER_PROGRAM_BASE + static_cast<uint32_t>(d->user_shaders.size() - 1);
+  return SG_OK;
+}
 
 int32_t sg_device_create(int32_t, void*, sg_device** out) {
   auto* d = new sg_device();
@@ -365,6 +452,15 @@ int32_t sg_draw(sg_device* d, const sg_draw_desc* desc, sg_draw_stats* stats) {
       colors.push_back(d->textures[desc->more_color_targets[i]]->subresource(0));
   }
   ps->nattr = desc->num_varyings;
+  if (desc->ps.program >= SG_USER_PROGRAM_BASE) {
+    if (desc->ps.program - SG_USER_PROGRAM_BASE >= d->user_shaders.size()) return SG_INVALID_PARAMETER;
+    ps->user = d->user_shaders[desc->ps.program - SG_USER_PROGRAM_BASE];
+  }
+  if (desc->bs.program >= SG_USER_PROGRAM_BASE) {
+    if (desc->bs.program - SG_USER_PROGRAM_BASE >= d->user_shaders.size()) return SG_INVALID_PARAMETER;
+    bs->user = d->user_shaders[desc->bs.program - SG_USER_PROGRAM_BASE];
+    std::memcpy(bs->constants, desc->bs.constants, sizeof(bs->constants));
+  }
   bs->ncolor = static_cast<uint32_t>(std::max<size_t>(1, colors.size()));
   surface_ptr ds = desc->ds_target ? d->textures[desc->ds_target]->subresource(0) : surface_ptr();
   if (r->set_render_targets(colors.size(), colors.empty() ? nullptr : colors.data(), ds) != result::ok)

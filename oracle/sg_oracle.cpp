@@ -771,6 +771,7 @@ struct draw_ctx;
 
 // ---------------------------------------------------------------------------
 struct device_state {
+  std::vector<sg_shader_module const*> user_shaders;  // program SG_USER_PROGRAM_BASE + i
   uint32_t next = 1;
   std::map<uint32_t, std::vector<uint8_t>> buffers;
   std::map<uint32_t, std::unique_ptr<texture>> textures;
@@ -805,6 +806,7 @@ struct draw_ctx {
   sampler const* vs_samp = nullptr;
   sampler const* ps_samp = nullptr;
   sg_draw_stats stats{};
+  mutable bool front = false;  // the triangle being rasterised faces front (rasterizer.cpp:915)
 };
 
 // stream_assembler::fetch_vertex / get_vec4 (stream_assembler.cpp:26-93)
@@ -1219,8 +1221,40 @@ struct rasterizer_state {
 
 // cpp_blend_shader programs (shader.h:209-215)
 // `more`: the pixel's colours 1.. (SG_MAX_COLOR_TARGETS - 1 of them)
+struct user_bs_backend {
+  draw_ctx const* c;
+  size_t x, y;
+};
+surface* user_bs_target(user_bs_backend const& u, uint32_t t) {
+  return t == 0 ? u.c->color : t <= u.c->nmore ? u.c->more[t - 1] : nullptr;
+}
+void ubs_get(void* b, uint32_t t, uint32_t s, float out[4]) {
+  auto& u = *static_cast<user_bs_backend*>(b);
+  surface* sf = user_bs_target(u, t);
+  vec4 v = sf ? sf->get(u.x, u.y, s) : mk(0, 0, 0, 0);
+  for (int k = 0; k < 4; ++k) out[k] = v[k];
+}
+void ubs_set(void* b, uint32_t t, uint32_t s, const float c[4]) {
+  auto& u = *static_cast<user_bs_backend*>(b);
+  if (surface* sf = user_bs_target(u, t)) sf->set(u.x, u.y, s, mk(c[0], c[1], c[2], c[3]));
+}
 void blend(draw_ctx const& c, size_t x, size_t y, size_t s, vec4 const& src, vec4 const* more) {
   if (!c.color) return;
+  if (c.d->bs.program >= SG_USER_PROGRAM_BASE) {  // a user blend shader's host body
+    sg_shader_module const* m = c.dev->user_shaders[c.d->bs.program - SG_USER_PROGRAM_BASE];
+    user_bs_backend ub{&c, x, y};
+    sg_host_bs_io io{};
+    io.sample = static_cast<uint32_t>(s);
+    for (int k = 0; k < 4; ++k) io.in_color[0][k] = src[k];
+    for (uint32_t t = 0; t + 1 < SG_MAX_COLOR_TARGETS; ++t)
+      for (int k = 0; k < 4; ++k) io.in_color[t + 1][k] = more[t][k];
+    io.constants = c.d->bs.constants;
+    io.backend = &ub;
+    io.get = ubs_get;
+    io.set = ubs_set;
+    m->host_bs(&io);
+    return;
+  }
   switch (c.d->bs.program) {
   case SG_BS_REPLACE_ALL:  // color(i, s) = in.color[i] for every bound target
     c.color->set(x, y, s, src);
@@ -1308,6 +1342,83 @@ void render_sample_quad(rasterizer_state& rs, size_t x, size_t y, uint64_t mask,
   }
 }
 
+// A user pixel shader's host body on pixel i of a quad: its registers and
+// this restatement's cpp_pixel_shader helpers (cpp_pixel_shader.cpp:13-60).
+struct user_ps_backend {
+  draw_ctx const* c;
+  vso const* quad;
+  int i;
+};
+void ups_reg(vso const& v, uint32_t reg, float out[4]) {
+  for (int k = 0; k < 4; ++k) out[k] = v.r[1 + reg][k];
+}
+void ups_ddx(void* b, uint32_t reg, float out[4]) {
+  auto& u = *static_cast<user_ps_backend*>(b);
+  vec4 d = sub(u.quad[1].r[1 + reg], u.quad[0].r[1 + reg]);
+  for (int k = 0; k < 4; ++k) out[k] = d[k];
+}
+void ups_ddy(void* b, uint32_t reg, float out[4]) {
+  auto& u = *static_cast<user_ps_backend*>(b);
+  vec4 d = sub(u.quad[2].r[1 + reg], u.quad[0].r[1 + reg]);
+  for (int k = 0; k < 4; ++k) out[k] = d[k];
+}
+void ups_put(vec4 const& v, float out[4]) {
+  for (int k = 0; k < 4; ++k) out[k] = v[k];
+}
+void ups_tex2d(void* b, uint32_t reg, float out[4]) {
+  auto& u = *static_cast<user_ps_backend*>(b);
+  vec4 dx = sub(u.quad[1].r[1 + reg], u.quad[0].r[1 + reg]), dy = sub(u.quad[2].r[1 + reg], u.quad[0].r[1 + reg]);
+  float lod = calc_lod_2d(*u.c->ps_samp, dx[0], dx[1], dy[0], dy[1]);
+  vec4 const& a = u.quad[u.i].r[1 + reg];
+  ups_put(sample_impl(*u.c->ps_samp, a[0], a[1], lod, nullptr), out);
+}
+void ups_tex2dlod(void* b, uint32_t reg, float out[4]) {
+  auto& u = *static_cast<user_ps_backend*>(b);
+  vec4 const& a = u.quad[u.i].r[1 + reg];
+  ups_put(sample_impl(*u.c->ps_samp, a[0], a[1], a[3], nullptr), out);
+}
+void ups_tex2dproj(void* b, uint32_t reg, float out[4]) {
+  auto& u = *static_cast<user_ps_backend*>(b);
+  vec4 const& a = u.quad[u.i].r[1 + reg];
+  vec4 nx = add(a, sub(u.quad[1].r[1 + reg], u.quad[0].r[1 + reg]));
+  vec4 ny = add(a, sub(u.quad[2].r[1 + reg], u.quad[0].r[1 + reg]));
+  auto proj = [](vec4 const& v, int k) { return (v[k] / v[3] + 1.0f) * 0.5f; };
+  float px = proj(a, 0), py = proj(a, 1);
+  ups_put(sample_2d_grad(*u.c->ps_samp, px, py, proj(nx, 0) - px, proj(nx, 1) - py, proj(ny, 0) - px,
+                         proj(ny, 1) - py, 0.0f),
+          out);
+}
+void ups_sample(void* b, float u_, float v, float lod, float out[4]) {
+  ups_put(sample_impl(*static_cast<user_ps_backend*>(b)->c->ps_samp, u_, v, lod, nullptr), out);
+}
+void ups_sample_grad(void* b, float u_, float v, float dxu, float dxv, float dyu, float dyv, float out[4]) {
+  ups_put(sample_2d_grad(*static_cast<user_ps_backend*>(b)->c->ps_samp, u_, v, dxu, dxv, dyu, dyv, 0.0f), out);
+}
+bool run_user_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, vec4* more) {
+  sg_shader_module const* m = c.dev->user_shaders[c.d->ps.program - SG_USER_PROGRAM_BASE];
+  user_ps_backend ub{&c, quad, i};
+  sg_host_ps_io io{};
+  for (uint32_t a = 0; a < SG_MAX_VARYINGS; ++a)
+    if (a < c.nattr) ups_reg(quad[i], a, io.attr[a]);
+  for (int k = 0; k < 4; ++k) io.position[k] = quad[i].r[0][k];
+  io.front_face = c.front ? 1u : 0u;
+  io.num_varyings = c.nattr;
+  io.constants = c.d->ps.constants;
+  io.backend = &ub;
+  io.ddx = ups_ddx;
+  io.ddy = ups_ddy;
+  io.tex2d = ups_tex2d;
+  io.tex2dlod = ups_tex2dlod;
+  io.tex2dproj = ups_tex2dproj;
+  io.sample = ups_sample;
+  io.sample_grad = ups_sample_grad;
+  bool const keep = m->host_ps(&io) != 0;
+  out = mk(io.color[0][0], io.color[0][1], io.color[0][2], io.color[0][3]);
+  for (uint32_t k = 0; k + 1 < SG_MAX_COLOR_TARGETS; ++k)
+    more[k] = mk(io.color[k + 1][0], io.color[k + 1][1], io.color[k + 1][2], io.color[k + 1][3]);
+  return keep;
+}
+
 // cpp_pixel_shader programs; tex2d's LOD is computed once per quad from
 // the quad's attribute differences (cpp_pixel_shader.cpp:13-31).
 // `more` receives out.color[1..] (zero unless the program writes them).
@@ -1315,6 +1426,7 @@ bool run_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, vec4* more, fl
   sg_shader const& s = c.d->ps;
   vso const& in = quad[i];
   for (uint32_t k = 0; k + 1 < SG_MAX_COLOR_TARGETS; ++k) more[k] = mk(0, 0, 0, 0);
+  if (s.program >= SG_USER_PROGRAM_BASE) return run_user_ps(c, quad, i, out, more);
   switch (s.program) {
   case SG_PS_COLOR: out = in.r[1]; return true;
   case SG_PS_COLOR_MRT:  // out.color[k] = in.attr[k]
@@ -1494,6 +1606,7 @@ void draw_quad(rasterizer_state& rs, tri_info const& ti, uint32_t left, uint32_t
   rs.st->ps_invocations += 4;
   vec4 col[4];
   vec4 colm[4][SG_MAX_COLOR_TARGETS - 1];
+  c.front = ti.front;  // cpp_pixel_shader::update_front_face (rasterizer.cpp:692)
   tested &= execute_ps(c, px, col, colm);
   if (full && tested == 0) return;  // draw_full_quad checks the PS-masked value
   rs.st->backend_input_pixels += 4;
@@ -1957,6 +2070,22 @@ int32_t sg_resolve(sg_device* d, uint32_t src, uint32_t dst) {
       for (uint32_t s = 0; s < a->samples; ++s) c = add(c, a->get(x, y, s));
       b->set(x, y, 0, mul(c, inv));
     }
+  return SG_OK;
+}
+
+int32_t sg_shader_register(sg_device* d, const sg_shader_module* m, uint32_t* out) {
+  if (!d || !m || !out || m->abi_version != SG_SHADER_ABI_VERSION ||
+      (m->stage == SG_STAGE_PIXEL && !m->host_ps) || (m->stage == SG_STAGE_BLEND && !m->host_bs) ||
+      (m->stage != SG_STAGE_PIXEL && m->stage != SG_STAGE_BLEND))
+    return SG_INVALID_PARAMETER;
+  auto& v = d->st.user_shaders;
+  for (size_t i = 0; i < v.size(); ++i)
+    if (v[i] == m) {
+      *out = SG_USER_PROGRAM_BASE + static_cast<uint32_t>(i);
+      return SG_OK;
+    }
+  v.push_back(m);
+  *out = SG_USER_PROGRAM_BASE + static_cast<uint32_t>(v.size() - 1);
   return SG_OK;
 }
 

@@ -178,6 +178,7 @@ SIGNATURES = {
     "sg_sampler_create": (C.c_int32, [C.c_void_p, C.POINTER(SamplerDesc), C.c_uint32, _u32p]),
     "sg_sampler_destroy": (C.c_int32, [C.c_void_p, C.c_uint32]),
     "sg_draw": (C.c_int32, [C.c_void_p, C.POINTER(DrawDesc), C.POINTER(DrawStats)]),
+    "sg_shader_register": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32)]),
     "sg_draw_static_scratch": (C.c_int32, [C.c_void_p, C.POINTER(DrawDesc), C.POINTER(DrawStats)]),
     "sg_clear_color": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(C.c_float)]),
     "sg_clear_depth_stencil": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,

@@ -180,6 +180,8 @@ struct PassPlan {
   std::set<uint32_t> cleared;                // textures its queued clears write
   std::vector<uint8_t> late_z;               // per target: a draw tests depth after shading
   uint32_t more_colors = 0;                  // most colour targets after the first of any of its targets
+  std::vector<sg_shader_module const*> user_ps;  // its user pixel shaders: shade key USER_CLASS * 8 + index
+  sg_shader_module const* user_bs = nullptr;     // its user blend shader (the merge runs that module's kernel)
   std::set<uint32_t> af_textures;            // textures its learned-filter draws take feature taps from
   uint64_t nprims = 0;
   uint64_t samples = 0;                      // target samples of the pass's targets
@@ -290,6 +292,7 @@ struct sg_device {
   int32_t pending = 0;                    // an error of earlier work, reported at the next sg_sync
   std::set<sg_graph*> graphs;
   std::map<uint32_t, AfModelDev> af_models;  // learned filters by id
+  std::vector<sg_shader_module const*> user_shaders;  // program SG_USER_PROGRAM_BASE + i
   sg_tuning tuning = default_tuning();
   std::string error;
   // profiling: event pairs per stage, summed at sg_profile_read
@@ -478,6 +481,11 @@ void stage_end(sg_device* d, int stage, cudaEvent_t b) {
 // ---------------------------------------------------------------------------
 // draw translation (renderer_impl state -> DrawParams)
 
+// The shade class of user pixel shaders' fragments: key USER_SHADE_CLASS * 8
+// + the shader's index in its pass (the stock classes are the varying
+// counts, plus 8 for the learned filter's draws).
+constexpr uint32_t USER_SHADE_CLASS = 14;
+
 struct DrawInfo {
   uint32_t color = 0, ds = 0;       // target textures: colour target 0, depth-stencil
   uint32_t more[SG_MAX_COLOR_TARGETS - 1] = {};  // colour targets 1.. (0 = none)
@@ -489,6 +497,8 @@ struct DrawInfo {
     return k;
   }
   uint32_t tex[2] = {0, 0};         // sampled textures
+  sg_shader_module const* user_ps = nullptr;  // a user pixel shader's module
+  sg_shader_module const* user_bs = nullptr;  // a user blend shader's module
   uint32_t af_model = 0;            // learned filter of an SG_PS_TEX_GRAD_LEARNED draw
   uint32_t af_texture = 0;          // the texture its feature taps read
 };
@@ -568,13 +578,23 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   p.bs_prog = desc->bs.program;
   std::memcpy(p.vs_k, desc->vs.constants, sizeof(p.vs_k));
   std::memcpy(p.ps_k, desc->ps.constants, sizeof(p.ps_k));
+  std::memcpy(p.bs_k, desc->bs.constants, sizeof(p.bs_k));
   if (int32_t r = build_sampler(d, desc->vs.samplers[0], p.vs_samp, &info.tex[0])) return r;
   if (int32_t r = build_sampler(d, desc->ps.samplers[0], p.ps_samp, &info.tex[1])) return r;
   if (p.vs_prog == SG_VS_MORPH_DISPLACE && !desc->vs.samplers[0]) return SG_INVALID_PARAMETER;
-  if (p.vs_prog < SG_VS_TRANSFORM || p.vs_prog > SG_VS_MORPH_DISPLACE || p.ps_prog < SG_PS_COLOR ||
-      p.ps_prog > SG_PS_COLOR_MRT || p.bs_prog < SG_BS_REPLACE || p.bs_prog > SG_BS_REPLACE_ALL)
+  // user programs: registered modules of the stage
+  auto user_module = [&](uint32_t prog, uint32_t stage) -> sg_shader_module const* {
+    if (prog < SG_USER_PROGRAM_BASE || prog - SG_USER_PROGRAM_BASE >= d->user_shaders.size()) return nullptr;
+    sg_shader_module const* m = d->user_shaders[prog - SG_USER_PROGRAM_BASE];
+    return m->stage == stage ? m : nullptr;
+  };
+  info.user_ps = user_module(p.ps_prog, SG_STAGE_PIXEL);
+  info.user_bs = user_module(p.bs_prog, SG_STAGE_BLEND);
+  if (p.vs_prog < SG_VS_TRANSFORM || p.vs_prog > SG_VS_MORPH_DISPLACE ||
+      ((p.ps_prog < SG_PS_COLOR || p.ps_prog > SG_PS_COLOR_MRT) && !info.user_ps) ||
+      ((p.bs_prog < SG_BS_REPLACE || p.bs_prog > SG_BS_REPLACE_ALL) && !info.user_bs))
     return SG_INVALID_PARAMETER;
-  if (p.ps_prog != SG_PS_COLOR && p.ps_prog != SG_PS_CONSTANT && p.ps_prog != SG_PS_COLOR_MRT &&
+  if (p.ps_prog != SG_PS_COLOR && p.ps_prog != SG_PS_CONSTANT && p.ps_prog != SG_PS_COLOR_MRT && !info.user_ps &&
       !desc->ps.samplers[0])
     return SG_INVALID_PARAMETER;
   if (p.ps_prog == SG_PS_TEX_GRAD_LEARNED) {
@@ -589,6 +609,7 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   // result is zero either way and the plain instance shades them
   p.shade_class = nattr + ((p.ps_prog == SG_PS_TEX_GRAD_LEARNED && nattr >= 2) ? 8u : 0u);
   p.shade_key = p.shade_class * 8u + (p.ps_prog & 7u);
+  if (info.user_ps) p.shade_class = USER_SHADE_CLASS;  // its key: set by the pass (add_draw)
   p.rec_stride = rec_stride_for(static_cast<int>(nattr));
   for (uint32_t i = 0; i < SG_MAX_VARYINGS; ++i) {
     p.mods[i] = desc->varying_modifiers[i];
@@ -694,6 +715,10 @@ bool draw_fits(sg_device* d, PassPlan const& pl, DrawParams const& p, DrawInfo c
     if (pl.sampled.count(s) || pl.resolved.count(s)) return false;
   }
   if (info.af_model && pl.af_model && info.af_model != pl.af_model) return false;
+  if (info.user_bs && pl.user_bs && info.user_bs != pl.user_bs) return false;  // one user merge per pass
+  if (info.user_ps && pl.user_ps.size() >= 8 &&
+      std::find(pl.user_ps.begin(), pl.user_ps.end(), info.user_ps) == pl.user_ps.end())
+    return false;
   auto it = pl.target_of.find(key);
   if (it == pl.target_of.end()) {
     // a new target may not share a surface with an existing one
@@ -733,6 +758,13 @@ void add_draw(sg_device* d, PassPlan& pl, DrawParams p, DrawInfo const& info, ui
     pl.af = d->af_models.at(info.af_model);
     pl.af_textures.insert(info.af_texture);
   }
+  if (info.user_ps) {
+    auto u = std::find(pl.user_ps.begin(), pl.user_ps.end(), info.user_ps);
+    uint32_t const slot = static_cast<uint32_t>(u - pl.user_ps.begin());
+    if (u == pl.user_ps.end()) pl.user_ps.push_back(info.user_ps);
+    p.shade_key = USER_SHADE_CLASS * 8u + slot;
+  }
+  if (info.user_bs) pl.user_bs = info.user_bs;
   p.prim_base = static_cast<uint32_t>(pl.nprims);
   pl.nprims += p.prim_count;
   pl.draws.push_back(p);
@@ -754,7 +786,7 @@ void finalize(PassPlan& pl, sg_device* d) {
     T.tiles_y = std::max(T.tiles_y, p.tiles_y);
     slots[p.target] += 3ull * p.prim_count;
     if ((p.zcfg & 128u) && T.ds) T.any_early_z = 1;
-    pl.na_mask |= 1u << p.shade_class;
+    if (p.shade_class != USER_SHADE_CLASS) pl.na_mask |= 1u << p.shade_class;
     pl.rec_units += 3ull * p.prim_count * p.rec_stride;
   }
   // slot ranges: targets in order, each target's draws in API order
@@ -1069,6 +1101,10 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
         }
         ++k;
       }
+      for (uint32_t u = 0; u < pl.user_ps.size(); ++u) {  // user pixel shaders, one launch each
+        pl.user_ps[u]->device_launch(&P, USER_SHADE_CLASS * 8u + u, shade_grid, s);
+        ++k;
+      }
       if (pl.af_model && P.af_capacity) {
         launch_af_pass(P, pl.af, sms, s);
         k += 2;
@@ -1080,7 +1116,10 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
         launch_cover_rollback(P, std::min<uint32_t>(pl.ntiles, sms * 8), s);
         ++k;
       }
-      launch_merge(P, merge_grid, s);
+      if (pl.user_bs)  // the merge with the pass's user blend shader
+        pl.user_bs->device_launch(&P, 0u, merge_grid, s);
+      else
+        launch_merge(P, merge_grid, s);
       stage_end(d, 4, ev);
       k += P.tile_order ? 11 : 9;  // geometry, bin count, 3 scans, tile ranges (+ 2 order), bin fill, cover, merge
       d->prof.raster_launches += 1;
@@ -1836,6 +1875,35 @@ int32_t sg_draw_static_scratch(sg_device* d, const sg_draw_desc* desc, sg_draw_s
   c.type = SG_CMD_DRAW;
   c.draw = desc;
   return submit_impl(d, &c, 1, stats, d->static_base);
+}
+
+int32_t sg_shader_register(sg_device* d, const sg_shader_module* m, uint32_t* out) {
+  if (!d || !m || !out) return SG_INVALID_PARAMETER;
+  if (m->abi_version != SG_SHADER_ABI_VERSION || !m->device_init || !m->device_launch ||
+      (m->stage != SG_STAGE_PIXEL && m->stage != SG_STAGE_BLEND))
+    return SG_INVALID_PARAMETER;
+  for (size_t i = 0; i < d->user_shaders.size(); ++i)
+    if (d->user_shaders[i] == m) {
+      *out = SG_USER_PROGRAM_BASE + static_cast<uint32_t>(i);
+      return SG_OK;
+    }
+  if (d->user_shaders.size() >= 255u - SG_USER_PROGRAM_BASE) return SG_OUT_OF_MEMORY;
+  // the module's kernels on this device: its own copy of the sampler's EWA table
+  int cur = -1;
+  SG_CUDA(d, cudaGetDevice(&cur));
+  if (cur != d->ordinal) SG_CUDA(d, cudaSetDevice(d->ordinal));
+  float tab[256];
+  make_ewa_table(tab);
+  int32_t const r = m->device_init(tab, d->stream);
+  cudaError_t const e = cudaStreamSynchronize(d->stream);
+  if (cur != d->ordinal) cudaSetDevice(cur);
+  if (r != 0 || e != cudaSuccess) {
+    d->error = std::string("sg_shader_register: the module's device set-up failed (") + (m->name ? m->name : "") + ")";
+    return SG_CUDA_ERROR;
+  }
+  d->user_shaders.push_back(m);
+  *out = SG_USER_PROGRAM_BASE + static_cast<uint32_t>(d->user_shaders.size() - 1);
+  return SG_OK;
 }
 
 int32_t sg_submit(sg_device* d, const sg_command* cmds, uint32_t n, sg_draw_stats* stats) {

@@ -105,7 +105,8 @@ struct DrawParams {
   // shaders
   uint32_t vs_prog, ps_prog, bs_prog;
   float vs_k[SG_MAX_SHADER_CONSTANTS];
-  float ps_k[4];
+  float ps_k[SG_MAX_SHADER_CONSTANTS];
+  float bs_k[SG_MAX_SHADER_CONSTANTS];
   dev_sampler vs_samp, ps_samp;
   uint32_t mods[SG_MAX_VARYINGS];
   uint32_t has_centroid;

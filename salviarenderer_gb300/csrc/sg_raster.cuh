@@ -26,6 +26,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "sg_draw.cuh"
 #include "sg_learned.cuh"
 
@@ -189,11 +191,30 @@ __device__ inline uint32_t blend_word(uint32_t fmt, uint32_t bs_prog, uint32_t d
   }
 }
 
+// A user blend shader's body on one sample (defined with the user shader
+// kernels, sg_user.cuh).
+template <class UBS>
+__device__ void user_blend(TargetParams const& T, DrawParams const& D, uint32_t x, uint32_t y, uint32_t s, v4 src,
+                           float4 const* more);
+// The draw's blend program: a stock one, or UBS's body for a user program.
+template <class UBS>
+__device__ inline void blend_t(TargetParams const& T, DrawParams const& D, uint32_t x, uint32_t y, uint32_t s, v4 src,
+                               float4 const* more) {
+  if constexpr (!std::is_void<UBS>::value) {
+    if (D.bs_prog >= SG_USER_PROGRAM_BASE) {
+      user_blend<UBS>(T, D, x, y, s, src, more);
+      return;
+    }
+  }
+  blend(T, D, x, y, s, src, more);
+}
+
 // framebuffer::render_sample (framebuffer.cpp:445-479)
+template <class UBS = void>
 __device__ inline void render_sample(TargetParams const& T, DrawParams const& D, uint32_t x, uint32_t y, uint32_t s,
                                      v4 src, float depth, bool front, float4 const* more) {
   if (D.early_z || !T.ds) {
-    blend(T, D, x, y, s, src, more);
+    blend_t<UBS>(T, D, x, y, s, src, more);
     return;
   }
   uint8_t* a = ds_addr(T, x, y, s);
@@ -203,7 +224,7 @@ __device__ inline void render_sample(TargetParams const& T, DrawParams const& D,
   bool sp = D.stencil ? cmpu(func, D.stencil_ref, old.stencil) : true;
   if (dp && sp) {
     uint32_t ns = D.stencil ? stencil_op(front ? D.front_pass : D.back_pass, D.stencil_ref, old.stencil) : 0u;
-    blend(T, D, x, y, s, src, more);
+    blend_t<UBS>(T, D, x, y, s, src, more);
     ds_write(T, D, a, depth, ns, D.write_mask);
   }
 }
@@ -939,12 +960,13 @@ __global__ void __launch_bounds__(256, MINB) k_shade(PassParams P) {
   }
 }
 
-#ifdef SG_RASTER_COVER_MERGE
 // Output merging: owners replay their fragments in primitive order
 // (framebuffer::render_sample_quad, framebuffer.cpp:481-520).
 // Work is handed out per warp -- 32 owners of a tile at a time, from a
 // device-wide cursor -- so tiles of very different cost spread over the SMs.
-__global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
+// UBS: a user blend shader the pass's user-blend draws run (void: none).
+template <class UBS>
+__device__ __forceinline__ void merge_pass(PassParams const& P) {
   if (pass_gated(P)) return;
   uint32_t const ovf = P.counters->overflow;  // final: geometry, binning, coverage and shading are done
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1031,7 +1053,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
           }
         }
         if ((D.early_z || !T.ds) && T.color && T.color_esz == 4 && T.samples == 4 &&
-            (T.nmore == 0 || D.bs_prog != SG_BS_REPLACE_ALL)) {
+            (T.nmore == 0 || D.bs_prog != SG_BS_REPLACE_ALL) && D.bs_prog < SG_USER_PROGRAM_BASE) {
           // colour only, four 4-byte samples per pixel: each covered pixel's
           // samples are read, blended and written as one 16-byte word
           uint4 w[4];
@@ -1074,10 +1096,10 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
               P.frag_color_more ? P.frag_color_more + (static_cast<size_t>(f) * 4 + i) * P.more_colors : nullptr;
           uint32_t x = qx + (i & 1), y = qy + (i >> 1);
           if (T.samples == 1) {
-            render_sample(T, D, x, y, 0, src, depth[i], front, more);
+            render_sample<UBS>(T, D, x, y, 0, src, depth[i], front, more);
           } else {
             for (uint32_t s = 0; s < T.samples; ++s)
-              if (pm & (1u << s)) render_sample(T, D, x, y, s, src, depth[i] + aa[s], front, more);
+              if (pm & (1u << s)) render_sample<UBS>(T, D, x, y, s, src, depth[i] + aa[s], front, more);
           }
         }
       }
@@ -1085,6 +1107,9 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) {
   }
   if (backend) atomicAdd(&P.draw_stats[cur_draw].backend_input_pixels, backend);
 }
+
+#ifdef SG_RASTER_COVER_MERGE
+__global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) { merge_pass<void>(P); }
 
 #endif  // SG_RASTER_COVER_MERGE
 

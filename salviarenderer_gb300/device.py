@@ -135,6 +135,14 @@ class Device:
         return h.value
 
     # -- commands ------------------------------------------------------------
+    def register_shader(self, module):
+        """sg_shader_register: a user shader module (a pointer returned by its
+        salvia_gb300_module_<name>() export) becomes a program id."""
+        pid = C.c_uint32()
+        self._check("sg_shader_register", self.lib.sg_shader_register(self.handle, C.c_void_p(module),
+                                                                        C.byref(pid)))
+        return pid.value
+
     def draw(self, desc, stats=False):
         st = abi.DrawStats() if stats else None
         self._check("sg_draw", self.lib.sg_draw(self.handle, C.byref(desc),

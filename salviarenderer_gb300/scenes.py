@@ -107,6 +107,26 @@ class Scene:
         return sum(d["prim_count"] for d in self.draws)
 
 
+# User shader modules (salvia_gb300/device_shader.cuh) by class name, from a
+# shared object built from the application's shader source; a scene names
+# such a program as "user:<class>".
+_USER_SHADER_LIBRARY = None
+
+
+def set_user_shader_library(path):
+    """Loads the shared object that exports salvia_gb300_module_<class>()."""
+    global _USER_SHADER_LIBRARY
+    import ctypes
+    _USER_SHADER_LIBRARY = ctypes.CDLL(path)
+
+
+def user_shader_module(name):
+    fn = getattr(_USER_SHADER_LIBRARY, "salvia_gb300_module_" + name)
+    import ctypes
+    fn.restype = ctypes.c_void_p
+    return fn()
+
+
 class Bound:
     """Device handles of a scene's resources on one backend."""
 
@@ -133,6 +153,8 @@ class Bound:
 
     def _shader(self, spec):
         spec = dict(spec)
+        if isinstance(spec.get("program"), str):  # "user:<class>": a registered user shader module
+            spec["program"] = self.dev.register_shader(user_shader_module(spec["program"].split(":", 1)[1]))
         spec["samplers"] = [self.samp[n] for n in spec.get("samplers", ())]
         if spec.get("learned_filter") == "model":
             # the CPU oracle renders learned-filter draws with the plain sampler
@@ -502,7 +524,8 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
                   depth_func=abi.CMP_LESS, depth_write=1, depth_enable=1, blend=abi.BS_REPLACE,
                   ps=abi.PS_COLOR, sampler=None, modifiers=(abi.AM_LINEAR, abi.AM_LINEAR),
                   color_fmt=abi.FMT_RGBA8, ds_fmt=abi.FMT_RG32F, tex_size=64, uv_scale=3.0,
-                  eye_dist=(2.2, 3.2), draws=1, clear_depth=1.0, uv_w=None, ps_constants=None, stencil=None):
+                  eye_dist=(2.2, 3.2), draws=1, clear_depth=1.0, uv_w=None, ps_constants=None, stencil=None,
+                  bs_constants=None):
     """A small scene that exercises one combination of pipeline state.
 
     Vertices carry position, a (u, v) pair and an RGBA colour.  Strips and
@@ -535,7 +558,7 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
     if index_format is not None:
         idx = rng.integers(0, npool, size=nv)
         s.buffers["ib"] = idx.astype(np.uint16 if index_format == abi.INDEX_U16 else np.uint32)
-    if ps in abi.TEXTURED_PS:
+    if ps in abi.TEXTURED_PS or isinstance(ps, str):  # user pixel shaders sample slot 0
         s.textures["tex"] = (to_rgba8(value_noise(rng, tex_size, octaves=4)), True)
         s.samplers["s0"] = ("tex", dict(sampler or {}))
     dsd = default_depth_stencil(depth_func=depth_func, depth_enable=depth_enable,
@@ -559,7 +582,7 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
                   vs=dict(program=abi.VS_TRANSFORM, constants=mvp),
                   ps=dict(program=ps, samplers=["s0"] if "s0" in s.samplers else [],
                           constants=list(ps_constants or [])),
-                  bs=dict(program=blend))
+                  bs=dict(program=blend, constants=list(bs_constants or [])))
         if index_format is not None:
             dd.update(index_buffer="ib", index_format=index_format,
                       start=first * (3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else 1))

@@ -35,6 +35,26 @@ def oracle_lib():
     return abi.bind(ctypes.CDLL(ORACLE_LIB))
 
 
+def build_user_shaders(out_dir):
+    """Compiles tests/cpp/user_shaders.cu (user shader bodies written against
+    salvia_gb300/device_shader.cuh) into a shader-module shared object and
+    makes it the scenes' user shader library."""
+    from salviarenderer_gb300 import build as pbuild, scenes
+    out = os.path.join(out_dir, "libuser_shaders.so")
+    cmd = [pbuild.nvcc()] + pbuild.ARCH + [
+        "-O3", "-std=c++17", "-fmad=false", "-Xcompiler", "-ffp-contract=off", "-shared", "-Xcompiler", "-fPIC",
+        "-cudart", "shared", "-I" + os.path.join(ROOT, "include"), "-I" + pbuild.CSRC,
+        os.path.join(ROOT, "tests", "cpp", "user_shaders.cu"), "-o", out]
+    subprocess.run(cmd, check=True)
+    scenes.set_user_shader_library(out)
+    return out
+
+
+@pytest.fixture(scope="session")
+def user_shader_lib(tmp_path_factory):
+    return build_user_shaders(str(tmp_path_factory.mktemp("user_shaders")))
+
+
 @pytest.fixture(scope="session")
 def product_lib():
     from salviarenderer_gb300 import build as pbuild

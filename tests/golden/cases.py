@@ -90,6 +90,18 @@ CASES = {
     "mrt_4x_5_targets": lambda: scenes.mrt_scene(seed=61, samples=4, ntris=80,
                                                  more=((abi.FMT_RGBA8, 96, 80), (abi.FMT_RGBA32F, 96, 80),
                                                        (abi.FMT_RGBA8, 100, 90), (abi.FMT_BGRA8, 96, 80))),
+    # user shader bodies (tests/cpp/user_shaders.cu, salvia_gb300/device_shader.cuh):
+    # a tinted alpha-tested lookup using ddx / ddy and a "screen" blend,
+    # with early and late depth; a front-face switch between tex2dproj and tex2dlod
+    "user_ps_bs_early_z": lambda: F(seed=70, ps="user:tinted_alpha_test_ps", sampler=TRILINEAR, ntris=160,
+                                    ps_constants=[0.9, 0.6, 0.3, 0.7, 40.0, 0.45],
+                                    blend="user:screen_blend_bs", bs_constants=[0.8]),
+    "user_ps_bs_4x_late_z": lambda: F(seed=71, ps="user:tinted_alpha_test_ps", sampler=TRILINEAR, samples=4,
+                                      ps_constants=[0.2, 0.9, 0.5, 0.5, 10.0, 0.4], ntris=140,
+                                      stencil=(abi.CMP_ALWAYS, abi.SOP_INCR_WRAP, 0),
+                                      blend="user:screen_blend_bs", bs_constants=[0.6]),
+    "user_ps_front_proj_back_lod": lambda: F(seed=72, ps="user:proj_or_lod_ps", sampler=TRILINEAR,
+                                             uv_w=(0.5, 2.0), blend=abi.BS_LERP_SRC_ALPHA),
     # C2 pattern (textured grid, trilinear + 16x AF, src-alpha blend)
     "c2_160x96_4x": lambda: scenes.c2_scene(width=160, height=96, grid=33, tex_size=128, ndraws=4),
     "c2_128x72_1x": lambda: scenes.c2_scene(width=128, height=72, grid=25, tex_size=64, samples=1,

@@ -82,6 +82,9 @@ def full_size(dev):
 def main():
     lib = abi.bind(ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libsalvia_ref.so")))
     dev = Device(lib)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from conftest import build_user_shaders  # the user shader cases' module, on the reference's host side
+    build_user_shaders(os.path.join(ROOT, "oracle", "_ref"))
     if "--full-size" in sys.argv[1:]:
         full_size(dev)
         return

@@ -24,7 +24,7 @@ def gdev():
 
 
 @pytest.fixture(scope="module")
-def odev(oracle_lib):
+def odev(oracle_lib, user_shader_lib):
     return Device(oracle_lib)
 
 

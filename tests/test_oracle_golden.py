@@ -20,7 +20,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 @pytest.fixture(scope="module")
-def odev(oracle_lib):
+def odev(oracle_lib, user_shader_lib):
     return Device(oracle_lib)
 
 
