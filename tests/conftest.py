@@ -50,7 +50,7 @@ def build_user_shaders(out_dir):
     return out
 
 
-@pytest.fixture(scope="session")
+@pytest.fixture(scope="session", autouse=True)
 def user_shader_lib(tmp_path_factory):
     return build_user_shaders(str(tmp_path_factory.mktemp("user_shaders")))
 
