@@ -151,7 +151,12 @@ enum {
   SG_PS_TEX_ALPHA_TEST = 8,
   /* out.color[i] = in.attr[i] for every varying i (one colour per bound
    * target); colours a program does not write are zero. */
-  SG_PS_COLOR_MRT = 9
+  SG_PS_COLOR_MRT = 9,
+  /* out.color[0] = sampler0.sample_cube(attr[0].x, attr[0].y, attr[0].z,
+   * attr[0].w) * in.attr[1]: the direction's major axis picks the face
+   * (sampler.cpp:771-829).  The reference declares the texcube helpers
+   * (shader.h:187-198) but defines none, so the program calls the sampler. */
+  SG_PS_TEXCUBE_MODULATE = 10
 };
 enum {
   SG_BS_REPLACE = 1,        /* color(0, s) = in.color[0] */
@@ -198,6 +203,7 @@ typedef struct sg_host_ps_io {
   void (*sample)(void* backend, float u, float v, float lod, float out[4]);  /* sampler::sample */
   void (*sample_grad)(void* backend, float u, float v, float dxu, float dxv, float dyu, float dyv,
                       float out[4]);   /* sampler::sample_2d_grad */
+  void (*sample_cube)(void* backend, float x, float y, float z, float lod, float out[4]); /* sampler::sample_cube */
   float color[SG_MAX_COLOR_TARGETS][4]; /* out: ps_output::color */
 } sg_host_ps_io;
 
@@ -386,6 +392,15 @@ int32_t sg_buffer_destroy(sg_device* dev, uint32_t buffer);
  * matches surface.cpp:277-295: ((y * w + x) * samples + s) * elem_size. */
 int32_t sg_texture_create(sg_device* dev, uint32_t width, uint32_t height, uint32_t samples,
                           uint32_t format, uint32_t* out_texture);
+/* renderer::create_texcube (renderer_impl.cpp:250-252): a texture_cube of
+ * six faces (texture.h:91-102), subresource `face` for cubemap_faces +x, -x,
+ * +y, -y, +z, -z (constants.h:118-125) -- the `level` of upload, download
+ * and info.  The reference leaves a cube's LOD range at [0, 0]: lookups read
+ * level 0, and sg_texture_gen_mipmap refuses a cube texture
+ * (texture_cube::gen_mipmap, texture_cube.cpp:18-30, reads a size it never
+ * set). */
+int32_t sg_texture_create_cube(sg_device* dev, uint32_t width, uint32_t height, uint32_t samples, uint32_t format,
+                               uint32_t* out_texture);
 int32_t sg_texture_upload(sg_device* dev, uint32_t texture, uint32_t level, const void* src, size_t size);
 int32_t sg_texture_download(sg_device* dev, uint32_t texture, uint32_t level, void* dst, size_t size);
 /* texture_2d::gen_mipmap(filter, true) (texture2d.cpp:25-36). */

@@ -102,6 +102,8 @@ protected:
   // sampler::sample(u, v, lod) and sample_2d_grad
   __host__ __device__ vec4 sample(float u, float v, float lod) const;
   __host__ __device__ vec4 sample_grad(float u, float v, float dxu, float dxv, float dyu, float dyv) const;
+  // sampler::sample_cube(x, y, z, lod) (sampler.cpp:771-829)
+  __host__ __device__ vec4 sample_cube(float x, float y, float z, float lod) const;
   __host__ __device__ bool front_face() const;
   __host__ __device__ float constant(int i) const;
 };
@@ -227,6 +229,16 @@ __host__ __device__ inline vec4 pixel_shader::sample_grad(float u, float v, floa
   auto io = static_cast<sg_host_ps_io const*>(ctx_);
   float o[4];
   io->sample_grad(io->backend, u, v, dxu, dxv, dyu, dyv, o);
+  return detail::host_out(o);
+#endif
+}
+__host__ __device__ inline vec4 pixel_shader::sample_cube(float x, float y, float z, float lod) const {
+#ifdef __CUDA_ARCH__
+  return detail::to_vec4(sg::sample_cube(SALVIA_GB300_PS_CTX.D->ps_samp, x, y, z, lod));
+#else
+  auto io = static_cast<sg_host_ps_io const*>(ctx_);
+  float o[4];
+  io->sample_cube(io->backend, x, y, z, lod, o);
   return detail::host_out(o);
 #endif
 }

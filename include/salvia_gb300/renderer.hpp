@@ -304,6 +304,8 @@ public:
     sg_texture_info(dev_->dev, handle_, 0, nullptr, nullptr, nullptr, nullptr, &n);
     return n;
   }
+  // texture_cube::subresource(face, lod) (texture.h:97-99): lod * 6 + face
+  surface_ptr subresource(size_t face, size_t lod) { return subresource(lod * 6 + face); }
   // texture::subresource (texture.h:17-80)
   surface_ptr subresource(size_t level) {
     if (level >= levels()) return nullptr;
@@ -903,8 +905,15 @@ public:
     uint32_t id = 0;
     return sg_shader_register(dev_->dev, m, &id) == SG_OK ? id : 0u;
   }
-  // Cube maps are not on this path (renderer.h:49): no texture.
-  texture_ptr create_texcube(size_t, size_t, size_t, pixel_format) { return nullptr; }
+  // renderer::create_texcube (renderer.h:49): six faces, subresource(face)
+  // in cubemap_faces order; a cube's LOD range stays [0, 0] as in the reference.
+  texture_ptr create_texcube(size_t width, size_t height, size_t num_samples, pixel_format fmt) {
+    uint32_t h = 0;
+    if (sg_texture_create_cube(dev_->dev, static_cast<uint32_t>(width), static_cast<uint32_t>(height),
+                               static_cast<uint32_t>(num_samples), static_cast<uint32_t>(fmt), &h) != SG_OK)
+      return nullptr;
+    return std::make_shared<resource::texture>(dev_, h);
+  }
   async_object_ptr create_query(async_object_ids id) {
     if (id != async_object_ids::pipeline_statistics && id != async_object_ids::internal_statistics) return nullptr;
     return std::make_shared<async_object>(id);

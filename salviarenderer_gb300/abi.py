@@ -39,9 +39,9 @@ SEMANTIC_POSITION, SEMANTIC_TEXCOORD, SEMANTIC_COLOR, SEMANTIC_NORMAL = 0, 1, 2,
 
 VS_TRANSFORM, VS_MORPH_DISPLACE = 1, 2
 PS_COLOR, PS_CONSTANT, PS_TEX_MODULATE, PS_TEX_GRAD_MODULATE, PS_TEX_GRAD_LEARNED = 1, 2, 3, 4, 5
-PS_TEX_LOD_MODULATE, PS_TEX_PROJ_MODULATE, PS_TEX_ALPHA_TEST, PS_COLOR_MRT = 6, 7, 8, 9
+PS_TEX_LOD_MODULATE, PS_TEX_PROJ_MODULATE, PS_TEX_ALPHA_TEST, PS_COLOR_MRT, PS_TEXCUBE_MODULATE = 6, 7, 8, 9, 10
 TEXTURED_PS = (PS_TEX_MODULATE, PS_TEX_GRAD_MODULATE, PS_TEX_GRAD_LEARNED, PS_TEX_LOD_MODULATE, PS_TEX_PROJ_MODULATE,
-               PS_TEX_ALPHA_TEST)
+               PS_TEX_ALPHA_TEST, PS_TEXCUBE_MODULATE)
 BS_REPLACE, BS_LERP_SRC_ALPHA, BS_ADD, BS_REPLACE_ALL = 1, 2, 3, 4
 MAX_COLOR_TARGETS = 7
 CMD_DRAW, CMD_CLEAR_COLOR, CMD_CLEAR_DEPTH_STENCIL, CMD_RESOLVE = 1, 2, 3, 4
@@ -179,6 +179,8 @@ SIGNATURES = {
     "sg_sampler_destroy": (C.c_int32, [C.c_void_p, C.c_uint32]),
     "sg_draw": (C.c_int32, [C.c_void_p, C.POINTER(DrawDesc), C.POINTER(DrawStats)]),
     "sg_shader_register": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32)]),
+    "sg_texture_create_cube": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                           C.POINTER(C.c_uint32)]),
     "sg_draw_static_scratch": (C.c_int32, [C.c_void_p, C.POINTER(DrawDesc), C.POINTER(DrawStats)]),
     "sg_clear_color": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(C.c_float)]),
     "sg_clear_depth_stencil": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,

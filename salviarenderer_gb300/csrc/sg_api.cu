@@ -73,6 +73,7 @@ struct Level {
 };
 struct Texture {
   uint32_t samples = 1, fmt = 0, esz = 0;
+  bool cube = false;        // texture_cube: levels are its six faces (subresources 0-5)
   std::vector<Level> levels;
   // the learned filter's texture-unit copies of the levels (made on first
   // use, refreshed by every pass that samples them, dropped with the levels)
@@ -345,13 +346,16 @@ int32_t build_sampler(sg_device* d, uint32_t handle, dev_sampler& out, uint32_t*
   out.max_anisotropy = s.max_anisotropy;
   out.fmt = t->fmt;
   out.esz = t->esz;
-  out.nlevels = static_cast<int>(t->levels.size());
-  if (out.nlevels > SG_MAX_LEVELS) return SG_INVALID_PARAMETER;
+  // a cube texture's LOD range stays [0, 0] (texture_cube never sets it): 2D
+  // lookups see face 0 as the only level, cube lookups face f as lv[f]
+  out.nlevels = t->cube ? 1 : static_cast<int>(t->levels.size());
+  out.cube = t->cube ? 1u : 0u;
+  if (t->levels.size() > static_cast<size_t>(SG_MAX_LEVELS)) return SG_INVALID_PARAMETER;
   for (int i = 0; i < 4; ++i) out.border[i] = s.border_color[i];
   out.width = t->levels[0].w;
   out.height = t->levels[0].h;
-  for (int i = 0; i < out.nlevels; ++i) out.lv[i] = dev_level{t->levels[i].ptr, static_cast<int>(t->levels[i].w),
-                                                              static_cast<int>(t->levels[i].h)};
+  for (size_t i = 0; i < t->levels.size(); ++i)
+    out.lv[i] = dev_level{t->levels[i].ptr, static_cast<int>(t->levels[i].w), static_cast<int>(t->levels[i].h)};
   return SG_OK;
 }
 
@@ -591,7 +595,7 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   info.user_ps = user_module(p.ps_prog, SG_STAGE_PIXEL);
   info.user_bs = user_module(p.bs_prog, SG_STAGE_BLEND);
   if (p.vs_prog < SG_VS_TRANSFORM || p.vs_prog > SG_VS_MORPH_DISPLACE ||
-      ((p.ps_prog < SG_PS_COLOR || p.ps_prog > SG_PS_COLOR_MRT) && !info.user_ps) ||
+      ((p.ps_prog < SG_PS_COLOR || p.ps_prog > SG_PS_TEXCUBE_MODULATE) && !info.user_ps) ||
       ((p.bs_prog < SG_BS_REPLACE || p.bs_prog > SG_BS_REPLACE_ALL) && !info.user_bs))
     return SG_INVALID_PARAMETER;
   if (p.ps_prog != SG_PS_COLOR && p.ps_prog != SG_PS_CONSTANT && p.ps_prog != SG_PS_COLOR_MRT && !info.user_ps &&
@@ -1751,7 +1755,9 @@ int32_t sg_buffer_destroy(sg_device* d, uint32_t h) {
   return SG_OK;
 }
 
-int32_t sg_texture_create(sg_device* d, uint32_t w, uint32_t h, uint32_t samples, uint32_t fmt, uint32_t* out) {
+namespace {
+int32_t create_texture(sg_device* d, uint32_t w, uint32_t h, uint32_t samples, uint32_t fmt, bool cube,
+                       uint32_t* out) {
   if (!d || !out) return SG_INVALID_PARAMETER;
   if (fmt_bytes(fmt) == 0 || w == 0 || h == 0 || w > SG_MAX_RT_SIZE || h > SG_MAX_RT_SIZE) return SG_INVALID_PARAMETER;
   if (samples != 1 && samples != 2 && samples != 4) return SG_INVALID_PARAMETER;
@@ -1759,16 +1765,28 @@ int32_t sg_texture_create(sg_device* d, uint32_t w, uint32_t h, uint32_t samples
   t.samples = samples;
   t.fmt = fmt;
   t.esz = fmt_bytes(fmt);
-  Level l;
-  l.w = w;
-  l.h = h;
-  size_t bytes = static_cast<size_t>(w) * h * samples * t.esz;
-  SG_CUDA(d, cudaMalloc(&l.ptr, (bytes + 255) & ~size_t(255)));
-  SG_CUDA(d, cudaMemsetAsync(l.ptr, 0, bytes, d->stream));
-  t.levels.push_back(l);
+  t.cube = cube;
+  for (int f = 0; f < (cube ? 6 : 1); ++f) {
+    Level l;
+    l.w = w;
+    l.h = h;
+    size_t bytes = static_cast<size_t>(w) * h * samples * t.esz;
+    SG_CUDA(d, cudaMalloc(&l.ptr, (bytes + 255) & ~size_t(255)));
+    SG_CUDA(d, cudaMemsetAsync(l.ptr, 0, bytes, d->stream));
+    t.levels.push_back(l);
+  }
   *out = d->next++;
   d->textures[*out] = t;
   return SG_OK;
+}
+}  // namespace
+
+int32_t sg_texture_create(sg_device* d, uint32_t w, uint32_t h, uint32_t samples, uint32_t fmt, uint32_t* out) {
+  return create_texture(d, w, h, samples, fmt, false, out);
+}
+// renderer::create_texcube (renderer_impl.cpp:250-252, texture_cube.cpp:12-16)
+int32_t sg_texture_create_cube(sg_device* d, uint32_t w, uint32_t h, uint32_t samples, uint32_t fmt, uint32_t* out) {
+  return create_texture(d, w, h, samples, fmt, true, out);
 }
 int32_t sg_texture_upload(sg_device* d, uint32_t h, uint32_t level, const void* src, size_t size) {
   Texture* t = d ? find_tex(d, h) : nullptr;
@@ -1790,7 +1808,7 @@ int32_t sg_texture_download(sg_device* d, uint32_t h, uint32_t level, void* dst,
 // texture_2d::gen_mipmap(filter, true) (texture2d.cpp:25-36, texture.h:26-36)
 int32_t sg_texture_gen_mipmap(sg_device* d, uint32_t h, uint32_t filter) {
   Texture* t = d ? find_tex(d, h) : nullptr;
-  if (!t || filter > SG_FILTER_LINEAR) return SG_INVALID_PARAMETER;
+  if (!t || filter > SG_FILTER_LINEAR || t->cube) return SG_INVALID_PARAMETER;
   uint32_t m = std::max(t->levels[0].w, std::max(t->levels[0].h, 1u)), n = 0;
   while (m > 0) {
     m >>= 1;

@@ -266,6 +266,7 @@ struct dev_sampler {
   int nlevels;
   float border[4];
   uint32_t width, height;  // texture size (level 0)
+  uint32_t cube;           // a cube texture: lv[0..5] are its faces, level 0 only
   dev_level lv[SG_MAX_LEVELS];
   // texture-unit copies of the levels (bilinear, the sampler's addressing),
   // for the learned filter's feature taps; 0 where the format has none
@@ -592,7 +593,10 @@ __device__ __forceinline__ v4 sample_impl_t(dev_sampler const& s, float cx, floa
     ml = iclamp(ml, max_lod, min_lod);
     return surface_lookup<WRAP8>(s, ml, cx, cy, s.min_filter);
   }
-  if (s.mip_filter == SG_FILTER_LINEAR) {
+  // a lookup without anisotropy parameters (tex2d, tex2dlod, sampler::sample)
+  // on an anisotropic sampler takes the linear mip path: the reference reads
+  // the absent parameters there (sampler.cpp:730-755)
+  if (s.mip_filter == SG_FILTER_LINEAR || !af) {
     int lo = fast_floori(static_cast<double>(miplevel));
     int hi = lo + 1;
     float frac = miplevel - static_cast<float>(lo);
@@ -633,6 +637,60 @@ __device__ inline float calc_lod_2d(dev_sampler const& s, float dxu, float dxv, 
     return af.lod;
   }
   return calc_lod(s, dxu, dxv, dyu, dyv, 0.0f);
+}
+
+// sampler::sample_cube (sampler.cpp:771-829): the major axis picks the face
+// (cubemap_faces order +x -x +y -y +z -z) and its coordinates; the lookup is
+// sample_impl<true> on that face.  The reference's cube textures keep the LOD
+// range [0, 0], so every lookup reads level 0: the magnification filter
+// below the mip threshold, else the minification filter (the linear mip
+// blend of level 0 with itself).  A cube sampler must be bound to a cube
+// texture (a 2D texture has face 0 only: other faces read face 0 here).
+__device__ inline v4 sample_cube(dev_sampler const& s, float x, float y, float z, float miplevel) {
+  float const ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+  float sc, tc, m;
+  int face;
+  if (ax > ay && ax > az) {
+    m = ax;
+    if (x > 0) {
+      sc = 0.5f * (z / m + 1.0f);
+      tc = 0.5f * (y / m + 1.0f);
+      face = 0;
+    } else {
+      sc = 0.5f * (-z / m + 1.0f);
+      tc = 0.5f * (y / m + 1.0f);
+      face = 1;
+    }
+  } else if (ay > ax && ay > az) {
+    m = ay;
+    if (y > 0) {
+      sc = 0.5f * (x / m + 1.0f);
+      tc = 0.5f * (z / m + 1.0f);
+      face = 2;
+    } else {
+      sc = 0.5f * (x / m + 1.0f);
+      tc = 0.5f * (-z / m + 1.0f);
+      face = 3;
+    }
+  } else {
+    m = az;
+    if (z > 0) {
+      sc = 0.5f * (-x / m + 1.0f);
+      tc = 0.5f * (y / m + 1.0f);
+      face = 4;
+    } else {
+      sc = 0.5f * (x / m + 1.0f);
+      tc = 0.5f * (y / m + 1.0f);
+      face = 5;
+    }
+  }
+  if (!s.cube) face = 0;
+  bool const is_mag = (s.mip_filter == SG_FILTER_POINT) ? (miplevel < 0.5f) : (miplevel < 0.0f);
+  if (is_mag) return surface_lookup<false>(s, face, sc, tc, s.mag_filter);
+  v4 const c0 = surface_lookup<false>(s, face, sc, tc, s.min_filter);
+  if (s.mip_filter == SG_FILTER_POINT) return c0;
+  float const frac = miplevel - static_cast<float>(fast_floori(static_cast<double>(miplevel)));
+  return mk4(lerp1(c0.x, c0.x, frac), lerp1(c0.y, c0.y, frac), lerp1(c0.z, c0.z, frac), lerp1(c0.w, c0.w, frac));
 }
 
 __device__ inline v4 sample_2d_grad(dev_sampler const& s, float u, float v, float dxu, float dxv, float dyu,

@@ -719,6 +719,8 @@ __device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q, bool& ke
     float const qyx = (nyx / nyw + 1.0f) * 0.5f, qyy = (nyy / nyw + 1.0f) * 0.5f;
     return mulv(sample_2d_grad(D.ps_samp, px, py, qxx - px, qxy - py, qyx - px, qyy - py, 0.0f), a1);
   }
+  case SG_PS_TEXCUBE_MODULATE:  // sampler::sample_cube(x, y, z, w) (sampler.cpp:771-829)
+    return mulv(sample_cube(D.ps_samp, a0.x, a0.y, a0.z, a0.w), a1);
   case SG_PS_TEX_ALPHA_TEST: {  // tex2d * attr[1], discarded below constants[0] alpha
     float lod = calc_lod_2d(D.ps_samp, u1 - u0, v1 - v0, u2 - u0, v2 - v0);
     v4 const c = mulv(sample_impl(D.ps_samp, a0.x, a0.y, lod, nullptr), a1);

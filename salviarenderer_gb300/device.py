@@ -87,6 +87,14 @@ class Device:
         self._textures[h.value] = (width, height, samples, fmt)
         return h.value
 
+    def texture_cube(self, width, height, samples=1, fmt=abi.FMT_RGBA8):
+        """sg_texture_create_cube: six faces, subresource = face (+x -x +y -y +z -z)."""
+        h = C.c_uint32()
+        self._check("sg_texture_create_cube",
+                    self.lib.sg_texture_create_cube(self.handle, width, height, samples, fmt, C.byref(h)))
+        self._textures[h.value] = (width, height, samples, fmt)
+        return h.value
+
     def texture_info(self, tex, level=0):
         vals = [C.c_uint32() for _ in range(5)]
         self._check("sg_texture_info",

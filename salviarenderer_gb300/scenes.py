@@ -136,6 +136,12 @@ class Bound:
         self.buf = {k: dev.buffer(v) for k, v in scene.buffers.items()}
         self.tex = {}
         for k, (img, mips) in scene.textures.items():
+            if isinstance(img, list):  # a cube texture's six faces (no mip chain: its LOD range is [0, 0])
+                t = dev.texture_cube(img[0].shape[1], img[0].shape[0], 1, abi.FMT_RGBA8)
+                for face, fimg in enumerate(img):
+                    dev.texture_upload(t, fimg, face)
+                self.tex[k] = t
+                continue
             h, w = img.shape[0], img.shape[1]
             fmt = abi.FMT_R32F if img.dtype == np.float32 and img.ndim == 2 else abi.FMT_RGBA8
             t = dev.texture(w, h, 1, fmt)
@@ -474,6 +480,38 @@ def mrt_scene(seed=1, width=96, height=80, samples=1, ntris=120, more=((abi.FMT_
                             varying_modifiers=[abi.AM_LINEAR] * nt,
                             vs=dict(program=abi.VS_TRANSFORM, constants=ident), ps=dict(program=ps),
                             bs=dict(program=bs)))
+    return s
+
+
+def cube_scene(seed=1, width=96, height=80, samples=1, ntris=100, sampler=None, major=None, lod=(-1.0, 2.0),
+               face_size=32):
+    """Cube-map lookups (sampler::sample_cube, SG_PS_TEXCUBE_MODULATE): random
+    clip-space triangles whose first varying is a direction (and the lookup's
+    level in w) and whose second modulates the colour; the cube's six faces
+    are seeded value noise.  `major` = "+x" keeps every direction's major
+    axis on +x -- for the quads' helper pixels too, whose directions are
+    extrapolated: +x is the only face the reference can reach."""
+    rng = np.random.default_rng(seed)
+    s = Scene("cube", width, height, samples)
+    s.clear_color = (0.0, 0.1, 0.2, 1.0)
+    nv = ntris * 3
+    pos = rng.uniform(-1.0, 1.0, size=(nv, 4))
+    pos[:, 2] = rng.uniform(0.05, 0.95, size=nv)
+    pos[:, 3] = 1.0
+    if major == "+x":  # linear in the position: extrapolated helper pixels stay on +x too
+        d = np.stack([np.full(nv, 8.0), 5.0 * pos[:, 0], 5.0 * pos[:, 1]], axis=1)
+    else:
+        d = rng.normal(size=(nv, 3))
+    dirs = np.concatenate([d, rng.uniform(*lod, size=(nv, 1))], axis=1)
+    col = rng.uniform(0.3, 1.0, size=(nv, 4))
+    s.buffers["vb"] = np.concatenate([pos, dirs, col], axis=1).astype(np.float32)
+    s.textures["cube"] = ([to_rgba8(value_noise(rng, face_size, octaves=3)) for _ in range(6)], False)
+    s.samplers["s0"] = ("cube", dict(sampler or {}))
+    s.draws.append(dict(viewport=(0, 0, width, height, 0.0, 1.0), prim_count=ntris, streams=[("vb", 48, 0)],
+                        inputs=GRID_INPUTS, num_varyings=2, varying_modifiers=[abi.AM_LINEAR, abi.AM_LINEAR],
+                        vs=dict(program=abi.VS_TRANSFORM, constants=np.identity(4, dtype=np.float32)),
+                        ps=dict(program=abi.PS_TEXCUBE_MODULATE, samplers=["s0"]),
+                        bs=dict(program=abi.BS_REPLACE)))
     return s
 
 

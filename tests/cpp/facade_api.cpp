@@ -65,7 +65,18 @@ int main() {
   if (r->create_input_layout(&el, 1, salvia::shader::shader_object_ptr())) return fail("SASL input layout");
   std::printf("ok shader-code state\n");
 
-  if (r->create_texcube(8, 8, 1, pixel_format_color_rgba8)) return fail("create_texcube");
+  {  // six faces, each its own subresource, written and read back
+    auto cube = r->create_texcube(8, 8, 1, pixel_format_color_rgba8);
+    if (!cube || cube->levels() != 6) return fail("create_texcube");
+    std::vector<uint8_t> px(8 * 8 * 4);
+    for (size_t f = 0; f < 6; ++f) {
+      std::memset(px.data(), static_cast<int>(10 + f), px.size());
+      if (cube->subresource(f, 0)->write(px.data(), px.size()) != salvia::result::ok) return fail("cube face write");
+    }
+    std::vector<uint8_t> back;
+    if (cube->subresource(3, 0)->read(back) != salvia::result::ok || back.size() != px.size() || back[5] != 13)
+      return fail("cube face read");
+  }
   std::printf("ok create_texcube\n");
   r->flush();
   return 0;

@@ -102,6 +102,13 @@ CASES = {
                                       blend="user:screen_blend_bs", bs_constants=[0.6]),
     "user_ps_front_proj_back_lod": lambda: F(seed=72, ps="user:proj_or_lod_ps", sampler=TRILINEAR,
                                              uv_w=(0.5, 2.0), blend=abi.BS_LERP_SRC_ALPHA),
+    # cube maps (sampler::sample_cube, sampler.cpp:771-829): directions whose
+    # major axis is +x, the only face the reference's cube textures reach;
+    # levels on both sides of the magnification threshold
+    "cube_px_linear": lambda: scenes.cube_scene(seed=80, major="+x", sampler=TRILINEAR),
+    "cube_px_point_4x": lambda: scenes.cube_scene(seed=81, major="+x", samples=4,
+                                                  sampler=dict(POINT, address_u=abi.ADDRESS_CLAMP,
+                                                               address_v=abi.ADDRESS_MIRROR)),
     # C2 pattern (textured grid, trilinear + 16x AF, src-alpha blend)
     "c2_160x96_4x": lambda: scenes.c2_scene(width=160, height=96, grid=33, tex_size=128, ndraws=4),
     "c2_128x72_1x": lambda: scenes.c2_scene(width=128, height=72, grid=25, tex_size=64, samples=1,

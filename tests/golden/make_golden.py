@@ -43,7 +43,9 @@ def scene_digest(scene):
         h.update(np.ascontiguousarray(scene.buffers[k]).tobytes())
     for k in sorted(scene.textures):
         h.update(k.encode())
-        h.update(np.ascontiguousarray(scene.textures[k][0]).tobytes())
+        img = scene.textures[k][0]
+        for part in (img if isinstance(img, list) else [img]):
+            h.update(np.ascontiguousarray(part).tobytes())
     return h.hexdigest()
 
 

@@ -93,6 +93,15 @@ def test_texture_sizes(gdev, odev, ps, tex_size):
                                              uv_scale=5.0))
 
 
+@pytest.mark.parametrize("sampler", ["trilinear", "point"])
+def test_cube_every_face(gdev, odev, sampler):
+    """sampler::sample_cube on all six faces (directions drawn on the sphere;
+    the reference's cube textures reach +x only, so the other faces are
+    checked against the oracle alone)."""
+    s = dict(trilinear=cases.TRILINEAR, point=dict(cases.POINT, address_u=abi.ADDRESS_CLAMP))[sampler]
+    compare(gdev, odev, scenes.cube_scene(seed=82, ntris=150, sampler=s, samples=4 if sampler == "point" else 1))
+
+
 def test_rgba16f_target(gdev, odev):
     compare(gdev, odev, scenes.feature_scene(seed=41, color_fmt=abi.FMT_RGBA16F, blend=abi.BS_LERP_SRC_ALPHA,
                                              samples=4))
