@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-uneven", action="store_true", help="skip the 256-frame batched-draw leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-filter leg")
     ap.add_argument("--no-autotune", action="store_true", help="time under the default scheduling parameters")
+    ap.add_argument("--cpu-configs", action="store_true",
+                    help="time the CPU restatement (and the reference, where built) on the five workloads")
     ap.add_argument("--size", default="1920x1080",
                     help="render-target size; smaller sizes are for profiling captures only")
     return ap.parse_args()
@@ -225,6 +227,62 @@ def run_reference(args):
                              "sample": f"{cores} full frames per step, one per process"},
             "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def run_cpu_configs(args):
+    """CPU time of the five workloads, for the CPU-baseline table: the
+    restatement (oracle/, one core) everywhere, and the reference renderer
+    itself (oracle/_ref, all its worker threads) where it was built (an
+    x86-64 host with the reference's sources; C1 and C2 only, as the others
+    use extension formats).  Bounded samples: C1 and C2 whole frames; C3 the first 16 of its 256 frames; C5 a clear + resolve
+    frame and a frame of 10 of its 1000 instances, extrapolated linearly to
+    1000 instances."""
+    from salviarenderer_gb300 import abi, Device, scenes
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    libs = {"port": os.path.join(ROOT, "oracle", "_build", "libsg_oracle.so")}
+    ref = os.path.join(ROOT, "oracle", "_ref", "libsalvia_ref.so")
+    if os.path.exists(ref):
+        libs["reference"] = ref
+
+    def seconds(fn, reps=1):
+        fn()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        return (time.perf_counter() - t0) / reps
+
+    out = {"host": {"cores": os.cpu_count(), "machine": os.uname().machine}}
+    try:
+        with open("/proc/cpuinfo") as f:
+            names = [l.split(":", 1)[1].strip() for l in f if l.lower().startswith(("model name", "cpu part"))]
+        out["host"]["cpu"] = names[0] if names else None
+    except OSError:
+        pass
+    for kind, path in libs.items():
+        dev = Device(abi.bind(ctypes.CDLL(path)))
+        r = {"cores": 1 if kind == "port" else os.cpu_count()}
+        b = scenes.Bound(dev, scenes.c1_scene(seed=SEED))
+        r["c1_frames_per_s"] = 1.0 / seconds(b.frame, 3)
+        b = scenes.Bound(dev, scenes.c2_scene(seed=SEED))
+        r["c2_frames_per_s"] = 1.0 / seconds(b.frame)
+        if kind == "reference":  # C3 and C5 use the extension formats (D24S8, RGBA16F, D32F)
+            out[kind] = r
+            continue
+        batch = scenes.UnevenBatch(seed=SEED)
+        k = 16
+        batch.frames = batch.frames[:k]
+        batch.vb = batch.vb[:3 * sum(f["ntris"] for f in batch.frames)]
+        u = scenes.BoundUneven(dev, batch)
+        t = seconds(u.render_plain)
+        r["c3_sample"] = {"frames": k, "triangles": batch.triangles, "pixels": batch.pixels,
+                          "frames_per_s": k / t, "mtris_per_s": batch.triangles / t / 1e6}
+        t0 = seconds(scenes.Bound(dev, scenes.c5_scene(seed=SEED, instances=0)).frame)
+        ki = 10
+        tk = seconds(scenes.Bound(dev, scenes.c5_scene(seed=SEED, instances=ki)).frame)
+        r["c5_frames_per_s_extrapolated"] = 1.0 / (t0 + (tk - t0) * 1000 / ki)
+        r["c5_sample"] = {"instances": ki, "clear_resolve_s": t0, "frame_s": tk}
+        out[kind] = r
+    print(json.dumps({"cpu_configs": out}), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -540,7 +598,9 @@ def run_gpu(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.cpu_configs:
+        run_cpu_configs(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

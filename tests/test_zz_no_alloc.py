@@ -3,13 +3,15 @@
 The allocation-free entry point runs the same kernels with its scratch in a
 static device array; its targets and counters must equal sg_draw's bit for
 bit, on two frames in a row (the second frame reuses the array as the first
-left it).  This file is collected last so that it also runs after the other
+left it), and the device's free memory must not change across the static
+calls.  This file is collected last so that it also runs after the other
 GPU tests in one process.
 """
 import ctypes
 
 import numpy as np
 import pytest
+import torch
 
 import cases
 from salviarenderer_gb300 import abi, Device, scenes
@@ -48,6 +50,8 @@ def test_static_scratch_matches_sg_draw_twice(gdev, name):
     ref_bound = scenes.Bound(gdev, scene)
     want, want_st = frame_with(ref_bound, gdev.draw, stats=True)
     bound = scenes.Bound(gdev, scene)
+    gdev.sync()
+    free_before = torch.cuda.mem_get_info(0)[0]
     for call in range(2):
         got, got_st = frame_with(bound, gdev.draw_static_scratch, stats=(call == 0))
         if call == 0:
@@ -56,6 +60,9 @@ def test_static_scratch_matches_sg_draw_twice(gdev, name):
             assert np.array_equal(got[k], want[k]), \
                 f"{name} call {call}: {k} differs in {(got[k] != want[k]).sum()} bytes"
     gdev.sync()
+    # the static calls (and the downloads between them, into host memory)
+    # allocated no device memory
+    assert torch.cuda.mem_get_info(0)[0] == free_before
 
 
 def test_static_scratch_rejects_oversized_draw(gdev):
