@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-uneven", action="store_true", help="skip the 256-frame batched-draw leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-filter leg")
+    ap.add_argument("--no-facade", action="store_true", help="skip the C++ facade leg")
     ap.add_argument("--no-autotune", action="store_true", help="time under the default scheduling parameters")
     ap.add_argument("--cpu-configs", action="store_true",
                     help="time the CPU restatement (and the reference, where built) on the five workloads")
@@ -444,6 +445,35 @@ def measure_c5(dev, stream, flush, args, model):
     return out
 
 
+def measure_facade(args, scene, resolved_want):
+    """The same frame through the C++ facade (include/salvia_gb300/renderer.hpp)
+    as a reference application drives it: tests/cpp/facade_scene.cpp, built
+    against the library, issues clears, one draw_index per draw, resolve and
+    flush each frame; the facade queues the calls and submits them as one
+    command list at flush.  Wall time per frame up to the end of its flush
+    (L2 flushed before each frame), and whether its resolved image equals
+    the recorded graph's."""
+    import tempfile
+    from salviarenderer_gb300 import scenes
+    from salviarenderer_gb300 import build as pbuild
+    libdir, libfile = os.path.split(pbuild.ensure_built())
+    with tempfile.TemporaryDirectory() as tmp:
+        exe, inp, out = (os.path.join(tmp, n) for n in ("facade_scene", "in.bin", "out.bin"))
+        subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "facade_scene.cpp"), "-o", exe, "-L", libdir,
+                        f"-l{libfile[3:-3]}", f"-Wl,-rpath,{libdir}"], check=True)
+        scenes.write_facade_input(scene, inp)
+        run = subprocess.run([exe, inp, out, str(args.steps), str(args.warmup)], check=True,
+                             capture_output=True, text=True)
+        ms = float(next(l for l in run.stdout.splitlines() if l.startswith("facade_ms_per_frame")).split()[1])
+        raw = open(out, "rb").read()
+    n = scene.width * scene.height
+    off = n * scene.samples * (4 + 8)
+    return {"frames_per_s": 1000.0 / ms, "ms_per_frame": ms,
+            "calls_per_frame": "clear_color, clear_depth_stencil, 8 x (set_pixel_shader, draw_index), resolve, flush",
+            "resolved_equals_graph": raw[off:off + n * 4] == bytes(resolved_want)}
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -539,6 +569,10 @@ def run_gpu(args):
         barrier()
         e2e_fps = frames / max_over_ranks(time.perf_counter() - t0)
     dev.sync()
+    facade = None
+    if rank == 0 and not args.no_facade and scene.samples > 1:
+        graph.launch()
+        facade = measure_facade(args, scene, b.outputs()["resolved"])
     uneven = None if args.no_uneven else measure_uneven(dev, stream, flush, args)
     learned = None if args.no_learned else measure_learned(dev, stream, flush, args, width, height)
 
@@ -563,7 +597,9 @@ def run_gpu(args):
             "config": dict(workload_config(scene), parallelism=f"replicas x{world}",
                            path="frame recorded as one CUDA graph (sg_graph_launch)"),
             "paths_frames_per_s": {"plain_per_draw": frames / plain_s, "submitted_list": frames / submit_s,
-                                   "recorded_graph": fps},
+                                   "recorded_graph": fps,
+                                   "cpp_facade": None if facade is None else facade["frames_per_s"]},
+            "facade": facade,
             "gpix_per_s": fps * scene.width * scene.height / 1e9,
             "gsamples_per_s": fps * scene.width * scene.height * scene.samples / 1e9,
             "mtris_per_s": fps * scene.triangles / 1e6,
@@ -584,6 +620,11 @@ def run_gpu(args):
                 "h2d_bytes_per_step": int(vb_host.numel() * 4 + ib_host.numel() * 4),
                 "d2h_bytes_per_step": out_bytes},
             "tuning": tuning,
+            "autotune": None if args.no_autotune else {
+                "searched": dev.autotune_space(), "chosen": {k: tuning[k] for k in dev.autotune_space()},
+                "not_searched": {"binning tile": "64x64: the reference's 64/16/4 classification decides edge samples",
+                                 "shade_quads_per_warp": "8 by construction (4 lanes per quad)",
+                                 "bin_capacity, frag_chunks": "sized from counters, grown after an overflow"}},
             "uneven_batch": uneven,
             "learned_filter": learned,
             "gpu_launches": int(ginfo["kernels"]) * args.steps,

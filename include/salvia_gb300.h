@@ -537,6 +537,17 @@ int32_t sg_set_tuning(sg_device* dev, const sg_tuning* tuning);
  * candidate. */
 int32_t sg_autotune(sg_device* dev, const sg_command* cmds, uint32_t n, uint32_t reps, sg_tuning* out,
                     float* best_ms);
+/* The autotuner's search space, in the order it searches (coordinate
+ * descent, two sweeps): each searched sg_tuning field by name with its
+ * candidate values.  Not searched: the binning tile (64x64 by the reference's
+ * classification), shade_quads_per_warp (8 by construction), and the
+ * capacities (sized from counters and grown after an overflow). */
+typedef struct sg_tuning_knob {
+  const char* field;
+  uint32_t count;
+  uint32_t values[8];
+} sg_tuning_knob;
+int32_t sg_autotune_space(const sg_tuning_knob** knobs, uint32_t* count);
 
 /* ---- learned anisotropic filter --------------------------------------------
  * No counterpart in the reference.  A small MLP (24 inputs -> 64 -> 64 -> 5,

@@ -139,6 +139,11 @@ class Tuning(C.Structure):
                 ("cover_ctas_per_sm", C.c_uint32), ("shade_resident", C.c_uint32)]
 
 
+class TuningKnob(C.Structure):
+    """sg_tuning_knob"""
+    _fields_ = [("field", C.c_char_p), ("count", C.c_uint32), ("values", C.c_uint32 * 8)]
+
+
 _u32p = C.POINTER(C.c_uint32)
 
 class AfTrainDesc(C.Structure):
@@ -195,6 +200,7 @@ SIGNATURES = {
     "sg_set_tuning": (C.c_int32, [C.c_void_p, C.POINTER(Tuning)]),
     "sg_autotune": (C.c_int32, [C.c_void_p, C.POINTER(Command), C.c_uint32, C.c_uint32,
                                 C.POINTER(Tuning), C.POINTER(C.c_float)]),
+    "sg_autotune_space": (C.c_int32, [C.POINTER(C.POINTER(TuningKnob)), C.POINTER(C.c_uint32)]),
     "sg_af_model_create": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
     "sg_af_model_destroy": (None, [C.c_void_p, C.c_void_p]),
     "sg_af_model_id": (C.c_uint32, [C.c_void_p]),
@@ -215,7 +221,7 @@ AF_FEATURES, AF_OUTPUTS, AF_PARAMS = 24, 5, 6085
 # Entry points of the GPU library with no counterpart in the reference (the
 # CPU oracle does not export them).
 PRODUCT_ONLY = {"sg_draw_static_scratch", "sg_graph_create", "sg_graph_launch", "sg_graph_info",
-                "sg_graph_destroy", "sg_get_tuning", "sg_set_tuning", "sg_autotune"}
+                "sg_graph_destroy", "sg_get_tuning", "sg_set_tuning", "sg_autotune", "sg_autotune_space"}
 PRODUCT_ONLY |= {name for name in SIGNATURES if name.startswith("sg_af_")}
 
 

@@ -229,6 +229,30 @@ void pack_plan(PassPlan const& pl, PlanLayout const& L, std::vector<uint8_t>& ou
   std::memcpy(out.data() + L.ct_off, pl.chunk_target.data(), pl.chunk_target.size() * 4);
 }
 
+// The autotuner's search space, searched in this order.
+sg_tuning_knob const kTuningKnobs[] = {
+    {"cover_threads_per_block", 2, {2u, 32u}},
+    {"cover_item", 2, {16u, 32u}},
+    {"split_entries", 4, {160u, 320u, 640u, 1280u}},
+    {"cover_ctas_per_sm", 2, {3u, 4u}},
+    {"bin_chunk", 4, {256u, 512u, 1024u, 2048u}},
+    {"shade_ctas_per_sm", 3, {4u, 8u, 16u}},
+    {"shade_resident", 2, {3u, 4u}},
+    {"merge_ctas_per_sm", 3, {2u, 3u, 6u}},
+};
+
+uint32_t* knob_field(sg_tuning& t, char const* name) {
+  std::string const n(name);
+  if (n == "cover_threads_per_block") return &t.cover_threads_per_block;
+  if (n == "cover_item") return &t.cover_item;
+  if (n == "split_entries") return &t.split_entries;
+  if (n == "cover_ctas_per_sm") return &t.cover_ctas_per_sm;
+  if (n == "bin_chunk") return &t.bin_chunk;
+  if (n == "shade_ctas_per_sm") return &t.shade_ctas_per_sm;
+  if (n == "shade_resident") return &t.shade_resident;
+  return &t.merge_ctas_per_sm;
+}
+
 sg_tuning default_tuning() {
   sg_tuning t{};
   t.cover_item = 32;
@@ -2059,6 +2083,13 @@ int32_t sg_set_tuning(sg_device* d, const sg_tuning* t) {
   return SG_OK;
 }
 
+int32_t sg_autotune_space(const sg_tuning_knob** knobs, uint32_t* count) {
+  if (!knobs || !count) return SG_INVALID_PARAMETER;
+  *knobs = kTuningKnobs;
+  *count = static_cast<uint32_t>(sizeof(kTuningKnobs) / sizeof(kTuningKnobs[0]));
+  return SG_OK;
+}
+
 int32_t sg_autotune(sg_device* d, const sg_command* cmds, uint32_t n, uint32_t reps, sg_tuning* out,
                     float* best_ms) {
   if (!d || (!cmds && n) || reps == 0) return SG_INVALID_PARAMETER;
@@ -2080,35 +2111,24 @@ int32_t sg_autotune(sg_device* d, const sg_command* cmds, uint32_t n, uint32_t r
     ms /= static_cast<float>(reps);
     return SG_OK;
   };
-  // coordinate descent over the parameters, two sweeps
+  // coordinate descent over the knobs, two sweeps
   sg_tuning best_t = d->tuning;
   float best = 0.0f;
   int32_t r = time_of(best_t, best);
   for (int sweep = 0; sweep < 2 && r == SG_OK; ++sweep) {
-    for (int param = 0; param < 8 && r == SG_OK; ++param) {
-      std::vector<uint32_t> vals;
-      switch (param) {
-      case 5: vals = {2u, 32u}; break;
-      case 6:
-      case 7: vals = {3u, 4u}; break;
-      case 0: vals = {16u, 32u}; break;
-      case 1: vals = {160u, 320u, 640u, 1280u}; break;
-      case 2: vals = {256u, 512u, 1024u, 2048u}; break;
-      case 3: vals = {4u, 8u, 16u}; break;
-      default: vals = {2u, 3u, 6u}; break;
-      }
-      for (uint32_t v : vals) {
+    for (sg_tuning_knob const& k : kTuningKnobs) {
+      if (r != SG_OK) break;
+      for (uint32_t vi = 0; vi < k.count; ++vi) {
         sg_tuning t = best_t;
-        uint32_t* field = param == 0 ? &t.cover_item : param == 1 ? &t.split_entries : param == 2 ? &t.bin_chunk
-                          : param == 3 ? &t.shade_ctas_per_sm : param == 4 ? &t.merge_ctas_per_sm
-                          : param == 5 ? &t.cover_threads_per_block : param == 6 ? &t.cover_ctas_per_sm
-                          : &t.shade_resident;
+        uint32_t* field = knob_field(t, k.field);
+        uint32_t const v = k.values[vi];
         if (*field == v) continue;
         // item size and split threshold only shape the warp-per-pair coverage,
         // the CTAs per SM only the 2-thread one
-        if (param <= 1 && t.cover_threads_per_block != 32) continue;
-        if (param == 6 && t.cover_threads_per_block != 2) continue;
-        if (param == 1 && t.cover_item == 16) continue;  // every item is 16x16 already
+        bool const warp_cover = t.cover_threads_per_block == 32;
+        if ((field == &t.cover_item || field == &t.split_entries) && !warp_cover) continue;
+        if (field == &t.cover_ctas_per_sm && warp_cover) continue;
+        if (field == &t.split_entries && t.cover_item == 16) continue;  // every item is 16x16 already
         *field = v;
         float ms = 0.0f;
         r = time_of(t, ms);

@@ -357,6 +357,50 @@ __global__ void __launch_bounds__(128) k_geometry(PassParams P) {
 
 // ---------------------------------------------------------------------------
 // binning (rasterizer::threaded_dispatch_primitive, rasterizer.cpp:775-862)
+
+// The per-tile test of a triangle spanning several tiles: trivial reject
+// (the tile is dropped) and trivial accept (bit 0 of the entry).
+struct TileTest {
+  float ez[3], ex[3], ey[3], r2a[3];
+  bool mx[3], my[3];
+  __device__ void init(float4 const& e0, float4 const& e1, float4 const& e2) {
+    float4 const e[3] = {e0, e1, e2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      ez[k] = e[k].z;
+      ex[k] = e[k].x;
+      ey[k] = e[k].y;
+      mx[k] = e[k].x > 0;
+      my[k] = e[k].y > 0;
+      float stx = TILE * e[k].x, sty = TILE * e[k].y;
+      r2a[k] = -fabsf(stx) - fabsf(sty);
+    }
+  }
+  // bit 0: accepted; bit 1: not rejected
+  __device__ int test(int x, int y) const {
+    int rej = 0, acc = 1;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float evv = ez[k] - (static_cast<float>(x + mx[k]) * TILE * ex[k] + static_cast<float>(y + my[k]) * TILE * ey[k]);
+      rej |= (0 < evv);
+      acc &= (r2a[k] >= evv);
+    }
+    return rej ? 0 : (2 | acc);
+  }
+};
+
+// Tiles up to which one lane tests a triangle's tiles alone in the count pass.
+constexpr int BIN_LANE_TILES = 8;
+
+// k_bin<false> counts the entries of every (tile, chunk); k_bin<true> writes
+// them, each (tile, chunk) run in slot order (API order).  A warp walks a
+// chunk of a target's slots 32 at a time, every lane fetching its own slot's
+// triangle.  Counting needs no order: each lane counts its own triangle's
+// tiles (same-tile increments of a warp aggregated), and the warp tests the
+// tiles of a triangle spanning more than BIN_LANE_TILES together.  Filling
+// walks the 32 slots in order: a run of consecutive single-tile triangles is
+// written in one step (lanes of one tile ranked by lane, one cursor update
+// per tile), a triangle spanning several tiles by the whole warp.
 template <bool FILL>
 __global__ void __launch_bounds__(128) k_bin(PassParams P) {
   uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -369,8 +413,8 @@ __global__ void __launch_bounds__(128) k_bin(PassParams P) {
   uint32_t begin = T.slot_base + c * T.chunk, end = min(begin + T.chunk, slot_end);
   int const tgx = T.tiles_x;
   uint32_t* cnt = P.bin_counts + T.count_base + c;
+  uint32_t const lt_mask = (1u << lane) - 1u;
   for (uint32_t base = begin; base < end; base += 32) {
-    // every lane fetches its own slot's triangle (parallel loads)
     uint32_t slot = base + lane;
     uint32_t rec = slot < end ? P.slot_rec[slot] : NO_REC;
     float4 e0 = make_float4(0, 0, 0, 0), e1 = e0, e2 = e0;
@@ -393,69 +437,99 @@ __global__ void __launch_bounds__(128) k_bin(PassParams P) {
       ex = max(ex, 0);
       ey = max(ey, 0);
     }
-    uint32_t valid = __ballot_sync(0xFFFFFFFFu, rec != NO_REC);
-    // then the warp walks them in slot order (API order), one at a time
-    while (valid) {
-      int i = __ffs(valid) - 1;
-      valid &= valid - 1;
-      uint32_t r = __shfl_sync(0xFFFFFFFFu, rec, i);
-      int tsx = __shfl_sync(0xFFFFFFFFu, sx, i), tsy = __shfl_sync(0xFFFFFFFFu, sy, i);
-      int tex = __shfl_sync(0xFFFFFFFFu, ex, i), tey = __shfl_sync(0xFFFFFFFFu, ey, i);
-      if (tsx + 1 == tex && tsy + 1 == tey) {
-        // single-tile primitive: pushed without the tile tests (rasterizer.cpp:809-811)
-        if (lane == 0) {
-          uint32_t* cc = cnt + static_cast<size_t>(tsy * tgx + tsx) * nch;
-          if (FILL) {
-            uint32_t pos = *cc;
-            *cc = pos + 1;
-            if (pos < P.bin_capacity) P.bin_entries[pos] = r << 1;
-          } else {
-            atomicAdd(cc, 1u);
-          }
-        }
-      } else if (tsx < tex && tsy < tey) {
-        float4 e[3];
-        e[0] = make_float4(__shfl_sync(0xFFFFFFFFu, e0.x, i), __shfl_sync(0xFFFFFFFFu, e0.y, i),
-                           __shfl_sync(0xFFFFFFFFu, e0.z, i), 0.0f);
-        e[1] = make_float4(__shfl_sync(0xFFFFFFFFu, e1.x, i), __shfl_sync(0xFFFFFFFFu, e1.y, i),
-                           __shfl_sync(0xFFFFFFFFu, e1.z, i), 0.0f);
-        e[2] = make_float4(__shfl_sync(0xFFFFFFFFu, e2.x, i), __shfl_sync(0xFFFFFFFFu, e2.y, i),
-                           __shfl_sync(0xFFFFFFFFu, e2.z, i), 0.0f);
-        bool mx[3], my[3];
-        float r2a[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          mx[k] = e[k].x > 0;
-          my[k] = e[k].y > 0;
-          float stx = TILE * e[k].x, sty = TILE * e[k].y;
-          r2a[k] = -fabsf(stx) - fabsf(sty);
-        }
-        int w = tex - tsx, nt = w * (tey - tsy);
-        for (int j = lane; j < nt; j += 32) {
-          int x = tsx + j % w, y = tsy + j / w;
-          int rej = 0, acc = 1;
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            float evv = e[k].z - (static_cast<float>(x + mx[k]) * TILE * e[k].x +
-                                  static_cast<float>(y + my[k]) * TILE * e[k].y);
-            rej |= (0 < evv);
-            acc &= (r2a[k] >= evv);
-          }
-          if (!rej) {
-            uint32_t* cc = cnt + static_cast<size_t>(y * tgx + x) * nch;
-            if (FILL) {
-              // the chunk's cursor of this tile: only this warp touches it, and the
-              // __syncwarp below orders one step's update before the next step's read
-              uint32_t pos = *cc;
-              *cc = pos + 1;
-              if (pos < P.bin_capacity) P.bin_entries[pos] = (r << 1) | static_cast<uint32_t>(acc);
-            } else {
-              atomicAdd(cc, 1u);
-            }
-          }
+    bool const has = rec != NO_REC && sx < ex && sy < ey;
+    // single-tile primitives are pushed without the tile tests (rasterizer.cpp:809-811)
+    bool const single = has && sx + 1 == ex && sy + 1 == ey;
+    int const w = ex - sx, nt = has ? w * (ey - sy) : 0;
+    uint32_t const single_m = __ballot_sync(0xFFFFFFFFu, single);
+    if (!FILL) {
+      // singles: one aggregated increment per tile
+      if (single) {
+        uint32_t const tile = static_cast<uint32_t>(sy * tgx + sx);
+        uint32_t const grp = __match_any_sync(single_m, tile);
+        if ((grp & lt_mask) == 0) atomicAdd(cnt + static_cast<size_t>(tile) * nch, static_cast<uint32_t>(__popc(grp)));
+      }
+      // few tiles: each lane its own; many: the warp together
+      bool const small = has && !single && nt <= BIN_LANE_TILES;
+      if (small) {
+        TileTest tt;
+        tt.init(e0, e1, e2);
+        for (int j = 0; j < nt; ++j) {
+          int x = sx + j % w, y = sy + j / w;
+          if (tt.test(x, y)) atomicAdd(cnt + static_cast<size_t>(y * tgx + x) * nch, 1u);
         }
       }
-      __syncwarp();
+      uint32_t big = __ballot_sync(0xFFFFFFFFu, has && nt > BIN_LANE_TILES);
+      while (big) {
+        int i = __ffs(big) - 1;
+        big &= big - 1;
+        TileTest tt;
+        tt.init(make_float4(__shfl_sync(0xFFFFFFFFu, e0.x, i), __shfl_sync(0xFFFFFFFFu, e0.y, i),
+                            __shfl_sync(0xFFFFFFFFu, e0.z, i), 0.0f),
+                make_float4(__shfl_sync(0xFFFFFFFFu, e1.x, i), __shfl_sync(0xFFFFFFFFu, e1.y, i),
+                            __shfl_sync(0xFFFFFFFFu, e1.z, i), 0.0f),
+                make_float4(__shfl_sync(0xFFFFFFFFu, e2.x, i), __shfl_sync(0xFFFFFFFFu, e2.y, i),
+                            __shfl_sync(0xFFFFFFFFu, e2.z, i), 0.0f));
+        int const tsx = __shfl_sync(0xFFFFFFFFu, sx, i), tsy = __shfl_sync(0xFFFFFFFFu, sy, i);
+        int const tw = __shfl_sync(0xFFFFFFFFu, w, i), tn = __shfl_sync(0xFFFFFFFFu, nt, i);
+        for (int j = lane; j < tn; j += 32) {
+          int x = tsx + j % tw, y = tsy + j / tw;
+          if (tt.test(x, y)) atomicAdd(cnt + static_cast<size_t>(y * tgx + x) * nch, 1u);
+        }
+      }
+      continue;
+    }
+    // fill, in slot order
+    uint32_t pending = __ballot_sync(0xFFFFFFFFu, has);
+    uint32_t const multi_m = pending & ~single_m;
+    while (pending) {
+      uint32_t const next_multi = multi_m & pending;
+      int const m = next_multi ? __ffs(next_multi) - 1 : 32;
+      uint32_t const run = pending & single_m & (m == 32 ? 0xFFFFFFFFu : ((1u << m) - 1u));
+      if (run) {
+        if ((run >> lane) & 1u) {
+          uint32_t const tile = static_cast<uint32_t>(sy * tgx + sx);
+          uint32_t const grp = __match_any_sync(run, tile);
+          int const leader = __ffs(grp) - 1;
+          uint32_t* cc = cnt + static_cast<size_t>(tile) * nch;
+          uint32_t pos = 0;
+          if (lane == leader) {
+            pos = *cc;
+            *cc = pos + static_cast<uint32_t>(__popc(grp));
+          }
+          pos = __shfl_sync(grp, pos, leader) + static_cast<uint32_t>(__popc(grp & lt_mask));
+          if (pos < P.bin_capacity) P.bin_entries[pos] = rec << 1;
+        }
+        pending &= ~run;
+        __syncwarp();
+      }
+      if (m < 32) {
+        pending &= ~(1u << m);
+        uint32_t const r = __shfl_sync(0xFFFFFFFFu, rec, m);
+        TileTest tt;
+        tt.init(make_float4(__shfl_sync(0xFFFFFFFFu, e0.x, m), __shfl_sync(0xFFFFFFFFu, e0.y, m),
+                            __shfl_sync(0xFFFFFFFFu, e0.z, m), 0.0f),
+                make_float4(__shfl_sync(0xFFFFFFFFu, e1.x, m), __shfl_sync(0xFFFFFFFFu, e1.y, m),
+                            __shfl_sync(0xFFFFFFFFu, e1.z, m), 0.0f),
+                make_float4(__shfl_sync(0xFFFFFFFFu, e2.x, m), __shfl_sync(0xFFFFFFFFu, e2.y, m),
+                            __shfl_sync(0xFFFFFFFFu, e2.z, m), 0.0f));
+        int const tsx = __shfl_sync(0xFFFFFFFFu, sx, m), tsy = __shfl_sync(0xFFFFFFFFu, sy, m);
+        int const tw = __shfl_sync(0xFFFFFFFFu, w, m), tn = __shfl_sync(0xFFFFFFFFu, nt, m);
+        for (int j = lane; j < tn; j += 32) {
+          int x = tsx + j % tw, y = tsy + j / tw;
+          int const res = tt.test(x, y);
+          if (res) {
+            // the chunk's cursor of this tile: only this warp touches it; each
+            // tile appears once per triangle, and the __syncwarp below orders
+            // one step's update before the next step's read
+            uint32_t* cc = cnt + static_cast<size_t>(y * tgx + x) * nch;
+            uint32_t pos = *cc;
+            *cc = pos + 1;
+            if (pos < P.bin_capacity) P.bin_entries[pos] = (r << 1) | static_cast<uint32_t>(res & 1);
+          }
+        }
+        __syncwarp();
+      }
     }
   }
 }

@@ -205,6 +205,13 @@ class Device:
                                                         C.byref(t), C.byref(ms)))
         return {k: getattr(t, k) for k, _ in abi.Tuning._fields_}, ms.value
 
+    def autotune_space(self):
+        """sg_autotune_space: {field: candidate values}, in search order."""
+        knobs = C.POINTER(abi.TuningKnob)()
+        n = C.c_uint32()
+        self._check("sg_autotune_space", self.lib.sg_autotune_space(C.byref(knobs), C.byref(n)))
+        return {knobs[i].field.decode(): list(knobs[i].values[:knobs[i].count]) for i in range(n.value)}
+
     def af_make_textures(self, count, size=512, seed=1):
         """sg_af_make_textures: the learned filter's procedural training
         textures; returns their handles."""

@@ -369,6 +369,29 @@ def c2_scene(seed=20261204, width=1920, height=1080, samples=4, grid=317, tex_si
     return s
 
 
+def write_facade_input(scene, path):
+    """A c2_scene in the input format of the C++ facade application
+    tests/cpp/facade_scene.cpp: u32 magic 'SGFS', width, height, samples,
+    vertex count, index count, texture side, draw count; per draw u32
+    start, count, anisotropic; the 16 f32 of the MVP; the vertices (12 f32
+    each); the u32 indices; the RGBA8 texture."""
+    import struct
+    vb, ib = scene.buffers["vb"], scene.buffers["ib"]
+    tex = scene.textures["noise"][0]
+    draws = []
+    for d in scene.draws:
+        aniso = d["ps"]["program"] == abi.PS_TEX_GRAD_MODULATE
+        draws += [d["start"], d["prim_count"], int(aniso)]
+    with open(path, "wb") as f:
+        f.write(struct.pack("<8I", 0x53464753, scene.width, scene.height, scene.samples,
+                            vb.shape[0], ib.size, tex.shape[0], len(scene.draws)))
+        f.write(np.asarray(draws, np.uint32).tobytes())
+        f.write(np.asarray(scene.mvp, np.float32).tobytes())
+        f.write(vb.astype(np.float32).tobytes())
+        f.write(ib.astype(np.uint32).tobytes())
+        f.write(tex.astype(np.uint8).tobytes())
+
+
 def stencil_mirror_scene(seed=7, width=128, height=128, samples=1, ntris=40):
     """Stencil-mirror pattern: REPLACE the stencil under a quad, then draw
     reflected geometry with stencil EQUAL (StencilMirror.cpp:560-578)."""

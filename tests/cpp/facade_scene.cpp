@@ -5,12 +5,19 @@
 // input layout bound to the vertex shader's semantics, a src-alpha blend
 // shader, clear + draw_index + resolve, a pipeline_statistics query).
 //
-// usage: facade_scene <in.bin> <out.bin>
+// usage: facade_scene <in.bin> <out.bin> [frames warmup]
+//   With `frames`, renders `warmup` untimed frames and then `frames` timed
+//   ones (each: clears, the draws one draw_index call at a time, resolve,
+//   flush -- the calls a reference application makes per frame), and prints
+//   "facade_ms_per_frame <ms>": the wall time of each frame up to the end of
+//   its flush, with the 129 MB L2 flushed before it (a clear of a 256 MiB
+//   target, untimed).  The outputs are those of the last frame.
 //   in:  u32 magic 'SGFS', width, height, samples, nverts, nidx, tex_size,
 //        ndraws; per draw u32 start, count, aniso; 16 f32 MVP (row-major);
 //        nverts x 12 f32 (position, texcoord, colour); nidx u32; tex_size^2 RGBA8
 //   out: colour bytes, depth-stencil bytes, resolved bytes (if samples > 1),
 //        then u64 ia_primitives, cprimitives, ps_invocations, backend_input_pixels
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -47,7 +54,8 @@ int fail(char const* what, renderer_ptr const& r = nullptr) {
 }  // namespace
 
 int main(int argc, char** argv) {
-  if (argc != 3) return fail("usage: facade_scene in.bin out.bin");
+  if (argc != 3 && argc != 5) return fail("usage: facade_scene in.bin out.bin [frames warmup]");
+  int const frames = argc == 5 ? std::atoi(argv[3]) : 0, warmup = argc == 5 ? std::atoi(argv[4]) : 0;
   FILE* f = std::fopen(argv[1], "rb");
   if (!f) return fail("cannot open input");
   uint32_t hdr[8];
@@ -123,21 +131,41 @@ int main(int argc, char** argv) {
 
   async_object_ptr q = rend->create_query(async_object_ids::pipeline_statistics);
   async_object_ptr qi = rend->create_query(async_object_ids::internal_statistics);
-  rend->clear_color(color, color_rgba32f(0.1f, 0.2f, 0.3f, 1.0f));
-  rend->clear_depth_stencil(ds, clear_depth | clear_stencil, 1.0f, 0);
-  rend->begin(q);
-  rend->begin(qi);
-  for (uint32_t i = 0; i < ndraws; ++i) {
-    rend->set_pixel_shader(draws[3 * i + 2] ? cpp_pixel_shader_ptr(ps_af) : cpp_pixel_shader_ptr(ps_tri));
-    if (rend->draw_index(draws[3 * i], draws[3 * i + 1], 0) != result::ok) return fail("draw_index", rend);
+  auto frame = [&]() -> int {
+    rend->clear_color(color, color_rgba32f(0.1f, 0.2f, 0.3f, 1.0f));
+    rend->clear_depth_stencil(ds, clear_depth | clear_stencil, 1.0f, 0);
+    rend->begin(q);
+    rend->begin(qi);
+    for (uint32_t i = 0; i < ndraws; ++i) {
+      rend->set_pixel_shader(draws[3 * i + 2] ? cpp_pixel_shader_ptr(ps_af) : cpp_pixel_shader_ptr(ps_tri));
+      if (rend->draw_index(draws[3 * i], draws[3 * i + 1], 0) != result::ok) return fail("draw_index", rend);
+    }
+    rend->end(q);
+    rend->end(qi);
+    if (resolved_tex) {
+      surface_ptr rs = resolved_tex->subresource(0);
+      if (color->resolve(*rs) != result::ok) return fail("resolve", rend);
+    }
+    if (rend->flush() != result::ok) return fail("flush", rend);
+    return 0;
+  };
+  if (frames > 0) {
+    texture_ptr l2 = rend->create_tex2d(8192, 8192, 1, pixel_format_color_rgba8);  // 256 MiB
+    if (!l2) return fail("create_tex2d", rend);
+    surface_ptr l2s = l2->subresource(0);
+    double total = 0.0;
+    for (int i = 0; i < warmup + frames; ++i) {
+      rend->clear_color(l2s, color_rgba32f(0.0f, 0.0f, 0.0f, 0.0f));
+      if (rend->flush() != result::ok) return fail("flush", rend);
+      auto t0 = std::chrono::steady_clock::now();
+      if (frame()) return 1;
+      auto t1 = std::chrono::steady_clock::now();
+      if (i >= warmup) total += std::chrono::duration<double, std::milli>(t1 - t0).count();
+    }
+    std::printf("facade_ms_per_frame %.6f\n", total / frames);
+  } else if (frame()) {
+    return 1;
   }
-  rend->end(q);
-  rend->end(qi);
-  if (resolved_tex) {
-    surface_ptr rs = resolved_tex->subresource(0);
-    if (color->resolve(*rs) != result::ok) return fail("resolve", rend);
-  }
-  if (rend->flush() != result::ok) return fail("flush", rend);
   pipeline_statistics ps{};
   internal_statistics is{};
   if (rend->get_data(q, &ps, false) != async_status::ready || rend->get_data(qi, &is, false) != async_status::ready)

@@ -65,3 +65,17 @@ def test_empty_draw_is_a_no_op(oracle_lib):
     out = scenes.render(dev, s, stats=True)
     assert out["stats"][0]["ps_invocations"] == 0
     assert not out["color"].any()
+
+
+def test_autotune_space_names_tuning_fields(product_lib):
+    """sg_autotune_space needs no device: every searched knob is a field of
+    sg_tuning with at least two candidates."""
+    lib = abi.bind(product_lib)
+    knobs = ctypes.POINTER(abi.TuningKnob)()
+    n = ctypes.c_uint32()
+    assert lib.sg_autotune_space(ctypes.byref(knobs), ctypes.byref(n)) == abi.SG_OK
+    fields = {f for f, _ in abi.Tuning._fields_}
+    names = [knobs[i].field.decode() for i in range(n.value)]
+    assert set(names) <= fields and len(names) == len(set(names)) == 8
+    assert all(2 <= knobs[i].count <= 8 for i in range(n.value))
+    assert "shade_quads_per_warp" not in names and "bin_capacity" not in names

@@ -26,20 +26,7 @@ def facade_scene():
 
 
 def write_input(scene, path):
-    vb, ib = scene.buffers["vb"], scene.buffers["ib"]
-    tex = scene.textures["noise"][0]
-    draws = []
-    for d in scene.draws:
-        aniso = d["ps"]["program"] == abi.PS_TEX_GRAD_MODULATE
-        draws += [d["start"], d["prim_count"], int(aniso)]
-    with open(path, "wb") as f:
-        f.write(struct.pack("<8I", 0x53464753, scene.width, scene.height, scene.samples,
-                            vb.shape[0], ib.size, tex.shape[0], len(scene.draws)))
-        f.write(np.asarray(draws, np.uint32).tobytes())
-        f.write(np.asarray(scene.mvp, np.float32).tobytes())
-        f.write(vb.astype(np.float32).tobytes())
-        f.write(ib.astype(np.uint32).tobytes())
-        f.write(tex.astype(np.uint8).tobytes())
+    scenes.write_facade_input(scene, path)
 
 
 def build_facade(lib_path, out_dir, src=SRC):
