@@ -575,47 +575,6 @@ __device__ __forceinline__ v4 surface_bilinear_wrap8(dev_sampler const& s, int l
   return lerp_2d_unorm8(s.fmt == SG_FMT_RGBA8, texel(x0, y0), texel(x1, y0), texel(x0, y1), texel(x1, y1), tx, ty);
 }
 
-// surface_bilinear_wrap8 in two phases, so that a caller can issue the
-// loads of several lookups before interpolating any: the texel offsets and
-// fractions (false where the reference's addressing leaves the surface:
-// such a lookup takes surface_bilinear_wrap8), then the four texels.
-struct Wrap8Tap {
-  uint32_t o00, o10, o01, o11;  // byte offsets of the four texels
-  float tx, ty;
-};
-__device__ __forceinline__ bool wrap8_tap(dev_level const& lv, float x, float y, Wrap8Tap& t) {
-  int const w = lv.w, h = lv.h;
-  int x0, x1, y0, y1;
-  wrap_linear(x, w, x0, x1, t.tx);
-  wrap_linear(y, h, y0, y1, t.ty);
-  bool const ok = x0 >= 0 && x1 >= 0 && y0 >= 0 && y1 >= 0 && x0 < w && x1 < w && y0 < h && y1 < h;
-  uint32_t const r0 = static_cast<uint32_t>(ok ? y0 : 0) * static_cast<uint32_t>(w);
-  uint32_t const r1 = static_cast<uint32_t>(ok ? y1 : 0) * static_cast<uint32_t>(w);
-  uint32_t const c0 = static_cast<uint32_t>(ok ? x0 : 0), c1 = static_cast<uint32_t>(ok ? x1 : 0);
-  t.o00 = (r0 + c0) * 4u;
-  t.o10 = (r0 + c1) * 4u;
-  t.o01 = (r1 + c0) * 4u;
-  t.o11 = (r1 + c1) * 4u;
-  return ok;
-}
-struct Wrap8Texels {
-  uint32_t a, b, c, d;
-};
-__device__ __forceinline__ Wrap8Texels wrap8_load(uint8_t const* data, Wrap8Tap const& t) {
-  return {__ldg(reinterpret_cast<uint32_t const*>(data + t.o00)), __ldg(reinterpret_cast<uint32_t const*>(data + t.o10)),
-          __ldg(reinterpret_cast<uint32_t const*>(data + t.o01)), __ldg(reinterpret_cast<uint32_t const*>(data + t.o11))};
-}
-// lerp_2d_unorm8 on loaded texels
-__device__ __forceinline__ v4 wrap8_lerp(bool rgba, Wrap8Texels const& q, float tx, float ty) {
-  auto cv = [&](uint32_t u) {
-    float x = static_cast<float>(u & 0xFF), y = static_cast<float>((u >> 8) & 0xFF),
-          z = static_cast<float>((u >> 16) & 0xFF), w = static_cast<float>(u >> 24);
-    return rgba ? mk4(x, y, z, w) : mk4(z, y, x, w);
-  };
-  v4 r = lerp4(cv(q.a), cv(q.b), cv(q.c), cv(q.d), tx, ty);
-  return r * (1.0f / 255);
-}
-
 // One surface lookup of sample_impl; WRAP8: the sampler is in wrap8_state.
 template <bool WRAP8>
 __device__ __forceinline__ v4 surface_lookup(dev_sampler const& s, int level, float x, float y, uint32_t filter) {
@@ -642,19 +601,8 @@ __device__ __forceinline__ v4 sample_impl_t(dev_sampler const& s, float cx, floa
     int hi = lo + 1;
     float frac = miplevel - static_cast<float>(lo);
     int lc = iclamp(lo, max_lod, min_lod), hc = iclamp(hi, max_lod, min_lod);
-    v4 c0, c1;
-    Wrap8Tap t0, t1;
-    if (WRAP8 && s.min_filter == SG_FILTER_LINEAR && wrap8_tap(s.lv[lc], cx, cy, t0) &&
-        wrap8_tap(s.lv[hc], cx, cy, t1)) {
-      // both levels' texels in flight together
-      Wrap8Texels const q0 = wrap8_load(s.lv[lc].data, t0), q1 = wrap8_load(s.lv[hc].data, t1);
-      bool const rgba = s.fmt == SG_FMT_RGBA8;
-      c0 = wrap8_lerp(rgba, q0, t0.tx, t0.ty);
-      c1 = wrap8_lerp(rgba, q1, t1.tx, t1.ty);
-    } else {
-      c0 = surface_lookup<WRAP8>(s, lc, cx, cy, s.min_filter);
-      c1 = surface_lookup<WRAP8>(s, hc, cx, cy, s.min_filter);
-    }
+    v4 c0 = surface_lookup<WRAP8>(s, lc, cx, cy, s.min_filter);
+    v4 c1 = surface_lookup<WRAP8>(s, hc, cx, cy, s.min_filter);
     return mk4(lerp1(c0.x, c1.x, frac), lerp1(c0.y, c1.y, frac), lerp1(c0.z, c1.z, frac), lerp1(c0.w, c1.w, frac));
   }
   float start = -0.5f * (af->probe_count - 1.0f);
@@ -666,49 +614,6 @@ __device__ __forceinline__ v4 sample_impl_t(dev_sampler const& s, float cx, floa
   v4 color = mk4(0, 0, 0, 0);
   float wsum = 0.0f;
   int pc = static_cast<int>(af->probe_count);
-  if (WRAP8 && s.min_filter == SG_FILTER_LINEAR) {
-    // the probes two at a time, both probes' texels in flight together; the
-    // positions, weights and sums in the reference's order
-    dev_level const lv = s.lv[lvl];
-    bool const rgba = s.fmt == SG_FMT_RGBA8;
-    int i = -pc + 1;
-    for (; i + 2 < pc; i += 4) {
-      float const x0 = sx, y0 = sy;
-      sx += af->du;
-      sy += af->dv;
-      float const x1 = sx, y1 = sy;
-      sx += af->du;
-      sy += af->dv;
-      Wrap8Tap t0, t1;
-      v4 c0, c1;
-      if (wrap8_tap(lv, x0, y0, t0) && wrap8_tap(lv, x1, y1, t1)) {
-        Wrap8Texels const q0 = wrap8_load(lv.data, t0), q1 = wrap8_load(lv.data, t1);
-        c0 = wrap8_lerp(rgba, q0, t0.tx, t0.ty);
-        c1 = wrap8_lerp(rgba, q1, t1.tx, t1.ty);
-      } else {
-        c0 = surface_bilinear_wrap8(s, lvl, x0, y0);
-        c1 = surface_bilinear_wrap8(s, lvl, x1, y1);
-      }
-      int const w0i = static_cast<int>(static_cast<float>(i * i) * af->weight_D);
-      float const w0 = c_ewa[w0i < 0 ? 0 : (w0i > 255 ? 255 : w0i)];
-      color = color + c0 * w0;
-      wsum += w0;
-      int const i1 = i + 2;
-      int const w1i = static_cast<int>(static_cast<float>(i1 * i1) * af->weight_D);
-      float const w1 = c_ewa[w1i < 0 ? 0 : (w1i > 255 ? 255 : w1i)];
-      color = color + c1 * w1;
-      wsum += w1;
-    }
-    if (i < pc) {  // an odd probe count's last probe
-      v4 c0 = surface_bilinear_wrap8(s, lvl, sx, sy);
-      int widx = static_cast<int>(static_cast<float>(i * i) * af->weight_D);
-      float w = c_ewa[widx < 0 ? 0 : (widx > 255 ? 255 : widx)];
-      color = color + c0 * w;
-      wsum += w;
-    }
-    float inv = 1.0f / wsum;
-    return color * inv;
-  }
   for (int i = -pc + 1; i < pc; i += 2) {
     v4 c0 = surface_lookup<WRAP8>(s, lvl, sx, sy, s.min_filter);
     int widx = static_cast<int>(static_cast<float>(i * i) * af->weight_D);
