@@ -45,6 +45,22 @@ __device__ inline int fast_roundi(double d) { return static_cast<int>(floor(d + 
 #define SG_ROUND_EPS (static_cast<double>(0.5f) - 1.5e-8)
 __device__ inline int fast_floori(double d) { return fast_roundi(d - SG_ROUND_EPS); }
 __device__ inline int fast_ceili(double d) { return fast_roundi(d + SG_ROUND_EPS); }
+// The same three of a float argument (the reference widens it to double)
+// without FP64 arithmetic, which is slow on this part.  Equal as values for
+// every float (all 2^32 checked against the double forms):
+// floor(double(f) + 0.5) is floor of f + 0.5 rounded down in float; the
+// floori form is floor(f) except on [-0x1.01b2b2p-26, 0), where the bias
+// lifts it to 0; the ceili form is ceil(f) except on (0, 0x1.01b2b2p-26],
+// where it drops to 0, for |f| < 2^26 -- above that the double sum rounds
+// the bias and the double form is kept.
+__device__ inline int fast_roundi_f(float f) { return static_cast<int>(floorf(__fadd_rd(f, 0.5f))); }
+__device__ inline int fast_floori_f(float f) {
+  return (f < 0.0f && f >= -0x1.01b2b2p-26f) ? 0 : static_cast<int>(floorf(f));
+}
+__device__ inline int fast_ceili_f(float f) {
+  if (!(fabsf(f) < 0x1p26f)) return fast_ceili(static_cast<double>(f));
+  return (f > 0.0f && f <= 0x1.01b2b2p-26f) ? 0 : static_cast<int>(ceilf(f));
+}
 __device__ inline float fast_log2(float val) {  // math.h:89-105
   int32_t x = __float_as_int(val);
   int log_2 = ((x >> 23) & 255) - 128;
@@ -63,12 +79,17 @@ __device__ inline int32_t cvt_rne(float f) {
   if (!(f > -2147483904.0f && f < 2147483648.0f)) return INT32_MIN;
   return __float2int_rn(f);
 }
-// vector_::length: sqrt in double of the float sum of squares (vector_generic.h:118-126)
+// vector_::length: sqrt in double of the float sum of squares
+// (vector_generic.h:118-126).  The double square root rounded to float is
+// the correctly rounded float square root (53 >= 2 * 24 + 2 bits: rounding
+// twice is innocuous for sqrt; all 2^31 non-negative floats checked), so
+// the float one is taken.
+__device__ inline float len_sqrt(float t) { return __fsqrt_rn(t); }
 __device__ inline float len2(float x, float y) {
   float t = 0.0f;
   t += x * x;
   t += y * y;
-  return static_cast<float>(sqrt(static_cast<double>(t)));
+  return len_sqrt(t);
 }
 
 struct v4 {
@@ -301,7 +322,7 @@ __device__ inline void wrap_linear(float coord, int size, int& lo, int& hi, floa
   hi = cvtt(a1 - d1 * fs);
 }
 __device__ inline void mirror_linear(float coord, int size, int& lo, int& hi, float& frac) {
-  int sel = fast_floori(coord);
+  int sel = fast_floori_f(coord);
   float o = ((sel & 1) ? static_cast<float>(1 + sel) - coord : coord - static_cast<float>(sel)) *
                 static_cast<float>(size) - 0.5f;
   float ip = static_cast<float>(cvtt(o));
@@ -348,7 +369,7 @@ __device__ inline int wrap_point(float coord, int size) {
   return cvtt(a - dv * fs);
 }
 __device__ inline int mirror_point(float coord, int size) {
-  int sel = fast_floori(coord);
+  int sel = fast_floori_f(coord);
   float o = ((sel & 1) ? static_cast<float>(1 + sel) - coord : coord - static_cast<float>(sel)) *
             static_cast<float>(size);
   float ip = static_cast<float>(cvtt(o));
@@ -379,7 +400,7 @@ __device__ inline float coordf(uint32_t mode, float coord, int size) {
   switch (mode) {
   case SG_ADDRESS_WRAP: return (coord - fast_floor(coord)) * fs - 0.5f;
   case SG_ADDRESS_MIRROR: {
-    int sel = fast_floori(coord);
+    int sel = fast_floori_f(coord);
     return ((sel & 1) ? static_cast<float>(1 + sel) - coord : coord - static_cast<float>(sel)) * fs - 0.5f;
   }
   case SG_ADDRESS_CLAMP: return sclamp(coord * fs, 0.5f, fs - 0.5f) - 0.5f;
@@ -419,8 +440,8 @@ static __device__ __noinline__ v4 sample_surface(dev_sampler const& s, int level
       if (0 <= ix && ix < w && 0 <= iy && iy < h) return read_texel(s.fmt, texel(ix, iy));
       return border_color(s);
     }
-    ix = coordi_1d(mu, fast_floori(coordf(mu, x, w) + 0.5f), w);
-    iy = coordi_1d(mv, fast_floori(coordf(mv, y, h) + 0.5f), h);
+    ix = coordi_1d(mu, fast_floori_f(coordf(mu, x, w) + 0.5f), w);
+    iy = coordi_1d(mv, fast_floori_f(coordf(mv, y, h) + 0.5f), h);
     if (ix < 0 || iy < 0 || ix >= w || iy >= h) return border_color(s);
     return read_texel(s.fmt, texel(ix, iy));
   }
@@ -435,12 +456,12 @@ static __device__ __noinline__ v4 sample_surface(dev_sampler const& s, int level
     }
   } else {
     float ox = coordf(mu, x, w);
-    int ixp = fast_floori(ox);
+    int ixp = fast_floori_f(ox);
     x0 = coordi_1d(mu, ixp, w);
     x1 = coordi_1d(mu, ixp + 1, w);
     tx = ox - static_cast<float>(ixp);
     float oy = coordf(mv, y, h);
-    int iyp = fast_floori(oy);
+    int iyp = fast_floori_f(oy);
     y0 = coordi_1d(mv, iyp, h);
     y1 = coordi_1d(mv, iyp + 1, h);
     ty = oy - static_cast<float>(iyp);
@@ -495,8 +516,8 @@ __device__ inline float calc_lod(dev_sampler const& s, float dxu, float dxv, flo
     t1 += dyt0 * dyt0;
     t1 += dyt1 * dyt1;
     t1 += dyz * dyz;
-    float lx = static_cast<float>(sqrt(static_cast<double>(t0)));
-    float ly = static_cast<float>(sqrt(static_cast<double>(t1)));
+    float lx = len_sqrt(t0);
+    float ly = len_sqrt(t1);
     rho = smax(lx, ly);
   }
   if (rho == 0.0f) rho = 0.000001f;
@@ -589,7 +610,7 @@ __device__ __forceinline__ v4 sample_impl_t(dev_sampler const& s, float cx, floa
   bool is_mag = (s.mip_filter == SG_FILTER_POINT) ? (miplevel < 0.5f) : (miplevel < 0.0f);
   if (is_mag) return surface_lookup<WRAP8>(s, max_lod, cx, cy, s.mag_filter);
   if (s.mip_filter == SG_FILTER_POINT) {
-    int ml = fast_floori(0.5 + static_cast<double>(miplevel));
+    int ml = fast_roundi_f(miplevel);  // floor(0.5 + m) with the floori bias: equal for every float
     ml = iclamp(ml, max_lod, min_lod);
     return surface_lookup<WRAP8>(s, ml, cx, cy, s.min_filter);
   }
@@ -597,7 +618,7 @@ __device__ __forceinline__ v4 sample_impl_t(dev_sampler const& s, float cx, floa
   // on an anisotropic sampler takes the linear mip path: the reference reads
   // the absent parameters there (sampler.cpp:730-755)
   if (s.mip_filter == SG_FILTER_LINEAR || !af) {
-    int lo = fast_floori(static_cast<double>(miplevel));
+    int lo = fast_floori_f(miplevel);
     int hi = lo + 1;
     float frac = miplevel - static_cast<float>(lo);
     int lc = iclamp(lo, max_lod, min_lod), hc = iclamp(hi, max_lod, min_lod);
@@ -608,7 +629,7 @@ __device__ __forceinline__ v4 sample_impl_t(dev_sampler const& s, float cx, floa
   float start = -0.5f * (af->probe_count - 1.0f);
   float sx = cx + af->du * start;
   float sy = cy + af->dv * start;
-  int lo = fast_roundi(static_cast<double>(miplevel));
+  int lo = fast_roundi_f(miplevel);
   // clamp(size_t(lo), max_lod, min_lod): a negative lo becomes a huge size_t
   int lvl = lo < 0 ? min_lod : (lo > min_lod ? min_lod : lo);
   v4 color = mk4(0, 0, 0, 0);
@@ -689,7 +710,7 @@ __device__ inline v4 sample_cube(dev_sampler const& s, float x, float y, float z
   if (is_mag) return surface_lookup<false>(s, face, sc, tc, s.mag_filter);
   v4 const c0 = surface_lookup<false>(s, face, sc, tc, s.min_filter);
   if (s.mip_filter == SG_FILTER_POINT) return c0;
-  float const frac = miplevel - static_cast<float>(fast_floori(static_cast<double>(miplevel)));
+  float const frac = miplevel - static_cast<float>(fast_floori_f(miplevel));
   return mk4(lerp1(c0.x, c0.x, frac), lerp1(c0.y, c0.y, frac), lerp1(c0.z, c0.z, frac), lerp1(c0.w, c0.w, frac));
 }
 

@@ -427,10 +427,10 @@ __global__ void __launch_bounds__(128) k_bin(PassParams P) {
       float4 bb = R[3];
       DrawParams const& D = P.draws[rec_draw(R)];
       int const tx_n = D.tiles_x, ty_n = D.tiles_y;
-      sx = min(fast_floori(static_cast<double>(smax(0.0f, bb.x) / TILE)), tx_n);
-      sy = min(fast_floori(static_cast<double>(smax(0.0f, bb.z) / TILE)), ty_n);
-      ex = min(fast_ceili(static_cast<double>(smax(0.0f, bb.y) / TILE)) + 1, tx_n);
-      ey = min(fast_ceili(static_cast<double>(smax(0.0f, bb.w) / TILE)) + 1, ty_n);
+      sx = min(fast_floori_f(smax(0.0f, bb.x) / TILE), tx_n);
+      sy = min(fast_floori_f(smax(0.0f, bb.z) / TILE), ty_n);
+      ex = min(fast_ceili_f(smax(0.0f, bb.y) / TILE) + 1, tx_n);
+      ey = min(fast_ceili_f(smax(0.0f, bb.w) / TILE) + 1, ty_n);
       // finite inputs always land in [0, n]; the clamps only bound non-finite ones
       sx = max(sx, 0);
       sy = max(sy, 0);

@@ -58,7 +58,7 @@ __device__ inline void af_features_from(dev_sampler const& s, float u, float v, 
   f[5] = log2f(fmaxf(lmax, 1.0f)) * 0.125f;
   f[6] = af.probe_count * 0.0625f;
   f[7] = log2f(fmaxf(lmax / lmin, 1.0f)) * 0.25f;
-  int const lo = fast_roundi(static_cast<double>(af.lod));
+  int const lo = fast_roundi_f(af.lod);
   int const min_lod = s.nlevels - 1;
   int const lvl = lo < 0 ? 0 : (lo > min_lod ? min_lod : lo);
   float const span = fmaxf(af.probe_count - 1.0f, 0.0f);
