@@ -53,11 +53,46 @@ enum {
 
 /* ---- enumerations (reference numeric values) ----------------------------- */
 /* primitive_topology (constants.h:44-52) */
-enum { SG_TOPOLOGY_TRIANGLE_LIST = 2, SG_TOPOLOGY_TRIANGLE_STRIP = 4 };
+enum {
+  SG_TOPOLOGY_LINE_LIST = 0, SG_TOPOLOGY_LINE_STRIP = 1,
+  SG_TOPOLOGY_TRIANGLE_LIST = 2, SG_TOPOLOGY_TRIANGLE_STRIP = 4
+};
 /* cull_mode (constants.h:58-63) */
 enum { SG_CULL_NONE = 0, SG_CULL_FRONT = 1, SG_CULL_BACK = 2 };
-/* fill_mode */
+/* fill_mode (constants.h:66-70) */
 enum { SG_FILL_WIREFRAME = 0, SG_FILL_SOLID = 1 };
+
+/* Lines and wireframe.  The reference declares line topologies and
+ * fill_wireframe but stops at ef_unimplemented (rasterizer.cpp:1019-1060,
+ * clipper.cpp:39-41); its rasterize_line (rasterizer.cpp:60-213) holds the
+ * intended DDA.  This library defines them as follows.
+ *   - Assembly: a line list takes vertices (2p, 2p + 1) for primitive p, a
+ *     strip (p, p + 1), through the index buffer as triangles do.  A
+ *     triangle topology with SG_FILL_WIREFRAME is assembled, clipped and
+ *     culled as a solid triangle; each triangle it yields is drawn as its
+ *     three edges (a, b), (b, c), (c, a).
+ *   - Clipping: a segment is cut at z >= 0, then at z <= w, the outside end
+ *     replaced by lerp(inside, outside, d_in / (d_in - d_out)), as the
+ *     triangle clipper does; lines are not culled.
+ *   - Rasterization: rasterize_line's DDA over the draw's viewport within
+ *     the render area, every pixel once: along the major axis (x when
+ *     |dx| > |dy|), from the end with the smaller coordinate, the pixels
+ *     i in [fast_floori(fast_floor(start + 0.5)), fast_floori(end - 0.5)),
+ *     both ends clamped to the viewport's [lo, hi] (rasterize_line clamps
+ *     the start to hi - 1, which would add an extrapolated pixel to a line
+ *     starting past the far edge); pixel i takes the endpoints' registers
+ *     lerped at t = (i + 0.5 - start) / (end - start), its minor
+ *     coordinate floori(t-lerped minor) (pixels outside the viewport are
+ *     skipped), depth the lerped z, attributes unprojected by the lerped w.
+ *   - Pixel shading: once per pixel; ddx / ddy of an attribute are its
+ *     values at the lerped registers plus the line's ddx / ddy (rasterize_
+ *     line's diff * (diff.x / |diff.xy|^2), diff * (diff.y / |diff.xy|^2))
+ *     minus its value at the pixel.  User pixel and blend shaders are not
+ *     taken (SG_INVALID_PARAMETER); learned-filter draws sample plainly.
+ *   - Output: sample 0 of the pixel (render_sample(..., 0, ...)), with the
+ *     depth and stencil tests after shading and the front-face stencil
+ *     state.  Pipeline counters: cprimitives counts the segments drawn,
+ *     ps_invocations and backend_input_pixels the pixels shaded. */
 /* compare_function (constants.h:143-152) */
 enum {
   SG_CMP_NEVER = 0, SG_CMP_LESS = 1, SG_CMP_EQUAL = 2, SG_CMP_LESS_EQUAL = 3,
@@ -242,7 +277,7 @@ typedef struct sg_viewport {           /* salvia/include/salvia/core/viewport.h 
 } sg_viewport;
 
 typedef struct sg_raster_desc {        /* raster_state.h:17-40 */
-  uint32_t fill_mode;                  /* SG_FILL_SOLID */
+  uint32_t fill_mode;                  /* SG_FILL_SOLID, or SG_FILL_WIREFRAME for triangle topologies */
   uint32_t cull_mode;                  /* SG_CULL_* */
   uint32_t front_ccw;
   uint32_t reserved;
@@ -325,7 +360,7 @@ typedef struct sg_draw_desc {
 /* Pipeline counters of one draw (async_object.h:90-175). */
 typedef struct sg_draw_stats {
   uint64_t ia_primitives;              /* input primitives */
-  uint64_t cprimitives;                /* triangles after clipping and culling */
+  uint64_t cprimitives;                /* triangles after clipping and culling (lines: segments drawn) */
   uint64_t ps_invocations;             /* pixel-shader invocations, helpers included */
   uint64_t backend_input_pixels;       /* pixels of quads that reached the output merger */
   /* vertices the input assembler fetched: three per primitive for lists and

@@ -47,7 +47,12 @@ enum map_mode {
   map_mode_none = 0, map_read = 1, map_write = 2, map_read_write = 3, map_write_discard = 4,
   map_write_no_overwrite = 5
 };
-enum primitive_topology { primitive_triangle_list = 2, primitive_triangle_strip = 4 };
+enum primitive_topology {
+  primitive_line_list = 0,
+  primitive_line_strip = 1,
+  primitive_triangle_list = 2,
+  primitive_triangle_strip = 4
+};
 enum cull_mode { cull_none = 0, cull_front = 1, cull_back = 2 };
 enum fill_mode { fill_wireframe = 0, fill_solid = 1 };
 enum address_mode { address_wrap = 0, address_mirror = 1, address_clamp = 2, address_border = 3 };

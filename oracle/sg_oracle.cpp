@@ -915,7 +915,12 @@ void run_vs(draw_ctx const& c, uint32_t index, vso& out) {
 void fetch_indexes(draw_ctx const& c, uint32_t prim, uint32_t out[3]) {
   sg_draw_desc const& d = *c.d;
   uint32_t ids[3];
-  if (d.topology == SG_TOPOLOGY_TRIANGLE_STRIP) {
+  if (d.topology == SG_TOPOLOGY_LINE_LIST || d.topology == SG_TOPOLOGY_LINE_STRIP) {
+    // index_fetcher.cpp:53-60; the third index is unused
+    ids[0] = d.topology == SG_TOPOLOGY_LINE_LIST ? prim * 2 : prim;
+    ids[1] = ids[0] + 1;
+    ids[2] = ids[1];
+  } else if (d.topology == SG_TOPOLOGY_TRIANGLE_STRIP) {
     ids[0] = prim + 0;
     ids[1] = prim + 1;
     ids[2] = prim + 2;
@@ -1795,12 +1800,124 @@ void rasterize_triangle(rasterizer_state& rs, uint32_t entry, float tile_x, floa
   }
 }
 
+// ---------------------------------------------------------------------------
+// Lines and wireframe (the header's definition; the reference stops at
+// ef_unimplemented, its rasterize_line in rasterizer.cpp:60-213 holds the
+// intended DDA).
+
+// A segment cut at z >= 0, then at z <= w; false when nothing is left.
+bool clip_line(draw_ctx const& c, vso*& a, vso*& b, std::vector<std::unique_ptr<vso>>& pool) {
+  for (int p = 0; p < 2; ++p) {
+    float da = clip_dot(p, a->pos()), db = clip_dot(p, b->pos());
+    if (da < 0.0f && db < 0.0f) return false;
+    if (da >= 0.0f && db < 0.0f) {
+      pool.push_back(std::make_unique<vso>());
+      vso_lerp(c, *pool.back(), *a, *b, da / (da - db));
+      b = pool.back().get();
+    } else if (da < 0.0f && db >= 0.0f) {
+      pool.push_back(std::make_unique<vso>());
+      vso_lerp(c, *pool.back(), *b, *a, db / (db - da));
+      a = pool.back().get();
+    }
+  }
+  return true;
+}
+
+// unproject_n (shader.cpp:136-160)
+void unproject(draw_ctx const& c, vso& out, vso const& in) {
+  float inv_w = 1.0f / in.pos()[3];
+  out.pos() = in.pos();
+  for (uint32_t i = 0; i < c.nattr; ++i)
+    out.r[1 + i] = (c.mods[i] & SG_AM_NOPERSPECTIVE) ? in.r[1 + i] : mul(in.r[1 + i], inv_w);
+}
+
+// lerp_n on every register (shader.cpp:171-180)
+void lerp_regs(draw_ctx const& c, vso& out, vso const& a, vso const& b, float t) { vso_lerp(c, out, a, b, t); }
+
+// rasterizer::rasterize_line over the draw's viewport within the render area.
+void rasterize_line(rasterizer_state& rs, vso const& v0, vso const& v1) {
+  draw_ctx const& c = *rs.c;
+  int const nreg = 1 + static_cast<int>(c.nattr);
+  vso diff;
+  for (auto& r : diff.r) r = mk(0, 0, 0, 0);
+  for (int i = 0; i < nreg; ++i) diff.r[i] = sub(v1.r[i], v0.r[i]);
+  vec4 const dir = diff.pos();
+  float const len_sqr = dir[0] * dir[0] + dir[1] * dir[1];
+  vso ddx, ddy;
+  float const fx = dir[0] / len_sqr, fy = dir[1] / len_sqr;
+  for (int i = 0; i < nreg; ++i) {
+    ddx.r[i] = mul(diff.r[i], fx);
+    ddy.r[i] = mul(diff.r[i], fy);
+  }
+  sg_viewport const& vp = c.d->viewport;
+  int const left = fast_floori(std::max(0.0f, vp.x)), top = fast_floori(std::max(0.0f, vp.y));
+  int const right = fast_floori(std::min(vp.x + vp.w, c.target_w));
+  int const bottom = fast_floori(std::min(vp.y + vp.h, c.target_h));
+  if (right <= left || bottom <= top) return;
+  bool const xmaj = std::fabs(dir[0]) > std::fabs(dir[1]);
+  int const ax = xmaj ? 0 : 1, bx = xmaj ? 1 : 0;  // major and minor axis
+  float diff_dir = xmaj ? dir[0] : dir[1];
+  vso const* start = &v0;
+  vso const* end = &v1;
+  if (diff_dir < 0) {
+    start = &v1;
+    end = &v0;
+    diff_dir = -diff_dir;
+  }
+  int const lo = xmaj ? left : top, hi = xmaj ? right : bottom;
+  int const mlo = xmaj ? top : left, mhi = xmaj ? bottom : right;
+  float const fs = fast_floor(start->pos()[ax] + 0.5f);
+  int sx = fast_floori(fs);
+  int ex = fast_floori(end->pos()[ax] - 0.5f);
+  // clamped to the viewport (rasterize_line clamps the start to hi - 1, which
+  // would draw one extrapolated pixel of a line that starts past the right
+  // or bottom edge; here such a line draws nothing there)
+  sx = std::min(std::max(sx, lo), hi);
+  ex = std::min(std::max(ex, lo), hi);
+  vec4 more[SG_MAX_COLOR_TARGETS - 1];
+  for (int i = sx; i < ex; ++i) {
+    float const step = static_cast<float>(i) + 0.5f - start->pos()[ax];
+    vso px;
+    for (auto& r : px.r) r = mk(0, 0, 0, 0);
+    lerp_regs(c, px, *start, *end, step / diff_dir);
+    float const m = px.pos()[bx];
+    if (m >= static_cast<float>(mhi) || m < static_cast<float>(mlo)) continue;
+    int const mi = fast_floori(m);
+    if (mi >= mhi) continue;
+    // the pixel, and the pixel moved by ddx / ddy, unprojected (the
+    // attribute differences are the pixel shader's ddx / ddy)
+    vso q[4], sx_, sy_;
+    for (int k = 0; k < nreg; ++k) {
+      bool const flat = k > 0 && (c.mods[k - 1] & SG_AM_NOINTERPOLATION);  // no derivative
+      sx_.r[k] = flat ? px.r[k] : add(px.r[k], ddx.r[k]);
+      sy_.r[k] = flat ? px.r[k] : add(px.r[k], ddy.r[k]);
+    }
+    unproject(c, q[0], px);
+    unproject(c, q[1], sx_);
+    unproject(c, q[2], sy_);
+    q[3] = q[0];
+    vec4 out;
+    float lod = 0;
+    bool have = false;
+    bool keep = run_ps(c, q, 0, out, more, lod, have);
+    ++rs.st->ps_invocations;
+    ++rs.st->backend_input_pixels;
+    if (!keep) continue;
+    size_t const x = static_cast<size_t>(xmaj ? i : mi), y = static_cast<size_t>(xmaj ? mi : i);
+    render_sample(rs, x, y, 0, out, px.pos()[2], true, more);
+  }
+}
+
 int32_t do_draw(device_state* dev, sg_draw_desc const* d, sg_draw_stats* stats_out) {
   draw_ctx c;
   c.dev = dev;
   c.d = d;
-  if (d->raster.fill_mode != SG_FILL_SOLID) return SG_INVALID_PARAMETER;
-  if (d->topology != SG_TOPOLOGY_TRIANGLE_LIST && d->topology != SG_TOPOLOGY_TRIANGLE_STRIP)
+  bool const lines = d->topology == SG_TOPOLOGY_LINE_LIST || d->topology == SG_TOPOLOGY_LINE_STRIP;
+  if (!lines && d->topology != SG_TOPOLOGY_TRIANGLE_LIST && d->topology != SG_TOPOLOGY_TRIANGLE_STRIP)
+    return SG_INVALID_PARAMETER;
+  if (d->raster.fill_mode != SG_FILL_SOLID && d->raster.fill_mode != SG_FILL_WIREFRAME) return SG_INVALID_PARAMETER;
+  bool const wire = !lines && d->raster.fill_mode == SG_FILL_WIREFRAME;
+  if ((lines || wire) && (d->ps.program >= SG_USER_PROGRAM_BASE || d->bs.program >= SG_USER_PROGRAM_BASE))
     return SG_INVALID_PARAMETER;
   if (d->num_varyings > SG_MAX_VARYINGS || d->num_inputs > SG_MAX_VS_INPUTS)
     return SG_INVALID_PARAMETER;
@@ -1853,14 +1970,65 @@ int32_t do_draw(device_state* dev, sg_draw_desc const* d, sg_draw_stats* stats_o
   }
   c.full_mask = (1ull << c.samples) - 1;
   c.quad_full_mask = c.full_mask | (c.full_mask << 16) | (c.full_mask << 32) | (c.full_mask << 48);
-  // early-Z enable (framebuffer.cpp:424)
-  c.early_z = c.ds != nullptr && !d->depth_stencil.stencil_enable;
+  // early-Z enable (framebuffer.cpp:424); lines test after shading
+  c.early_z = c.ds != nullptr && !d->depth_stencil.stencil_enable && !lines && !wire;
+  uint32_t const corners = lines ? 2u : 3u;
   c.stats.ia_primitives = d->prim_count;
-  c.stats.ia_vertices = 3ull * d->prim_count;  // three per fetched primitive (default_vertex_cache.cpp:363)
+  c.stats.ia_vertices = uint64_t(corners) * d->prim_count;  // per fetched primitive (default_vertex_cache.cpp:363)
   c.stats.cinvocations = d->prim_count;        // every primitive enters the clipper (geom_setup_engine.cpp:108-123)
   // the GPU path's count (one run per primitive corner); the reference's
   // depends on its worker threads' vertex caches and is not compared
-  c.stats.vs_invocations = 3ull * d->prim_count;
+  c.stats.vs_invocations = uint64_t(corners) * d->prim_count;
+  if (lines || wire) {
+    std::unordered_map<uint32_t, std::unique_ptr<vso>> vcache;
+    std::vector<std::unique_ptr<vso>> pool;
+    std::vector<vso*> segs;  // pairs, in primitive order
+    auto vertex = [&](uint32_t index) {
+      auto it = vcache.find(index);
+      if (it == vcache.end()) {
+        auto v = std::make_unique<vso>();
+        for (auto& r : v->r) r = mk(0, 0, 0, 0);
+        run_vs(c, index, *v);
+        it = vcache.emplace(index, std::move(v)).first;
+      }
+      return it->second.get();
+    };
+    for (uint32_t p = 0; p < d->prim_count; ++p) {
+      uint32_t idx[3];
+      fetch_indexes(c, p, idx);
+      if (lines) {
+        vso* a = vertex(idx[0]);
+        vso* b = vertex(idx[1]);
+        if (clip_line(c, a, b, pool)) {
+          segs.push_back(a);
+          segs.push_back(b);
+        }
+        continue;
+      }
+      vso* tv[3] = {vertex(idx[0]), vertex(idx[1]), vertex(idx[2])};
+      std::vector<vso*> tri;
+      clip_triangle(c, tv, pool, tri);
+      for (size_t t = 0; t + 2 < tri.size(); t += 3)
+        for (int e = 0; e < 3; ++e) {
+          segs.push_back(tri[t + e]);
+          segs.push_back(tri[t + (e + 1) % 3]);
+        }
+    }
+    c.stats.cprimitives = segs.size() / 2;
+    // project every distinct vertex once, in place
+    std::vector<vso*> uniq(segs.begin(), segs.end());
+    std::sort(uniq.begin(), uniq.end());
+    uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+    for (vso* v : uniq) vp_project(c, *v);
+    rasterizer_state rs;
+    rs.c = &c;
+    rs.tris = nullptr;
+    rs.f = ds_functions(c);
+    rs.st = &c.stats;
+    for (size_t i = 0; i < segs.size(); i += 2) rasterize_line(rs, *segs[i], *segs[i + 1]);
+    if (stats_out) *stats_out = c.stats;
+    return SG_OK;
+  }
 
   // Vertex processing: the vertex shader is a pure function of the index,
   // so one result per distinct index stands for the reference's caches.

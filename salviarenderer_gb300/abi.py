@@ -16,7 +16,7 @@ SG_MAX_STREAMS = 8
 SG_MAX_SHADER_CONSTANTS = 48
 SG_MAX_SHADER_SAMPLERS = 2
 
-TOPOLOGY_TRIANGLE_LIST, TOPOLOGY_TRIANGLE_STRIP = 2, 4
+TOPOLOGY_LINE_LIST, TOPOLOGY_LINE_STRIP, TOPOLOGY_TRIANGLE_LIST, TOPOLOGY_TRIANGLE_STRIP = 0, 1, 2, 4
 CULL_NONE, CULL_FRONT, CULL_BACK = 0, 1, 2
 FILL_WIREFRAME, FILL_SOLID = 0, 1
 CMP_NEVER, CMP_LESS, CMP_EQUAL, CMP_LESS_EQUAL, CMP_GREATER, CMP_NOT_EQUAL, \

@@ -42,6 +42,8 @@ void launch_cover_rollback(PassParams const& p, uint32_t grid, cudaStream_t s);
 cudaError_t init_learned();
 cudaError_t init_af_filter();
 void launch_merge(PassParams const& p, uint32_t grid, cudaStream_t s);
+void launch_lines(PassParams const& p, uint32_t grid, cudaStream_t s);
+cudaError_t upload_ewa_table_line(float const* tab, cudaStream_t s);
 void launch_shade_0(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
 void launch_shade_1(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
 void launch_shade_2(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
@@ -195,6 +197,8 @@ struct PassPlan {
   uint64_t ncounts = 0, rec_units = 0;
   bool any_early_z = false;
   uint32_t na_mask = 0;
+  bool lines = false;                        // a line pass: segments (line_mode != 0) only
+  uint64_t slots = 0;                        // record slots its draws take
   bool empty() const { return draws.empty() && clears.empty() && resolves.empty(); }
 };
 
@@ -532,9 +536,12 @@ struct DrawInfo {
 };
 
 int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, DrawInfo& info) {
-  if (desc->raster.fill_mode != SG_FILL_SOLID) return SG_INVALID_PARAMETER;
-  if (desc->topology != SG_TOPOLOGY_TRIANGLE_LIST && desc->topology != SG_TOPOLOGY_TRIANGLE_STRIP)
+  bool const lines = desc->topology == SG_TOPOLOGY_LINE_LIST || desc->topology == SG_TOPOLOGY_LINE_STRIP;
+  if (!lines && desc->topology != SG_TOPOLOGY_TRIANGLE_LIST && desc->topology != SG_TOPOLOGY_TRIANGLE_STRIP)
     return SG_INVALID_PARAMETER;
+  if (desc->raster.fill_mode != SG_FILL_SOLID && desc->raster.fill_mode != SG_FILL_WIREFRAME)
+    return SG_INVALID_PARAMETER;
+  uint32_t const line_mode = lines ? 1u : desc->raster.fill_mode == SG_FILL_WIREFRAME ? 2u : 0u;
   if (desc->num_varyings > SG_MAX_VARYINGS || desc->num_inputs > SG_MAX_VS_INPUTS ||
       desc->num_streams > SG_MAX_STREAMS || desc->num_inputs == 0)
     return SG_INVALID_PARAMETER;
@@ -598,7 +605,9 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   }
   // draw() has no base vertex (renderer_impl.cpp:337-344)
   p.base_vertex = desc->indexed ? desc->base_vertex : 0;
-  p.strip = desc->topology == SG_TOPOLOGY_TRIANGLE_STRIP;
+  p.strip = desc->topology == SG_TOPOLOGY_TRIANGLE_STRIP || desc->topology == SG_TOPOLOGY_LINE_STRIP;
+  p.line_mode = line_mode;
+  p.slots_per_prim = line_mode == 1 ? 1u : line_mode == 2 ? 9u : 3u;
   p.prim_count = desc->prim_count;
   // shaders
   p.vs_prog = desc->vs.program;
@@ -618,6 +627,8 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   };
   info.user_ps = user_module(p.ps_prog, SG_STAGE_PIXEL);
   info.user_bs = user_module(p.bs_prog, SG_STAGE_BLEND);
+  // line pixels are shaded and merged by k_lines: stock programs only
+  if (line_mode && (p.ps_prog >= SG_USER_PROGRAM_BASE || p.bs_prog >= SG_USER_PROGRAM_BASE)) return SG_INVALID_PARAMETER;
   if (p.vs_prog < SG_VS_TRANSFORM || p.vs_prog > SG_VS_MORPH_DISPLACE ||
       ((p.ps_prog < SG_PS_COLOR || p.ps_prog > SG_PS_TEXCUBE_MODULATE) && !info.user_ps) ||
       ((p.bs_prog < SG_BS_REPLACE || p.bs_prog > SG_BS_REPLACE_ALL) && !info.user_bs))
@@ -625,7 +636,7 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   if (p.ps_prog != SG_PS_COLOR && p.ps_prog != SG_PS_CONSTANT && p.ps_prog != SG_PS_COLOR_MRT && !info.user_ps &&
       !desc->ps.samplers[0])
     return SG_INVALID_PARAMETER;
-  if (p.ps_prog == SG_PS_TEX_GRAD_LEARNED) {
+  if (p.ps_prog == SG_PS_TEX_GRAD_LEARNED && !line_mode) {  // (line pixels sample plainly)
     if (!d->af_models.count(desc->ps.learned_filter)) return SG_INVALID_PARAMETER;
     info.af_model = desc->ps.learned_filter;
     info.af_texture = info.tex[1];
@@ -664,7 +675,7 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
       p.write_depth = ds.depth_write && ds.depth_func != SG_CMP_NEVER;
     }
     p.stencil = ds.stencil_enable && dt->fmt != SG_FMT_D32F;
-    p.early_z = !ds.stencil_enable;
+    p.early_z = !ds.stencil_enable && !line_mode;  // line pixels test after shading
   }
   p.depth_func = ds.depth_enable ? ds.depth_func : SG_CMP_ALWAYS;
   // the masks are 8-bit fields of depth_stencil_desc (framebuffer.h:35-52)
@@ -730,6 +741,8 @@ void fill_target(sg_device* d, DrawInfo const& info, TargetParams& T) {
 // Whether the draw can join the pass; if not, the pass must run first.
 bool draw_fits(sg_device* d, PassPlan const& pl, DrawParams const& p, DrawInfo const& info) {
   if (pl.nprims + p.prim_count > SG_PASS_MAX_PRIMS) return false;
+  if (pl.slots + uint64_t(p.slots_per_prim) * p.prim_count > 3ull * SG_PASS_MAX_PRIMS) return false;
+  if (!pl.draws.empty() && pl.lines != (p.line_mode != 0)) return false;  // segments and triangles: own passes
   if (!pl.draws.empty() && !pl.target_of.count(info.key())) {
     Texture* t = find_tex(d, info.color ? info.color : info.ds);
     uint64_t const smp = static_cast<uint64_t>(t->levels[0].w) * t->levels[0].h * t->samples;
@@ -793,6 +806,8 @@ void add_draw(sg_device* d, PassPlan& pl, DrawParams p, DrawInfo const& info, ui
     p.shade_key = USER_SHADE_CLASS * 8u + slot;
   }
   if (info.user_bs) pl.user_bs = info.user_bs;
+  pl.lines = p.line_mode != 0;
+  pl.slots += uint64_t(p.slots_per_prim) * p.prim_count;
   p.prim_base = static_cast<uint32_t>(pl.nprims);
   pl.nprims += p.prim_count;
   pl.draws.push_back(p);
@@ -812,10 +827,10 @@ void finalize(PassPlan& pl, sg_device* d) {
     TargetParams& T = pl.targets[p.target];
     T.tiles_x = std::max(T.tiles_x, p.tiles_x);
     T.tiles_y = std::max(T.tiles_y, p.tiles_y);
-    slots[p.target] += 3ull * p.prim_count;
+    slots[p.target] += uint64_t(p.slots_per_prim) * p.prim_count;
     if ((p.zcfg & 128u) && T.ds) T.any_early_z = 1;
     if (p.shade_class != USER_SHADE_CLASS) pl.na_mask |= 1u << p.shade_class;
-    pl.rec_units += 3ull * p.prim_count * p.rec_stride;
+    pl.rec_units += uint64_t(p.slots_per_prim) * p.prim_count * p.rec_stride;
   }
   // slot ranges: targets in order, each target's draws in API order
   std::vector<uint64_t> tslot(nt, 0);
@@ -828,7 +843,7 @@ void finalize(PassPlan& pl, sg_device* d) {
   std::vector<uint64_t> cursor = tslot;
   for (auto& p : pl.draws) {
     p.slot_base = static_cast<uint32_t>(cursor[p.target]);
-    cursor[p.target] += 3ull * p.prim_count;
+    cursor[p.target] += uint64_t(p.slots_per_prim) * p.prim_count;
   }
   // tiles and binning chunks; counters stay under 32M in total
   uint32_t const max_chunks = static_cast<uint32_t>(std::max(1, d->num_sms)) * 32;
@@ -1100,6 +1115,19 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       if (P.tile_order) SG_CUDA(d, launch_tile_order(P, P.tile_order + pl.ntiles, s));
       launch_bin(P, true, s);
       stage_end(d, 1, ev);
+      if (pl.lines) {  // segments: rasterized, shaded and merged per tile in one kernel
+        ev = stage_begin(d, profile);
+        launch_lines(P, std::min<uint32_t>(pl.ntiles, sms * 16), s);
+        stage_end(d, 2, ev);
+        k += P.tile_order ? 10 : 8;  // geometry, bin count, 3 scans, tile ranges (+ 2 order), bin fill, lines
+        d->prof.raster_launches += 1;
+        d->prof.draws += pl.draws.size();
+        if (!pl.resolves.empty()) k += launch_jobs(pl.resolves.data(), static_cast<uint32_t>(pl.resolves.size()),
+                                                   static_cast<uint32_t>(d->num_sms), s, d->status, true);
+        SG_CUDA(d, cudaGetLastError());
+        *kernels = k;
+        return SG_OK;
+      }
       ev = stage_begin(d, profile);
       if (tu.cover_threads_per_block == 2)
         launch_cover2(P, pl.max_samples, pl.any_early_z, tu.cover_ctas_per_sm, std::min<uint32_t>(pl.ntiles * 4, sms * 8),
@@ -1276,7 +1304,7 @@ int32_t run_plan(sg_device* d, PassPlan& pl, sg_draw_stats* stats, uint8_t* fixe
         o.cprimitives = d->stats_host[i].cprimitives;
         o.ps_invocations = d->stats_host[i].ps_invocations;
         o.backend_input_pixels = d->stats_host[i].backend_input_pixels;
-        o.ia_vertices = 3ull * pl.draws[i].prim_count;  // default_vertex_cache.cpp:363
+        o.ia_vertices = (pl.draws[i].line_mode == 1 ? 2ull : 3ull) * pl.draws[i].prim_count;  // default_vertex_cache.cpp:363
         o.vs_invocations = d->stats_host[i].vs_invocations;
         o.cinvocations = pl.draws[i].prim_count;        // geom_setup_engine.cpp:108-123
       }
@@ -1670,6 +1698,7 @@ int32_t sg_device_create(int32_t cuda_device, void* cuda_stream, sg_device** out
   for (auto up : {upload_ewa_table_raster_a, upload_ewa_table_raster_b, upload_ewa_table_raster_c})
     if (up(tab, d->stream) != cudaSuccess) return SG_CUDA_ERROR;
   if (upload_ewa_table_geometry(tab, d->stream) != cudaSuccess) return SG_CUDA_ERROR;
+  if (upload_ewa_table_line(tab, d->stream) != cudaSuccess) return SG_CUDA_ERROR;
   if (upload_ewa_table_af(tab, d->stream) != cudaSuccess) return SG_CUDA_ERROR;
   if (upload_ewa_table_filter(tab, d->stream) != cudaSuccess) return SG_CUDA_ERROR;
   if (cudaStreamSynchronize(d->stream) != cudaSuccess) return SG_CUDA_ERROR;

@@ -446,9 +446,9 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
                                            (static_cast<size_t>(by0) * 4 * TILE + bx0 * 4) * S
                                      : nullptr;
       for (uint32_t i = tid; i < qh * zrow; i += CV_THREADS) {
-        uint32_t y = i / zrow, k = i % zrow;
+        uint32_t y = i >> (__ffs(zrow) - 1), k = i & (zrow - 1);  // zrow: a power of two
         if (k >= qw * S) continue;
-        uint32_t x = k / S, sm = k % S;
+        uint32_t x = k >> (S >> 1), sm = k & (S - 1);
         uint32_t const v = *reinterpret_cast<uint32_t const*>(ds_addr(T, x0 + x, y0 + y, sm));
         ztile[i] = v;
         if (zb) zb[static_cast<size_t>(y) * TILE * S + k] = v;
@@ -584,9 +584,9 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
     if (stage_z) {
       __syncthreads();
       for (uint32_t i = tid; i < qh * zrow; i += CV_THREADS) {
-        uint32_t y = i / zrow, k = i % zrow;
+        uint32_t y = i >> (__ffs(zrow) - 1), k = i & (zrow - 1);  // zrow: a power of two
         if (k >= qw * S) continue;
-        uint32_t x = k / S, sm = k % S;
+        uint32_t x = k >> (S >> 1), sm = k & (S - 1);
         *reinterpret_cast<uint32_t*>(ds_addr(T, x0 + x, y0 + y, sm)) = ztile[i];
       }
     }
@@ -619,7 +619,7 @@ __global__ void __launch_bounds__(256) k_cover_rollback(PassParams P) {
     uint32_t const th = min(static_cast<uint32_t>(TILE), T.height - min(T.height, ty0));
     uint32_t const* zb = P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words;
     for (uint32_t i = threadIdx.x; i < th * TILE * S; i += blockDim.x) {
-      uint32_t const y = i / (TILE * S), k = i % (TILE * S), x = k / S, sm = k % S;
+      uint32_t const y = i >> (6 + (S >> 1)), k = i & (TILE * S - 1), x = k >> (S >> 1), sm = k & (S - 1);
       if (x >= tw) continue;
       *reinterpret_cast<uint32_t*>(ds_addr(T, tx0 + x, ty0 + y, sm)) = zb[i];
     }

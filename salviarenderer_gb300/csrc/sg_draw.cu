@@ -222,8 +222,102 @@ __device__ void emit_triangle(PassParams const& P, DrawParams const& D, uint32_t
   P.slot_rec[slot] = idx;
 }
 
-// clipper::clip_solid_triangle + clip_triangle_to_poly_general (clipper.cpp:43-228)
+// A projected segment's record (the segment record layout) into `slot`.
 template <int NA>
+__device__ void emit_segment(PassParams const& P, DrawParams const& D, uint32_t draw, uint32_t slot, vtx<NA> const& a,
+                             vtx<NA> const& b) {
+  constexpr uint32_t STRIDE = rec_stride_for(NA);
+  constexpr int R = 1 + NA;
+  uint32_t idx = atomicAdd(&P.counters->rec_units, STRIDE);
+  if (idx > P.rec_capacity - STRIDE || P.rec_capacity < STRIDE) {
+    atomicOr(&P.counters->overflow, OVF_REC);
+    idx = NO_REC;
+  } else {
+    float4* dst = P.recs + idx;
+    float4 const never = make_float4(0.0f, 0.0f, -1.0f, 0.0f);
+    dst[0] = never;
+    dst[1] = never;
+    dst[2] = never;
+    // the box binning lists the segment under: its pixels' positions are
+    // lerped, so widened past the rounding of the lerp (two units in the
+    // last place of the largest coordinate, and two pixels), and bounded so
+    // that the tile range stays in int
+    v4 const pa = a.r[0], pb = b.r[0];
+    float const mag = fmaxf(fmaxf(fabsf(pa.x), fabsf(pb.x)), fmaxf(fabsf(pa.y), fabsf(pb.y)));
+    float const mg = 2.0f + mag * 0x1p-20f;
+    auto bound = [](float v) { return fminf(fmaxf(v, -0x1p30f), 0x1p30f); };
+    dst[3] = make_float4(bound(smin(pa.x, pb.x) - mg), bound(smax(pa.x, pb.x) + mg), bound(smin(pa.y, pb.y) - mg),
+                         bound(smax(pa.y, pb.y) + mg));
+    dst[4] = make_float4(0.0f, 0.0f, __uint_as_float(draw), __uint_as_float(rec_flags(true, D.shade_key, D.zcfg)));
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      dst[5 + i] = make_float4(a.r[i].x, a.r[i].y, a.r[i].z, a.r[i].w);
+      dst[5 + R + i] = make_float4(b.r[i].x, b.r[i].y, b.r[i].z, b.r[i].w);
+    }
+  }
+  P.slot_rec[slot] = idx;
+}
+
+// A triangle of the solid clipper drawn as its edges (a, b), (b, c), (c, a)
+// into slots slot .. slot + 2.
+template <int NA>
+__device__ void emit_wire(PassParams const& P, DrawParams const& D, uint32_t draw, uint32_t slot, vtx<NA> a,
+                          vtx<NA> b, vtx<NA> c, uint32_t& nseg) {
+  nseg += 3;
+  vp_project(D, a);
+  vp_project(D, b);
+  vp_project(D, c);
+  emit_segment<NA>(P, D, draw, slot, a, b);
+  emit_segment<NA>(P, D, draw, slot + 1, b, c);
+  emit_segment<NA>(P, D, draw, slot + 2, c, a);
+}
+
+// The k-th output triangle of a primitive: a record, or (WIRE) three segments.
+template <int NA, bool WIRE>
+__device__ inline void emit_tri(PassParams const& P, DrawParams const& D, uint32_t draw, uint32_t slot0, int k,
+                                vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c, uint32_t& ntri) {
+  if constexpr (WIRE)
+    emit_wire<NA>(P, D, draw, slot0 + 3 * k, a, b, c, ntri);
+  else
+    emit_triangle<NA>(P, D, draw, slot0 + k, a, b, c, ntri);
+}
+
+// A line primitive: assembled (index_fetcher.cpp:53-60), shaded, cut at
+// z >= 0 then z <= w (the outside end replaced by lerp(inside, outside,
+// d_in / (d_in - d_out))), projected, one segment record.
+template <int NA>
+__device__ void geometry_line(PassParams const& P, DrawParams const& D, uint32_t draw, uint32_t prim,
+                              uint32_t& nseg) {
+  uint32_t const i0 = D.strip ? prim : prim * 2;
+  vtx<NA> v[2];
+  run_vs(P, D, fetch_index(P, D, i0), v[0]);
+  run_vs(P, D, fetch_index(P, D, i0 + 1), v[1]);
+  uint32_t const slot = D.slot_base + prim;
+#pragma unroll
+  for (int pl = 0; pl < 2; ++pl) {
+    float const da = clip_d(pl, v[0].r[0]), db = clip_d(pl, v[1].r[0]);
+    if (da < 0.0f && db < 0.0f) {
+      P.slot_rec[slot] = NO_REC;
+      return;
+    }
+    vtx<NA> t;
+    if (da >= 0.0f && db < 0.0f) {
+      vtx_lerp(D, t, v[0], v[1], da / (da - db));
+      v[1] = t;
+    } else if (da < 0.0f && db >= 0.0f) {
+      vtx_lerp(D, t, v[1], v[0], db / (db - da));
+      v[0] = t;
+    }
+  }
+  ++nseg;
+  vp_project(D, v[0]);
+  vp_project(D, v[1]);
+  emit_segment<NA>(P, D, draw, slot, v[0], v[1]);
+}
+
+// clipper::clip_solid_triangle + clip_triangle_to_poly_general (clipper.cpp:43-228);
+// WIRE: each output triangle as its three edges (9 slots per primitive)
+template <int NA, bool WIRE = false>
 __device__ void geometry_prim(PassParams const& P, DrawParams const& D, uint32_t draw, uint32_t prim,
                               uint32_t& ntri) {
   uint32_t ids[3];
@@ -244,9 +338,14 @@ __device__ void geometry_prim(PassParams const& P, DrawParams const& D, uint32_t
   vtx<NA> tv[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) run_vs(P, D, fetch_index(P, D, ids[i]), tv[i]);
-  uint32_t slot0 = D.slot_base + prim * 3;
-  P.slot_rec[slot0 + 1] = NO_REC;
-  P.slot_rec[slot0 + 2] = NO_REC;
+  uint32_t slot0 = D.slot_base + prim * (WIRE ? 9u : 3u);
+  if constexpr (WIRE) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) P.slot_rec[slot0 + k] = NO_REC;
+  } else {
+    P.slot_rec[slot0 + 1] = NO_REC;
+    P.slot_rec[slot0 + 2] = NO_REC;
+  }
   bool in_frustum = true;
 #pragma unroll
   for (int pl = 0; pl < 2; ++pl)
@@ -266,9 +365,9 @@ __device__ void geometry_prim(PassParams const& P, DrawParams const& D, uint32_t
     if (cull(D, front ? 1.0f : -1.0f)) {
       P.slot_rec[slot0] = NO_REC;
     } else if (front) {
-      emit_triangle<NA>(P, D, draw, slot0, tv[0], tv[1], tv[2], ntri);
+      emit_tri<NA, WIRE>(P, D, draw, slot0, 0, tv[0], tv[1], tv[2], ntri);
     } else {
-      emit_triangle<NA>(P, D, draw, slot0, tv[0], tv[2], tv[1], ntri);
+      emit_tri<NA, WIRE>(P, D, draw, slot0, 0, tv[0], tv[2], tv[1], ntri);
     }
     return;
   }
@@ -323,35 +422,48 @@ __device__ void geometry_prim(PassParams const& P, DrawParams const& D, uint32_t
   P.slot_rec[slot0] = NO_REC;
   for (int t = 1; t + 1 < nv; ++t) {
     int ia = poly[src][0], ib = poly[src][is_front ? t : t + 1], ic = poly[src][is_front ? t + 1 : t];
-    emit_triangle<NA>(P, D, draw, slot0 + (t - 1), pool[ia], pool[ib], pool[ic], ntri);
+    emit_tri<NA, WIRE>(P, D, draw, slot0, t - 1, pool[ia], pool[ib], pool[ic], ntri);
   }
+}
+
+template <int NA>
+__device__ inline void geometry_any(PassParams const& P, DrawParams const& D, uint32_t draw, uint32_t prim,
+                                    uint32_t& ntri) {
+  if (D.line_mode == 1)
+    geometry_line<NA>(P, D, draw, prim, ntri);
+  else if (D.line_mode == 2)
+    geometry_prim<NA, true>(P, D, draw, prim, ntri);
+  else
+    geometry_prim<NA>(P, D, draw, prim, ntri);
 }
 
 __global__ void __launch_bounds__(128) k_geometry(PassParams P) {
   if (pass_gated(P)) return;
   uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t ntri = 0, draw = 0xFFFFFFFFu;
+  uint32_t ntri = 0, draw = 0xFFFFFFFFu, corners = 3;
   if (g < P.nprims) {
     draw = upper_index(P.draw_prim_base, P.ndraws, g);
     DrawParams const& D = P.draws[draw];
     uint32_t prim = g - D.prim_base;
+    if (D.line_mode == 1) corners = 2;
     switch (D.nattr) {
-    case 0: geometry_prim<0>(P, D, draw, prim, ntri); break;
-    case 1: geometry_prim<1>(P, D, draw, prim, ntri); break;
-    case 2: geometry_prim<2>(P, D, draw, prim, ntri); break;
-    case 3: geometry_prim<3>(P, D, draw, prim, ntri); break;
-    case 4: geometry_prim<4>(P, D, draw, prim, ntri); break;
-    default: geometry_prim<5>(P, D, draw, prim, ntri); break;
+    case 0: geometry_any<0>(P, D, draw, prim, ntri); break;
+    case 1: geometry_any<1>(P, D, draw, prim, ntri); break;
+    case 2: geometry_any<2>(P, D, draw, prim, ntri); break;
+    case 3: geometry_any<3>(P, D, draw, prim, ntri); break;
+    case 4: geometry_any<4>(P, D, draw, prim, ntri); break;
+    default: geometry_any<5>(P, D, draw, prim, ntri); break;
     }
   }
   // per-draw counters, aggregated over the lanes of one draw: clipped
-  // triangles, and vertex-shader runs (one per corner of every primitive)
+  // triangles (segments for lines), and vertex-shader runs (one per corner
+  // of every primitive)
   uint32_t grp = __match_any_sync(0xFFFFFFFFu, draw);
   uint32_t sum = __reduce_add_sync(grp, ntri);
   uint32_t const leader = static_cast<uint32_t>(__ffs(grp) - 1);
   if (draw != 0xFFFFFFFFu && (threadIdx.x & 31) == leader) {
     if (sum) atomicAdd(&P.draw_stats[draw].cprimitives, static_cast<unsigned long long>(sum));
-    atomicAdd(&P.draw_stats[draw].vs_invocations, 3ull * static_cast<unsigned>(__popc(grp)));
+    atomicAdd(&P.draw_stats[draw].vs_invocations, static_cast<unsigned long long>(corners) * __popc(grp));
   }
 }
 

@@ -95,9 +95,11 @@ struct DrawParams {
   uint32_t index_stride;
   int32_t base_vertex;
   uint32_t strip;
+  uint32_t line_mode;           // 0: triangles; 1: lines (list / strip); 2: triangles drawn as their edges
+  uint32_t slots_per_prim;      // record slots of a primitive: 3 triangles; 1 segment; 9 wireframe segments
   uint32_t prim_count;
   uint32_t prim_base;           // first global primitive of the draw in the pass
-  uint32_t slot_base;           // first triangle slot (3 per primitive)
+  uint32_t slot_base;           // first record slot (slots_per_prim per primitive)
   uint32_t target;              // index into the pass's targets
   uint32_t nattr, rec_stride;
   uint32_t shade_class;         // nattr, plus 8 for learned-filter draws: which k_shade instance runs it
@@ -212,6 +214,10 @@ constexpr uint32_t AF_PLAIN_UNITS = 3;
 // the three units of the plain record (for a fallback).
 constexpr uint32_t AF_NET_UNITS = 8;
 
+// segment record layout (lines and wireframe edges): [0..2] (0, 0, -1, 0),
+// edge factors no tile test rejects, so binning lists the segment in every
+// tile of its bounding box; [3] bbox, [4] (0, 0, draw index bits, flags
+// bits), then the two projected endpoints' registers (1 + nattr each).
 // triangle record layout (float4 units): [0..2] edge factors (x, y, z) with
 // v0's projected x, y, z in .w, [3] bbox, [4] (ddx.z, ddy.z of the position,
 // draw index bits, flags bits), then v0, ddx, ddy registers (1 + nattr each).

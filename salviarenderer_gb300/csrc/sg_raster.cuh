@@ -559,9 +559,9 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
                                            (static_cast<size_t>(by0) * 4 * TILE + bx0 * 4) * S
                                      : nullptr;
       for (uint32_t i = tid; i < qh * zrow; i += COVER_THREADS) {
-        uint32_t y = i / zrow, k = i % zrow;
+        uint32_t y = i >> (__ffs(zrow) - 1), k = i & (zrow - 1);  // zrow: a power of two
         if (k >= qw * S) continue;
-        uint32_t x = k / S, sm = k % S;
+        uint32_t x = k >> (S >> 1), sm = k & (S - 1);
         uint32_t const v = *reinterpret_cast<uint32_t const*>(ds_addr(T, x0 + x, y0 + y, sm));
         ztile[i] = v;
         if (zb) zb[static_cast<size_t>(y) * TILE * S + k] = v;
@@ -656,9 +656,9 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
     if (stage_z) {
       __syncthreads();
       for (uint32_t i = tid; i < qh * zrow; i += COVER_THREADS) {
-        uint32_t y = i / zrow, k = i % zrow;
+        uint32_t y = i >> (__ffs(zrow) - 1), k = i & (zrow - 1);  // zrow: a power of two
         if (k >= qw * S) continue;
-        uint32_t x = k / S, sm = k % S;
+        uint32_t x = k >> (S >> 1), sm = k & (S - 1);
         *reinterpret_cast<uint32_t*>(ds_addr(T, x0 + x, y0 + y, sm)) = ztile[i];
       }
     }
@@ -685,15 +685,39 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
 // (lanes 4k..4k+3 of the warp); ddx / ddy are the quad differences and
 // tex2d's LOD uses them (cpp_pixel_shader.cpp:13-31).  `keep` is the
 // program's return value: false discards the pixel.
-template <int NA>
-__device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q, bool& keep) {
+// Attribute 0 at the quad's pixels 0, 1 (x + 1) and 2 (y + 1), from which
+// the programs take ddx / ddy: read from the quad's lanes by shuffles.
+struct QuadNb {
+  int base;
+  unsigned mask;
+  float a0w;
+  float u0, v0, u1, v1, u2, v2;
+  __device__ explicit QuadNb(v4 a0) {
+    base = (threadIdx.x & 31) & ~3;
+    mask = 0xFu << base;
+    a0w = a0.w;
+    u0 = __shfl_sync(mask, a0.x, base);
+    v0 = __shfl_sync(mask, a0.y, base);
+    u1 = __shfl_sync(mask, a0.x, base + 1);
+    v1 = __shfl_sync(mask, a0.y, base + 1);
+    u2 = __shfl_sync(mask, a0.x, base + 2);
+    v2 = __shfl_sync(mask, a0.y, base + 2);
+  }
+  __device__ float w(int i) const { return __shfl_sync(mask, a0w, base + i); }  // every lane of the quad calls it
+};
+// The same for one pixel of a line: the pixel and its neighbours one ddx /
+// one ddy along the line, given.
+struct LineNb {
+  float u0, v0, u1, v1, u2, v2;
+  float ws[3];
+  __device__ float w(int i) const { return ws[i]; }
+};
+
+template <int NA, class NB>
+__device__ inline v4 run_ps_nb(DrawParams const& D, v4 const* attr, NB const& nb, bool& keep) {
   v4 a0 = NA > 0 ? attr[0] : mk4(0, 0, 0, 0);
   v4 a1 = NA > 1 ? attr[1 < NA ? 1 : 0] : mk4(0, 0, 0, 0);
-  int base = (threadIdx.x & 31) & ~3;
-  unsigned mask = 0xFu << base;
-  float u0 = __shfl_sync(mask, a0.x, base), v0 = __shfl_sync(mask, a0.y, base);
-  float u1 = __shfl_sync(mask, a0.x, base + 1), v1 = __shfl_sync(mask, a0.y, base + 1);
-  float u2 = __shfl_sync(mask, a0.x, base + 2), v2 = __shfl_sync(mask, a0.y, base + 2);
+  float const u0 = nb.u0, v0 = nb.v0, u1 = nb.u1, v1 = nb.v1, u2 = nb.u2, v2 = nb.v2;
   keep = true;
   switch (D.ps_prog) {
   case SG_PS_COLOR:
@@ -709,8 +733,7 @@ __device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q, bool& ke
   case SG_PS_TEX_LOD_MODULATE:  // tex2dlod(s, 0) = s.sample(x, y, w) (cpp_pixel_shader.cpp:33-40)
     return mulv(sample_impl(D.ps_samp, a0.x, a0.y, a0.w, nullptr), a1);
   case SG_PS_TEX_PROJ_MODULATE: {  // tex2dproj(s, 0) (cpp_pixel_shader.cpp:42-60)
-    float const w0 = __shfl_sync(mask, a0.w, base), w1 = __shfl_sync(mask, a0.w, base + 1),
-                w2 = __shfl_sync(mask, a0.w, base + 2);
+    float const w0 = nb.w(0), w1 = nb.w(1), w2 = nb.w(2);
     // this pixel's attribute, and it stepped by ddx and by ddy
     float const nxx = a0.x + (u1 - u0), nxy = a0.y + (v1 - v0), nxw = a0.w + (w1 - w0);
     float const nyx = a0.x + (u2 - u0), nyy = a0.y + (v2 - v0), nyw = a0.w + (w2 - w0);
@@ -729,6 +752,11 @@ __device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int q, bool& ke
   }
   default: return mk4(0, 0, 0, 0);
   }
+}
+template <int NA>
+__device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int, bool& keep) {
+  QuadNb const nb(NA > 0 ? attr[0] : mk4(0, 0, 0, 0));
+  return run_ps_nb<NA>(D, attr, nb, keep);
 }
 
 

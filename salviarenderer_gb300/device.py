@@ -418,7 +418,7 @@ def make_draw_desc(**kw):
     """Builds an sg_draw_desc; keyword names follow the C fields."""
     d = abi.DrawDesc()
     d.topology = kw.get("topology", abi.TOPOLOGY_TRIANGLE_LIST)
-    d.raster.fill_mode = abi.FILL_SOLID
+    d.raster.fill_mode = kw.get("fill_mode", abi.FILL_SOLID)
     d.raster.cull_mode = kw.get("cull_mode", abi.CULL_NONE)
     d.raster.front_ccw = kw.get("front_ccw", 0)
     d.depth_stencil = kw.get("depth_stencil") or default_depth_stencil()

@@ -580,21 +580,53 @@ def overdraw_scene(seed=1, width=256, height=256, samples=1, ntris=60, draws=3, 
     return s
 
 
+def window_lines_scene(lines, width=16, height=16, samples=1, colors=None, depth_func=abi.CMP_LESS,
+                       blend=abi.BS_REPLACE, viewport=None):
+    """Line segments given in window coordinates, (x0, y0, z0, x1, y1, z1)
+    each, drawn as one SG_TOPOLOGY_LINE_LIST draw with an identity vertex
+    shader: the clip-space positions are chosen so that the viewport
+    transform lands exactly on the given coordinates (all values here are
+    exact in float).  The colour varying is `colors` (RGBA per vertex) or
+    the segment index."""
+    vp = viewport or (0, 0, width, height, 0.0, 1.0)
+    verts = []
+    for k, (x0, y0, z0, x1, y1, z1) in enumerate(lines):
+        for (x, y, z) in ((x0, y0, z0), (x1, y1, z1)):
+            cx = (x - (vp[0] + vp[2]) * 0.5) / (vp[2] * 0.5)
+            cy = -(y - (vp[1] + vp[3]) * 0.5) / (vp[3] * 0.5)
+            col = colors[len(verts)] if colors is not None else ((k + 1) / 16.0, 0.5, 1.0 - (k + 1) / 16.0, 1.0)
+            verts.append([cx, cy, z, 1.0, 0, 0, 0, 0] + list(col))
+    s = Scene("window_lines", width, height, samples)
+    s.clear_color = (0.0, 0.0, 0.0, 0.0)
+    s.buffers["vb"] = np.asarray(verts, dtype=np.float32)
+    s.draws.append(dict(viewport=vp, prim_count=len(lines), topology=abi.TOPOLOGY_LINE_LIST,
+                        streams=[("vb", 48, 0)], inputs=COLOR_FIRST_INPUTS, num_varyings=1,
+                        varying_modifiers=[abi.AM_LINEAR],
+                        depth_stencil=default_depth_stencil(depth_func=depth_func),
+                        vs=dict(program=abi.VS_TRANSFORM, constants=np.eye(4, dtype=np.float32)),
+                        ps=dict(program=abi.PS_COLOR), bs=dict(program=blend)))
+    return s
+
+
 def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=abi.TOPOLOGY_TRIANGLE_LIST,
                   index_format=None, base_vertex=0, cull=abi.CULL_NONE, front_ccw=0,
                   depth_func=abi.CMP_LESS, depth_write=1, depth_enable=1, blend=abi.BS_REPLACE,
                   ps=abi.PS_COLOR, sampler=None, modifiers=(abi.AM_LINEAR, abi.AM_LINEAR),
                   color_fmt=abi.FMT_RGBA8, ds_fmt=abi.FMT_RG32F, tex_size=64, uv_scale=3.0,
                   eye_dist=(2.2, 3.2), draws=1, clear_depth=1.0, uv_w=None, ps_constants=None, stencil=None,
-                  bs_constants=None):
+                  bs_constants=None, fill_mode=abi.FILL_SOLID):
     """A small scene that exercises one combination of pipeline state.
 
     Vertices carry position, a (u, v) pair and an RGBA colour.  Strips and
     indexed draws reuse the same vertex pool; `draws` splits the primitives
-    over several draw calls sharing the state.
+    over several draw calls sharing the state.  Line topologies and
+    SG_FILL_WIREFRAME draw the same kind of vertices as lines.
     """
     rng = np.random.default_rng(seed)
-    nv = ntris * 3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else ntris + 2
+    # vertices per primitive of a list, and the extra vertices of a strip
+    per, extra = {abi.TOPOLOGY_TRIANGLE_LIST: (3, 0), abi.TOPOLOGY_TRIANGLE_STRIP: (1, 2),
+                  abi.TOPOLOGY_LINE_LIST: (2, 0), abi.TOPOLOGY_LINE_STRIP: (1, 1)}[topology]
+    nv = ntris * per + extra
     npool = nv if index_format is None else max(8, nv // 2)
     pos = rng.uniform(-1.0, 1.0, size=(npool, 4))
     pos[:, 3] = 1.0
@@ -638,20 +670,19 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
                   topology=topology, streams=[("vb", 48, 0)],
                   inputs=COLOR_FIRST_INPUTS if ps in (abi.PS_COLOR, abi.PS_CONSTANT) else GRID_INPUTS,
                   num_varyings=len(modifiers), varying_modifiers=list(modifiers),
-                  cull_mode=cull, front_ccw=front_ccw, depth_stencil=dsd,
+                  cull_mode=cull, front_ccw=front_ccw, depth_stencil=dsd, fill_mode=fill_mode,
                   base_vertex=base_vertex, stencil_ref=stencil[2] if stencil is not None else 0,
                   vs=dict(program=abi.VS_TRANSFORM, constants=mvp),
                   ps=dict(program=ps, samplers=["s0"] if "s0" in s.samplers else [],
                           constants=list(ps_constants or [])),
                   bs=dict(program=blend, constants=list(bs_constants or [])))
         if index_format is not None:
-            dd.update(index_buffer="ib", index_format=index_format,
-                      start=first * (3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else 1))
+            dd.update(index_buffer="ib", index_format=index_format, start=first * per)
         else:
             # draw(start, count) ignores `start` and has no base vertex in the
             # reference (renderer_impl.cpp:337-344, index_fetcher.cpp:104-107):
             # split draws start at a vertex-stream offset instead.
-            first_vertex = base_vertex + first * (3 if topology == abi.TOPOLOGY_TRIANGLE_LIST else 1)
+            first_vertex = base_vertex + first * per
             dd["streams"] = [("vb", 48, 48 * first_vertex)]
             dd["base_vertex"] = 0
         s.draws.append(dd)
