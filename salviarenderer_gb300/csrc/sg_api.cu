@@ -78,9 +78,12 @@ struct Texture {
   bool cube = false;        // texture_cube: levels are its six faces (subresources 0-5)
   std::vector<Level> levels;
   // the learned filter's texture-unit copies of the levels (made on first
-  // use, refreshed by every pass that samples them, dropped with the levels)
+  // use, dropped with the levels) and the texture's write count they hold:
+  // a pass that samples the texture copies the levels again only when
+  // something wrote it since (`version` counts the writes queued so far)
   std::vector<cudaArray_t> af_arrays;
   uint32_t af_gen = 0;
+  uint64_t version = 1, af_version = 0;
 };
 struct Buffer {
   uint8_t* ptr = nullptr;
@@ -278,6 +281,10 @@ sg_tuning default_tuning() {
 struct sg_graph {
   Scratch scratch;
   std::vector<PassPlan> plans;
+  // textures its learned-filter passes sample that it does not write first
+  // (their copies are brought up to date before each launch), and the
+  // textures it writes (a launch counts as a write of each)
+  std::set<uint32_t> af_pre, written;
   std::vector<uint32_t> plan_kernels;  // kernels each pass launches (a pass with none is not logged)
   Arena params;                   // every pass's parameter blocks
   cudaGraph_t graph = nullptr;
@@ -317,6 +324,7 @@ struct sg_device {
   unsigned int* status_host = nullptr;    // pinned: their copy when the host looks
   uint8_t* static_base = nullptr;         // this device's g_static_scratch (looked up at creation)
   std::vector<LogEntry> log;              // passes launched since the host last looked
+  sg_graph* capture = nullptr;            // the graph being recorded, during graph_build
   unsigned int done_base = 0;             // the completed-pass count when the host last looked
   int32_t pending = 0;                    // an error of earlier work, reported at the next sg_sync
   std::set<sg_graph*> graphs;
@@ -416,6 +424,7 @@ void af_release_arrays(Texture& t) {
     if (a) cudaFreeArray(a);
   t.af_arrays.clear();
   ++t.af_gen;
+  t.af_version = 0;  // new copies are filled before their first use
 }
 cudaTextureAddressMode af_address(uint32_t m) {
   switch (m) {
@@ -1079,6 +1088,16 @@ int32_t scratch_static(sg_device* d, uint8_t* base, PassPlan const& pl, PlanLayo
 // ordered).  Returns the number of kernels launched in `*kernels`.  The
 // pass's last kernel counts it as completed in the device's status words
 // (none when the pass launches no kernel).
+// Counts the textures a pass writes (its targets, clears and resolves) as
+// written: the learned filter's copies of them are stale from here on.
+void note_writes(sg_device* d, PassPlan const& pl) {
+  for (std::set<uint32_t> const* set : {&pl.surfaces, &pl.cleared, &pl.resolved})
+    for (uint32_t t : *set) {
+      if (Texture* tx = find_tex(d, t)) ++tx->version;
+      if (d->capture) d->capture->written.insert(t);
+    }
+}
+
 int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vector<uint8_t> const* packed,
                     bool profile, uint32_t* kernels) {
   cudaStream_t s = d->stream;
@@ -1094,8 +1113,20 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
   if (!pl.draws.empty()) {
     if (packed) SG_CUDA(d, cudaMemcpyAsync(v.params, packed->data(), packed->size(), cudaMemcpyHostToDevice, s));
     if (P.af_capacity)  // the texture-unit copies the filter's feature taps read, current as of this pass
-      for (uint32_t t : pl.af_textures)
-        if (int32_t r = af_refresh(d, t)) return r;
+      for (uint32_t t : pl.af_textures) {
+        Texture* tx = find_tex(d, t);
+        if (!tx) continue;
+        if (d->capture) {  // recording: copy inside the graph only what the graph itself wrote before
+          if (d->capture->written.count(t)) {
+            if (int32_t r = af_refresh(d, t)) return r;
+          } else {
+            d->capture->af_pre.insert(t);
+          }
+        } else if (tx->af_version != tx->version) {
+          if (int32_t r = af_refresh(d, t)) return r;
+          tx->af_version = tx->version;
+        }
+      }
     SG_CUDA(d, cudaMemsetAsync(P.counters, 0, sizeof(PassCounters), s));
     SG_CUDA(d, cudaMemsetAsync(P.draw_stats, 0, pl.draws.size() * sizeof(DrawStatsDev), s));
     if (pl.nprims > 0 && pl.ntiles > 0) {
@@ -1125,6 +1156,7 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
         if (!pl.resolves.empty()) k += launch_jobs(pl.resolves.data(), static_cast<uint32_t>(pl.resolves.size()),
                                                    static_cast<uint32_t>(d->num_sms), s, d->status, true);
         SG_CUDA(d, cudaGetLastError());
+        note_writes(d, pl);
         *kernels = k;
         return SG_OK;
       }
@@ -1185,6 +1217,7 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
   if (!pl.resolves.empty()) k += launch_jobs(pl.resolves.data(), static_cast<uint32_t>(pl.resolves.size()),
                                              static_cast<uint32_t>(d->num_sms), s, d->status, true);
   SG_CUDA(d, cudaGetLastError());
+  note_writes(d, pl);
   *kernels = k;
   return SG_OK;
 }
@@ -1602,12 +1635,16 @@ int32_t graph_build(sg_device* d, sg_graph* g) {
   bool saved = d->profiling;
   d->profiling = false;
   g->plan_kernels.assign(g->plans.size(), 0);
+  g->af_pre.clear();
+  g->written.clear();
+  d->capture = g;
   for (size_t i = 0; i < g->plans.size() && r == SG_OK; ++i) {
     uint32_t k = 0;
     r = launch_pass(d, g->plans[i], views[i], nullptr, false, &k);
     g->plan_kernels[i] = k;
     kernels += k;
   }
+  d->capture = nullptr;
   d->profiling = saved;
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamEndCapture(d->stream, &graph);
@@ -1849,6 +1886,7 @@ int32_t sg_texture_upload(sg_device* d, uint32_t h, uint32_t level, const void* 
   if (int32_t r = settle_before_change(d)) return r;
   SG_CUDA(d, cudaMemcpyAsync(l.ptr, src, size, cudaMemcpyHostToDevice, d->stream));
   SG_CUDA(d, cudaStreamSynchronize(d->stream));
+  ++t->version;
   return SG_OK;
 }
 int32_t sg_texture_download(sg_device* d, uint32_t h, uint32_t level, void* dst, size_t size) {
@@ -1871,6 +1909,7 @@ int32_t sg_texture_gen_mipmap(sg_device* d, uint32_t h, uint32_t filter) {
   if (int32_t r = settle_before_change(d)) return r;
   SG_CUDA(d, cudaStreamSynchronize(d->stream));
   af_release_arrays(*t);
+  ++t->version;
   for (size_t i = 1; i < t->levels.size(); ++i) cudaFree(t->levels[i].ptr);
   t->levels.resize(1);
   for (uint32_t i = 1; i < n; ++i) {
@@ -2057,7 +2096,16 @@ int32_t sg_graph_launch(sg_device* d, sg_graph* g) {
     d->error = "sg_graph_launch: the graph could not be recorded again after an overflow";
     return SG_FAILED;
   }
+  for (uint32_t t : g->af_pre) {  // the filter's copies of what it samples, current as of this launch
+    Texture* tx = find_tex(d, t);
+    if (tx && tx->af_version != tx->version) {
+      if (int32_t r = af_refresh(d, t)) return r;
+      tx->af_version = tx->version;
+    }
+  }
   SG_CUDA(d, cudaGraphLaunch(g->exec, d->stream));
+  for (uint32_t t : g->written)
+    if (Texture* tx = find_tex(d, t)) ++tx->version;
   for (uint32_t k = 0; k < g->plans.size(); ++k)
     if (g->plan_kernels[k]) {
       LogEntry e;

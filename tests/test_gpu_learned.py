@@ -114,3 +114,51 @@ def test_learned_graph_replays_like_submit(gdev, model):
     for k in want:
         assert np.array_equal(got[k], want[k]), k
     g.close()
+
+
+def test_texture_rewritten_between_frames(gdev, model):
+    """The filter samples texture-unit copies of the texture, refreshed only
+    after the texture was written: uploads between two frames -- issued
+    immediately, and before the launch of a graph recorded earlier -- must
+    show in the next frame exactly as on a device that never saw the old
+    contents.  (Every level is uploaded in place: a graph keeps the level
+    allocations it was recorded with.)"""
+    s_old = scene((0.5, 16.0))
+    s_new = scene((0.5, 16.0))
+    img = s_new.textures["noise"][0]
+    s_new.textures["noise"] = (np.ascontiguousarray(img[::-1, ::-1]), True)  # other contents, same size
+    want = scenes.render(gdev, s_new, af_model=model, batched=True)
+
+    def chain(image):  # the image's mip chain as the device builds it
+        t = gdev.texture(image.shape[1], image.shape[0], 1, abi.FMT_RGBA8)
+        gdev.texture_upload(t, image)
+        gdev.gen_mipmap(t, abi.FILTER_LINEAR)
+        levels = [gdev.texture_download(t, lv) for lv in range(gdev.levels(t))]
+        gdev.lib.sg_texture_destroy(gdev.handle, t)
+        return levels
+
+    old_chain, new_chain = chain(s_old.textures["noise"][0]), chain(s_new.textures["noise"][0])
+    b = scenes.Bound(gdev, s_old, model)
+    tex = b.tex["noise"]
+
+    def upload(levels):
+        for lv, data in enumerate(levels):
+            gdev.texture_upload(tex, data, lv)
+
+    cl = b.commands()
+    g = gdev.graph_create(cl)
+    gdev.submit(cl)
+    before = b.outputs()
+    upload(new_chain)
+    gdev.submit(cl)
+    after = b.outputs()
+    assert not np.array_equal(before["resolved"], after["resolved"])
+    for k in want:
+        assert np.array_equal(after[k], want[k]), k
+    upload(old_chain)
+    upload(new_chain)
+    g.launch()
+    after_g = b.outputs()
+    for k in want:
+        assert np.array_equal(after_g[k], want[k]), k
+    g.close()
