@@ -562,6 +562,7 @@ typedef struct sg_tuning {
   uint32_t cover_threads_per_block; /* 2 or 32 */
   uint32_t cover_ctas_per_sm;  /* 3 or 4: the 2-thread coverage kernel's registers cut for that many CTAs per SM */
   uint32_t shade_resident;     /* 3 or 4: the shading kernels' registers cut for that many CTAs per SM */
+  uint32_t merge_resident;     /* 3 or 4: the merging kernel's registers cut for that many CTAs per SM */
 } sg_tuning;
 int32_t sg_get_tuning(sg_device* dev, sg_tuning* out);
 int32_t sg_set_tuning(sg_device* dev, const sg_tuning* tuning);

@@ -136,7 +136,8 @@ class Tuning(C.Structure):
                 ("bin_capacity", C.c_uint32), ("frag_chunks", C.c_uint32),
                 ("shade_quads_per_warp", C.c_uint32), ("shade_ctas_per_sm", C.c_uint32),
                 ("merge_ctas_per_sm", C.c_uint32), ("cover_threads_per_block", C.c_uint32),
-                ("cover_ctas_per_sm", C.c_uint32), ("shade_resident", C.c_uint32)]
+                ("cover_ctas_per_sm", C.c_uint32), ("shade_resident", C.c_uint32),
+                ("merge_resident", C.c_uint32)]
 
 
 class TuningKnob(C.Structure):

@@ -41,7 +41,7 @@ cudaError_t init_cover2();
 void launch_cover_rollback(PassParams const& p, uint32_t grid, cudaStream_t s);
 cudaError_t init_learned();
 cudaError_t init_af_filter();
-void launch_merge(PassParams const& p, uint32_t grid, cudaStream_t s);
+void launch_merge(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
 void launch_lines(PassParams const& p, uint32_t grid, cudaStream_t s);
 cudaError_t upload_ewa_table_line(float const* tab, cudaStream_t s);
 void launch_shade_0(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s);
@@ -246,6 +246,7 @@ sg_tuning_knob const kTuningKnobs[] = {
     {"shade_ctas_per_sm", 3, {4u, 8u, 16u}},
     {"shade_resident", 2, {3u, 4u}},
     {"merge_ctas_per_sm", 3, {2u, 3u, 6u}},
+    {"merge_resident", 2, {3u, 4u}},
 };
 
 uint32_t* knob_field(sg_tuning& t, char const* name) {
@@ -257,6 +258,7 @@ uint32_t* knob_field(sg_tuning& t, char const* name) {
   if (n == "bin_chunk") return &t.bin_chunk;
   if (n == "shade_ctas_per_sm") return &t.shade_ctas_per_sm;
   if (n == "shade_resident") return &t.shade_resident;
+  if (n == "merge_resident") return &t.merge_resident;
   return &t.merge_ctas_per_sm;
 }
 
@@ -273,6 +275,7 @@ sg_tuning default_tuning() {
   t.cover_threads_per_block = 2;
   t.cover_ctas_per_sm = 4;
   t.shade_resident = 4;
+  t.merge_resident = 3;
   return t;
 }
 
@@ -1207,7 +1210,7 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       if (pl.user_bs)  // the merge with the pass's user blend shader
         pl.user_bs->device_launch(&P, 0u, merge_grid, s);
       else
-        launch_merge(P, merge_grid, s);
+        launch_merge(P, merge_grid, tu.merge_resident, s);
       stage_end(d, 4, ev);
       k += P.tile_order ? 11 : 9;  // geometry, bin count, 3 scans, tile ranges (+ 2 order), bin fill, cover, merge
       d->prof.raster_launches += 1;
@@ -1907,9 +1910,20 @@ int32_t sg_texture_gen_mipmap(sg_device* d, uint32_t h, uint32_t filter) {
   }
   if (n > static_cast<uint32_t>(SG_MAX_LEVELS)) return SG_INVALID_PARAMETER;
   if (int32_t r = settle_before_change(d)) return r;
+  ++t->version;
+  if (t->levels.size() == n) {
+    // the chain exists: rebuilt in place, stream-ordered, so that the level
+    // allocations recorded graphs and samplers hold stay valid
+    for (uint32_t i = 1; i < n; ++i) {
+      Level const& src = t->levels[i - 1];
+      Level const& l = t->levels[i];
+      launch_mip(src.ptr, src.w, src.h, l.ptr, l.w, l.h, t->samples, t->fmt, filter, d->stream);
+    }
+    SG_CUDA(d, cudaGetLastError());
+    return SG_OK;
+  }
   SG_CUDA(d, cudaStreamSynchronize(d->stream));
   af_release_arrays(*t);
-  ++t->version;
   for (size_t i = 1; i < t->levels.size(); ++i) cudaFree(t->levels[i].ptr);
   t->levels.resize(1);
   for (uint32_t i = 1; i < n; ++i) {
@@ -2150,7 +2164,8 @@ int32_t sg_set_tuning(sg_device* d, const sg_tuning* t) {
       t->shade_quads_per_warp != 8 || t->shade_ctas_per_sm == 0 || t->shade_ctas_per_sm > 32 ||
       t->merge_ctas_per_sm == 0 || t->merge_ctas_per_sm > 8 ||
       (t->cover_threads_per_block != 2 && t->cover_threads_per_block != 32) ||
-      (t->cover_ctas_per_sm != 3 && t->cover_ctas_per_sm != 4) || (t->shade_resident != 3 && t->shade_resident != 4))
+      (t->cover_ctas_per_sm != 3 && t->cover_ctas_per_sm != 4) || (t->shade_resident != 3 && t->shade_resident != 4) ||
+      (t->merge_resident != 3 && t->merge_resident != 4))
     return SG_INVALID_PARAMETER;
   // a changed initial capacity is where the next passes start from (they
   // grow again on overflow)

@@ -1139,7 +1139,10 @@ __device__ __forceinline__ void merge_pass(PassParams const& P) {
 }
 
 #ifdef SG_RASTER_COVER_MERGE
-__global__ void __launch_bounds__(RASTER_THREADS) k_merge(PassParams P) { merge_pass<void>(P); }
+// MINB: CTAs per SM the registers are cut for (3: 80 registers, no spills;
+// 4: 64, with spills) -- a tuning choice
+template <int MINB>
+__global__ void __launch_bounds__(RASTER_THREADS, MINB) k_merge(PassParams P) { merge_pass<void>(P); }
 
 #endif  // SG_RASTER_COVER_MERGE
 

@@ -31,8 +31,11 @@ cudaError_t init_cover() {
                               static_cast<int>(cover_smem(4, true)));
 }
 
-void launch_merge(PassParams const& p, uint32_t grid, cudaStream_t s) {
-  k_merge<<<grid, RASTER_THREADS, 0, s>>>(p);
+void launch_merge(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s) {
+  if (resident >= 4)
+    k_merge<4><<<grid, RASTER_THREADS, 0, s>>>(p);
+  else
+    k_merge<3><<<grid, RASTER_THREADS, 0, s>>>(p);
 }
 
 }  // namespace sg

@@ -76,6 +76,6 @@ def test_autotune_space_names_tuning_fields(product_lib):
     assert lib.sg_autotune_space(ctypes.byref(knobs), ctypes.byref(n)) == abi.SG_OK
     fields = {f for f, _ in abi.Tuning._fields_}
     names = [knobs[i].field.decode() for i in range(n.value)]
-    assert set(names) <= fields and len(names) == len(set(names)) == 8
+    assert set(names) <= fields and len(names) == len(set(names)) == 9
     assert all(2 <= knobs[i].count <= 8 for i in range(n.value))
     assert "shade_quads_per_warp" not in names and "bin_capacity" not in names
