@@ -605,6 +605,10 @@ def run_gpu(args):
             "mtris_per_s": fps * scene.triangles / 1e6,
             "stage_ms_per_frame": {k: prof[k + "_ms"] / args.steps
                                    for k in ("geometry", "binning", "cover", "shade", "merge")},
+            "cover_work_per_frame": {"items": 4 * ((scene.width + 63) // 64) * ((scene.height + 63) // 64),
+                                     "batches": prof["cover_batches"] / args.steps,
+                                     "rounds": prof["cover_rounds"] / args.steps,
+                                     "pairs": prof["cover_pairs"] / args.steps},
             "roofline": {"bound": "hbm", "kernel": "k_cover2", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": read_traffic() if (width, height) == (1920, 1080) else None,

@@ -396,6 +396,9 @@ typedef struct sg_profile_data {
   uint64_t raster_launches;
   uint64_t af_lookups;        /* lookups the learned filter took */
   uint64_t af_fallbacks;      /* of those, the ones it sent back to the plain sampler */
+  uint64_t cover_batches;     /* coverage work: staged triangle batches, */
+  uint64_t cover_rounds;      /* walk rounds, */
+  uint64_t cover_pairs;       /* and (triangle, 4x4 block) pairs past the hierarchical depth test */
 } sg_profile_data;
 
 /* ---- device (create_benchmark_renderer, renderer.h:133-134) --------------- */

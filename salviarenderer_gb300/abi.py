@@ -110,7 +110,8 @@ class ProfileData(C.Structure):
     _fields_ = [("geometry_ms", C.c_double), ("binning_ms", C.c_double), ("raster_ms", C.c_double),
                 ("cover_ms", C.c_double), ("shade_ms", C.c_double), ("merge_ms", C.c_double),
                 ("draws", C.c_uint64), ("launches", C.c_uint64), ("raster_launches", C.c_uint64),
-                ("af_lookups", C.c_uint64), ("af_fallbacks", C.c_uint64)]
+                ("af_lookups", C.c_uint64), ("af_fallbacks", C.c_uint64), ("cover_batches", C.c_uint64),
+                ("cover_rounds", C.c_uint64), ("cover_pairs", C.c_uint64)]
 
 
 class DrawStats(C.Structure):

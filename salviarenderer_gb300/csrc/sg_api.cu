@@ -59,6 +59,7 @@ cudaError_t upload_ewa_table_filter(float const* tab, cudaStream_t s);
 void launch_af_pass(PassParams const& P, AfModelDev const& M, uint32_t num_sms, cudaStream_t s);
 void launch_shade_learned(uint32_t na, PassParams const& P, uint32_t grid, cudaStream_t s);
 void launch_af_count(PassParams const& P, unsigned long long* acc, cudaStream_t s);
+void launch_cover_count(PassParams const& p, unsigned long long* acc, cudaStream_t s);
 uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaStream_t s, unsigned int* status,
                      bool count_pass);
 void launch_mip(uint8_t const* src, uint32_t sw, uint32_t sh, uint8_t* dst, uint32_t dw, uint32_t dh,
@@ -341,7 +342,8 @@ struct sg_device {
   size_t events_used = 0;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;  // (stage, begin, end)
   sg_profile_data prof{};
-  unsigned long long* prof_af = nullptr;   // device: learned-filter lookups and fallbacks while profiling
+  unsigned long long* prof_af = nullptr;   // device, while profiling: learned-filter lookups and fallbacks,
+                                           // coverage batches, rounds and pairs
 };
 
 namespace {
@@ -1170,6 +1172,10 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       else
         launch_cover(P, pl.max_samples, pl.any_early_z, cover_grid, s);
       stage_end(d, 2, ev);
+      if (profile && d->profiling && d->prof_af) {
+        launch_cover_count(P, d->prof_af, s);
+        ++k;
+      }
       ev = stage_begin(d, profile);
       if (P.frag_list) {
         SG_CUDA(d, launch_frag_classes(P, sms, s));
@@ -1783,8 +1789,8 @@ int32_t sg_profile_enable(sg_device* d, int32_t enable) {
   d->marks.clear();
   d->events_used = 0;
   d->prof = sg_profile_data{};
-  if (!d->prof_af) SG_CUDA(d, cudaMalloc(&d->prof_af, 2 * sizeof(unsigned long long)));
-  SG_CUDA(d, cudaMemset(d->prof_af, 0, 2 * sizeof(unsigned long long)));
+  if (!d->prof_af) SG_CUDA(d, cudaMalloc(&d->prof_af, 5 * sizeof(unsigned long long)));
+  SG_CUDA(d, cudaMemset(d->prof_af, 0, 5 * sizeof(unsigned long long)));
   return SG_OK;
 }
 
@@ -1805,10 +1811,13 @@ int32_t sg_profile_read(sg_device* d, sg_profile_data* out) {
   out->merge_ms = acc[4];
   out->raster_ms = acc[2] + acc[3] + acc[4];
   if (d->prof_af) {
-    unsigned long long af[2];
+    unsigned long long af[5];
     SG_CUDA(d, cudaMemcpy(af, d->prof_af, sizeof(af), cudaMemcpyDeviceToHost));
     out->af_lookups = af[0];
     out->af_fallbacks = af[1];
+    out->cover_batches = af[2];
+    out->cover_rounds = af[3];
+    out->cover_pairs = af[4];
   }
   return SG_OK;
 }

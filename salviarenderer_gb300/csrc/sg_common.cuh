@@ -650,6 +650,17 @@ __device__ __forceinline__ v4 sample_impl_t(dev_sampler const& s, float cx, floa
 static __device__ __noinline__ v4 sample_impl(dev_sampler const& s, float cx, float cy, float miplevel, af_info const* af) {
   return wrap8_state(s) ? sample_impl_t<true>(s, cx, cy, miplevel, af) : sample_impl_t<false>(s, cx, cy, miplevel, af);
 }
+// The same, called (INL false) or inlined into the caller (INL true): a call
+// keeps the caller's register count down at the cost of the registers saved
+// around it; inlined, the caller gets registers for both.
+template <bool INL>
+__device__ __forceinline__ v4 sample_impl_sel(dev_sampler const& s, float cx, float cy, float miplevel,
+                                              af_info const* af) {
+  if constexpr (INL)
+    return wrap8_state(s) ? sample_impl_t<true>(s, cx, cy, miplevel, af) : sample_impl_t<false>(s, cx, cy, miplevel, af);
+  else
+    return sample_impl(s, cx, cy, miplevel, af);
+}
 
 __device__ inline float calc_lod_2d(dev_sampler const& s, float dxu, float dxv, float dyu, float dyv) {
   if (s.mip_filter == SG_FILTER_ANISOTROPIC && s.max_anisotropy > 1) {
@@ -714,6 +725,7 @@ __device__ inline v4 sample_cube(dev_sampler const& s, float x, float y, float z
   return mk4(lerp1(c0.x, c0.x, frac), lerp1(c0.y, c0.y, frac), lerp1(c0.z, c0.z, frac), lerp1(c0.w, c0.w, frac));
 }
 
+template <bool INL = false>
 __device__ inline v4 sample_2d_grad(dev_sampler const& s, float u, float v, float dxu, float dxv, float dyu,
                                     float dyv, float bias) {
   af_info af{0, 0, 0, 0, 0};
@@ -724,7 +736,7 @@ __device__ inline v4 sample_2d_grad(dev_sampler const& s, float u, float v, floa
   } else {
     lod = calc_lod(s, dxu, dxv, dyu, dyv, bias);
   }
-  return sample_impl(s, u, v, lod, &af);
+  return sample_impl_sel<INL>(s, u, v, lod, &af);
 }
 
 }  // namespace sg

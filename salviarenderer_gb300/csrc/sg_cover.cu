@@ -475,6 +475,7 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
       for (int i = tid; i < (64 + 64 + 4) * CV_WORDS; i += CV_THREADS) masks[i] = 0;
       uint32_t const nb = cv_fill(P, bpos, end, tile_x0, tile_y0, bx0 * 4, by0 * 4, sh);
       if (nb == 0) break;
+      if (tid == 0) atomicAdd(&P.counters->cover_batches, 1u);
       cv_stage(P, T, nb, tile_x0, tile_y0, bx0, by0, sh);
       __syncthreads();
       // the block's triangles without the hidden ones; the block's four
@@ -530,6 +531,10 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
         __syncthreads();
         // coverage of every pair of the round, spread over all threads
         uint32_t const total = sh.off[64];
+        if (tid == 0) {
+          atomicAdd(&P.counters->cover_rounds, 1u);
+          atomicAdd(&P.counters->cover_pairs, total);
+        }
         for (uint32_t d = tid; d < total; d += CV_THREADS) {
           uint32_t const b = upper_index(sh.off, 64, d), k = d - sh.off[b];
           uint32_t const e8 = sh.slot[b][k];
@@ -624,6 +629,17 @@ __global__ void __launch_bounds__(256) k_cover_rollback(PassParams P) {
       *reinterpret_cast<uint32_t*>(ds_addr(T, tx0 + x, ty0 + y, sm)) = zb[i];
     }
   }
+}
+
+// Adds the pass's coverage work counts to the device's profile totals.
+__global__ void k_cover_count(PassParams P, unsigned long long* acc) {
+  if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
+  acc[2] += P.counters->cover_batches;
+  acc[3] += P.counters->cover_rounds;
+  acc[4] += P.counters->cover_pairs;
+}
+void launch_cover_count(PassParams const& p, unsigned long long* acc, cudaStream_t s) {
+  k_cover_count<<<1, 1, 0, s>>>(p, acc);
 }
 
 void launch_cover_rollback(PassParams const& p, uint32_t grid, cudaStream_t s) {

@@ -43,6 +43,11 @@ struct PassCounters {
   unsigned int af_lookups;           // lookups queued for the learned filter's network
   unsigned int af_fallbacks;         // of those, lookups sent back to the plain sampler
   unsigned int af_plain;             // lookups of learned-filter draws queued for the plain sampler
+  // coverage work (k_cover2): staged batches, walk rounds, (triangle, block)
+  // pairs left after the hierarchical depth test
+  unsigned int cover_batches;
+  unsigned int cover_rounds;
+  unsigned int cover_pairs;
 };
 
 // Per-draw pipeline counters (async_object.h:90-175).

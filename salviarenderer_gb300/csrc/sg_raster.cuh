@@ -713,7 +713,8 @@ struct LineNb {
   __device__ float w(int i) const { return ws[i]; }
 };
 
-template <int NA, class NB>
+// INL: the sampler inlined (sample_impl_sel)
+template <int NA, class NB, bool INL = false>
 __device__ inline v4 run_ps_nb(DrawParams const& D, v4 const* attr, NB const& nb, bool& keep) {
   v4 a0 = NA > 0 ? attr[0] : mk4(0, 0, 0, 0);
   v4 a1 = NA > 1 ? attr[1 < NA ? 1 : 0] : mk4(0, 0, 0, 0);
@@ -725,13 +726,13 @@ __device__ inline v4 run_ps_nb(DrawParams const& D, v4 const* attr, NB const& nb
   case SG_PS_CONSTANT: return mk4(D.ps_k[0], D.ps_k[1], D.ps_k[2], D.ps_k[3]);
   case SG_PS_TEX_MODULATE: {
     float lod = calc_lod_2d(D.ps_samp, u1 - u0, v1 - v0, u2 - u0, v2 - v0);
-    return mulv(sample_impl(D.ps_samp, a0.x, a0.y, lod, nullptr), a1);
+    return mulv(sample_impl_sel<INL>(D.ps_samp, a0.x, a0.y, lod, nullptr), a1);
   }
   case SG_PS_TEX_GRAD_MODULATE:
   case SG_PS_TEX_GRAD_LEARNED:  // the lookups the learned filter does not take
-    return mulv(sample_2d_grad(D.ps_samp, a0.x, a0.y, u1 - u0, v1 - v0, u2 - u0, v2 - v0, 0.0f), a1);
+    return mulv(sample_2d_grad<INL>(D.ps_samp, a0.x, a0.y, u1 - u0, v1 - v0, u2 - u0, v2 - v0, 0.0f), a1);
   case SG_PS_TEX_LOD_MODULATE:  // tex2dlod(s, 0) = s.sample(x, y, w) (cpp_pixel_shader.cpp:33-40)
-    return mulv(sample_impl(D.ps_samp, a0.x, a0.y, a0.w, nullptr), a1);
+    return mulv(sample_impl_sel<INL>(D.ps_samp, a0.x, a0.y, a0.w, nullptr), a1);
   case SG_PS_TEX_PROJ_MODULATE: {  // tex2dproj(s, 0) (cpp_pixel_shader.cpp:42-60)
     float const w0 = nb.w(0), w1 = nb.w(1), w2 = nb.w(2);
     // this pixel's attribute, and it stepped by ddx and by ddy
@@ -740,23 +741,23 @@ __device__ inline v4 run_ps_nb(DrawParams const& D, v4 const* attr, NB const& nb
     float const px = (a0.x / a0.w + 1.0f) * 0.5f, py = (a0.y / a0.w + 1.0f) * 0.5f;
     float const qxx = (nxx / nxw + 1.0f) * 0.5f, qxy = (nxy / nxw + 1.0f) * 0.5f;
     float const qyx = (nyx / nyw + 1.0f) * 0.5f, qyy = (nyy / nyw + 1.0f) * 0.5f;
-    return mulv(sample_2d_grad(D.ps_samp, px, py, qxx - px, qxy - py, qyx - px, qyy - py, 0.0f), a1);
+    return mulv(sample_2d_grad<INL>(D.ps_samp, px, py, qxx - px, qxy - py, qyx - px, qyy - py, 0.0f), a1);
   }
   case SG_PS_TEXCUBE_MODULATE:  // sampler::sample_cube(x, y, z, w) (sampler.cpp:771-829)
     return mulv(sample_cube(D.ps_samp, a0.x, a0.y, a0.z, a0.w), a1);
   case SG_PS_TEX_ALPHA_TEST: {  // tex2d * attr[1], discarded below constants[0] alpha
     float lod = calc_lod_2d(D.ps_samp, u1 - u0, v1 - v0, u2 - u0, v2 - v0);
-    v4 const c = mulv(sample_impl(D.ps_samp, a0.x, a0.y, lod, nullptr), a1);
+    v4 const c = mulv(sample_impl_sel<INL>(D.ps_samp, a0.x, a0.y, lod, nullptr), a1);
     keep = !(c.w < D.ps_k[0]);
     return c;
   }
   default: return mk4(0, 0, 0, 0);
   }
 }
-template <int NA>
+template <int NA, bool INL = false>
 __device__ inline v4 run_ps(DrawParams const& D, v4 const* attr, int, bool& keep) {
   QuadNb const nb(NA > 0 ? attr[0] : mk4(0, 0, 0, 0));
-  return run_ps_nb<NA>(D, attr, nb, keep);
+  return run_ps_nb<NA, QuadNb, INL>(D, attr, nb, keep);
 }
 
 
@@ -919,7 +920,9 @@ __global__ void __launch_bounds__(256, MINB) k_shade(PassParams P) {
             P.frag_color_more[(static_cast<size_t>(f) * 4 + q) * P.more_colors + i] = make_float4(0, 0, 0, 0);
       } else {
         bool keep = true;
-        v4 out = run_ps<NA>(D, attr, q, keep);  // all four lanes of a quad take the same path
+        // all four lanes of a quad take the same path; the 80-register
+        // instances inline the sampler, the 64-register ones call it
+        v4 out = run_ps<NA, (MINB <= 3)>(D, attr, q, keep);
         P.frag_color[static_cast<size_t>(f) * 4 + q] = make_float4(out.x, out.y, out.z, out.w);
         if (P.frag_color_more)  // colours 1..: attributes 1.. of SG_PS_COLOR_MRT, else zero
           for (uint32_t i = 0; i < P.more_colors; ++i) {
