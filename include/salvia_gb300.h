@@ -202,21 +202,38 @@ enum {
 
 /* ---- user shader programs ----------------------------------------------------
  * The reference's applications write shader bodies as C++ classes
- * (cpp_pixel_shader / cpp_blend_shader, shader.h:159-215).  Here a shader
- * body is a class compiled by the application with nvcc against
- * <salvia_gb300/device_shader.cuh> and exported by SALVIA_GB300_PIXEL_SHADER
- * or SALVIA_GB300_BLEND_SHADER as an sg_shader_module: the pass kernels
+ * (cpp_vertex_shader / cpp_pixel_shader / cpp_blend_shader, shader.h:159-215).
+ * Here a shader body is a class compiled by the application with nvcc
+ * against <salvia_gb300/device_shader.cuh> and exported by
+ * SALVIA_GB300_VERTEX_SHADER, SALVIA_GB300_PIXEL_SHADER or
+ * SALVIA_GB300_BLEND_SHADER as an sg_shader_module: the pass kernels
  * instantiated for the class (device code in the application's own module),
  * and the same body compiled for the host, which CPU backends of this ABI
  * run.  sg_shader_register gives the module a program id (at least
  * SG_USER_PROGRAM_BASE) that draws name in sg_shader.program, beside the
- * stock SG_PS_* / SG_BS_* programs.  Pixel shaders read sampler slot 0 and
- * the pixel shader's constants; blend shaders the blend shader's constants.
- * A pass holds draws of at most 8 user pixel shaders and one user blend
- * shader (more split the pass). */
-#define SG_SHADER_ABI_VERSION 1
+ * stock SG_VS_* / SG_PS_* / SG_BS_* programs.  Vertex shaders read sampler
+ * slot 0 and the constants of the draw's vertex shader; pixel shaders those
+ * of its pixel shader; blend shaders the blend shader's constants.  A pass
+ * holds draws of at most one user vertex shader, 8 user pixel shaders and
+ * one user blend shader (more split the pass). */
+#define SG_SHADER_ABI_VERSION 2
 #define SG_USER_PROGRAM_BASE 64
-enum { SG_STAGE_PIXEL = 1, SG_STAGE_BLEND = 2 };
+enum { SG_STAGE_PIXEL = 1, SG_STAGE_BLEND = 2, SG_STAGE_VERTEX = 3 };
+
+/* What a host backend hands a vertex-shader body for one vertex
+ * (cpp_vertex_shader::execute, shader.cpp:520-522): the fetched input
+ * registers (vs_input, stream_assembler.cpp:26-93) and the backend's
+ * sampler::sample for vertex texture fetch (sampler slot 0 of the draw's
+ * vertex shader); the body writes the position and the varyings. */
+typedef struct sg_host_vs_io {
+  float in[SG_MAX_VS_INPUTS][4];       /* vs_input::attribute(i) */
+  uint32_t num_varyings;
+  const float* constants;              /* the vertex shader's SG_MAX_SHADER_CONSTANTS */
+  void* backend;
+  void (*sample)(void* backend, float u, float v, float lod, float out[4]);  /* sampler::sample */
+  float position[4];                   /* out: vs_output::position() */
+  float attr[SG_MAX_VARYINGS][4];      /* out: vs_output::attribute(i) */
+} sg_host_vs_io;
 
 /* What a host backend hands a pixel-shader body for one pixel of a quad
  * (cpp_pixel_shader::execute, cpp_pixel_shader.cpp:62-74): the pixel's
@@ -256,7 +273,7 @@ typedef struct sg_host_bs_io {
 
 typedef struct sg_shader_module {
   uint32_t abi_version;                /* SG_SHADER_ABI_VERSION */
-  uint32_t stage;                      /* SG_STAGE_PIXEL or SG_STAGE_BLEND */
+  uint32_t stage;                      /* SG_STAGE_VERTEX, SG_STAGE_PIXEL or SG_STAGE_BLEND */
   const char* name;
   /* Called by a GPU device at registration, its CUDA device current:
    * prepares the module's kernels there (the sampler's weight table of
@@ -264,11 +281,13 @@ typedef struct sg_shader_module {
   int32_t (*device_init)(const float* ewa_table, void* cuda_stream);
   /* Launches the module's kernel for one pass: `pass` is the library's pass
    * parameter block (opaque here), `key` the shade key of the module's
-   * fragments (pixel stage) or 0 (blend stage: the pass's merge). */
+   * fragments (pixel stage) or 0 (blend stage: the pass's merge; vertex
+   * stage: the pass's geometry, every draw of the pass). */
   void (*device_launch)(const void* pass, uint32_t key, uint32_t grid, void* cuda_stream);
   /* The body compiled for the host: shader_prog's result (0 discards). */
   int32_t (*host_ps)(sg_host_ps_io* io);
   int32_t (*host_bs)(sg_host_bs_io* io);
+  int32_t (*host_vs)(sg_host_vs_io* io);
 } sg_shader_module;
 
 /* ---- descriptors ------------------------------------------------------------ */

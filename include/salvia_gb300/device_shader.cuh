@@ -1,12 +1,13 @@
 // salvia_gb300/device_shader.cuh -- user shader bodies for the GB300 pipeline.
 //
 // The reference's applications write shaders as C++ classes deriving from
-// cpp_pixel_shader / cpp_blend_shader and overriding shader_prog
-// (salvia/include/salvia/core/shader.h:169-215).  Here such a class derives
-// from salvia_gb300::pixel_shader or salvia_gb300::blend_shader, with the
-// same shader_prog signatures and the same helpers (ddx, ddy, tex2d,
-// tex2dlod, tex2dproj, front_face; pixel_accessor::color), written
-// __host__ __device__, and is exported as a shader module:
+// cpp_vertex_shader / cpp_pixel_shader / cpp_blend_shader and overriding
+// shader_prog (salvia/include/salvia/core/shader.h:159-215).  Here such a
+// class derives from salvia_gb300::vertex_shader, pixel_shader or
+// blend_shader, with the same shader_prog signatures and the same helpers
+// (ddx, ddy, tex2d, tex2dlod, tex2dproj, front_face; pixel_accessor::color;
+// a vertex shader's sampler lookup), written __host__ __device__, and is
+// exported as a shader module:
 //
 //     #include <salvia_gb300/device_shader.cuh>
 //     struct my_ps : salvia_gb300::pixel_shader {
@@ -17,6 +18,15 @@
 //       }
 //     };
 //     SALVIA_GB300_PIXEL_SHADER(my_ps)   // extern "C" salvia_gb300_module_my_ps()
+//
+//     struct my_vs : salvia_gb300::vertex_shader {
+//       __host__ __device__ void shader_prog(salvia_gb300::vs_input const& in,
+//                                            salvia_gb300::vs_output& out) const {
+//         out.position = in.attribute(0) * constant(0);
+//         out.attribute(0) = in.attribute(1);
+//       }
+//     };
+//     SALVIA_GB300_VERTEX_SHADER(my_vs)
 //
 // compiled with nvcc for sm_103a into the application (or a shared object):
 //
@@ -46,6 +56,7 @@
 #include "salvia_gb300.h"
 
 #ifdef __CUDACC__
+#include "sg_geometry.cuh"
 #include "sg_raster.cuh"
 #endif
 
@@ -72,6 +83,12 @@ struct vs_output {
   vec4 position;
   vec4 attr[SG_MAX_VARYINGS];
   __host__ __device__ vec4 const& attribute(int i) const { return attr[i]; }
+  __host__ __device__ vec4& attribute(int i) { return attr[i]; }
+};
+// shader_regs.h:16-30: a vertex's input registers (the draw's inputs in order)
+struct vs_input {
+  vec4 attr[SG_MAX_VS_INPUTS];
+  __host__ __device__ vec4 const& attribute(int i) const { return attr[i]; }
 };
 struct ps_output {
   vec4 color[SG_MAX_COLOR_TARGETS];
@@ -83,6 +100,20 @@ struct ps_device_ctx;
 // Gives a shader body's base class its context (device kernel or host io).
 struct shader_access;
 }  // namespace detail
+
+// Base of a user vertex shader (cpp_vertex_shader, shader.h:159-165).  The
+// number and modifiers of its outputs are the draw's num_varyings and
+// varying_modifiers.
+class vertex_shader {
+  friend struct detail::shader_access;
+  void const* ctx_ = nullptr;  // DrawParams (device) or sg_host_vs_io (host)
+
+protected:
+  // sampler::sample(u, v, lod) on sampler slot 0 of the vertex shader
+  // (vertex texture fetch)
+  __host__ __device__ vec4 sample(float u, float v, float lod) const;
+  __host__ __device__ float constant(int i) const;
+};
 
 // Base of a user pixel shader (cpp_pixel_shader, shader.h:169-205).
 class pixel_shader {
@@ -172,6 +203,7 @@ __device__ inline vec4 to_vec4(sg::v4 v) { return vec4(v.x, v.y, v.z, v.w); }
 #endif
 
 struct shader_access {
+  __host__ __device__ static void bind(vertex_shader& s, void const* ctx) { s.ctx_ = ctx; }
   __host__ __device__ static void bind(pixel_shader& s, void const* ctx) { s.ctx_ = ctx; }
   __host__ __device__ static void bind(blend_shader& s, void const* ctx) { s.ctx_ = ctx; }
   __host__ __device__ static void bind(pixel_accessor& a, void const* ctx, uint32_t x, uint32_t y) {
@@ -190,6 +222,28 @@ inline vec4 host_call(sg_host_ps_io const* io, void (*fn)(void*, uint32_t, float
 }
 
 }  // namespace detail
+
+// (device helpers: a draw without a sampler in the slot samples zeros)
+__host__ __device__ inline vec4 vertex_shader::sample(float u, float v, float lod) const {
+#ifdef __CUDA_ARCH__
+  sg::dev_sampler const& sp = static_cast<sg::DrawParams const*>(ctx_)->vs_samp;
+  if (sp.nlevels <= 0) return vec4();
+  return detail::to_vec4(sg::sample_impl(sp, u, v, lod, nullptr));
+#else
+  auto io = static_cast<sg_host_vs_io const*>(ctx_);
+  float o[4] = {0, 0, 0, 0};
+  io->sample(io->backend, u, v, lod, o);
+  return detail::host_out(o);
+#endif
+}
+__host__ __device__ inline float vertex_shader::constant(int i) const {
+  if (i < 0 || i >= SG_MAX_SHADER_CONSTANTS) return 0.0f;
+#ifdef __CUDA_ARCH__
+  return static_cast<sg::DrawParams const*>(ctx_)->vs_k[i];
+#else
+  return static_cast<sg_host_vs_io const*>(ctx_)->constants[i];
+#endif
+}
 
 #ifdef __CUDA_ARCH__
 #define SALVIA_GB300_PS_CTX (*static_cast<detail::ps_device_ctx const*>(ctx_))
@@ -213,6 +267,7 @@ __host__ __device__ inline vec4 pixel_shader::ddy(int reg) const {
 }
 __host__ __device__ inline vec4 pixel_shader::sample(float u, float v, float lod) const {
 #ifdef __CUDA_ARCH__
+  if (SALVIA_GB300_PS_CTX.D->ps_samp.nlevels <= 0) return vec4();
   return detail::to_vec4(sg::sample_impl(SALVIA_GB300_PS_CTX.D->ps_samp, u, v, lod, nullptr));
 #else
   auto io = static_cast<sg_host_ps_io const*>(ctx_);
@@ -224,6 +279,7 @@ __host__ __device__ inline vec4 pixel_shader::sample(float u, float v, float lod
 __host__ __device__ inline vec4 pixel_shader::sample_grad(float u, float v, float dxu, float dxv, float dyu,
                                                           float dyv) const {
 #ifdef __CUDA_ARCH__
+  if (SALVIA_GB300_PS_CTX.D->ps_samp.nlevels <= 0) return vec4();
   return detail::to_vec4(sg::sample_2d_grad(SALVIA_GB300_PS_CTX.D->ps_samp, u, v, dxu, dxv, dyu, dyv, 0.0f));
 #else
   auto io = static_cast<sg_host_ps_io const*>(ctx_);
@@ -234,6 +290,7 @@ __host__ __device__ inline vec4 pixel_shader::sample_grad(float u, float v, floa
 }
 __host__ __device__ inline vec4 pixel_shader::sample_cube(float x, float y, float z, float lod) const {
 #ifdef __CUDA_ARCH__
+  if (SALVIA_GB300_PS_CTX.D->ps_samp.nlevels <= 0) return vec4();
   return detail::to_vec4(sg::sample_cube(SALVIA_GB300_PS_CTX.D->ps_samp, x, y, z, lod));
 #else
   auto io = static_cast<sg_host_ps_io const*>(ctx_);
@@ -348,6 +405,20 @@ __host__ __device__ inline void pixel_accessor::color(int target, int sample, ve
 
 #ifdef __CUDACC__
 namespace sg {
+
+// A user vertex shader on one vertex: its input registers to the position
+// and the NA varyings.
+template <class UVS, int NA>
+__device__ void user_vs(DrawParams const& D, v4 const* in, v4* out) {
+  salvia_gb300::vs_input vin;
+  for (int r = 0; r < SG_MAX_VS_INPUTS; ++r) vin.attr[r] = salvia_gb300::detail::to_vec4(in[r]);
+  salvia_gb300::vs_output vout;
+  UVS vs;
+  salvia_gb300::detail::shader_access::bind(vs, &D);
+  vs.shader_prog(vin, vout);
+  out[0] = mk4(vout.position.x, vout.position.y, vout.position.z, vout.position.w);
+  for (int i = 0; i < NA; ++i) out[1 + i] = mk4(vout.attr[i].x, vout.attr[i].y, vout.attr[i].z, vout.attr[i].w);
+}
 
 // A user blend shader on one sample: ps_output from the fragment's colours.
 template <class UBS>
@@ -481,6 +552,43 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge_user(PassParams P) {
                : 1;                                                                                            \
   }
 
+// Exports a vertex-shader class as extern "C" salvia_gb300_module_<cls>():
+// the pass's geometry kernel instantiated for it (every draw of the pass; a
+// pass holds one user vertex shader).
+#define SALVIA_GB300_VERTEX_SHADER(cls)                                                                        \
+  SALVIA_GB300_MODULE_INIT_(cls)                                                                               \
+  __global__ void __launch_bounds__(128) salvia_gb300_geometry_##cls(sg::PassParams P) {                     \
+    sg::geometry_pass<cls>(P);                                                                                 \
+  }                                                                                                            \
+  static void salvia_gb300_launch_##cls(const void* pass, uint32_t, uint32_t grid, void* stream) {            \
+    salvia_gb300_geometry_##cls<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(                         \
+        *static_cast<sg::PassParams const*>(pass));                                                            \
+  }                                                                                                            \
+  static int32_t salvia_gb300_host_##cls(sg_host_vs_io* io) {                                                \
+    salvia_gb300::vs_input in;                                                                                 \
+    for (int i = 0; i < SG_MAX_VS_INPUTS; ++i) in.attr[i] = salvia_gb300::detail::host_out(io->in[i]);        \
+    salvia_gb300::vs_output out;                                                                               \
+    cls vs;                                                                                                    \
+    salvia_gb300::detail::shader_access::bind(vs, io);                                                         \
+    vs.shader_prog(in, out);                                                                                   \
+    io->position[0] = out.position.x;                                                                          \
+    io->position[1] = out.position.y;                                                                          \
+    io->position[2] = out.position.z;                                                                          \
+    io->position[3] = out.position.w;                                                                          \
+    for (int i = 0; i < SG_MAX_VARYINGS; ++i) {                                                                \
+      io->attr[i][0] = out.attr[i].x;                                                                          \
+      io->attr[i][1] = out.attr[i].y;                                                                          \
+      io->attr[i][2] = out.attr[i].z;                                                                          \
+      io->attr[i][3] = out.attr[i].w;                                                                          \
+    }                                                                                                          \
+    return 1;                                                                                                  \
+  }                                                                                                            \
+  extern "C" sg_shader_module const* salvia_gb300_module_##cls() {                                            \
+    static sg_shader_module const m = {SG_SHADER_ABI_VERSION, SG_STAGE_VERTEX, #cls, salvia_gb300_init_##cls, \
+                                       salvia_gb300_launch_##cls, nullptr, nullptr, salvia_gb300_host_##cls}; \
+    return &m;                                                                                                 \
+  }
+
 // Exports a pixel-shader class as extern "C" salvia_gb300_module_<cls>().
 #define SALVIA_GB300_PIXEL_SHADER(cls)                                                                         \
   SALVIA_GB300_MODULE_INIT_(cls)                                                                               \
@@ -507,7 +615,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge_user(PassParams P) {
   }                                                                                                            \
   extern "C" sg_shader_module const* salvia_gb300_module_##cls() {                                            \
     static sg_shader_module const m = {SG_SHADER_ABI_VERSION, SG_STAGE_PIXEL, #cls, salvia_gb300_init_##cls,  \
-                                       salvia_gb300_launch_##cls, salvia_gb300_host_##cls, nullptr};           \
+                                       salvia_gb300_launch_##cls, salvia_gb300_host_##cls, nullptr, nullptr};  \
     return &m;                                                                                                 \
   }
 
@@ -529,7 +637,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge_user(PassParams P) {
   }                                                                                                            \
   extern "C" sg_shader_module const* salvia_gb300_module_##cls() {                                            \
     static sg_shader_module const m = {SG_SHADER_ABI_VERSION, SG_STAGE_BLEND, #cls, salvia_gb300_init_##cls,  \
-                                       salvia_gb300_launch_##cls, nullptr, salvia_gb300_host_##cls};           \
+                                       salvia_gb300_launch_##cls, nullptr, salvia_gb300_host_##cls, nullptr};  \
     return &m;                                                                                                 \
   }
 #endif  // __CUDACC__

@@ -748,6 +748,21 @@ private:
 };
 // A user pixel or blend shader (a registered module's program id); its
 // constants and sampler are declared by a subclass as for any cpp shader.
+// A registered user vertex shader module (SALVIA_GB300_VERTEX_SHADER): the
+// application declares its constants (up to SG_MAX_SHADER_CONSTANTS floats,
+// in declaration order) and its sampler like any cpp_vertex_shader.
+class module_vertex_shader : public cpp_vertex_shader {
+public:
+  module_vertex_shader(uint32_t program_id, uint32_t num_attributes, uint32_t modifiers = am::am_linear)
+      : prog_(program_id), nattr_(num_attributes), mods_(modifiers) {}
+  uint32_t program() const override { return prog_; }
+  uint32_t num_output_attributes() const override { return nattr_; }
+  uint32_t output_attribute_modifiers(uint32_t) const override { return mods_; }
+  SALVIA_GB300_CLONE(module_vertex_shader)
+
+private:
+  uint32_t prog_, nattr_, mods_;
+};
 class module_pixel_shader : public cpp_pixel_shader {
 public:
   explicit module_pixel_shader(uint32_t program_id) : prog_(program_id) {}
@@ -905,7 +920,8 @@ public:
   // No counterpart in the reference: makes a user shader module
   // (salvia_gb300/device_shader.cuh) a program of this renderer's device; a
   // cpp_pixel_shader / cpp_blend_shader subclass returns the id from
-  // program() (module_pixel_shader / module_blend_shader do).  0 on failure.
+  // program() (module_vertex_shader / module_pixel_shader /
+  // module_blend_shader do).  0 on failure.
   uint32_t register_shader(sg_shader_module const* m) {
     uint32_t id = 0;
     return sg_shader_register(dev_->dev, m, &id) == SG_OK ? id : 0u;

@@ -74,7 +74,31 @@ public:
     }
   }
 
+  sg_shader_module const* user = nullptr;  // a user vertex shader's module
+
+  // the reference's sampler::sample for a user body's vertex texture fetch
+  static void io_sample(void* b, float u, float v, float lod, float out[4]) {
+    color_rgba32f const c = static_cast<ref_vs*>(b)->samp->sample(u, v, lod);
+    out[0] = c.r;
+    out[1] = c.g;
+    out[2] = c.b;
+    out[3] = c.a;
+  }
+
   void shader_prog(vs_input const& in, vs_output& out) override {
+    if (user) {  // the user body, compiled for the host
+      sg_host_vs_io io{};
+      for (uint32_t r = 0; r < SG_MAX_VS_INPUTS; ++r)
+        for (int k = 0; k < 4; ++k) io.in[r][k] = in.attribute(r)[k];
+      io.num_varyings = nvary;
+      io.constants = prog.constants;
+      io.backend = this;
+      io.sample = io_sample;
+      user->host_vs(&io);
+      out.position() = vec4(io.position[0], io.position[1], io.position[2], io.position[3]);
+      for (uint32_t i = 0; i < nvary; ++i) out.attribute(i) = vec4(io.attr[i][0], io.attr[i][1], io.attr[i][2], io.attr[i][3]);
+      return;
+    }
     mat44 m = load_mat(prog.constants);
     switch (prog.program) {
     case SG_VS_TRANSFORM:
@@ -274,7 +298,8 @@ extern "C" {
 int32_t sg_shader_register(sg_device* d, const sg_shader_module* m, uint32_t* out) {
   if (!d || !m || !out || m->abi_version != SG_SHADER_ABI_VERSION ||
       (m->stage == SG_STAGE_PIXEL && !m->host_ps) || (m->stage == SG_STAGE_BLEND && !m->host_bs) ||
-      (m->stage != SG_STAGE_PIXEL && m->stage != SG_STAGE_BLEND))
+      (m->stage == SG_STAGE_VERTEX && !m->host_vs) ||
+      (m->stage != SG_STAGE_PIXEL && m->stage != SG_STAGE_BLEND && m->stage != SG_STAGE_VERTEX))
     return SG_INVALID_PARAMETER;
   for (size_t i = 0; i < d->user_shaders.size(); ++i)
     if (d->user_shaders[i] == m) {
@@ -472,6 +497,10 @@ int32_t sg_draw(sg_device* d, const sg_draw_desc* desc, sg_draw_stats* stats) {
       colors.push_back(d->textures[desc->more_color_targets[i]]->subresource(0));
   }
   ps->nattr = desc->num_varyings;
+  if (desc->vs.program >= SG_USER_PROGRAM_BASE) {
+    if (desc->vs.program - SG_USER_PROGRAM_BASE >= d->user_shaders.size()) return SG_INVALID_PARAMETER;
+    vs->user = d->user_shaders[desc->vs.program - SG_USER_PROGRAM_BASE];
+  }
   if (desc->ps.program >= SG_USER_PROGRAM_BASE) {
     if (desc->ps.program - SG_USER_PROGRAM_BASE >= d->user_shaders.size()) return SG_INVALID_PARAMETER;
     ps->user = d->user_shaders[desc->ps.program - SG_USER_PROGRAM_BASE];

@@ -884,11 +884,36 @@ vec4 sample_level0(sampler const& sp, float u, float v) {  // sampler::sample(u,
   return sample_impl(sp, u, v, 0.0f, nullptr);
 }
 
+// sampler::sample for a user vertex body's vertex texture fetch
+void uvs_sample(void* b, float u, float v, float lod, float out[4]) {
+  sampler const* sp = static_cast<draw_ctx const*>(b)->vs_samp;
+  if (!sp) {  // no sampler in the slot: zeros (as on the device)
+    for (int k = 0; k < 4; ++k) out[k] = 0.0f;
+    return;
+  }
+  vec4 const r = sample_impl(*sp, u, v, lod, nullptr);
+  for (int k = 0; k < 4; ++k) out[k] = r[k];
+}
+
 void run_vs(draw_ctx const& c, uint32_t index, vso& out) {
   vec4 in[SG_MAX_VS_INPUTS];
   for (auto& x : in) x = mk(0, 0, 0, 0);
   fetch_vertex(c, index, in);
   sg_shader const& s = c.d->vs;
+  if (s.program >= SG_USER_PROGRAM_BASE) {  // a user vertex shader's host body
+    sg_shader_module const* m = c.dev->user_shaders[s.program - SG_USER_PROGRAM_BASE];
+    sg_host_vs_io io{};
+    for (int r = 0; r < SG_MAX_VS_INPUTS; ++r)
+      for (int k = 0; k < 4; ++k) io.in[r][k] = in[r][k];
+    io.num_varyings = c.nattr;
+    io.constants = s.constants;
+    io.backend = const_cast<draw_ctx*>(&c);
+    io.sample = uvs_sample;
+    m->host_vs(&io);
+    out.pos() = mk(io.position[0], io.position[1], io.position[2], io.position[3]);
+    for (uint32_t i = 0; i < c.nattr; ++i) out.r[1 + i] = mk(io.attr[i][0], io.attr[i][1], io.attr[i][2], io.attr[i][3]);
+    return;
+  }
   switch (s.program) {
   case SG_VS_TRANSFORM:
     out.pos() = transform(in[0], s.constants);
@@ -1411,7 +1436,14 @@ void ups_ddy(void* b, uint32_t reg, float out[4]) {
 void ups_put(vec4 const& v, float out[4]) {
   for (int k = 0; k < 4; ++k) out[k] = v[k];
 }
+// a draw without a sampler in the slot samples zeros (as on the device)
+bool ups_no_sampler(void* b, float out[4]) {
+  if (static_cast<user_ps_backend*>(b)->c->ps_samp) return false;
+  for (int k = 0; k < 4; ++k) out[k] = 0.0f;
+  return true;
+}
 void ups_tex2d(void* b, uint32_t reg, float out[4]) {
+  if (ups_no_sampler(b, out)) return;
   auto& u = *static_cast<user_ps_backend*>(b);
   vec4 dx = sub(u.quad[1].r[1 + reg], u.quad[0].r[1 + reg]), dy = sub(u.quad[2].r[1 + reg], u.quad[0].r[1 + reg]);
   float lod = calc_lod_2d(*u.c->ps_samp, dx[0], dx[1], dy[0], dy[1]);
@@ -1419,11 +1451,13 @@ void ups_tex2d(void* b, uint32_t reg, float out[4]) {
   ups_put(sample_impl(*u.c->ps_samp, a[0], a[1], lod, nullptr), out);
 }
 void ups_tex2dlod(void* b, uint32_t reg, float out[4]) {
+  if (ups_no_sampler(b, out)) return;
   auto& u = *static_cast<user_ps_backend*>(b);
   vec4 const& a = u.quad[u.i].r[1 + reg];
   ups_put(sample_impl(*u.c->ps_samp, a[0], a[1], a[3], nullptr), out);
 }
 void ups_tex2dproj(void* b, uint32_t reg, float out[4]) {
+  if (ups_no_sampler(b, out)) return;
   auto& u = *static_cast<user_ps_backend*>(b);
   vec4 const& a = u.quad[u.i].r[1 + reg];
   vec4 nx = add(a, sub(u.quad[1].r[1 + reg], u.quad[0].r[1 + reg]));
@@ -1435,12 +1469,15 @@ void ups_tex2dproj(void* b, uint32_t reg, float out[4]) {
           out);
 }
 void ups_sample(void* b, float u_, float v, float lod, float out[4]) {
+  if (ups_no_sampler(b, out)) return;
   ups_put(sample_impl(*static_cast<user_ps_backend*>(b)->c->ps_samp, u_, v, lod, nullptr), out);
 }
 void ups_sample_grad(void* b, float u_, float v, float dxu, float dxv, float dyu, float dyv, float out[4]) {
+  if (ups_no_sampler(b, out)) return;
   ups_put(sample_2d_grad(*static_cast<user_ps_backend*>(b)->c->ps_samp, u_, v, dxu, dxv, dyu, dyv, 0.0f), out);
 }
 void ups_sample_cube(void* b, float x, float y, float z, float lod, float out[4]) {
+  if (ups_no_sampler(b, out)) return;
   ups_put(sample_cube(*static_cast<user_ps_backend*>(b)->c->ps_samp, x, y, z, lod), out);
 }
 bool run_user_ps(draw_ctx const& c, vso const* quad, int i, vec4& out, vec4* more) {
@@ -1919,6 +1956,15 @@ int32_t do_draw(device_state* dev, sg_draw_desc const* d, sg_draw_stats* stats_o
   bool const wire = !lines && d->raster.fill_mode == SG_FILL_WIREFRAME;
   if ((lines || wire) && (d->ps.program >= SG_USER_PROGRAM_BASE || d->bs.program >= SG_USER_PROGRAM_BASE))
     return SG_INVALID_PARAMETER;
+  // user programs: registered modules of the stage
+  auto user_ok = [&](uint32_t prog, uint32_t stage) {
+    if (prog < SG_USER_PROGRAM_BASE) return true;
+    size_t const i = prog - SG_USER_PROGRAM_BASE;
+    return i < dev->user_shaders.size() && dev->user_shaders[i]->stage == stage;
+  };
+  if (!user_ok(d->vs.program, SG_STAGE_VERTEX) || !user_ok(d->ps.program, SG_STAGE_PIXEL) ||
+      !user_ok(d->bs.program, SG_STAGE_BLEND))
+    return SG_INVALID_PARAMETER;
   if (d->num_varyings > SG_MAX_VARYINGS || d->num_inputs > SG_MAX_VS_INPUTS)
     return SG_INVALID_PARAMETER;
   if (d->color_target) {
@@ -2304,7 +2350,8 @@ int32_t sg_resolve(sg_device* d, uint32_t src, uint32_t dst) {
 int32_t sg_shader_register(sg_device* d, const sg_shader_module* m, uint32_t* out) {
   if (!d || !m || !out || m->abi_version != SG_SHADER_ABI_VERSION ||
       (m->stage == SG_STAGE_PIXEL && !m->host_ps) || (m->stage == SG_STAGE_BLEND && !m->host_bs) ||
-      (m->stage != SG_STAGE_PIXEL && m->stage != SG_STAGE_BLEND))
+      (m->stage == SG_STAGE_VERTEX && !m->host_vs) ||
+      (m->stage != SG_STAGE_PIXEL && m->stage != SG_STAGE_BLEND && m->stage != SG_STAGE_VERTEX))
     return SG_INVALID_PARAMETER;
   auto& v = d->st.user_shaders;
   for (size_t i = 0; i < v.size(); ++i)

@@ -189,6 +189,7 @@ struct PassPlan {
   uint32_t more_colors = 0;                  // most colour targets after the first of any of its targets
   std::vector<sg_shader_module const*> user_ps;  // its user pixel shaders: shade key USER_CLASS * 8 + index
   sg_shader_module const* user_bs = nullptr;     // its user blend shader (the merge runs that module's kernel)
+  sg_shader_module const* user_vs = nullptr;     // its user vertex shader (the geometry runs that module's kernel)
   std::set<uint32_t> af_textures;            // textures its learned-filter draws take feature taps from
   uint64_t nprims = 0;
   uint64_t samples = 0;                      // target samples of the pass's targets
@@ -545,6 +546,7 @@ struct DrawInfo {
   uint32_t tex[2] = {0, 0};         // sampled textures
   sg_shader_module const* user_ps = nullptr;  // a user pixel shader's module
   sg_shader_module const* user_bs = nullptr;  // a user blend shader's module
+  sg_shader_module const* user_vs = nullptr;  // a user vertex shader's module
   uint32_t af_model = 0;            // learned filter of an SG_PS_TEX_GRAD_LEARNED draw
   uint32_t af_texture = 0;          // the texture its feature taps read
 };
@@ -641,9 +643,10 @@ int32_t translate_draw(sg_device* d, sg_draw_desc const* desc, DrawParams& p, Dr
   };
   info.user_ps = user_module(p.ps_prog, SG_STAGE_PIXEL);
   info.user_bs = user_module(p.bs_prog, SG_STAGE_BLEND);
+  info.user_vs = user_module(p.vs_prog, SG_STAGE_VERTEX);
   // line pixels are shaded and merged by k_lines: stock programs only
   if (line_mode && (p.ps_prog >= SG_USER_PROGRAM_BASE || p.bs_prog >= SG_USER_PROGRAM_BASE)) return SG_INVALID_PARAMETER;
-  if (p.vs_prog < SG_VS_TRANSFORM || p.vs_prog > SG_VS_MORPH_DISPLACE ||
+  if (((p.vs_prog < SG_VS_TRANSFORM || p.vs_prog > SG_VS_MORPH_DISPLACE) && !info.user_vs) ||
       ((p.ps_prog < SG_PS_COLOR || p.ps_prog > SG_PS_TEXCUBE_MODULATE) && !info.user_ps) ||
       ((p.bs_prog < SG_BS_REPLACE || p.bs_prog > SG_BS_REPLACE_ALL) && !info.user_bs))
     return SG_INVALID_PARAMETER;
@@ -771,6 +774,7 @@ bool draw_fits(sg_device* d, PassPlan const& pl, DrawParams const& p, DrawInfo c
   }
   if (info.af_model && pl.af_model && info.af_model != pl.af_model) return false;
   if (info.user_bs && pl.user_bs && info.user_bs != pl.user_bs) return false;  // one user merge per pass
+  if (info.user_vs && pl.user_vs && info.user_vs != pl.user_vs) return false;  // one user geometry per pass
   if (info.user_ps && pl.user_ps.size() >= 8 &&
       std::find(pl.user_ps.begin(), pl.user_ps.end(), info.user_ps) == pl.user_ps.end())
     return false;
@@ -820,6 +824,7 @@ void add_draw(sg_device* d, PassPlan& pl, DrawParams p, DrawInfo const& info, ui
     p.shade_key = USER_SHADE_CLASS * 8u + slot;
   }
   if (info.user_bs) pl.user_bs = info.user_bs;
+  if (info.user_vs) pl.user_vs = info.user_vs;
   pl.lines = p.line_mode != 0;
   pl.slots += uint64_t(p.slots_per_prim) * p.prim_count;
   p.prim_base = static_cast<uint32_t>(pl.nprims);
@@ -1141,7 +1146,10 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       uint32_t cover_grid = std::min<uint32_t>(pl.ntiles * 16, sms * 4);
       uint32_t shade_grid = sms * tu.shade_ctas_per_sm;
       cudaEvent_t ev = stage_begin(d, profile);
-      launch_geometry(P, s);
+      if (pl.user_vs)  // the geometry with the pass's user vertex shader, every draw
+        pl.user_vs->device_launch(&P, 0u, (pl.nprims + 127) / 128, s);
+      else
+        launch_geometry(P, s);
       stage_end(d, 0, ev);
       ev = stage_begin(d, profile);
       SG_CUDA(d, cudaMemsetAsync(P.bin_counts, 0, pl.ncounts * 4, s));
@@ -2013,7 +2021,7 @@ int32_t sg_draw_static_scratch(sg_device* d, const sg_draw_desc* desc, sg_draw_s
 int32_t sg_shader_register(sg_device* d, const sg_shader_module* m, uint32_t* out) {
   if (!d || !m || !out) return SG_INVALID_PARAMETER;
   if (m->abi_version != SG_SHADER_ABI_VERSION || !m->device_init || !m->device_launch ||
-      (m->stage != SG_STAGE_PIXEL && m->stage != SG_STAGE_BLEND))
+      (m->stage != SG_STAGE_PIXEL && m->stage != SG_STAGE_BLEND && m->stage != SG_STAGE_VERTEX))
     return SG_INVALID_PARAMETER;
   for (size_t i = 0; i < d->user_shaders.size(); ++i)
     if (d->user_shaders[i] == m) {

@@ -614,7 +614,7 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
                   ps=abi.PS_COLOR, sampler=None, modifiers=(abi.AM_LINEAR, abi.AM_LINEAR),
                   color_fmt=abi.FMT_RGBA8, ds_fmt=abi.FMT_RG32F, tex_size=64, uv_scale=3.0,
                   eye_dist=(2.2, 3.2), draws=1, clear_depth=1.0, uv_w=None, ps_constants=None, stencil=None,
-                  bs_constants=None, fill_mode=abi.FILL_SOLID):
+                  bs_constants=None, fill_mode=abi.FILL_SOLID, user_vs=None, vs_shear=0.25):
     """A small scene that exercises one combination of pipeline state.
 
     Vertices carry position, a (u, v) pair and an RGBA colour.  Strips and
@@ -654,6 +654,10 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
     if ps in abi.TEXTURED_PS or isinstance(ps, str):  # user pixel shaders sample slot 0
         s.textures["tex"] = (to_rgba8(value_noise(rng, tex_size, octaves=4)), True)
         s.samplers["s0"] = ("tex", dict(sampler or {}))
+    if user_vs is not None:  # a user vertex shader: the matrix, the shear, a vertex texture to fetch
+        s.textures["vtex"] = (to_rgba8(value_noise(rng, 32, octaves=3)), False)
+        s.samplers["vs0"] = ("vtex", dict(min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+                                          mip_filter=abi.FILTER_POINT))
     dsd = default_depth_stencil(depth_func=depth_func, depth_enable=depth_enable,
                                 depth_write=depth_write)
     if stencil is not None:  # (func, pass_op, ref) on both faces: late depth test
@@ -672,7 +676,8 @@ def feature_scene(seed=1, width=96, height=80, samples=1, ntris=120, topology=ab
                   num_varyings=len(modifiers), varying_modifiers=list(modifiers),
                   cull_mode=cull, front_ccw=front_ccw, depth_stencil=dsd, fill_mode=fill_mode,
                   base_vertex=base_vertex, stencil_ref=stencil[2] if stencil is not None else 0,
-                  vs=dict(program=abi.VS_TRANSFORM, constants=mvp),
+                  vs=(dict(program=abi.VS_TRANSFORM, constants=mvp) if user_vs is None else
+                      dict(program=user_vs, constants=list(mvp.ravel()) + [vs_shear], samplers=["vs0"])),
                   ps=dict(program=ps, samplers=["s0"] if "s0" in s.samplers else [],
                           constants=list(ps_constants or [])),
                   bs=dict(program=blend, constants=list(bs_constants or [])))

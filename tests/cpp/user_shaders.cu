@@ -46,3 +46,26 @@ struct screen_blend_bs : salvia_gb300::blend_shader {
   }
 };
 SALVIA_GB300_BLEND_SHADER(screen_blend_bs)
+
+// A vertex shader with a height-dependent shear and a vertex texture fetch:
+// x += y^2 * constant(16), then the row-vector transform by the matrix in
+// constants 0-15 (eflib::transform's dot products, left to right); the
+// texture coordinate (register 1) passes through, and the colour (register
+// 2) is modulated by the texel fetched at it (sampler::sample, level 0).
+struct shear_fetch_vs : salvia_gb300::vertex_shader {
+  __host__ __device__ void shader_prog(salvia_gb300::vs_input const& in, vs_output& out) const {
+    vec4 p = in.attribute(0);
+    p.x = p.x + (p.y * p.y) * constant(16);
+    vec4 o;
+    o.x = ((p.x * constant(0) + p.y * constant(4)) + p.z * constant(8)) + p.w * constant(12);
+    o.y = ((p.x * constant(1) + p.y * constant(5)) + p.z * constant(9)) + p.w * constant(13);
+    o.z = ((p.x * constant(2) + p.y * constant(6)) + p.z * constant(10)) + p.w * constant(14);
+    o.w = ((p.x * constant(3) + p.y * constant(7)) + p.z * constant(11)) + p.w * constant(15);
+    out.position = o;
+    vec4 const uv = in.attribute(1);
+    out.attribute(0) = uv;
+    vec4 const t = sample(uv.x, uv.y, 0.0f);
+    out.attribute(1) = in.attribute(2) * vec4(t.x, t.y, t.z, 1.0f);
+  }
+};
+SALVIA_GB300_VERTEX_SHADER(shear_fetch_vs)

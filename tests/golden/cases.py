@@ -102,6 +102,13 @@ CASES = {
                                       blend="user:screen_blend_bs", bs_constants=[0.6]),
     "user_ps_front_proj_back_lod": lambda: F(seed=72, ps="user:proj_or_lod_ps", sampler=TRILINEAR,
                                              uv_w=(0.5, 2.0), blend=abi.BS_LERP_SRC_ALPHA),
+    # a user vertex shader (a shear and a vertex texture fetch), alone and
+    # with a user pixel shader at 4x
+    "user_vs_shear_fetch": lambda: F(seed=73, user_vs="user:shear_fetch_vs", ps=abi.PS_TEX_MODULATE,
+                                     sampler=TRILINEAR, ntris=150),
+    "user_vs_ps_4x": lambda: F(seed=74, user_vs="user:shear_fetch_vs", vs_shear=-0.4,
+                               ps="user:tinted_alpha_test_ps", sampler=TRILINEAR, samples=4, ntris=130,
+                               ps_constants=[0.9, 0.6, 0.3, 0.7, 40.0, 0.45]),
     # cube maps (sampler::sample_cube, sampler.cpp:771-829): directions whose
     # major axis is +x, the only face the reference's cube textures reach;
     # levels on both sides of the magnification threshold

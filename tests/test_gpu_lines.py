@@ -70,6 +70,9 @@ LINE_CASES = {
     "noperspective_nointerp": dict(topology=abi.TOPOLOGY_LINE_STRIP,
                                    modifiers=(abi.AM_NOPERSPECTIVE, abi.AM_NOINTERPOLATION)),
     "wireframe": dict(fill_mode=abi.FILL_WIREFRAME),
+    "user_vs_lines": dict(topology=abi.TOPOLOGY_LINE_STRIP, user_vs="user:shear_fetch_vs", ps=abi.PS_TEX_MODULATE,
+                          sampler=dict(min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+                                       mip_filter=abi.FILTER_LINEAR)),
     "wireframe_strip_cull_back": dict(fill_mode=abi.FILL_WIREFRAME, topology=abi.TOPOLOGY_TRIANGLE_STRIP,
                                       cull=abi.CULL_BACK),
     "wireframe_near_clip": dict(fill_mode=abi.FILL_WIREFRAME, eye_dist=(0.6, 1.0)),
