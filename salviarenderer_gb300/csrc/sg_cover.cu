@@ -64,7 +64,7 @@ struct CvShared {
   // dense pair numbering, and each pair's coverage (uncut, cut to the
   // target; quad-major, so quad q's 16 bits are its 16-bit word q)
   uint8_t slot[64][CV_K];
-  uint32_t cnt[64], off[65];
+  uint32_t off[64], wtot[CV_THREADS / 32];
   unsigned long long cov_uc[64][CV_K], cov_cv[64][CV_K];
   float spx[4], spy[4];
   uint32_t item;
@@ -513,30 +513,37 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
         bool more = false;
 #pragma unroll
         for (int w = 0; w < CV_WORDS; ++w) more = more || live[w] != 0;
-        if (q == 0) sh.cnt[ib] = n;
-        __syncthreads();
-        if (tid < 32) {  // offsets of the blocks in the dense pair numbering
-          uint32_t const c0 = sh.cnt[2 * tid], c1 = sh.cnt[2 * tid + 1];
-          uint32_t incl = c0 + c1;
+        {  // the blocks' offsets in the dense pair numbering: within each warp
+           // (its eight blocks) by a shuffle scan, across warps by their totals
+          uint32_t const lane = tid & 31, v = q == 0 ? n : 0u;
+          uint32_t incl = v;
 #pragma unroll
           for (int o = 1; o < 32; o <<= 1) {
             uint32_t const y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (tid >= o) incl += y;
+            if (lane >= static_cast<uint32_t>(o)) incl += y;
           }
-          uint32_t const excl = incl - (c0 + c1);
-          sh.off[2 * tid] = excl;
-          sh.off[2 * tid + 1] = excl + c0;
-          if (tid == 31) sh.off[64] = incl;
+          if (q == 0) sh.off[ib] = incl - v;  // warp-local
+          if (lane == 31) sh.wtot[tid >> 5] = incl;
         }
         __syncthreads();
         // coverage of every pair of the round, spread over all threads
-        uint32_t const total = sh.off[64];
+        uint32_t total = 0;
+#pragma unroll
+        for (int w = 0; w < CV_THREADS / 32; ++w) total += sh.wtot[w];
         if (tid == 0) {
           atomicAdd(&P.counters->cover_rounds, 1u);
           atomicAdd(&P.counters->cover_pairs, total);
         }
         for (uint32_t d = tid; d < total; d += CV_THREADS) {
-          uint32_t const b = upper_index(sh.off, 64, d), k = d - sh.off[b];
+          uint32_t w = 0, base = 0;
+          for (;;) {  // the warp whose blocks hold pair d (d < total: one does)
+            uint32_t const t = sh.wtot[w];
+            if (d < base + t || w + 1 == CV_THREADS / 32) break;
+            base += t;
+            ++w;
+          }
+          uint32_t const dl = d - base;
+          uint32_t const b = w * 8 + upper_index(sh.off + w * 8, 8, dl), k = dl - sh.off[b];
           uint32_t const e8 = sh.slot[b][k];
           int const pbx = tile_x0 + (bx0 + static_cast<int>(b & 7)) * 4;
           int const pby = tile_y0 + (by0 + static_cast<int>(b >> 3)) * 4;
