@@ -148,65 +148,10 @@ __device__ inline void vp_project(DrawParams const& D, vtx<NA>& v) {
 }
 
 // rasterizer::compute_triangle_info (rasterizer.cpp:864-945) + compute_derivative_n
-// (shader.cpp:414-449); writes the record, returns false for zero area.
-template <int NA>
-__device__ bool setup_triangle(uint32_t draw, uint32_t zcfg, uint32_t shade_key, vtx<NA> const& a, vtx<NA> const& b, vtx<NA> const& c,
-                               float4* rec) {
-  vtx<NA> const* verts[3] = {&a, &b, &c};
-  double dist[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-    dist[i] = fabs(static_cast<double>(verts[i]->r[0].x)) + fabs(static_cast<double>(verts[i]->r[0].y));
-  int r0;
-  if (dist[0] < dist[1])
-    r0 = dist[0] < dist[2] ? 0 : 2;
-  else
-    r0 = dist[1] < dist[2] ? 1 : 2;
-  int r1 = (r0 + 1) % 3, r2 = (r1 + 1) % 3;
-  vtx<NA> const& v0 = *verts[r0];
-  vtx<NA> const& v1 = *verts[r1];
-  vtx<NA> const& v2 = *verts[r2];
-  v4 e01p = v1.r[0] - v0.r[0], e02p = v2.r[0] - v0.r[0];
-  float area = e02p.x * e01p.y - e02p.y * e01p.x;
-  if (eq_eps(area, 0.0f)) return false;
-  float inv_area = 1.0f / area;
-  v4 pa = a.r[0], pb = b.r[0], pc = c.r[0];
-  float4 bb = make_float4(smin(smin(pa.x, pb.x), pc.x), smax(smax(pa.x, pb.x), pc.x),
-                          smin(smin(pa.y, pb.y), pc.y), smax(smax(pa.y, pb.y), pc.y));
-  v4 vp[3] = {pa, pb, pc};
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    v4 s = vp[i], e = vp[(i + 1) % 3];
-    rec[i] = make_float4(s.y - e.y, e.x - s.x, e.x * s.y - e.y * s.x, 0.0f);
-  }
-  rec[3] = bb;
-  float e01x = e01p.x, e01y = e01p.y, e02x = e02p.x, e02y = e02p.y;
-  constexpr int R = 1 + NA;
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    v4 e01 = v1.r[i] - v0.r[i], e02 = v2.r[i] - v0.r[i];
-    float xd[4], yd[4];
-    float const* p01 = &e01.x;
-    float const* p02 = &e02.x;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      xd[k] = (p02[k] * e01y - p01[k] * e02y) * inv_area;
-      yd[k] = (p01[k] * e02x - p02[k] * e01x) * inv_area;
-    }
-    rec[5 + i] = make_float4(v0.r[i].x, v0.r[i].y, v0.r[i].z, v0.r[i].w);
-    rec[5 + R + i] = make_float4(xd[0], xd[1], xd[2], xd[3]);
-    rec[5 + 2 * R + i] = make_float4(yd[0], yd[1], yd[2], yd[3]);
-  }
-  // what coverage and early-Z read, in the first five slots: the position
-  // of v0 beside the edge factors, its depth gradients and the draw's flags
-  rec[0].w = v0.r[0].x;
-  rec[1].w = v0.r[0].y;
-  rec[2].w = v0.r[0].z;
-  rec[4] = make_float4(rec[5 + R].z, rec[5 + 2 * R].z, __uint_as_float(draw),
-                       __uint_as_float(rec_flags(area > 0.0f, shade_key, zcfg)));
-  return true;
-}
-
+// (shader.cpp:414-449) of a projected triangle, written straight into its
+// record (no zero-area triangle gets one).  The vertices are picked by
+// register selects rather than through pointers, so that they stay in
+// registers.
 template <int NA>
 __device__ void emit_triangle(PassParams const& P, DrawParams const& D, uint32_t draw, uint32_t slot, vtx<NA> a,
                               vtx<NA> b, vtx<NA> c, uint32_t& ntri) {
@@ -215,20 +160,69 @@ __device__ void emit_triangle(PassParams const& P, DrawParams const& D, uint32_t
   vp_project(D, b);
   vp_project(D, c);
   constexpr uint32_t STRIDE = rec_stride_for(NA);
-  alignas(16) float4 rec[STRIDE];
-  bool ok = setup_triangle(draw, D.zcfg, D.shade_key, a, b, c, rec);
-  uint32_t idx = NO_REC;
-  if (ok) {
-    idx = atomicAdd(&P.counters->rec_units, STRIDE);
-    if (idx > P.rec_capacity - STRIDE || P.rec_capacity < STRIDE) {
-      atomicOr(&P.counters->overflow, OVF_REC);
-      idx = NO_REC;
-    } else {
-      float4* dst = P.recs + idx;
+  constexpr int R = 1 + NA;
+  // v0: the vertex nearest the origin by |x| + |y| in double (rasterizer.cpp:880-899)
+  double dist[3];
+  dist[0] = fabs(static_cast<double>(a.r[0].x)) + fabs(static_cast<double>(a.r[0].y));
+  dist[1] = fabs(static_cast<double>(b.r[0].x)) + fabs(static_cast<double>(b.r[0].y));
+  dist[2] = fabs(static_cast<double>(c.r[0].x)) + fabs(static_cast<double>(c.r[0].y));
+  int r0;
+  if (dist[0] < dist[1])
+    r0 = dist[0] < dist[2] ? 0 : 2;
+  else
+    r0 = dist[1] < dist[2] ? 1 : 2;
+  int const r1 = (r0 + 1) % 3, r2 = (r1 + 1) % 3;
+  auto pick = [&](int r, int i) -> v4 { return r == 0 ? a.r[i] : (r == 1 ? b.r[i] : c.r[i]); };
+  v4 const p0 = pick(r0, 0), p1 = pick(r1, 0), p2 = pick(r2, 0);
+  v4 const e01p = p1 - p0, e02p = p2 - p0;
+  float const area = e02p.x * e01p.y - e02p.y * e01p.x;
+  if (eq_eps(area, 0.0f)) {
+    P.slot_rec[slot] = NO_REC;
+    return;
+  }
+  uint32_t idx = atomicAdd(&P.counters->rec_units, STRIDE);
+  if (idx > P.rec_capacity - STRIDE || P.rec_capacity < STRIDE) {
+    atomicOr(&P.counters->overflow, OVF_REC);
+    P.slot_rec[slot] = NO_REC;
+    return;
+  }
+  float4* const rec = P.recs + idx;
+  float const inv_area = 1.0f / area;
+  v4 const pa = a.r[0], pb = b.r[0], pc = c.r[0];
+  // edge factors, with v0's projected x, y, z beside them (what coverage and
+  // early-Z read, in the first five slots)
+  v4 const vp[3] = {pa, pb, pc};
+  float const v0w[3] = {p0.x, p0.y, p0.z};
 #pragma unroll
-      for (int i = 0; i < static_cast<int>(STRIDE); ++i) dst[i] = rec[i];
+  for (int i = 0; i < 3; ++i) {
+    v4 const sv = vp[i], ev = vp[(i + 1) % 3];
+    rec[i] = make_float4(sv.y - ev.y, ev.x - sv.x, ev.x * sv.y - ev.y * sv.x, v0w[i]);
+  }
+  rec[3] = make_float4(smin(smin(pa.x, pb.x), pc.x), smax(smax(pa.x, pb.x), pc.x), smin(smin(pa.y, pb.y), pc.y),
+                       smax(smax(pa.y, pb.y), pc.y));
+  float const e01x = e01p.x, e01y = e01p.y, e02x = e02p.x, e02y = e02p.y;
+  float dzx = 0.0f, dzy = 0.0f;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    v4 const q0 = pick(r0, i);
+    v4 const e01 = pick(r1, i) - q0, e02 = pick(r2, i) - q0;
+    float xd[4], yd[4];
+    float const* p01 = &e01.x;
+    float const* p02 = &e02.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      xd[k] = (p02[k] * e01y - p01[k] * e02y) * inv_area;
+      yd[k] = (p01[k] * e02x - p02[k] * e01x) * inv_area;
+    }
+    rec[5 + i] = make_float4(q0.x, q0.y, q0.z, q0.w);
+    rec[5 + R + i] = make_float4(xd[0], xd[1], xd[2], xd[3]);
+    rec[5 + 2 * R + i] = make_float4(yd[0], yd[1], yd[2], yd[3]);
+    if (i == 0) {
+      dzx = xd[2];
+      dzy = yd[2];
     }
   }
+  rec[4] = make_float4(dzx, dzy, __uint_as_float(draw), __uint_as_float(rec_flags(area > 0.0f, D.shade_key, D.zcfg)));
   P.slot_rec[slot] = idx;
 }
 
