@@ -575,7 +575,7 @@ void sg_graph_destroy(sg_device* dev, sg_graph* graph);
 typedef struct sg_tuning {
   uint32_t cover_item;       /* 16 or 32 */
   uint32_t split_entries;    /* 32x32 items become 16x16 above this many bin entries */
-  uint32_t bin_chunk;        /* slots per binning warp, power of two >= 256 */
+  uint32_t bin_chunk;        /* slots per binning warp, power of two >= 64 */
   uint32_t bin_capacity;     /* initial bin entries */
   uint32_t frag_chunks;      /* initial fragment chunks (16 quads each) */
   uint32_t shade_quads_per_warp; /* 8 (4 lanes per quad) */

@@ -244,7 +244,7 @@ sg_tuning_knob const kTuningKnobs[] = {
     {"cover_item", 2, {16u, 32u}},
     {"split_entries", 4, {160u, 320u, 640u, 1280u}},
     {"cover_ctas_per_sm", 2, {3u, 4u}},
-    {"bin_chunk", 4, {256u, 512u, 1024u, 2048u}},
+    {"bin_chunk", 4, {64u, 128u, 256u, 512u}},
     {"shade_ctas_per_sm", 3, {4u, 8u, 16u}},
     {"shade_resident", 2, {3u, 4u}},
     {"merge_ctas_per_sm", 3, {2u, 3u, 6u}},
@@ -268,7 +268,7 @@ sg_tuning default_tuning() {
   sg_tuning t{};
   t.cover_item = 32;
   t.split_entries = 320;
-  t.bin_chunk = BIN_CHUNK_MIN;
+  t.bin_chunk = 128;
   t.bin_capacity = 1u << 24;
   t.frag_chunks = 1u << 18;
   t.shade_quads_per_warp = 8;
@@ -865,7 +865,7 @@ void finalize(PassPlan& pl, sg_device* d) {
     cursor[p.target] += uint64_t(p.slots_per_prim) * p.prim_count;
   }
   // tiles and binning chunks; counters stay under 32M in total
-  uint32_t const max_chunks = static_cast<uint32_t>(std::max(1, d->num_sms)) * 32;
+  uint32_t const max_chunks = static_cast<uint32_t>(std::max(1, d->num_sms)) * 64;
   std::vector<uint32_t> chunk(nt);
   for (uint32_t t = 0; t < nt; ++t) {
     uint32_t c = std::max<uint32_t>(BIN_CHUNK_MIN, d->tuning.bin_chunk);

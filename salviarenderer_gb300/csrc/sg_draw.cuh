@@ -21,7 +21,7 @@ constexpr int RASTER_THREADS = 256;   // 4x4 blocks per 64x64 tile (threads of a
 constexpr int QUAD_OWNERS = 1024;     // owners (2x2 quads) per 64x64 tile: quad (x, y) is owner y * 32 + x
 constexpr int FRAG_CHUNK = 4;         // fragments per chunk of an owner's fragment list
 constexpr uint32_t NO_CHUNK = 0xFFFFFFFFu;
-constexpr int BIN_CHUNK_MIN = 256;    // triangle slots per binning warp (minimum)
+constexpr int BIN_CHUNK_MIN = 64;     // triangle slots per binning warp (minimum)
 constexpr uint32_t NO_REC = 0xFFFFFFFFu;
 
 // overflow bits of PassCounters::overflow
