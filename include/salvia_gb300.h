@@ -466,6 +466,92 @@ int32_t sg_texture_info(sg_device* dev, uint32_t texture, uint32_t level, uint32
                         uint32_t* height, uint32_t* samples, uint32_t* format, uint32_t* levels);
 int32_t sg_texture_destroy(sg_device* dev, uint32_t texture);
 
+/* ---- image ingest and export (salvia/src/ext/resource/texture/tex_io.cpp) ---
+ * The reference decodes with FreeImage (load_image, freeimage_utility.cpp:8-18)
+ * and copies the bitmap into a surface (copy_image_to_surface_impl,
+ * tex_io.cpp:27-53).  Here a project-written PNG decoder stands in for
+ * FreeImage; an sg_image is the bitmap as copy_image_to_surface reads it:
+ * FreeImage's scanline order (row 0 is the image's BOTTOM line), R, G, B[, A]
+ * bytes per pixel, no padding.
+ *
+ * Decodable: PNG, 8 bits per channel, colour type 2 (RGB, FIT_BITMAP 24 bpp)
+ * or 6 (RGBA, 32 bpp), interlaced or not -- the bitmaps check_image_type_support
+ * (freeimage_utility.cpp:20-50) accepts.  Everything else returns SG_FAILED
+ * (the reference's load_texture returns a null texture for 16-bit and float
+ * bitmaps and copies garbage from palette and grey ones).  Critical chunks
+ * must pass their CRC, the zlib stream its Adler-32, and the image data must
+ * fill the image exactly. */
+typedef struct sg_image {
+  uint32_t width;
+  uint32_t height;
+  uint32_t channels;  /* 3: RGB (alpha reads 0, tex_io.cpp:29-31,66); 4: RGBA */
+  uint32_t reserved;
+  uint8_t* pixels;    /* width * height * channels bytes, owned by the library */
+} sg_image;
+/* A byte string the library allocated (an encoded file). */
+typedef struct sg_blob {
+  uint8_t* data;
+  size_t size;
+} sg_blob;
+/* load_image: decodes `size` bytes of an image file (host only, no device). */
+int32_t sg_image_decode(const void* file, size_t size, sg_image* out);
+void sg_image_release(sg_image* image);
+void sg_blob_release(sg_blob* blob);
+/* copy_image_to_surface (tex_io.cpp:27-74): converts the image into level
+ * `level` (a cube face for a cube texture) of a 1-sample colour texture of
+ * the same size, each pixel color_rgba8 -> the texture's format
+ * (pixel_format_convertor, color_convertors.cpp), on the device. */
+int32_t sg_texture_write_image(sg_device* dev, uint32_t texture, uint32_t level, const sg_image* image);
+/* save_surface (tex_io.cpp:139-188): encodes level `level` of a 1-sample
+ * colour texture as a PNG (image_format SG_FMT_BGRA8: 8-bit RGBA) or a
+ * Radiance RGBE file (SG_FMT_RGB32F), rows in FreeImage's order (the file's
+ * top line is the surface's last row).  Other formats: SG_INVALID_PARAMETER
+ * (the reference stops at ef_unimplemented). */
+int32_t sg_texture_encode_image(sg_device* dev, uint32_t texture, uint32_t level, uint32_t image_format,
+                                sg_blob* out);
+/* The host encoders behind sg_texture_encode_image: `image` rows in
+ * FreeImage's order (row 0 is written as the file's last line).  PNG: 3 or 4
+ * channels.  HDR: `rgb` holds width * height * 3 floats. */
+int32_t sg_image_encode_png(const sg_image* image, sg_blob* out);
+int32_t sg_image_encode_hdr(const float* rgb, uint32_t width, uint32_t height, sg_blob* out);
+
+/* ---- mesh ingest (salvia/src/ext/resource/mesh/mesh_io_obj.cpp) ------------
+ * create_mesh_from_obj (mesh_io_obj.cpp:436-455): parses a Wavefront OBJ file
+ * as load_obj_mesh_c does (mesh_io_obj.cpp:140-263: v / vt / vn / f with the
+ * first three corners of each face, usemtl, mtllib, vertices shared by
+ * (position, texcoord, normal) index triple, the rest of each line skipped)
+ * and its material library as load_material does (mesh_io_obj.cpp:59-138),
+ * then splits the faces per material as construct_meshes does
+ * (mesh_io_obj.cpp:375-434).  One sg_obj_material per mesh the reference
+ * returns: the materials with at least one face, in material order.  An index
+ * outside its array (the reference reads out of bounds) or a token longer
+ * than the reference's 2048-byte buffer returns SG_FAILED. */
+typedef struct sg_obj_material {
+  const char* name;       /* obj_material::name ("default" for material 0) */
+  const char* tex_name;   /* map_Kd with '\\' replaced by '/' ("" when none) */
+  const char* tex_path;   /* tex_name against the OBJ file's directory ("" when none) */
+  float ambient[4];
+  float diffuse[4];
+  float specular[4];
+  int32_t shininess;
+  float alpha;
+  int32_t is_specular;
+  uint32_t first_index;   /* this mesh's triangles: indices[first_index, first_index + index_count) */
+  uint32_t index_count;
+  uint32_t reserved;
+} sg_obj_material;
+typedef struct sg_obj_mesh {
+  uint32_t num_vertices;
+  uint32_t num_indices;
+  uint32_t num_materials;
+  uint32_t reserved;
+  const float* vertices;   /* obj_mesh_vertex: position, texcoord, normal, 4 floats each */
+  const uint32_t* indices; /* format_r32_uint, grouped by material */
+  const sg_obj_material* materials;
+} sg_obj_mesh;
+int32_t sg_obj_load(const char* path, int32_t flip_tex_v, sg_obj_mesh** out);
+void sg_obj_release(sg_obj_mesh* mesh);
+
 /* ---- samplers (create_sampler, renderer.h:49) ------------------------------- */
 int32_t sg_sampler_create(sg_device* dev, const sg_sampler_desc* desc, uint32_t texture,
                           uint32_t* out_sampler);

@@ -160,6 +160,28 @@ class AfReport(C.Structure):
                 ("train_ms", C.c_float)]
 
 
+class Image(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("channels", C.c_uint32),
+                ("reserved", C.c_uint32), ("pixels", C.POINTER(C.c_uint8))]
+
+
+class Blob(C.Structure):
+    _fields_ = [("data", C.POINTER(C.c_uint8)), ("size", C.c_size_t)]
+
+
+class ObjMaterial(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("tex_name", C.c_char_p), ("tex_path", C.c_char_p),
+                ("ambient", C.c_float * 4), ("diffuse", C.c_float * 4), ("specular", C.c_float * 4),
+                ("shininess", C.c_int32), ("alpha", C.c_float), ("is_specular", C.c_int32),
+                ("first_index", C.c_uint32), ("index_count", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class ObjMesh(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("num_indices", C.c_uint32), ("num_materials", C.c_uint32),
+                ("reserved", C.c_uint32), ("vertices", C.POINTER(C.c_float)), ("indices", C.POINTER(C.c_uint32)),
+                ("materials", C.POINTER(ObjMaterial))]
+
+
 SIGNATURES = {
     "sg_device_create": (C.c_int32, [C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
     "sg_device_destroy": (None, [C.c_void_p]),
@@ -216,6 +238,15 @@ SIGNATURES = {
                                           C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "sg_af_make_textures": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, _u32p]),
     "sg_af_model_train": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(AfTrainDesc), C.POINTER(AfReport)]),
+    "sg_image_decode": (C.c_int32, [C.c_void_p, C.c_size_t, C.POINTER(Image)]),
+    "sg_image_release": (None, [C.POINTER(Image)]),
+    "sg_blob_release": (None, [C.POINTER(Blob)]),
+    "sg_image_encode_png": (C.c_int32, [C.POINTER(Image), C.POINTER(Blob)]),
+    "sg_image_encode_hdr": (C.c_int32, [C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.POINTER(Blob)]),
+    "sg_texture_write_image": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(Image)]),
+    "sg_texture_encode_image": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(Blob)]),
+    "sg_obj_load": (C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(C.POINTER(ObjMesh))]),
+    "sg_obj_release": (None, [C.POINTER(ObjMesh)]),
 }
 
 AF_FEATURES, AF_OUTPUTS, AF_PARAMS = 24, 5, 6085
@@ -225,6 +256,12 @@ AF_FEATURES, AF_OUTPUTS, AF_PARAMS = 24, 5, 6085
 PRODUCT_ONLY = {"sg_draw_static_scratch", "sg_graph_create", "sg_graph_launch", "sg_graph_info",
                 "sg_graph_destroy", "sg_get_tuning", "sg_set_tuning", "sg_autotune", "sg_autotune_space"}
 PRODUCT_ONLY |= {name for name in SIGNATURES if name.startswith("sg_af_")}
+
+# Image and mesh ingest (tex_io.cpp, mesh_io_obj.cpp): host codecs and the
+# OBJ loader in the GPU library; the draw oracle does not export them (their
+# checkers are oracle/ingest_oracle.py and the reference's own loader).
+INGEST = {"sg_image_decode", "sg_image_release", "sg_blob_release", "sg_image_encode_png", "sg_image_encode_hdr",
+          "sg_texture_write_image", "sg_texture_encode_image", "sg_obj_load", "sg_obj_release"}
 
 
 def bind(lib, extra=None):

@@ -23,6 +23,7 @@
 
 #include "salvia_gb300.h"
 #include "sg_draw.cuh"
+#include "sg_ingest.h"
 #include "sg_jobs.cuh"
 #include "sg_learned.cuh"
 
@@ -64,6 +65,10 @@ uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaS
                      bool count_pass);
 void launch_mip(uint8_t const* src, uint32_t sw, uint32_t sh, uint8_t* dst, uint32_t dw, uint32_t dh,
                 uint32_t samples, uint32_t fmt, uint32_t filter, cudaStream_t s);
+void launch_ingest(uint8_t const* src, uint32_t n, uint32_t channels, uint8_t* dst, uint32_t fmt, uint32_t num_sms,
+                   cudaStream_t s);
+void launch_export(uint8_t const* src, uint32_t n, uint32_t fmt, uint8_t* dst, uint32_t out_fmt, uint32_t num_sms,
+                   cudaStream_t s);
 }  // namespace sg
 
 using namespace sg;
@@ -1967,6 +1972,65 @@ int32_t sg_texture_info(sg_device* d, uint32_t h, uint32_t level, uint32_t* w, u
   if (levels) *levels = static_cast<uint32_t>(t->levels.size());
   return SG_OK;
 }
+namespace {
+bool is_color_format(uint32_t fmt) { return fmt_bytes(fmt) != 0 && fmt != SG_FMT_D32F && fmt != SG_FMT_D24S8; }
+}  // namespace
+
+// copy_image_to_surface (tex_io.cpp:27-74) into one level (or cube face)
+int32_t sg_texture_write_image(sg_device* d, uint32_t h, uint32_t level, const sg_image* img) {
+  Texture* t = d ? find_tex(d, h) : nullptr;
+  if (!t || !img || !img->pixels || level >= t->levels.size() || t->samples != 1 || !is_color_format(t->fmt) ||
+      (img->channels != 3 && img->channels != 4))
+    return SG_INVALID_PARAMETER;
+  Level const& l = t->levels[level];
+  if (img->width != l.w || img->height != l.h) return SG_INVALID_PARAMETER;
+  if (int32_t r = settle_before_change(d)) return r;
+  uint32_t const n = l.w * l.h;
+  size_t const bytes = static_cast<size_t>(n) * img->channels;
+  uint8_t* staging = nullptr;
+  SG_CUDA(d, cudaMallocAsync(reinterpret_cast<void**>(&staging), bytes, d->stream));
+  cudaError_t e = cudaMemcpyAsync(staging, img->pixels, bytes, cudaMemcpyHostToDevice, d->stream);
+  if (e == cudaSuccess) {
+    launch_ingest(staging, n, img->channels, l.ptr, t->fmt, static_cast<uint32_t>(d->num_sms), d->stream);
+    e = cudaGetLastError();
+  }
+  cudaError_t const ef = cudaFreeAsync(staging, d->stream);
+  SG_CUDA(d, e);
+  SG_CUDA(d, ef);
+  SG_CUDA(d, cudaStreamSynchronize(d->stream));
+  ++t->version;
+  return SG_OK;
+}
+
+// save_surface (tex_io.cpp:139-188): PNG for BGRA8, Radiance RGBE for RGB32F
+int32_t sg_texture_encode_image(sg_device* d, uint32_t h, uint32_t level, uint32_t image_format, sg_blob* out) {
+  Texture* t = d ? find_tex(d, h) : nullptr;
+  if (!t || !out || level >= t->levels.size() || t->samples != 1 || !is_color_format(t->fmt) ||
+      (image_format != SG_FMT_BGRA8 && image_format != SG_FMT_RGB32F))
+    return SG_INVALID_PARAMETER;
+  *out = sg_blob{};
+  if (int32_t r = settle_before_change(d)) return r;
+  Level const& l = t->levels[level];
+  uint32_t const n = l.w * l.h;
+  size_t const bytes = static_cast<size_t>(n) * fmt_bytes(image_format);
+  std::vector<uint8_t> host(bytes);
+  uint8_t* staging = nullptr;
+  SG_CUDA(d, cudaMallocAsync(reinterpret_cast<void**>(&staging), bytes, d->stream));
+  launch_export(l.ptr, n, t->fmt, staging, image_format, static_cast<uint32_t>(d->num_sms), d->stream);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host.data(), staging, bytes, cudaMemcpyDeviceToHost, d->stream);
+  cudaError_t const ef = cudaFreeAsync(staging, d->stream);
+  SG_CUDA(d, e);
+  SG_CUDA(d, ef);
+  SG_CUDA(d, cudaStreamSynchronize(d->stream));
+  if (image_format == SG_FMT_RGB32F)
+    return sg_image_encode_hdr(reinterpret_cast<float const*>(host.data()), l.w, l.h, out);
+  // a 32-bit FreeImage bitmap is B, G, R, A in memory; PNG stores R, G, B, A
+  for (size_t i = 0; i < bytes; i += 4) std::swap(host[i], host[i + 2]);
+  sg_image img{l.w, l.h, 4, 0, host.data()};
+  return sg_image_encode_png(&img, out);
+}
+
 int32_t sg_texture_destroy(sg_device* d, uint32_t h) {
   Texture* t = d ? find_tex(d, h) : nullptr;
   if (!t) return SG_INVALID_PARAMETER;

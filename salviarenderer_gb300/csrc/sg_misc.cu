@@ -139,6 +139,42 @@ uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaS
   return launches;
 }
 
+// copy_image_to_surface_impl (tex_io.cpp:27-53): each pixel of a decoded
+// image (3 or 4 bytes, alpha 0 without an alpha channel) as color_rgba8,
+// converted to the texture's format through color_rgba32f
+// (pixel_format_convertor, color_convertors.cpp: to_rgba32f, then assign).
+// Rows arrive in FreeImage's order, which is the surface's.  Grid-stride.
+__global__ void __launch_bounds__(256) k_ingest(uint8_t const* src, uint32_t n, uint32_t channels, uint8_t* dst,
+                                                uint32_t fmt) {
+  uint32_t const esz = fmt_bytes(fmt);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint8_t const* p = src + static_cast<size_t>(i) * channels;
+    uint32_t const a = channels == 4 ? p[3] : 0u;
+    write_texel(fmt, dst + static_cast<size_t>(i) * esz, unorm8_to_f(p[0], p[1], p[2], a));
+  }
+}
+
+// save_surface's conversion (tex_io.cpp:170-180): each texel of a
+// 1-sample surface into BGRA8 or RGB32F through color_rgba32f.
+__global__ void __launch_bounds__(256) k_export(uint8_t const* src, uint32_t n, uint32_t fmt, uint8_t* dst,
+                                                uint32_t out_fmt) {
+  uint32_t const esz = fmt_bytes(fmt), osz = fmt_bytes(out_fmt);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    write_texel(out_fmt, dst + static_cast<size_t>(i) * osz, read_texel(fmt, src + static_cast<size_t>(i) * esz));
+}
+
+void launch_ingest(uint8_t const* src, uint32_t n, uint32_t channels, uint8_t* dst, uint32_t fmt, uint32_t num_sms,
+                   cudaStream_t s) {
+  uint32_t const blocks = std::max(1u, std::min((n + 255) / 256, num_sms * 8));
+  if (n) k_ingest<<<blocks, 256, 0, s>>>(src, n, channels, dst, fmt);
+}
+
+void launch_export(uint8_t const* src, uint32_t n, uint32_t fmt, uint8_t* dst, uint32_t out_fmt, uint32_t num_sms,
+                   cudaStream_t s) {
+  uint32_t const blocks = std::max(1u, std::min((n + 255) / 256, num_sms * 8));
+  if (n) k_export<<<blocks, 256, 0, s>>>(src, n, fmt, dst, out_fmt);
+}
+
 void launch_mip(uint8_t const* src, uint32_t sw, uint32_t sh, uint8_t* dst, uint32_t dw, uint32_t dh,
                 uint32_t samples, uint32_t fmt, uint32_t filter, cudaStream_t s) {
   uint32_t n = dw * dh * samples;
