@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-filter leg")
     ap.add_argument("--no-facade", action="store_true", help="skip the C++ facade leg")
     ap.add_argument("--no-autotune", action="store_true", help="time under the default scheduling parameters")
+    ap.add_argument("--no-ingest", action="store_true", help="skip the texture / mesh ingest leg")
     ap.add_argument("--cpu-configs", action="store_true",
                     help="time the CPU restatement (and the reference, where built) on the five workloads")
     ap.add_argument("--size", default="1920x1080",
@@ -474,6 +475,92 @@ def measure_facade(args, scene, resolved_want):
             "resolved_equals_graph": raw[off:off + n * 4] == bytes(resolved_want)}
 
 
+def synthetic_obj(path, n):
+    """An n x n height-field grid as a Wavefront OBJ file: positions,
+    texcoords and normals per grid point, two triangles per cell with
+    v/vt/vn corners, the two halves in two materials."""
+    import numpy as np
+    rng = np.random.default_rng(SEED)
+    ax = np.linspace(-1.0, 1.0, n + 1, dtype=np.float32)
+    x, y = np.meshgrid(ax, ax)
+    z = rng.uniform(-0.05, 0.05, size=x.shape).astype(np.float32)
+    with open(path, "w") as f:
+        f.write("mtllib grid.mtl\n")
+        f.write("".join(f"v {a:.6f} {b:.6f} {c:.6f}\n" for a, b, c in zip(x.ravel(), y.ravel(), z.ravel())))
+        f.write("".join(f"vt {a * 0.5 + 0.5:.5f} {b * 0.5 + 0.5:.5f}\n" for a, b in zip(x.ravel(), y.ravel())))
+        f.write("vn 0 0 1\n")
+        for half, name in ((0, "left"), (1, "right")):
+            f.write(f"usemtl {name}\n")
+            rows = []
+            for r in range(n):
+                for c in range(half * n // 2, (half + 1) * n // 2):
+                    a, b, d, e = (r * (n + 1) + c + 1, r * (n + 1) + c + 2, (r + 1) * (n + 1) + c + 1,
+                                  (r + 1) * (n + 1) + c + 2)
+                    rows.append(f"f {a}/{a}/1 {b}/{b}/1 {e}/{e}/1\nf {a}/{a}/1 {e}/{e}/1 {d}/{d}/1\n")
+            f.write("".join(rows))
+    with open(os.path.join(os.path.dirname(path), "grid.mtl"), "w") as f:
+        f.write("newmtl left\nKd 0.8 0.2 0.2\nnewmtl right\nKd 0.2 0.8 0.2\n")
+    return 2 * n * n
+
+
+def measure_ingest(dev, stream, args):
+    """Texture and mesh ingest (tex_io.cpp, mesh_io_obj.cpp): the library's
+    host PNG codec on a 2048^2 RGBA value-noise image, load_texture end to
+    end (decode, upload, device conversion) into RGBA8 and RGBA32F, and the
+    OBJ loader on a 512 x 512-cell grid (524,288 faces)."""
+    import tempfile
+    import numpy as np
+    from salviarenderer_gb300 import abi, ingest, scenes
+    reps = max(2, min(args.steps, 5))
+    img = scenes.to_rgba8(scenes.value_noise(np.random.default_rng(SEED), 2048))[::-1].copy()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        png = ingest.encode_png(dev.lib, img)
+    enc_s = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        got = ingest.decode_image(dev.lib, png)
+    dec_s = (time.perf_counter() - t0) / reps
+    assert np.array_equal(got, img)
+    out = {"image": "2048x2048 RGBA8 value noise", "png_bytes": len(png),
+           "png_encode_mpix_per_s": img.shape[0] * img.shape[1] / enc_s / 1e6,
+           "png_decode_mpix_per_s": img.shape[0] * img.shape[1] / dec_s / 1e6,
+           "png_decode_mb_per_s": len(png) / dec_s / 1e6}
+    for fmt, name in ((abi.FMT_RGBA8, "rgba8"), (abi.FMT_RGBA32F, "rgba32f")):
+        tex = dev.texture(2048, 2048, 1, fmt)
+        ingest.write_image(dev, tex, img)
+        dev.sync()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            ingest.write_image(dev, tex, img)
+        dev.sync()
+        w_s = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            dev.texture_destroy(ingest.load_texture(dev, png, fmt))
+        dev.sync()
+        l_s = (time.perf_counter() - t0) / reps
+        out[f"write_image_{name}_ms"] = w_s * 1e3
+        out[f"load_texture_{name}_ms"] = l_s * 1e3
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "grid.obj")
+        faces = synthetic_obj(path, 512)
+        size = os.path.getsize(path)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            data = ingest.load_obj(dev.lib, path, False)
+        obj_s = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        meshes = ingest.create_mesh_from_obj(dev, path, False)
+        dev.sync()
+        mesh_s = time.perf_counter() - t0
+    out.update({"obj": "512x512-cell grid, v/vt/vn corners, 2 materials", "obj_bytes": size, "obj_faces": faces,
+                "obj_vertices": int(data.vertices.shape[0]), "obj_meshes": len(meshes),
+                "obj_load_mb_per_s": size / obj_s / 1e6, "obj_load_mfaces_per_s": faces / obj_s / 1e6,
+                "create_mesh_from_obj_ms": mesh_s * 1e3})
+    return out
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -575,6 +662,7 @@ def run_gpu(args):
         facade = measure_facade(args, scene, b.outputs()["resolved"])
     uneven = None if args.no_uneven else measure_uneven(dev, stream, flush, args)
     learned = None if args.no_learned else measure_learned(dev, stream, flush, args, width, height)
+    ingest_leg = None if (args.no_ingest or rank != 0) else measure_ingest(dev, stream, args)
 
     if rank == 0:
         peak, peak_kind = measured_peak()
@@ -631,6 +719,7 @@ def run_gpu(args):
                                  "bin_capacity, frag_chunks": "sized from counters, grown after an overflow"}},
             "uneven_batch": uneven,
             "learned_filter": learned,
+            "ingest": ingest_leg,
             "gpu_launches": int(ginfo["kernels"]) * args.steps,
             "clocks": clk.summary(),
         }

@@ -754,7 +754,8 @@ typedef struct sg_af_train_desc {
   uint64_t seed;
 } sg_af_train_desc;
 typedef struct sg_af_report {
-  float first_loss;         /* mean loss of the first and last batches */
+  float first_loss;         /* mean per-sample loss over the first and the last
+                               min(16, steps / 4) batches (at least one) */
   float last_loss;
   uint32_t steps;
   float train_ms;           /* device time of the steps (CUDA events) */

@@ -398,7 +398,10 @@ public:
   sampler(core::detail::device_sp d, uint32_t h, sampler_desc const& desc, texture_ptr tex)
       : dev_(std::move(d)), handle_(h), desc_(desc), tex_(std::move(tex)) {}
   ~sampler() {
-    if (handle_) sg_sampler_destroy(dev_->dev, handle_);
+    if (handle_) {
+      dev_->flush();  // queued draws may sample through it
+      sg_sampler_destroy(dev_->dev, handle_);
+    }
   }
   uint32_t handle() const { return handle_; }
   sampler_desc const& get_desc() const { return desc_; }

@@ -342,9 +342,20 @@ int32_t sg_af_model_train(sg_device* d, sg_af_model* m, const sg_af_train_desc* 
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rep) {
-    uint32_t const last_cnt = n - (steps_per_epoch - 1) * t->batch;
-    rep->first_loss = losses[0] / static_cast<float>(std::min(t->batch, n));
-    rep->last_loss = losses[steps - 1] / static_cast<float>(last_cnt);
+    // mean per-sample loss over the first and the last `win` batches (one
+    // batch's loss is too noisy to show a trend over a short run)
+    uint32_t const win = std::max(1u, std::min(16u, steps / 4));
+    auto window_mean = [&](uint32_t from) {
+      double sum = 0.0, cnt = 0.0;
+      for (uint32_t k = from; k < from + win; ++k) {
+        uint32_t const b = k % steps_per_epoch;
+        sum += losses[k];
+        cnt += static_cast<double>(std::min(t->batch, n - b * t->batch));
+      }
+      return static_cast<float>(sum / cnt);
+    };
+    rep->first_loss = window_mean(0);
+    rep->last_loss = window_mean(steps - win);
     rep->steps = steps;
     rep->train_ms = ms;
   }

@@ -122,6 +122,10 @@ class Device:
     def levels(self, tex):
         return self.texture_info(tex)[4]
 
+    def texture_destroy(self, tex):
+        self._check("sg_texture_destroy", self.lib.sg_texture_destroy(self.handle, tex))
+        self._textures.pop(tex, None)
+
     # -- samplers ------------------------------------------------------------
     def sampler(self, tex, **kw):
         d = abi.SamplerDesc()

@@ -94,3 +94,28 @@ def test_facade_on_gpu_matches_oracle(oracle_lib, tmp_path):
     for k in ("color", "resolved"):
         d = np.abs(got[k].astype(np.int16) - want[k].astype(np.int16))
         assert d.max() <= 1, f"{k}: max diff {d.max()}"
+
+
+def _lifetime_outputs(lib_path, tmp_path):
+    exe = build_facade(lib_path, str(tmp_path), os.path.join(ROOT, "tests", "cpp", "queued_lifetime.cpp"))
+    out = []
+    for release in (0, 1):
+        path = os.path.join(str(tmp_path), f"out{release}.bin")
+        subprocess.run([exe, str(release), path], check=True)
+        out.append(open(path, "rb").read())
+    return out
+
+
+def test_queued_draw_outlives_its_sampler_on_oracle(oracle_lib, tmp_path):
+    """A sampler released while a draw that samples through it is queued:
+    the facade submits the queue first, so the draw is unchanged."""
+    from conftest import ORACLE_LIB
+    alive, released = _lifetime_outputs(ORACLE_LIB, tmp_path)
+    assert alive == released and any(alive)
+
+
+@pytest.mark.gpu
+def test_queued_draw_outlives_its_sampler_on_gpu(tmp_path):
+    from salviarenderer_gb300 import build as pbuild
+    alive, released = _lifetime_outputs(pbuild.ensure_built(), tmp_path)
+    assert alive == released and any(alive)

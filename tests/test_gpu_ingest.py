@@ -204,3 +204,42 @@ def test_obj_scene_matches_oracle(gdev, odev, tmp_path, samples, flip):
     # the cube covers part of the frame with both textures
     c = got["color"].reshape(H, W, samples, 4)[..., 0, :]
     assert (c != c[0, 0]).any(axis=-1).mean() > 0.2
+
+
+def test_facade_obj_scene(gdev, tmp_path):
+    """tests/cpp/obj_scene.cpp (ext_resource.hpp: create_mesh_from_obj,
+    mesh::render, save_surface) against the same frame drawn through the
+    Python wrapper of the same library."""
+    import struct
+    import subprocess
+    from test_facade import build_facade
+    path = obj_dir(tmp_path)
+    exe = build_facade(pbuild.ensure_built(), str(tmp_path), os.path.join(ROOT, "tests", "cpp", "obj_scene.cpp"))
+    view = scenes.look_at_lh([2.2, 1.7, -3.0], [0.0, 0.0, 0.0], [0.0, 1.0, 0.0])
+    mvp = (view @ scenes.perspective_fov_lh(math.radians(55.0), W / H, 0.5, 20.0)).astype(np.float32)
+    (tmp_path / "mvp.bin").write_bytes(mvp.tobytes())
+    samples = 4
+    out, png = tmp_path / "out.bin", tmp_path / "out.png"
+    subprocess.run([exe, str(path), str(samples), "1", str(tmp_path / "mvp.bin"), str(out), str(png)], check=True)
+    raw = out.read_bytes()
+    n = W * H
+    color, ds = raw[:n * samples * 4], raw[n * samples * 4:n * samples * 12]
+    resolved = raw[n * samples * 12:n * samples * 12 + n * 4]
+    stats = struct.unpack("<3Q", raw[n * samples * 12 + n * 4:])
+    # the same frame through the Python wrapper
+    meshes = ingest.create_mesh_from_obj(gdev, str(path), True)
+    c, d = frame(gdev, samples)
+    st = []
+    for m in meshes:
+        samp = gdev.sampler(m.texture, min_filter=abi.FILTER_LINEAR, mag_filter=abi.FILTER_LINEAR,
+                            mip_filter=abi.FILTER_LINEAR)
+        st.append(gdev.draw(m.draw_desc(viewport=(0, 0, W, H, 0.0, 1.0), color_target=c, ds_target=d,
+                                        num_varyings=2, varying_modifiers=[abi.AM_LINEAR, abi.AM_LINEAR],
+                                        vs=dict(program=abi.VS_TRANSFORM, constants=mvp),
+                                        ps=dict(program=abi.PS_TEX_MODULATE, samplers=[samp]),
+                                        bs=dict(program=abi.BS_REPLACE)), stats=True))
+    want = outputs(gdev, c, d, samples)
+    assert stats == tuple(sum(s[k] for s in st) for k in ("ia_primitives", "cprimitives", "ps_invocations"))
+    assert color == want["color"].tobytes() and ds == want["ds"].tobytes() and resolved == want["resolved"].tobytes()
+    bgra = oracle.export_bgra8(np.frombuffer(resolved, np.uint8), abi.FMT_RGBA8, n).reshape(H, W, 4)
+    np.testing.assert_array_equal(oracle.png_decode(png.read_bytes()), bgra[..., [2, 1, 0, 3]])
