@@ -190,6 +190,7 @@ struct PassPlan {
   std::set<uint32_t> sampled;                // textures its draws sample
   std::set<uint32_t> resolved;               // textures its queued resolves read or write
   std::set<uint32_t> cleared;                // textures its queued clears write
+  std::map<uint8_t const*, uint32_t> ds_clear_word;  // depth surface -> the depth word its clear leaves
   std::vector<uint8_t> late_z;               // per target: a draw tests depth after shading
   uint32_t more_colors = 0;                  // most colour targets after the first of any of its targets
   std::vector<sg_shader_module const*> user_ps;  // its user pixel shaders: shade key USER_CLASS * 8 + index
@@ -206,6 +207,7 @@ struct PassPlan {
   uint32_t ntiles = 0, nslots = 0, nchunks = 0, max_samples = 1;
   uint64_t ncounts = 0, rec_units = 0;
   bool any_early_z = false;
+  bool need_zbackup = false;                 // an early-Z target whose starting depth is not known
   uint32_t na_mask = 0;
   bool lines = false;                        // a line pass: segments (line_mode != 0) only
   uint64_t slots = 0;                        // record slots its draws take
@@ -844,6 +846,7 @@ void finalize(PassPlan& pl, sg_device* d) {
   std::vector<uint64_t> slots(nt, 0);
   for (auto& T : pl.targets) T.tiles_x = T.tiles_y = 0;
   pl.any_early_z = false;
+  pl.need_zbackup = false;
   pl.na_mask = 0;
   pl.max_samples = 1;
   pl.rec_units = 0;
@@ -916,6 +919,10 @@ void finalize(PassPlan& pl, sg_device* d) {
     pl.ncounts += static_cast<uint64_t>(T.tiles_x) * T.tiles_y * T.nchunks;
     pl.max_samples = std::max(pl.max_samples, T.samples);
     if (T.any_early_z) pl.any_early_z = true;
+    auto const known = pl.ds_clear_word.find(T.ds);
+    T.zpre_known = (T.any_early_z && known != pl.ds_clear_word.end()) ? 1u : 0u;
+    T.zpre_word = T.zpre_known ? known->second : 0u;
+    if (T.any_early_z && !T.zpre_known) pl.need_zbackup = true;
   }
   for (auto const& p : pl.draws) pl.draw_prim_base.push_back(p.prim_base);
 }
@@ -985,7 +992,7 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   // pre-images of the depth the coverage pass writes back (early-Z only)
   P.zbackup = nullptr;
   P.zbackup_tile_words = TILE * TILE * pl.max_samples;
-  if (pl.any_early_z) {
+  if (pl.need_zbackup) {
     SG_CUDA(d, sc.zbackup.ensure(static_cast<size_t>(pl.ntiles) * P.zbackup_tile_words * 4));
     P.zbackup = static_cast<uint32_t*>(sc.zbackup.ptr);
   }
@@ -1061,7 +1068,7 @@ int32_t scratch_static(sg_device* d, uint8_t* base, PassPlan const& pl, PlanLayo
   P.tile_begin = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(pl.ntiles) + 1) * 4));
   P.owner_first = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(pl.ntiles) * QUAD_OWNERS * 4));
   P.zbackup_tile_words = TILE * TILE * pl.max_samples;
-  P.zbackup = pl.any_early_z ? reinterpret_cast<uint32_t*>(take(static_cast<size_t>(pl.ntiles) *
+  P.zbackup = pl.need_zbackup ? reinterpret_cast<uint32_t*>(take(static_cast<size_t>(pl.ntiles) *
                                                                  P.zbackup_tile_words * 4))
                              : nullptr;
   if (off > SG_STATIC_SCRATCH_TABLE_LIMIT) {
@@ -1222,7 +1229,7 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       }
       stage_end(d, 3, ev);
       ev = stage_begin(d, profile);
-      if (P.zbackup) {  // undoes the coverage pass's depth writes if the pass overflowed
+      if (pl.any_early_z) {  // undoes the coverage pass's depth writes if the pass overflowed
         launch_cover_rollback(P, std::min<uint32_t>(pl.ntiles, sms * 8), s);
         ++k;
       }
@@ -1544,6 +1551,21 @@ int32_t make_resolve_job(sg_device* d, uint32_t src, uint32_t dst, SurfaceJob& j
   return SG_OK;
 }
 
+// The depth word (the 4 bytes early-Z reads and writes) of every sample of
+// a depth-stencil texture after a clear, when the clear sets all of it: the
+// depth of RG32F / D32F (clear_ds_job's values), both parts of D24S8.
+bool ds_clear_word(Texture const* t, uint32_t flags, float depth, uint32_t stencil, uint32_t& word) {
+  if (!t || !(flags & SG_CLEAR_DEPTH)) return false;
+  if (t->fmt == SG_FMT_RG32F || t->fmt == SG_FMT_D32F) {
+    std::memcpy(&word, &depth, 4);
+    return true;
+  }
+  if (t->fmt != SG_FMT_D24S8 || !(flags & SG_CLEAR_STENCIL)) return false;
+  float const c = std::fmin(std::fmax(depth, 0.0f), 1.0f) * 16777215.0f;
+  word = static_cast<uint32_t>(std::nearbyint(c)) | ((stencil & 0xFFu) << 24);
+  return true;
+}
+
 // Appends the commands to passes (starting a new pass where order requires)
 // and hands every completed pass to `sink`.
 template <class Sink>
@@ -1582,6 +1604,11 @@ int32_t plan_commands(sg_device* d, sg_command const* cmds, uint32_t n, Sink&& s
       pl.clears.push_back(j);
       pl.clear_cmd.push_back(i);
       pl.cleared.insert(c.texture);
+      if (c.type == SG_CMD_CLEAR_DEPTH_STENCIL) {
+        uint32_t word = 0;
+        if (ds_clear_word(find_tex(d, c.texture), c.flags, c.depth, c.stencil, word))
+          pl.ds_clear_word[find_tex(d, c.texture)->levels[0].ptr] = word;
+      }
       break;
     }
     case SG_CMD_RESOLVE: {

@@ -72,6 +72,12 @@ struct CvShared {
   uint32_t cand[CV_STAGE];
   uint32_t wcnt[CV_THREADS / 32];
   uint32_t next;
+  // the walk: each quad's fragment list cursor, the quads with covered
+  // pairs in the round (quad << 16 | pair bits), packed, and per block
+  // whether a walk wrote depth since its range was last taken
+  uint32_t own_first[CV_THREADS], own_cur[CV_THREADS], own_count[CV_THREADS];
+  uint32_t walk[CV_THREADS];
+  uint8_t zdirty[64];
 };
 // followed by the staged depth: CV_PX * CV_PX * samples words (early-Z only)
 inline size_t cv_smem(uint32_t samples, bool early_z) {
@@ -398,7 +404,6 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
   int const tid = threadIdx.x, q = tid & 3, ib = tid >> 2;
   int const ibx = ib & 7, iby = ib >> 3, qx0 = (q & 1) * 2, qy0 = (q >> 1) * 2;
   uint32_t const nitems = P.ntiles * 4;
-  OwnerList L{NO_CHUNK, NO_CHUNK, 0};
   for (;;) {
     if (tid == 0) sh.item = atomicAdd(&P.counters->tile_cursor, 1u);
     __syncthreads();
@@ -419,8 +424,9 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
     }
     int const bx = bx0 + ibx, by = by0 + iby;  // this thread's block, tile numbering
     int const own16 = (iby >> 2) * 2 + (ibx >> 2);  // its 16x16 region within the quadrant
-    L.first = L.cur = NO_CHUNK;
-    L.count = 0;
+    sh.own_first[tid] = sh.own_cur[tid] = NO_CHUNK;
+    sh.own_count[tid] = 0;
+    if (q == 0) sh.zdirty[ib] = 0;
     Quad qd;
     qd.x = tile_x0 + bx * 4 + qx0;
     qd.y = tile_y0 + by * 4 + qy0;
@@ -442,7 +448,7 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
     uint32_t const zrow = CV_PX * S;
     if (stage_z) {
       // the quadrant's depth, and its pre-image for k_cover_rollback
-      uint32_t* const zb = P.zbackup ? P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words +
+      uint32_t* const zb = (P.zbackup && !T.zpre_known) ? P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words +
                                            (static_cast<size_t>(by0) * 4 * TILE + bx0 * 4) * S
                                      : nullptr;
       for (uint32_t i = tid; i < qh * zrow; i += CV_THREADS) {
@@ -457,8 +463,9 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
     uint32_t* const zq = ztile + (iby * 4 + qy0) * zrow + (ibx * 4 + qx0) * S;
     ZRange zr{-INFINITY, INFINITY, 0u, 0xFFFFFFu};  // the block's
     bool z_dirty = stage_z;  // the depth range is recomputed before a batch's culling when stale
-    if (stage_z) __syncthreads();
+    __syncthreads();
     for (uint32_t bpos = begin; bpos < end;) {
+      z_dirty = z_dirty || sh.zdirty[ib] != 0;
       if (__any_sync(0xFFFFFFFFu, z_dirty)) {  // the block's range: its four quads' ranges combined
         z_range(zq, static_cast<int>(zrow), qd, d24, zr);
 #pragma unroll
@@ -471,6 +478,7 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
         z_dirty = false;
       }
       __syncthreads();
+      if (q == 0) sh.zdirty[ib] = 0;
       uint32_t* const masks = &sh.mask4[0][0];
       for (int i = tid; i < (64 + 64 + 4) * CV_WORDS; i += CV_THREADS) masks[i] = 0;
       uint32_t const nb = cv_fill(P, bpos, end, tile_x0, tile_y0, bx0 * 4, by0 * 4, sh);
@@ -557,38 +565,85 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
           sh.cov_cv[b][k] = cv;
         }
         __syncthreads();
-        // the block's pairs in primitive order on this thread's quad: early-Z,
-        // then the surviving quad into the quad's fragment list
-        uint32_t const fm = (1u << S) - 1u, qfull = fm | (fm << 4) | (fm << 8) | (fm << 12);
-        for (uint32_t k = 0; k < n; ++k) {
-          uint32_t const e8 = sh.slot[ib][k], idx = e8 & 127u;
-          uint32_t const cq = quad_bits(sh.cov_cv[ib][k], q);
-          if (!cq) continue;
-          TriCv const& t = sh.stage[idx];
-          uint32_t tq = cq;
-          if (t.zcfg & 128u) {
-            bool wrote = false;
-            // the common depth functions with the compare as code, not data
-            uint32_t const zc = t.zcfg, func = (zc >> 8) & 15u;
-            bool const d24z = (zc >> 6) & 1u;
-            int const zr_ = static_cast<int>(zrow);
-            if (func == SG_CMP_LESS)
-              tq = d24z ? early_z_quad<SG_CMP_LESS, true>(t, cq, zq, zr_, qd, wrote)
-                        : early_z_quad<SG_CMP_LESS, false>(t, cq, zq, zr_, qd, wrote);
-            else if (func == SG_CMP_LESS_EQUAL)
-              tq = d24z ? early_z_quad<SG_CMP_LESS_EQUAL, true>(t, cq, zq, zr_, qd, wrote)
-                        : early_z_quad<SG_CMP_LESS_EQUAL, false>(t, cq, zq, zr_, qd, wrote);
-            else
-              tq = early_z_quad<-1, false>(t, cq, zq, zr_, qd, wrote);
-            z_dirty = z_dirty || wrote;
+        // the block's pairs in primitive order on each quad: early-Z, then the
+        // surviving quad into the quad's fragment list.  The quads with a
+        // covered pair this round are packed onto the first threads (any
+        // thread walks any quad: its list cursor is in shared memory), so
+        // the walk runs on as few, as full warps as the round allows.
+        {
+          uint32_t covb = 0;
+          for (uint32_t k = 0; k < n; ++k) covb |= (quad_bits(sh.cov_cv[ib][k], q) != 0u ? 1u : 0u) << k;
+          uint32_t const lane = tid & 31, warp = tid >> 5;
+          uint32_t const bal = __ballot_sync(0xFFFFFFFFu, covb != 0u);
+          if (lane == 0) sh.wcnt[warp] = __popc(bal);
+          __syncthreads();
+          uint32_t excl = __popc(bal & ((1u << lane) - 1u)), nwalk = 0;
+#pragma unroll
+          for (int w = 0; w < CV_THREADS / 32; ++w) {
+            uint32_t const c = sh.wcnt[w];
+            excl += static_cast<uint32_t>(w) < warp ? c : 0u;
+            nwalk += c;
           }
-          if (!tq) continue;
-          uint32_t const uq = quad_bits(sh.cov_uc[ib][k], q);
-          bool const fullq = (e8 >> 7) ? cq == qfull : (uq == qfull && cq == uq);
-          owner_append(P, L, t.entry >> 1,
-                       (static_cast<uint32_t>(qd.x) >> 1) | ((static_cast<uint32_t>(qd.y) >> 1) << 12) |
-                           (fullq ? 1u << 24 : 0u) | (t.shade_key << 25),
-                       tq | (cq << 16));
+          if (covb) sh.walk[excl] = (static_cast<uint32_t>(tid) << 16) | covb;
+          __syncthreads();
+          if (static_cast<uint32_t>(tid) < nwalk) {
+            uint32_t const wk = sh.walk[tid], h = wk >> 16, hq = h & 3u, hb = h >> 2;
+            uint32_t pend = wk & 0xFFFFu;
+            // the walked quad
+            Quad qw;
+            qw.x = tile_x0 + (bx0 + static_cast<int>(hb & 7u)) * 4 + static_cast<int>(hq & 1u) * 2;
+            qw.y = tile_y0 + (by0 + static_cast<int>(hb >> 3)) * 4 + static_cast<int>(hq >> 1) * 2;
+            qw.samples = S;
+#pragma unroll
+            for (uint32_t sm = 0; sm < 4; ++sm) {
+              qw.ax[sm] = sh.spx[min(sm, S - 1)] - 0.5f;
+              qw.ay[sm] = sh.spy[min(sm, S - 1)] - 0.5f;
+            }
+            qw.inside = 0;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if (static_cast<uint32_t>(qw.x + (i & 1)) < W && static_cast<uint32_t>(qw.y + (i >> 1)) < H)
+                qw.inside |= 1u << i;
+            uint32_t* const zqw = ztile + ((hb >> 3) * 4 + (hq >> 1) * 2) * zrow + ((hb & 7u) * 4 + (hq & 1u) * 2) * S;
+            OwnerList Lw{sh.own_first[h], sh.own_cur[h], sh.own_count[h]};
+            uint32_t const fm = (1u << S) - 1u, qfull = fm | (fm << 4) | (fm << 8) | (fm << 12);
+            bool wrote_any = false;
+            while (pend) {
+              uint32_t const k = static_cast<uint32_t>(__ffs(pend) - 1);
+              pend &= pend - 1u;
+              uint32_t const e8 = sh.slot[hb][k], idx = e8 & 127u;
+              uint32_t const cq = quad_bits(sh.cov_cv[hb][k], static_cast<int>(hq));
+              TriCv const& t = sh.stage[idx];
+              uint32_t tq = cq;
+              if (t.zcfg & 128u) {
+                bool wrote = false;
+                // the common depth functions with the compare as code, not data
+                uint32_t const zc = t.zcfg, func = (zc >> 8) & 15u;
+                bool const d24z = (zc >> 6) & 1u;
+                int const zr_ = static_cast<int>(zrow);
+                if (func == SG_CMP_LESS)
+                  tq = d24z ? early_z_quad<SG_CMP_LESS, true>(t, cq, zqw, zr_, qw, wrote)
+                            : early_z_quad<SG_CMP_LESS, false>(t, cq, zqw, zr_, qw, wrote);
+                else if (func == SG_CMP_LESS_EQUAL)
+                  tq = d24z ? early_z_quad<SG_CMP_LESS_EQUAL, true>(t, cq, zqw, zr_, qw, wrote)
+                            : early_z_quad<SG_CMP_LESS_EQUAL, false>(t, cq, zqw, zr_, qw, wrote);
+                else
+                  tq = early_z_quad<-1, false>(t, cq, zqw, zr_, qw, wrote);
+                wrote_any = wrote_any || wrote;
+              }
+              if (!tq) continue;
+              uint32_t const uq = quad_bits(sh.cov_uc[hb][k], static_cast<int>(hq));
+              bool const fullq = (e8 >> 7) ? cq == qfull : (uq == qfull && cq == uq);
+              owner_append(P, Lw, t.entry >> 1,
+                           (static_cast<uint32_t>(qw.x) >> 1) | ((static_cast<uint32_t>(qw.y) >> 1) << 12) |
+                               (fullq ? 1u << 24 : 0u) | (t.shade_key << 25),
+                           tq | (cq << 16));
+            }
+            sh.own_first[h] = Lw.first;
+            sh.own_cur[h] = Lw.cur;
+            sh.own_count[h] = Lw.count;
+            if (wrote_any) sh.zdirty[hb] = 1;
+          }
         }
         if (!__syncthreads_or(more)) break;
       }
@@ -603,11 +658,14 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
       }
     }
     // close the quad's list for the item
-    if (L.cur != NO_CHUNK) {
-      P.chunk_next[L.cur] = NO_CHUNK;
-      P.chunk_count[L.cur] = L.count;
+    __syncthreads();
+    uint32_t const lcur = sh.own_cur[tid];
+    if (lcur != NO_CHUNK) {
+      P.chunk_next[lcur] = NO_CHUNK;
+      P.chunk_count[lcur] = sh.own_count[tid];
     }
-    P.owner_first[static_cast<size_t>(tile) * QUAD_OWNERS + (by * 2 + (q >> 1)) * 32 + bx * 2 + (q & 1)] = L.first;
+    P.owner_first[static_cast<size_t>(tile) * QUAD_OWNERS + (by * 2 + (q >> 1)) * 32 + bx * 2 + (q & 1)] =
+        sh.own_first[tid];
   }
 }
 
@@ -624,16 +682,17 @@ __global__ void __launch_bounds__(256) k_cover_rollback(PassParams P) {
     if (P.tile_begin[tile] == P.tile_begin[tile + 1]) continue;
     TargetParams const& T = P.targets[target_of_tile(P, tile)];
     if (!T.any_early_z) continue;
+    bool const known = T.zpre_known != 0;  // the pass's clear set every depth word
     uint32_t const ltile = tile - T.tile_base, S = T.samples;
     uint32_t const tx0 = (ltile % static_cast<uint32_t>(T.tiles_x)) * TILE;
     uint32_t const ty0 = (ltile / static_cast<uint32_t>(T.tiles_x)) * TILE;
     uint32_t const tw = min(static_cast<uint32_t>(TILE), T.width - min(T.width, tx0));
     uint32_t const th = min(static_cast<uint32_t>(TILE), T.height - min(T.height, ty0));
-    uint32_t const* zb = P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words;
+    uint32_t const* zb = known ? nullptr : P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words;
     for (uint32_t i = threadIdx.x; i < th * TILE * S; i += blockDim.x) {
       uint32_t const y = i >> (6 + (S >> 1)), k = i & (TILE * S - 1), x = k >> (S >> 1), sm = k & (S - 1);
       if (x >= tw) continue;
-      *reinterpret_cast<uint32_t*>(ds_addr(T, tx0 + x, ty0 + y, sm)) = zb[i];
+      *reinterpret_cast<uint32_t*>(ds_addr(T, tx0 + x, ty0 + y, sm)) = known ? T.zpre_word : zb[i];
     }
   }
 }

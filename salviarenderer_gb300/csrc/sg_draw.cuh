@@ -81,6 +81,11 @@ struct TargetParams {
   // binning: the target's slots are cut into chunks of `chunk` slots, one warp each
   uint32_t slot_base, nslots;
   uint32_t chunk_base, nchunks, chunk;
+  // the depth word every sample holds when the pass starts, known when the
+  // pass's own clears set it (zpre_known): the coverage pass then keeps no
+  // pre-image of the tiles it stages, and a rollback writes zpre_word back
+  uint32_t zpre_known;
+  uint32_t zpre_word;
   uint32_t pad;
   uint64_t count_base;               // first (tile, chunk) counter of the target
 };

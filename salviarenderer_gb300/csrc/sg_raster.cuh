@@ -272,8 +272,19 @@ struct OwnerList {
 };
 
 __device__ inline void owner_append(PassParams const& P, OwnerList& L, uint32_t rec, uint32_t pos, uint32_t mask) {
-  if (L.cur == NO_CHUNK || L.count == FRAG_CHUNK) {
-    uint32_t c = atomicAdd(&P.counters->chunk_total, 1u);
+  // a new chunk when the list has none or its chunk is full: the threads of
+  // the warp appending together take theirs with one atomic on the shared
+  // counter (one address every SM allocates from)
+  bool const need = L.cur == NO_CHUNK || L.count == FRAG_CHUNK;
+  unsigned const act = __activemask();
+  unsigned const want = __ballot_sync(act, need);
+  if (need) {
+    unsigned const lane = threadIdx.x & 31u;
+    int const leader = __ffs(want) - 1;
+    uint32_t base = 0;
+    if (static_cast<int>(lane) == leader) base = atomicAdd(&P.counters->chunk_total, static_cast<uint32_t>(__popc(want)));
+    base = __shfl_sync(want, base, leader);
+    uint32_t const c = base + static_cast<uint32_t>(__popc(want & ((1u << lane) - 1u)));
     if (c >= P.chunk_capacity) {
       atomicOr(&P.counters->overflow, OVF_FRAG);
       return;
@@ -555,7 +566,7 @@ __global__ void __launch_bounds__(COVER_THREADS, 4) k_cover(PassParams P) {
     uint32_t const zrow = px * S;
     if (stage_z) {
       // the item's depth, and its pre-image for k_cover_rollback
-      uint32_t* const zb = P.zbackup ? P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words +
+      uint32_t* const zb = (P.zbackup && !T.zpre_known) ? P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words +
                                            (static_cast<size_t>(by0) * 4 * TILE + bx0 * 4) * S
                                      : nullptr;
       for (uint32_t i = tid; i < qh * zrow; i += COVER_THREADS) {

@@ -68,6 +68,21 @@ def test_fragment_overflow_submitted_list(odev):
     assert_same(got, want)
 
 
+@pytest.mark.parametrize("ds_fmt", [abi.FMT_RG32F, abi.FMT_D24S8, abi.FMT_D32F])
+def test_fragment_overflow_after_an_in_pass_clear(odev, ds_fmt):
+    """The list's depth clear joins the pass that overflows: the coverage
+    pass keeps no pre-image (every depth word is the clear's), and the
+    rollback writes the clear's word back -- for D24S8 the stencil byte with
+    it -- before the pass runs again."""
+    s = scenes.overdraw_scene(samples=4, width=192, height=160, seed=13)
+    s.ds_fmt = ds_fmt
+    s.clear_depth, s.clear_stencil = 0.75, 0x5A
+    want = scenes.render(odev, s)
+    dev = fresh()
+    got = outputs_of(dev, s, lambda b: dev.submit(b.commands()))
+    assert_same(got, want)
+
+
 def test_fragment_overflow_with_statistics(odev):
     s = scenes.overdraw_scene(seed=5)
     compare(fresh(), odev, s)
