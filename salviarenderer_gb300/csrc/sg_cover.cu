@@ -262,6 +262,53 @@ __device__ inline uint32_t early_z_quad(TriCv const& t, uint32_t cq, uint32_t* z
   return tz;
 }
 
+// early_z_quad for four samples and a compiled LESS / LESS_EQUAL: a pixel's
+// four depth words are one 16-byte word of the staged depth, read once,
+// tested sample by sample without branches and written once.  The sample
+// depth is the same expression as early_z_quad's, in the same order.
+template <int FUNC, bool D24>
+__device__ inline uint32_t early_z_quad4(TriCv const& t, uint32_t cq, uint32_t* zq, int zrow, Quad const& qd,
+                                         bool& wrote) {
+  bool const wr = (t.zcfg >> 5) & 1u;
+  float const dx = 0.5f + static_cast<float>(qd.x) - t.p0x;
+  float const dy = 0.5f + static_cast<float>(qd.y) - t.p0y;
+  float const z00 = t.p0z + (t.dzx * dx + t.dzy * dy);
+  float off[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) off[s] = qd.ax[s] * t.dzx + qd.ay[s] * t.dzy;
+  uint32_t tz = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    uint32_t const pbits = (cq >> (4 * i)) & 0xFu;
+    if (!pbits) continue;
+    float const z = (i & 2) ? ((i & 1) ? (z00 + t.dzx) + t.dzy : z00 + t.dzy) : ((i & 1) ? z00 + t.dzx : z00);
+    uint4* const zp = reinterpret_cast<uint4*>(zq + (i >> 1) * zrow + (i & 1) * 4);
+    uint4 const w4 = *zp;
+    uint32_t w[4] = {w4.x, w4.y, w4.z, w4.w};
+    uint32_t pass = 0;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      float const nd = off[s] + z;
+      uint32_t const q24 = D24 ? d24_quantize(nd) : 0u;
+      bool p;
+      if constexpr (FUNC == SG_CMP_LESS)
+        p = D24 ? q24 < (w[s] & 0xFFFFFFu) : nd < __uint_as_float(w[s]);
+      else
+        p = D24 ? q24 <= (w[s] & 0xFFFFFFu) : nd <= __uint_as_float(w[s]);
+      p = p && ((pbits >> s) & 1u);
+      pass |= static_cast<uint32_t>(p) << s;
+      uint32_t const nw = D24 ? ((w[s] & 0xFF000000u) | q24) : __float_as_uint(nd);
+      w[s] = p ? nw : w[s];
+    }
+    if (pass && wr) {
+      *zp = make_uint4(w[0], w[1], w[2], w[3]);
+      wrote = true;
+    }
+    tz |= pass << (4 * i);
+  }
+  return tz;
+}
+
 // Fills the batch: from bin entry `bpos` on, the entries whose triangle's
 // bounding box reaches the quadrant (x in [qx0, qx0 + 32), y in [qy0,
 // qy0 + 32) of the tile), in order, at most CV_STAGE of them.  A triangle
@@ -621,7 +668,13 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
                 uint32_t const zc = t.zcfg, func = (zc >> 8) & 15u;
                 bool const d24z = (zc >> 6) & 1u;
                 int const zr_ = static_cast<int>(zrow);
-                if (func == SG_CMP_LESS)
+                if (S == 4 && func == SG_CMP_LESS)
+                  tq = d24z ? early_z_quad4<SG_CMP_LESS, true>(t, cq, zqw, zr_, qw, wrote)
+                            : early_z_quad4<SG_CMP_LESS, false>(t, cq, zqw, zr_, qw, wrote);
+                else if (S == 4 && func == SG_CMP_LESS_EQUAL)
+                  tq = d24z ? early_z_quad4<SG_CMP_LESS_EQUAL, true>(t, cq, zqw, zr_, qw, wrote)
+                            : early_z_quad4<SG_CMP_LESS_EQUAL, false>(t, cq, zqw, zr_, qw, wrote);
+                else if (func == SG_CMP_LESS)
                   tq = d24z ? early_z_quad<SG_CMP_LESS, true>(t, cq, zqw, zr_, qw, wrote)
                             : early_z_quad<SG_CMP_LESS, false>(t, cq, zqw, zr_, qw, wrote);
                 else if (func == SG_CMP_LESS_EQUAL)
