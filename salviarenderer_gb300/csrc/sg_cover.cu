@@ -108,6 +108,21 @@ __device__ inline void z_range(uint32_t const* zq, int zrow, Quad const& qd, boo
   for (int i = 0; i < 4; ++i) {
     if (!((qd.inside >> i) & 1u)) continue;
     uint32_t const* zp = zq + (i >> 1) * zrow + (i & 1) * S;
+    if (S == 4) {  // the pixel's four words are one 16-byte word
+      uint4 const w4 = *reinterpret_cast<uint4 const*>(zp);
+      uint32_t const w[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        if (d24) {
+          r.qmax = max(r.qmax, w[s] & 0xFFFFFFu);
+          r.qmin = min(r.qmin, w[s] & 0xFFFFFFu);
+        } else {
+          r.zmax = fmaxf(r.zmax, __uint_as_float(w[s]));
+          r.zmin = fminf(r.zmin, __uint_as_float(w[s]));
+        }
+      }
+      continue;
+    }
     for (uint32_t s = 0; s < S; ++s) {
       uint32_t w = zp[s];
       if (d24) {
@@ -498,6 +513,7 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
       uint32_t* const zb = (P.zbackup && !T.zpre_known) ? P.zbackup + static_cast<size_t>(tile) * P.zbackup_tile_words +
                                            (static_cast<size_t>(by0) * 4 * TILE + bx0 * 4) * S
                                      : nullptr;
+#pragma unroll 4
       for (uint32_t i = tid; i < qh * zrow; i += CV_THREADS) {
         uint32_t y = i >> (__ffs(zrow) - 1), k = i & (zrow - 1);  // zrow: a power of two
         if (k >= qw * S) continue;
