@@ -44,7 +44,7 @@ constexpr int CV_THREADS = 256;              // 64 blocks x 4 quads
 constexpr int CV_STAGE = 128;                // triangles per staged batch
 constexpr int CV_WORDS = CV_STAGE / 32;
 constexpr int CV_PX = 32;                    // quadrant edge
-constexpr int CV_K = 12;                     // pairs per block per round
+constexpr int CV_K = 16;                     // pairs per block per round
 
 struct TriCv {  // what coverage and early-Z read of a triangle
   float4 e0, e1, e2, bbox;
