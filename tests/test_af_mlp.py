@@ -91,8 +91,8 @@ def test_training_beats_tap_average(gdev):
     tex = scenes.AfTextures(gdev, count=192, size=256, seed=1)
     held = scenes.AfTextures(gdev, count=48, size=256, seed=2)
     m = AfModel(gdev, seed=3)
-    rep = m.train(tex.samplers, samples=1 << 21, batch=8192, epochs=2, lr=2e-3, seed=5)
-    assert rep["steps"] == 512
+    rep = m.train(tex.samplers, samples=1 << 22, batch=8192, epochs=3, lr=2e-3, seed=5)
+    assert rep["steps"] == 1536
     assert rep["last_loss"] < rep["first_loss"], rep
     f, y = gdev.af_sample(held.samplers, 1 << 16, seed=99)
     assert np.all(np.isfinite(f)) and np.all((y >= 0) & (y <= 1))
