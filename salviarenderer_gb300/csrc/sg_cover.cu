@@ -77,6 +77,7 @@ struct CvShared {
   // whether a walk wrote depth since its range was last taken
   uint32_t own_first[CV_THREADS], own_cur[CV_THREADS], own_count[CV_THREADS];
   uint32_t walk[CV_THREADS];
+  uint32_t nwalk;
   uint8_t zdirty[64];
 };
 // followed by the staged depth: CV_PX * CV_PX * samples words (early-Z only)
@@ -571,6 +572,7 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
       for (;;) {
         // this round's pairs: the block's next CV_K triangles in primitive order
         uint32_t n = 0;
+        if (tid == 0) sh.nwalk = 0;
 #pragma unroll
         for (int w = 0; w < CV_WORDS; ++w) {
           uint32_t const fulls = sh.mask4f[w][ib] | sh.mask16[w][own16];
@@ -636,19 +638,14 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
         {
           uint32_t covb = 0;
           for (uint32_t k = 0; k < n; ++k) covb |= (quad_bits(sh.cov_cv[ib][k], q) != 0u ? 1u : 0u) << k;
-          uint32_t const lane = tid & 31, warp = tid >> 5;
+          uint32_t const lane = tid & 31;
           uint32_t const bal = __ballot_sync(0xFFFFFFFFu, covb != 0u);
-          if (lane == 0) sh.wcnt[warp] = __popc(bal);
+          uint32_t wbase = 0;  // the warp's walkers take consecutive slots
+          if (lane == 0 && bal) wbase = atomicAdd(&sh.nwalk, static_cast<uint32_t>(__popc(bal)));
+          wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
+          if (covb) sh.walk[wbase + __popc(bal & ((1u << lane) - 1u))] = (static_cast<uint32_t>(tid) << 16) | covb;
           __syncthreads();
-          uint32_t excl = __popc(bal & ((1u << lane) - 1u)), nwalk = 0;
-#pragma unroll
-          for (int w = 0; w < CV_THREADS / 32; ++w) {
-            uint32_t const c = sh.wcnt[w];
-            excl += static_cast<uint32_t>(w) < warp ? c : 0u;
-            nwalk += c;
-          }
-          if (covb) sh.walk[excl] = (static_cast<uint32_t>(tid) << 16) | covb;
-          __syncthreads();
+          uint32_t const nwalk = sh.nwalk;
           if (static_cast<uint32_t>(tid) < nwalk) {
             uint32_t const wk = sh.walk[tid], h = wk >> 16, hq = h & 3u, hb = h >> 2;
             uint32_t pend = wk & 0xFFFFu;
