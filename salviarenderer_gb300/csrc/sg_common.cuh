@@ -125,16 +125,33 @@ __host__ __device__ inline uint32_t fmt_bytes(uint32_t fmt) {
   }
 }
 
+// Byte `sel & 3` of u as a float, exactly: the byte in the low mantissa bits
+// of 2^23 (one byte permute), minus 2^23 -- a byte permute and an add in
+// place of an integer-to-float conversion.  `sel` is 0x7440 + the byte.
+__device__ __forceinline__ float byte_to_f(uint32_t u, uint32_t sel) {
+  return __uint_as_float(__byte_perm(u, 0x4B000000u, sel)) - 8388608.0f;
+}
 __device__ inline v4 unorm8_to_f(uint32_t r, uint32_t g, uint32_t b, uint32_t a) {  // colors.h:176-179
   const float inv_255 = 1.0f / 255;
   return mk4(static_cast<float>(r) * inv_255, static_cast<float>(g) * inv_255,
              static_cast<float>(b) * inv_255, static_cast<float>(a) * inv_255);
 }
+// the four bytes of an RGBA8 (rgba) or BGRA8 texel word as colors.h:176-179
+// converts them
+__device__ __forceinline__ v4 unorm8_word_to_f(uint32_t u, bool rgba) {
+  const float inv_255 = 1.0f / 255;
+  float const b0 = byte_to_f(u, 0x7440u), b1 = byte_to_f(u, 0x7441u), b2 = byte_to_f(u, 0x7442u),
+              b3 = byte_to_f(u, 0x7443u);
+  return rgba ? mk4(b0 * inv_255, b1 * inv_255, b2 * inv_255, b3 * inv_255)
+              : mk4(b2 * inv_255, b1 * inv_255, b0 * inv_255, b3 * inv_255);
+}
 __device__ inline uint32_t f_to_unorm8(float c) {  // color_rgba8::assign, SSE path (colors.h:182-192)
   float m = c * 255.0f;
   m = sse_max(m, 0.0f);
   m = sse_min(m, 255.0f);
-  return static_cast<uint32_t>(cvt_rne(m)) & 0xFFu;
+  // m is in [0, 255] (NaN became 0): adding 2^23 rounds it to the nearest
+  // integer, ties to even, in the low mantissa bits -- cvt_rne's value
+  return __float_as_uint(m + 8388608.0f) & 0xFFu;
 }
 // EXTENSION (RGBA16F): IEEE binary16, round to nearest even.
 __device__ inline uint16_t f32_to_f16(float f) { return __half_as_ushort(__float2half_rn(f)); }
@@ -150,14 +167,8 @@ __device__ inline v4 read_texel(uint32_t fmt, uint8_t const* p) {
     float const* f = reinterpret_cast<float const*>(p);
     return mk4(f[0], f[1], f[2], 1.0f);
   }
-  case SG_FMT_BGRA8: {
-    uint32_t u = *reinterpret_cast<uint32_t const*>(p);
-    return unorm8_to_f((u >> 16) & 0xFF, (u >> 8) & 0xFF, u & 0xFF, u >> 24);
-  }
-  case SG_FMT_RGBA8: {
-    uint32_t u = *reinterpret_cast<uint32_t const*>(p);
-    return unorm8_to_f(u & 0xFF, (u >> 8) & 0xFF, (u >> 16) & 0xFF, u >> 24);
-  }
+  case SG_FMT_BGRA8: return unorm8_word_to_f(*reinterpret_cast<uint32_t const*>(p), false);
+  case SG_FMT_RGBA8: return unorm8_word_to_f(*reinterpret_cast<uint32_t const*>(p), true);
   case SG_FMT_R32F: return mk4(*reinterpret_cast<float const*>(p), 0.0f, 0.0f, 0.0f);
   case SG_FMT_RG32F: {
     float2 f = *reinterpret_cast<float2 const*>(p);
@@ -226,8 +237,7 @@ __device__ inline v4 lerp_2d_unorm8(bool rgba, uint8_t const* a, uint8_t const* 
                                     uint8_t const* d, float tx, float ty) {
   auto ld = [&](uint8_t const* p) {
     uint32_t u = *reinterpret_cast<uint32_t const*>(p);
-    float x = static_cast<float>(u & 0xFF), y = static_cast<float>((u >> 8) & 0xFF),
-          z = static_cast<float>((u >> 16) & 0xFF), w = static_cast<float>(u >> 24);
+    float x = byte_to_f(u, 0x7440u), y = byte_to_f(u, 0x7441u), z = byte_to_f(u, 0x7442u), w = byte_to_f(u, 0x7443u);
     return rgba ? mk4(x, y, z, w) : mk4(z, y, x, w);
   };
   v4 r = lerp4(ld(a), ld(b), ld(c), ld(d), tx, ty);

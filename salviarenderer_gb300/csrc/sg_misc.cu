@@ -69,7 +69,7 @@ __device__ void resolve_job(SurfaceJob const& j, uint32_t part, uint32_t nparts)
       uint32_t w[4] = {s.x, s.y, s.z, s.w};
 #pragma unroll
       for (int k = 0; k < 4; ++k)
-        c = c + unorm8_to_f(w[k] & 0xFF, (w[k] >> 8) & 0xFF, (w[k] >> 16) & 0xFF, w[k] >> 24);
+        c = c + unorm8_word_to_f(w[k], true);
     } else {
       for (uint32_t s = 0; s < samples; ++s) c = c + read_texel(j.fmt, j.src + (i * samples + s) * j.esz);
     }

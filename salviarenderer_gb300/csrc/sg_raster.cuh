@@ -163,8 +163,8 @@ __device__ inline void blend(TargetParams const& T, DrawParams const& D, uint32_
 // conversions), and the blend programs on a decoded value.
 __device__ inline v4 decode_word(uint32_t fmt, uint32_t u) {
   switch (fmt) {
-  case SG_FMT_BGRA8: return unorm8_to_f((u >> 16) & 0xFF, (u >> 8) & 0xFF, u & 0xFF, u >> 24);
-  case SG_FMT_RGBA8: return unorm8_to_f(u & 0xFF, (u >> 8) & 0xFF, (u >> 16) & 0xFF, u >> 24);
+  case SG_FMT_BGRA8: return unorm8_word_to_f(u, false);
+  case SG_FMT_RGBA8: return unorm8_word_to_f(u, true);
   case SG_FMT_R32F: return mk4(__uint_as_float(u), 0.0f, 0.0f, 0.0f);
   case SG_FMT_R32I: return mk4(static_cast<float>(static_cast<int32_t>(u)), 0.0f, 0.0f, 0.0f);
   default: return mk4(0, 0, 0, 0);
