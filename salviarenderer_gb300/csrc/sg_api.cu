@@ -33,7 +33,7 @@ void launch_bin(PassParams const& p, bool fill, cudaStream_t s);
 void launch_scan(uint32_t* data, size_t n, uint32_t* sums, PassCounters* ctr, cudaStream_t s);
 void launch_tile_ranges(PassParams const& p, cudaStream_t s);
 cudaError_t launch_tile_order(PassParams const& P, uint32_t* counts, cudaStream_t s);
-cudaError_t launch_frag_classes(PassParams const& P, uint32_t num_sms, cudaStream_t s);
+cudaError_t launch_frag_classes(PassParams const& P, uint32_t num_sms, bool counted, cudaStream_t s);
 void launch_cover(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t grid, cudaStream_t s);
 cudaError_t init_cover();
 void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t ctas_per_sm, uint32_t grid,
@@ -1186,11 +1186,17 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
         return SG_OK;
       }
       ev = stage_begin(d, profile);
-      if (tu.cover_threads_per_block == 2)
-        launch_cover2(P, pl.max_samples, pl.any_early_z, tu.cover_ctas_per_sm, std::min<uint32_t>(pl.ntiles * 4, sms * 8),
-                      s);
-      else
+      // k_cover2 counts its fragments per shade key into the class counters
+      bool const cover_counts = P.frag_list && tu.cover_threads_per_block == 2;
+      if (cover_counts) SG_CUDA(d, cudaMemsetAsync(P.class_counts, 0, 256 * sizeof(uint32_t), s));
+      if (tu.cover_threads_per_block == 2) {
+        PassParams Pc = P;
+        Pc.cover_counts_classes = cover_counts ? 1u : 0u;
+        launch_cover2(Pc, pl.max_samples, pl.any_early_z, tu.cover_ctas_per_sm,
+                      std::min<uint32_t>(pl.ntiles * 4, sms * 8), s);
+      } else {
         launch_cover(P, pl.max_samples, pl.any_early_z, cover_grid, s);
+      }
       stage_end(d, 2, ev);
       if (profile && d->profiling && d->prof_af) {
         launch_cover_count(P, d->prof_af, s);
@@ -1198,8 +1204,8 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       }
       ev = stage_begin(d, profile);
       if (P.frag_list) {
-        SG_CUDA(d, launch_frag_classes(P, sms, s));
-        k += 2;
+        SG_CUDA(d, launch_frag_classes(P, sms, cover_counts, s));
+        k += cover_counts ? 1 : 2;
       }
       // shade classes: varyings, plus 8 for learned-filter draws (which the
       // plain instances shade when the pass has no lookup queue)

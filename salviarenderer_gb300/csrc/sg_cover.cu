@@ -78,6 +78,7 @@ struct CvShared {
   uint32_t own_first[CV_THREADS], own_cur[CV_THREADS], own_count[CV_THREADS];
   uint32_t walk[CV_THREADS];
   uint32_t nwalk;
+  uint32_t keycnt[128];  // fragments per shade key (cover_counts_classes)
   uint8_t zdirty[64];
 };
 // followed by the staged depth: CV_PX * CV_PX * samples words (early-Z only)
@@ -467,6 +468,7 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
   int const tid = threadIdx.x, q = tid & 3, ib = tid >> 2;
   int const ibx = ib & 7, iby = ib >> 3, qx0 = (q & 1) * 2, qy0 = (q >> 1) * 2;
   uint32_t const nitems = P.ntiles * 4;
+  if (tid < 128) sh.keycnt[tid] = 0;  // ordered before use by the item loop's first barrier
   for (;;) {
     if (tid == 0) sh.item = atomicAdd(&P.counters->tile_cursor, 1u);
     __syncthreads();
@@ -700,10 +702,12 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
               if (!tq) continue;
               uint32_t const uq = quad_bits(sh.cov_uc[hb][k], static_cast<int>(hq));
               bool const fullq = (e8 >> 7) ? cq == qfull : (uq == qfull && cq == uq);
-              owner_append(P, Lw, t.entry >> 1,
-                           (static_cast<uint32_t>(qw.x) >> 1) | ((static_cast<uint32_t>(qw.y) >> 1) << 12) |
-                               (fullq ? 1u << 24 : 0u) | (t.shade_key << 25),
-                           tq | (cq << 16));
+              if (owner_append(P, Lw, t.entry >> 1,
+                               (static_cast<uint32_t>(qw.x) >> 1) | ((static_cast<uint32_t>(qw.y) >> 1) << 12) |
+                                   (fullq ? 1u << 24 : 0u) | (t.shade_key << 25),
+                               tq | (cq << 16)) &&
+                  P.cover_counts_classes)
+                atomicAdd(&sh.keycnt[t.shade_key], 1u);
             }
             sh.own_first[h] = Lw.first;
             sh.own_cur[h] = Lw.cur;
@@ -732,6 +736,10 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
     }
     P.owner_first[static_cast<size_t>(tile) * QUAD_OWNERS + (by * 2 + (q >> 1)) * 32 + bx * 2 + (q & 1)] =
         sh.own_first[tid];
+  }
+  if (P.cover_counts_classes) {  // the CTA's fragments per shade key, once
+    __syncthreads();
+    if (tid < 128 && sh.keycnt[tid]) atomicAdd(&P.class_counts[tid], sh.keycnt[tid]);
   }
 }
 

@@ -384,10 +384,14 @@ void launch_tile_ranges(PassParams const& P, cudaStream_t s) {
   k_tile_ranges<<<(P.ntiles + 255) / 256, 256, 0, s>>>(P);
 }
 // P.frag_list / P.class_counts (zeroed here) in scratch.
-cudaError_t launch_frag_classes(PassParams const& P, uint32_t num_sms, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(P.class_counts, 0, 256 * sizeof(uint32_t), s);
-  if (e != cudaSuccess) return e;
-  k_frag_classes<<<num_sms * 4, 256, 0, s>>>(P, 0u);
+// With `counted`, the coverage pass counted the keys into zeroed counters
+// already (cover_counts_classes): only the scatter runs.
+cudaError_t launch_frag_classes(PassParams const& P, uint32_t num_sms, bool counted, cudaStream_t s) {
+  if (!counted) {
+    cudaError_t e = cudaMemsetAsync(P.class_counts, 0, 256 * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    k_frag_classes<<<num_sms * 4, 256, 0, s>>>(P, 0u);
+  }
   k_frag_classes<<<num_sms * 4, 256, 0, s>>>(P, 1u);
   return cudaGetLastError();
 }

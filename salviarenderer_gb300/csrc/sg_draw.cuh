@@ -214,6 +214,9 @@ struct PassParams {
   uint32_t af_net_capacity;     // records of af_net (and entries of af_fallback)
   uint32_t af_capacity;         // records of af_plain: every pixel of the pass; 0 = no queues, the plain
                                 // shading instances take the learned-filter draws
+  // set for the coverage kernel that counts its fragments per shade key into
+  // class_counts[0..127] itself (k_frag_classes then only scatters)
+  uint32_t cover_counts_classes;
 };
 
 // A lookup for the plain sampler: (u, v, ddx.u, ddx.v), (ddy.u, ddy.v,

@@ -271,7 +271,7 @@ struct OwnerList {
   uint32_t first, cur, count;  // first chunk, current chunk, slots used in it
 };
 
-__device__ inline void owner_append(PassParams const& P, OwnerList& L, uint32_t rec, uint32_t pos, uint32_t mask) {
+__device__ inline bool owner_append(PassParams const& P, OwnerList& L, uint32_t rec, uint32_t pos, uint32_t mask) {
   // a new chunk when the list has none or its chunk is full: the threads of
   // the warp appending together take theirs with one atomic on the shared
   // counter (one address every SM allocates from)
@@ -287,7 +287,7 @@ __device__ inline void owner_append(PassParams const& P, OwnerList& L, uint32_t 
     uint32_t const c = base + static_cast<uint32_t>(__popc(want & ((1u << lane) - 1u)));
     if (c >= P.chunk_capacity) {
       atomicOr(&P.counters->overflow, OVF_FRAG);
-      return;
+      return false;
     }
     if (L.cur == NO_CHUNK) {
       L.first = c;
@@ -302,6 +302,7 @@ __device__ inline void owner_append(PassParams const& P, OwnerList& L, uint32_t 
   P.frag_rec[f] = rec;
   P.frag_pos[f] = pos;
   P.frag_mask[f] = mask;
+  return true;
 }
 
 // Per-level edge parameters of one triangle: TILE * e, then * 0.25 per level
