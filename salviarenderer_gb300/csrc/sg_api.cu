@@ -966,7 +966,7 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   SG_CUDA(d, sc.recs.ensure(static_cast<size_t>(pl.rec_units) * sizeof(float4)));
   SG_CUDA(d, sc.bin_counts.ensure(pl.ncounts * 4));
   SG_CUDA(d, sc.scan_sums.ensure((pl.ncounts / 4096 + 2) * 4));
-  SG_CUDA(d, sc.bin_entries.ensure(static_cast<size_t>(sc.entry_capacity) * 5));  // entries, then their quadrant bytes
+  SG_CUDA(d, sc.bin_entries.ensure(static_cast<size_t>(sc.entry_capacity) * 4));
   SG_CUDA(d, sc.tile_begin.ensure((static_cast<size_t>(pl.ntiles) + 1) * 4));
   SG_CUDA(d, sc.tile_order.ensure((static_cast<size_t>(pl.ntiles) + 64) * 4));
   // fragment room: a chunk for every quad owner of the pass's targets, and
@@ -1026,7 +1026,6 @@ int32_t scratch_arenas(sg_device* d, Scratch& sc, PassPlan const& pl, PlanLayout
   P.rec_capacity = static_cast<uint32_t>(pl.rec_units);
   P.bin_counts = static_cast<uint32_t*>(sc.bin_counts.ptr);
   P.bin_entries = static_cast<uint32_t*>(sc.bin_entries.ptr);
-  P.bin_quad = reinterpret_cast<uint8_t*>(P.bin_entries + sc.entry_capacity);
   P.bin_capacity = sc.entry_capacity;
   P.tile_begin = static_cast<uint32_t*>(sc.tile_begin.ptr);
   P.tile_order = static_cast<uint32_t*>(sc.tile_order.ptr);
@@ -1082,9 +1081,8 @@ int32_t scratch_static(sg_device* d, uint8_t* base, PassPlan const& pl, PlanLayo
     return SG_INVALID_PARAMETER;
   }
   size_t rest = SG_STATIC_SCRATCH_BYTES - off;
-  uint32_t entries = static_cast<uint32_t>(rest / 4 / 5);  // 4 bytes and a quadrant byte each
+  uint32_t entries = static_cast<uint32_t>(rest / 4 / 4);
   P.bin_entries = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(entries) * 4));
-  P.bin_quad = take(entries);
   P.bin_capacity = entries;
   uint32_t chunks = static_cast<uint32_t>((SG_STATIC_SCRATCH_BYTES - off - 7 * 256) / per_chunk_bytes(pl.more_colors));
   size_t nfrag = static_cast<size_t>(chunks) * FRAG_CHUNK;

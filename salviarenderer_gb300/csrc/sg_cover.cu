@@ -327,12 +327,15 @@ __device__ inline uint32_t early_z_quad4(TriCv const& t, uint32_t cq, uint32_t* 
 }
 
 // Fills the batch: from bin entry `bpos` on, the entries whose triangle's
-// bounding box reaches quadrant `sub` of the tile (bit `sub` of the
-// entry's quadrant byte), in order, at most CV_STAGE of them.  A triangle
+// bounding box reaches the quadrant (x in [qx0, qx0 + 32), y in [qy0,
+// qy0 + 32) of the tile), in order, at most CV_STAGE of them.  A triangle
 // whose box misses the quadrant misses every one of its regions, so the
 // classification below would give it no bit.  Returns the batch's size and
 // advances `bpos` past the last entry taken (or examined).
-__device__ inline uint32_t cv_fill(PassParams const& P, uint32_t& bpos, uint32_t end, uint32_t sub, CvShared& sh) {
+__device__ inline uint32_t cv_fill(PassParams const& P, uint32_t& bpos, uint32_t end, int tile_x0, int tile_y0,
+                                   int qx0, int qy0, CvShared& sh) {
+  float const tx0f = static_cast<float>(tile_x0), ty0f = static_cast<float>(tile_y0);
+  float const xs = static_cast<float>(qx0), xe = xs + CV_PX, ys = static_cast<float>(qy0), ye = ys + CV_PX;
   int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   uint32_t nst = 0;
   for (;;) {
@@ -341,9 +344,11 @@ __device__ inline uint32_t cv_fill(PassParams const& P, uint32_t& bpos, uint32_t
     bool reach = false;
     if (cand < end) {
       e = P.bin_entries[cand];
-      // accepted for the whole tile by the binner, or its bounding box
-      // reaches the quadrant (the binner's quadrant bits)
-      reach = (e & 1u) != 0 || ((P.bin_quad[cand] >> sub) & 1u) != 0;
+      reach = (e & 1u) != 0;  // accepted for the whole tile by the binner
+      if (!reach) {
+        float4 const bb = P.recs[(e >> 1) + 3];
+        reach = !(bb.x - tx0f >= xe || bb.y - tx0f < xs || bb.z - ty0f >= ye || bb.w - ty0f < ys);
+      }
     }
     uint32_t const bal = __ballot_sync(0xFFFFFFFFu, reach);
     if (lane == 0) sh.wcnt[warp] = __popc(bal);
@@ -542,7 +547,7 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
       if (q == 0) sh.zdirty[ib] = 0;
       uint32_t* const masks = &sh.mask4[0][0];
       for (int i = tid; i < (64 + 64 + 4) * CV_WORDS; i += CV_THREADS) masks[i] = 0;
-      uint32_t const nb = cv_fill(P, bpos, end, sub, sh);
+      uint32_t const nb = cv_fill(P, bpos, end, tile_x0, tile_y0, bx0 * 4, by0 * 4, sh);
       if (nb == 0) break;
       if (tid == 0) atomicAdd(&P.counters->cover_batches, 1u);
       cv_stage(P, T, nb, tile_x0, tile_y0, bx0, by0, sh);

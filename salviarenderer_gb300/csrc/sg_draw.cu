@@ -53,22 +53,6 @@ struct TileTest {
   }
 };
 
-// The 32x32 quadrants of tile (tx, ty) that bounding box `bb` reaches, bit
-// qy * 2 + qx: the coverage pass's fill test, with the same float operations.
-__device__ inline uint32_t quadrant_bits(float4 const& bb, int tx, int ty) {
-  float const tx0f = static_cast<float>(tx * TILE), ty0f = static_cast<float>(ty * TILE);
-  uint32_t m = 0;
-#pragma unroll
-  for (int qy = 0; qy < 2; ++qy)
-#pragma unroll
-    for (int qx = 0; qx < 2; ++qx) {
-      float const xs = static_cast<float>(qx * 32), xe = xs + 32, ys = static_cast<float>(qy * 32), ye = ys + 32;
-      bool const reach = !(bb.x - tx0f >= xe || bb.y - tx0f < xs || bb.z - ty0f >= ye || bb.w - ty0f < ys);
-      m |= static_cast<uint32_t>(reach) << (qy * 2 + qx);
-    }
-  return m;
-}
-
 // Tiles up to which one lane tests a triangle's tiles alone in the count pass.
 constexpr int BIN_LANE_TILES = 8;
 
@@ -97,14 +81,14 @@ __global__ void __launch_bounds__(128) k_bin(PassParams P) {
   for (uint32_t base = begin; base < end; base += 32) {
     uint32_t slot = base + lane;
     uint32_t rec = slot < end ? P.slot_rec[slot] : NO_REC;
-    float4 e0 = make_float4(0, 0, 0, 0), e1 = e0, e2 = e0, bb = e0;
+    float4 e0 = make_float4(0, 0, 0, 0), e1 = e0, e2 = e0;
     int sx = 0, sy = 0, ex = 0, ey = 0;
     if (rec != NO_REC) {
       float4 const* R = P.recs + rec;
       e0 = R[0];
       e1 = R[1];
       e2 = R[2];
-      bb = R[3];
+      float4 bb = R[3];
       DrawParams const& D = P.draws[rec_draw(R)];
       int const tx_n = D.tiles_x, ty_n = D.tiles_y;
       sx = min(fast_floori_f(smax(0.0f, bb.x) / TILE), tx_n);
@@ -178,10 +162,7 @@ __global__ void __launch_bounds__(128) k_bin(PassParams P) {
             *cc = pos + static_cast<uint32_t>(__popc(grp));
           }
           pos = __shfl_sync(grp, pos, leader) + static_cast<uint32_t>(__popc(grp & lt_mask));
-          if (pos < P.bin_capacity) {
-            P.bin_entries[pos] = rec << 1;
-            P.bin_quad[pos] = static_cast<uint8_t>(quadrant_bits(bb, sx, sy));
-          }
+          if (pos < P.bin_capacity) P.bin_entries[pos] = rec << 1;
         }
         pending &= ~run;
         __syncwarp();
@@ -198,8 +179,6 @@ __global__ void __launch_bounds__(128) k_bin(PassParams P) {
                             __shfl_sync(0xFFFFFFFFu, e2.z, m), 0.0f));
         int const tsx = __shfl_sync(0xFFFFFFFFu, sx, m), tsy = __shfl_sync(0xFFFFFFFFu, sy, m);
         int const tw = __shfl_sync(0xFFFFFFFFu, w, m), tn = __shfl_sync(0xFFFFFFFFu, nt, m);
-        float4 const tbb = make_float4(__shfl_sync(0xFFFFFFFFu, bb.x, m), __shfl_sync(0xFFFFFFFFu, bb.y, m),
-                                       __shfl_sync(0xFFFFFFFFu, bb.z, m), __shfl_sync(0xFFFFFFFFu, bb.w, m));
         for (int j = lane; j < tn; j += 32) {
           int x = tsx + j % tw, y = tsy + j / tw;
           int const res = tt.test(x, y);
@@ -210,10 +189,7 @@ __global__ void __launch_bounds__(128) k_bin(PassParams P) {
             uint32_t* cc = cnt + static_cast<size_t>(y * tgx + x) * nch;
             uint32_t pos = *cc;
             *cc = pos + 1;
-            if (pos < P.bin_capacity) {
-              P.bin_entries[pos] = (r << 1) | static_cast<uint32_t>(res & 1);
-              P.bin_quad[pos] = static_cast<uint8_t>(quadrant_bits(tbb, x, y));
-            }
+            if (pos < P.bin_capacity) P.bin_entries[pos] = (r << 1) | static_cast<uint32_t>(res & 1);
           }
         }
         __syncwarp();

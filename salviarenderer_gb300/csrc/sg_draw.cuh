@@ -217,9 +217,6 @@ struct PassParams {
   // set for the coverage kernel that counts its fragments per shade key into
   // class_counts[0..127] itself (k_frag_classes then only scatters)
   uint32_t cover_counts_classes;
-  // beside each bin entry: the 32x32 quadrants of its tile the triangle's
-  // bounding box reaches (bit qy * 2 + qx), for the coverage pass's fill
-  uint8_t* bin_quad;
 };
 
 // A lookup for the plain sampler: (u, v, ddx.u, ddx.v), (ddy.u, ddy.v,
