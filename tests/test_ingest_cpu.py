@@ -178,3 +178,27 @@ def test_obj_out_of_range_is_refused(product_lib, tmp_path, text):
 def test_obj_missing_file(product_lib, tmp_path):
     assert ingest.load_obj(product_lib, str(tmp_path / "none.obj"), False) is None
     assert oracle.obj_load(str(tmp_path / "none.obj"), False) is None
+
+
+# the reference's source tree, as __graft_entry__ finds it: $SALVIA_REFERENCE,
+# else a "reference" directory beside the repository
+REF_ROOT = os.environ.get("SALVIA_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
+
+
+@pytest.mark.parametrize("rel", ["resources/texture_and_blending/chessboard.png", "resources/font/font_enu.png",
+                                 "res/Logo2D_2012.png", "res/Logo3DWithIBL.png"])
+def test_reference_repository_pngs(product_lib, rel):
+    """The PNG files the reference's own repository ships (the
+    TextureAndBlending sample's chessboard texture among them), where a
+    checkout of it is at hand: the library and the oracle agree, 16-bit files
+    included (both refuse them)."""
+    path = os.path.join(REF_ROOT, rel)
+    if not os.path.exists(path):
+        pytest.skip("no reference checkout here")
+    data = open(path, "rb").read()
+    want = oracle.png_decode(data)
+    got = ingest.decode_image(product_lib, data)
+    if want is None:
+        assert got is None
+    else:
+        np.testing.assert_array_equal(got, want)
