@@ -17,7 +17,7 @@
 namespace sg {
 
 // the geometry kernel without user vertex shaders
-__global__ void __launch_bounds__(128) k_geometry(PassParams P) { geometry_pass<void>(P); }
+__global__ void __launch_bounds__(128, 4) k_geometry(PassParams P) { geometry_pass<void>(P); }
 
 // ---------------------------------------------------------------------------
 // binning (rasterizer::threaded_dispatch_primitive, rasterizer.cpp:775-862)
