@@ -1157,6 +1157,14 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
       uint32_t merge_grid = std::min<uint32_t>(pl.ntiles, sms * tu.merge_ctas_per_sm);
       uint32_t cover_grid = std::min<uint32_t>(pl.ntiles * 16, sms * 4);
       uint32_t shade_grid = sms * tu.shade_ctas_per_sm;
+      // k_cover2 counts its fragments per shade key into the class counters
+      bool const cover_counts = P.frag_list && tu.cover_threads_per_block == 2 && !pl.lines;
+      // the pass's counters are cleared before its first kernel, so that the
+      // kernels after it follow one another with no other work between them
+      // (programmatic dependent launches)
+      SG_CUDA(d, cudaMemsetAsync(P.bin_counts, 0, pl.ncounts * 4, s));
+      if (P.tile_order) SG_CUDA(d, cudaMemsetAsync(P.tile_order + pl.ntiles, 0, 64 * sizeof(uint32_t), s));
+      if (cover_counts) SG_CUDA(d, cudaMemsetAsync(P.class_counts, 0, 256 * sizeof(uint32_t), s));
       cudaEvent_t ev = stage_begin(d, profile);
       if (pl.user_vs)  // the geometry with the pass's user vertex shader, every draw
         pl.user_vs->device_launch(&P, 0u, (pl.nprims + 127) / 128, s);
@@ -1164,7 +1172,6 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
         launch_geometry(P, s);
       stage_end(d, 0, ev);
       ev = stage_begin(d, profile);
-      SG_CUDA(d, cudaMemsetAsync(P.bin_counts, 0, pl.ncounts * 4, s));
       launch_bin(P, false, s);
       launch_scan(P.bin_counts, pl.ncounts, v.scan_sums, P.counters, s);
       launch_tile_ranges(P, s);
@@ -1186,9 +1193,6 @@ int32_t launch_pass(sg_device* d, PassPlan const& pl, ScratchView& v, std::vecto
         return SG_OK;
       }
       ev = stage_begin(d, profile);
-      // k_cover2 counts its fragments per shade key into the class counters
-      bool const cover_counts = P.frag_list && tu.cover_threads_per_block == 2;
-      if (cover_counts) SG_CUDA(d, cudaMemsetAsync(P.class_counts, 0, 256 * sizeof(uint32_t), s));
       if (tu.cover_threads_per_block == 2) {
         PassParams Pc = P;
         Pc.cover_counts_classes = cover_counts ? 1u : 0u;

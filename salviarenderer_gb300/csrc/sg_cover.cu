@@ -459,6 +459,7 @@ __device__ inline void cv_stage(PassParams const& P, TargetParams const& T, uint
 // MINB: CTAs per SM the register budget is cut for (3: 80 registers, 4: 64)
 template <int MINB>
 __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
+  pdl_wait();
   extern __shared__ __align__(16) uint8_t smem_raw[];
   CvShared& sh = *reinterpret_cast<CvShared*>(smem_raw);
   uint32_t* const ztile = reinterpret_cast<uint32_t*>(smem_raw + ((sizeof(CvShared) + 15) & ~size_t(15)));
@@ -749,6 +750,7 @@ __global__ void __launch_bounds__(CV_THREADS, MINB) k_cover2(PassParams P) {
 // leaves its targets as it found them and the host can run it again.  (A
 // pass that overflowed its bins or records skipped the coverage pass.)
 __global__ void __launch_bounds__(256) k_cover_rollback(PassParams P) {
+  pdl_wait();
   if (pass_gated(P)) return;
   uint32_t const ovf = P.counters->overflow;
   if (!(ovf & (OVF_FRAG | OVF_AF_QUEUE)) || (ovf & (OVF_BIN | OVF_REC))) return;
@@ -783,15 +785,15 @@ void launch_cover_count(PassParams const& p, unsigned long long* acc, cudaStream
 }
 
 void launch_cover_rollback(PassParams const& p, uint32_t grid, cudaStream_t s) {
-  k_cover_rollback<<<grid, 256, 0, s>>>(p);
+  launch_pdl(k_cover_rollback, grid, 256, 0, s, p);
 }
 
 void launch_cover2(PassParams const& p, uint32_t max_samples, bool early_z, uint32_t ctas_per_sm, uint32_t grid,
                    cudaStream_t s) {
   if (ctas_per_sm >= 4)
-    k_cover2<4><<<grid, CV_THREADS, cv_smem(max_samples, early_z), s>>>(p);
+    launch_pdl(k_cover2<4>, grid, CV_THREADS, cv_smem(max_samples, early_z), s, p);
   else
-    k_cover2<3><<<grid, CV_THREADS, cv_smem(max_samples, early_z), s>>>(p);
+    launch_pdl(k_cover2<3>, grid, CV_THREADS, cv_smem(max_samples, early_z), s, p);
 }
 
 // Per device (function attributes are per device): the largest dynamic

@@ -67,6 +67,7 @@ constexpr int BIN_LANE_TILES = 8;
 // per tile), a triangle spanning several tiles by the whole warp.
 template <bool FILL>
 __global__ void __launch_bounds__(128) k_bin(PassParams P) {
+  pdl_wait();
   uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= P.nchunks || pass_gated(P)) return;
@@ -228,6 +229,7 @@ __device__ inline uint32_t block_exclusive_scan(uint32_t v, uint32_t* smem, uint
 }
 
 __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_local(uint32_t* data, size_t n, uint32_t* sums) {
+  pdl_wait();
   __shared__ uint32_t smem[32];
   size_t base = static_cast<size_t>(blockIdx.x) * SCAN_BLOCK * SCAN_ITEMS + threadIdx.x * SCAN_ITEMS;
   uint32_t v[SCAN_ITEMS], s = 0;
@@ -248,6 +250,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_local(uint32_t* data, size_
 
 // single-block scan of the block sums
 __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_sums(uint32_t* sums, uint32_t nsums, PassCounters* ctr) {
+  pdl_wait();
   __shared__ uint32_t smem[32];
   uint32_t carry = 0;
   for (uint32_t start = 0; start < nsums; start += SCAN_BLOCK * SCAN_ITEMS) {
@@ -271,12 +274,14 @@ __global__ void __launch_bounds__(SCAN_BLOCK) k_scan_sums(uint32_t* sums, uint32
 }
 
 __global__ void k_scan_add(uint32_t* data, size_t n, uint32_t const* sums) {
+  pdl_wait();
   size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n) data[i] += sums[i / (SCAN_BLOCK * SCAN_ITEMS)];
 }
 
 // tile ranges from the scanned counts, and the overflow check
 __global__ void k_tile_ranges(PassParams P) {
+  pdl_wait();
   if (pass_gated(P)) return;
   uint32_t tile = blockIdx.x * blockDim.x + threadIdx.x;
   if (tile < P.ntiles) {
@@ -296,6 +301,7 @@ __global__ void k_tile_ranges(PassParams P) {
 // depends on the order tiles are taken in).  counts[0..31] count the
 // buckets (phase 0), counts[32..63] are the buckets' cursors (phase 1).
 __global__ void k_tile_order(PassParams P, uint32_t* counts, uint32_t phase) {
+  pdl_wait();
   uint32_t const tile = blockIdx.x * blockDim.x + threadIdx.x;
   if (tile >= P.ntiles || pass_gated(P)) return;
   uint32_t const entries = P.tile_begin[tile + 1] - P.tile_begin[tile];
@@ -315,6 +321,7 @@ __global__ void k_tile_order(PassParams P, uint32_t* counts, uint32_t phase) {
 // slot).  Phase 0 counts the keys, phase 1 scatters the fragment indices;
 // one atomic per warp and key.
 __global__ void __launch_bounds__(256) k_frag_classes(PassParams P, uint32_t phase) {
+  pdl_wait();
   __shared__ uint32_t base[128];
   if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
   uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
@@ -366,22 +373,22 @@ void launch_bin(PassParams const& P, bool fill, cudaStream_t s) {
   uint32_t blocks = (P.nchunks * 32 + 127) / 128;
   if (!blocks) return;
   if (fill)
-    k_bin<true><<<blocks, 128, 0, s>>>(P);
+    launch_pdl(k_bin<true>, blocks, 128, 0, s, P);
   else
-    k_bin<false><<<blocks, 128, 0, s>>>(P);
+    launch_pdl(k_bin<false>, blocks, 128, 0, s, P);
 }
 
 // exclusive scan of `n` counts in place; `sums` needs ceil(n / 4096) entries
 void launch_scan(uint32_t* data, size_t n, uint32_t* sums, PassCounters* ctr, cudaStream_t s) {
   size_t nblocks = (n + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS);
   if (nblocks == 0) return;
-  k_scan_local<<<static_cast<uint32_t>(nblocks), SCAN_BLOCK, 0, s>>>(data, n, sums);
-  k_scan_sums<<<1, SCAN_BLOCK, 0, s>>>(sums, static_cast<uint32_t>(nblocks), ctr);
-  k_scan_add<<<static_cast<uint32_t>((n + 255) / 256), 256, 0, s>>>(data, n, sums);
+  launch_pdl(k_scan_local, static_cast<uint32_t>(nblocks), SCAN_BLOCK, 0, s, data, n, sums);
+  launch_pdl(k_scan_sums, 1, SCAN_BLOCK, 0, s, sums, static_cast<uint32_t>(nblocks), ctr);
+  launch_pdl(k_scan_add, static_cast<uint32_t>((n + 255) / 256), 256, 0, s, data, n, sums);
 }
 
 void launch_tile_ranges(PassParams const& P, cudaStream_t s) {
-  k_tile_ranges<<<(P.ntiles + 255) / 256, 256, 0, s>>>(P);
+  launch_pdl(k_tile_ranges, (P.ntiles + 255) / 256, 256, 0, s, P);
 }
 // P.frag_list / P.class_counts (zeroed here) in scratch.
 // With `counted`, the coverage pass counted the keys into zeroed counters
@@ -392,17 +399,16 @@ cudaError_t launch_frag_classes(PassParams const& P, uint32_t num_sms, bool coun
     if (e != cudaSuccess) return e;
     k_frag_classes<<<num_sms * 4, 256, 0, s>>>(P, 0u);
   }
-  k_frag_classes<<<num_sms * 4, 256, 0, s>>>(P, 1u);
+  launch_pdl(k_frag_classes, num_sms * 4, 256, 0, s, P, 1u);
   return cudaGetLastError();
 }
 
-// P.tile_order (ntiles) and `counts` (64 words, zeroed here) in scratch.
+// P.tile_order (ntiles) and `counts` (64 words, zeroed by the caller at the
+// pass's start) in scratch.
 cudaError_t launch_tile_order(PassParams const& P, uint32_t* counts, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(counts, 0, 64 * sizeof(uint32_t), s);
-  if (e != cudaSuccess) return e;
   uint32_t const blocks = (P.ntiles + 255) / 256;
-  k_tile_order<<<blocks, 256, 0, s>>>(P, counts, 0u);
-  k_tile_order<<<blocks, 256, 0, s>>>(P, counts, 1u);
+  launch_pdl(k_tile_order, blocks, 256, 0, s, P, counts, 0u);
+  launch_pdl(k_tile_order, blocks, 256, 0, s, P, counts, 1u);
   return cudaGetLastError();
 }
 

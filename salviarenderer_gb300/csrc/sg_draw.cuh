@@ -16,6 +16,30 @@
 
 namespace sg {
 
+// Programmatic dependent launch inside a pass: a kernel launched with
+// launch_pdl may be scheduled while the kernel before it in the stream is
+// finishing (its launch and the previous kernel's tail overlap); it waits
+// at its first statement (pdl_wait, griddepcontrol.wait) until that kernel
+// has completed and its memory is visible.  Launched without the
+// attribute, the wait returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args const&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+
 constexpr int TILE = 64;              // rasterizer.cpp:32 (also the classification tree's root)
 constexpr int RASTER_THREADS = 256;   // 4x4 blocks per 64x64 tile (threads of a merging CTA)
 constexpr int QUAD_OWNERS = 1024;     // owners (2x2 quads) per 64x64 tile: quad (x, y) is owner y * 32 + x

@@ -792,6 +792,7 @@ __device__ inline bool af_takes(DrawParams const& D, float dxu, float dxv, float
 // SM (64 registers) where the plain instances run 3.
 template <int NA, bool LEARNED, int MINB = (LEARNED ? 4 : 3)>
 __global__ void __launch_bounds__(256, MINB) k_shade(PassParams P) {
+  pdl_wait();
   if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
   uint32_t const nfrag = min(P.counters->chunk_total, P.chunk_capacity) * FRAG_CHUNK;
   int const q = threadIdx.x & 3;
@@ -1012,6 +1013,7 @@ __global__ void __launch_bounds__(256, MINB) k_shade(PassParams P) {
 // UBS: a user blend shader the pass's user-blend draws run (void: none).
 template <class UBS>
 __device__ __forceinline__ void merge_pass(PassParams const& P) {
+  pdl_wait();
   if (pass_gated(P)) return;
   uint32_t const ovf = P.counters->overflow;  // final: geometry, binning, coverage and shading are done
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1166,9 +1168,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, MINB) k_merge(PassParams P) { 
 template <int NA>
 void launch_shade_t(PassParams const& P, uint32_t grid, uint32_t resident, cudaStream_t s) {
   if (resident >= 4)
-    k_shade<NA, false, 4><<<grid, 256, 0, s>>>(P);
+    launch_pdl(k_shade<NA, false, 4>, grid, 256, 0, s, P);
   else
-    k_shade<NA, false, 3><<<grid, 256, 0, s>>>(P);
+    launch_pdl(k_shade<NA, false, 3>, grid, 256, 0, s, P);
 }
 template <int NA>
 void launch_shade_learned_t(PassParams const& P, uint32_t grid, cudaStream_t s) {

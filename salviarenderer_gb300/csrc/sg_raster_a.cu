@@ -33,9 +33,9 @@ cudaError_t init_cover() {
 
 void launch_merge(PassParams const& p, uint32_t grid, uint32_t resident, cudaStream_t s) {
   if (resident >= 4)
-    k_merge<4><<<grid, RASTER_THREADS, 0, s>>>(p);
+    launch_pdl(k_merge<4>, grid, RASTER_THREADS, 0, s, p);
   else
-    k_merge<3><<<grid, RASTER_THREADS, 0, s>>>(p);
+    launch_pdl(k_merge<3>, grid, RASTER_THREADS, 0, s, p);
 }
 
 }  // namespace sg
