@@ -41,6 +41,7 @@ constexpr uint32_t FILTER_TMEM_COLS = 64;
 __device__ inline bool unorm_format(uint32_t fmt) { return fmt == SG_FMT_RGBA8 || fmt == SG_FMT_BGRA8; }
 
 __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassParams P, AfModelDev M) {
+  pdl_wait();
   if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
   uint32_t const n = min(P.counters->af_lookups, P.af_net_capacity);
   if (blockIdx.x * AF_TILE >= n) return;  // no tile for this CTA: no tensor memory either
@@ -179,6 +180,7 @@ __global__ void __launch_bounds__(AF_TILE, FILTER_CTAS_PER_SM) k_af_filter(PassP
 }
 
 __global__ void __launch_bounds__(256) k_af_fallback(PassParams P) {
+  pdl_wait();
   if ((P.counters->overflow & OVF_FATAL) || pass_gated(P)) return;
   // the network's rejects (af_fallback into af_net), then the lookups
   // k_shade queued for the plain sampler (af_plain)
@@ -195,8 +197,8 @@ __global__ void __launch_bounds__(256) k_af_fallback(PassParams P) {
 }
 
 void launch_af_pass(PassParams const& P, AfModelDev const& M, uint32_t num_sms, cudaStream_t s) {
-  k_af_filter<<<num_sms * FILTER_CTAS_PER_SM, AF_TILE, sizeof(FilterSmem), s>>>(P, M);
-  k_af_fallback<<<num_sms * 4, 256, 0, s>>>(P);
+  launch_pdl(k_af_filter, num_sms * FILTER_CTAS_PER_SM, AF_TILE, sizeof(FilterSmem), s, P, M);
+  launch_pdl(k_af_fallback, num_sms * 4, 256, 0, s, P);
 }
 
 // k_af_filter's shared-memory limit on the current device.

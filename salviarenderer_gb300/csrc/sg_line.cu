@@ -130,6 +130,7 @@ __device__ bool line_pixel(TargetParams const& T, DrawParams const& D, float4 co
 }
 
 __global__ void __launch_bounds__(LINE_THREADS) k_lines(PassParams P) {
+  pdl_wait();
   if (pass_gated(P)) return;
   uint32_t const ovf = P.counters->overflow;  // final: geometry and binning are done
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -169,7 +170,9 @@ __global__ void __launch_bounds__(LINE_THREADS) k_lines(PassParams P) {
   }
 }
 
-void launch_lines(PassParams const& p, uint32_t grid, cudaStream_t s) { k_lines<<<grid, LINE_THREADS, 0, s>>>(p); }
+void launch_lines(PassParams const& p, uint32_t grid, cudaStream_t s) {
+  launch_pdl(k_lines, grid, LINE_THREADS, 0, s, p);
+}
 
 // The EWA table of this translation unit's sampler.
 cudaError_t upload_ewa_table_line(float const* tab, cudaStream_t s) {

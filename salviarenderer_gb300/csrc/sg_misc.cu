@@ -80,6 +80,7 @@ __device__ void resolve_job(SurfaceJob const& j, uint32_t part, uint32_t nparts)
 // One launch runs a list of jobs: blockIdx.y selects the job, the x blocks
 // stride over its elements.
 __global__ void __launch_bounds__(256) k_jobs(JobList L) {
+  pdl_wait();
   if (L.status) {  // a job of a pass: nothing after an overflow the host has not handled yet
     if (L.status[0] & OVF_FATAL) return;
     if (L.count_pass && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(&L.status[1], 1u);
@@ -133,7 +134,7 @@ uint32_t launch_jobs(SurfaceJob const* jobs, uint32_t n, uint32_t num_sms, cudaS
     // enough x blocks for the largest job, at most 16 per SM
     uint32_t bx = static_cast<uint32_t>(std::min<size_t>((most + 1023) / 1024, static_cast<size_t>(num_sms) * 16));
     bx = std::max<uint32_t>(1, bx);
-    k_jobs<<<dim3(bx, L.n), 256, 0, s>>>(L);
+    launch_pdl(k_jobs, dim3(bx, L.n), 256, 0, s, L);
     ++launches;
   }
   return launches;

@@ -1174,7 +1174,7 @@ void launch_shade_t(PassParams const& P, uint32_t grid, uint32_t resident, cudaS
 }
 template <int NA>
 void launch_shade_learned_t(PassParams const& P, uint32_t grid, cudaStream_t s) {
-  k_shade<NA, true><<<grid, 256, 0, s>>>(P);
+  launch_pdl(k_shade<NA, true>, grid, 256, 0, s, P);
 }
 
 }  // namespace sg
