@@ -552,6 +552,25 @@ typedef struct sg_obj_mesh {
 int32_t sg_obj_load(const char* path, int32_t flip_tex_v, sg_obj_mesh** out);
 void sg_obj_release(sg_obj_mesh* mesh);
 
+/* ---- SASL shaders -------------------------------------------------------------
+ * renderer.h:136-147 compile(code, lang) runs the reference's SASL compiler
+ * (an LLVM JIT) on a vertex or pixel shader.  sg_sasl_translate turns the
+ * same source into the C++ class of a user shader module: the text of a
+ * translation unit that includes <salvia_gb300/sasl_rt.cuh> and exports
+ * salvia_gb300_module_<class_name>(), to be built with nvcc (the GPU module)
+ * or a host C++ compiler (the host body alone).  `language` is the
+ * reference's languages value (constants.h:11-20); `entry` names the entry
+ * function (NULL: main, vs_main or ps_main, else the last function).  The
+ * reflection text lists the stage interface one item a line ("input
+ * SEMANTIC INDEX REGISTER COMPONENTS", "output ...", "uniform NAME WORD
+ * WORDS BASE ROWS COLS", "sampler NAME SLOT", "varyings N", "words N").
+ * Returns SG_INVALID_PARAMETER with the message in *out_log when the source
+ * does not translate; the strings are freed with sg_sasl_free. */
+enum { SG_LANG_GENERAL = 1, SG_LANG_VERTEX_SHADER = 2, SG_LANG_PIXEL_SHADER = 3, SG_LANG_BLENDING_SHADER = 4 };
+int32_t sg_sasl_translate(const char* source, uint32_t language, const char* entry, const char* class_name,
+                          char** out_source, char** out_reflection, char** out_log);
+void sg_sasl_free(char* p);
+
 /* ---- samplers (create_sampler, renderer.h:49) ------------------------------- */
 int32_t sg_sampler_create(sg_device* dev, const sg_sampler_desc* desc, uint32_t texture,
                           uint32_t* out_sampler);

@@ -58,6 +58,14 @@
 #ifdef __CUDACC__
 #include "sg_geometry.cuh"
 #include "sg_raster.cuh"
+#else
+// a host compiler builds the bodies for CPU backends only
+#ifndef __host__
+#define __host__
+#endif
+#ifndef __device__
+#define __device__
+#endif
 #endif
 
 namespace salvia_gb300 {
@@ -400,6 +408,58 @@ __host__ __device__ inline void pixel_accessor::color(int target, int sample, ve
 
 }  // namespace salvia_gb300
 
+// The body compiled for the host: the sg_host_*_io entry of a module.
+#define SALVIA_GB300_HOST_VE_(cls)                                                                  \
+  static int32_t salvia_gb300_host_##cls(sg_host_vs_io* io) {                                                \
+    salvia_gb300::vs_input in;                                                                                 \
+    for (int i = 0; i < SG_MAX_VS_INPUTS; ++i) in.attr[i] = salvia_gb300::detail::host_out(io->in[i]);        \
+    salvia_gb300::vs_output out;                                                                               \
+    cls vs;                                                                                                    \
+    salvia_gb300::detail::shader_access::bind(vs, io);                                                         \
+    vs.shader_prog(in, out);                                                                                   \
+    io->position[0] = out.position.x;                                                                          \
+    io->position[1] = out.position.y;                                                                          \
+    io->position[2] = out.position.z;                                                                          \
+    io->position[3] = out.position.w;                                                                          \
+    for (int i = 0; i < SG_MAX_VARYINGS; ++i) {                                                                \
+      io->attr[i][0] = out.attr[i].x;                                                                          \
+      io->attr[i][1] = out.attr[i].y;                                                                          \
+      io->attr[i][2] = out.attr[i].z;                                                                          \
+      io->attr[i][3] = out.attr[i].w;                                                                          \
+    }                                                                                                          \
+    return 1;                                                                                                  \
+  }
+
+#define SALVIA_GB300_HOST_PI_(cls)                                                                  \
+  static int32_t salvia_gb300_host_##cls(sg_host_ps_io* io) {                                                \
+    salvia_gb300::vs_output in;                                                                                \
+    float const* p = io->position;                                                                             \
+    in.position = salvia_gb300::vec4(p[0], p[1], p[2], p[3]);                                                  \
+    for (int i = 0; i < SG_MAX_VARYINGS; ++i) in.attr[i] = salvia_gb300::detail::host_out(io->attr[i]);      \
+    salvia_gb300::ps_output out;                                                                               \
+    cls ps;                                                                                                    \
+    salvia_gb300::detail::shader_access::bind(ps, io);                                                         \
+    bool const keep = ps.shader_prog(in, out);                                                                 \
+    for (int i = 0; i < SG_MAX_COLOR_TARGETS; ++i) {                                                           \
+      io->color[i][0] = out.color[i].x;                                                                        \
+      io->color[i][1] = out.color[i].y;                                                                        \
+      io->color[i][2] = out.color[i].z;                                                                        \
+      io->color[i][3] = out.color[i].w;                                                                        \
+    }                                                                                                          \
+    return keep ? 1 : 0;                                                                                       \
+  }
+
+#define SALVIA_GB300_HOST_BL_(cls)                                                                  \
+  static int32_t salvia_gb300_host_##cls(sg_host_bs_io* io) {                                                \
+    salvia_gb300::ps_output in;                                                                                \
+    for (int i = 0; i < SG_MAX_COLOR_TARGETS; ++i) in.color[i] = salvia_gb300::detail::host_out(io->in_color[i]); \
+    cls bs;                                                                                                    \
+    salvia_gb300::detail::shader_access::bind(bs, io);                                                         \
+    salvia_gb300::pixel_accessor acc;                                                                          \
+    salvia_gb300::detail::shader_access::bind(acc, io, 0u, 0u);                                                \
+    return bs.shader_prog(io->sample, acc, in) ? 1 : 0;                                                        \
+  }
+
 // ---------------------------------------------------------------------------
 // the kernels instantiated for a user shader
 
@@ -564,25 +624,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge_user(PassParams P) {
     salvia_gb300_geometry_##cls<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(                         \
         *static_cast<sg::PassParams const*>(pass));                                                            \
   }                                                                                                            \
-  static int32_t salvia_gb300_host_##cls(sg_host_vs_io* io) {                                                \
-    salvia_gb300::vs_input in;                                                                                 \
-    for (int i = 0; i < SG_MAX_VS_INPUTS; ++i) in.attr[i] = salvia_gb300::detail::host_out(io->in[i]);        \
-    salvia_gb300::vs_output out;                                                                               \
-    cls vs;                                                                                                    \
-    salvia_gb300::detail::shader_access::bind(vs, io);                                                         \
-    vs.shader_prog(in, out);                                                                                   \
-    io->position[0] = out.position.x;                                                                          \
-    io->position[1] = out.position.y;                                                                          \
-    io->position[2] = out.position.z;                                                                          \
-    io->position[3] = out.position.w;                                                                          \
-    for (int i = 0; i < SG_MAX_VARYINGS; ++i) {                                                                \
-      io->attr[i][0] = out.attr[i].x;                                                                          \
-      io->attr[i][1] = out.attr[i].y;                                                                          \
-      io->attr[i][2] = out.attr[i].z;                                                                          \
-      io->attr[i][3] = out.attr[i].w;                                                                          \
-    }                                                                                                          \
-    return 1;                                                                                                  \
-  }                                                                                                            \
+  SALVIA_GB300_HOST_VE_(cls)                                                                                  \
   extern "C" sg_shader_module const* salvia_gb300_module_##cls() {                                            \
     static sg_shader_module const m = {SG_SHADER_ABI_VERSION, SG_STAGE_VERTEX, #cls, salvia_gb300_init_##cls, \
                                        salvia_gb300_launch_##cls, nullptr, nullptr, salvia_gb300_host_##cls}; \
@@ -596,23 +638,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge_user(PassParams P) {
     sg::k_shade_user<cls><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(                              \
         *static_cast<sg::PassParams const*>(pass), key);                                                       \
   }                                                                                                            \
-  static int32_t salvia_gb300_host_##cls(sg_host_ps_io* io) {                                                \
-    salvia_gb300::vs_output in;                                                                                \
-    float const* p = io->position;                                                                             \
-    in.position = salvia_gb300::vec4(p[0], p[1], p[2], p[3]);                                                  \
-    for (int i = 0; i < SG_MAX_VARYINGS; ++i) in.attr[i] = salvia_gb300::detail::host_out(io->attr[i]);      \
-    salvia_gb300::ps_output out;                                                                               \
-    cls ps;                                                                                                    \
-    salvia_gb300::detail::shader_access::bind(ps, io);                                                         \
-    bool const keep = ps.shader_prog(in, out);                                                                 \
-    for (int i = 0; i < SG_MAX_COLOR_TARGETS; ++i) {                                                           \
-      io->color[i][0] = out.color[i].x;                                                                        \
-      io->color[i][1] = out.color[i].y;                                                                        \
-      io->color[i][2] = out.color[i].z;                                                                        \
-      io->color[i][3] = out.color[i].w;                                                                        \
-    }                                                                                                          \
-    return keep ? 1 : 0;                                                                                       \
-  }                                                                                                            \
+  SALVIA_GB300_HOST_PI_(cls)                                                                                  \
   extern "C" sg_shader_module const* salvia_gb300_module_##cls() {                                            \
     static sg_shader_module const m = {SG_SHADER_ABI_VERSION, SG_STAGE_PIXEL, #cls, salvia_gb300_init_##cls,  \
                                        salvia_gb300_launch_##cls, salvia_gb300_host_##cls, nullptr, nullptr};  \
@@ -626,18 +652,29 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_merge_user(PassParams P) {
     sg::k_merge_user<cls><<<grid, sg::RASTER_THREADS, 0, static_cast<cudaStream_t>(stream)>>>(                \
         *static_cast<sg::PassParams const*>(pass));                                                            \
   }                                                                                                            \
-  static int32_t salvia_gb300_host_##cls(sg_host_bs_io* io) {                                                \
-    salvia_gb300::ps_output in;                                                                                \
-    for (int i = 0; i < SG_MAX_COLOR_TARGETS; ++i) in.color[i] = salvia_gb300::detail::host_out(io->in_color[i]); \
-    cls bs;                                                                                                    \
-    salvia_gb300::detail::shader_access::bind(bs, io);                                                         \
-    salvia_gb300::pixel_accessor acc;                                                                          \
-    salvia_gb300::detail::shader_access::bind(acc, io, 0u, 0u);                                                \
-    return bs.shader_prog(io->sample, acc, in) ? 1 : 0;                                                        \
-  }                                                                                                            \
+  SALVIA_GB300_HOST_BL_(cls)                                                                                  \
   extern "C" sg_shader_module const* salvia_gb300_module_##cls() {                                            \
     static sg_shader_module const m = {SG_SHADER_ABI_VERSION, SG_STAGE_BLEND, #cls, salvia_gb300_init_##cls,  \
                                        salvia_gb300_launch_##cls, nullptr, salvia_gb300_host_##cls, nullptr};  \
     return &m;                                                                                                 \
   }
 #endif  // __CUDACC__
+
+#ifndef __CUDACC__
+// Host-only modules (no device entries), which CPU backends of the ABI
+// register and run: the same bodies built by a host C++ compiler.
+#define SALVIA_GB300_HOST_MODULE_(cls, stage, ps, bs, vs)                                                      \
+  extern "C" sg_shader_module const* salvia_gb300_module_##cls() {                                            \
+    static sg_shader_module const m = {SG_SHADER_ABI_VERSION, stage, #cls, nullptr, nullptr, ps, bs, vs};      \
+    return &m;                                                                                                 \
+  }
+#define SALVIA_GB300_VERTEX_SHADER(cls) \
+  SALVIA_GB300_HOST_VE_(cls)            \
+  SALVIA_GB300_HOST_MODULE_(cls, SG_STAGE_VERTEX, nullptr, nullptr, salvia_gb300_host_##cls)
+#define SALVIA_GB300_PIXEL_SHADER(cls) \
+  SALVIA_GB300_HOST_PI_(cls)           \
+  SALVIA_GB300_HOST_MODULE_(cls, SG_STAGE_PIXEL, salvia_gb300_host_##cls, nullptr, nullptr)
+#define SALVIA_GB300_BLEND_SHADER(cls) \
+  SALVIA_GB300_HOST_BL_(cls)           \
+  SALVIA_GB300_HOST_MODULE_(cls, SG_STAGE_BLEND, nullptr, salvia_gb300_host_##cls, nullptr)
+#endif

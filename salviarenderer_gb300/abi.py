@@ -247,6 +247,9 @@ SIGNATURES = {
     "sg_texture_encode_image": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(Blob)]),
     "sg_obj_load": (C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(C.POINTER(ObjMesh))]),
     "sg_obj_release": (None, [C.POINTER(ObjMesh)]),
+    "sg_sasl_translate": (C.c_int32, [C.c_char_p, C.c_uint32, C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p),
+                                      C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "sg_sasl_free": (None, [C.c_void_p]),
 }
 
 AF_FEATURES, AF_OUTPUTS, AF_PARAMS = 24, 5, 6085
@@ -262,6 +265,12 @@ PRODUCT_ONLY |= {name for name in SIGNATURES if name.startswith("sg_af_")}
 # checkers are oracle/ingest_oracle.py and the reference's own loader).
 INGEST = {"sg_image_decode", "sg_image_release", "sg_blob_release", "sg_image_encode_png", "sg_image_encode_hdr",
           "sg_texture_write_image", "sg_texture_encode_image", "sg_obj_load", "sg_obj_release"}
+
+# The SASL translator (renderer.h compile()): host code of the GPU library;
+# the draw oracle runs the modules it makes, built for the host.
+SASL = {"sg_sasl_translate", "sg_sasl_free"}
+LANG_VERTEX_SHADER = 2
+LANG_PIXEL_SHADER = 3
 
 
 def bind(lib, extra=None):

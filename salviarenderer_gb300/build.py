@@ -19,7 +19,8 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT, "libsalvia_gb300.so")
 SOURCES = ["sg_raster_a.cu", "sg_raster_b.cu", "sg_raster_c.cu", "sg_cover.cu", "sg_draw.cu", "sg_misc.cu",
-           "sg_api.cu", "sg_learned.cu", "sg_af_api.cu", "sg_af_data.cu", "sg_af_filter.cu", "sg_line.cu", "sg_ingest.cpp"]
+           "sg_api.cu", "sg_learned.cu", "sg_af_api.cu", "sg_af_data.cu", "sg_af_filter.cu", "sg_line.cu", "sg_ingest.cpp",
+           "sg_sasl.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -110,21 +110,24 @@ class Scene:
 # User shader modules (salvia_gb300/device_shader.cuh) by class name, from a
 # shared object built from the application's shader source; a scene names
 # such a program as "user:<class>".
-_USER_SHADER_LIBRARY = None
+_USER_SHADER_LIBRARIES = []
 
 
 def set_user_shader_library(path):
-    """Loads the shared object that exports salvia_gb300_module_<class>()."""
-    global _USER_SHADER_LIBRARY
+    """Loads a shared object that exports salvia_gb300_module_<class>()
+    (several may be loaded; a class is looked up in the latest first)."""
     import ctypes
-    _USER_SHADER_LIBRARY = ctypes.CDLL(path)
+    _USER_SHADER_LIBRARIES.insert(0, ctypes.CDLL(path))
 
 
 def user_shader_module(name):
-    fn = getattr(_USER_SHADER_LIBRARY, "salvia_gb300_module_" + name)
     import ctypes
-    fn.restype = ctypes.c_void_p
-    return fn()
+    for lib in _USER_SHADER_LIBRARIES:
+        fn = getattr(lib, "salvia_gb300_module_" + name, None)
+        if fn is not None:
+            fn.restype = ctypes.c_void_p
+            return fn()
+    raise KeyError("no loaded shader library exports the module " + name)
 
 
 class Bound:

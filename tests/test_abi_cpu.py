@@ -35,7 +35,7 @@ def test_product_library_exports_every_declared_symbol(product_lib):
 
 def test_oracle_library_exports_the_draw_abi(oracle_lib):
     missing = [s for s in abi.SIGNATURES
-               if s not in abi.PRODUCT_ONLY | abi.INGEST and not hasattr(oracle_lib, s)]
+               if s not in abi.PRODUCT_ONLY | abi.INGEST | abi.SASL and not hasattr(oracle_lib, s)]
     assert not missing, missing
 
 
