@@ -24,11 +24,19 @@
 // Header-only, C++17.  Link with libsalvia_gb300.so.
 #pragma once
 
+#include <dlfcn.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <cstddef>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <fstream>
+#include <functional>
 #include <map>
 #include <memory>
 #include <string>
@@ -91,13 +99,77 @@ inline result to_result(int32_t s) { return static_cast<result>(s); }
 
 }  // namespace salvia
 
-// Compiled SASL shader objects (shader_object.h) are not on this path; the
-// type is declared so that the renderer's shader-code entry points keep
-// their signatures.
+// Compiled SASL shaders (shader_object.h, renderer.h:136-147).  compile()
+// translates the source with the GPU library's sg_sasl_translate into the
+// class of a user shader module, builds that with nvcc (or, with
+// SALVIA_GB300_SASL_HOST_ONLY set, the host body alone with the host
+// compiler, for CPU backends of the ABI) into $SALVIA_GB300_SHADER_CACHE
+// (default /tmp/salvia_gb300_shaders), loads it, and keeps the stage
+// interface the translator reported.  The renderer binds such an object with
+// set_vertex_shader_code / set_pixel_shader_code; its uniforms and samplers
+// come from set_vs_variable / set_ps_variable / set_vs_sampler /
+// set_ps_sampler by name.
 namespace salvia::shader {
-class shader_object;
+// constants.h:11-20
+enum languages { lang_none, lang_general, lang_vertex_shader, lang_pixel_shader, lang_blending_shader, lang_count };
+struct shader_profile {  // reflection.h:10-12
+  languages language;
+};
+
+class shader_object {
+public:
+  struct io_item {
+    std::string semantic;  // upper case, without the index
+    uint32_t index;
+    int32_t reg;  // register, link slot or colour target; -1 the position
+    uint32_t comps;
+  };
+  struct uniform {
+    std::string name;
+    uint32_t word, words;
+  };
+  languages language = lang_none;
+  std::string cls, source;
+  std::vector<io_item> inputs, outputs;
+  std::vector<uniform> uniforms;
+  std::vector<std::string> samplers;
+  uint32_t varyings = 0;
+  sg_shader_module const* module = nullptr;
+};
 using shader_object_ptr = std::shared_ptr<shader_object>;
 }  // namespace salvia::shader
+
+namespace salvia::detail {
+// the tree this header lies in: $SALVIA_GB300_ROOT, else three levels above it
+inline std::string gb300_root() {
+  if (char const* r = std::getenv("SALVIA_GB300_ROOT")) return r;
+  std::string f = __FILE__;
+  for (int i = 0; i < 3; ++i) {
+    size_t const p = f.find_last_of('/');
+    f = p == std::string::npos ? std::string(".") : f.substr(0, p);
+  }
+  return f;
+}
+// the translator: the linked library's, else the GPU library of the tree
+inline void* sasl_library() {
+  if (dlsym(RTLD_DEFAULT, "sg_sasl_translate")) return RTLD_DEFAULT;
+  static void* const h =
+      dlopen((gb300_root() + "/salviarenderer_gb300/_lib/libsalvia_gb300.so").c_str(), RTLD_NOW | RTLD_LOCAL);
+  return h;
+}
+inline std::string upper(std::string s) {
+  for (char& c : s)
+    if (c >= 'a' && c <= 'z') c = static_cast<char>(c - 'a' + 'A');
+  return s;
+}
+inline bool same_semantic(std::string a, std::string b) {
+  a = upper(a);
+  b = upper(b);
+  if (a == "SV_POSITION") a = "POSITION";
+  if (b == "SV_POSITION") b = "POSITION";
+  return a == b;
+}
+}  // namespace salvia::detail
 
 namespace salvia::core {
 
@@ -942,19 +1014,36 @@ public:
     if (id != async_object_ids::pipeline_statistics && id != async_object_ids::internal_statistics) return nullptr;
     return std::make_shared<async_object>(id);
   }
-  // The SASL overload (renderer.h:52-54): compiled shader objects are not on
-  // this path, so there is no layout.
-  input_layout_ptr create_input_layout(input_element_desc const*, size_t, shader::shader_object_ptr const&) {
-    return nullptr;
+  // The SASL overload (renderer.h:52-54): the elements bound to the
+  // compiled vertex shader's input registers by semantic.
+  input_layout_ptr create_input_layout(input_element_desc const* descs, size_t count,
+                                       shader::shader_object_ptr const& vs) {
+    if (!vs || vs->language != shader::lang_vertex_shader) return nullptr;
+    return make_layout(descs, count, [&](std::string const& name, size_t index, size_t& reg) {
+      for (auto const& in : vs->inputs)
+        if (salvia::detail::same_semantic(in.semantic, name) && in.index == index) {
+          reg = static_cast<size_t>(in.reg);
+          return true;
+        }
+      return false;
+    });
   }
   // Binds the elements to the shader's input registers by semantic
   // (renderer::create_input_layout(descs, n, cpp_vertex_shader_ptr)).
   input_layout_ptr create_input_layout(input_element_desc const* descs, size_t count, cpp_vertex_shader_ptr const& vs) {
     if (!vs) return nullptr;
+    return make_layout(descs, count, [&](std::string const& name, size_t index, size_t& reg) {
+      return vs->find_register(name.c_str(), index, reg) == result::ok;
+    });
+  }
+
+private:
+  input_layout_ptr make_layout(input_element_desc const* descs, size_t count,
+                               std::function<bool(std::string const&, size_t, size_t&)> const& find) {
     auto il = std::make_shared<resource::input_layout>();
     for (size_t i = 0; i < count; ++i) {
       size_t reg = 0;
-      if (vs->find_register(descs[i].semantic_name.c_str(), descs[i].semantic_index, reg) != result::ok) continue;
+      if (!find(descs[i].semantic_name, descs[i].semantic_index, reg)) continue;
       if (reg >= SG_MAX_VS_INPUTS) return nullptr;
       if (il->registers.size() <= reg) il->registers.resize(reg + 1, sg_vs_input{SG_SEMANTIC_TEXCOORD, 0,
                                                                                   SG_VFMT_R32G32B32A32_FLOAT, 0, 0});
@@ -969,6 +1058,8 @@ public:
     }
     return il;
   }
+
+public:
 
   // map / unmap (renderer.h:61-63): a host copy, written back on unmap.
   result map(mapped_resource& mr, buffer_ptr const& buf, map_mode mm) {
@@ -1076,13 +1167,19 @@ public:
     vp_ = vp;
     return result::ok;
   }
-  // Shader-code state (renderer.h:75-101, renderer_impl.cpp:287-335).  The
-  // reference keeps these variables and samplers in constant buffers that
-  // only compiled SASL shaders read; cpp shaders take theirs through
-  // set_constant / set_sampler.  They are kept here the same way; shader
-  // objects themselves are not on this path and are refused.
-  result set_vertex_shader_code(shader::shader_object_ptr const&) { return result::failed; }
-  result set_pixel_shader_code(shader::shader_object_ptr const&) { return result::failed; }
+  // Shader-code state (renderer.h:75-101, renderer_impl.cpp:287-335): a
+  // compiled SASL shader replaces the stage's cpp shader while it is set
+  // (null clears it) and reads the variables and samplers set by name.
+  result set_vertex_shader_code(shader::shader_object_ptr const& s) {
+    if (s && (s->language != shader::lang_vertex_shader || !s->module)) return result::failed;
+    vs_code_ = s;
+    return result::ok;
+  }
+  result set_pixel_shader_code(shader::shader_object_ptr const& s) {
+    if (s && (s->language != shader::lang_pixel_shader || !s->module)) return result::failed;
+    ps_code_ = s;
+    return result::ok;
+  }
   result set_vs_variable_value(std::string const& name, void const* data, size_t sz) {
     return keep(vs_vars_, name, data, sz);
   }
@@ -1116,8 +1213,8 @@ public:
   cpp_pixel_shader_ptr get_pixel_shader() const { return ps_; }
   cpp_blend_shader_ptr get_blend_shader() const { return bs_; }
   viewport get_viewport() const { return vp_; }
-  shader::shader_object_ptr get_vertex_shader_code() const { return nullptr; }
-  shader::shader_object_ptr get_pixel_shader_code() const { return nullptr; }
+  shader::shader_object_ptr get_vertex_shader_code() const { return vs_code_; }
+  shader::shader_object_ptr get_pixel_shader_code() const { return ps_code_; }
 
   // queries
   result begin(async_object_ptr const& q) {
@@ -1183,7 +1280,7 @@ public:
   // The C-ABI descriptor of a draw under the current state.
   result build_desc(bool indexed, size_t startpos, size_t primcnt, int basevert, sg_draw_desc& d) const {
     std::memset(&d, 0, sizeof(d));
-    if (!vs_ || !ps_ || !bs_ || !layout_) return result::failed;
+    if ((!vs_ && !vs_code_) || (!ps_ && !ps_code_) || !bs_ || !layout_) return result::failed;
     d.color_target = colors_.empty() ? 0 : colors_[0]->get_texture()->handle();
     for (size_t i = 1; i < colors_.size(); ++i) d.more_color_targets[i - 1] = colors_[i]->get_texture()->handle();
     d.ds_target = ds_ ? ds_->get_texture()->handle() : 0;
@@ -1209,9 +1306,10 @@ public:
     }
     d.num_inputs = static_cast<uint32_t>(layout_->registers.size());
     for (uint32_t i = 0; i < d.num_inputs; ++i) d.inputs[i] = layout_->registers[i];
-    d.num_varyings = vs_->num_output_attributes();
+    d.num_varyings = vs_code_ ? vs_code_->varyings : vs_->num_output_attributes();
     if (d.num_varyings > SG_MAX_VARYINGS) return result::invalid_parameter;
-    for (uint32_t i = 0; i < d.num_varyings; ++i) d.varying_modifiers[i] = vs_->output_attribute_modifiers(i);
+    for (uint32_t i = 0; i < d.num_varyings; ++i)
+      d.varying_modifiers[i] = vs_code_ ? static_cast<uint32_t>(am::am_linear) : vs_->output_attribute_modifiers(i);
     raster_desc const& r = rs_->get_desc();
     d.raster = sg_raster_desc{static_cast<uint32_t>(r.fm), static_cast<uint32_t>(r.cm), r.front_ccw ? 1u : 0u, 0u};
     depth_stencil_desc const& s = dss_->get_desc();
@@ -1230,8 +1328,39 @@ public:
                                                 static_cast<uint32_t>(s.back_face.stencil_pass_op),
                                                 static_cast<uint32_t>(s.back_face.stencil_func)};
     d.stencil_ref = stencil_ref_;
-    if (vs_->pack(d.vs) != result::ok || ps_->pack(d.ps) != result::ok || bs_->pack(d.bs) != result::ok)
-      return result::invalid_parameter;
+    result const rv = vs_code_ ? pack_code(*vs_code_, vs_vars_, vs_samplers_, d.vs) : vs_->pack(d.vs);
+    result const rp = ps_code_ ? pack_code(*ps_code_, ps_vars_, ps_samplers_, d.ps) : ps_->pack(d.ps);
+    if (rv != result::ok || rp != result::ok || bs_->pack(d.bs) != result::ok) return result::invalid_parameter;
+    return result::ok;
+  }
+
+  // A compiled shader's program, its uniforms' words from the variables set
+  // by name (missing ones are 0), its sampler, and a pixel shader's input
+  // links to the compiled vertex shader's outputs (its own order with a cpp
+  // vertex shader).
+  result pack_code(shader::shader_object const& o, std::unordered_map<std::string, std::vector<uint8_t>> const& vars,
+                   std::unordered_map<std::string, sampler_ptr> const& samps, sg_shader& s) const {
+    std::memset(&s, 0, sizeof(s));
+    if (sg_shader_register(dev_->dev, o.module, &s.program) != SG_OK) return result::failed;
+    for (auto const& u : o.uniforms) {
+      auto it = vars.find(u.name);
+      if (it != vars.end())
+        std::memcpy(&s.constants[u.word], it->second.data(), std::min<size_t>(it->second.size(), 4u * u.words));
+    }
+    if (!o.samplers.empty()) {
+      auto it = samps.find(o.samplers[0]);
+      s.samplers[0] = it != samps.end() && it->second ? it->second->handle() : 0;
+    }
+    if (o.language == shader::lang_pixel_shader && vs_code_) {
+      uint32_t link = 0;
+      for (auto const& in : o.inputs) {
+        if (in.reg < 0) continue;
+        for (auto const& out : vs_code_->outputs)
+          if (out.reg >= 0 && salvia::detail::same_semantic(out.semantic, in.semantic) && out.index == in.index)
+            link |= static_cast<uint32_t>(out.reg + 1) << (3 * in.reg);
+      }
+      std::memcpy(&s.constants[47], &link, sizeof link);
+    }
     return result::ok;
   }
 
@@ -1256,6 +1385,7 @@ private:
   cpp_vertex_shader_ptr vs_;
   cpp_pixel_shader_ptr ps_;
   cpp_blend_shader_ptr bs_;
+  shader::shader_object_ptr vs_code_, ps_code_;
   raster_state_ptr rs_;
   depth_stencil_state_ptr dss_;
   int32_t stencil_ref_ = 0;
@@ -1288,6 +1418,79 @@ inline renderer_ptr create_gpu_renderer(int cuda_device = 0, void* cuda_stream =
   return std::make_shared<renderer>(d);
 }
 inline renderer_ptr create_benchmark_renderer() { return create_gpu_renderer(0); }
+
+// compile(code, lang) (renderer.h:136-147): null when the source does not
+// translate (the translator's message goes to stderr) or the module does not
+// build.
+inline shader::shader_object_ptr compile(std::string const& code, shader::languages lang) {
+  using translate_fn = int32_t (*)(char const*, uint32_t, char const*, char const*, char**, char**, char**);
+  using free_fn = void (*)(char*);
+  void* lib = salvia::detail::sasl_library();
+  if (!lib) return nullptr;
+  auto tr = reinterpret_cast<translate_fn>(dlsym(lib, "sg_sasl_translate"));
+  auto fr = reinterpret_cast<free_fn>(dlsym(lib, "sg_sasl_free"));
+  if (!tr || !fr) return nullptr;
+  bool const host_only = std::getenv("SALVIA_GB300_SASL_HOST_ONLY") != nullptr;
+  char hex[24];
+  std::snprintf(hex, sizeof hex, "%016zx", std::hash<std::string>{}(code + static_cast<char>('0' + lang)));
+  auto obj = std::make_shared<shader::shader_object>();
+  obj->language = lang;
+  obj->cls = std::string("sasl_") + hex;
+  char *src = nullptr, *refl = nullptr, *log = nullptr;
+  if (tr(code.c_str(), static_cast<uint32_t>(lang), nullptr, obj->cls.c_str(), &src, &refl, &log) != SG_OK) {
+    if (log) std::fputs(log, stderr);
+    fr(log);
+    return nullptr;
+  }
+  obj->source = src;
+  std::string const text = refl;
+  fr(src);
+  fr(refl);
+  size_t at = 0;
+  while (at < text.size()) {
+    size_t const e = text.find('\n', at);
+    std::string const line = text.substr(at, e == std::string::npos ? std::string::npos : e - at);
+    at = e == std::string::npos ? text.size() : e + 1;
+    char kind[16] = {0}, name[128] = {0};
+    int a = 0, b = 0, c = 0;
+    if (std::sscanf(line.c_str(), "%15s %127s %d %d %d", kind, name, &a, &b, &c) < 2) continue;
+    std::string const k = kind;
+    if (k == "input" || k == "output")
+      (k == "input" ? obj->inputs : obj->outputs)
+          .push_back({name, static_cast<uint32_t>(a), static_cast<int32_t>(b), static_cast<uint32_t>(c)});
+    else if (k == "uniform")
+      obj->uniforms.push_back({name, static_cast<uint32_t>(a), static_cast<uint32_t>(b)});
+    else if (k == "sampler")
+      obj->samplers.push_back(name);
+    else if (k == "varyings")
+      obj->varyings = static_cast<uint32_t>(std::atoi(name));
+  }
+  char const* cache = std::getenv("SALVIA_GB300_SHADER_CACHE");
+  std::string const dir = cache ? cache : "/tmp/salvia_gb300_shaders";
+  ::mkdir(dir.c_str(), 0755);
+  std::string const so = dir + "/lib" + obj->cls + (host_only ? "_host" : "") + ".so";
+  if (::access(so.c_str(), R_OK) != 0) {
+    std::string const cu = dir + "/" + obj->cls + ".cu", tmp = so + "." + std::to_string(::getpid()) + ".tmp";
+    std::ofstream(cu) << obj->source;
+    std::string const root = salvia::detail::gb300_root(), inc = " -I" + root + "/include -I" + root + "/salviarenderer_gb300/csrc ";
+    char const* nvcc = std::getenv("NVCC");
+    std::string const cmd =
+        host_only ? std::string("g++ -std=c++17 -O2 -ffp-contract=off -fPIC -shared -x c++ ") + cu + inc + "-o " + tmp
+                  : std::string(nvcc ? nvcc : "nvcc") +
+                        " -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 -fmad=false -Xcompiler -ffp-contract=off"
+                        " -shared -Xcompiler -fPIC -cudart shared " + cu + inc + "-o " + tmp;
+    if (std::system(cmd.c_str()) != 0 || std::rename(tmp.c_str(), so.c_str()) != 0) return nullptr;
+  }
+  void* h = dlopen(so.c_str(), RTLD_NOW | RTLD_LOCAL);  // kept loaded: devices hold the module
+  if (!h) return nullptr;
+  auto mod = reinterpret_cast<sg_shader_module const* (*)()>(dlsym(h, ("salvia_gb300_module_" + obj->cls).c_str()));
+  if (!mod) return nullptr;
+  obj->module = mod();
+  return obj;
+}
+inline shader::shader_object_ptr compile(std::string const& code, shader::shader_profile const& profile) {
+  return compile(code, profile.language);
+}
 inline renderer_ptr create_software_renderer() { return create_gpu_renderer(0); }
 
 }  // namespace salvia::core

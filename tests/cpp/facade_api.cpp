@@ -58,8 +58,9 @@ int main() {
   if (!smp) return fail("create_sampler");
   if (r->set_vs_sampler("s", smp) != salvia::result::ok || r->set_ps_sampler("s", smp) != salvia::result::ok)
     return fail("set_vs_sampler / set_ps_sampler");
-  if (r->set_vertex_shader_code(nullptr) != salvia::result::failed) return fail("set_vertex_shader_code");
-  if (r->set_pixel_shader_code(nullptr) != salvia::result::failed) return fail("set_pixel_shader_code");
+  // a null shader object clears the stage's compiled shader (renderer_impl.cpp:94-97, 310-316)
+  if (r->set_vertex_shader_code(nullptr) != salvia::result::ok) return fail("set_vertex_shader_code");
+  if (r->set_pixel_shader_code(nullptr) != salvia::result::ok) return fail("set_pixel_shader_code");
   if (r->get_vertex_shader_code() || r->get_pixel_shader_code()) return fail("shader code getters");
   input_element_desc el{};
   if (r->create_input_layout(&el, 1, salvia::shader::shader_object_ptr())) return fail("SASL input layout");

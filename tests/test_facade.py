@@ -119,3 +119,34 @@ def test_queued_draw_outlives_its_sampler_on_gpu(tmp_path):
     from salviarenderer_gb300 import build as pbuild
     alive, released = _lifetime_outputs(pbuild.ensure_built(), tmp_path)
     assert alive == released and any(alive)
+
+
+def _sasl_app_outputs(lib_path, tmp_path, host_only):
+    """tests/cpp/sasl_app.cpp drawn with compiled SASL shaders and with the
+    cpp shaders of the same transform: (sasl bytes, cpp bytes)."""
+    exe = build_facade(lib_path, str(tmp_path), os.path.join(ROOT, "tests", "cpp", "sasl_app.cpp"))
+    env = dict(os.environ, SALVIA_GB300_SHADER_CACHE=os.path.join(str(tmp_path), "shaders"))
+    if host_only:
+        env["SALVIA_GB300_SASL_HOST_ONLY"] = "1"
+    out = []
+    for mode in ("sasl", "cpp"):
+        path = os.path.join(str(tmp_path), f"{mode}.bin")
+        r = subprocess.run([exe, mode, path], env=env, capture_output=True, text=True)
+        assert r.returncode == 0, (mode, r.returncode, r.stdout, r.stderr)
+        out.append(open(path, "rb").read())
+    return out
+
+
+def test_facade_sasl_shaders_on_oracle(oracle_lib, tmp_path):
+    """compile() / set_*_shader_code / variables by name: the compiled
+    shaders (host bodies) draw the bytes of the cpp transform and colour."""
+    from conftest import ORACLE_LIB
+    sasl_out, cpp_out = _sasl_app_outputs(ORACLE_LIB, tmp_path, host_only=True)
+    assert sasl_out == cpp_out and any(sasl_out)
+
+
+@pytest.mark.gpu
+def test_facade_sasl_shaders_on_gpu(oracle_lib, tmp_path):
+    from salviarenderer_gb300 import build as pbuild
+    sasl_out, cpp_out = _sasl_app_outputs(pbuild.ensure_built(), tmp_path, host_only=False)
+    assert sasl_out == cpp_out and any(sasl_out)
