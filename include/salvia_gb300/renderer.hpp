@@ -152,7 +152,8 @@ inline std::string gb300_root() {
 }
 // the translator: the linked library's, else the GPU library of the tree
 inline void* sasl_library() {
-  if (dlsym(RTLD_DEFAULT, "sg_sasl_translate")) return RTLD_DEFAULT;
+  // (RTLD_DEFAULT is a null handle: the program's own handle searches the same scope)
+  if (dlsym(RTLD_DEFAULT, "sg_sasl_translate")) return dlopen(nullptr, RTLD_NOW);
   static void* const h =
       dlopen((gb300_root() + "/salviarenderer_gb300/_lib/libsalvia_gb300.so").c_str(), RTLD_NOW | RTLD_LOCAL);
   return h;
@@ -1425,11 +1426,15 @@ inline renderer_ptr create_benchmark_renderer() { return create_gpu_renderer(0);
 inline shader::shader_object_ptr compile(std::string const& code, shader::languages lang) {
   using translate_fn = int32_t (*)(char const*, uint32_t, char const*, char const*, char**, char**, char**);
   using free_fn = void (*)(char*);
+  auto fail = [](std::string const& why) {
+    std::fprintf(stderr, "compile: %s\n", why.c_str());
+    return shader::shader_object_ptr();
+  };
   void* lib = salvia::detail::sasl_library();
-  if (!lib) return nullptr;
+  if (!lib) return fail("the SASL translator (libsalvia_gb300.so) is not loaded");
   auto tr = reinterpret_cast<translate_fn>(dlsym(lib, "sg_sasl_translate"));
   auto fr = reinterpret_cast<free_fn>(dlsym(lib, "sg_sasl_free"));
-  if (!tr || !fr) return nullptr;
+  if (!tr || !fr) return fail("the library exports no SASL translator");
   bool const host_only = std::getenv("SALVIA_GB300_SASL_HOST_ONLY") != nullptr;
   char hex[24];
   std::snprintf(hex, sizeof hex, "%016zx", std::hash<std::string>{}(code + static_cast<char>('0' + lang)));
@@ -1437,10 +1442,11 @@ inline shader::shader_object_ptr compile(std::string const& code, shader::langua
   obj->language = lang;
   obj->cls = std::string("sasl_") + hex;
   char *src = nullptr, *refl = nullptr, *log = nullptr;
-  if (tr(code.c_str(), static_cast<uint32_t>(lang), nullptr, obj->cls.c_str(), &src, &refl, &log) != SG_OK) {
-    if (log) std::fputs(log, stderr);
+  int32_t const st = tr(code.c_str(), static_cast<uint32_t>(lang), nullptr, obj->cls.c_str(), &src, &refl, &log);
+  if (st != SG_OK) {
+    std::string const why = log ? std::string(log) : "status " + std::to_string(st);
     fr(log);
-    return nullptr;
+    return fail("the source does not translate: " + why);
   }
   obj->source = src;
   std::string const text = refl;
@@ -1474,17 +1480,19 @@ inline shader::shader_object_ptr compile(std::string const& code, shader::langua
     std::ofstream(cu) << obj->source;
     std::string const root = salvia::detail::gb300_root(), inc = " -I" + root + "/include -I" + root + "/salviarenderer_gb300/csrc ";
     char const* nvcc = std::getenv("NVCC");
+    if (!nvcc && ::access("/usr/local/cuda/bin/nvcc", X_OK) == 0) nvcc = "/usr/local/cuda/bin/nvcc";
     std::string const cmd =
         host_only ? std::string("g++ -std=c++17 -O2 -ffp-contract=off -fPIC -shared -x c++ ") + cu + inc + "-o " + tmp
                   : std::string(nvcc ? nvcc : "nvcc") +
                         " -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 -fmad=false -Xcompiler -ffp-contract=off"
                         " -shared -Xcompiler -fPIC -cudart shared " + cu + inc + "-o " + tmp;
-    if (std::system(cmd.c_str()) != 0 || std::rename(tmp.c_str(), so.c_str()) != 0) return nullptr;
+    if (std::system(cmd.c_str()) != 0 || std::rename(tmp.c_str(), so.c_str()) != 0)
+      return fail("building the shader module failed: " + cmd);
   }
   void* h = dlopen(so.c_str(), RTLD_NOW | RTLD_LOCAL);  // kept loaded: devices hold the module
-  if (!h) return nullptr;
+  if (!h) return fail(std::string("loading the shader module failed: ") + dlerror());
   auto mod = reinterpret_cast<sg_shader_module const* (*)()>(dlsym(h, ("salvia_gb300_module_" + obj->cls).c_str()));
-  if (!mod) return nullptr;
+  if (!mod) return fail("the shader module exports no " + obj->cls);
   obj->module = mod();
   return obj;
 }
