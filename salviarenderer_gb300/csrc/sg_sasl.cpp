@@ -32,8 +32,9 @@
 //    outputs COLOR(n) / SV_Target(n) write colour target n;
 //  - uniforms take consecutive 32-bit constant words in declaration order
 //    (a matrix row by row), 47 words at most in a pixel shader, 48 in a
-//    vertex shader; a stage samples through sampler slot 0, so it may use
-//    one sampler.
+//    vertex shader, loaded into the invocation's own copies at entry (a
+//    shader may assign to them); a stage samples through sampler slot 0, so
+//    it may use one sampler.
 // ddx / ddy (and tex2D, which takes the derivatives of its coordinate,
 // cg_impl.cpp:902-908) apply to a pixel-shader input read directly in the
 // entry function (in.uv, in.uv.xy): the pipeline gives the quad's
@@ -311,7 +312,7 @@ class Translator {
   std::vector<std::string> struct_order_;
   std::map<std::string, std::vector<Func>> funcs_;
   std::vector<std::map<std::string, Sym>> scopes_;
-  std::ostringstream structs_out_, members_out_, refl_;
+  std::ostringstream structs_out_, members_out_, refl_, uniform_loads_;
   int next_word_ = 0;
   std::set<std::string> samplers_used_;
   bool in_entry_ = false, have_entry_ = false;
@@ -511,18 +512,18 @@ class Translator {
       int const words = ty.comps();
       int const cap = vs() ? SG_MAX_SHADER_CONSTANTS : SG_MAX_SHADER_CONSTANTS - 1;
       if (next_word_ + words > cap) fail("uniforms exceed the stage's " + std::to_string(cap) + " constant words");
+      // an invocation's own copy, loaded at entry: a shader may assign to it
       s.kind = Sym::Uniform;
-      s.code = "u_" + name + "()";
+      s.code = "u_" + name;
       std::string const e = ty.elem_cpp();
-      members_out_ << "  __host__ __device__ " << ty.cpp() << " u_" << name << "() const {\n";
+      members_out_ << "  mutable " << ty.cpp() << " u_" << name << ";\n";
       if (ty.kind == Type::Scalar) {
-        members_out_ << "    return sasl_rt::from_word<" << e << ">(constant(" << next_word_ << "));\n";
+        uniform_loads_ << "    u_" << name << " = sasl_rt::from_word<" << e << ">(constant(" << next_word_ << "));\n";
       } else {
-        members_out_ << "    " << ty.cpp() << " r;\n    for (int i = 0; i < " << words << "; ++i) r"
-                     << (ty.kind == Type::Vector ? ".v[i]" : ".r[i / " + std::to_string(ty.cols) + "].v[i % " + std::to_string(ty.cols) + "]")
-                     << " = sasl_rt::from_word<" << e << ">(constant(" << next_word_ << " + i));\n    return r;\n";
+        uniform_loads_ << "    for (int i = 0; i < " << words << "; ++i) u_" << name
+                       << (ty.kind == Type::Vector ? ".v[i]" : ".r[i / " + std::to_string(ty.cols) + "].v[i % " + std::to_string(ty.cols) + "]")
+                       << " = sasl_rt::from_word<" << e << ">(constant(" << next_word_ << " + i));\n";
       }
-      members_out_ << "  }\n";
       refl_ << "uniform " << name << " " << next_word_ << " " << words << " " << ty.base << " " << ty.rows << " "
             << (ty.kind == Type::Scalar ? 1 : ty.cols) << "\n";
       next_word_ += words;
@@ -1219,8 +1220,8 @@ class Translator {
       e.code = "0";
       return e;
     }
-    e.code = s->kind == Sym::Local ? s->code : s->code;
-    e.lvalue = s->kind == Sym::Local;
+    e.code = s->code;
+    e.lvalue = s->kind == Sym::Local || s->kind == Sym::Uniform;
     if (in_entry_ && s->vary >= 0) {
       e.vary = s->vary;
       e.vary_type = s->type;
@@ -1262,6 +1263,7 @@ class Translator {
     rf << "stage " << (vs() ? "vertex" : "pixel") << "\nentry " << entry_ << "\nclass " << cls_ << "\n";
     w << "  __host__ __device__ " << (vs() ? "void shader_prog(salvia_gb300::vs_input const& sg_in, salvia_gb300::vs_output& sg_out) const {\n"
                                            : "bool shader_prog(salvia_gb300::vs_output const& sg_in, salvia_gb300::ps_output& sg_out) const {\n");
+    w << uniform_loads_.str();
     for (size_t i = 0; i < f.params.size(); ++i) {
       Param const& p = f.params[i];
       w << "    " << p.type.cpp() << " a" << i << (p.type.array ? "[" + std::to_string(p.type.array) + "]" : "") << "{};\n";

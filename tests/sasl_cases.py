@@ -85,3 +85,38 @@ def run_ps(lib, cls, attrs, constants, ddx=None, ddy=None, position=(0, 0, 0, 1)
     io.sample, io.sample_grad, io.sample_cube = keep[3], keep[4], keep[5]
     kept = m.host_ps(C.byref(io))
     return kept, np.array([[io.color[t][i] for i in range(4)] for t in range(7)], np.float32)
+
+
+# sg_host_vs_io (include/salvia_gb300.h)
+class HostVsIo(C.Structure):
+    _fields_ = [("inp", (C.c_float * 4) * 8), ("num_varyings", C.c_uint32), ("constants", C.POINTER(C.c_float)),
+                ("backend", C.c_void_p), ("sample", SAMPLEFN), ("position", C.c_float * 4),
+                ("attr", (C.c_float * 4) * 5)]
+
+
+class VsModule(C.Structure):
+    _fields_ = [("abi_version", C.c_uint32), ("stage", C.c_uint32), ("name", C.c_char_p),
+                ("device_init", C.c_void_p), ("device_launch", C.c_void_p), ("host_ps", C.c_void_p),
+                ("host_bs", C.c_void_p), ("host_vs", C.CFUNCTYPE(C.c_int32, C.POINTER(HostVsIo)))]
+
+
+def run_vs(lib, cls, inputs, constants):
+    """Calls the module's host vertex-shader body once: (position, varyings)."""
+    fn = getattr(lib, "salvia_gb300_module_" + cls)
+    fn.restype = C.POINTER(VsModule)
+    m = fn().contents
+    io = HostVsIo()
+    for r, a in enumerate(inputs):
+        for i, x in enumerate(a):
+            io.inp[r][i] = x
+    k = (C.c_float * 48)(*np.asarray(constants, np.float32))
+    io.constants = C.cast(k, C.POINTER(C.c_float))
+
+    def no_sample(*a):
+        raise AssertionError("unexpected texture lookup")
+
+    keep = SAMPLEFN(no_sample)
+    io.sample = keep
+    m.host_vs(C.byref(io))
+    return (np.array(list(io.position), np.float32),
+            np.array([[io.attr[t][i] for i in range(4)] for t in range(5)], np.float32))

@@ -145,7 +145,7 @@ def test_sasl_linked_input_renders_as_the_stock_color_shader(objs, odev):
     ("float4 ps_main(float4 c): COLOR { return c; }", "no semantic"),
     ("#define X 1\nfloat4 ps_main(float4 c: COLOR0): COLOR { return c; }", "preprocessor"),
     ("float4 ps_main(float4 c: COLOR0): COLOR { return foo(c); }", "unknown function"),
-    ("float u; float4 ps_main(float4 c: COLOR0): COLOR { u = 1.0f; return c; }", "not assignable"),
+    ("float4 ps_main(float4 c: COLOR0): COLOR { c.x + 1.0f = 2.0f; return c; }", "not assignable"),
     ("float4 ps_main(float4 c: COLOR0): DEPTH { return c; }", "DEPTH"),
     ("float4 ps_main(float4 c: COLOR0): COLOR { return c.xyzq; }", "bad swizzle"),
     ("float4 ps_main(float4 c: COLOR0): COLOR { return c }", "expected ';'"),
@@ -173,8 +173,8 @@ def test_vertex_shader_refusals(product_lib):
 REF_ROOT = os.environ.get("SALVIA_REFERENCE") or os.path.join(os.path.dirname(sc.ROOT), "reference")
 REPO = os.path.join(REF_ROOT, "sasl", "test", "repo")
 # stage shaders the translator refuses: a uniform array sized by a uniform,
-# a matrix stage input, assignment to a uniform
-REFUSED = {"array.svs", "auto_semantic.svs", "input_assigned.svs", "scalar.sps"}
+# matrix stage inputs
+REFUSED = {"array.svs", "auto_semantic.svs", "scalar.sps"}
 
 
 def ref_files():
@@ -284,3 +284,18 @@ def test_reference_ps_ddx_ddy(ref_module):
     np.testing.assert_array_equal(got[1, :2], X[1][[0, 1]] + Y[1][[1, 0]])
     np.testing.assert_array_equal(got[2, :3], X[2][[0, 1, 2]] + Y[2][[1, 2, 0]])
     np.testing.assert_array_equal(got[3], X[3][[0, 3, 2, 1]] + Y[3][[1, 2, 0, 3]])
+
+
+def test_reference_vs_assigns_its_uniform(ref_module):
+    """input_assigned.svs: a uniform assigned in the body is the invocation's
+    own copy (x += 0.5; in.pos.x += x; o.pos.x += 0.5)."""
+    lib, _ = ref_module
+    p = np.array([1.25, -2.0, 0.5, 1.0], np.float32)
+    k = [0.0] * 48
+    k[0] = 3.0
+    for _ in range(2):  # the second call starts from the uniform again
+        pos, _ = sc.run_vs(lib, "ref_input_assigned_svs", [tuple(p)], k)
+        x = np.float32(3.0) + np.float32(0.5)
+        want = p.copy()
+        want[0] = (p[0] + x) + np.float32(0.5)
+        np.testing.assert_array_equal(pos, want)
