@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-facade", action="store_true", help="skip the C++ facade leg")
     ap.add_argument("--no-autotune", action="store_true", help="time under the default scheduling parameters")
     ap.add_argument("--no-ingest", action="store_true", help="skip the texture / mesh ingest leg")
+    ap.add_argument("--no-sasl", action="store_true", help="skip the SASL-compiled pixel shader leg")
     ap.add_argument("--cpu-configs", action="store_true",
                     help="time the CPU restatement (and the reference, where built) on the five workloads")
     ap.add_argument("--size", default="1920x1080",
@@ -475,6 +476,60 @@ def measure_facade(args, scene, resolved_want):
             "resolved_equals_graph": raw[off:off + n * 4] == bytes(resolved_want)}
 
 
+# The anisotropic draws' pixel shader in SASL: tex2D (sample_2d_grad with the
+# coordinate's quad differences) modulated by the colour, SG_PS_TEX_GRAD_MODULATE's
+# arithmetic.
+SASL_GRAD_PS = """
+sampler s;
+struct PSIn {
+    float4 uv:    TEXCOORD0;
+    float4 color: COLOR0;
+};
+float4 ps_main(PSIn in): COLOR {
+    return tex2D(s, in.uv.xy) * in.color;
+}
+"""
+
+
+def measure_sasl(dev, stream, flush, args, width, height):
+    """The 1080p frame with its anisotropic draws' pixel shader compiled from
+    SASL (sg_sasl_translate -> a user shader module built with nvcc) against
+    the stock program: translate + build time, frames/s of both (recorded
+    graphs) and whether the resolved images are equal."""
+    import tempfile
+    import numpy as np
+    from salviarenderer_gb300 import abi, sasl, scenes
+    t0 = time.perf_counter()
+    obj = sasl.compile(dev.lib, SASL_GRAD_PS, sasl.LANG_PIXEL_SHADER, cls="bench_sasl_grad_ps")
+    sasl.load(sasl.build_module([obj], tempfile.mkdtemp(prefix="sasl_bench_")))
+    build_s = time.perf_counter() - t0
+    steps = max(1, min(args.steps, 10))
+
+    def frame(use_sasl):
+        sc = scenes.c2_scene(seed=SEED, width=width, height=height)
+        if use_sasl:
+            for d in sc.draws:
+                if d["ps"]["program"] == abi.PS_TEX_GRAD_MODULATE:
+                    d["ps"] = dict(d["ps"], program=obj.program)
+        b = scenes.Bound(dev, sc)
+        cl = b.commands()
+        dev.submit(cl)
+        img = b.outputs()["resolved"]
+        g = dev.graph_create(cl)
+        for _ in range(args.warmup):
+            g.launch()
+        dev.sync()
+        sec = time_steps(stream, flush, steps, g.launch)
+        g.close()
+        return steps / sec, img
+
+    fs, a = frame(False)
+    fu, b = frame(True)
+    return {"shader": "tex2D(s, in.uv.xy) * in.color on the 4 anisotropic draws", "translate_and_build_s": build_s,
+            "stock_frames_per_s": fs, "sasl_frames_per_s": fu, "sasl_over_stock": fu / fs,
+            "resolved_equal": bool(np.array_equal(a, b))}
+
+
 def synthetic_obj(path, n):
     """An n x n height-field grid as a Wavefront OBJ file: positions,
     texcoords and normals per grid point, two triangles per cell with
@@ -663,6 +718,7 @@ def run_gpu(args):
     uneven = None if args.no_uneven else measure_uneven(dev, stream, flush, args)
     learned = None if args.no_learned else measure_learned(dev, stream, flush, args, width, height)
     ingest_leg = None if (args.no_ingest or rank != 0) else measure_ingest(dev, stream, args)
+    sasl_leg = None if (args.no_sasl or rank != 0) else measure_sasl(dev, stream, flush, args, width, height)
 
     if rank == 0:
         peak, peak_kind = measured_peak()
@@ -688,6 +744,7 @@ def run_gpu(args):
                                    "recorded_graph": fps,
                                    "cpp_facade": None if facade is None else facade["frames_per_s"]},
             "facade": facade,
+            "sasl": sasl_leg,
             "gpix_per_s": fps * scene.width * scene.height / 1e9,
             "gsamples_per_s": fps * scene.width * scene.height * scene.samples / 1e9,
             "mtris_per_s": fps * scene.triangles / 1e6,
