@@ -574,11 +574,13 @@ __global__ void __launch_bounds__(256) k_shade_user(PassParams P, uint32_t key) 
       bool const keep = ps.shader_prog(in, out);
       salvia_gb300::vec4 const o = out.color[0];
       P.frag_color[static_cast<size_t>(f) * 4 + q] = make_float4(o.x, o.y, o.z, o.w);
-      if (P.frag_color_more)
-        for (uint32_t i = 0; i < P.more_colors; ++i) {
-          salvia_gb300::vec4 const m = i + 1 < SG_MAX_COLOR_TARGETS ? out.color[i + 1] : salvia_gb300::vec4();
-          P.frag_color_more[(static_cast<size_t>(f) * 4 + q) * P.more_colors + i] = make_float4(m.x, m.y, m.z, m.w);
-        }
+      if (P.frag_color_more)  // (a fixed trip count: out stays in registers)
+#pragma unroll
+        for (uint32_t i = 0; i + 1 < SG_MAX_COLOR_TARGETS; ++i)
+          if (i < P.more_colors) {
+            salvia_gb300::vec4 const m = out.color[i + 1];
+            P.frag_color_more[(static_cast<size_t>(f) * 4 + q) * P.more_colors + i] = make_float4(m.x, m.y, m.z, m.w);
+          }
       // the pass mask from int shifts of 0xFFFF by 16 i (cpp_pixel_shader.cpp:
       // 62-74): pixel 0 kept when pixel 0 or 2 passes, pixels 1-3 when 1 or 3 do
       int const qb = (threadIdx.x & 31) & ~3;

@@ -377,6 +377,15 @@ SASL_HD T from4(salvia_gb300::vec4 const& r) {
     return o;
   }
 }
+// varying register r of a pixel: selected among the registers rather than
+// indexed, so that the interpolated registers stay in registers
+SASL_HD salvia_gb300::vec4 varying(salvia_gb300::vs_output const& in, int r) {
+  salvia_gb300::vec4 v = in.attr[0];
+#pragma unroll
+  for (int i = 1; i < SG_MAX_VARYINGS; ++i)
+    if (r == i) v = in.attr[i];
+  return v;
+}
 // a value written to a register: missing components are 0
 template <class T>
 SASL_HD salvia_gb300::vec4 to4(T const& x) {

@@ -1282,7 +1282,7 @@ class Translator {
       } else {
         if (link >= SG_MAX_VARYINGS)
           throw SaslError{0, "more than " + std::to_string(SG_MAX_VARYINGS) + " pixel inputs besides the position"};
-        w << "    " << it.path << " = sasl_rt::from4<" << it.type.cpp() << ">(sg_in.attribute(sasl_link(" << link << ")));\n";
+        w << "    " << it.path << " = sasl_rt::from4<" << it.type.cpp() << ">(sasl_rt::varying(sg_in, sasl_link(" << link << ")));\n";
         rf << "input " << it.sem.name << " " << it.sem.index << " " << link << " " << it.type.comps() << "\n";
         ++link;
       }
