@@ -186,6 +186,12 @@ struct ps_device_ctx {
   int pixel;
 };
 
+// element p of a quad's four values, selected rather than indexed (the
+// context stays in registers)
+__device__ __forceinline__ float quad_sel(float const (&a)[4], int p) {
+  return p == 0 ? a[0] : p == 1 ? a[1] : p == 2 ? a[2] : a[3];
+}
+
 // Register `reg` (0-based varying) of `pixel` exactly as k_shade computes it
 // (step_2d_unproj_attr_n_quad / step_2d_unproj_attr_n, shader.cpp:208-367).
 __device__ inline sg::v4 pixel_attr(ps_device_ctx const& c, int reg, int p) {
@@ -197,7 +203,7 @@ __device__ inline sg::v4 pixel_attr(ps_device_ctx const& c, int reg, int p) {
   if (mods & SG_AM_NOINTERPOLATION) {
     a = in;
   } else if (c.centroid) {
-    float const px = c.pdx[p], py = c.pdy[p];
+    float const px = quad_sel(c.pdx, p), py = quad_sel(c.pdy, p);
     a = mk4(in.x + (d0.x * px + d1.x * py), in.y + (d0.y * px + d1.y * py), in.z + (d0.z * px + d1.z * py),
             in.w + (d0.w * px + d1.w * py));
   } else {
@@ -205,7 +211,7 @@ __device__ inline sg::v4 pixel_attr(ps_device_ctx const& c, int reg, int p) {
                  in.z + (d0.z * c.dx + d1.z * c.dy), in.w + (d0.w * c.dx + d1.w * c.dy));
     a = p == 0 ? a00 : p == 1 ? a00 + d0 : p == 2 ? a00 + d1 : (a00 + d0) + d1;
   }
-  return (mods & SG_AM_NOPERSPECTIVE) ? a : a * c.invw[p];
+  return (mods & SG_AM_NOPERSPECTIVE) ? a : a * quad_sel(c.invw, p);
 }
 __device__ inline vec4 to_vec4(sg::v4 v) { return vec4(v.x, v.y, v.z, v.w); }
 #endif
